@@ -1,0 +1,154 @@
+/*
+ * reaxgpu -- GB300 (sm_103a) ReaxFF force step behind a C ABI.
+ *
+ * This is the seam that replaces the reference's per-kernel C entry points
+ * (`extern "C" void X_C(pack*)`, reaxc_ctypes_sunway.h:915-1074) and the
+ * LAMMPS plugin classes above them.  A LAMMPS `pair_style reax/c/...`,
+ * `fix qeq/reax/...` and `fix nve/...` wrapper calls these functions; the
+ * mapping is, per entry point:
+ *
+ *   rg_create        PairReaxCSunway::settings + coeff (Read_Force_Field,
+ *                    pair_reaxc_sunway.cpp:202-362, reaxc_ffield_sunway.cpp:35)
+ *   rg_extract       PairReaxCSunway::extract("chi"/"eta"/"gamma"),
+ *                    pair_reaxc_sunway.cpp:1106-1128
+ *   rg_set_box /
+ *   rg_set_atoms     write_reax_atoms + the LAMMPS atom arrays x/type/tag/q/v
+ *                    (pair_reaxc_sunway.cpp:797-831)
+ *   rg_qeq           FixQEqReaxSunway::pre_force, fix_qeq_reax_sunway.cpp:539-600
+ *   rg_compute       PairReaxCSunway::compute(eflag, vflag),
+ *                    pair_reaxc_sunway.cpp:541-793
+ *   rg_nve_initial   FixNVESunway::initial_integrate, fix_nve_sunway.cpp:67-100
+ *   rg_nve_final     FixNVESunway::final_integrate, fix_nve_sunway.cpp:102-135
+ *   rg_run           the Verlet loop those classes are driven by (LAMMPS
+ *                    Verlet::run): initial_integrate -> pre_force (QEq) ->
+ *                    pair compute -> final_integrate, all on the device
+ *
+ * All functions return 0 on success and a negative RG_E_* code on error
+ * (the reference aborts through error->all / MPI_Abort instead;
+ * reaxc_defs_sunway.h:148-151).  rg_last_error() gives the message.  A
+ * handle owns one CUDA stream and its device memory; handles are not
+ * thread-safe, distinct handles may be used from distinct threads.
+ *
+ * Units are LAMMPS real: Angstrom, fs, g/mol, kcal/mol, electron charge.
+ */
+#ifndef REAXGPU_H
+#define REAXGPU_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct rg_system rg_system;
+
+enum {
+  RG_OK = 0,
+  RG_E_ARG = -1,        /* invalid argument                        */
+  RG_E_FILE = -2,       /* force field unreadable / inconsistent   */
+  RG_E_CUDA = -3,       /* CUDA runtime error                      */
+  RG_E_CAPACITY = -4,   /* list capacity could not be grown        */
+  RG_E_STATE = -5,      /* call order (e.g. no atoms set)          */
+  RG_E_NUMERIC = -6     /* non-finite result detected              */
+};
+
+enum { RG_PREC_FP64 = 0, RG_PREC_MIXED = 1 };
+
+/* Run-time controls.  rg_default_params() gives the reference defaults of
+ * `pair_style reax/c NULL` (pair_reaxc_sunway.cpp:208-242) and
+ * `fix qeq/reax 1 0.0 10.0 1.0e-6 reax/c`. */
+typedef struct {
+  double bond_cut;      /* 5.0   near-neighbour cutoff for bonds        */
+  double hbond_cut;     /* 7.5   hydrogen-bond partner cutoff           */
+  double thb_cut;       /* 0.001 three/four-body bond-order cutoff      */
+  double thb_cutsq;     /* 1e-5                                         */
+  int enobondsflag;     /* 1     e_un/e_lp also for atoms without bonds */
+  int lgflag;           /* 0     low-gradient vdW correction            */
+  double qeq_swa;       /* 0.0   QEq taper inner radius                 */
+  double qeq_swb;       /* 10.0  QEq taper outer radius                 */
+  double qeq_tol;       /* 1e-6  CG relative tolerance                  */
+  int qeq_imax;         /* 200   CG iteration limit                     */
+  int precision;        /* RG_PREC_FP64 or RG_PREC_MIXED               */
+  int device;           /* CUDA device ordinal                          */
+} rg_params;
+
+/* Energy vector of rg_compute: entries 0..13 are the pair's pvector in the
+ * reference order (pair_reaxc_sunway.cpp:657-670): e_bond, e_ov+e_un, e_lp,
+ * 0, e_ang, e_pen, e_coa, e_hb, e_tor, e_con, e_vdW, e_ele, 0, e_pol; then
+ * the tallied eng_vdwl and eng_coul, then the physical polarisation sum.
+ * As in the reference, e_vdW and e_ele are summed over the full neighbour
+ * list (twice the physical value) and e_pol is the reference's running-sum
+ * value; eng_vdwl + eng_coul is the potential energy. */
+enum { RG_NENERGY = 17 };
+
+typedef struct {
+  long long n_atoms, n_pairs, n_bonds, n_hbond_pairs, n_H_entries;
+  int cg_iters_s, cg_iters_t;
+  int max_nbrs, max_bonds, max_hbonds;
+  int regrows;
+} rg_stats;
+
+void rg_default_params(rg_params *p);
+
+/* Read the force field and create a handle on p->device. */
+int rg_create(const char *ffield_path, const rg_params *p, rg_system **out);
+int rg_destroy(rg_system *h);
+const char *rg_last_error(const rg_system *h);
+
+int rg_num_types(const rg_system *h);
+/* element name of ffield type t (0-based), upper case */
+int rg_element_name(const rg_system *h, int t, char *buf, int len);
+/* per-type "chi", "eta", "gamma" or "mass" into out[ntypes] */
+int rg_extract(const rg_system *h, const char *name, double *out);
+
+/* Orthogonal periodic box [0,L0)x[0,L1)x[0,L2). */
+int rg_set_box(rg_system *h, const double *L3);
+
+/* Host arrays of n atoms: x[3n] (wrapped into the box), type[n] (0-based
+ * ffield type), tag[n] (1-based global id; NULL -> 1..n), q[n] (NULL -> 0),
+ * v[3n] (NULL -> 0).  Resets the QEq histories. */
+int rg_set_atoms(rg_system *h, int n, const double *x, const int *type,
+                 const int *tag, const double *q, const double *v);
+/* Same, reading device pointers (no host copies). */
+int rg_set_atoms_device(rg_system *h, int n, const double *x,
+                        const int *type, const int *tag, const double *q,
+                        const double *v);
+/* Update positions only (host array), keeping histories. */
+int rg_set_positions(rg_system *h, const double *x);
+
+/* QEq charge equilibration (pre_force).  q_out[n] host or NULL. */
+int rg_qeq(rg_system *h, double *q_out, int *iters_s, int *iters_t);
+
+/* Force step.  f_out[3n] host or NULL (forces, kcal/mol/A), energies
+ * [RG_NENERGY] host or NULL; eflag = 0 skips the energy reductions. */
+int rg_compute(rg_system *h, int eflag, int vflag, double *f_out,
+               double *energies);
+
+/* Velocity-Verlet halves (dt in fs). */
+int rg_nve_initial(rg_system *h, double dt);
+int rg_nve_final(rg_system *h, double dt);
+
+/* nsteps of NVE MD entirely on the device: per step initial_integrate,
+ * QEq, force step, final_integrate.  energies of the last step or NULL. */
+int rg_run(rg_system *h, int nsteps, double dt, double *energies);
+
+/* Read back the current state (host arrays, original atom order). */
+int rg_get_atoms(rg_system *h, double *x, double *v, double *q, double *f);
+/* Device pointers of the state arrays (original order, 3n/n doubles). */
+int rg_device_arrays(rg_system *h, double **x, double **v, double **q,
+                     double **f);
+
+int rg_get_stats(const rg_system *h, rg_stats *s);
+int rg_synchronize(rg_system *h);
+
+/* List dumps for parity checks, from the last force step.  Each entry is
+ * (tag_i, tag_j, image) with image = (sx+8) | (sy+8)<<4 | (sz+8)<<8 the
+ * periodic image of j relative to i.  Pass NULL arrays to get the count.
+ * rg_dump_bonds also returns the corrected bond orders bo[4*k] = BO, BO_s,
+ * BO_pi, BO_pi2. */
+long long rg_dump_pairs(rg_system *h, int *ti, int *tj, int *img);
+long long rg_dump_bonds(rg_system *h, int *ti, int *tj, int *img, double *bo);
+long long rg_dump_hbonds(rg_system *h, int *ti, int *tj, int *img);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,242 @@
+"""ctypes binding of libreaxgpu.so (the C ABI in include/reaxgpu.h).
+
+The library is the product: every call here goes to the CUDA kernels.  If
+the shared library cannot be loaded the import of this module's classes
+fails loudly; there is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIBPATH = os.path.join(HERE, "libreaxgpu.so")
+DEFAULT_FFIELD = os.path.join(HERE, "data", "ffield.reax")
+
+ENERGY_NAMES = ["e_bond", "e_ovun", "e_lp", "e_3", "e_ang", "e_pen", "e_coa",
+                "e_hb", "e_tor", "e_con", "e_vdW", "e_ele", "e_12", "e_pol",
+                "eng_vdwl", "eng_coul", "e_pol_phys"]
+NENERGY = len(ENERGY_NAMES)
+
+PREC_FP64, PREC_MIXED = 0, 1
+
+EXPORTED = ["rg_default_params", "rg_create", "rg_destroy", "rg_last_error",
+            "rg_num_types", "rg_element_name", "rg_extract", "rg_set_box",
+            "rg_set_atoms", "rg_set_atoms_device", "rg_set_positions", "rg_qeq",
+            "rg_compute", "rg_nve_initial", "rg_nve_final", "rg_run",
+            "rg_get_atoms", "rg_device_arrays", "rg_get_stats", "rg_synchronize",
+            "rg_dump_pairs", "rg_dump_bonds", "rg_dump_hbonds"]
+
+
+class Params(C.Structure):
+    _fields_ = [("bond_cut", C.c_double), ("hbond_cut", C.c_double),
+                ("thb_cut", C.c_double), ("thb_cutsq", C.c_double),
+                ("enobondsflag", C.c_int), ("lgflag", C.c_int),
+                ("qeq_swa", C.c_double), ("qeq_swb", C.c_double),
+                ("qeq_tol", C.c_double), ("qeq_imax", C.c_int),
+                ("precision", C.c_int), ("device", C.c_int)]
+
+
+class Stats(C.Structure):
+    _fields_ = [("n_atoms", C.c_longlong), ("n_pairs", C.c_longlong),
+                ("n_bonds", C.c_longlong), ("n_hbond_pairs", C.c_longlong),
+                ("n_H_entries", C.c_longlong), ("cg_iters_s", C.c_int),
+                ("cg_iters_t", C.c_int), ("max_nbrs", C.c_int),
+                ("max_bonds", C.c_int), ("max_hbonds", C.c_int),
+                ("regrows", C.c_int)]
+
+
+class ReaxError(RuntimeError):
+    pass
+
+
+_lib = None
+
+
+def load_library(path: str = LIBPATH):
+    """Load libreaxgpu.so and declare its C signatures."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise ReaxError(f"{path} is missing: build it with "
+                        "`python sw_reaxff_gb300/build.py` (or __graft_entry__.build())")
+    L = C.CDLL(path)
+    P = C.POINTER
+    dp, ip = P(C.c_double), P(C.c_int)
+    L.rg_default_params.argtypes = [P(Params)]
+    L.rg_create.argtypes = [C.c_char_p, P(Params), P(C.c_void_p)]
+    L.rg_destroy.argtypes = [C.c_void_p]
+    L.rg_last_error.restype = C.c_char_p
+    L.rg_last_error.argtypes = [C.c_void_p]
+    L.rg_num_types.argtypes = [C.c_void_p]
+    L.rg_element_name.argtypes = [C.c_void_p, C.c_int, C.c_char_p, C.c_int]
+    L.rg_extract.argtypes = [C.c_void_p, C.c_char_p, dp]
+    L.rg_set_box.argtypes = [C.c_void_p, dp]
+    L.rg_set_atoms.argtypes = [C.c_void_p, C.c_int, dp, ip, ip, dp, dp]
+    L.rg_set_atoms_device.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p,
+                                      C.c_void_p, C.c_void_p, C.c_void_p]
+    L.rg_set_positions.argtypes = [C.c_void_p, dp]
+    L.rg_qeq.argtypes = [C.c_void_p, dp, ip, ip]
+    L.rg_compute.argtypes = [C.c_void_p, C.c_int, C.c_int, dp, dp]
+    L.rg_nve_initial.argtypes = [C.c_void_p, C.c_double]
+    L.rg_nve_final.argtypes = [C.c_void_p, C.c_double]
+    L.rg_run.argtypes = [C.c_void_p, C.c_int, C.c_double, dp]
+    L.rg_get_atoms.argtypes = [C.c_void_p, dp, dp, dp, dp]
+    L.rg_device_arrays.argtypes = [C.c_void_p] + [P(C.c_void_p)] * 4
+    L.rg_get_stats.argtypes = [C.c_void_p, P(Stats)]
+    L.rg_synchronize.argtypes = [C.c_void_p]
+    for f in ("rg_dump_pairs", "rg_dump_hbonds"):
+        getattr(L, f).restype = C.c_longlong
+        getattr(L, f).argtypes = [C.c_void_p, ip, ip, ip]
+    L.rg_dump_bonds.restype = C.c_longlong
+    L.rg_dump_bonds.argtypes = [C.c_void_p, ip, ip, ip, dp]
+    _lib = L
+    return L
+
+
+def _dp(a):
+    return None if a is None else a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def _ip(a):
+    return None if a is None else a.ctypes.data_as(C.POINTER(C.c_int))
+
+
+def default_params(**kw) -> Params:
+    L = load_library()
+    p = Params()
+    L.rg_default_params(C.byref(p))
+    for k, v in kw.items():
+        setattr(p, k, v)
+    return p
+
+
+class ReaxGPU:
+    """One periodic system on one GPU, driven through the C ABI."""
+
+    def __init__(self, ffield: str = DEFAULT_FFIELD, **params):
+        self.L = load_library()
+        self.params = default_params(**params)
+        h = C.c_void_p()
+        rc = self.L.rg_create(ffield.encode(), C.byref(self.params), C.byref(h))
+        if rc != 0:
+            raise ReaxError(f"rg_create failed ({rc}) for {ffield}")
+        self.h = h
+        self.n = 0
+        self.elements = []
+        buf = C.create_string_buffer(16)
+        for t in range(self.L.rg_num_types(h)):
+            self.L.rg_element_name(h, t, buf, 16)
+            self.elements.append(buf.value.decode())
+
+    def _chk(self, rc, what):
+        if rc != 0:
+            msg = self.L.rg_last_error(self.h)
+            raise ReaxError(f"{what} failed ({rc}): {msg.decode() if msg else ''}")
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.rg_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def extract(self, name: str) -> np.ndarray:
+        out = np.zeros(len(self.elements))
+        self._chk(self.L.rg_extract(self.h, name.encode(), _dp(out)), "rg_extract")
+        return out
+
+    def set_box(self, box):
+        box = np.ascontiguousarray(box, np.float64)
+        self._chk(self.L.rg_set_box(self.h, _dp(box)), "rg_set_box")
+
+    def set_atoms(self, x, types, tags=None, q=None, v=None):
+        x = np.ascontiguousarray(x, np.float64)
+        n = x.shape[0]
+        types = np.ascontiguousarray(types, np.int32)
+        tags = None if tags is None else np.ascontiguousarray(tags, np.int32)
+        q = None if q is None else np.ascontiguousarray(q, np.float64)
+        v = None if v is None else np.ascontiguousarray(v, np.float64)
+        self._chk(self.L.rg_set_atoms(self.h, n, _dp(x), _ip(types), _ip(tags), _dp(q), _dp(v)),
+                  "rg_set_atoms")
+        self.n = n
+
+    def set_system(self, system):
+        """Load a sw_reaxff_gb300.systems.System."""
+        self.set_box(system.box)
+        self.set_atoms(system.x, system.types(self.elements), system.tag, None, system.v)
+
+    def set_positions(self, x):
+        x = np.ascontiguousarray(x, np.float64)
+        self._chk(self.L.rg_set_positions(self.h, _dp(x)), "rg_set_positions")
+
+    def qeq(self):
+        q = np.zeros(self.n)
+        a, b = C.c_int(), C.c_int()
+        self._chk(self.L.rg_qeq(self.h, _dp(q), C.byref(a), C.byref(b)), "rg_qeq")
+        return q, a.value, b.value
+
+    def compute(self, eflag=1):
+        f = np.zeros((self.n, 3))
+        e = np.zeros(NENERGY)
+        self._chk(self.L.rg_compute(self.h, eflag, 0, _dp(f), _dp(e)), "rg_compute")
+        return f, dict(zip(ENERGY_NAMES, e))
+
+    def nve_initial(self, dt):
+        self._chk(self.L.rg_nve_initial(self.h, dt), "rg_nve_initial")
+
+    def nve_final(self, dt):
+        self._chk(self.L.rg_nve_final(self.h, dt), "rg_nve_final")
+
+    def run(self, nsteps, dt, energies=True):
+        e = np.zeros(NENERGY) if energies else None
+        self._chk(self.L.rg_run(self.h, nsteps, dt, _dp(e)), "rg_run")
+        return dict(zip(ENERGY_NAMES, e)) if energies else None
+
+    def get_atoms(self):
+        n = self.n
+        x, v, f = np.zeros((n, 3)), np.zeros((n, 3)), np.zeros((n, 3))
+        q = np.zeros(n)
+        self._chk(self.L.rg_get_atoms(self.h, _dp(x), _dp(v), _dp(q), _dp(f)), "rg_get_atoms")
+        return x, v, q, f
+
+    def device_arrays(self):
+        ptrs = [C.c_void_p() for _ in range(4)]
+        self._chk(self.L.rg_device_arrays(self.h, *[C.byref(p) for p in ptrs]), "rg_device_arrays")
+        return [p.value for p in ptrs]
+
+    def stats(self):
+        s = Stats()
+        self._chk(self.L.rg_get_stats(self.h, C.byref(s)), "rg_get_stats")
+        return {k: getattr(s, k) for k, _ in Stats._fields_}
+
+    def synchronize(self):
+        self._chk(self.L.rg_synchronize(self.h), "rg_synchronize")
+
+    def _dump(self, fn, with_bo=False):
+        k = fn(self.h, None, None, None, None) if with_bo else fn(self.h, None, None, None)
+        if k < 0:
+            raise ReaxError("list dump needs a preceding force step")
+        ti, tj, im = (np.zeros(k, np.int32) for _ in range(3))
+        if with_bo:
+            bo = np.zeros((k, 4))
+            fn(self.h, _ip(ti), _ip(tj), _ip(im), _dp(bo))
+            return ti, tj, im, bo
+        fn(self.h, _ip(ti), _ip(tj), _ip(im))
+        return ti, tj, im
+
+    def pair_list(self):
+        return self._dump(self.L.rg_dump_pairs)
+
+    def bond_list(self):
+        return self._dump(self.L.rg_dump_bonds, True)
+
+    def hbond_list(self):
+        return self._dump(self.L.rg_dump_hbonds)

@@ -1,0 +1,427 @@
+// Cell binning, atom sort, pair list, bond list and H-bond partner list.
+//
+// Replaces, on the GPU:
+//  * the binned full/ghost neighbour build (npair_full_bin_atomonly_sw5.c:
+//    57-181, npair_full_bin_ghost_sw5.c:80-231) and the far-list filter to
+//    d <= nonb_cut (write_reax_lists_c, pair_reaxc_sw64.c:42-96);
+//  * the QEq H-matrix build (compute_H_Full_C, fix_qeq_reax_sw64.c:768-911),
+//    fused into the pair-list pass because it uses the same pairs;
+//  * the uncorrected bond orders and the full bond list
+//    (Init_Forces_noQEq_Full_C_para, reaxc_forces_sw64.c:996-1318; CPU form
+//    BOp_single, reaxc_forces_sunway.cpp:677-825);
+//  * the H-bond partner list (Init_Forces_noQEq_HB_Full_C,
+//    reaxc_forces_sw64.c:787-863).
+//
+// Instead of ghost atoms every atom is local and each list entry carries the
+// periodic image of its partner.  Membership tests (d^2 <= cut^2, d <=
+// bond_cut, BO' >= bo_cut, d <= hbond_cut) are evaluated in FP64 with
+// explicitly rounded, non-contracted operations so that they reproduce the
+// reference's decisions bit for bit.
+#include <cstdio>
+
+#include "rg_internal.h"
+
+namespace {
+
+constexpr unsigned FULL = 0xffffffffu;
+
+__device__ __forceinline__ unsigned lanemask_lt() {
+  unsigned m;
+  asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+  return m;
+}
+
+// wrap into [0,L) like the host oracle: x - L*floor(x/L), rounded per op
+__device__ __forceinline__ double wrap1(double x, double L) {
+  double y = __dsub_rn(x, __dmul_rn(L, floor(__ddiv_rn(x, L))));
+  if (y >= L) y = __dsub_rn(y, L);
+  if (y < 0.0) y = 0.0;
+  return y;
+}
+
+__device__ __forceinline__ int cell_of(double x, double w, int nc) {
+  int c = (int)(x / w);
+  return c < 0 ? 0 : (c >= nc ? nc - 1 : c);
+}
+
+// -------------------------------------------------------------------
+// binning and sort
+
+__global__ void k_cell_assign(Dev d) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= d.n) return;
+  double x = wrap1(d.x_o[3 * i + 0], d.L[0]);
+  double y = wrap1(d.x_o[3 * i + 1], d.L[1]);
+  double z = wrap1(d.x_o[3 * i + 2], d.L[2]);
+  d.x_o[3 * i + 0] = x;
+  d.x_o[3 * i + 1] = y;
+  d.x_o[3 * i + 2] = z;
+  int cx = cell_of(x, d.cellw[0], d.nc[0]);
+  int cy = cell_of(y, d.cellw[1], d.nc[1]);
+  int cz = cell_of(z, d.cellw[2], d.nc[2]);
+  int c = (cz * d.nc[1] + cy) * d.nc[0] + cx;
+  d.cell_o[i] = c;
+  atomicAdd(&d.cell_count[c], 1);
+}
+
+// exclusive scan of cell_count into cell_start (one block per 1024 cells,
+// then a single-block pass over block sums; enough for < 1M cells)
+__global__ void k_scan_blocks(const int *in, int *out, int *bsum, int n) {
+  __shared__ int s[1024];
+  int t = threadIdx.x, g = blockIdx.x * 1024 + t;
+  int v = g < n ? in[g] : 0;
+  s[t] = v;
+  __syncthreads();
+  for (int off = 1; off < 1024; off <<= 1) {
+    int a = t >= off ? s[t - off] : 0;
+    __syncthreads();
+    s[t] += a;
+    __syncthreads();
+  }
+  if (g < n) out[g] = s[t] - v;
+  if (t == 1023) bsum[blockIdx.x] = s[t];
+}
+
+__global__ void k_scan_sums(int *bsum, int nb, int *total_out) {
+  __shared__ int s[1024];
+  int t = threadIdx.x;
+  // serial over chunks of 1024
+  int carry = 0;
+  for (int base = 0; base < nb; base += 1024) {
+    int v = base + t < nb ? bsum[base + t] : 0;
+    s[t] = v;
+    __syncthreads();
+    for (int off = 1; off < 1024; off <<= 1) {
+      int a = t >= off ? s[t - off] : 0;
+      __syncthreads();
+      s[t] += a;
+      __syncthreads();
+    }
+    if (base + t < nb) bsum[base + t] = carry + s[t] - v;
+    int tot = s[1023];
+    __syncthreads();
+    carry += tot;
+  }
+  if (t == 0 && total_out) *total_out = carry;
+}
+
+__global__ void k_scan_add(int *out, const int *bsum, int n) {
+  int g = blockIdx.x * 1024 + threadIdx.x;
+  if (g < n) out[g] += bsum[blockIdx.x];
+}
+
+__global__ void k_scatter(Dev d) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= d.n) return;
+  int c = d.cell_o[i];
+  int slot = d.cell_start[c] + atomicAdd(&d.cell_fill[c], 1);
+  d.perm[slot] = i;
+}
+
+// deterministic order inside a cell: by original index
+__global__ void k_cell_order(Dev d, int ncell) {
+  int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= ncell) return;
+  int b = d.cell_start[c], e = d.cell_start[c + 1];
+  for (int a = b + 1; a < e; ++a) {
+    int v = d.perm[a], z = a - 1;
+    while (z >= b && d.perm[z] > v) {
+      d.perm[z + 1] = d.perm[z];
+      --z;
+    }
+    d.perm[z + 1] = v;
+  }
+}
+
+__global__ void k_gather(Dev d) {
+  int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= d.n) return;
+  int i = d.perm[s];
+  double x = d.x_o[3 * i], y = d.x_o[3 * i + 1], z = d.x_o[3 * i + 2];
+  d.xs[s] = make_double4(x, y, z, d.q_o[i]);
+  int t = d.type_o[i];
+  d.xf[s] = make_float4((float)x, (float)y, (float)z, __int_as_float(t));
+  d.ts[s] = t;
+  d.tags[s] = d.tag_o[i];
+  d.iperm[i] = s;
+}
+
+// -------------------------------------------------------------------
+// pair list (full, both directions) + QEq H values
+
+__global__ void __launch_bounds__(256) k_build_nbrs(Dev d) {
+  const int lane = threadIdx.x & 31;
+  const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (i >= d.n) return;
+  const Control &C = *d.ctl;
+  const ForceField &F = *d.ff;
+  const double4 xi = d.xs[i];
+  const float4 xif = d.xf[i];
+  const int ti = d.ts[i];
+  const double cut2 = C.list_cut2;
+  const float cut2f = (float)(cut2 * (1.0 + 1e-5) + 0.05);
+  const double nc2 = C.near_cut * C.near_cut;
+  const double nc2lo = nc2 * (1.0 - 1e-12), nc2hi = nc2 * (1.0 + 1e-12);
+  const int cx = cell_of(xi.x, d.cellw[0], d.nc[0]);
+  const int cy = cell_of(xi.y, d.cellw[1], d.nc[1]);
+  const int cz = cell_of(xi.z, d.cellw[2], d.nc[2]);
+  const long long row = (long long)i * d.nb_cap;
+  const int cap = d.nb_cap;
+  const double gam_i = F.sbp[ti].gamma;
+  int cntN = 0, cntF = 0;
+  for (int oz = -d.S; oz <= d.S; ++oz) {
+    int rz = cz + oz, sz = 0;
+    while (rz < 0) { rz += d.nc[2]; --sz; }
+    while (rz >= d.nc[2]) { rz -= d.nc[2]; ++sz; }
+    for (int oy = -d.S; oy <= d.S; ++oy) {
+      int ry = cy + oy, sy = 0;
+      while (ry < 0) { ry += d.nc[1]; --sy; }
+      while (ry >= d.nc[1]) { ry -= d.nc[1]; ++sy; }
+      for (int ox = -d.S; ox <= d.S; ++ox) {
+        int rx = cx + ox, sx = 0;
+        while (rx < 0) { rx += d.nc[0]; --sx; }
+        while (rx >= d.nc[0]) { rx -= d.nc[0]; ++sx; }
+        const int cw = (rz * d.nc[1] + ry) * d.nc[0] + rx;
+        const int beg = d.cell_start[cw], end = d.cell_start[cw + 1];
+        const double shx = sx * d.L[0], shy = sy * d.L[1], shz = sz * d.L[2];
+        const float shxf = (float)shx, shyf = (float)shy, shzf = (float)shz;
+        const bool self_img = (sx == 0 && sy == 0 && sz == 0);
+        const int img = img_pack(sx, sy, sz);
+        for (int base = beg; base < end; base += 32) {
+          const int j = base + lane;
+          bool in = false, near = false;
+          double d2 = 0.0;
+          if (j < end && !(self_img && j == i)) {
+            const float4 xjf = d.xf[j];
+            const float fx = xjf.x + shxf - xif.x;
+            const float fy = xjf.y + shyf - xif.y;
+            const float fz = xjf.z + shzf - xif.z;
+            if (fx * fx + fy * fy + fz * fz <= cut2f) {
+              const double4 xj = d.xs[j];
+              const double dx = __dsub_rn(__dadd_rn(xj.x, shx), xi.x);
+              const double dy = __dsub_rn(__dadd_rn(xj.y, shy), xi.y);
+              const double dz = __dsub_rn(__dadd_rn(xj.z, shz), xi.z);
+              d2 = __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)),
+                             __dmul_rn(dz, dz));
+              in = d2 <= cut2;
+              if (in) {
+                if (d2 <= nc2lo) near = true;
+                else if (d2 > nc2hi) near = false;
+                else near = __dsqrt_rn(d2) <= C.near_cut;
+              }
+            }
+          }
+          const unsigned mn = __ballot_sync(FULL, in && near);
+          const unsigned mf = __ballot_sync(FULL, in && !near);
+          const int tot = cntN + __popc(mn) + cntF + __popc(mf);
+          if (in && tot <= cap) {
+            int pos;
+            if (near) pos = cntN + __popc(mn & lanemask_lt());
+            else pos = cap - 1 - (cntF + __popc(mf & lanemask_lt()));
+            double h = 0.0;
+            if (d2 <= C.swb2) {
+              const double r = __dsqrt_rn(d2);
+              const double *T = C.qTap;
+              double tp = fma(T[7], r, T[6]);
+              tp = fma(tp, r, T[5]);
+              tp = fma(tp, r, T[4]);
+              tp = fma(tp, r, T[3]);
+              tp = fma(tp, r, T[2]);
+              tp = fma(tp, r, T[1]);
+              tp = fma(tp, r, T[0]);
+              const int tj = __float_as_int(d.xf[j].w);
+              // shielding (gamma_i*gamma_j)^-1.5, init_shielding
+              // fix_qeq_reax_sunway.cpp:440-454 (= tbp gamma)
+              const double shld = F.tbp[ti][tj].gamma;
+              (void)gam_i;
+              const double den = cbrt(r * r * r + shld);
+              h = tp * 14.4 / den;
+            }
+            d.nbr[row + pos] = ((uint32_t)j << 8) | (uint32_t)img;
+            d.hval[row + pos] = h;
+          }
+          cntN += __popc(mn);
+          cntF += __popc(mf);
+        }
+      }
+    }
+  }
+  if (lane == 0) {
+    d.n_near[i] = cntN;
+    d.n_far[i] = cntF;
+    if (cntN + cntF > cap) atomicOr(&d.status[ST_OVF], OVF_NBR);
+    atomicMax(&d.status[ST_MAXNB], cntN + cntF);
+  }
+}
+
+// -------------------------------------------------------------------
+// bond list with uncorrected bond orders, and H-bond partners
+
+__global__ void __launch_bounds__(256) k_build_bonds(Dev d) {
+  const int lane = threadIdx.x & 31;
+  const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (i >= d.n) return;
+  const Control &C = *d.ctl;
+  const ForceField &F = *d.ff;
+  const double4 xi = d.xs[i];
+  const int ti = d.ts[i];
+  const Sbp &si = F.sbp[ti];
+  const bool ihb = (si.p_hbond == 1) && C.hbond_cut > 0.0;
+  const long long row = (long long)i * d.nb_cap;
+  const int nn = d.n_near[i] < d.nb_cap ? d.n_near[i] : d.nb_cap;
+  const int n = d.n;
+  int nb = 0, nh = 0;
+  double ddx = 0.0, ddy = 0.0, ddz = 0.0, bsum = 0.0;
+  for (int base = 0; base < nn; base += 32) {
+    const int p = base + lane;
+    bool isb = false, ish = false;
+    uint32_t e = 0;
+    double dist = 0, dx = 0, dy = 0, dz = 0, BO = 0, BOs = 0, BOpi = 0, BOpi2 = 0;
+    double Cs = 0, Cpi = 0, Cpi2 = 0;
+    int tj = 0;
+    if (p < nn) {
+      e = d.nbr[row + p];
+      const int j = (int)(e >> 8);
+      int sx, sy, sz;
+      img_unpack((int)(e & 255u), &sx, &sy, &sz);
+      const double4 xj = d.xs[j];
+      dx = __dsub_rn(__dadd_rn(xj.x, sx * d.L[0]), xi.x);
+      dy = __dsub_rn(__dadd_rn(xj.y, sy * d.L[1]), xi.y);
+      dz = __dsub_rn(__dadd_rn(xj.z, sz * d.L[2]), xi.z);
+      const double d2 = __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)),
+                                  __dmul_rn(dz, dz));
+      dist = __dsqrt_rn(d2);
+      tj = d.ts[j];
+      const Sbp &sj = F.sbp[tj];
+      if (ihb && dist <= C.hbond_cut && sj.p_hbond == 2) ish = true;
+      if (dist <= C.bond_cut) {
+        const Tbp &tw = F.tbp[ti][tj];
+        double C12 = 0, C34 = 0, C56 = 0;
+        if (si.r_s > 0.0 && sj.r_s > 0.0) {
+          C12 = tw.p_bo1 * pow(dist / tw.r_s, tw.p_bo2);
+          BOs = (1.0 + C.bo_cut) * exp(C12);
+        }
+        if (si.r_pi > 0.0 && sj.r_pi > 0.0) {
+          C34 = tw.p_bo3 * pow(dist / tw.r_p, tw.p_bo4);
+          BOpi = exp(C34);
+        }
+        if (si.r_pi_pi > 0.0 && sj.r_pi_pi > 0.0) {
+          C56 = tw.p_bo5 * pow(dist / tw.r_pp, tw.p_bo6);
+          BOpi2 = exp(C56);
+        }
+        BO = BOs + BOpi + BOpi2;
+        if (BO >= C.bo_cut) {
+          isb = true;
+          const double r2 = dist * dist;
+          Cs = tw.p_bo2 * C12 / r2;
+          Cpi = tw.p_bo4 * C34 / r2;
+          Cpi2 = tw.p_bo6 * C56 / r2;
+        }
+      }
+    }
+    const unsigned mb = __ballot_sync(FULL, isb);
+    const unsigned mh = __ballot_sync(FULL, ish);
+    if (isb) {
+      const int k = nb + __popc(mb & lanemask_lt());
+      const double g = -(BOs * Cs + BOpi * Cpi + BOpi2 * Cpi2);
+      const double gx = g * dx, gy = g * dy, gz = g * dz;
+      ddx += gx; ddy += gy; ddz += gz;
+      const double BOc = BO - C.bo_cut;
+      bsum += BOc;
+      if (k < d.bond_cap) {
+        const long long s = (long long)k * n + i;
+        const long long S3 = (long long)d.bond_cap * n;
+        d.b_nbr[s] = e;
+        d.b_d[s] = dist;
+        d.b_dx[s] = dx; d.b_dy[s] = dy; d.b_dz[s] = dz;
+        d.b_BO[s] = BOc;
+        d.b_BOs[s] = BOs - C.bo_cut;
+        d.b_BOpi[s] = BOpi;
+        d.b_BOpi2[s] = BOpi2;
+        d.b_dBOp[s] = gx; d.b_dBOp[S3 + s] = gy; d.b_dBOp[2 * S3 + s] = gz;
+        const double api = -BOpi * Cpi, api2 = -BOpi2 * Cpi2;
+        d.b_dlnpi[s] = api * dx; d.b_dlnpi[S3 + s] = api * dy; d.b_dlnpi[2 * S3 + s] = api * dz;
+        d.b_dlnpi2[s] = api2 * dx; d.b_dlnpi2[S3 + s] = api2 * dy; d.b_dlnpi2[2 * S3 + s] = api2 * dz;
+        d.b_Cdbo[s] = 0.0; d.b_Cdbopi[s] = 0.0; d.b_Cdbopi2[s] = 0.0;
+      }
+    }
+    if (ish) {
+      const int k = nh + __popc(mh & lanemask_lt());
+      if (k < d.hb_cap) d.hb_nbr[(long long)i * d.hb_cap + k] = e;
+    }
+    nb += __popc(mb);
+    nh += __popc(mh);
+  }
+  // warp sums in lane order (deterministic)
+  for (int off = 16; off > 0; off >>= 1) {
+    ddx += __shfl_down_sync(FULL, ddx, off);
+    ddy += __shfl_down_sync(FULL, ddy, off);
+    ddz += __shfl_down_sync(FULL, ddz, off);
+    bsum += __shfl_down_sync(FULL, bsum, off);
+  }
+  if (lane == 0) {
+    d.nbonds[i] = nb;
+    d.nhb[i] = nh;
+    d.dDeltap[i] = ddx;
+    d.dDeltap[n + i] = ddy;
+    d.dDeltap[2 * n + i] = ddz;
+    d.bo0[i] = bsum;
+    if (nb > d.bond_cap) atomicOr(&d.status[ST_OVF], OVF_BOND);
+    if (nh > d.hb_cap) atomicOr(&d.status[ST_OVF], OVF_HB);
+    atomicMax(&d.status[ST_MAXB], nb);
+    atomicMax(&d.status[ST_MAXHB], nh);
+  }
+}
+
+// symmetric partner of each bond: (j -> i, -image) in j's list
+__global__ void k_bond_sym(Dev d) {
+  const int n = d.n;
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = (int)(t % n), k = (int)(t / n);
+  if (k >= d.bond_cap || i >= n) return;
+  if (k >= d.nbonds[i]) return;
+  const long long s = (long long)k * n + i;
+  const uint32_t e = d.b_nbr[s];
+  const int j = (int)(e >> 8);
+  int sx, sy, sz;
+  img_unpack((int)(e & 255u), &sx, &sy, &sz);
+  const uint32_t want = ((uint32_t)i << 8) | (uint32_t)img_pack(-sx, -sy, -sz);
+  const int nbj = min(d.nbonds[j], d.bond_cap);
+  int sym = -1;
+  for (int q = 0; q < nbj; ++q)
+    if (d.b_nbr[(long long)q * n + j] == want) sym = q * n + j;
+  d.b_sym[s] = sym;
+}
+
+}  // namespace
+
+void launch_bin_sort(const Dev &d, cudaStream_t st) {
+  const int ncell = d.nc[0] * d.nc[1] * d.nc[2];
+  cudaMemsetAsync(d.cell_count, 0, sizeof(int) * (ncell + 1), st);
+  cudaMemsetAsync(d.cell_fill, 0, sizeof(int) * (ncell + 1), st);
+  const int B = 256;
+  k_cell_assign<<<(d.n + B - 1) / B, B, 0, st>>>(d);
+  const int nb = (ncell + 1 + 1023) / 1024;
+  // block sums live after the cell_fill counters
+  int *bsum = d.cell_fill + (ncell + 1);
+  k_scan_blocks<<<nb, 1024, 0, st>>>(d.cell_count, d.cell_start, bsum, ncell + 1);
+  k_scan_sums<<<1, 1024, 0, st>>>(bsum, nb, nullptr);
+  k_scan_add<<<nb, 1024, 0, st>>>(d.cell_start, bsum, ncell + 1);
+  k_scatter<<<(d.n + B - 1) / B, B, 0, st>>>(d);
+  k_cell_order<<<(ncell + B - 1) / B, B, 0, st>>>(d, ncell);
+  k_gather<<<(d.n + B - 1) / B, B, 0, st>>>(d);
+}
+
+void launch_build_nbrs(const Dev &d, cudaStream_t st) {
+  const long long threads = (long long)d.n * 32;
+  k_build_nbrs<<<(unsigned)((threads + 255) / 256), 256, 0, st>>>(d);
+}
+
+void launch_build_bonds(const Dev &d, cudaStream_t st) {
+  const long long threads = (long long)d.n * 32;
+  k_build_bonds<<<(unsigned)((threads + 255) / 256), 256, 0, st>>>(d);
+  const long long slots = (long long)d.n * d.bond_cap;
+  k_bond_sym<<<(unsigned)((slots + 255) / 256), 256, 0, st>>>(d);
+}
+
+void launch_zero(void *p, size_t bytes, cudaStream_t st) { cudaMemsetAsync(p, 0, bytes, st); }

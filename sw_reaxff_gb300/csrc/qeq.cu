@@ -1,0 +1,305 @@
+// QEq charge equilibration: the s and t systems of the reference solved
+// together ("dual"), each with the reference's pipelined Jacobi-PCG.
+//
+//  k_qeq_setup   init_matvec: Jacobi diagonal, b_s = -chi, b_t = -1, cubic
+//                (s) / quadratic (t) extrapolation from the 5-deep
+//                histories (fix_qeq_reax_sunway.cpp:618-723)
+//  k_spmv        sparse_matvec: b_i = eta_i x_i + sum_j H_ij x_j over the
+//                full rows (fix_qeq_reax_sw64.c:357-498), both systems per
+//                read of H
+//  k_cg_*        CG_v2 (fix_qeq_reax_sunway.cpp:983-1167): the same
+//                recurrences per system; a system that has converged stops
+//                updating, so each keeps the iterate and iteration count
+//                of a solve on its own
+//  k_qeq_finish  calculate_Q (fix_qeq_reax_sunway.cpp:1697-1755)
+#include "rg_internal.h"
+
+namespace {
+
+constexpr unsigned FULL = 0xffffffffu;
+
+// scalar slots in d.red (pairs: [s, t])
+enum {
+  R_ACC0 = 0, R_ACC1 = 2, R_ACC2 = 4, R_ALPHA = 6, R_ALPHA_OLD = 8, R_BETA = 10,
+  R_SIG = 12, R_HETA = 14, R_BNORM = 16, R_DOTP = 18, R_ACTIVE = 20, R_ITERS = 22,
+  R_SUM = 24, R_TOL = 26, R_IMAX = 27, R_NRED = 32
+};
+
+__device__ __forceinline__ double warp_sum(double v) {
+  for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(FULL, v, off);
+  return v;
+}
+
+// block-reduce up to 6 values and atomically add to dst[0..k)
+template <int K>
+__device__ __forceinline__ void block_add_k(double *v, double *dst) {
+  __shared__ double red[K][32];
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+#pragma unroll
+  for (int c = 0; c < K; ++c) v[c] = warp_sum(v[c]);
+  if (l == 0)
+#pragma unroll
+    for (int c = 0; c < K; ++c) red[c][w] = v[c];
+  __syncthreads();
+  if (w == 0) {
+#pragma unroll
+    for (int c = 0; c < K; ++c) {
+      double x = (l < (int)(blockDim.x >> 5)) ? red[c][l] : 0.0;
+      x = warp_sum(x);
+      if (l == 0) atomicAdd(&dst[c], x);
+    }
+  }
+}
+
+__global__ void k_qeq_setup(Dev d) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= d.n) return;
+  const int n = d.n, i = d.perm[s];
+  const Sbp &sb = d.ff->sbp[d.ts[s]];
+  d.Hdia_inv[s] = 1. / sb.eta;
+  d.qb[s] = make_double2(-sb.chi, -1.0);
+  const double *sh = d.s_hist, *th = d.t_hist;
+  const double s0 = 4 * (sh[0 * n + i] + sh[2 * n + i]) - (6 * sh[1 * n + i] + sh[3 * n + i]);
+  const double t0 = th[2 * n + i] + 3 * (th[0 * n + i] - th[1 * n + i]);
+  d.qx[s] = make_double2(s0, t0);
+}
+
+// y = H x (+ eta x on the diagonal), one warp per row
+__global__ void __launch_bounds__(256) k_spmv(Dev d, const double2 *__restrict__ x, double2 *__restrict__ y) {
+  const int lane = threadIdx.x & 31;
+  const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (i >= d.n) return;
+  const long long row = (long long)i * d.nb_cap;
+  const int nn = d.n_near[i], nf = d.n_far[i], cap = d.nb_cap;
+  const int tot = min(nn + nf, cap);
+  double as = 0.0, at = 0.0;
+  for (int p = lane; p < tot; p += 32) {
+    const int slot = p < nn ? p : cap - 1 - (p - nn);
+    const uint32_t e = d.nbr[row + slot];
+    const double h = d.hval[row + slot];
+    const double2 xj = x[e >> 8];
+    as = fma(h, xj.x, as);
+    at = fma(h, xj.y, at);
+  }
+  as = warp_sum(as);
+  at = warp_sum(at);
+  if (lane == 0) {
+    const double eta = d.ff->sbp[d.ts[i]].eta;
+    const double2 xi = x[i];
+    y[i] = make_double2(fma(eta, xi.x, as), fma(eta, xi.y, at));
+  }
+}
+
+// r = b - q; u = r*Hdia_inv; d = u
+__global__ void k_cg_init1(Dev d) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= d.n) return;
+  const double hi = d.Hdia_inv[s];
+  const double2 b = d.qb[s], q = d.qq[s];
+  const double2 r = make_double2(b.x - 1 * q.x, b.y - 1 * q.y);
+  d.qr[s] = r;
+  const double2 u = make_double2(r.x * hi, r.y * hi);
+  d.qu[s] = u;
+  d.qd[s] = u;
+}
+
+// w = q; m = q*Hdia_inv; d = m
+__global__ void k_cg_init2(Dev d) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= d.n) return;
+  const double hi = d.Hdia_inv[s];
+  const double2 q = d.qq[s];
+  d.qw[s] = q;
+  const double2 m = make_double2(q.x * hi, q.y * hi);
+  d.qm[s] = m;
+  d.qd[s] = m;
+}
+
+// p = u; s = w; v = m; z = q; sums b.b, u.r, u.w
+__global__ void k_cg_init3(Dev d) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  double v[6] = {0, 0, 0, 0, 0, 0};
+  if (s < d.n) {
+    const double2 u = d.qu[s], w = d.qw[s], m = d.qm[s], r = d.qr[s], b = d.qb[s];
+    d.qp[s] = u;
+    d.qs[s] = w;
+    d.qv[s] = m;
+    d.qz[s] = d.qq[s];
+    v[0] = b.x * b.x; v[1] = b.y * b.y;
+    v[2] = u.x * r.x; v[3] = u.y * r.y;
+    v[4] = u.x * w.x; v[5] = u.y * w.y;
+  }
+  block_add_k<6>(v, d.red + R_ACC2 + 64);   // scratch area 68..73
+}
+
+__global__ void k_cg_init_ctrl(Dev d) {
+  double *R = d.red;
+  const double tol = R[R_TOL];
+  const int imax = (int)R[R_IMAX];
+  for (int c = 0; c < 2; ++c) {
+    const double bb = R[68 + c], ur = R[70 + c], uw = R[72 + c];
+    R[R_BNORM + c] = sqrt(bb);
+    R[R_SIG + c] = ur;
+    R[R_HETA + c] = uw;
+    R[R_ALPHA + c] = ur / uw;
+    R[R_DOTP + c] = ur;
+    R[R_ITERS + c] = 1.0;
+    R[R_ACTIVE + c] = (1 < imax && sqrt(ur) / R[R_BNORM + c] > tol) ? 1.0 : 0.0;
+    R[R_ACC0 + c] = 0.0;
+    R[R_ACC1 + c] = 0.0;
+  }
+}
+
+// A: r -= a s; u -= a v; w -= a z; acc u.r, u.w; d = w*Hdia_inv
+__global__ void k_cg_A(Dev d) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  const double *R = d.red;
+  const bool as = R[R_ACTIVE] != 0.0, at = R[R_ACTIVE + 1] != 0.0;
+  double v[2] = {0, 0}, v1[2] = {0, 0};
+  if (s < d.n && (as || at)) {
+    const double hi = d.Hdia_inv[s];
+    double2 r = d.qr[s], u = d.qu[s], w = d.qw[s];
+    const double2 ss = d.qs[s], vv = d.qv[s], z = d.qz[s];
+    double2 dd = d.qd[s];
+    if (as) {
+      const double a = R[R_ALPHA];
+      r.x -= a * ss.x; u.x -= a * vv.x; w.x -= a * z.x;
+      v[0] = u.x * r.x; v1[0] = u.x * w.x;
+      dd.x = w.x * hi;
+    }
+    if (at) {
+      const double a = R[R_ALPHA + 1];
+      r.y -= a * ss.y; u.y -= a * vv.y; w.y -= a * z.y;
+      v[1] = u.y * r.y; v1[1] = u.y * w.y;
+      dd.y = w.y * hi;
+    }
+    d.qr[s] = r; d.qu[s] = u; d.qw[s] = w; d.qd[s] = dd;
+  }
+  double all[4] = {v[0], v[1], v1[0], v1[1]};
+  block_add_k<4>(all, d.red + R_ACC0);   // ACC0[2], ACC1[2] are contiguous
+}
+
+// scalars after A: beta, heta, alpha; activity of the next iteration
+__global__ void k_cg_ctrl(Dev d) {
+  double *R = d.red;
+  const double tol = R[R_TOL];
+  const int imax = (int)R[R_IMAX];
+  for (int c = 0; c < 2; ++c) {
+    if (R[R_ACTIVE + c] == 0.0) {
+      R[R_ACC0 + c] = 0.0;
+      R[R_ACC1 + c] = 0.0;
+      continue;
+    }
+    const double dot0 = R[R_ACC0 + c], dot1 = R[R_ACC1 + c];
+    const double beta = dot0 / R[R_SIG + c];
+    const double heta = dot1 - beta * beta * R[R_HETA + c];
+    R[R_BETA + c] = beta;
+    R[R_HETA + c] = heta;
+    R[R_ALPHA_OLD + c] = R[R_ALPHA + c];
+    R[R_ALPHA + c] = dot0 / heta;
+    R[R_SIG + c] = dot0;
+    R[R_DOTP + c] = dot0;
+    R[R_ACC0 + c] = 0.0;
+    R[R_ACC1 + c] = 0.0;
+    // loop increment and test of the next iteration
+    const double it = R[R_ITERS + c] + 1.0;
+    R[R_ITERS + c] = it;
+    R[R_ACTIVE + c + 32] = (it < imax && sqrt(dot0) / R[R_BNORM + c] > tol) ? 1.0 : 0.0;
+  }
+}
+
+// C: x += a_old p; p = u + b p; s = w + b s; v = d + b v; z = q + b z
+__global__ void k_cg_C(Dev d) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  double *R = d.red;
+  const bool as = R[R_ACTIVE] != 0.0, at = R[R_ACTIVE + 1] != 0.0;
+  if (s < d.n && (as || at)) {
+    double2 x = d.qx[s], p = d.qp[s], ss = d.qs[s], v = d.qv[s], z = d.qz[s];
+    const double2 u = d.qu[s], w = d.qw[s], dd = d.qd[s], q = d.qq[s];
+    if (as) {
+      const double a = R[R_ALPHA_OLD], b = R[R_BETA];
+      x.x += a * p.x; p.x = u.x + p.x * b; ss.x = w.x + ss.x * b; v.x = dd.x + v.x * b; z.x = q.x + z.x * b;
+    }
+    if (at) {
+      const double a = R[R_ALPHA_OLD + 1], b = R[R_BETA + 1];
+      x.y += a * p.y; p.y = u.y + p.y * b; ss.y = w.y + ss.y * b; v.y = dd.y + v.y * b; z.y = q.y + z.y * b;
+    }
+    d.qx[s] = x; d.qp[s] = p; d.qs[s] = ss; d.qv[s] = v; d.qz[s] = z;
+  }
+}
+
+// the activity decided in k_cg_ctrl takes effect for the next iteration
+__global__ void k_cg_flip(Dev d) {
+  double *R = d.red;
+  for (int c = 0; c < 2; ++c)
+    if (R[R_ACTIVE + c] != 0.0) R[R_ACTIVE + c] = R[R_ACTIVE + c + 32];
+}
+
+__global__ void k_qeq_sums(Dev d) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  double v[2] = {0, 0};
+  if (s < d.n) {
+    const double2 x = d.qx[s];
+    v[0] = x.x;
+    v[1] = x.y;
+  }
+  block_add_k<2>(v, d.red + R_SUM);
+}
+
+// q = s - (sum s / sum t) t; shift histories (original order)
+__global__ void k_qeq_finish(Dev d) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= d.n) return;
+  const int n = d.n, i = d.perm[s];
+  const double u = d.red[R_SUM] / d.red[R_SUM + 1];
+  const double2 x = d.qx[s];
+  const double q = x.x - u * x.y;
+  d.q_o[i] = q;
+  d.xs[s].w = q;
+  for (int k = 4; k > 0; --k) {
+    d.s_hist[k * n + i] = d.s_hist[(k - 1) * n + i];
+    d.t_hist[k * n + i] = d.t_hist[(k - 1) * n + i];
+  }
+  d.s_hist[i] = x.x;
+  d.t_hist[i] = x.y;
+}
+
+}  // namespace
+
+void launch_qeq_setup(const Dev &d, cudaStream_t st) {
+  const int B = 256;
+  k_qeq_setup<<<(d.n + B - 1) / B, B, 0, st>>>(d);
+}
+
+void launch_qeq_spmv(const Dev &d, cudaStream_t st, const double2 *x, double2 *y) {
+  const long long threads = (long long)d.n * 32;
+  k_spmv<<<(unsigned)((threads + 255) / 256), 256, 0, st>>>(d, x, y);
+}
+
+void launch_qeq_cg_init(const Dev &d, cudaStream_t st) {
+  const int B = 256, G = (d.n + B - 1) / B;
+  launch_qeq_spmv(d, st, d.qx, d.qq);
+  k_cg_init1<<<G, B, 0, st>>>(d);
+  launch_qeq_spmv(d, st, d.qd, d.qq);
+  k_cg_init2<<<G, B, 0, st>>>(d);
+  launch_qeq_spmv(d, st, d.qd, d.qq);
+  cudaMemsetAsync(d.red + 68, 0, 6 * sizeof(double), st);
+  k_cg_init3<<<G, B, 0, st>>>(d);
+  k_cg_init_ctrl<<<1, 1, 0, st>>>(d);
+}
+
+void launch_qeq_cg_iter(const Dev &d, cudaStream_t st) {
+  const int B = 256, G = (d.n + B - 1) / B;
+  k_cg_A<<<G, B, 0, st>>>(d);
+  launch_qeq_spmv(d, st, d.qd, d.qq);
+  k_cg_ctrl<<<1, 1, 0, st>>>(d);
+  k_cg_C<<<G, B, 0, st>>>(d);
+  k_cg_flip<<<1, 1, 0, st>>>(d);
+}
+
+void launch_qeq_finish(const Dev &d, cudaStream_t st) {
+  const int B = 256, G = (d.n + B - 1) / B;
+  cudaMemsetAsync(d.red + R_SUM, 0, 2 * sizeof(double), st);
+  k_qeq_sums<<<G, B, 0, st>>>(d);
+  k_qeq_finish<<<G, B, 0, st>>>(d);
+}

@@ -1,0 +1,671 @@
+// Host side of the reaxgpu C ABI (include/reaxgpu.h): handle management,
+// device memory, list capacity growth and the per-step orchestration of the
+// kernels in lists.cu, bonded.cu, nonbonded.cu, qeq.cu and nve.cu.
+//
+// The step order follows PairReaxCSunway::compute (pair_reaxc_sunway.cpp:
+// 541-793) / Compute_Forces (reaxc_forces_sunway.cpp:1297-1365): lists ->
+// bond orders -> bonded terms (bond/lp/ov/un, H-bonds, valence+torsion) ->
+// nonbonded -> dBond force assembly -> force copy-out; QEq
+// (FixQEqReaxSunway::pre_force) runs before it on the same pair list.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/reaxgpu.h"
+#include "rg_internal.h"
+
+struct rg_system {
+  rg_params p{};
+  ForceField ff{};
+  Control ctl{};
+  ForceField *d_ff = nullptr;
+  Control *d_ctl = nullptr;
+  cudaStream_t st = nullptr;
+  std::string err;
+  int n = 0;
+  double L[3] = {0, 0, 0};
+  bool have_box = false;
+  Dev d{};
+  std::vector<void *> per_n;    // allocations sized by n
+  std::vector<void *> per_nb;   // sized by n * nb_cap
+  std::vector<void *> per_b;    // sized by n * bond_cap
+  std::vector<void *> per_hb;   // sized by n * hb_cap
+  void *cells = nullptr;
+  int ncell_alloc = 0;
+  bool lists_valid = false;
+  bool forces_valid = false;
+  rg_stats stats{};
+  double energy[RG_NE] = {0};
+};
+
+namespace {
+
+int fail(rg_system *h, int code, const std::string &msg) {
+  if (h) h->err = msg;
+  return code;
+}
+
+#define CK(call)                                                              \
+  do {                                                                        \
+    cudaError_t e_ = (call);                                                  \
+    if (e_ != cudaSuccess)                                                    \
+      return fail(h, RG_E_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+  } while (0)
+
+template <class T>
+int dalloc(rg_system *h, std::vector<void *> &bucket, T **p, size_t count) {
+  void *q = nullptr;
+  cudaError_t e = cudaMalloc(&q, std::max<size_t>(count, 1) * sizeof(T));
+  if (e != cudaSuccess)
+    return fail(h, RG_E_CUDA, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+  bucket.push_back(q);
+  *p = (T *)q;
+  return 0;
+}
+
+void free_bucket(std::vector<void *> &b) {
+  for (void *p : b) cudaFree(p);
+  b.clear();
+}
+
+double list_cutoff(const rg_system *h) {
+  return std::max(h->ctl.nonb_cut, h->p.qeq_swb);
+}
+
+int setup_cells(rg_system *h) {
+  const double rc = list_cutoff(h);
+  const int S = 2;
+  Dev &d = h->d;
+  d.S = S;
+  for (int k = 0; k < 3; ++k) {
+    if (h->L[k] < rc / S)
+      return fail(h, RG_E_ARG, "box edge shorter than half the pair cutoff is not supported");
+    int nc = (int)std::floor(h->L[k] * S / (rc * (1.0 + 1e-9)));
+    nc = std::max(nc, 1);
+    d.nc[k] = nc;
+    d.cellw[k] = h->L[k] / nc;
+    d.L[k] = h->L[k];
+  }
+  const long long ncell = (long long)d.nc[0] * d.nc[1] * d.nc[2];
+  if (ncell > (1LL << 26)) return fail(h, RG_E_ARG, "too many cells");
+  if (ncell > h->ncell_alloc) {
+    if (h->cells) cudaFree(h->cells);
+    const size_t nb = (ncell + 1 + 1023) / 1024 + 1;
+    // count | start | fill + block sums
+    CK(cudaMalloc(&h->cells, sizeof(int) * (3 * (ncell + 1) + nb)));
+    h->ncell_alloc = (int)ncell;
+  }
+  int *c = (int *)h->cells;
+  d.cell_count = c;
+  d.cell_start = c + (ncell + 1);
+  d.cell_fill = c + 2 * (ncell + 1);
+  return 0;
+}
+
+int alloc_bonds(rg_system *h) {
+  free_bucket(h->per_b);
+  Dev &d = h->d;
+  const size_t S = (size_t)d.n * d.bond_cap;
+  int r = 0;
+  r |= dalloc(h, h->per_b, &d.b_nbr, S);
+  r |= dalloc(h, h->per_b, &d.b_sym, S);
+  r |= dalloc(h, h->per_b, &d.b_d, S);
+  r |= dalloc(h, h->per_b, &d.b_dx, S);
+  r |= dalloc(h, h->per_b, &d.b_dy, S);
+  r |= dalloc(h, h->per_b, &d.b_dz, S);
+  r |= dalloc(h, h->per_b, &d.b_BO, S);
+  r |= dalloc(h, h->per_b, &d.b_BOs, S);
+  r |= dalloc(h, h->per_b, &d.b_BOpi, S);
+  r |= dalloc(h, h->per_b, &d.b_BOpi2, S);
+  r |= dalloc(h, h->per_b, &d.b_dBOp, 3 * S);
+  r |= dalloc(h, h->per_b, &d.b_dlnpi, 3 * S);
+  r |= dalloc(h, h->per_b, &d.b_dlnpi2, 3 * S);
+  r |= dalloc(h, h->per_b, &d.b_C, 11 * S);
+  r |= dalloc(h, h->per_b, &d.b_Cdbo, S);
+  r |= dalloc(h, h->per_b, &d.b_Cdbopi, S);
+  r |= dalloc(h, h->per_b, &d.b_Cdbopi2, S);
+  return r;
+}
+
+int alloc_nbrs(rg_system *h) {
+  free_bucket(h->per_nb);
+  Dev &d = h->d;
+  const size_t S = (size_t)d.n * d.nb_cap;
+  int r = 0;
+  r |= dalloc(h, h->per_nb, &d.nbr, S);
+  r |= dalloc(h, h->per_nb, &d.hval, S);
+  return r;
+}
+
+int alloc_hb(rg_system *h) {
+  free_bucket(h->per_hb);
+  Dev &d = h->d;
+  return dalloc(h, h->per_hb, &d.hb_nbr, (size_t)d.n * d.hb_cap);
+}
+
+int alloc_atoms(rg_system *h, int n) {
+  free_bucket(h->per_n);
+  Dev &d = h->d;
+  d.n = n;
+  int r = 0;
+  auto &B = h->per_n;
+  r |= dalloc(h, B, &d.x_o, 3 * (size_t)n);
+  r |= dalloc(h, B, &d.v_o, 3 * (size_t)n);
+  r |= dalloc(h, B, &d.q_o, (size_t)n);
+  r |= dalloc(h, B, &d.f_o, 3 * (size_t)n);
+  r |= dalloc(h, B, &d.type_o, (size_t)n);
+  r |= dalloc(h, B, &d.tag_o, (size_t)n);
+  r |= dalloc(h, B, &d.s_hist, 5 * (size_t)n);
+  r |= dalloc(h, B, &d.t_hist, 5 * (size_t)n);
+  r |= dalloc(h, B, &d.cell_o, (size_t)n);
+  r |= dalloc(h, B, &d.perm, (size_t)n);
+  r |= dalloc(h, B, &d.iperm, (size_t)n);
+  r |= dalloc(h, B, &d.xs, (size_t)n);
+  r |= dalloc(h, B, &d.xf, (size_t)n);
+  r |= dalloc(h, B, &d.ts, (size_t)n);
+  r |= dalloc(h, B, &d.tags, (size_t)n);
+  r |= dalloc(h, B, &d.n_near, (size_t)n);
+  r |= dalloc(h, B, &d.n_far, (size_t)n);
+  r |= dalloc(h, B, &d.nbonds, (size_t)n);
+  r |= dalloc(h, B, &d.nhb, (size_t)n);
+  double **pd[] = {&d.bo0, &d.Deltap, &d.Deltap_boc, &d.Delta, &d.Delta_e, &d.Delta_boc,
+                   &d.Delta_val, &d.vlpex, &d.nlp, &d.Delta_lp, &d.Delta_lp_temp,
+                   &d.dDelta_lp, &d.nlp_temp, &d.Hdia_inv};
+  for (double **q : pd) r |= dalloc(h, B, q, (size_t)n);
+  r |= dalloc(h, B, &d.dDeltap, 3 * (size_t)n);
+  r |= dalloc(h, B, &d.fC, 4 * (size_t)n);
+  double2 **pv[] = {&d.qx, &d.qb, &d.qr, &d.qu, &d.qw, &d.qd, &d.qq, &d.qp, &d.qs, &d.qv, &d.qz, &d.qm};
+  for (double2 **q : pv) r |= dalloc(h, B, q, (size_t)n);
+  r |= dalloc(h, B, &d.red, 128);
+  r |= dalloc(h, B, &d.energy, RG_NE);
+  r |= dalloc(h, B, &d.status, 8);
+  if (r) return RG_E_CUDA;
+  // capacity estimates from the mean density
+  const double vol = h->L[0] * h->L[1] * h->L[2];
+  const double rho = n / vol;
+  const double rc = list_cutoff(h);
+  const double pi = 3.14159265358979;
+  int nb = (int)(1.6 * 4.0 / 3.0 * pi * rc * rc * rc * rho) + 64;
+  nb = (nb + 31) / 32 * 32;
+  d.nb_cap = nb;
+  d.bond_cap = 16;
+  const double hc = std::max(h->ctl.hbond_cut, 1.0);
+  d.hb_cap = (int)(1.6 * 4.0 / 3.0 * pi * hc * hc * hc * rho) + 32;
+  r |= alloc_nbrs(h);
+  r |= alloc_bonds(h);
+  r |= alloc_hb(h);
+  return r ? RG_E_CUDA : 0;
+}
+
+int read_status(rg_system *h, int *st) {
+  CK(cudaMemcpyAsync(st, h->d.status, 8 * sizeof(int), cudaMemcpyDeviceToHost, h->st));
+  CK(cudaStreamSynchronize(h->st));
+  return 0;
+}
+
+int build_lists(rg_system *h) {
+  Dev &d = h->d;
+  if (!d.n) return fail(h, RG_E_STATE, "no atoms set");
+  int rc = setup_cells(h);
+  if (rc) return rc;
+  CK(cudaMemsetAsync(d.status, 0, 8 * sizeof(int), h->st));
+  launch_bin_sort(d, h->st);
+  int st[8];
+  for (int attempt = 0;; ++attempt) {
+    launch_build_nbrs(d, h->st);
+    if ((rc = read_status(h, st))) return rc;
+    if (!(st[ST_OVF] & OVF_NBR)) break;
+    if (attempt > 3) return fail(h, RG_E_CAPACITY, "pair list capacity");
+    d.nb_cap = (int)(st[ST_MAXNB] * 1.2) / 32 * 32 + 64;
+    h->stats.regrows++;
+    if ((rc = alloc_nbrs(h))) return rc;
+    CK(cudaMemsetAsync(d.status, 0, 8 * sizeof(int), h->st));
+  }
+  for (int attempt = 0;; ++attempt) {
+    launch_build_bonds(d, h->st);
+    if ((rc = read_status(h, st))) return rc;
+    if (!(st[ST_OVF] & (OVF_BOND | OVF_HB))) break;
+    if (attempt > 3) return fail(h, RG_E_CAPACITY, "bond list capacity");
+    if (st[ST_OVF] & OVF_BOND) {
+      d.bond_cap = st[ST_MAXB] + 4;
+      if ((rc = alloc_bonds(h))) return rc;
+    }
+    if (st[ST_OVF] & OVF_HB) {
+      d.hb_cap = (int)(st[ST_MAXHB] * 1.2) + 16;
+      if ((rc = alloc_hb(h))) return rc;
+    }
+    h->stats.regrows++;
+    CK(cudaMemsetAsync(d.status, 0, 8 * sizeof(int), h->st));
+  }
+  h->stats.max_nbrs = st[ST_MAXNB];
+  h->stats.max_bonds = st[ST_MAXB];
+  h->stats.max_hbonds = st[ST_MAXHB];
+  h->lists_valid = true;
+  return 0;
+}
+
+int do_compute(rg_system *h, int eflag) {
+  Dev &d = h->d;
+  int rc;
+  if (!h->lists_valid && (rc = build_lists(h))) return rc;
+  CK(cudaMemsetAsync(d.fC, 0, 4 * sizeof(double) * (size_t)d.n, h->st));
+  CK(cudaMemsetAsync(d.energy, 0, RG_NE * sizeof(double), h->st));
+  launch_bond_orders(d, h->st);
+  launch_bonded_terms(d, h->st, eflag);
+  launch_nonbonded(d, h->st, eflag);
+  launch_dbond_forces(d, h->st);
+  launch_force_out(d, h->st);
+  CK(cudaGetLastError());
+  h->forces_valid = true;
+  return 0;
+}
+
+int do_qeq(rg_system *h, int *its, int *itt) {
+  Dev &d = h->d;
+  int rc;
+  if (!h->lists_valid && (rc = build_lists(h))) return rc;
+  double hostred[2] = {h->p.qeq_tol, (double)h->p.qeq_imax};
+  CK(cudaMemcpyAsync(d.red + 26, hostred, 2 * sizeof(double), cudaMemcpyHostToDevice, h->st));
+  launch_qeq_setup(d, h->st);
+  launch_qeq_cg_init(d, h->st);
+  // iterate; poll the activity flags every few iterations
+  double flags[4];
+  int done_iters = 0;
+  const int chunk = 4;
+  for (;;) {
+    CK(cudaMemcpyAsync(flags, d.red + 20, 4 * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+    CK(cudaStreamSynchronize(h->st));
+    if (flags[0] == 0.0 && flags[1] == 0.0) break;
+    if (done_iters > h->p.qeq_imax + 8) return fail(h, RG_E_NUMERIC, "QEq iteration control lost");
+    for (int k = 0; k < chunk; ++k) launch_qeq_cg_iter(d, h->st);
+    done_iters += chunk;
+  }
+  h->stats.cg_iters_s = (int)flags[2];
+  h->stats.cg_iters_t = (int)flags[3];
+  if (its) *its = (int)flags[2];
+  if (itt) *itt = (int)flags[3];
+  launch_qeq_finish(d, h->st);
+  CK(cudaGetLastError());
+  return 0;
+}
+
+}  // namespace
+
+extern "C" {
+
+void rg_default_params(rg_params *p) {
+  p->bond_cut = 5.0;
+  p->hbond_cut = 7.5;
+  p->thb_cut = 0.001;
+  p->thb_cutsq = 0.00001;
+  p->enobondsflag = 1;
+  p->lgflag = 0;
+  p->qeq_swa = 0.0;
+  p->qeq_swb = 10.0;
+  p->qeq_tol = 1e-6;
+  p->qeq_imax = 200;
+  p->precision = RG_PREC_FP64;
+  p->device = 0;
+}
+
+int rg_create(const char *ffield_path, const rg_params *pin, rg_system **out) {
+  if (!out || !ffield_path) return RG_E_ARG;
+  *out = nullptr;
+  rg_system *h = new rg_system();
+  if (pin) h->p = *pin;
+  else rg_default_params(&h->p);
+  std::string e = rg_read_ffield(ffield_path, h->p.lgflag, &h->ff);
+  if (!e.empty()) {
+    delete h;
+    return RG_E_FILE;
+  }
+  Control &c = h->ctl;
+  // reaxc_ffield_sunway.cpp:86-88 and the pair_style defaults
+  c.bo_cut = 0.01 * h->ff.gp[29];
+  c.nonb_low = h->ff.gp[11];
+  c.nonb_cut = h->ff.gp[12];
+  c.bond_cut = h->p.bond_cut;
+  c.hbond_cut = h->p.hbond_cut;
+  c.thb_cut = h->p.thb_cut;
+  c.thb_cutsq = h->p.thb_cutsq;
+  c.enobondsflag = h->p.enobondsflag;
+  c.lgflag = h->p.lgflag;
+  const double lc = std::max(c.nonb_cut, h->p.qeq_swb);
+  c.list_cut2 = lc * lc;
+  c.nonb_cut2 = c.nonb_cut * c.nonb_cut;
+  c.swb2 = h->p.qeq_swb * h->p.qeq_swb;
+  c.near_cut = std::max(c.bond_cut, c.hbond_cut);
+  rg_init_taper(c.nonb_low, c.nonb_cut, c.Tap);
+  rg_init_taper(h->p.qeq_swa, h->p.qeq_swb, c.qTap);
+  if (c.near_cut > lc) {
+    delete h;
+    return RG_E_ARG;
+  }
+  cudaError_t ce = cudaSetDevice(h->p.device);
+  if (ce == cudaSuccess) ce = cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking);
+  if (ce == cudaSuccess) ce = cudaMalloc(&h->d_ff, sizeof(ForceField));
+  if (ce == cudaSuccess) ce = cudaMalloc(&h->d_ctl, sizeof(Control));
+  if (ce == cudaSuccess) ce = cudaMemcpy(h->d_ff, &h->ff, sizeof(ForceField), cudaMemcpyHostToDevice);
+  if (ce == cudaSuccess) ce = cudaMemcpy(h->d_ctl, &h->ctl, sizeof(Control), cudaMemcpyHostToDevice);
+  if (ce != cudaSuccess) {
+    if (h->d_ff) cudaFree(h->d_ff);
+    if (h->d_ctl) cudaFree(h->d_ctl);
+    delete h;
+    return RG_E_CUDA;
+  }
+  h->d.ff = h->d_ff;
+  h->d.ctl = h->d_ctl;
+  *out = h;
+  return RG_OK;
+}
+
+int rg_destroy(rg_system *h) {
+  if (!h) return RG_E_ARG;
+  cudaSetDevice(h->p.device);
+  cudaStreamSynchronize(h->st);
+  free_bucket(h->per_n);
+  free_bucket(h->per_nb);
+  free_bucket(h->per_b);
+  free_bucket(h->per_hb);
+  if (h->cells) cudaFree(h->cells);
+  cudaFree(h->d_ff);
+  cudaFree(h->d_ctl);
+  cudaStreamDestroy(h->st);
+  delete h;
+  return RG_OK;
+}
+
+const char *rg_last_error(const rg_system *h) { return h ? h->err.c_str() : "null handle"; }
+
+int rg_num_types(const rg_system *h) { return h ? h->ff.ntypes : 0; }
+
+int rg_element_name(const rg_system *h, int t, char *buf, int len) {
+  if (!h || t < 0 || t >= h->ff.ntypes || !buf || len < 1) return RG_E_ARG;
+  std::snprintf(buf, len, "%s", h->ff.sbp[t].name);
+  return RG_OK;
+}
+
+int rg_extract(const rg_system *h, const char *name, double *out) {
+  if (!h || !name || !out) return RG_E_ARG;
+  for (int t = 0; t < h->ff.ntypes; ++t) {
+    const Sbp &s = h->ff.sbp[t];
+    if (!std::strcmp(name, "chi")) out[t] = s.chi;
+    else if (!std::strcmp(name, "eta")) out[t] = s.eta;
+    else if (!std::strcmp(name, "gamma")) out[t] = s.gamma;
+    else if (!std::strcmp(name, "mass")) out[t] = s.mass;
+    else return RG_E_ARG;
+  }
+  return RG_OK;
+}
+
+int rg_set_box(rg_system *h, const double *L3) {
+  if (!h || !L3) return RG_E_ARG;
+  for (int k = 0; k < 3; ++k)
+    if (!(L3[k] > 0.0) || !std::isfinite(L3[k])) return fail(h, RG_E_ARG, "box edge must be positive");
+  for (int k = 0; k < 3; ++k) h->L[k] = L3[k];
+  h->have_box = true;
+  h->lists_valid = false;
+  h->forces_valid = false;
+  return RG_OK;
+}
+
+static int set_atoms_impl(rg_system *h, int n, const double *x, const int *type, const int *tag,
+                          const double *q, const double *v, cudaMemcpyKind kind) {
+  if (!h) return RG_E_ARG;
+  if (!h->have_box) return fail(h, RG_E_STATE, "rg_set_box must precede rg_set_atoms");
+  if (n <= 0 || n >= (1 << 24) || !x || !type) return fail(h, RG_E_ARG, "bad atom arrays");
+  CK(cudaSetDevice(h->p.device));
+  if (kind == cudaMemcpyHostToDevice) {
+    for (int i = 0; i < n; ++i)
+      if (type[i] < 0 || type[i] >= h->ff.ntypes) return fail(h, RG_E_ARG, "atom type out of range");
+  }
+  if (n != h->d.n) {
+    int rc = alloc_atoms(h, n);
+    if (rc) return rc;
+  }
+  Dev &d = h->d;
+  CK(cudaMemcpyAsync(d.x_o, x, 3 * sizeof(double) * n, kind, h->st));
+  CK(cudaMemcpyAsync(d.type_o, type, sizeof(int) * n, kind, h->st));
+  if (tag) {
+    CK(cudaMemcpyAsync(d.tag_o, tag, sizeof(int) * n, kind, h->st));
+  } else {
+    std::vector<int> t(n);
+    for (int i = 0; i < n; ++i) t[i] = i + 1;
+    CK(cudaMemcpyAsync(d.tag_o, t.data(), sizeof(int) * n, cudaMemcpyHostToDevice, h->st));
+    CK(cudaStreamSynchronize(h->st));
+  }
+  if (q) CK(cudaMemcpyAsync(d.q_o, q, sizeof(double) * n, kind, h->st));
+  else CK(cudaMemsetAsync(d.q_o, 0, sizeof(double) * n, h->st));
+  if (v) CK(cudaMemcpyAsync(d.v_o, v, 3 * sizeof(double) * n, kind, h->st));
+  else CK(cudaMemsetAsync(d.v_o, 0, 3 * sizeof(double) * n, h->st));
+  CK(cudaMemsetAsync(d.s_hist, 0, 5 * sizeof(double) * n, h->st));
+  CK(cudaMemsetAsync(d.t_hist, 0, 5 * sizeof(double) * n, h->st));
+  CK(cudaMemsetAsync(d.f_o, 0, 3 * sizeof(double) * n, h->st));
+  CK(cudaStreamSynchronize(h->st));
+  h->n = n;
+  h->lists_valid = false;
+  h->forces_valid = false;
+  return RG_OK;
+}
+
+int rg_set_atoms(rg_system *h, int n, const double *x, const int *type, const int *tag,
+                 const double *q, const double *v) {
+  return set_atoms_impl(h, n, x, type, tag, q, v, cudaMemcpyHostToDevice);
+}
+
+int rg_set_atoms_device(rg_system *h, int n, const double *x, const int *type, const int *tag,
+                        const double *q, const double *v) {
+  return set_atoms_impl(h, n, x, type, tag, q, v, cudaMemcpyDeviceToDevice);
+}
+
+int rg_set_positions(rg_system *h, const double *x) {
+  if (!h || !x) return RG_E_ARG;
+  if (!h->n) return fail(h, RG_E_STATE, "no atoms set");
+  CK(cudaMemcpyAsync(h->d.x_o, x, 3 * sizeof(double) * h->n, cudaMemcpyHostToDevice, h->st));
+  h->lists_valid = false;
+  h->forces_valid = false;
+  return RG_OK;
+}
+
+int rg_qeq(rg_system *h, double *q_out, int *iters_s, int *iters_t) {
+  if (!h) return RG_E_ARG;
+  if (!h->n) return fail(h, RG_E_STATE, "no atoms set");
+  CK(cudaSetDevice(h->p.device));
+  int rc = do_qeq(h, iters_s, iters_t);
+  if (rc) return rc;
+  if (q_out) {
+    CK(cudaMemcpyAsync(q_out, h->d.q_o, sizeof(double) * h->n, cudaMemcpyDeviceToHost, h->st));
+    CK(cudaStreamSynchronize(h->st));
+  }
+  return RG_OK;
+}
+
+int rg_compute(rg_system *h, int eflag, int vflag, double *f_out, double *energies) {
+  (void)vflag;
+  if (!h) return RG_E_ARG;
+  if (!h->n) return fail(h, RG_E_STATE, "no atoms set");
+  CK(cudaSetDevice(h->p.device));
+  int rc = do_compute(h, eflag || energies != nullptr);
+  if (rc) return rc;
+  if (f_out) CK(cudaMemcpyAsync(f_out, h->d.f_o, 3 * sizeof(double) * h->n, cudaMemcpyDeviceToHost, h->st));
+  if (energies) CK(cudaMemcpyAsync(energies, h->d.energy, RG_NE * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+  int st[8];
+  if ((rc = read_status(h, st))) return rc;
+  if (st[ST_NAN]) return fail(h, RG_E_NUMERIC, "non-finite force");
+  return RG_OK;
+}
+
+int rg_nve_initial(rg_system *h, double dt) {
+  if (!h) return RG_E_ARG;
+  if (!h->n) return fail(h, RG_E_STATE, "no atoms set");
+  launch_nve_initial(h->d, h->st, dt);
+  CK(cudaGetLastError());
+  h->lists_valid = false;
+  h->forces_valid = false;
+  return RG_OK;
+}
+
+int rg_nve_final(rg_system *h, double dt) {
+  if (!h) return RG_E_ARG;
+  if (!h->n) return fail(h, RG_E_STATE, "no atoms set");
+  launch_nve_final(h->d, h->st, dt);
+  CK(cudaGetLastError());
+  return RG_OK;
+}
+
+int rg_run(rg_system *h, int nsteps, double dt, double *energies) {
+  if (!h || nsteps < 0) return RG_E_ARG;
+  if (!h->n) return fail(h, RG_E_STATE, "no atoms set");
+  CK(cudaSetDevice(h->p.device));
+  int rc;
+  if (!h->forces_valid) {  // Verlet setup: pre_force + force
+    if ((rc = do_qeq(h, nullptr, nullptr))) return rc;
+    if ((rc = do_compute(h, 1))) return rc;
+  }
+  for (int s = 0; s < nsteps; ++s) {
+    launch_nve_initial(h->d, h->st, dt);
+    h->lists_valid = false;
+    if ((rc = do_qeq(h, nullptr, nullptr))) return rc;
+    if ((rc = do_compute(h, energies != nullptr && s == nsteps - 1))) return rc;
+    launch_nve_final(h->d, h->st, dt);
+  }
+  if (energies) CK(cudaMemcpyAsync(energies, h->d.energy, RG_NE * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+  CK(cudaStreamSynchronize(h->st));
+  CK(cudaGetLastError());
+  return RG_OK;
+}
+
+int rg_get_atoms(rg_system *h, double *x, double *v, double *q, double *f) {
+  if (!h) return RG_E_ARG;
+  const int n = h->n;
+  if (x) CK(cudaMemcpyAsync(x, h->d.x_o, 3 * sizeof(double) * n, cudaMemcpyDeviceToHost, h->st));
+  if (v) CK(cudaMemcpyAsync(v, h->d.v_o, 3 * sizeof(double) * n, cudaMemcpyDeviceToHost, h->st));
+  if (q) CK(cudaMemcpyAsync(q, h->d.q_o, sizeof(double) * n, cudaMemcpyDeviceToHost, h->st));
+  if (f) CK(cudaMemcpyAsync(f, h->d.f_o, 3 * sizeof(double) * n, cudaMemcpyDeviceToHost, h->st));
+  CK(cudaStreamSynchronize(h->st));
+  return RG_OK;
+}
+
+int rg_device_arrays(rg_system *h, double **x, double **v, double **q, double **f) {
+  if (!h) return RG_E_ARG;
+  if (x) *x = h->d.x_o;
+  if (v) *v = h->d.v_o;
+  if (q) *q = h->d.q_o;
+  if (f) *f = h->d.f_o;
+  return RG_OK;
+}
+
+int rg_get_stats(const rg_system *h, rg_stats *s) {
+  if (!h || !s) return RG_E_ARG;
+  *s = h->stats;
+  s->n_atoms = h->n;
+  return RG_OK;
+}
+
+int rg_synchronize(rg_system *h) {
+  if (!h) return RG_E_ARG;
+  CK(cudaStreamSynchronize(h->st));
+  return RG_OK;
+}
+
+}  // extern "C"
+
+// ------------------------------------------------------------------
+// list dumps (host side, for parity checks)
+
+namespace {
+
+int oracle_img(int c) {
+  int sx, sy, sz;
+  img_unpack(c, &sx, &sy, &sz);
+  return (sx + 8) | ((sy + 8) << 4) | ((sz + 8) << 8);
+}
+
+template <class T>
+std::vector<T> fetch(rg_system *h, const T *p, size_t count) {
+  std::vector<T> v(count);
+  if (count) cudaMemcpyAsync(v.data(), p, count * sizeof(T), cudaMemcpyDeviceToHost, h->st);
+  cudaStreamSynchronize(h->st);
+  return v;
+}
+
+}  // namespace
+
+extern "C" long long rg_dump_pairs(rg_system *h, int *ti, int *tj, int *img) {
+  if (!h || !h->lists_valid) return -1;
+  const Dev &d = h->d;
+  const int n = d.n, cap = d.nb_cap;
+  auto nn = fetch(h, d.n_near, n), nf = fetch(h, d.n_far, n);
+  long long tot = 0;
+  for (int i = 0; i < n; ++i) tot += nn[i] + nf[i];
+  if (!ti) return tot;
+  auto tags = fetch(h, d.tags, n);
+  auto nbr = fetch(h, d.nbr, (size_t)n * cap);
+  long long k = 0;
+  for (int i = 0; i < n; ++i)
+    for (int p = 0; p < nn[i] + nf[i]; ++p) {
+      const int slot = p < nn[i] ? p : cap - 1 - (p - nn[i]);
+      const uint32_t e = nbr[(size_t)i * cap + slot];
+      ti[k] = tags[i];
+      tj[k] = tags[e >> 8];
+      img[k] = oracle_img((int)(e & 255u));
+      ++k;
+    }
+  return k;
+}
+
+extern "C" long long rg_dump_bonds(rg_system *h, int *ti, int *tj, int *img, double *bo) {
+  if (!h || !h->forces_valid) return -1;
+  const Dev &d = h->d;
+  const int n = d.n;
+  auto nb = fetch(h, d.nbonds, n);
+  long long tot = 0;
+  for (int i = 0; i < n; ++i) tot += nb[i];
+  if (!ti) return tot;
+  const size_t S = (size_t)n * d.bond_cap;
+  auto tags = fetch(h, d.tags, n);
+  auto bn = fetch(h, d.b_nbr, S);
+  auto BO = fetch(h, d.b_BO, S), BOs = fetch(h, d.b_BOs, S);
+  auto BOpi = fetch(h, d.b_BOpi, S), BOpi2 = fetch(h, d.b_BOpi2, S);
+  long long k = 0;
+  for (int i = 0; i < n; ++i)
+    for (int q = 0; q < nb[i]; ++q) {
+      const size_t s = (size_t)q * n + i;
+      ti[k] = tags[i];
+      tj[k] = tags[bn[s] >> 8];
+      img[k] = oracle_img((int)(bn[s] & 255u));
+      if (bo) {
+        bo[4 * k + 0] = BO[s];
+        bo[4 * k + 1] = BOs[s];
+        bo[4 * k + 2] = BOpi[s];
+        bo[4 * k + 3] = BOpi2[s];
+      }
+      ++k;
+    }
+  return k;
+}
+
+extern "C" long long rg_dump_hbonds(rg_system *h, int *ti, int *tj, int *img) {
+  if (!h || !h->lists_valid) return -1;
+  const Dev &d = h->d;
+  const int n = d.n;
+  auto nh = fetch(h, d.nhb, n);
+  long long tot = 0;
+  for (int i = 0; i < n; ++i) tot += nh[i];
+  if (!ti) return tot;
+  auto tags = fetch(h, d.tags, n);
+  auto hb = fetch(h, d.hb_nbr, (size_t)n * d.hb_cap);
+  long long k = 0;
+  for (int i = 0; i < n; ++i)
+    for (int q = 0; q < nh[i]; ++q) {
+      const uint32_t e = hb[(size_t)i * d.hb_cap + q];
+      ti[k] = tags[i];
+      tj[k] = tags[e >> 8];
+      img[k] = oracle_img((int)(e & 255u));
+      ++k;
+    }
+  return k;
+}

@@ -1,0 +1,191 @@
+// Internal types of the reaxgpu library (host + device).
+#pragma once
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#define RG_MAXT 8       // force-field atom types supported
+#define RG_MAX3 5       // three-body parameter sets per type triple
+#define RG_NE 17        // energy vector length (RG_NENERGY)
+
+// energy slots (pvector order of pair_reaxc_sunway.cpp:657-670, then
+// eng_vdwl, eng_coul, physical e_pol)
+enum {
+  E_BOND = 0, E_OVUN, E_LP, E_3, E_ANG, E_PEN, E_COA, E_HB, E_TOR, E_CON,
+  E_VDW, E_ELE, E_12, E_POL, E_ENG_VDWL, E_ENG_COUL, E_POL_PHYS
+};
+
+struct Sbp {
+  double r_s, valency, mass, r_vdw, epsilon, gamma, r_pi, valency_e, nlp_opt;
+  double alpha, gamma_w, valency_boc, p_ovun5, chi, eta;
+  double r_pi_pi, p_lp2, b_o_131, b_o_132, b_o_133;
+  double p_ovun2, p_val3, valency_val, p_val5, rcore2, ecore2, acore2;
+  double lgcij, lgre;
+  int p_hbond;
+  int is_carbon;
+  char name[8];
+};
+
+struct Tbp {
+  double r_s, r_p, r_pp, p_bo1, p_bo2, p_bo3, p_bo4, p_bo5, p_bo6;
+  double p_boc3, p_boc4, p_boc5, v13cor, ovc;
+  double De_s, De_p, De_pp, p_be1, p_be2, p_ovun1;
+  double D, alpha, r_vdW, gamma_w, gamma, rcore, ecore, acore, lgcij, lgre;
+  // derived for the nonbonded kernel
+  double powgi_vdW1;   // pow(1/gamma_w, p_vdW1)
+};
+
+struct Thbp {
+  double theta_00, p_val1, p_val2, p_coa1, p_val7, p_pen1, p_val4;
+};
+struct Thbh {
+  int cnt;
+  Thbp prm[RG_MAX3];
+};
+struct Fbp {
+  double V1, V2, V3, p_tor1, p_cot1;
+};
+struct Fbh {
+  int cnt;
+  Fbp prm;
+};
+struct Hbp {
+  double r0_hb, p_hb1, p_hb2, p_hb3;
+};
+
+// Whole force field, plain data, copied once to device memory.
+struct ForceField {
+  int ntypes, vdw_type, ngp;
+  double gp[64];
+  Sbp sbp[RG_MAXT];
+  Tbp tbp[RG_MAXT][RG_MAXT];
+  Thbh thbp[RG_MAXT][RG_MAXT][RG_MAXT];
+  Hbp hbp[RG_MAXT][RG_MAXT][RG_MAXT];
+  Fbh fbp[RG_MAXT][RG_MAXT][RG_MAXT][RG_MAXT];
+};
+
+// Scalar controls shared by all kernels.
+struct Control {
+  double bo_cut, nonb_cut, nonb_low, bond_cut, hbond_cut, thb_cut, thb_cutsq;
+  double list_cut2;   // squared pair-list cutoff max(nonb_cut, qeq_swb)^2
+  double nonb_cut2, swb2;
+  double near_cut;    // max(bond_cut, hbond_cut): "near" part of a row
+  double Tap[8];      // pair taper (swa = nonb_low, swb = nonb_cut)
+  double qTap[8];     // QEq taper
+  int enobondsflag, lgflag;
+};
+
+// Parse an ffield file (restates Read_Force_Field,
+// reaxc_ffield_sunway.cpp:35-714).  Returns empty string or an error.
+std::string rg_read_ffield(const char *path, int lgflag, ForceField *ff);
+void rg_init_taper(double swa, double swb, double *Tap);
+
+// ---------------------------------------------------------------------
+// Device-side view of one system (sorted atom order unless noted).
+struct Dev {
+  int n;              // atoms
+  int nb_cap;         // neighbour row capacity (row-major rows)
+  int bond_cap;       // bond slots per atom (slot-major: k*n + i)
+  int hb_cap;         // H-bond partner slots per H atom (row-major)
+  double L[3];        // box
+  int nc[3];          // cells per dimension
+  int S;              // stencil half-width (cells)
+  double cellw[3];
+
+  const ForceField *ff;
+  const Control *ctl;
+
+  // original order (persistent state)
+  double *x_o, *v_o, *q_o, *f_o;
+  int *type_o, *tag_o;
+  double *s_hist, *t_hist;     // [5][n]  (k*n + i, original order)
+
+  // binning / sort
+  int *cell_o;        // cell of original atom
+  int *cell_count, *cell_start, *cell_fill;
+  int *perm;          // sorted -> original
+  int *iperm;         // original -> sorted
+
+  // sorted atoms
+  double4 *xs;        // x, y, z, q
+  float4 *xf;         // fp32 x, y, z, (type as float)
+  int *ts, *tags;
+
+  // full pair list, row-major rows of nb_cap; near entries from the front,
+  // far entries from the back
+  uint32_t *nbr;      // (j << 8) | image
+  double *hval;       // QEq H_ij per entry
+  int *n_near, *n_far;
+
+  // bonds (slot-major, slot = k*n + i)
+  int *nbonds;
+  uint32_t *b_nbr;
+  int *b_sym;
+  double *b_d, *b_dx, *b_dy, *b_dz;
+  double *b_BO, *b_BOs, *b_BOpi, *b_BOpi2;
+  double *b_dBOp;     // 3 * slots (xyz blocks)
+  double *b_dlnpi, *b_dlnpi2;  // 3 * slots
+  double *b_C;        // 11 * slots: C1dbo C2dbo C3dbo C1dbopi C2dbopi C3dbopi C4dbopi C1dbopi2 C2dbopi2 C3dbopi2 C4dbopi2
+  double *b_Cdbo, *b_Cdbopi, *b_Cdbopi2;
+
+  // H-bond partners of H atoms (row-major hb_cap), entry = nbr-row index
+  int *nhb;
+  uint32_t *hb_nbr;
+
+  // per-atom bond-order workspace (sorted order)
+  double *bo0;        // total (uncorrected, then corrected) bond order
+  double *Deltap, *Deltap_boc, *Delta, *Delta_e, *Delta_boc, *Delta_val;
+  double *vlpex, *nlp, *Delta_lp, *Delta_lp_temp, *dDelta_lp, *nlp_temp;
+  double *dDeltap;    // 3 * n (xyz blocks)
+  double *fC;         // 4 * n: force xyz blocks + CdDelta block
+
+  // QEq vectors (sorted order), two solves s,t interleaved as double2
+  double2 *qx, *qb, *qr, *qu, *qw, *qd, *qq, *qp, *qs, *qv, *qz, *qm;
+  double *Hdia_inv;
+  double *red;        // device scalars / reduction accumulators
+  double *energy;     // [RG_NE]
+
+  int *status;        // [8]: 0 overflow flags, 1 max nbrs, 2 max bonds, 3 max hb, 4 nonfinite
+};
+
+// status slots
+enum { ST_OVF = 0, ST_MAXNB = 1, ST_MAXB = 2, ST_MAXHB = 3, ST_NAN = 4 };
+enum { OVF_NBR = 1, OVF_BOND = 2, OVF_HB = 4, OVF_CELL = 8 };
+
+// image code of a neighbour entry: sx,sy,sz in [-2,2]
+__host__ __device__ inline int img_pack(int sx, int sy, int sz) {
+  return (sx + 2) + 5 * (sy + 2) + 25 * (sz + 2);
+}
+__host__ __device__ inline void img_unpack(int c, int *sx, int *sy, int *sz) {
+  *sx = c % 5 - 2;
+  *sy = (c / 5) % 5 - 2;
+  *sz = c / 25 - 2;
+}
+
+// kernel launchers (lists.cu, bonded.cu, nonbonded.cu, qeq.cu, nve.cu)
+void launch_bin_sort(const Dev &d, cudaStream_t st);
+void launch_build_nbrs(const Dev &d, cudaStream_t st);
+void launch_build_bonds(const Dev &d, cudaStream_t st);
+void launch_bond_orders(const Dev &d, cudaStream_t st);
+void launch_bonded_terms(const Dev &d, cudaStream_t st, int eflag);
+void launch_nonbonded(const Dev &d, cudaStream_t st, int eflag);
+void launch_dbond_forces(const Dev &d, cudaStream_t st);
+void launch_force_out(const Dev &d, cudaStream_t st);
+void launch_energy_pol(const Dev &d, cudaStream_t st);
+
+// QEq
+void launch_qeq_setup(const Dev &d, cudaStream_t st);
+void launch_qeq_spmv(const Dev &d, cudaStream_t st, const double2 *x, double2 *y);
+void launch_qeq_cg_init(const Dev &d, cudaStream_t st);
+void launch_qeq_cg_iter(const Dev &d, cudaStream_t st);
+void launch_qeq_finish(const Dev &d, cudaStream_t st);
+
+// NVE
+void launch_nve_initial(const Dev &d, cudaStream_t st, double dt);
+void launch_nve_final(const Dev &d, cudaStream_t st, double dt);
+
+// generic
+void launch_zero(void *p, size_t bytes, cudaStream_t st);

@@ -1,0 +1,244 @@
+"""Seeded synthetic molecular systems for the ReaxFF force step.
+
+The reference ships only a TATB crystal deck; the workloads measured here are
+seeded synthetic liquids with the molecule mix, density and temperature of
+each workload (2,000-molecule water box; 1,048,576-atom H2O/CH4/C2H6/NH3
+mixture; small random packs of H2O/CH4/NH3/CO2/C2H6).  Molecules sit on a
+jittered cubic lattice with uniformly random orientations; orientations that
+put two atoms of different molecules closer than ``min_dist`` are redrawn.
+
+Units are LAMMPS ``real``: Angstrom, g/mol, fs, kcal/mol.
+"""
+from __future__ import annotations
+
+import math
+from dataclasses import dataclass, field
+
+import numpy as np
+
+AVOGADRO = 6.0221367e23
+KB_KCAL = 0.0019872067          # kcal/mol/K
+MVV2E = 48.88821291 ** 2        # (g/mol) (A/fs)^2 -> kcal/mol
+
+# Element masses used for densities and velocities (matching ffield.reax).
+MASS = {"C": 12.0, "H": 1.008, "O": 15.999, "N": 14.0}
+
+
+def _water():
+    r, ang = 0.9572, math.radians(104.52)
+    return ["O", "H", "H"], np.array([
+        [0.0, 0.0, 0.0],
+        [r * math.sin(ang / 2), r * math.cos(ang / 2), 0.0],
+        [-r * math.sin(ang / 2), r * math.cos(ang / 2), 0.0]])
+
+
+def _methane():
+    r = 1.09 / math.sqrt(3.0)
+    return ["C", "H", "H", "H", "H"], np.array([
+        [0, 0, 0], [r, r, r], [r, -r, -r], [-r, r, -r], [-r, -r, r]], float)
+
+
+def _ammonia():
+    r, hnh = 1.012, math.radians(106.7)
+    # three H on a cone around z
+    s = 2 * math.sin(hnh / 2) / math.sqrt(3.0)        # sin(cone angle)
+    c = math.sqrt(max(0.0, 1 - s * s))
+    pos = [[0.0, 0.0, 0.0]]
+    for k in range(3):
+        phi = 2 * math.pi * k / 3
+        pos.append([r * s * math.cos(phi), r * s * math.sin(phi), -r * c])
+    return ["N", "H", "H", "H"], np.array(pos)
+
+
+def _ethane():
+    rcc, rch = 1.54, 1.09
+    th = math.radians(180 - 109.47)
+    pos = [[0, 0, -rcc / 2], [0, 0, rcc / 2]]
+    for k in range(3):                       # staggered
+        phi = 2 * math.pi * k / 3
+        pos.append([rch * math.sin(th) * math.cos(phi),
+                    rch * math.sin(th) * math.sin(phi),
+                    -rcc / 2 - rch * math.cos(th)])
+    for k in range(3):
+        phi = 2 * math.pi * k / 3 + math.pi / 3
+        pos.append([rch * math.sin(th) * math.cos(phi),
+                    rch * math.sin(th) * math.sin(phi),
+                    rcc / 2 + rch * math.cos(th)])
+    return ["C", "C", "H", "H", "H", "H", "H", "H"], np.array(pos)
+
+
+def _co2():
+    r = 1.16
+    return ["C", "O", "O"], np.array([[0, 0, 0], [0, 0, r], [0, 0, -r]], float)
+
+
+MOLECULES = {"H2O": _water(), "CH4": _methane(), "NH3": _ammonia(),
+             "C2H6": _ethane(), "CO2": _co2()}
+
+
+@dataclass
+class System:
+    """A periodic orthogonal box of atoms (positions in [0, L))."""
+    box: np.ndarray            # (3,) edge lengths
+    x: np.ndarray              # (n, 3) float64
+    elem: list                 # element symbol per atom
+    tag: np.ndarray            # (n,) int32, 1-based
+    v: np.ndarray              # (n, 3) float64, A/fs
+    mol: np.ndarray            # (n,) molecule index
+    meta: dict = field(default_factory=dict)
+
+    @property
+    def n(self) -> int:
+        return self.x.shape[0]
+
+    def types(self, element_order) -> np.ndarray:
+        """ffield type index per atom given the ffield's element order."""
+        idx = {e.upper(): i for i, e in enumerate(element_order)}
+        return np.array([idx[e.upper()] for e in self.elem], dtype=np.int32)
+
+    def masses(self) -> np.ndarray:
+        return np.array([MASS[e] for e in self.elem])
+
+
+def _random_rotations(rng, k):
+    """k uniform random rotation matrices (via unit quaternions)."""
+    q = rng.normal(size=(k, 4))
+    q /= np.linalg.norm(q, axis=1, keepdims=True)
+    w, x, y, z = q.T
+    return np.stack([
+        np.stack([1 - 2 * (y * y + z * z), 2 * (x * y - z * w), 2 * (x * z + y * w)], -1),
+        np.stack([2 * (x * y + z * w), 1 - 2 * (x * x + z * z), 2 * (y * z - x * w)], -1),
+        np.stack([2 * (x * z - y * w), 2 * (y * z + x * w), 1 - 2 * (x * x + y * y)], -1),
+    ], 1)
+
+
+def _close_molecules(x, mol, box, dmin):
+    """Indices of molecules with an atom closer than dmin to an atom of
+    another molecule (periodic).  Cell hashing with 27 neighbour cells."""
+    n = x.shape[0]
+    nc = np.maximum((box // dmin).astype(int), 1)
+    cw = box / nc
+    ci = np.minimum((x // cw).astype(int), nc - 1)
+    cid = (ci[:, 2] * nc[1] + ci[:, 1]) * nc[0] + ci[:, 0]
+    order = np.argsort(cid, kind="stable")
+    cs = cid[order]
+    ncell = int(nc.prod())
+    start = np.searchsorted(cs, np.arange(ncell), "left")
+    end = np.searchsorted(cs, np.arange(ncell), "right")
+    occ = end - start
+    M = int(occ.max()) if n else 0
+    table = np.full((ncell, max(M, 1)), -1, dtype=np.int64)
+    rank = np.arange(n) - start[cs]
+    table[cs, rank] = order
+    bad = np.zeros(int(mol.max()) + 1 if n else 0, dtype=bool)
+    for dz in (-1, 0, 1):
+        for dy in (-1, 0, 1):
+            for dx in (-1, 0, 1):
+                nb = (ci + np.array([dx, dy, dz])) % nc
+                nid = (nb[:, 2] * nc[1] + nb[:, 1]) * nc[0] + nb[:, 0]
+                cand = table[nid]                       # (n, M)
+                valid = cand >= 0
+                cj = np.where(valid, cand, 0)
+                d = x[cj] - x[:, None, :]
+                d -= box * np.round(d / box)
+                r2 = (d * d).sum(-1)
+                hit = valid & (r2 < dmin * dmin) & (mol[cj] != mol[:, None])
+                rows = np.nonzero(hit.any(1))[0]
+                bad[mol[rows]] = True
+    return np.nonzero(bad)[0]
+
+
+def pack_molecules(counts: dict, density: float, seed: int, *,
+                   temperature: float = 300.0, jitter: float = 0.3,
+                   min_dist: float = 1.6, max_redraw: int = 60,
+                   box=None) -> System:
+    """Place molecules (counts: name -> number) in a cubic periodic box at
+    ``density`` g/cm^3 on a jittered lattice with random orientations."""
+    rng = np.random.default_rng(seed)
+    names = []
+    for name, k in counts.items():
+        names += [name] * int(k)
+    names = np.array(names)
+    rng.shuffle(names)
+    nmol = len(names)
+    mass_total = sum(sum(MASS[e] for e in MOLECULES[nm][0]) * int(k)
+                     for nm, k in counts.items())
+    if box is None:
+        vol = mass_total / AVOGADRO / density * 1e24     # A^3
+        L = vol ** (1.0 / 3.0)
+        box = np.array([L, L, L])
+    box = np.asarray(box, float)
+    m = int(math.ceil(nmol ** (1.0 / 3.0) - 1e-9))
+    sites = np.stack(np.meshgrid(np.arange(m), np.arange(m), np.arange(m),
+                                 indexing="ij"), -1).reshape(-1, 3)
+    sites = sites[rng.permutation(len(sites))[:nmol]]
+    centers = (sites + 0.5) * (box / m)
+    centers += rng.uniform(-jitter, jitter, size=centers.shape)
+    # atoms
+    tmpl_e, tmpl_x, mol_of, atom_mol_slot = [], [], [], []
+    offs = [0]
+    for k, nm in enumerate(names):
+        e, xyz = MOLECULES[nm]
+        tmpl_e += e
+        tmpl_x.append(xyz - xyz.mean(0))
+        mol_of += [k] * len(e)
+        offs.append(offs[-1] + len(e))
+    mol_of = np.array(mol_of)
+    local = np.concatenate(tmpl_x)
+    rot = _random_rotations(rng, nmol)
+    x = np.einsum("aij,aj->ai", rot[mol_of], local) + centers[mol_of]
+    x %= box
+    for _ in range(max_redraw):
+        bad = _close_molecules(x, mol_of, box, min_dist)
+        if len(bad) == 0:
+            break
+        newrot = _random_rotations(rng, len(bad))
+        rot[bad] = newrot
+        sel = np.isin(mol_of, bad)
+        x[sel] = (np.einsum("aij,aj->ai", rot[mol_of[sel]], local[sel]) +
+                  centers[mol_of[sel]] + 0.0) % box
+    n = x.shape[0]
+    masses = np.array([MASS[e] for e in tmpl_e])
+    sig = np.sqrt(KB_KCAL * temperature / (masses * MVV2E))
+    v = rng.normal(size=(n, 3)) * sig[:, None]
+    p = (v * masses[:, None]).sum(0) / masses.sum()
+    v -= p
+    x = np.where(x >= box, x - box, x)
+    return System(box=box, x=np.ascontiguousarray(x), elem=list(tmpl_e),
+                  tag=np.arange(1, n + 1, dtype=np.int32),
+                  v=np.ascontiguousarray(v), mol=mol_of,
+                  meta={"counts": dict(counts), "density": density,
+                        "seed": seed, "temperature": temperature})
+
+
+def water_box(n_molecules: int = 2000, density: float = 1.0,
+              seed: int = 2024) -> System:
+    """Liquid water box: 2,000 H2O at 1.0 g/cm^3 is the 6,000-atom case."""
+    return pack_molecules({"H2O": n_molecules}, density, seed)
+
+
+# 1,048,576 atoms exactly: 3*116511 + 5*46603 + 8*46603 + 4*23301
+MIXTURE_1M = {"H2O": 116511, "CH4": 46603, "C2H6": 46603, "NH3": 23301}
+
+
+def mixture(scale: float = 1.0, density: float = 0.8,
+            seed: int = 7) -> System:
+    """H2O/CH4/C2H6/NH3 mixture, mole fractions 0.5/0.2/0.2/0.1.
+    scale=1 gives the 1,048,576-atom system; smaller scales keep the mix."""
+    counts = {k: max(1, int(round(v * scale))) for k, v in MIXTURE_1M.items()}
+    return pack_molecules(counts, density, seed)
+
+
+def small_pack(n_atoms_target: int, density: float, seed: int) -> System:
+    """Random pack of H2O/CH4/NH3/CO2/C2H6 of about n_atoms_target atoms
+    (one system of the batched workload)."""
+    rng = np.random.default_rng(seed)
+    kinds = ["H2O", "CH4", "NH3", "CO2", "C2H6"]
+    counts = {k: 0 for k in kinds}
+    n = 0
+    while n < n_atoms_target:
+        k = kinds[rng.integers(len(kinds))]
+        counts[k] += 1
+        n += len(MOLECULES[k][0])
+    counts = {k: v for k, v in counts.items() if v}
+    return pack_molecules(counts, density, seed + 1)

@@ -1,0 +1,350 @@
+#!/usr/bin/env python3
+"""ReaxFF MD throughput on GB300: atom-steps/s of NVE molecular dynamics.
+
+One step = initial_integrate -> QEq (dual pipelined CG) -> full ReaxFF force
+step (pair list, bond orders, bonded terms, H-bonds, vdW+Coulomb, dBond
+forces) -> final_integrate, on the seeded 1,048,576-atom H2O/CH4/C2H6/NH3
+mixture at 0.8 g/cm^3 (synthetic; the reference publishes no dataset), FP64.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+Prints one JSON line.  With N>1 (launched under torch.distributed.run) every
+rank runs an independent replica of the workload on its own GPU ("replicas
+only": the single-GPU path has no cross-GPU exchange) and value is the sum
+of atom-steps over the max time over ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+METRIC = "atom-steps/s at 1M atoms (FP64 NVE MD step incl. QEq)"
+UNIT = "atom-steps/s"
+DT = 0.25          # fs
+SEED = 7
+
+# FP64 operations per unit of the dominant kernels (per half pair for the
+# nonbonded kernel, per (centre, bond) slot for valence/torsion), counted
+# from ncu's SASS instruction counters on a small case of the same workload
+# (2*dfma + dmul + dadd per unit); profiles/ holds the capture summary.
+FP64_OPS_PER_UNIT = {"nonbonded": None, "valence_torsion": None}
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=5)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
+    p.add_argument("--scale", type=float, default=1.0,
+                   help="workload size relative to the 1,048,576-atom mixture")
+    p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--no-cpu", action="store_true")
+    p.add_argument("--cpu-scale", type=float, default=0.02,
+                   help="size of the CPU-baseline sample relative to 1M atoms")
+    return p.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", 0))
+    world = int(os.environ.get("WORLD_SIZE", 1))
+    local = int(os.environ.get("LOCAL_RANK", 0))
+    return rank, world, local
+
+
+class Dist:
+    def __init__(self, backend):
+        self.rank, self.world, self.local = dist_env()
+        self.pg = None
+        if self.world > 1:
+            import torch.distributed as td
+            td.init_process_group(backend)
+            self.td = td
+
+    def barrier(self):
+        if self.world > 1:
+            self.td.barrier()
+
+    def max(self, x: float) -> float:
+        if self.world == 1:
+            return x
+        import torch
+        dev = "cuda" if self.td.get_backend() == "nccl" else "cpu"
+        t = torch.tensor([x], dtype=torch.float64, device=dev)
+        self.td.all_reduce(t, op=self.td.ReduceOp.MAX)
+        return float(t.item())
+
+    def sum(self, x: float) -> float:
+        if self.world == 1:
+            return x
+        import torch
+        dev = "cuda" if self.td.get_backend() == "nccl" else "cpu"
+        t = torch.tensor([x], dtype=torch.float64, device=dev)
+        self.td.all_reduce(t, op=self.td.ReduceOp.SUM)
+        return float(t.item())
+
+    def close(self):
+        if self.world > 1:
+            self.td.destroy_process_group()
+
+
+class Clocks:
+    """nvidia-smi samples during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(5)
+        except Exception:
+            self.proc.kill()
+        rows = []
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) >= 9:
+                rows.append(f)
+        os.unlink(self.path)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in rows for k in range(4) if r[5 + k].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons,
+                "samples": len(rows)}
+
+
+def measured_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        return json.load(open(path))
+    except Exception:
+        return {}
+
+
+def cpu_baseline(cpu_scale: float, procs: int = 1):
+    """The oracle (single-threaded restatement of the reference CPU path) on a
+    bounded sample of the same workload: a smaller periodic box of the same
+    mixture at the same density, one MD force step (QEq + forces)."""
+    import multiprocessing as mp
+    if procs <= 1:
+        n, t = _cpu_sample((cpu_scale, SEED))
+        return n / t, 1, n
+    ctx = mp.get_context("spawn")
+    t0 = time.perf_counter()
+    with ctx.Pool(procs) as pool:
+        res = pool.map(_cpu_sample, [(cpu_scale, SEED + k) for k in range(procs)])
+    wall = time.perf_counter() - t0
+    tot = sum(r[0] for r in res)
+    # per-process compute time excludes interpreter start-up
+    slowest = max(r[1] for r in res)
+    return tot / slowest, procs, tot // procs
+
+
+def _cpu_sample(arg):
+    cpu_scale, seed = arg
+    sys.path.insert(0, ROOT)
+    from oracle.pyoracle import Oracle
+    from sw_reaxff_gb300 import systems
+    from sw_reaxff_gb300.api import DEFAULT_FFIELD
+    s = systems.mixture(scale=cpu_scale, seed=seed)
+    o = Oracle(DEFAULT_FFIELD)
+    o.set_system(s.box, s.x, s.types(["C", "H", "O", "N"]), s.tag, None, s.v)
+    t0 = time.perf_counter()
+    o.qeq()
+    o.compute()
+    return s.n, time.perf_counter() - t0
+
+
+def reference_arm(args):
+    """--impl reference: the reference's CPU algorithm (the oracle port; the
+    reference itself needs LAMMPS and the Sunway toolchain) on all host
+    cores, each process a bounded sample of the workload per step."""
+    dist = Dist("gloo")
+    if dist.rank != 0:
+        dist.close()
+        return
+    procs = os.cpu_count() or 1
+    vals = []
+    for _ in range(args.warmup):
+        pass  # the oracle has no warm-up state worth timing
+    t0 = time.perf_counter()
+    for _ in range(max(1, args.steps)):
+        v, cores, sample = cpu_baseline(args.cpu_scale, procs)
+        vals.append(v)
+    value = float(np.mean(vals))
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 0, "impl": "reference",
+        "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": "H2O/CH4/C2H6/NH3 mixture 0.8 g/cm3, QEq tol 1e-6, dt 0.25 fs",
+                   "sample_atoms_per_process": sample, "processes": procs},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": procs, "kind": "port",
+                         "sample": f"{procs} processes x one QEq+force step of a "
+                                   f"{sample}-atom box of the same mixture"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "wall_s": time.perf_counter() - t0,
+    }
+    print(json.dumps(line), flush=True)
+    dist.close()
+
+
+def gpu_arm(args):
+    import torch
+    from sw_reaxff_gb300 import ReaxGPU, systems
+    from sw_reaxff_gb300.api import DEFAULT_FFIELD, measure_fp64_peak
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    dist = Dist("nccl")
+    s = systems.mixture(scale=args.scale, seed=SEED + rank)
+    n = s.n
+    g = ReaxGPU(DEFAULT_FFIELD, device=local)
+    g.set_system(s)
+    g.run(max(args.warmup, 1), DT, energies=False)          # setup + warm-up steps
+    stream = torch.cuda.ExternalStream(g.stream())
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    clocks = Clocks(local)
+    dist.barrier()
+    g.synchronize()
+    torch.cuda.synchronize()
+    clocks.start()
+    g.profile(True)
+    launches0 = g.stats()["kernel_launches"]
+    ev0.record(stream)
+    g.run(args.steps, DT, energies=False)
+    ev1.record(stream)
+    g.synchronize()
+    torch.cuda.synchronize()
+    dist.barrier()
+    ck = clocks.stop()
+    prof = g.profile_get()
+    g.profile(False)
+    st = g.stats()
+    launches = st["kernel_launches"] - launches0
+    ms = ev0.elapsed_time(ev1)
+    tmax = dist.max(ms / 1e3)
+    value = n * args.steps * world / tmax
+
+    # end to end through the C ABI with host (pinned) buffers: per step the
+    # state x, v, f goes host->device, the step runs, x, v, q, f come back
+    e2e = None
+    if not args.no_e2e:
+        pin = lambda shape: torch.empty(shape, dtype=torch.float64, pin_memory=True).numpy()
+        hx, hv, hf, hq = pin((n, 3)), pin((n, 3)), pin((n, 3)), pin((n,))
+        g.get_atoms_into(hx, hv, hq, hf)
+        dist.barrier()
+        g.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.steps):
+            g.set_state(hx, hv, hf)
+            g.run(1, DT, energies=False)
+            g.get_atoms_into(hx, hv, hq, hf)
+        e1.record(stream)
+        g.synchronize()
+        dist.barrier()
+        t_e2e = dist.max(e0.elapsed_time(e1) / 1e3)
+        e2e = {"value": n * args.steps * world / t_e2e, "unit": UNIT,
+               "h2d_bytes_per_step": int(hx.nbytes + hv.nbytes + hf.nbytes),
+               "d2h_bytes_per_step": int(hx.nbytes + hv.nbytes + hq.nbytes + hf.nbytes)}
+
+    # roofline of the dominant kernel (FP64-ALU bound)
+    fp64_peak = measure_fp64_peak(local)
+    phases = {k: v for k, v in prof.items() if v[1] > 0}
+    tot_ms = sum(v[0] for v in phases.values())
+    dom = max(phases, key=lambda k: phases[k][0])
+    roof = {"kernel": dom, "share": phases[dom][0] / tot_ms if tot_ms else None}
+    avg_ms = phases[dom][0] / phases[dom][1]
+    units = None
+    if dom == "nonbonded":
+        units = st["n_pairs"] / 2
+    elif dom == "valence_torsion":
+        units = st["n_bonds"]
+    ops = FP64_OPS_PER_UNIT.get(dom)
+    if ops and units:
+        ach = ops * units / (avg_ms * 1e-3) / 1e12
+        roof.update({"bound": "fp64", "achieved": ach, "peak": fp64_peak,
+                     "unit": "TFLOP/s", "frac": ach / fp64_peak, "traffic": None,
+                     "peak_source": "FP64 FMA probe measured in this run"})
+    else:
+        roof.update({"bound": "fp64", "achieved": None, "peak": fp64_peak, "unit": "TFLOP/s",
+                     "frac": None, "traffic": None,
+                     "peak_source": "FP64 FMA probe measured in this run"})
+    peaks = measured_peaks()
+
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": tmax * 1e3 / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64", "data": "synthetic (seeded molecular mixture)",
+        "config": {"workload": f"H2O/CH4/C2H6/NH3 0.5/0.2/0.2/0.1 mixture, {n} atoms, "
+                               "0.8 g/cm3, 300 K, NVE dt 0.25 fs, QEq tol 1e-6, FP64",
+                   "atoms": n, "parallelism": f"replicas x{world}",
+                   "l2": "inputs larger than L2 (pair list ~GBs)"},
+        "e2e": e2e,
+        "gpu_launches": None,
+        "clocks": ck,
+        "roofline": roof,
+        "phases_ms_per_step": {k: round(v[0] / args.steps, 4) for k, v in phases.items()},
+        "counts": {"pairs": st["n_pairs"], "bonds": st["n_bonds"], "hbond_pairs": st["n_hbond_pairs"],
+                   "cg_iters_s": st["cg_iters_s"], "cg_iters_t": st["cg_iters_t"]},
+        "hbm_peak_gbs": peaks.get("hbm_gbs"),
+    }
+    line["gpu_launches"] = int(launches)
+    if rank == 0 and not args.no_cpu:
+        v, cores, sample = cpu_baseline(args.cpu_scale, 1)
+        line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
+                                "sample": f"one QEq+force step of a {sample}-atom box of the "
+                                          "same mixture, single thread"}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    g.close()
+    dist.close()
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        reference_arm(args)
+    else:
+        gpu_arm(args)
+
+
+if __name__ == "__main__":
+    main()

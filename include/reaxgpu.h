@@ -84,6 +84,7 @@ typedef struct {
   int cg_iters_s, cg_iters_t;
   int max_nbrs, max_bonds, max_hbonds;
   int regrows;
+  long long kernel_launches;   /* kernels launched by this handle so far */
 } rg_stats;
 
 void rg_default_params(rg_params *p);
@@ -113,6 +114,12 @@ int rg_set_atoms_device(rg_system *h, int n, const double *x,
                         const double *v);
 /* Update positions only (host array), keeping histories. */
 int rg_set_positions(rg_system *h, const double *x);
+/* Per-step input of a host-driven MD loop (host arrays, original order):
+ * positions, and optionally velocities and the forces of those positions
+ * (from the previous step), keeping the QEq histories.  With f given the
+ * next rg_run continues the Verlet loop without recomputing forces. */
+int rg_set_state(rg_system *h, const double *x, const double *v,
+                 const double *f);
 
 /* QEq charge equilibration (pre_force).  q_out[n] host or NULL. */
 int rg_qeq(rg_system *h, double *q_out, int *iters_s, int *iters_t);
@@ -138,6 +145,21 @@ int rg_device_arrays(rg_system *h, double **x, double **v, double **q,
 
 int rg_get_stats(const rg_system *h, rg_stats *s);
 int rg_synchronize(rg_system *h);
+/* The cudaStream_t (as void*) all work of the handle is issued on. */
+void *rg_stream(rg_system *h);
+
+/* Phase timing with CUDA events on the handle's stream (the reference
+ * times the same phases with GPTL regions, e.g. pair_reaxc_sunway.cpp:
+ * 550-792).  rg_profile_enable(h,1) resets and starts; rg_profile_get fills
+ * up to max entries of names (32 chars each), milliseconds and interval
+ * counts, and returns the number of phases. */
+int rg_profile_enable(rg_system *h, int on);
+int rg_profile_get(rg_system *h, int max, char *names, double *ms,
+                   long long *count);
+
+/* Measured FP64 FMA throughput of a device (TFLOP/s): the roofline
+ * denominator of the FP64 form, whose kernels are bound by the FP64 units. */
+int rg_measure_fp64_peak(int device, double *tflops);
 
 /* List dumps for parity checks, from the last force step.  Each entry is
  * (tag_i, tag_j, image) with image = (sx+8) | (sy+8)<<4 | (sz+8)<<8 the

@@ -27,7 +27,8 @@ EXPORTED = ["rg_default_params", "rg_create", "rg_destroy", "rg_last_error",
             "rg_set_atoms", "rg_set_atoms_device", "rg_set_positions", "rg_qeq",
             "rg_compute", "rg_nve_initial", "rg_nve_final", "rg_run",
             "rg_get_atoms", "rg_device_arrays", "rg_get_stats", "rg_synchronize",
-            "rg_dump_pairs", "rg_dump_bonds", "rg_dump_hbonds"]
+            "rg_dump_pairs", "rg_dump_bonds", "rg_dump_hbonds", "rg_set_state",
+            "rg_stream", "rg_profile_enable", "rg_profile_get", "rg_measure_fp64_peak"]
 
 
 class Params(C.Structure):
@@ -45,7 +46,7 @@ class Stats(C.Structure):
                 ("n_H_entries", C.c_longlong), ("cg_iters_s", C.c_int),
                 ("cg_iters_t", C.c_int), ("max_nbrs", C.c_int),
                 ("max_bonds", C.c_int), ("max_hbonds", C.c_int),
-                ("regrows", C.c_int)]
+                ("regrows", C.c_int), ("kernel_launches", C.c_longlong)]
 
 
 class ReaxError(RuntimeError):
@@ -93,6 +94,12 @@ def load_library(path: str = LIBPATH):
         getattr(L, f).argtypes = [C.c_void_p, ip, ip, ip]
     L.rg_dump_bonds.restype = C.c_longlong
     L.rg_dump_bonds.argtypes = [C.c_void_p, ip, ip, ip, dp]
+    L.rg_set_state.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+    L.rg_stream.restype = C.c_void_p
+    L.rg_stream.argtypes = [C.c_void_p]
+    L.rg_profile_enable.argtypes = [C.c_void_p, C.c_int]
+    L.rg_profile_get.argtypes = [C.c_void_p, C.c_int, C.c_char_p, dp, P(C.c_longlong)]
+    L.rg_measure_fp64_peak.argtypes = [C.c_int, dp]
     _lib = L
     return L
 
@@ -103,6 +110,15 @@ def _dp(a):
 
 def _ip(a):
     return None if a is None else a.ctypes.data_as(C.POINTER(C.c_int))
+
+
+def measure_fp64_peak(device: int = 0) -> float:
+    """FP64 FMA throughput of the device in TFLOP/s."""
+    L = load_library()
+    t = C.c_double()
+    if L.rg_measure_fp64_peak(device, C.byref(t)) != 0:
+        raise ReaxError("rg_measure_fp64_peak failed")
+    return t.value
 
 
 def default_params(**kw) -> Params:
@@ -199,6 +215,35 @@ class ReaxGPU:
         e = np.zeros(NENERGY) if energies else None
         self._chk(self.L.rg_run(self.h, nsteps, dt, _dp(e)), "rg_run")
         return dict(zip(ENERGY_NAMES, e)) if energies else None
+
+    def set_state(self, x, v=None, f=None):
+        """Positions (and optionally velocities and current forces) from host
+        memory -- numpy arrays or raw pointers to pinned buffers -- keeping
+        the QEq histories."""
+        ptr = [a.ctypes.data if isinstance(a, np.ndarray) else a for a in (x, v, f)]
+        self._chk(self.L.rg_set_state(self.h, *ptr), "rg_set_state")
+
+    def get_atoms_into(self, x=None, v=None, q=None, f=None):
+        """Copy the state into caller-provided host arrays (e.g. pinned)."""
+        self._chk(self.L.rg_get_atoms(self.h, _dp(x), _dp(v), _dp(q), _dp(f)), "rg_get_atoms")
+
+    def stream(self) -> int:
+        return self.L.rg_stream(self.h)
+
+    def profile(self, on: bool):
+        self._chk(self.L.rg_profile_enable(self.h, 1 if on else 0), "rg_profile_enable")
+
+    def profile_get(self) -> dict:
+        names = C.create_string_buffer(32 * 64)
+        ms = np.zeros(64)
+        cnt = np.zeros(64, np.int64)
+        k = self.L.rg_profile_get(self.h, 64, names, _dp(ms),
+                                  cnt.ctypes.data_as(C.POINTER(C.c_longlong)))
+        out = {}
+        for i in range(k):
+            nm = names.raw[32 * i:32 * i + 32].split(b"\0")[0].decode()
+            out[nm] = (float(ms[i]), int(cnt[i]))
+        return out
 
     def get_atoms(self):
         n = self.n

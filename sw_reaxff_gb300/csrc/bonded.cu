@@ -829,10 +829,15 @@ void launch_bond_orders(const Dev &d, cudaStream_t st) {
   k_bo_atom<<<(d.n + B - 1) / B, B, 0, st>>>(d);
 }
 
-void launch_bonded_terms(const Dev &d, cudaStream_t st, int eflag) {
-  const int B = 256;
-  k_atom_energy<<<(d.n + B - 1) / B, B, 0, st>>>(d, eflag);
-  k_hbonds<<<(d.n + B - 1) / B, B, 0, st>>>(d, eflag);
+void launch_atom_energy(const Dev &d, cudaStream_t st, int eflag) {
+  k_atom_energy<<<(d.n + 255) / 256, 256, 0, st>>>(d, eflag);
+}
+
+void launch_hbonds(const Dev &d, cudaStream_t st, int eflag) {
+  k_hbonds<<<(d.n + 255) / 256, 256, 0, st>>>(d, eflag);
+}
+
+void launch_valence_torsion(const Dev &d, cudaStream_t st, int eflag) {
   const long long slots = (long long)d.n * d.bond_cap;
   k_valence_torsion<<<(unsigned)((slots + 127) / 128), 128, 0, st>>>(d, eflag);
 }
@@ -847,4 +852,3 @@ void launch_force_out(const Dev &d, cudaStream_t st) {
   k_force_out<<<(d.n + B - 1) / B, B, 0, st>>>(d);
 }
 
-void launch_energy_pol(const Dev &, cudaStream_t) {}

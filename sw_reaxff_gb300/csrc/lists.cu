@@ -234,7 +234,7 @@ __global__ void __launch_bounds__(256) k_build_nbrs(Dev d) {
               // fix_qeq_reax_sunway.cpp:440-454 (= tbp gamma)
               const double shld = F.tbp[ti][tj].gamma;
               (void)gam_i;
-              const double den = cbrt(r * r * r + shld);
+              const double den = pow_third(r * r * r + shld, RG_C3_QEQ);
               h = tp * 14.4 / den;
             }
             d.nbr[row + pos] = ((uint32_t)j << 8) | (uint32_t)img;
@@ -393,7 +393,32 @@ __global__ void k_bond_sym(Dev d) {
   d.b_sym[s] = sym;
 }
 
+// list sizes for the statistics (status slots 5..7)
+__global__ void k_count(Dev d) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  int a = 0, b = 0, c = 0;
+  if (i < d.n) {
+    a = d.n_near[i] + d.n_far[i];
+    b = d.nbonds[i];
+    c = d.nhb[i];
+  }
+  for (int off = 16; off > 0; off >>= 1) {
+    a += __shfl_down_sync(FULL, a, off);
+    b += __shfl_down_sync(FULL, b, off);
+    c += __shfl_down_sync(FULL, c, off);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    atomicAdd(&d.status[5], a);
+    atomicAdd(&d.status[6], b);
+    atomicAdd(&d.status[7], c);
+  }
+}
+
 }  // namespace
+
+void launch_count(const Dev &d, cudaStream_t st) {
+  k_count<<<(d.n + 255) / 256, 256, 0, st>>>(d);
+}
 
 void launch_bin_sort(const Dev &d, cudaStream_t st) {
   const int ncell = d.nc[0] * d.nc[1] * d.nc[2];

@@ -124,7 +124,7 @@ __global__ void __launch_bounds__(256) k_nonbonded(Dev d, int eflag) {
       }
       // shielded Coulomb: Tap * qi qj / (r^3 + gamma)^(1/3)
       const double dr3gamij_1 = r * r * r + tw.gamma;
-      const double dr3gamij_3 = cbrt(dr3gamij_1);
+      const double dr3gamij_3 = pow_third(dr3gamij_1, RG_C3_ELE);
       const double qq = C_ele * xi.w * xj.w;
       const double e_ele = qq * Tp / dr3gamij_3;
       const double CEclmb = qq * (dTap - Tp * r / dr3gamij_1) / dr3gamij_3;

@@ -288,10 +288,14 @@ void launch_qeq_cg_init(const Dev &d, cudaStream_t st) {
   k_cg_init_ctrl<<<1, 1, 0, st>>>(d);
 }
 
-void launch_qeq_cg_iter(const Dev &d, cudaStream_t st) {
+// one CG iteration = launch_qeq_cg_A, SpMV of d into q, launch_qeq_cg_C
+void launch_qeq_cg_A(const Dev &d, cudaStream_t st) {
   const int B = 256, G = (d.n + B - 1) / B;
   k_cg_A<<<G, B, 0, st>>>(d);
-  launch_qeq_spmv(d, st, d.qd, d.qq);
+}
+
+void launch_qeq_cg_C(const Dev &d, cudaStream_t st) {
+  const int B = 256, G = (d.n + B - 1) / B;
   k_cg_ctrl<<<1, 1, 0, st>>>(d);
   k_cg_C<<<G, B, 0, st>>>(d);
   k_cg_flip<<<1, 1, 0, st>>>(d);

@@ -17,6 +17,60 @@
 #include "../../include/reaxgpu.h"
 #include "rg_internal.h"
 
+// Phase timer: CUDA events recorded on the handle's stream around each
+// kernel group; intervals are resolved lazily (after a stream sync).
+enum {
+  PH_BIN = 0, PH_NBR, PH_BOND, PH_BO, PH_ATOM, PH_HB, PH_VALTOR, PH_NONB, PH_DBOND,
+  PH_FOUT, PH_QSETUP, PH_QSPMV, PH_QVEC, PH_QFIN, PH_NVE, PH_N
+};
+static const char *kPhaseNames[PH_N] = {
+    "bin_sort", "pair_list+H", "bond_list", "bond_orders", "atom_energy", "hbonds",
+    "valence_torsion", "nonbonded", "dbond_forces", "force_out", "qeq_setup",
+    "qeq_spmv", "qeq_vector", "qeq_finish", "nve"};
+
+struct Prof {
+  bool on = false;
+  std::vector<cudaEvent_t> pool;
+  std::vector<int> phase;   // phase of each recorded event (-1 = gap)
+  size_t used = 0;
+  double ms[PH_N] = {0};
+  long long cnt[PH_N] = {0};
+  void mark(cudaStream_t st, int ph) {
+    if (!on) return;
+    if (used == pool.size()) {
+      if (used >= 4096) resolve();
+      if (used == pool.size()) {
+        cudaEvent_t e;
+        cudaEventCreate(&e);
+        pool.push_back(e);
+        phase.push_back(-1);
+      }
+    }
+    cudaEventRecord(pool[used], st);
+    phase[used] = ph;
+    ++used;
+  }
+  void resolve() {
+    if (used == 0) return;
+    cudaEventSynchronize(pool[used - 1]);
+    for (size_t k = 0; k + 1 < used; ++k) {
+      if (phase[k] < 0) continue;
+      float t = 0.f;
+      cudaEventElapsedTime(&t, pool[k], pool[k + 1]);
+      ms[phase[k]] += t;
+      cnt[phase[k]] += 1;
+    }
+    used = 0;
+  }
+  void reset() {
+    used = 0;
+    for (int k = 0; k < PH_N; ++k) ms[k] = 0, cnt[k] = 0;
+  }
+  ~Prof() {
+    for (auto e : pool) cudaEventDestroy(e);
+  }
+};
+
 struct rg_system {
   rg_params p{};
   ForceField ff{};
@@ -39,9 +93,20 @@ struct rg_system {
   bool forces_valid = false;
   rg_stats stats{};
   double energy[RG_NE] = {0};
+  Prof prof;
+  long long launches = 0;   // kernels of this library launched so far
 };
 
 namespace {
+
+struct Scope {
+  rg_system *h;
+  Scope(rg_system *hh, int ph, int kernels) : h(hh) {
+    h->prof.mark(h->st, ph);
+    h->launches += kernels;
+  }
+  ~Scope() { h->prof.mark(h->st, -1); }
+};
 
 int fail(rg_system *h, int code, const std::string &msg) {
   if (h) h->err = msg;
@@ -212,10 +277,16 @@ int build_lists(rg_system *h) {
   int rc = setup_cells(h);
   if (rc) return rc;
   CK(cudaMemsetAsync(d.status, 0, 8 * sizeof(int), h->st));
-  launch_bin_sort(d, h->st);
+  {
+    Scope sc(h, PH_BIN, 7);
+    launch_bin_sort(d, h->st);
+  }
   int st[8];
   for (int attempt = 0;; ++attempt) {
-    launch_build_nbrs(d, h->st);
+    {
+      Scope sc(h, PH_NBR, 1);
+      launch_build_nbrs(d, h->st);
+    }
     if ((rc = read_status(h, st))) return rc;
     if (!(st[ST_OVF] & OVF_NBR)) break;
     if (attempt > 3) return fail(h, RG_E_CAPACITY, "pair list capacity");
@@ -225,7 +296,11 @@ int build_lists(rg_system *h) {
     CK(cudaMemsetAsync(d.status, 0, 8 * sizeof(int), h->st));
   }
   for (int attempt = 0;; ++attempt) {
-    launch_build_bonds(d, h->st);
+    {
+      Scope sc(h, PH_BOND, 3);
+      launch_build_bonds(d, h->st);
+      launch_count(d, h->st);
+    }
     if ((rc = read_status(h, st))) return rc;
     if (!(st[ST_OVF] & (OVF_BOND | OVF_HB))) break;
     if (attempt > 3) return fail(h, RG_E_CAPACITY, "bond list capacity");
@@ -240,6 +315,10 @@ int build_lists(rg_system *h) {
     h->stats.regrows++;
     CK(cudaMemsetAsync(d.status, 0, 8 * sizeof(int), h->st));
   }
+  h->stats.n_pairs = st[5];
+  h->stats.n_H_entries = st[5];
+  h->stats.n_bonds = st[6];
+  h->stats.n_hbond_pairs = st[7];
   h->stats.max_nbrs = st[ST_MAXNB];
   h->stats.max_bonds = st[ST_MAXB];
   h->stats.max_hbonds = st[ST_MAXHB];
@@ -253,11 +332,13 @@ int do_compute(rg_system *h, int eflag) {
   if (!h->lists_valid && (rc = build_lists(h))) return rc;
   CK(cudaMemsetAsync(d.fC, 0, 4 * sizeof(double) * (size_t)d.n, h->st));
   CK(cudaMemsetAsync(d.energy, 0, RG_NE * sizeof(double), h->st));
-  launch_bond_orders(d, h->st);
-  launch_bonded_terms(d, h->st, eflag);
-  launch_nonbonded(d, h->st, eflag);
-  launch_dbond_forces(d, h->st);
-  launch_force_out(d, h->st);
+  { Scope sc(h, PH_BO, 3); launch_bond_orders(d, h->st); }
+  { Scope sc(h, PH_ATOM, 1); launch_atom_energy(d, h->st, eflag); }
+  { Scope sc(h, PH_HB, 1); launch_hbonds(d, h->st, eflag); }
+  { Scope sc(h, PH_VALTOR, 1); launch_valence_torsion(d, h->st, eflag); }
+  { Scope sc(h, PH_NONB, 1); launch_nonbonded(d, h->st, eflag); }
+  { Scope sc(h, PH_DBOND, 1); launch_dbond_forces(d, h->st); }
+  { Scope sc(h, PH_FOUT, 1); launch_force_out(d, h->st); }
   CK(cudaGetLastError());
   h->forces_valid = true;
   return 0;
@@ -269,8 +350,11 @@ int do_qeq(rg_system *h, int *its, int *itt) {
   if (!h->lists_valid && (rc = build_lists(h))) return rc;
   double hostred[2] = {h->p.qeq_tol, (double)h->p.qeq_imax};
   CK(cudaMemcpyAsync(d.red + 26, hostred, 2 * sizeof(double), cudaMemcpyHostToDevice, h->st));
-  launch_qeq_setup(d, h->st);
-  launch_qeq_cg_init(d, h->st);
+  {
+    Scope sc(h, PH_QSETUP, 9);
+    launch_qeq_setup(d, h->st);
+    launch_qeq_cg_init(d, h->st);
+  }
   // iterate; poll the activity flags every few iterations
   double flags[4];
   int done_iters = 0;
@@ -280,14 +364,18 @@ int do_qeq(rg_system *h, int *its, int *itt) {
     CK(cudaStreamSynchronize(h->st));
     if (flags[0] == 0.0 && flags[1] == 0.0) break;
     if (done_iters > h->p.qeq_imax + 8) return fail(h, RG_E_NUMERIC, "QEq iteration control lost");
-    for (int k = 0; k < chunk; ++k) launch_qeq_cg_iter(d, h->st);
+    for (int k = 0; k < chunk; ++k) {
+      { Scope sc(h, PH_QVEC, 1); launch_qeq_cg_A(d, h->st); }
+      { Scope sc(h, PH_QSPMV, 1); launch_qeq_spmv(d, h->st, d.qd, d.qq); }
+      { Scope sc(h, PH_QVEC, 3); launch_qeq_cg_C(d, h->st); }
+    }
     done_iters += chunk;
   }
   h->stats.cg_iters_s = (int)flags[2];
   h->stats.cg_iters_t = (int)flags[3];
   if (its) *its = (int)flags[2];
   if (itt) *itt = (int)flags[3];
-  launch_qeq_finish(d, h->st);
+  { Scope sc(h, PH_QFIN, 2); launch_qeq_finish(d, h->st); }
   CK(cudaGetLastError());
   return 0;
 }
@@ -526,16 +614,50 @@ int rg_run(rg_system *h, int nsteps, double dt, double *energies) {
     if ((rc = do_compute(h, 1))) return rc;
   }
   for (int s = 0; s < nsteps; ++s) {
-    launch_nve_initial(h->d, h->st, dt);
+    { Scope sc(h, PH_NVE, 1); launch_nve_initial(h->d, h->st, dt); }
     h->lists_valid = false;
+    h->forces_valid = false;
     if ((rc = do_qeq(h, nullptr, nullptr))) return rc;
     if ((rc = do_compute(h, energies != nullptr && s == nsteps - 1))) return rc;
-    launch_nve_final(h->d, h->st, dt);
+    { Scope sc(h, PH_NVE, 1); launch_nve_final(h->d, h->st, dt); }
   }
   if (energies) CK(cudaMemcpyAsync(energies, h->d.energy, RG_NE * sizeof(double), cudaMemcpyDeviceToHost, h->st));
   CK(cudaStreamSynchronize(h->st));
   CK(cudaGetLastError());
   return RG_OK;
+}
+
+int rg_set_state(rg_system *h, const double *x, const double *v, const double *f) {
+  if (!h || !x) return RG_E_ARG;
+  if (!h->n) return fail(h, RG_E_STATE, "no atoms set");
+  CK(cudaMemcpyAsync(h->d.x_o, x, 3 * sizeof(double) * h->n, cudaMemcpyHostToDevice, h->st));
+  if (v) CK(cudaMemcpyAsync(h->d.v_o, v, 3 * sizeof(double) * h->n, cudaMemcpyHostToDevice, h->st));
+  if (f) CK(cudaMemcpyAsync(h->d.f_o, f, 3 * sizeof(double) * h->n, cudaMemcpyHostToDevice, h->st));
+  h->lists_valid = false;
+  h->forces_valid = f != nullptr;
+  return RG_OK;
+}
+
+void *rg_stream(rg_system *h) { return h ? (void *)h->st : nullptr; }
+
+int rg_profile_enable(rg_system *h, int on) {
+  if (!h) return RG_E_ARG;
+  if (on) h->prof.reset();
+  else h->prof.resolve();
+  h->prof.on = on != 0;
+  return RG_OK;
+}
+
+int rg_profile_get(rg_system *h, int max, char *names, double *ms, long long *count) {
+  if (!h) return RG_E_ARG;
+  h->prof.resolve();
+  const int k = std::min(max, (int)PH_N);
+  for (int i = 0; i < k; ++i) {
+    if (names) std::snprintf(names + 32 * i, 32, "%s", kPhaseNames[i]);
+    if (ms) ms[i] = h->prof.ms[i];
+    if (count) count[i] = h->prof.cnt[i];
+  }
+  return PH_N;
 }
 
 int rg_get_atoms(rg_system *h, double *x, double *v, double *q, double *f) {
@@ -562,6 +684,7 @@ int rg_get_stats(const rg_system *h, rg_stats *s) {
   if (!h || !s) return RG_E_ARG;
   *s = h->stats;
   s->n_atoms = h->n;
+  s->kernel_launches = h->launches;
   return RG_OK;
 }
 

@@ -148,12 +148,23 @@ struct Dev {
   double *red;        // device scalars / reduction accumulators
   double *energy;     // [RG_NE]
 
-  int *status;        // [8]: 0 overflow flags, 1 max nbrs, 2 max bonds, 3 max hb, 4 nonfinite
+  int *status;        // [8]: 0 overflow flags, 1 max nbrs, 2 max bonds, 3 max hb, 4 nonfinite,
+                      //      5 pair entries, 6 bonds, 7 H-bond partners
 };
 
 // status slots
 enum { ST_OVF = 0, ST_MAXNB = 1, ST_MAXB = 2, ST_MAXHB = 3, ST_NAN = 4 };
 enum { OVF_NBR = 1, OVF_BOND = 2, OVF_HB = 4, OVF_CELL = 8 };
+
+// x^c for the reference's truncated cube-root exponents c = 0.3333333333333
+// (QEq H, fix_qeq_reax_sw64.c:885) and 0.33333333333333 (Coulomb,
+// reaxc_nonbonded_sw64.c:195): cbrt(x) * x^(c - 1/3), where the tiny second
+// factor is 1 + (c - 1/3) ln x to far below an ulp (ln x in FP32 suffices).
+#define RG_C3_QEQ (0.3333333333333 - 1.0 / 3.0)
+#define RG_C3_ELE (0.33333333333333 - 1.0 / 3.0)
+__device__ __forceinline__ double pow_third(double x, double dc) {
+  return cbrt(x) * (1.0 + dc * (double)__logf((float)x));
+}
 
 // image code of a neighbour entry: sx,sy,sz in [-2,2]
 __host__ __device__ inline int img_pack(int sx, int sy, int sz) {
@@ -169,18 +180,21 @@ __host__ __device__ inline void img_unpack(int c, int *sx, int *sy, int *sz) {
 void launch_bin_sort(const Dev &d, cudaStream_t st);
 void launch_build_nbrs(const Dev &d, cudaStream_t st);
 void launch_build_bonds(const Dev &d, cudaStream_t st);
+void launch_count(const Dev &d, cudaStream_t st);
 void launch_bond_orders(const Dev &d, cudaStream_t st);
-void launch_bonded_terms(const Dev &d, cudaStream_t st, int eflag);
+void launch_atom_energy(const Dev &d, cudaStream_t st, int eflag);
+void launch_hbonds(const Dev &d, cudaStream_t st, int eflag);
+void launch_valence_torsion(const Dev &d, cudaStream_t st, int eflag);
 void launch_nonbonded(const Dev &d, cudaStream_t st, int eflag);
 void launch_dbond_forces(const Dev &d, cudaStream_t st);
 void launch_force_out(const Dev &d, cudaStream_t st);
-void launch_energy_pol(const Dev &d, cudaStream_t st);
 
 // QEq
 void launch_qeq_setup(const Dev &d, cudaStream_t st);
 void launch_qeq_spmv(const Dev &d, cudaStream_t st, const double2 *x, double2 *y);
 void launch_qeq_cg_init(const Dev &d, cudaStream_t st);
-void launch_qeq_cg_iter(const Dev &d, cudaStream_t st);
+void launch_qeq_cg_A(const Dev &d, cudaStream_t st);
+void launch_qeq_cg_C(const Dev &d, cudaStream_t st);
 void launch_qeq_finish(const Dev &d, cudaStream_t st);
 
 // NVE

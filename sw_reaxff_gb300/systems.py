@@ -4,7 +4,7 @@ The reference ships only a TATB crystal deck; the workloads measured here are
 seeded synthetic liquids with the molecule mix, density and temperature of
 each workload (2,000-molecule water box; 1,048,576-atom H2O/CH4/C2H6/NH3
 mixture; small random packs of H2O/CH4/NH3/CO2/C2H6).  Molecules sit on a
-jittered cubic lattice with uniformly random orientations; orientations that
+jittered FCC lattice with uniformly random orientations; orientations that
 put two atoms of different molecules closer than ``min_dist`` are redrawn.
 
 Units are LAMMPS ``real``: Angstrom, g/mol, fs, kcal/mol.
@@ -112,11 +112,8 @@ def _random_rotations(rng, k):
     ], 1)
 
 
-def _close_molecules(x, mol, box, dmin):
-    """Indices of molecules with an atom closer than dmin to an atom of
-    another molecule (periodic).  Cell hashing with 27 neighbour cells."""
-    n = x.shape[0]
-    nc = np.maximum((box // dmin).astype(int), 1)
+def _cell_table(x, box, cw_min):
+    nc = np.maximum((box // cw_min).astype(int), 1)
     cw = box / nc
     ci = np.minimum((x // cw).astype(int), nc - 1)
     cid = (ci[:, 2] * nc[1] + ci[:, 1]) * nc[0] + ci[:, 0]
@@ -125,35 +122,57 @@ def _close_molecules(x, mol, box, dmin):
     ncell = int(nc.prod())
     start = np.searchsorted(cs, np.arange(ncell), "left")
     end = np.searchsorted(cs, np.arange(ncell), "right")
-    occ = end - start
-    M = int(occ.max()) if n else 0
+    M = int((end - start).max()) if len(x) else 1
     table = np.full((ncell, max(M, 1)), -1, dtype=np.int64)
-    rank = np.arange(n) - start[cs]
+    rank = np.arange(len(x)) - start[cs]
     table[cs, rank] = order
-    bad = np.zeros(int(mol.max()) + 1 if n else 0, dtype=bool)
+    return nc, ci, table
+
+
+def _min_contact(xq, molq, x, mol, box, dmin, table=None):
+    """Per query point: the smallest periodic distance to an atom of x that
+    belongs to another molecule, when below dmin (else inf)."""
+    nc, ci, tab = table if table is not None else _cell_table(x, box, dmin)
+    out = np.full(len(xq), np.inf)
+    cw = box / nc
+    cq = np.minimum((xq // cw).astype(int), nc - 1) % nc
     for dz in (-1, 0, 1):
         for dy in (-1, 0, 1):
             for dx in (-1, 0, 1):
-                nb = (ci + np.array([dx, dy, dz])) % nc
+                nb = (cq + np.array([dx, dy, dz])) % nc
                 nid = (nb[:, 2] * nc[1] + nb[:, 1]) * nc[0] + nb[:, 0]
-                cand = table[nid]                       # (n, M)
+                cand = tab[nid]
                 valid = cand >= 0
                 cj = np.where(valid, cand, 0)
-                d = x[cj] - x[:, None, :]
+                d = x[cj] - xq[:, None, :]
                 d -= box * np.round(d / box)
                 r2 = (d * d).sum(-1)
-                hit = valid & (r2 < dmin * dmin) & (mol[cj] != mol[:, None])
-                rows = np.nonzero(hit.any(1))[0]
-                bad[mol[rows]] = True
-    return np.nonzero(bad)[0]
+                r2 = np.where(valid & (mol[cj] != molq[:, None]), r2, np.inf)
+                out = np.minimum(out, np.sqrt(r2.min(1)))
+    return out
+
+
+def _fcc_sites(nmol, box, rng):
+    """nmol random sites of the smallest FCC lattice with >= nmol points."""
+    m = 1
+    while 4 * m ** 3 < nmol:
+        m += 1
+    g = np.stack(np.meshgrid(np.arange(m), np.arange(m), np.arange(m),
+                             indexing="ij"), -1).reshape(-1, 3).astype(float)
+    basis = np.array([[0, 0, 0], [0.5, 0.5, 0], [0.5, 0, 0.5], [0, 0.5, 0.5]])
+    pts = (g[:, None, :] + basis[None]).reshape(-1, 3) + 0.25
+    pts = pts[rng.permutation(len(pts))[:nmol]]
+    return pts * (box / m)
 
 
 def pack_molecules(counts: dict, density: float, seed: int, *,
-                   temperature: float = 300.0, jitter: float = 0.3,
-                   min_dist: float = 1.6, max_redraw: int = 60,
-                   box=None) -> System:
+                   temperature: float = 300.0, jitter: float = 0.2,
+                   min_dist: float = 1.5, max_redraw: int = 200,
+                   atom_jitter: float = 0.02, box=None) -> System:
     """Place molecules (counts: name -> number) in a cubic periodic box at
-    ``density`` g/cm^3 on a jittered lattice with random orientations."""
+    ``density`` g/cm^3 on a jittered FCC lattice with random orientations;
+    molecules with an intermolecular contact closer than ``min_dist`` get
+    new orientations until none is left (or ``max_redraw`` rounds)."""
     rng = np.random.default_rng(seed)
     names = []
     for name, k in counts.items():
@@ -168,35 +187,53 @@ def pack_molecules(counts: dict, density: float, seed: int, *,
         L = vol ** (1.0 / 3.0)
         box = np.array([L, L, L])
     box = np.asarray(box, float)
-    m = int(math.ceil(nmol ** (1.0 / 3.0) - 1e-9))
-    sites = np.stack(np.meshgrid(np.arange(m), np.arange(m), np.arange(m),
-                                 indexing="ij"), -1).reshape(-1, 3)
-    sites = sites[rng.permutation(len(sites))[:nmol]]
-    centers = (sites + 0.5) * (box / m)
-    centers += rng.uniform(-jitter, jitter, size=centers.shape)
-    # atoms
-    tmpl_e, tmpl_x, mol_of, atom_mol_slot = [], [], [], []
-    offs = [0]
+    sites = _fcc_sites(nmol, box, rng)
+    centers = sites + rng.uniform(-jitter, jitter, size=sites.shape)
+    tries = np.zeros(nmol, dtype=int)
+    tmpl_e, tmpl_x, mol_of = [], [], []
     for k, nm in enumerate(names):
         e, xyz = MOLECULES[nm]
         tmpl_e += e
         tmpl_x.append(xyz - xyz.mean(0))
         mol_of += [k] * len(e)
-        offs.append(offs[-1] + len(e))
     mol_of = np.array(mol_of)
     local = np.concatenate(tmpl_x)
+    # small per-atom distortion: no molecule sits exactly on a symmetric
+    # (e.g. linear CO2) geometry, where angle derivatives are singular
+    local = local + rng.normal(scale=atom_jitter, size=local.shape)
     rot = _random_rotations(rng, nmol)
-    x = np.einsum("aij,aj->ai", rot[mol_of], local) + centers[mol_of]
-    x %= box
-    for _ in range(max_redraw):
-        bad = _close_molecules(x, mol_of, box, min_dist)
+    x = (np.einsum("aij,aj->ai", rot[mol_of], local) + centers[mol_of]) % box
+    atoms_of = np.split(np.arange(len(x)), np.cumsum(np.bincount(mol_of))[:-1])
+    check = np.arange(len(x))
+    K = 8
+    for it in range(max_redraw):
+        tab = _cell_table(x, box, min_dist)
+        close = _min_contact(x[check], mol_of[check], x, mol_of, box, min_dist, tab) < min_dist
+        bad = np.unique(mol_of[check[close]])
         if len(bad) == 0:
             break
-        newrot = _random_rotations(rng, len(bad))
-        rot[bad] = newrot
-        sel = np.isin(mol_of, bad)
-        x[sel] = (np.einsum("aij,aj->ai", rot[mol_of[sel]], local[sel]) +
-                  centers[mol_of[sel]] + 0.0) % box
+        # best of K new placements (orientation + small move off the site),
+        # scored by the closest contact with the current configuration
+        tries[bad] += 1
+        sel = np.concatenate([atoms_of[b] for b in bad])
+        msel = mol_of[sel]
+        best = np.full(len(bad), -1.0)
+        best_x = x[sel].copy()
+        pos_in_bad = np.searchsorted(bad, msel)
+        for _ in range(K):
+            r = _random_rotations(rng, len(bad))
+            amp = np.minimum(jitter + 0.05 * tries[bad], 0.8)[:, None]
+            c = sites[bad] + rng.uniform(-1, 1, size=(len(bad), 3)) * amp
+            xc = (np.einsum("aij,aj->ai", r[pos_in_bad], local[sel]) + c[pos_in_bad]) % box
+            dmin_atom = _min_contact(xc, msel, x, mol_of, box, 3.0, tab)
+            dmin_mol = np.full(len(bad), np.inf)
+            np.minimum.at(dmin_mol, pos_in_bad, dmin_atom)
+            take = dmin_mol > best
+            best = np.where(take, dmin_mol, best)
+            ta = take[pos_in_bad]
+            best_x[ta] = xc[ta]
+        x[sel] = best_x
+        check = sel
     n = x.shape[0]
     masses = np.array([MASS[e] for e in tmpl_e])
     sig = np.sqrt(KB_KCAL * temperature / (masses * MVV2E))

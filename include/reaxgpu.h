@@ -157,6 +157,25 @@ int rg_profile_enable(rg_system *h, int on);
 int rg_profile_get(rg_system *h, int max, char *names, double *ms,
                    long long *count);
 
+/* Allocation-free QEq (no counterpart in the reference).  For callers that
+ * cannot call cudaMalloc when they need charges -- code running under a host
+ * application's own device-memory manager, or where an allocation would
+ * synchronize or fail.  Same charges as rg_qeq's first solve after
+ * rg_set_atoms (zero initial guesses), within the CG tolerance, for at most
+ * RG_NOALLOC_MAX_ATOMS atoms: H is evaluated on the fly and the CG vectors
+ * live in one static device array of that size, held by every GPU that loads
+ * the library until exit.  Inputs and output are the caller's device arrays:
+ * x[3n] (wrapped into the box), type[n], q_out[n]; box3 is a host array;
+ * stream is a cudaStream_t (NULL: legacy default stream).  h only supplies
+ * the force-field tables copied at rg_create.  The first call on a device
+ * looks up the array's device address (cudaGetSymbolAddress); make it before
+ * any stream capture.  All calls share the array and leave their contents in
+ * it; calls whose GPU work overlaps race.  Larger n is rejected (RG_E_ARG). */
+#define RG_NOALLOC_MAX_ATOMS 8192
+int rg_qeq_noalloc(rg_system *h, int n, const double *x, const int *type,
+                   const double *box3, double *q_out, int *iters_s,
+                   int *iters_t, void *stream);
+
 /* Measured FP64 FMA throughput of a device (TFLOP/s): the roofline
  * denominator of the FP64 form, whose kernels are bound by the FP64 units. */
 int rg_measure_fp64_peak(int device, double *tflops);

@@ -28,7 +28,8 @@ EXPORTED = ["rg_default_params", "rg_create", "rg_destroy", "rg_last_error",
             "rg_compute", "rg_nve_initial", "rg_nve_final", "rg_run",
             "rg_get_atoms", "rg_device_arrays", "rg_get_stats", "rg_synchronize",
             "rg_dump_pairs", "rg_dump_bonds", "rg_dump_hbonds", "rg_set_state",
-            "rg_stream", "rg_profile_enable", "rg_profile_get", "rg_measure_fp64_peak"]
+            "rg_stream", "rg_profile_enable", "rg_profile_get", "rg_measure_fp64_peak",
+            "rg_qeq_noalloc"]
 
 
 class Params(C.Structure):
@@ -100,6 +101,8 @@ def load_library(path: str = LIBPATH):
     L.rg_profile_enable.argtypes = [C.c_void_p, C.c_int]
     L.rg_profile_get.argtypes = [C.c_void_p, C.c_int, C.c_char_p, dp, P(C.c_longlong)]
     L.rg_measure_fp64_peak.argtypes = [C.c_int, dp]
+    L.rg_qeq_noalloc.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, dp,
+                                 C.c_void_p, ip, ip, C.c_void_p]
     _lib = L
     return L
 

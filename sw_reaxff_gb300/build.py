@@ -16,7 +16,7 @@ CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "libreaxgpu.so")
 BUILD = os.path.join(HERE, "_build")
 SOURCES = ["ffield.cpp", "lists.cu", "bonded.cu", "nonbonded.cu", "qeq.cu",
-           "nve.cu", "peak.cu", "reaxgpu.cu"]
+           "nve.cu", "peak.cu", "noalloc.cu", "reaxgpu.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

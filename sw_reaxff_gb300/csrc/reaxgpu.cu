@@ -696,6 +696,20 @@ int rg_synchronize(rg_system *h) {
 
 }  // extern "C"
 
+void rg_set_error(rg_system *h, const std::string &msg) {
+  if (h) h->err = msg;
+}
+
+void rg_noalloc_tables(const rg_system *h, const ForceField **ff, const Control **ctl,
+                       int *device, double *swb, double *tol, int *imax) {
+  *ff = h->d_ff;
+  *ctl = h->d_ctl;
+  *device = h->p.device;
+  *swb = h->p.qeq_swb;
+  *tol = h->p.qeq_tol;
+  *imax = h->p.qeq_imax;
+}
+
 // ------------------------------------------------------------------
 // list dumps (host side, for parity checks)
 

@@ -203,3 +203,9 @@ void launch_nve_final(const Dev &d, cudaStream_t st, double dt);
 
 // generic
 void launch_zero(void *p, size_t bytes, cudaStream_t st);
+
+// accessors used by noalloc.cu (the handle type is private to reaxgpu.cu)
+struct rg_system;
+void rg_set_error(rg_system *h, const std::string &msg);
+void rg_noalloc_tables(const rg_system *h, const ForceField **ff, const Control **ctl,
+                       int *device, double *swb, double *tol, int *imax);

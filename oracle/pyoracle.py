@@ -13,6 +13,9 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB = os.path.join(HERE, "libreax_oracle.so")
+# the reference's own host-side code + harness (built only where the
+# reference sources exist: oracle/ref/Makefile)
+REF_LIB = os.path.join(HERE, "_ref", "libreax_ref.so")
 
 ENERGY_NAMES = ["e_bond", "e_ovun", "e_lp", "e_3", "e_ang", "e_pen", "e_coa",
                 "e_hb", "e_tor", "e_con", "e_vdW", "e_ele", "e_12", "e_pol",
@@ -43,13 +46,31 @@ def build(force: bool = False) -> str:
 
 
 _lib = None
+_reflib = None
 
 
-def lib():
-    global _lib
+def ref_available() -> bool:
+    return os.path.exists(REF_LIB)
+
+
+def lib(path=None):
+    global _lib, _reflib
+    if path == REF_LIB:
+        if _reflib is None:
+            _reflib = _declare(C.CDLL(REF_LIB))
+            P = C.POINTER
+            _reflib.ro_ref_compute.argtypes = [C.c_void_p, P(C.c_double), P(C.c_double),
+                                               P(C.c_double), P(C.c_int), P(C.c_int),
+                                               P(C.c_int), P(C.c_longlong)]
+        return _reflib
     if _lib is None:
         build()
-        L = C.CDLL(LIB)
+        _lib = _declare(C.CDLL(LIB))
+    return _lib
+
+
+def _declare(L):
+    if True:
         P = C.POINTER
         L.ro_default_control.argtypes = [P(Control)]
         L.ro_create.restype = C.c_void_p
@@ -74,8 +95,7 @@ def lib():
         L.ro_dump_atom_terms.argtypes = [C.c_void_p, P(C.c_double)]
         L.ro_last_time.restype = C.c_double
         L.ro_last_time.argtypes = [C.c_void_p, C.c_int]
-        _lib = L
-    return _lib
+    return L
 
 
 def _dp(a):
@@ -89,8 +109,10 @@ def _ip(a):
 class Oracle:
     """Stateful CPU oracle for one periodic system."""
 
-    def __init__(self, ffield: str, **control):
-        L = lib()
+    def __init__(self, ffield: str, reference: bool = False, **control):
+        """reference=True loads the build that also carries the reference's
+        own host-side code (ref_compute)."""
+        L = lib(REF_LIB if reference else None)
         ctl = Control()
         L.ro_default_control(C.byref(ctl))
         for k, v in control.items():
@@ -137,6 +159,24 @@ class Oracle:
         e = np.zeros(NENERGY)
         self.L.ro_compute(self.h, _dp(f), _dp(e))
         return f, dict(zip(ENERGY_NAMES, e))
+
+    def ref_compute(self):
+        """The reference's own CPU routines on this oracle's lists: forces,
+        energies, corrected bond orders (local bond entries in the oracle's
+        order) and the reference-built H-bond list."""
+        f = np.zeros((self.n, 3))
+        e = np.zeros(NENERGY)
+        nb = self.L.ro_dump_bonds(self.h, None, None, None, None)
+        bo = np.zeros((max(nb, 1), 4))
+        cap = max(self.stats()["n_far_local"], 1)
+        ti = np.zeros(cap, np.int32); tj = np.zeros(cap, np.int32); im = np.zeros(cap, np.int32)
+        nh = C.c_longlong()
+        rc = self.L.ro_ref_compute(self.h, _dp(f), _dp(e), _dp(bo), _ip(ti), _ip(tj), _ip(im),
+                                   C.byref(nh))
+        if rc:
+            raise RuntimeError(f"reference code aborted with {rc}")
+        k = nh.value
+        return f, dict(zip(ENERGY_NAMES, e)), bo[:nb], (ti[:k], tj[:k], im[:k])
 
     def run_nve(self, nsteps, dt):
         e = np.zeros(NENERGY)

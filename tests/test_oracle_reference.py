@@ -1,0 +1,38 @@
+"""The oracle against the reference's own compiled host-side code, live
+(only where the reference sources were available to build
+oracle/_ref/libreax_ref.so; elsewhere the golden fixtures carry this
+check)."""
+import numpy as np
+import pytest
+
+from oracle.pyoracle import Oracle, ref_available
+from sw_reaxff_gb300 import systems
+
+pytestmark = pytest.mark.skipif(not ref_available(), reason="reference build not present")
+
+SYSTEMS = {
+    "water": lambda: systems.water_box(120, seed=77),
+    "mixture": lambda: systems.mixture(scale=0.0008, seed=78),
+    "pack_co2": lambda: systems.small_pack(200, 0.7, seed=79),
+}
+
+
+@pytest.mark.parametrize("name", list(SYSTEMS))
+def test_oracle_equals_reference(name, ffield):
+    s = SYSTEMS[name]()
+    t = s.types(["C", "H", "O", "N"])
+    o = Oracle(ffield, reference=True)
+    o.set_system(s.box, s.x, t, s.tag, None, s.v)
+    q, _, _ = o.qeq()
+    o.set_system(s.box, s.x, t, s.tag, q, s.v)
+    fo, eo = o.compute()
+    _, _, _, boo = o.bond_list()
+    hb_o = set(zip(*[a.tolist() for a in o.hbond_list()]))
+    fr, er, bor, hb = o.ref_compute()
+    assert np.abs(boo - bor).max() == 0.0
+    assert hb_o == set(zip(*[a.tolist() for a in hb]))
+    assert np.sqrt(((fo - fr) ** 2).sum() / (fr ** 2).sum()) < 1e-12
+    for k in eo:
+        if k == "e_pol_phys":
+            continue
+        assert abs(eo[k] - er[k]) <= max(1e-12 * abs(er[k]), 1e-10), (k, eo[k], er[k])

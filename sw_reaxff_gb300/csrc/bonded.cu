@@ -349,66 +349,88 @@ __global__ void k_atom_energy(Dev d, int eflag) {
 }
 
 // ------------------------------------------------------------------
-// hydrogen bonds: one thread per H atom j
+// hydrogen bonds: one warp per H atom j; for each bonded acceptor i
+// (p_hbond 2, BO >= 0.01) the lanes take the H-bond partners k
 
-__global__ void k_hbonds(Dev d, int eflag) {
-  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ double warp_sum_d(double v) {
+  for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(FULL, v, off);
+  return v;
+}
+
+__global__ void __launch_bounds__(256) k_hbonds(Dev d, int eflag) {
+  const int lane = threadIdx.x & 31;
+  const int j = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int n = d.n;
   double ehb = 0.0;
-  if (j < n) {
+  if (j < n && d.ff->sbp[d.ts[j]].p_hbond == 1) {
     const ForceField &F = *d.ff;
     const int tj = d.ts[j];
-    if (F.sbp[tj].p_hbond == 1) {
-      const int nb = min(d.nbonds[j], d.bond_cap);
-      const int nh = min(d.nhb[j], d.hb_cap);
-      const double4 xj = d.xs[j];
-      double *fC = d.fC;
-      for (int pk = 0; pk < nh; ++pk) {
+    const int nb = min(d.nbonds[j], d.bond_cap);
+    const int nh = min(d.nhb[j], d.hb_cap);
+    const double4 xj = d.xs[j];
+    double *fC = d.fC;
+    double fjx = 0, fjy = 0, fjz = 0;
+    for (int q = 0; q < nb; ++q) {
+      const long long s = (long long)q * n + j;
+      const int i = nbr_of(d.b_nbr[s]);
+      const int ti = d.ts[i];
+      const double BO = d.b_BO[s];
+      if (F.sbp[ti].p_hbond != 2 || !(BO >= HB_THRESHOLD)) continue;
+      const double dij[3] = {d.b_dx[s], d.b_dy[s], d.b_dz[s]};
+      const double r_ij = d.b_d[s];
+      const int tag_i = d.tags[i];
+      double fix = 0, fiy = 0, fiz = 0, cdbo = 0;
+      for (int pk = lane; pk < nh; pk += 32) {
         const uint32_t ek = d.hb_nbr[(long long)j * d.hb_cap + pk];
         const int k = nbr_of(ek), tk = d.ts[k];
+        if (d.tags[k] == tag_i) continue;
+        const Hbp &hbp = F.hbp[ti][tj][tk];
+        if (hbp.r0_hb <= 0.0) continue;
         int sx, sy, sz;
         img_unpack((int)(ek & 255u), &sx, &sy, &sz);
         const double4 xk = d.xs[k];
-        double dvec_jk[3];
-        dvec_jk[0] = __dsub_rn(__dadd_rn(xk.x, sx * d.L[0]), xj.x);
-        dvec_jk[1] = __dsub_rn(__dadd_rn(xk.y, sy * d.L[1]), xj.y);
-        dvec_jk[2] = __dsub_rn(__dadd_rn(xk.z, sz * d.L[2]), xj.z);
-        const double r_jk = __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(dvec_jk[0], dvec_jk[0]),
-                                                           __dmul_rn(dvec_jk[1], dvec_jk[1])),
-                                                 __dmul_rn(dvec_jk[2], dvec_jk[2])));
-        for (int q = 0; q < nb; ++q) {
-          const long long s = (long long)q * n + j;
-          const int i = nbr_of(d.b_nbr[s]);
-          const int ti = d.ts[i];
-          if (F.sbp[ti].p_hbond != 2 || !(d.b_BO[s] >= HB_THRESHOLD)) continue;
-          if (d.tags[i] == d.tags[k]) continue;
-          const Hbp &hbp = F.hbp[ti][tj][tk];
-          if (hbp.r0_hb <= 0.0) continue;
-          const double dij[3] = {d.b_dx[s], d.b_dy[s], d.b_dz[s]};
-          double theta, cos_theta, di[3], djv[3], dk[3];
-          theta_dcos(dij, d.b_d[s], dvec_jk, r_jk, theta, cos_theta, di, djv, dk);
-          const double sin_theta2 = sin(theta / 2.0);
-          double sin_xhz4 = sqr(sin_theta2);
-          sin_xhz4 *= sin_xhz4;
-          const double cos_xhz1 = 1.0 - cos_theta;
-          const double BO = d.b_BO[s];
-          const double exp_hb2 = exp(-hbp.p_hb2 * BO);
-          const double exp_hb3 = exp(-hbp.p_hb3 * (hbp.r0_hb / r_jk + r_jk / hbp.r0_hb - 2.0));
-          const double e_hb = hbp.p_hb1 * (1.0 - exp_hb2) * exp_hb3 * sin_xhz4;
-          ehb += e_hb;
-          const double CEhb1 = hbp.p_hb1 * hbp.p_hb2 * exp_hb2 * exp_hb3 * sin_xhz4;
-          const double CEhb2 = -hbp.p_hb1 / 2.0 * (1.0 - exp_hb2) * exp_hb3 * cos_xhz1;
-          const double CEhb3 = -hbp.p_hb3 * (-hbp.r0_hb / sqr(r_jk) + 1.0 / hbp.r0_hb) * e_hb;
-          d.b_Cdbo[s] += CEhb1;
-          add3(fC, n, i, CEhb2, di[0], di[1], di[2]);
-          const double c3 = CEhb3 / r_jk;
-          add3(fC, n, j, 1.0, CEhb2 * djv[0] - c3 * dvec_jk[0], CEhb2 * djv[1] - c3 * dvec_jk[1],
-               CEhb2 * djv[2] - c3 * dvec_jk[2]);
-          add3(fC, n, k, 1.0, CEhb2 * dk[0] + c3 * dvec_jk[0], CEhb2 * dk[1] + c3 * dvec_jk[1],
-               CEhb2 * dk[2] + c3 * dvec_jk[2]);
-        }
+        double djk[3];
+        djk[0] = __dsub_rn(__dadd_rn(xk.x, sx * d.L[0]), xj.x);
+        djk[1] = __dsub_rn(__dadd_rn(xk.y, sy * d.L[1]), xj.y);
+        djk[2] = __dsub_rn(__dadd_rn(xk.z, sz * d.L[2]), xj.z);
+        const double r_jk = __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(djk[0], djk[0]),
+                                                           __dmul_rn(djk[1], djk[1])),
+                                                 __dmul_rn(djk[2], djk[2])));
+        double theta, cos_theta, di[3], djv[3], dk[3];
+        theta_dcos(dij, r_ij, djk, r_jk, theta, cos_theta, di, djv, dk);
+        const double sin_theta2 = sin(theta / 2.0);
+        double sin_xhz4 = sqr(sin_theta2);
+        sin_xhz4 *= sin_xhz4;
+        const double cos_xhz1 = 1.0 - cos_theta;
+        const double exp_hb2 = exp(-hbp.p_hb2 * BO);
+        const double exp_hb3 = exp(-hbp.p_hb3 * (hbp.r0_hb / r_jk + r_jk / hbp.r0_hb - 2.0));
+        const double e_hb = hbp.p_hb1 * (1.0 - exp_hb2) * exp_hb3 * sin_xhz4;
+        ehb += e_hb;
+        const double CEhb1 = hbp.p_hb1 * hbp.p_hb2 * exp_hb2 * exp_hb3 * sin_xhz4;
+        const double CEhb2 = -hbp.p_hb1 / 2.0 * (1.0 - exp_hb2) * exp_hb3 * cos_xhz1;
+        const double CEhb3 = -hbp.p_hb3 * (-hbp.r0_hb / sqr(r_jk) + 1.0 / hbp.r0_hb) * e_hb;
+        cdbo += CEhb1;
+        fix += CEhb2 * di[0]; fiy += CEhb2 * di[1]; fiz += CEhb2 * di[2];
+        const double c3 = CEhb3 / r_jk;
+        fjx += CEhb2 * djv[0] - c3 * djk[0];
+        fjy += CEhb2 * djv[1] - c3 * djk[1];
+        fjz += CEhb2 * djv[2] - c3 * djk[2];
+        add3(fC, n, k, 1.0, CEhb2 * dk[0] + c3 * djk[0], CEhb2 * dk[1] + c3 * djk[1],
+             CEhb2 * dk[2] + c3 * djk[2]);
+      }
+      cdbo = warp_sum_d(cdbo);
+      fix = warp_sum_d(fix);
+      fiy = warp_sum_d(fiy);
+      fiz = warp_sum_d(fiz);
+      if (lane == 0) {
+        d.b_Cdbo[s] += cdbo;
+        if (fix != 0.0 || fiy != 0.0 || fiz != 0.0) add3(fC, n, i, 1.0, fix, fiy, fiz);
       }
     }
+    fjx = warp_sum_d(fjx);
+    fjy = warp_sum_d(fjy);
+    fjz = warp_sum_d(fjz);
+    if (lane == 0 && (fjx != 0.0 || fjy != 0.0 || fjz != 0.0)) add3(fC, n, j, 1.0, fjx, fjy, fjz);
   }
   if (eflag) {
     block_add(ehb, &d.energy[E_HB]);
@@ -834,7 +856,8 @@ void launch_atom_energy(const Dev &d, cudaStream_t st, int eflag) {
 }
 
 void launch_hbonds(const Dev &d, cudaStream_t st, int eflag) {
-  k_hbonds<<<(d.n + 255) / 256, 256, 0, st>>>(d, eflag);
+  const long long threads = (long long)d.n * 32;
+  k_hbonds<<<(unsigned)((threads + 255) / 256), 256, 0, st>>>(d, eflag);
 }
 
 void launch_valence_torsion(const Dev &d, cudaStream_t st, int eflag) {

@@ -148,27 +148,99 @@ __global__ void k_gather(Dev d) {
 
 // -------------------------------------------------------------------
 // pair list (full, both directions) + QEq H values
+//
+// One warp per atom i.  The 5x5x5 stencil is walked as 25 rows of cells
+// along x; a row is one or two runs of consecutive cells, i.e. contiguous
+// ranges of the cell-sorted atoms, so 32 candidates are tested per step
+// (FP32 distance prefilter with a safety margin).  Survivors go to a
+// per-warp shared queue; every full batch of 32 is finished with all lanes
+// busy: exact FP64 distance, list membership, near/far split and the H_ij
+// value, written by ballot compaction (near entries from the front of the
+// row, far entries from the back).
 
-__global__ void __launch_bounds__(256) k_build_nbrs(Dev d) {
+constexpr int NB_WARPS = 8;          // warps per block in k_build_nbrs
+constexpr int QCAP = 64;             // queue slots per warp
+
+struct NbrQueue {
+  int j[QCAP];
+  int img[QCAP];
+};
+
+// finish 32 queued candidates (lanes with q < cnt hold one each)
+__device__ __forceinline__ void nbr_flush(const Dev &d, const Control &C, const ForceField &F,
+                                          const NbrQueue &Q, int cnt, int lane, int i,
+                                          const double4 &xi, int ti, long long row, int cap,
+                                          int &cntN, int &cntF) {
+  bool in = false, near = false;
+  double d2 = 0.0;
+  int j = 0, img = 0;
+  if (lane < cnt) {
+    j = Q.j[lane];
+    img = Q.img[lane];
+    int sx, sy, sz;
+    img_unpack(img, &sx, &sy, &sz);
+    const double4 xj = d.xs[j];
+    const double dx = __dsub_rn(__dadd_rn(xj.x, sx * d.L[0]), xi.x);
+    const double dy = __dsub_rn(__dadd_rn(xj.y, sy * d.L[1]), xi.y);
+    const double dz = __dsub_rn(__dadd_rn(xj.z, sz * d.L[2]), xi.z);
+    d2 = __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
+    in = d2 <= C.list_cut2;
+    if (in) {
+      const double nc2 = C.near_cut * C.near_cut;
+      if (d2 <= nc2 * (1.0 - 1e-12)) near = true;
+      else if (d2 > nc2 * (1.0 + 1e-12)) near = false;
+      else near = __dsqrt_rn(d2) <= C.near_cut;
+    }
+  }
+  const unsigned mn = __ballot_sync(FULL, in && near);
+  const unsigned mf = __ballot_sync(FULL, in && !near);
+  const int tot = cntN + __popc(mn) + cntF + __popc(mf);
+  if (in && tot <= cap) {
+    const int pos = near ? cntN + __popc(mn & lanemask_lt())
+                         : cap - 1 - (cntF + __popc(mf & lanemask_lt()));
+    double h = 0.0;
+    if (d2 <= C.swb2) {
+      // H_ij = Tap(r) * 14.4 / (r^3 + shld)^c, c = 0.3333333333333
+      const double r = d2 * rsqrt(d2);
+      const double *T = C.qTap;
+      double tp = fma(T[7], r, T[6]);
+      tp = fma(tp, r, T[5]);
+      tp = fma(tp, r, T[4]);
+      tp = fma(tp, r, T[3]);
+      tp = fma(tp, r, T[2]);
+      tp = fma(tp, r, T[1]);
+      tp = fma(tp, r, T[0]);
+      const int tj = __float_as_int(d.xf[j].w);
+      const double x = fma(d2, r, F.tbp[ti][tj].gamma);
+      h = tp * 14.4 * rpow_third(x, RG_C3_QEQ);
+    }
+    d.nbr[row + pos] = ((uint32_t)j << 8) | (uint32_t)img;
+    d.hval[row + pos] = h;
+  }
+  cntN += __popc(mn);
+  cntF += __popc(mf);
+}
+
+__global__ void __launch_bounds__(NB_WARPS * 32) k_build_nbrs(Dev d) {
+  __shared__ NbrQueue queues[NB_WARPS];
   const int lane = threadIdx.x & 31;
+  const int wib = threadIdx.x >> 5;
   const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   if (i >= d.n) return;
+  NbrQueue &Q = queues[wib];
   const Control &C = *d.ctl;
   const ForceField &F = *d.ff;
   const double4 xi = d.xs[i];
   const float4 xif = d.xf[i];
   const int ti = d.ts[i];
-  const double cut2 = C.list_cut2;
-  const float cut2f = (float)(cut2 * (1.0 + 1e-5) + 0.05);
-  const double nc2 = C.near_cut * C.near_cut;
-  const double nc2lo = nc2 * (1.0 - 1e-12), nc2hi = nc2 * (1.0 + 1e-12);
+  const float cut2f = (float)(C.list_cut2 * (1.0 + 1e-5) + 0.05);
   const int cx = cell_of(xi.x, d.cellw[0], d.nc[0]);
   const int cy = cell_of(xi.y, d.cellw[1], d.nc[1]);
   const int cz = cell_of(xi.z, d.cellw[2], d.nc[2]);
   const long long row = (long long)i * d.nb_cap;
   const int cap = d.nb_cap;
-  const double gam_i = F.sbp[ti].gamma;
-  int cntN = 0, cntF = 0;
+  const int nx = d.nc[0];
+  int cntN = 0, cntF = 0, qn = 0;
   for (int oz = -d.S; oz <= d.S; ++oz) {
     int rz = cz + oz, sz = 0;
     while (rz < 0) { rz += d.nc[2]; --sz; }
@@ -177,75 +249,64 @@ __global__ void __launch_bounds__(256) k_build_nbrs(Dev d) {
       int ry = cy + oy, sy = 0;
       while (ry < 0) { ry += d.nc[1]; --sy; }
       while (ry >= d.nc[1]) { ry -= d.nc[1]; ++sy; }
-      for (int ox = -d.S; ox <= d.S; ++ox) {
+      const int rowcell = (rz * d.nc[1] + ry) * nx;
+      // runs of consecutive cells with one x image each
+      int ox = -d.S;
+      while (ox <= d.S) {
         int rx = cx + ox, sx = 0;
-        while (rx < 0) { rx += d.nc[0]; --sx; }
-        while (rx >= d.nc[0]) { rx -= d.nc[0]; ++sx; }
-        const int cw = (rz * d.nc[1] + ry) * d.nc[0] + rx;
-        const int beg = d.cell_start[cw], end = d.cell_start[cw + 1];
-        const double shx = sx * d.L[0], shy = sy * d.L[1], shz = sz * d.L[2];
-        const float shxf = (float)shx, shyf = (float)shy, shzf = (float)shz;
+        while (rx < 0) { rx += nx; --sx; }
+        while (rx >= nx) { rx -= nx; ++sx; }
+        int len = 1;
+        while (ox + len <= d.S && rx + len < nx) ++len;
+        const int beg = d.cell_start[rowcell + rx];
+        const int end = d.cell_start[rowcell + rx + len];
+        ox += len;
+        const float shxf = (float)(sx * d.L[0]);
+        const float shyf = (float)(sy * d.L[1]);
+        const float shzf = (float)(sz * d.L[2]);
         const bool self_img = (sx == 0 && sy == 0 && sz == 0);
         const int img = img_pack(sx, sy, sz);
         for (int base = beg; base < end; base += 32) {
           const int j = base + lane;
-          bool in = false, near = false;
-          double d2 = 0.0;
+          bool cand = false;
           if (j < end && !(self_img && j == i)) {
             const float4 xjf = d.xf[j];
             const float fx = xjf.x + shxf - xif.x;
             const float fy = xjf.y + shyf - xif.y;
             const float fz = xjf.z + shzf - xif.z;
-            if (fx * fx + fy * fy + fz * fz <= cut2f) {
-              const double4 xj = d.xs[j];
-              const double dx = __dsub_rn(__dadd_rn(xj.x, shx), xi.x);
-              const double dy = __dsub_rn(__dadd_rn(xj.y, shy), xi.y);
-              const double dz = __dsub_rn(__dadd_rn(xj.z, shz), xi.z);
-              d2 = __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)),
-                             __dmul_rn(dz, dz));
-              in = d2 <= cut2;
-              if (in) {
-                if (d2 <= nc2lo) near = true;
-                else if (d2 > nc2hi) near = false;
-                else near = __dsqrt_rn(d2) <= C.near_cut;
-              }
-            }
+            cand = fx * fx + fy * fy + fz * fz <= cut2f;
           }
-          const unsigned mn = __ballot_sync(FULL, in && near);
-          const unsigned mf = __ballot_sync(FULL, in && !near);
-          const int tot = cntN + __popc(mn) + cntF + __popc(mf);
-          if (in && tot <= cap) {
-            int pos;
-            if (near) pos = cntN + __popc(mn & lanemask_lt());
-            else pos = cap - 1 - (cntF + __popc(mf & lanemask_lt()));
-            double h = 0.0;
-            if (d2 <= C.swb2) {
-              const double r = __dsqrt_rn(d2);
-              const double *T = C.qTap;
-              double tp = fma(T[7], r, T[6]);
-              tp = fma(tp, r, T[5]);
-              tp = fma(tp, r, T[4]);
-              tp = fma(tp, r, T[3]);
-              tp = fma(tp, r, T[2]);
-              tp = fma(tp, r, T[1]);
-              tp = fma(tp, r, T[0]);
-              const int tj = __float_as_int(d.xf[j].w);
-              // shielding (gamma_i*gamma_j)^-1.5, init_shielding
-              // fix_qeq_reax_sunway.cpp:440-454 (= tbp gamma)
-              const double shld = F.tbp[ti][tj].gamma;
-              (void)gam_i;
-              const double den = pow_third(r * r * r + shld, RG_C3_QEQ);
-              h = tp * 14.4 / den;
-            }
-            d.nbr[row + pos] = ((uint32_t)j << 8) | (uint32_t)img;
-            d.hval[row + pos] = h;
+          const unsigned mc = __ballot_sync(FULL, cand);
+          if (cand) {
+            const int slot = qn + __popc(mc & lanemask_lt());
+            Q.j[slot] = j;
+            Q.img[slot] = img;
           }
-          cntN += __popc(mn);
-          cntF += __popc(mf);
+          qn += __popc(mc);
+          __syncwarp();
+          if (qn >= 32) {
+            nbr_flush(d, C, F, Q, 32, lane, i, xi, ti, row, cap, cntN, cntF);
+            __syncwarp();
+            // move the leftover (< 32) to the front of the queue
+            const int left = qn - 32;
+            int lj = 0, limg = 0;
+            if (lane < left) {
+              lj = Q.j[32 + lane];
+              limg = Q.img[32 + lane];
+            }
+            __syncwarp();
+            if (lane < left) {
+              Q.j[lane] = lj;
+              Q.img[lane] = limg;
+            }
+            qn = left;
+            __syncwarp();
+          }
         }
       }
     }
   }
+  if (qn > 0) nbr_flush(d, C, F, Q, qn, lane, i, xi, ti, row, cap, cntN, cntF);
   if (lane == 0) {
     d.n_near[i] = cntN;
     d.n_far[i] = cntF;
@@ -256,101 +317,177 @@ __global__ void __launch_bounds__(256) k_build_nbrs(Dev d) {
 
 // -------------------------------------------------------------------
 // bond list with uncorrected bond orders, and H-bond partners
+//
+// One warp per atom i over the near part of its row.  H-bond partners are
+// decided from the exact distance directly.  Bond candidates (d <= bond_cut)
+// whose FP32 estimate of BO' is above half of bo_cut (FP32 errors are ~1e-4
+// relative here) are queued; full batches of 32 then get the FP64 BO' and
+// the exact BO' >= bo_cut decision with all lanes busy.
 
-__global__ void __launch_bounds__(256) k_build_bonds(Dev d) {
+struct BondQueue {
+  uint32_t e[QCAP];
+  double dist[QCAP], dx[QCAP], dy[QCAP], dz[QCAP];
+};
+
+__device__ __forceinline__ void bond_flush(const Dev &d, const Control &C, const ForceField &F,
+                                           const BondQueue &Q, int cnt, int lane, int i, int ti,
+                                           int &nb, double &ddx, double &ddy, double &ddz,
+                                           double &bsum) {
+  bool isb = false;
+  double dist = 0, dx = 0, dy = 0, dz = 0, BOs = 0, BOpi = 0, BOpi2 = 0, Cs = 0, Cpi = 0, Cpi2 = 0;
+  uint32_t e = 0;
+  if (lane < cnt) {
+    e = Q.e[lane];
+    dist = Q.dist[lane];
+    dx = Q.dx[lane]; dy = Q.dy[lane]; dz = Q.dz[lane];
+    const int tj = d.ts[(int)(e >> 8)];
+    const Sbp &si = F.sbp[ti], &sj = F.sbp[tj];
+    const Tbp &tw = F.tbp[ti][tj];
+    double C12 = 0, C34 = 0, C56 = 0;
+    if (si.r_s > 0.0 && sj.r_s > 0.0) {
+      C12 = tw.p_bo1 * pow(dist / tw.r_s, tw.p_bo2);
+      BOs = (1.0 + C.bo_cut) * exp(C12);
+    }
+    if (si.r_pi > 0.0 && sj.r_pi > 0.0) {
+      C34 = tw.p_bo3 * pow(dist / tw.r_p, tw.p_bo4);
+      BOpi = exp(C34);
+    }
+    if (si.r_pi_pi > 0.0 && sj.r_pi_pi > 0.0) {
+      C56 = tw.p_bo5 * pow(dist / tw.r_pp, tw.p_bo6);
+      BOpi2 = exp(C56);
+    }
+    const double BO = BOs + BOpi + BOpi2;
+    if (BO >= C.bo_cut) {
+      isb = true;
+      const double r2 = dist * dist;
+      Cs = tw.p_bo2 * C12 / r2;
+      Cpi = tw.p_bo4 * C34 / r2;
+      Cpi2 = tw.p_bo6 * C56 / r2;
+    }
+  }
+  const unsigned mb = __ballot_sync(FULL, isb);
+  if (isb) {
+    const int n = d.n;
+    const int k = nb + __popc(mb & lanemask_lt());
+    const double g = -(BOs * Cs + BOpi * Cpi + BOpi2 * Cpi2);
+    const double gx = g * dx, gy = g * dy, gz = g * dz;
+    ddx += gx; ddy += gy; ddz += gz;
+    const double BOc = BOs + BOpi + BOpi2 - C.bo_cut;
+    bsum += BOc;
+    if (k < d.bond_cap) {
+      const long long s = (long long)k * n + i;
+      const long long S3 = (long long)d.bond_cap * n;
+      d.b_nbr[s] = e;
+      d.b_d[s] = dist;
+      d.b_dx[s] = dx; d.b_dy[s] = dy; d.b_dz[s] = dz;
+      d.b_BO[s] = BOc;
+      d.b_BOs[s] = BOs - C.bo_cut;
+      d.b_BOpi[s] = BOpi;
+      d.b_BOpi2[s] = BOpi2;
+      d.b_dBOp[s] = gx; d.b_dBOp[S3 + s] = gy; d.b_dBOp[2 * S3 + s] = gz;
+      const double api = -BOpi * Cpi, api2 = -BOpi2 * Cpi2;
+      d.b_dlnpi[s] = api * dx; d.b_dlnpi[S3 + s] = api * dy; d.b_dlnpi[2 * S3 + s] = api * dz;
+      d.b_dlnpi2[s] = api2 * dx; d.b_dlnpi2[S3 + s] = api2 * dy; d.b_dlnpi2[2 * S3 + s] = api2 * dz;
+      d.b_Cdbo[s] = 0.0; d.b_Cdbopi[s] = 0.0; d.b_Cdbopi2[s] = 0.0;
+    }
+  }
+  nb += __popc(mb);
+}
+
+__global__ void __launch_bounds__(NB_WARPS * 32) k_build_bonds(Dev d) {
+  __shared__ BondQueue queues[NB_WARPS];
   const int lane = threadIdx.x & 31;
   const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   if (i >= d.n) return;
+  BondQueue &Q = queues[threadIdx.x >> 5];
   const Control &C = *d.ctl;
   const ForceField &F = *d.ff;
   const double4 xi = d.xs[i];
+  const float4 xif = d.xf[i];
   const int ti = d.ts[i];
   const Sbp &si = F.sbp[ti];
   const bool ihb = (si.p_hbond == 1) && C.hbond_cut > 0.0;
   const long long row = (long long)i * d.nb_cap;
   const int nn = d.n_near[i] < d.nb_cap ? d.n_near[i] : d.nb_cap;
   const int n = d.n;
-  int nb = 0, nh = 0;
+  // FP32 prefilter radius: anything that could be within bond_cut, and for
+  // H atoms within hbond_cut
+  const float rpre = (float)((ihb ? fmax(C.bond_cut, C.hbond_cut) : C.bond_cut) + 0.01);
+  const float rpre2 = rpre * rpre;
+  const float bo_half = (float)(0.5 * C.bo_cut);
+  int nb = 0, nh = 0, qn = 0;
   double ddx = 0.0, ddy = 0.0, ddz = 0.0, bsum = 0.0;
-  for (int base = 0; base < nn; base += 32) {
-    const int p = base + lane;
-    bool isb = false, ish = false;
-    uint32_t e = 0;
-    double dist = 0, dx = 0, dy = 0, dz = 0, BO = 0, BOs = 0, BOpi = 0, BOpi2 = 0;
-    double Cs = 0, Cpi = 0, Cpi2 = 0;
-    int tj = 0;
-    if (p < nn) {
-      e = d.nbr[row + p];
-      const int j = (int)(e >> 8);
-      int sx, sy, sz;
-      img_unpack((int)(e & 255u), &sx, &sy, &sz);
-      const double4 xj = d.xs[j];
-      dx = __dsub_rn(__dadd_rn(xj.x, sx * d.L[0]), xi.x);
-      dy = __dsub_rn(__dadd_rn(xj.y, sy * d.L[1]), xi.y);
-      dz = __dsub_rn(__dadd_rn(xj.z, sz * d.L[2]), xi.z);
-      const double d2 = __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)),
-                                  __dmul_rn(dz, dz));
-      dist = __dsqrt_rn(d2);
-      tj = d.ts[j];
-      const Sbp &sj = F.sbp[tj];
-      if (ihb && dist <= C.hbond_cut && sj.p_hbond == 2) ish = true;
-      if (dist <= C.bond_cut) {
-        const Tbp &tw = F.tbp[ti][tj];
-        double C12 = 0, C34 = 0, C56 = 0;
-        if (si.r_s > 0.0 && sj.r_s > 0.0) {
-          C12 = tw.p_bo1 * pow(dist / tw.r_s, tw.p_bo2);
-          BOs = (1.0 + C.bo_cut) * exp(C12);
-        }
-        if (si.r_pi > 0.0 && sj.r_pi > 0.0) {
-          C34 = tw.p_bo3 * pow(dist / tw.r_p, tw.p_bo4);
-          BOpi = exp(C34);
-        }
-        if (si.r_pi_pi > 0.0 && sj.r_pi_pi > 0.0) {
-          C56 = tw.p_bo5 * pow(dist / tw.r_pp, tw.p_bo6);
-          BOpi2 = exp(C56);
-        }
-        BO = BOs + BOpi + BOpi2;
-        if (BO >= C.bo_cut) {
-          isb = true;
-          const double r2 = dist * dist;
-          Cs = tw.p_bo2 * C12 / r2;
-          Cpi = tw.p_bo4 * C34 / r2;
-          Cpi2 = tw.p_bo6 * C56 / r2;
+  for (int base = 0; base < nn + 32; base += 32) {
+    if (base < nn) {
+      const int p = base + lane;
+      bool ish = false, cand = false;
+      uint32_t e = 0;
+      double dist = 0, dx = 0, dy = 0, dz = 0;
+      if (p < nn) {
+        e = d.nbr[row + p];
+        const int j = (int)(e >> 8);
+        int sx, sy, sz;
+        img_unpack((int)(e & 255u), &sx, &sy, &sz);
+        const float4 xjf = d.xf[j];
+        const float fx = xjf.x + (float)(sx * d.L[0]) - xif.x;
+        const float fy = xjf.y + (float)(sy * d.L[1]) - xif.y;
+        const float fz = xjf.z + (float)(sz * d.L[2]) - xif.z;
+        if (fx * fx + fy * fy + fz * fz <= rpre2) {
+          const double4 xj = d.xs[j];
+          dx = __dsub_rn(__dadd_rn(xj.x, sx * d.L[0]), xi.x);
+          dy = __dsub_rn(__dadd_rn(xj.y, sy * d.L[1]), xi.y);
+          dz = __dsub_rn(__dadd_rn(xj.z, sz * d.L[2]), xi.z);
+          const double d2 = __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
+          dist = __dsqrt_rn(d2);
+          const int tj = __float_as_int(xjf.w);
+          const Sbp &sj = F.sbp[tj];
+          if (ihb && dist <= C.hbond_cut && sj.p_hbond == 2) ish = true;
+          if (dist <= C.bond_cut) {
+            const Tbp &tw = F.tbp[ti][tj];
+            const float df = (float)dist;
+            float est = 0.f;
+            if (si.r_s > 0.0 && sj.r_s > 0.0)
+              est += (float)(1.0 + C.bo_cut) * expf((float)tw.p_bo1 * powf(df / (float)tw.r_s, (float)tw.p_bo2));
+            if (si.r_pi > 0.0 && sj.r_pi > 0.0)
+              est += expf((float)tw.p_bo3 * powf(df / (float)tw.r_p, (float)tw.p_bo4));
+            if (si.r_pi_pi > 0.0 && sj.r_pi_pi > 0.0)
+              est += expf((float)tw.p_bo5 * powf(df / (float)tw.r_pp, (float)tw.p_bo6));
+            cand = est >= bo_half;
+          }
         }
       }
-    }
-    const unsigned mb = __ballot_sync(FULL, isb);
-    const unsigned mh = __ballot_sync(FULL, ish);
-    if (isb) {
-      const int k = nb + __popc(mb & lanemask_lt());
-      const double g = -(BOs * Cs + BOpi * Cpi + BOpi2 * Cpi2);
-      const double gx = g * dx, gy = g * dy, gz = g * dz;
-      ddx += gx; ddy += gy; ddz += gz;
-      const double BOc = BO - C.bo_cut;
-      bsum += BOc;
-      if (k < d.bond_cap) {
-        const long long s = (long long)k * n + i;
-        const long long S3 = (long long)d.bond_cap * n;
-        d.b_nbr[s] = e;
-        d.b_d[s] = dist;
-        d.b_dx[s] = dx; d.b_dy[s] = dy; d.b_dz[s] = dz;
-        d.b_BO[s] = BOc;
-        d.b_BOs[s] = BOs - C.bo_cut;
-        d.b_BOpi[s] = BOpi;
-        d.b_BOpi2[s] = BOpi2;
-        d.b_dBOp[s] = gx; d.b_dBOp[S3 + s] = gy; d.b_dBOp[2 * S3 + s] = gz;
-        const double api = -BOpi * Cpi, api2 = -BOpi2 * Cpi2;
-        d.b_dlnpi[s] = api * dx; d.b_dlnpi[S3 + s] = api * dy; d.b_dlnpi[2 * S3 + s] = api * dz;
-        d.b_dlnpi2[s] = api2 * dx; d.b_dlnpi2[S3 + s] = api2 * dy; d.b_dlnpi2[2 * S3 + s] = api2 * dz;
-        d.b_Cdbo[s] = 0.0; d.b_Cdbopi[s] = 0.0; d.b_Cdbopi2[s] = 0.0;
+      const unsigned mh = __ballot_sync(FULL, ish);
+      if (ish) {
+        const int k = nh + __popc(mh & lanemask_lt());
+        if (k < d.hb_cap) d.hb_nbr[(long long)i * d.hb_cap + k] = e;
       }
+      nh += __popc(mh);
+      const unsigned mc = __ballot_sync(FULL, cand);
+      if (cand) {
+        const int q = qn + __popc(mc & lanemask_lt());
+        Q.e[q] = e; Q.dist[q] = dist; Q.dx[q] = dx; Q.dy[q] = dy; Q.dz[q] = dz;
+      }
+      qn += __popc(mc);
+      __syncwarp();
     }
-    if (ish) {
-      const int k = nh + __popc(mh & lanemask_lt());
-      if (k < d.hb_cap) d.hb_nbr[(long long)i * d.hb_cap + k] = e;
+    while (qn >= 32 || (base >= nn && qn > 0)) {
+      const int cnt = min(qn, 32);
+      bond_flush(d, C, F, Q, cnt, lane, i, ti, nb, ddx, ddy, ddz, bsum);
+      __syncwarp();
+      const int left = qn - cnt;
+      uint32_t le = 0;
+      double l0 = 0, l1 = 0, l2 = 0, l3 = 0;
+      if (lane < left) {
+        le = Q.e[cnt + lane]; l0 = Q.dist[cnt + lane];
+        l1 = Q.dx[cnt + lane]; l2 = Q.dy[cnt + lane]; l3 = Q.dz[cnt + lane];
+      }
+      __syncwarp();
+      if (lane < left) {
+        Q.e[lane] = le; Q.dist[lane] = l0; Q.dx[lane] = l1; Q.dy[lane] = l2; Q.dz[lane] = l3;
+      }
+      qn = left;
+      __syncwarp();
     }
-    nb += __popc(mb);
-    nh += __popc(mh);
   }
   // warp sums in lane order (deterministic)
   for (int off = 16; off > 0; off >>= 1) {
@@ -438,13 +575,14 @@ void launch_bin_sort(const Dev &d, cudaStream_t st) {
 }
 
 void launch_build_nbrs(const Dev &d, cudaStream_t st) {
+  const int B = NB_WARPS * 32;
   const long long threads = (long long)d.n * 32;
-  k_build_nbrs<<<(unsigned)((threads + 255) / 256), 256, 0, st>>>(d);
+  k_build_nbrs<<<(unsigned)((threads + B - 1) / B), B, 0, st>>>(d);
 }
 
 void launch_build_bonds(const Dev &d, cudaStream_t st) {
   const long long threads = (long long)d.n * 32;
-  k_build_bonds<<<(unsigned)((threads + 255) / 256), 256, 0, st>>>(d);
+  k_build_bonds<<<(unsigned)((threads + NB_WARPS * 32 - 1) / (NB_WARPS * 32)), NB_WARPS * 32, 0, st>>>(d);
   const long long slots = (long long)d.n * d.bond_cap;
   k_bond_sym<<<(unsigned)((slots + 255) / 256), 256, 0, st>>>(d);
 }

@@ -35,108 +35,160 @@ __device__ __forceinline__ void block_add(double v, double *dst) {
   }
 }
 
-// one warp per atom i, lanes over i's pair-list row; a pair (i,j,image) is
-// taken when j > i, or j == i with the "positive" image
-__global__ void __launch_bounds__(256) k_nonbonded(Dev d, int eflag) {
+constexpr int NBW = 8;     // warps per block
+constexpr int QC = 64;     // queue slots per warp
+
+__device__ __forceinline__ unsigned lanemask_lt() {
+  unsigned m;
+  asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+  return m;
+}
+
+struct PairQueue {
+  uint32_t e[QC];
+};
+
+// vdW + Coulomb of up to 32 queued pairs (one per lane); returns dE/dr / r
+// and the displacement in (c, dx, dy, dz), zero for idle lanes
+__device__ __forceinline__ void pair_terms(const Dev &d, const ForceField &F, const Control &C,
+                                          uint32_t e, bool act, const double4 &xi, int ti,
+                                          double &evdw, double &eele, double &c, double &dx,
+                                          double &dy, double &dz, int &j) {
+  c = 0.0; dx = dy = dz = 0.0;
+  j = (int)(e >> 8);
+  if (!act) return;
+  int sx, sy, sz;
+  img_unpack((int)(e & 255u), &sx, &sy, &sz);
+  const double4 xj = d.xs[j];
+  // same rounding as the pair-list membership test
+  dx = __dsub_rn(__dadd_rn(xj.x, sx * d.L[0]), xi.x);
+  dy = __dsub_rn(__dadd_rn(xj.y, sy * d.L[1]), xi.y);
+  dz = __dsub_rn(__dadd_rn(xj.z, sz * d.L[2]), xi.z);
+  const double d2 = __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
+  if (d2 > C.nonb_cut2) { dx = dy = dz = 0.0; return; }
+  const double rinv = rsqrt(d2);
+  const double r = d2 * rinv;
+  const Tbp &tw = F.tbp[ti][d.ts[j]];
+  const double *Tap = C.Tap;
+  double Tp = fma(Tap[7], r, Tap[6]);
+  Tp = fma(Tp, r, Tap[5]);
+  Tp = fma(Tp, r, Tap[4]);
+  Tp = fma(Tp, r, Tap[3]);
+  Tp = fma(Tp, r, Tap[2]);
+  Tp = fma(Tp, r, Tap[1]);
+  Tp = fma(Tp, r, Tap[0]);
+  double dTap = fma(7 * Tap[7], r, 6 * Tap[6]);
+  dTap = fma(dTap, r, 5 * Tap[5]);
+  dTap = fma(dTap, r, 4 * Tap[4]);
+  dTap = fma(dTap, r, 3 * Tap[3]);
+  dTap = fma(dTap, r, 2 * Tap[2]);
+  dTap = fma(Tap[1], rinv, dTap);
+  const double p_vdW1 = F.gp[28];
+  const int vdw_type = F.vdw_type;
+  const double ar = tw.alpha / tw.r_vdW;
+  double e_vdW, CEvd, e_core = 0.0, e_lg = 0.0;
+  if (vdw_type == 1 || vdw_type == 3) {
+    // shielded Morse: fn13 = (r^p + gamma_w^-p)^(1/p)
+    const double powr = exp(p_vdW1 * log(r));                 // r^p
+    const double S = powr + tw.powgi_vdW1;
+    const double fn13 = exp(log(S) / p_vdW1);                 // S^(1/p)
+    const double exp2 = exp(0.5 * tw.alpha * (1.0 - fn13 / tw.r_vdW));
+    const double exp1 = exp2 * exp2;
+    e_vdW = tw.D * (exp1 - 2.0 * exp2);
+    const double dfn13 = (fn13 / S) * (powr / d2);            // S^(1/p-1) r^(p-2)
+    CEvd = dTap * e_vdW - Tp * tw.D * ar * (exp1 - exp2) * dfn13;
+  } else {
+    const double exp2 = exp(0.5 * tw.alpha * (1.0 - r / tw.r_vdW));
+    const double exp1 = exp2 * exp2;
+    e_vdW = tw.D * (exp1 - 2.0 * exp2);
+    CEvd = dTap * e_vdW - Tp * tw.D * ar * (exp1 - exp2) * rinv;
+  }
+  if (vdw_type == 2 || vdw_type == 3) {
+    e_core = tw.ecore * exp(tw.acore * (1.0 - (r / tw.rcore)));
+    const double de_core = -(tw.acore / tw.rcore) * e_core;
+    CEvd += dTap * e_core + Tp * de_core * rinv;
+    if (C.lgflag) {
+      const double r5 = d2 * d2 * r, r6 = d2 * d2 * d2;
+      const double lg2 = tw.lgre * tw.lgre;
+      const double re6 = lg2 * lg2 * lg2;
+      e_lg = -(tw.lgcij / (r6 + re6));
+      const double de_lg = -6.0 * e_lg * r5 / (r6 + re6);
+      CEvd += dTap * e_lg + Tp * de_lg * rinv;
+    }
+  }
+  // shielded Coulomb: Tap qi qj / (r^3 + gamma)^c
+  const double dr3gamij_1 = fma(d2, r, tw.gamma);
+  const double inv3 = rpow_third(dr3gamij_1, RG_C3_ELE);
+  const double qq = C_ele * xi.w * xj.w;
+  const double e_ele = qq * Tp * inv3;
+  const double CEclmb = qq * (dTap - Tp * r / dr3gamij_1) * inv3;
+  evdw += Tp * (e_vdW + e_core + e_lg);
+  eele += e_ele;
+  c = CEvd + CEclmb;
+}
+
+// one warp per atom i; the pairs (i,j,image) with j > i, or j == i with the
+// "positive" image, are queued and evaluated 32 at a time
+__global__ void __launch_bounds__(NBW * 32) k_nonbonded(Dev d, int eflag) {
+  __shared__ PairQueue queues[NBW];
   const int lane = threadIdx.x & 31;
   const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   double evdw = 0.0, eele = 0.0;
   if (i < d.n) {
+    PairQueue &Q = queues[threadIdx.x >> 5];
     const ForceField &F = *d.ff;
     const Control &C = *d.ctl;
     const int n = d.n;
     const double4 xi = d.xs[i];
     const int ti = d.ts[i];
-    const double p_vdW1 = F.gp[28], p_vdW1i = 1.0 / p_vdW1;
-    const double *Tap = C.Tap;
-    const int vdw_type = F.vdw_type;
     const long long row = (long long)i * d.nb_cap;
     const int nn = d.n_near[i], nf = d.n_far[i];
     const int cap = d.nb_cap;
     const int tot = min(nn + nf, cap);
     double fx = 0, fy = 0, fz = 0;
     double *fC = d.fC;
-    for (int p = lane; p < tot; p += 32) {
-      // front segment [0,nn) then back segment [cap-nf, cap)
-      const int slot = p < nn ? p : cap - 1 - (p - nn);
-      const uint32_t e = d.nbr[row + slot];
-      const int j = (int)(e >> 8);
-      const int img = (int)(e & 255u);
-      if (j < i || (j == i && img <= IMG0)) continue;
-      int sx, sy, sz;
-      img_unpack(img, &sx, &sy, &sz);
-      const double4 xj = d.xs[j];
-      // same rounding as the pair-list membership test
-      const double dx = __dsub_rn(__dadd_rn(xj.x, sx * d.L[0]), xi.x);
-      const double dy = __dsub_rn(__dadd_rn(xj.y, sy * d.L[1]), xi.y);
-      const double dz = __dsub_rn(__dadd_rn(xj.z, sz * d.L[2]), xi.z);
-      const double d2 = __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
-      if (d2 > C.nonb_cut2) continue;
-      const double r = sqrt(d2);
-      const int tj = d.ts[j];
-      const Tbp &tw = F.tbp[ti][tj];
-      double Tp = fma(Tap[7], r, Tap[6]);
-      Tp = fma(Tp, r, Tap[5]);
-      Tp = fma(Tp, r, Tap[4]);
-      Tp = fma(Tp, r, Tap[3]);
-      Tp = fma(Tp, r, Tap[2]);
-      Tp = fma(Tp, r, Tap[1]);
-      Tp = fma(Tp, r, Tap[0]);
-      double dTap = fma(7 * Tap[7], r, 6 * Tap[6]);
-      dTap = fma(dTap, r, 5 * Tap[5]);
-      dTap = fma(dTap, r, 4 * Tap[4]);
-      dTap = fma(dTap, r, 3 * Tap[3]);
-      dTap = fma(dTap, r, 2 * Tap[2]);
-      dTap += Tap[1] / r;
-      double e_vdW, CEvd, e_core = 0.0, e_lg = 0.0;
-      if (vdw_type == 1 || vdw_type == 3) {
-        // shielded Morse: fn13 = (r^p + gamma_w^-p)^(1/p)
-        const double lr = log(r);
-        const double powr = exp(p_vdW1 * lr);                  // r^p
-        const double S = powr + tw.powgi_vdW1;
-        const double fn13 = exp(p_vdW1i * log(S));             // S^(1/p)
-        const double x = tw.alpha * (1.0 - fn13 / tw.r_vdW);
-        const double exp2 = exp(0.5 * x);
-        const double exp1 = exp2 * exp2;
-        e_vdW = tw.D * (exp1 - 2.0 * exp2);
-        // dfn13 = S^(1/p - 1) * r^(p - 2)
-        const double dfn13 = (fn13 / S) * (powr / d2);
-        CEvd = dTap * e_vdW - Tp * tw.D * (tw.alpha / tw.r_vdW) * (exp1 - exp2) * dfn13;
-      } else {
-        const double x = tw.alpha * (1.0 - r / tw.r_vdW);
-        const double exp2 = exp(0.5 * x);
-        const double exp1 = exp2 * exp2;
-        e_vdW = tw.D * (exp1 - 2.0 * exp2);
-        CEvd = dTap * e_vdW - Tp * tw.D * (tw.alpha / tw.r_vdW) * (exp1 - exp2) / r;
-      }
-      if (vdw_type == 2 || vdw_type == 3) {
-        e_core = tw.ecore * exp(tw.acore * (1.0 - (r / tw.rcore)));
-        const double de_core = -(tw.acore / tw.rcore) * e_core;
-        CEvd += dTap * e_core + Tp * de_core / r;
-        if (C.lgflag) {
-          const double r5 = d2 * d2 * r, r6 = d2 * d2 * d2;
-          const double lg2 = tw.lgre * tw.lgre;
-          const double re6 = lg2 * lg2 * lg2;
-          e_lg = -(tw.lgcij / (r6 + re6));
-          const double de_lg = -6.0 * e_lg * r5 / (r6 + re6);
-          CEvd += dTap * e_lg + Tp * de_lg / r;
+    int qn = 0;
+    for (int base = 0; base < tot + 32; base += 32) {
+      if (base < tot) {
+        const int p = base + lane;
+        bool take = false;
+        uint32_t e = 0;
+        if (p < tot) {
+          const int slot = p < nn ? p : cap - 1 - (p - nn);
+          e = d.nbr[row + slot];
+          const int j = (int)(e >> 8);
+          take = j > i || (j == i && (int)(e & 255u) > IMG0);
         }
+        const unsigned m = __ballot_sync(FULL, take);
+        if (take) Q.e[qn + __popc(m & lanemask_lt())] = e;
+        qn += __popc(m);
+        __syncwarp();
       }
-      // shielded Coulomb: Tap * qi qj / (r^3 + gamma)^(1/3)
-      const double dr3gamij_1 = r * r * r + tw.gamma;
-      const double dr3gamij_3 = pow_third(dr3gamij_1, RG_C3_ELE);
-      const double qq = C_ele * xi.w * xj.w;
-      const double e_ele = qq * Tp / dr3gamij_3;
-      const double CEclmb = qq * (dTap - Tp * r / dr3gamij_1) / dr3gamij_3;
-      evdw += Tp * (e_vdW + e_core + e_lg);
-      eele += e_ele;
-      const double c = CEvd + CEclmb;   // dE/dr / r
-      fx -= c * dx;
-      fy -= c * dy;
-      fz -= c * dz;
-      atomicAdd(&fC[j], c * dx);
-      atomicAdd(&fC[n + j], c * dy);
-      atomicAdd(&fC[2 * n + j], c * dz);
+      // evaluate a full batch, or the remainder after the last entry
+      while (qn >= 32 || (base >= tot && qn > 0)) {
+        const int cnt = min(qn, 32);
+        const bool act = lane < cnt;
+        const uint32_t e = act ? Q.e[lane] : 0u;
+        double c, dx, dy, dz;
+        int j;
+        pair_terms(d, F, C, e, act, xi, ti, evdw, eele, c, dx, dy, dz, j);
+        if (act && c != 0.0) {
+          fx -= c * dx;
+          fy -= c * dy;
+          fz -= c * dz;
+          atomicAdd(&fC[j], c * dx);
+          atomicAdd(&fC[n + j], c * dy);
+          atomicAdd(&fC[2 * n + j], c * dz);
+        }
+        __syncwarp();
+        const int left = qn - cnt;
+        uint32_t le = 0;
+        if (lane < left) le = Q.e[cnt + lane];
+        __syncwarp();
+        if (lane < left) Q.e[lane] = le;
+        qn = left;
+        __syncwarp();
+      }
     }
     fx = warp_sum(fx);
     fy = warp_sum(fy);
@@ -159,5 +211,5 @@ __global__ void __launch_bounds__(256) k_nonbonded(Dev d, int eflag) {
 
 void launch_nonbonded(const Dev &d, cudaStream_t st, int eflag) {
   const long long threads = (long long)d.n * 32;
-  k_nonbonded<<<(unsigned)((threads + 255) / 256), 256, 0, st>>>(d, eflag);
+  k_nonbonded<<<(unsigned)((threads + NBW * 32 - 1) / (NBW * 32)), NBW * 32, 0, st>>>(d, eflag);
 }

@@ -162,9 +162,15 @@ enum { OVF_NBR = 1, OVF_BOND = 2, OVF_HB = 4, OVF_CELL = 8 };
 // factor is 1 + (c - 1/3) ln x to far below an ulp (ln x in FP32 suffices).
 #define RG_C3_QEQ (0.3333333333333 - 1.0 / 3.0)
 #define RG_C3_ELE (0.33333333333333 - 1.0 / 3.0)
+#ifdef __CUDACC__
 __device__ __forceinline__ double pow_third(double x, double dc) {
   return cbrt(x) * (1.0 + dc * (double)__logf((float)x));
 }
+// 1 / x^c for the same exponents
+__device__ __forceinline__ double rpow_third(double x, double dc) {
+  return rcbrt(x) * (1.0 - dc * (double)__logf((float)x));
+}
+#endif
 
 // image code of a neighbour entry: sx,sy,sz in [-2,2]
 __host__ __device__ inline int img_pack(int sx, int sy, int sz) {

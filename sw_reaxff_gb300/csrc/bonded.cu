@@ -782,6 +782,389 @@ __global__ void __launch_bounds__(128) k_valence_torsion(Dev d, int eflag) {
 }
 
 // ------------------------------------------------------------------
+// valence angles and torsions as work lists: every angle (centre j, bonds
+// pk < ph) and every torsion (centre bond j-k counted at one end, bonds ph
+// of j and pw of k) that passes the reference's bond-order tests becomes
+// one item, so each thread evaluates one term with uniform work.  Torsions
+// whose four parameters V1, V2, V3 and p_cot1 are all zero contribute
+// exactly zero and are not listed.
+
+// per centre: SBO2, CSBO2, dSBO1, dSBO2, expval6
+__global__ void k_vt_prep_center(Dev d) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  const int n = d.n;
+  if (j >= n) return;
+  const ForceField &F = *d.ff;
+  const double p_val6 = F.gp[14], p_val8 = F.gp[33], p_val9 = F.gp[16];
+  const int nbj = min(d.nbonds[j], d.bond_cap);
+  double SBOp = 0, prod_SBO = 1;
+  for (int q = 0; q < nbj; ++q) {
+    const long long sq = (long long)q * n + j;
+    SBOp += d.b_BOpi[sq] + d.b_BOpi2[sq];
+    double tmp = sqr(d.b_BO[sq]);
+    tmp *= tmp;
+    tmp *= tmp;
+    prod_SBO *= exp(-tmp);
+  }
+  const double Delta_j = d.Delta_boc[j];
+  double vlpadj, dSBO2;
+  if (d.vlpex[j] >= 0) {
+    vlpadj = 0;
+    dSBO2 = prod_SBO - 1;
+  } else {
+    vlpadj = d.nlp[j];
+    dSBO2 = (prod_SBO - 1) * (1 - p_val8 * d.dDelta_lp[j]);
+  }
+  const double SBO = SBOp + (1 - prod_SBO) * (-Delta_j - p_val8 * vlpadj);
+  const double dSBO1 = -8 * prod_SBO * (Delta_j + p_val8 * vlpadj);
+  double SBO2, CSBO2;
+  if (SBO <= 0) SBO2 = 0, CSBO2 = 0;
+  else if (SBO > 0 && SBO <= 1) {
+    SBO2 = pow(SBO, p_val9);
+    CSBO2 = p_val9 * pow(SBO, p_val9 - 1);
+  } else if (SBO > 1 && SBO < 2) {
+    SBO2 = 2 - pow(2 - SBO, p_val9);
+    CSBO2 = p_val9 * pow(2 - SBO, p_val9 - 1);
+  } else SBO2 = 2, CSBO2 = 0;
+  d.c_sbo[j] = SBO2;
+  d.c_sbo[n + j] = CSBO2;
+  d.c_sbo[2 * n + j] = dSBO1;
+  d.c_sbo[3 * n + j] = dSBO2;
+  d.c_sbo[4 * n + j] = exp(p_val6 * Delta_j);
+}
+
+// per bond slot: exp(-p_tor2 BOA), exp(-p_cot2 (BOA - 1.5)^2)
+__global__ void k_vt_prep_bond(Dev d) {
+  const int n = d.n;
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = (int)(t % n), k = (int)(t / n);
+  if (k >= d.bond_cap || i >= n || k >= d.nbonds[i]) return;
+  const long long s = (long long)k * n + i;
+  const double BOA = d.b_BO[s] - d.ctl->thb_cut;
+  d.b_et2[s] = exp(-d.ff->gp[23] * BOA);
+  d.b_ec2[s] = exp(-d.ff->gp[27] * sqr(BOA - 1.5));
+}
+
+__device__ __forceinline__ bool fbp_nonzero(const Fbp &p) {
+  return p.V1 != 0.0 || p.V2 != 0.0 || p.V3 != 0.0 || p.p_cot1 != 0.0;
+}
+
+// enumerate the items of slot (j, kk); FILL writes them at the offsets
+template <bool FILL>
+__device__ void vt_enumerate(const Dev &d, int j, int kk, int &cv, int &ct, long long ov,
+                             long long ot) {
+  const int n = d.n;
+  const ForceField &F = *d.ff;
+  const double thb_cut = d.ctl->thb_cut, thb_cutsq = d.ctl->thb_cutsq;
+  cv = ct = 0;
+  const int nbj = min(d.nbonds[j], d.bond_cap);
+  if (kk >= nbj) return;
+  const long long spk = (long long)kk * n + j;
+  const double BO_jk = d.b_BO[spk];
+  if (!(BO_jk - thb_cut > 0.0) || d.b_sym[spk] < 0) return;
+  const uint32_t ejk = d.b_nbr[spk];
+  const int k = nbr_of(ejk), tj = d.ts[j], tk = d.ts[k];
+  const long long spj = d.b_sym[spk];
+  const int nbk = min(d.nbonds[k], d.bond_cap);
+  const bool do_tor = tag_first(d, j, k, ejk);
+  int sjk[3];
+  img_unpack((int)(ejk & 255u), &sjk[0], &sjk[1], &sjk[2]);
+  for (int ph = 0; ph < nbj; ++ph) {
+    if (ph == kk) continue;
+    const long long sph = (long long)ph * n + j;
+    const double BO_hj = d.b_BO[sph];
+    const uint32_t ehj = d.b_nbr[sph];
+    const int h = nbr_of(ehj), th = d.ts[h];
+    if (ph > kk && BO_jk > thb_cut && BO_hj > thb_cut && BO_jk * BO_hj > thb_cutsq) {
+      const Thbh &thbh = F.thbp[tk][tj][th];
+      bool any = false;
+      for (int c = 0; c < thbh.cnt; ++c) any |= fabs(thbh.prm[c].p_val1) > 0.001;
+      if (any) {
+        if (FILL)
+          d.w_val[ov + cv] = ((unsigned long long)j << 16) | ((unsigned long long)kk << 8) | ph;
+        ++cv;
+      }
+    }
+    if (!do_tor || !(BO_hj > thb_cut)) continue;
+    int shj[3];
+    img_unpack((int)(ehj & 255u), &shj[0], &shj[1], &shj[2]);
+    for (int pw = 0; pw < nbk; ++pw) {
+      const long long spw = (long long)pw * n + k;
+      if (spw == spj) continue;
+      const double BO_kl = d.b_BO[spw];
+      if (!(BO_kl > thb_cut) || !(BO_hj * BO_jk * BO_kl > thb_cut)) continue;
+      const uint32_t ekl = d.b_nbr[spw];
+      const int l = nbr_of(ekl);
+      const Fbh &fbh = F.fbp[th][tj][tk][d.ts[l]];
+      if (!fbh.cnt || !fbp_nonzero(fbh.prm)) continue;
+      int skl[3];
+      img_unpack((int)(ekl & 255u), &skl[0], &skl[1], &skl[2]);
+      if (l == h && sjk[0] + skl[0] == shj[0] && sjk[1] + skl[1] == shj[1] &&
+          sjk[2] + skl[2] == shj[2])
+        continue;   // i and l are the same atom instance
+      if (FILL)
+        d.w_tor[ot + ct] = ((unsigned long long)j << 24) | ((unsigned long long)kk << 16) |
+                           ((unsigned long long)ph << 8) | pw;
+      ++ct;
+    }
+  }
+}
+
+__global__ void k_vt_count(Dev d) {
+  const int n = d.n;
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long slots = (long long)d.bond_cap * n;
+  if (t > slots) return;
+  if (t == slots) {   // trailing zero for the exclusive scans
+    d.w_cnt_v[t] = 0;
+    d.w_cnt_t[t] = 0;
+    return;
+  }
+  int cv, ct;
+  vt_enumerate<false>(d, (int)(t % n), (int)(t / n), cv, ct, 0, 0);
+  d.w_cnt_v[t] = cv;
+  d.w_cnt_t[t] = ct;
+}
+
+__global__ void k_vt_fill(Dev d) {
+  const int n = d.n;
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (long long)d.bond_cap * n) return;
+  if (d.w_cnt_v[t] == 0 && d.w_cnt_t[t] == 0) return;
+  int cv, ct;
+  vt_enumerate<true>(d, (int)(t % n), (int)(t / n), cv, ct, d.w_off_v[t], d.w_off_t[t]);
+}
+
+// one valence angle h-j-k (with its penalty and coalition terms)
+__global__ void __launch_bounds__(128) k_valence(Dev d, int eflag, long long nitems) {
+  const long long w = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  double e_ang = 0, e_pen = 0, e_coa = 0;
+  if (w < nitems) {
+    const unsigned long long it = d.w_val[w];
+    const int j = (int)(it >> 16), kk = (int)((it >> 8) & 255), ph = (int)(it & 255);
+    const int n = d.n;
+    const ForceField &F = *d.ff;
+    const double thb_cut = d.ctl->thb_cut;
+    const double p_val6 = F.gp[14], p_val10 = F.gp[17];
+    const double p_pen2 = F.gp[19], p_pen3 = F.gp[20], p_pen4 = F.gp[21];
+    const double p_coa2 = F.gp[2], p_coa3 = F.gp[38], p_coa4 = F.gp[30];
+    double *fC = d.fC;
+    double *CdD = d.fC + 3 * (long long)n;
+    const int tj = d.ts[j];
+    const double p_val3 = F.sbp[tj].p_val3, p_val5 = F.sbp[tj].p_val5;
+    const double SBO2 = d.c_sbo[j], CSBO2 = d.c_sbo[n + j];
+    const double dSBO1 = d.c_sbo[2 * n + j], dSBO2 = d.c_sbo[3 * n + j];
+    const double expval6 = d.c_sbo[4 * n + j];
+    const double Delta_j = d.Delta_boc[j];
+    const long long spk = (long long)kk * n + j, sph = (long long)ph * n + j;
+    const int k = nbr_of(d.b_nbr[spk]), h = nbr_of(d.b_nbr[sph]);
+    const int tk = d.ts[k], th = d.ts[h];
+    const double BOA_jk = d.b_BO[spk] - thb_cut, BOA_hj = d.b_BO[sph] - thb_cut;
+    const double djk[3] = {d.b_dx[spk], d.b_dy[spk], d.b_dz[spk]};
+    const double dhj[3] = {d.b_dx[sph], d.b_dy[sph], d.b_dz[sph]};
+    double theta_hjk, cos_theta_hjk, di[3], dj[3], dk[3];
+    theta_dcos(djk, d.b_d[spk], dhj, d.b_d[sph], theta_hjk, cos_theta_hjk, di, dj, dk);
+    double sin_theta_hjk = sin(theta_hjk);
+    if (sin_theta_hjk < 1.0e-5) sin_theta_hjk = 1.0e-5;
+    const Thbh &thbh = F.thbp[tk][tj][th];
+    const int nbj = min(d.nbonds[j], d.bond_cap);
+    for (int cnt = 0; cnt < thbh.cnt; ++cnt) {
+      const Thbp &tp = thbh.prm[cnt];
+      if (!(fabs(tp.p_val1) > 0.001)) continue;
+      const double p_val1 = tp.p_val1, p_val2 = tp.p_val2, p_val4 = tp.p_val4, p_val7 = tp.p_val7;
+      const double theta_00 = tp.theta_00;
+      const double exp3jk = exp(-p_val3 * pow(BOA_jk, p_val4));
+      const double f7_jk = 1.0 - exp3jk;
+      const double Cf7jk = p_val3 * p_val4 * pow(BOA_jk, p_val4 - 1.0) * exp3jk;
+      const double exp3hj = exp(-p_val3 * pow(BOA_hj, p_val4));
+      const double f7_hj = 1.0 - exp3hj;
+      const double Cf7hj = p_val3 * p_val4 * pow(BOA_hj, p_val4 - 1.0) * exp3hj;
+      const double expval7 = exp(-p_val7 * Delta_j);
+      const double trm8 = 1.0 + expval6 + expval7;
+      const double f8_Dj = p_val5 - ((p_val5 - 1.0) * (2.0 + expval6) / trm8);
+      const double Cf8j = ((1.0 - p_val5) / sqr(trm8)) *
+                          (p_val6 * expval6 * trm8 - (2.0 + expval6) * (p_val6 * expval6 - p_val7 * expval7));
+      double theta_0 = 180.0 - theta_00 * (1.0 - exp(-p_val10 * (2.0 - SBO2)));
+      theta_0 = deg2rad(theta_0);
+      const double expval2theta = exp(-p_val2 * sqr(theta_0 - theta_hjk));
+      const double expval12theta = (p_val1 >= 0) ? p_val1 * (1.0 - expval2theta) : p_val1 * -expval2theta;
+      const double CEval1 = Cf7jk * f7_hj * f8_Dj * expval12theta;
+      const double CEval2 = Cf7hj * f7_jk * f8_Dj * expval12theta;
+      const double CEval3 = Cf8j * f7_hj * f7_jk * expval12theta;
+      const double CEval4 = -2.0 * p_val1 * p_val2 * f7_jk * f7_hj * f8_Dj * expval2theta * (theta_0 - theta_hjk);
+      const double Ctheta_0 = p_val10 * deg2rad(theta_00) * exp(-p_val10 * (2.0 - SBO2));
+      const double CEval5 = -CEval4 * Ctheta_0 * CSBO2;
+      const double CEval6 = CEval5 * dSBO1;
+      const double CEval7 = CEval5 * dSBO2;
+      const double CEval8 = -CEval4 / sin_theta_hjk;
+      e_ang += f7_jk * f7_hj * f8_Dj * expval12theta;
+      const double exp_pen2jk = exp(-p_pen2 * sqr(BOA_jk - 2.0));
+      const double exp_pen2hj = exp(-p_pen2 * sqr(BOA_hj - 2.0));
+      const double exp_pen3 = exp(-p_pen3 * d.Delta[j]);
+      const double exp_pen4 = exp(p_pen4 * d.Delta[j]);
+      const double trm_pen34 = 1.0 + exp_pen3 + exp_pen4;
+      const double f9_Dj = (2.0 + exp_pen3) / trm_pen34;
+      const double Cf9j = (-p_pen3 * exp_pen3 * trm_pen34 -
+                           (2.0 + exp_pen3) * (-p_pen3 * exp_pen3 + p_pen4 * exp_pen4)) / sqr(trm_pen34);
+      const double epen = tp.p_pen1 * f9_Dj * exp_pen2jk * exp_pen2hj;
+      e_pen += epen;
+      const double CEpen1 = epen * Cf9j / f9_Dj;
+      const double temp = -2.0 * p_pen2 * epen;
+      const double CEpen2 = temp * (BOA_jk - 2.0);
+      const double CEpen3 = temp * (BOA_hj - 2.0);
+      const double exp_coa2 = exp(p_coa2 * d.Delta_val[j]);
+      const double bo0k = d.bo0[k], bo0h = d.bo0[h];
+      const double ecoa = tp.p_coa1 / (1. + exp_coa2) * exp(-p_coa3 * sqr(bo0k - BOA_jk)) *
+                          exp(-p_coa3 * sqr(bo0h - BOA_hj)) * exp(-p_coa4 * sqr(BOA_jk - 1.5)) *
+                          exp(-p_coa4 * sqr(BOA_hj - 1.5));
+      e_coa += ecoa;
+      const double CEcoa1 = -2 * p_coa4 * (BOA_jk - 1.5) * ecoa;
+      const double CEcoa2 = -2 * p_coa4 * (BOA_hj - 1.5) * ecoa;
+      const double CEcoa3 = -p_coa2 * exp_coa2 * ecoa / (1 + exp_coa2);
+      const double CEcoa4 = -2 * p_coa3 * (bo0k - BOA_jk) * ecoa;
+      const double CEcoa5 = -2 * p_coa3 * (bo0h - BOA_hj) * ecoa;
+      atomicAdd(&d.b_Cdbo[spk], CEval1 + CEpen2 + (CEcoa1 - CEcoa4));
+      atomicAdd(&d.b_Cdbo[sph], CEval2 + CEpen3 + (CEcoa2 - CEcoa5));
+      atomicAdd(&CdD[j], (CEval3 + CEval7) + CEpen1 + CEcoa3);
+      atomicAdd(&CdD[k], CEcoa4);
+      atomicAdd(&CdD[h], CEcoa5);
+      for (int q = 0; q < nbj; ++q) {
+        const long long sq = (long long)q * n + j;
+        const double b = d.b_BO[sq];
+        const double b3 = b * b * b;
+        atomicAdd(&d.b_Cdbo[sq], CEval6 * (b3 * b3 * b));
+        atomicAdd(&d.b_Cdbopi[sq], CEval5);
+        atomicAdd(&d.b_Cdbopi2[sq], CEval5);
+      }
+      add3(fC, n, k, CEval8, di[0], di[1], di[2]);
+      add3(fC, n, j, CEval8, dj[0], dj[1], dj[2]);
+      add3(fC, n, h, CEval8, dk[0], dk[1], dk[2]);
+    }
+  }
+  if (eflag) {
+    block_add(e_ang, &d.energy[E_ANG]);
+    block_add(e_pen, &d.energy[E_PEN]);
+    block_add(e_coa, &d.energy[E_COA]);
+    block_add(e_ang + e_pen + e_coa, &d.energy[E_ENG_VDWL]);
+  }
+}
+
+// one torsion h-j-k-l (with its 4-body conjugation term)
+__global__ void __launch_bounds__(128) k_torsion(Dev d, int eflag, long long nitems) {
+  const long long w = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  double e_tor = 0, e_con = 0;
+  if (w < nitems) {
+    const unsigned long long it = d.w_tor[w];
+    const int j = (int)(it >> 24), kk = (int)((it >> 16) & 255);
+    const int ph = (int)((it >> 8) & 255), pw = (int)(it & 255);
+    const int n = d.n;
+    const ForceField &F = *d.ff;
+    const double thb_cut = d.ctl->thb_cut;
+    const double p_tor2 = F.gp[23], p_tor3 = F.gp[24], p_tor4 = F.gp[25], p_cot2 = F.gp[27];
+    double *fC = d.fC;
+    double *CdD = d.fC + 3 * (long long)n;
+    const long long spk = (long long)kk * n + j, sph = (long long)ph * n + j;
+    const int k = nbr_of(d.b_nbr[spk]), i = nbr_of(d.b_nbr[sph]);
+    const long long spj = d.b_sym[spk];
+    const long long spw = (long long)pw * n + k;
+    const int l = nbr_of(d.b_nbr[spw]);
+    const Fbp &fbp = F.fbp[d.ts[i]][d.ts[j]][d.ts[k]][d.ts[l]].prm;
+    const double BOA_jk = d.b_BO[spk] - thb_cut, BOA_ij = d.b_BO[sph] - thb_cut;
+    const double BOA_kl = d.b_BO[spw] - thb_cut;
+    const double Delta_j = d.Delta_boc[j], Delta_k = d.Delta_boc[k];
+    const double exp_tor3_DjDk = exp(-p_tor3 * (Delta_j + Delta_k));
+    const double exp_tor4_DjDk = exp(p_tor4 * (Delta_j + Delta_k));
+    const double exp_tor34_inv = 1.0 / (1.0 + exp_tor3_DjDk + exp_tor4_DjDk);
+    const double f11_DjDk = (2.0 + exp_tor3_DjDk) * exp_tor34_inv;
+    const double exp_tor2_jk = d.b_et2[spk], exp_cot2_jk = d.b_ec2[spk];
+    const double exp_tor2_ij = d.b_et2[sph], exp_cot2_ij = d.b_ec2[sph];
+    const double exp_tor2_kl = d.b_et2[spw], exp_cot2_kl = d.b_ec2[spw];
+    const double djk[3] = {d.b_dx[spk], d.b_dy[spk], d.b_dz[spk]};
+    const double dhj[3] = {d.b_dx[sph], d.b_dy[sph], d.b_dz[sph]};
+    const double dkl[3] = {d.b_dx[spw], d.b_dy[spw], d.b_dz[spw]};
+    const double dpj[3] = {d.b_dx[spj], d.b_dy[spj], d.b_dz[spj]};
+    const double r_jk = d.b_d[spk], r_ij = d.b_d[sph], r_kl = d.b_d[spw];
+    Thb p_ijk, p_jkl;
+    double cth;
+    theta_dcos(djk, r_jk, dhj, r_ij, p_ijk.theta, cth, p_ijk.di, p_ijk.dj, p_ijk.dk);
+    theta_dcos(dpj, d.b_d[spj], dkl, r_kl, p_jkl.theta, cth, p_jkl.di, p_jkl.dj, p_jkl.dk);
+    double sin_ijk, cos_ijk, tan_ijk_i, sin_jkl, cos_jkl, tan_jkl_i;
+    sincos(p_ijk.theta, &sin_ijk, &cos_ijk);
+    if (sin_ijk >= 0 && sin_ijk <= MIN_SINE) tan_ijk_i = cos_ijk / MIN_SINE;
+    else if (sin_ijk <= 0 && sin_ijk >= -MIN_SINE) tan_ijk_i = cos_ijk / -MIN_SINE;
+    else tan_ijk_i = cos_ijk / sin_ijk;
+    sincos(p_jkl.theta, &sin_jkl, &cos_jkl);
+    if (sin_jkl >= 0 && sin_jkl <= MIN_SINE) tan_jkl_i = cos_jkl / MIN_SINE;
+    else if (sin_jkl <= 0 && sin_jkl >= -MIN_SINE) tan_jkl_i = cos_jkl / -MIN_SINE;
+    else tan_jkl_i = cos_jkl / sin_jkl;
+    double dli[3];
+    dli[0] = dhj[0] - djk[0] - dkl[0];
+    dli[1] = dhj[1] - djk[1] - dkl[1];
+    dli[2] = dhj[2] - djk[2] - dkl[2];
+    const double r_li = sqrt(sqr(dli[0]) + sqr(dli[1]) + sqr(dli[2]));
+    double doi[3], doj[3], dok[3], dol[3];
+    const double omega = calc_omega(dhj, r_ij, djk, r_jk, dkl, r_kl, dli, r_li, p_ijk, p_jkl,
+                                    doi, doj, dok, dol);
+    const double cos_omega = cos(omega);
+    const double cos2omega = cos(2. * omega);
+    const double cos3omega = cos(3. * omega);
+    const double BOpi_jk = d.b_BOpi[spk];
+    const double exp_tor1 = exp(fbp.p_tor1 * sqr(2.0 - BOpi_jk - f11_DjDk));
+    const double fn10 = (1.0 - exp_tor2_ij) * (1.0 - exp_tor2_jk) * (1.0 - exp_tor2_kl);
+    const double CV = 0.5 * (fbp.V1 * (1.0 + cos_omega) + fbp.V2 * exp_tor1 * (1.0 - cos2omega) +
+                             fbp.V3 * (1.0 + cos3omega));
+    e_tor = fn10 * sin_ijk * sin_jkl * CV;
+    const double dfn11 = (-p_tor3 * exp_tor3_DjDk +
+                          (p_tor3 * exp_tor3_DjDk - p_tor4 * exp_tor4_DjDk) * (2.0 + exp_tor3_DjDk) * exp_tor34_inv) *
+                         exp_tor34_inv;
+    const double CEtors1 = sin_ijk * sin_jkl * CV;
+    const double CEtors2 = -fn10 * 2.0 * fbp.p_tor1 * fbp.V2 * exp_tor1 * (2.0 - BOpi_jk - f11_DjDk) *
+                           (1.0 - sqr(cos_omega)) * sin_ijk * sin_jkl;
+    const double CEtors3 = CEtors2 * dfn11;
+    const double CEtors4 = CEtors1 * p_tor2 * exp_tor2_ij * (1.0 - exp_tor2_jk) * (1.0 - exp_tor2_kl);
+    const double CEtors5 = CEtors1 * p_tor2 * (1.0 - exp_tor2_ij) * exp_tor2_jk * (1.0 - exp_tor2_kl);
+    const double CEtors6 = CEtors1 * p_tor2 * (1.0 - exp_tor2_ij) * (1.0 - exp_tor2_jk) * exp_tor2_kl;
+    const double cmn = -fn10 * CV;
+    const double CEtors7 = cmn * sin_jkl * tan_ijk_i;
+    const double CEtors8 = cmn * sin_ijk * tan_jkl_i;
+    const double CEtors9 = fn10 * sin_ijk * sin_jkl *
+                           (0.5 * fbp.V1 - 2.0 * fbp.V2 * exp_tor1 * cos_omega +
+                            1.5 * fbp.V3 * (cos2omega + 2.0 * sqr(cos_omega)));
+    const double fn12 = exp_cot2_ij * exp_cot2_jk * exp_cot2_kl;
+    e_con = fbp.p_cot1 * fn12 * (1.0 + (sqr(cos_omega) - 1.0) * sin_ijk * sin_jkl);
+    const double Cconj = -2.0 * fn12 * fbp.p_cot1 * p_cot2 * (1.0 + (sqr(cos_omega) - 1.0) * sin_ijk * sin_jkl);
+    const double CEconj1 = Cconj * (BOA_ij - 1.5e0);
+    const double CEconj2 = Cconj * (BOA_jk - 1.5e0);
+    const double CEconj3 = Cconj * (BOA_kl - 1.5e0);
+    const double CEconj4 = -fbp.p_cot1 * fn12 * (sqr(cos_omega) - 1.0) * sin_jkl * tan_ijk_i;
+    const double CEconj5 = -fbp.p_cot1 * fn12 * (sqr(cos_omega) - 1.0) * sin_ijk * tan_jkl_i;
+    const double CEconj6 = 2.0 * fbp.p_cot1 * fn12 * cos_omega * sin_ijk * sin_jkl;
+    atomicAdd(&d.b_Cdbopi[spk], CEtors2);
+    atomicAdd(&CdD[j], CEtors3);
+    atomicAdd(&CdD[k], CEtors3);
+    atomicAdd(&d.b_Cdbo[sph], CEtors4 + CEconj1);
+    atomicAdd(&d.b_Cdbo[spk], CEtors5 + CEconj2);
+    atomicAdd(&d.b_Cdbo[spw], CEtors6 + CEconj3);
+    const double c78 = CEtors7 + CEconj4, c85 = CEtors8 + CEconj5, c96 = CEtors9 + CEconj6;
+    add3(fC, n, i, 1.0, c78 * p_ijk.dk[0] + c96 * doi[0], c78 * p_ijk.dk[1] + c96 * doi[1],
+         c78 * p_ijk.dk[2] + c96 * doi[2]);
+    add3(fC, n, j, 1.0, c78 * p_ijk.dj[0] + c85 * p_jkl.di[0] + c96 * doj[0],
+         c78 * p_ijk.dj[1] + c85 * p_jkl.di[1] + c96 * doj[1],
+         c78 * p_ijk.dj[2] + c85 * p_jkl.di[2] + c96 * doj[2]);
+    add3(fC, n, k, 1.0, c78 * p_ijk.di[0] + c85 * p_jkl.dj[0] + c96 * dok[0],
+         c78 * p_ijk.di[1] + c85 * p_jkl.dj[1] + c96 * dok[1],
+         c78 * p_ijk.di[2] + c85 * p_jkl.dj[2] + c96 * dok[2]);
+    add3(fC, n, l, 1.0, c85 * p_jkl.dk[0] + c96 * dol[0], c85 * p_jkl.dk[1] + c96 * dol[1],
+         c85 * p_jkl.dk[2] + c96 * dol[2]);
+  }
+  if (eflag) {
+    block_add(e_tor, &d.energy[E_TOR]);
+    block_add(e_con, &d.energy[E_CON]);
+    block_add(e_tor + e_con, &d.energy[E_ENG_VDWL]);
+  }
+}
+
+// ------------------------------------------------------------------
 // bond-order derivative forces: one thread per atom i over its bonds
 
 __global__ void k_dbond(Dev d) {
@@ -863,6 +1246,24 @@ void launch_hbonds(const Dev &d, cudaStream_t st, int eflag) {
 void launch_valence_torsion(const Dev &d, cudaStream_t st, int eflag) {
   const long long slots = (long long)d.n * d.bond_cap;
   k_valence_torsion<<<(unsigned)((slots + 127) / 128), 128, 0, st>>>(d, eflag);
+}
+
+void launch_vt_count(const Dev &d, cudaStream_t st) {
+  const int B = 256;
+  const long long slots = (long long)d.n * d.bond_cap;
+  k_vt_prep_center<<<(d.n + B - 1) / B, B, 0, st>>>(d);
+  k_vt_prep_bond<<<(unsigned)((slots + B - 1) / B), B, 0, st>>>(d);
+  k_vt_count<<<(unsigned)((slots + 1 + B - 1) / B), B, 0, st>>>(d);
+  launch_scan(d.w_cnt_v, d.w_off_v, (int)(slots + 1), d.w_bsum, st);
+  launch_scan(d.w_cnt_t, d.w_off_t, (int)(slots + 1), d.w_bsum, st);
+}
+
+void launch_vt_run(const Dev &d, cudaStream_t st, int eflag, long long nval, long long ntor) {
+  const int B = 256;
+  const long long slots = (long long)d.n * d.bond_cap;
+  k_vt_fill<<<(unsigned)((slots + B - 1) / B), B, 0, st>>>(d);
+  if (nval > 0) k_valence<<<(unsigned)((nval + 127) / 128), 128, 0, st>>>(d, eflag, nval);
+  if (ntor > 0) k_torsion<<<(unsigned)((ntor + 127) / 128), 128, 0, st>>>(d, eflag, ntor);
 }
 
 void launch_dbond_forces(const Dev &d, cudaStream_t st) {

@@ -553,6 +553,14 @@ __global__ void k_count(Dev d) {
 
 }  // namespace
 
+// exclusive scan of n ints (n < 2^30); bsum needs (n + 1023) / 1024 ints
+void launch_scan(const int *in, int *out, int n, int *bsum, cudaStream_t st) {
+  const int nb = (n + 1023) / 1024;
+  k_scan_blocks<<<nb, 1024, 0, st>>>(in, out, bsum, n);
+  k_scan_sums<<<1, 1024, 0, st>>>(bsum, nb, nullptr);
+  k_scan_add<<<nb, 1024, 0, st>>>(out, bsum, n);
+}
+
 void launch_count(const Dev &d, cudaStream_t st) {
   k_count<<<(d.n + 255) / 256, 256, 0, st>>>(d);
 }

@@ -87,6 +87,7 @@ struct rg_system {
   std::vector<void *> per_nb;   // sized by n * nb_cap
   std::vector<void *> per_b;    // sized by n * bond_cap
   std::vector<void *> per_hb;   // sized by n * hb_cap
+  std::vector<void *> per_items;  // valence / torsion work items
   void *cells = nullptr;
   int ncell_alloc = 0;
   bool lists_valid = false;
@@ -95,6 +96,7 @@ struct rg_system {
   double energy[RG_NE] = {0};
   Prof prof;
   long long launches = 0;   // kernels of this library launched so far
+  long long n_val = 0, n_tor = 0;   // valence angles / torsions of the last step
 };
 
 namespace {
@@ -192,6 +194,24 @@ int alloc_bonds(rg_system *h) {
   r |= dalloc(h, h->per_b, &d.b_Cdbo, S);
   r |= dalloc(h, h->per_b, &d.b_Cdbopi, S);
   r |= dalloc(h, h->per_b, &d.b_Cdbopi2, S);
+  r |= dalloc(h, h->per_b, &d.b_et2, S);
+  r |= dalloc(h, h->per_b, &d.b_ec2, S);
+  r |= dalloc(h, h->per_b, &d.w_cnt_v, S + 1);
+  r |= dalloc(h, h->per_b, &d.w_cnt_t, S + 1);
+  r |= dalloc(h, h->per_b, &d.w_off_v, S + 1);
+  r |= dalloc(h, h->per_b, &d.w_off_t, S + 1);
+  r |= dalloc(h, h->per_b, &d.w_bsum, (S + 1 + 1023) / 1024 + 1);
+  return r;
+}
+
+int alloc_items(rg_system *h, long long nval, long long ntor) {
+  free_bucket(h->per_items);
+  Dev &d = h->d;
+  d.cap_val = nval;
+  d.cap_tor = ntor;
+  int r = 0;
+  r |= dalloc(h, h->per_items, &d.w_val, (size_t)nval);
+  r |= dalloc(h, h->per_items, &d.w_tor, (size_t)ntor);
   return r;
 }
 
@@ -242,6 +262,7 @@ int alloc_atoms(rg_system *h, int n) {
   for (double **q : pd) r |= dalloc(h, B, q, (size_t)n);
   r |= dalloc(h, B, &d.dDeltap, 3 * (size_t)n);
   r |= dalloc(h, B, &d.fC, 4 * (size_t)n);
+  r |= dalloc(h, B, &d.c_sbo, 5 * (size_t)n);
   double2 **pv[] = {&d.qx, &d.qb, &d.qr, &d.qu, &d.qw, &d.qd, &d.qq, &d.qp, &d.qs, &d.qv, &d.qz, &d.qm};
   for (double2 **q : pv) r |= dalloc(h, B, q, (size_t)n);
   r |= dalloc(h, B, &d.red, 128);
@@ -262,6 +283,7 @@ int alloc_atoms(rg_system *h, int n) {
   r |= alloc_nbrs(h);
   r |= alloc_bonds(h);
   r |= alloc_hb(h);
+  r |= alloc_items(h, (long long)n * 16 + 1024, (long long)n * 24 + 1024);
   return r ? RG_E_CUDA : 0;
 }
 
@@ -335,7 +357,28 @@ int do_compute(rg_system *h, int eflag) {
   { Scope sc(h, PH_BO, 3); launch_bond_orders(d, h->st); }
   { Scope sc(h, PH_ATOM, 1); launch_atom_energy(d, h->st, eflag); }
   { Scope sc(h, PH_HB, 1); launch_hbonds(d, h->st, eflag); }
-  { Scope sc(h, PH_VALTOR, 1); launch_valence_torsion(d, h->st, eflag); }
+  {
+    Scope sc(h, PH_VALTOR, 9);
+    launch_vt_count(d, h->st);
+  }
+  {
+    // item totals sit after the last slot of the exclusive scans
+    const long long slots = (long long)d.n * d.bond_cap;
+    int tot[2];
+    CK(cudaMemcpyAsync(&tot[0], d.w_off_v + slots, sizeof(int), cudaMemcpyDeviceToHost, h->st));
+    CK(cudaMemcpyAsync(&tot[1], d.w_off_t + slots, sizeof(int), cudaMemcpyDeviceToHost, h->st));
+    CK(cudaStreamSynchronize(h->st));
+    if (tot[0] > d.cap_val || tot[1] > d.cap_tor) {
+      if (alloc_items(h, std::max<long long>(d.cap_val, (long long)(tot[0] * 1.3) + 1024),
+                      std::max<long long>(d.cap_tor, (long long)(tot[1] * 1.3) + 1024)))
+        return RG_E_CUDA;
+      h->stats.regrows++;
+    }
+    h->n_val = tot[0];
+    h->n_tor = tot[1];
+    Scope sc(h, PH_VALTOR, 3);
+    launch_vt_run(d, h->st, eflag, tot[0], tot[1]);
+  }
   { Scope sc(h, PH_NONB, 1); launch_nonbonded(d, h->st, eflag); }
   { Scope sc(h, PH_DBOND, 1); launch_dbond_forces(d, h->st); }
   { Scope sc(h, PH_FOUT, 1); launch_force_out(d, h->st); }
@@ -458,6 +501,7 @@ int rg_destroy(rg_system *h) {
   free_bucket(h->per_nb);
   free_bucket(h->per_b);
   free_bucket(h->per_hb);
+  free_bucket(h->per_items);
   if (h->cells) cudaFree(h->cells);
   cudaFree(h->d_ff);
   cudaFree(h->d_ctl);

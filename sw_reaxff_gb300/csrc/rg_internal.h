@@ -148,6 +148,15 @@ struct Dev {
   double *red;        // device scalars / reduction accumulators
   double *energy;     // [RG_NE]
 
+  // valence / torsion work lists (built per force step)
+  double *c_sbo;      // 5 * n: SBO2, CSBO2, dSBO1, dSBO2, expval6 per centre
+  double *b_et2, *b_ec2;   // per bond slot: exp(-p_tor2 BOA), exp(-p_cot2 (BOA-1.5)^2)
+  int *w_cnt_v, *w_cnt_t;  // per (centre, bond) slot counts (+1 trailing zero)
+  int *w_off_v, *w_off_t;  // exclusive scans (+1: totals)
+  int *w_bsum;             // scan block sums
+  unsigned long long *w_val, *w_tor;   // packed items
+  long long cap_val, cap_tor;
+
   int *status;        // [8]: 0 overflow flags, 1 max nbrs, 2 max bonds, 3 max hb, 4 nonfinite,
                       //      5 pair entries, 6 bonds, 7 H-bond partners
 };
@@ -191,6 +200,10 @@ void launch_bond_orders(const Dev &d, cudaStream_t st);
 void launch_atom_energy(const Dev &d, cudaStream_t st, int eflag);
 void launch_hbonds(const Dev &d, cudaStream_t st, int eflag);
 void launch_valence_torsion(const Dev &d, cudaStream_t st, int eflag);
+// work-list form: prep + count (then the host reads the totals), fill + run
+void launch_vt_count(const Dev &d, cudaStream_t st);
+void launch_vt_run(const Dev &d, cudaStream_t st, int eflag, long long nval, long long ntor);
+void launch_scan(const int *in, int *out, int n, int *bsum, cudaStream_t st);
 void launch_nonbonded(const Dev &d, cudaStream_t st, int eflag);
 void launch_dbond_forces(const Dev &d, cudaStream_t st);
 void launch_force_out(const Dev &d, cudaStream_t st);

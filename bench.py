@@ -51,6 +51,8 @@ def parse():
     p.add_argument("--scale", type=float, default=1.0,
                    help="workload size relative to the 1,048,576-atom mixture")
     p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--no-mixed", action="store_true",
+                   help="skip the mixed-precision measurement of the same workload")
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--cpu-scale", type=float, default=0.02,
                    help="size of the CPU-baseline sample relative to 1M atoms")
@@ -260,6 +262,34 @@ def gpu_arm(args):
     tmax = dist.max(ms / 1e3)
     value = n * args.steps * world / tmax
 
+    # the mixed-precision form on the same workload (FP32 pair/bond arithmetic
+    # and QEq SpMV, FP64 accumulation), timed the same way
+    mixed = None
+    if not args.no_mixed:
+        from sw_reaxff_gb300.api import PREC_MIXED
+        gm = ReaxGPU(DEFAULT_FFIELD, device=local, precision=PREC_MIXED)
+        gm.set_system(s)
+        gm.run(max(args.warmup, 1), DT, energies=False)
+        sm = torch.cuda.ExternalStream(gm.stream())
+        m0 = torch.cuda.Event(enable_timing=True)
+        m1 = torch.cuda.Event(enable_timing=True)
+        dist.barrier()
+        gm.synchronize()
+        gm.profile(True)
+        m0.record(sm)
+        gm.run(args.steps, DT, energies=False)
+        m1.record(sm)
+        gm.synchronize()
+        dist.barrier()
+        pm = gm.profile_get()
+        gm.profile(False)
+        tm = dist.max(m0.elapsed_time(m1) / 1e3)
+        mixed = {"value": n * args.steps * world / tm, "unit": UNIT,
+                 "ms_per_step": tm * 1e3 / args.steps, "speedup_vs_fp64": tmax / tm,
+                 "phases_ms_per_step": {k: round(v[0] / args.steps, 4)
+                                        for k, v in pm.items() if v[1] > 0}}
+        gm.close()
+
     # end to end through the C ABI with host (pinned) buffers: per step the
     # state x, v, f goes host->device, the step runs, x, v, q, f come back
     e2e = None
@@ -318,6 +348,7 @@ def gpu_arm(args):
                    "atoms": n, "parallelism": f"replicas x{world}",
                    "l2": "inputs larger than L2 (pair list ~GBs)"},
         "e2e": e2e,
+        "mixed": mixed,
         "gpu_launches": None,
         "clocks": ck,
         "roofline": roof,

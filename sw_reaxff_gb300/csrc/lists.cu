@@ -167,6 +167,7 @@ struct NbrQueue {
 };
 
 // finish 32 queued candidates (lanes with q < cnt hold one each)
+template <bool MIXED>
 __device__ __forceinline__ void nbr_flush(const Dev &d, const Control &C, const ForceField &F,
                                           const NbrQueue &Q, int cnt, int lane, int i,
                                           const double4 &xi, int ti, long long row, int cap,
@@ -199,7 +200,32 @@ __device__ __forceinline__ void nbr_flush(const Dev &d, const Control &C, const 
     const int pos = near ? cntN + __popc(mn & lanemask_lt())
                          : cap - 1 - (cntF + __popc(mf & lanemask_lt()));
     double h = 0.0;
-    if (d2 <= C.swb2) {
+    if (MIXED && d2 <= C.swb2) {
+      // FP32: factored taper when swa = 0
+      const int tj = __float_as_int(d.xf[j].w);
+      const float d2f = (float)d2;
+      const float r = d2f * rsqrtf(d2f);
+      float tp;
+      if (C.qtap_factored) {
+        const float t = r * (float)C.inv_swb_q, u = 1.f - t, u2 = u * u;
+        tp = u2 * u2 * (1.f + t * (4.f + t * (10.f + t * 20.f)));
+      } else {
+        const double *T = C.qTap;
+        tp = fmaf((float)T[7], r, (float)T[6]);
+        tp = fmaf(tp, r, (float)T[5]);
+        tp = fmaf(tp, r, (float)T[4]);
+        tp = fmaf(tp, r, (float)T[3]);
+        tp = fmaf(tp, r, (float)T[2]);
+        tp = fmaf(tp, r, (float)T[1]);
+        tp = fmaf(tp, r, (float)T[0]);
+      }
+      const float x = fmaf(d2f, r, (float)F.tbp[ti][tj].gamma);
+      d.nbr[row + pos] = ((uint32_t)j << 8) | (uint32_t)img;
+      d.hval32[row + pos] = tp * 14.4f * rcbrtf(x);
+    } else if (MIXED) {
+      d.nbr[row + pos] = ((uint32_t)j << 8) | (uint32_t)img;
+      d.hval32[row + pos] = 0.f;
+    } else if (d2 <= C.swb2) {
       // H_ij = Tap(r) * 14.4 / (r^3 + shld)^c, c = 0.3333333333333
       const double r = d2 * rsqrt(d2);
       const double *T = C.qTap;
@@ -214,13 +240,16 @@ __device__ __forceinline__ void nbr_flush(const Dev &d, const Control &C, const 
       const double x = fma(d2, r, F.tbp[ti][tj].gamma);
       h = tp * 14.4 * rpow_third(x, RG_C3_QEQ);
     }
-    d.nbr[row + pos] = ((uint32_t)j << 8) | (uint32_t)img;
-    d.hval[row + pos] = h;
+    if (!MIXED) {
+      d.nbr[row + pos] = ((uint32_t)j << 8) | (uint32_t)img;
+      d.hval[row + pos] = h;
+    }
   }
   cntN += __popc(mn);
   cntF += __popc(mf);
 }
 
+template <bool MIXED>
 __global__ void __launch_bounds__(NB_WARPS * 32) k_build_nbrs(Dev d) {
   __shared__ NbrQueue queues[NB_WARPS];
   const int lane = threadIdx.x & 31;
@@ -285,7 +314,7 @@ __global__ void __launch_bounds__(NB_WARPS * 32) k_build_nbrs(Dev d) {
           qn += __popc(mc);
           __syncwarp();
           if (qn >= 32) {
-            nbr_flush(d, C, F, Q, 32, lane, i, xi, ti, row, cap, cntN, cntF);
+            nbr_flush<MIXED>(d, C, F, Q, 32, lane, i, xi, ti, row, cap, cntN, cntF);
             __syncwarp();
             // move the leftover (< 32) to the front of the queue
             const int left = qn - 32;
@@ -306,7 +335,7 @@ __global__ void __launch_bounds__(NB_WARPS * 32) k_build_nbrs(Dev d) {
       }
     }
   }
-  if (qn > 0) nbr_flush(d, C, F, Q, qn, lane, i, xi, ti, row, cap, cntN, cntF);
+  if (qn > 0) nbr_flush<MIXED>(d, C, F, Q, qn, lane, i, xi, ti, row, cap, cntN, cntF);
   if (lane == 0) {
     d.n_near[i] = cntN;
     d.n_far[i] = cntF;
@@ -329,6 +358,26 @@ struct BondQueue {
   double dist[QCAP], dx[QCAP], dy[QCAP], dz[QCAP];
 };
 
+// uncorrected bond order terms of one pair in arithmetic R
+template <typename R>
+__device__ __forceinline__ void bo_prime(const Sbp &si, const Sbp &sj, const Tbp &tw, R dist, R bo_cut,
+                                         R &BOs, R &BOpi, R &BOpi2, R &C12, R &C34, R &C56) {
+  BOs = BOpi = BOpi2 = C12 = C34 = C56 = 0;
+  if (si.r_s > 0.0 && sj.r_s > 0.0) {
+    C12 = (R)tw.p_bo1 * pow(dist / (R)tw.r_s, (R)tw.p_bo2);
+    BOs = (R(1) + bo_cut) * exp(C12);
+  }
+  if (si.r_pi > 0.0 && sj.r_pi > 0.0) {
+    C34 = (R)tw.p_bo3 * pow(dist / (R)tw.r_p, (R)tw.p_bo4);
+    BOpi = exp(C34);
+  }
+  if (si.r_pi_pi > 0.0 && sj.r_pi_pi > 0.0) {
+    C56 = (R)tw.p_bo5 * pow(dist / (R)tw.r_pp, (R)tw.p_bo6);
+    BOpi2 = exp(C56);
+  }
+}
+
+template <bool MIXED>
 __device__ __forceinline__ void bond_flush(const Dev &d, const Control &C, const ForceField &F,
                                            const BondQueue &Q, int cnt, int lane, int i, int ti,
                                            int &nb, double &ddx, double &ddy, double &ddz,
@@ -343,22 +392,26 @@ __device__ __forceinline__ void bond_flush(const Dev &d, const Control &C, const
     const int tj = d.ts[(int)(e >> 8)];
     const Sbp &si = F.sbp[ti], &sj = F.sbp[tj];
     const Tbp &tw = F.tbp[ti][tj];
-    double C12 = 0, C34 = 0, C56 = 0;
-    if (si.r_s > 0.0 && sj.r_s > 0.0) {
-      C12 = tw.p_bo1 * pow(dist / tw.r_s, tw.p_bo2);
-      BOs = (1.0 + C.bo_cut) * exp(C12);
+    double C12, C34, C56;
+    if (MIXED) {
+      // FP32 bond orders; the exact FP64 decision only within 1e-4 of
+      // the threshold, so the bond list equals the FP64 form's
+      float a, b, c, c12, c34, c56;
+      bo_prime<float>(si, sj, tw, (float)dist, (float)C.bo_cut, a, b, c, c12, c34, c56);
+      BOs = a; BOpi = b; BOpi2 = c; C12 = c12; C34 = c34; C56 = c56;
+      const double BO32 = (double)(a + b + c);
+      if (fabs(BO32 - C.bo_cut) <= 1e-4 * C.bo_cut) {
+        double x0, x1, x2, y0, y1, y2;
+        bo_prime<double>(si, sj, tw, dist, C.bo_cut, x0, x1, x2, y0, y1, y2);
+        isb = (x0 + x1 + x2) >= C.bo_cut;
+      } else {
+        isb = BO32 >= C.bo_cut;
+      }
+    } else {
+      bo_prime<double>(si, sj, tw, dist, C.bo_cut, BOs, BOpi, BOpi2, C12, C34, C56);
+      isb = (BOs + BOpi + BOpi2) >= C.bo_cut;
     }
-    if (si.r_pi > 0.0 && sj.r_pi > 0.0) {
-      C34 = tw.p_bo3 * pow(dist / tw.r_p, tw.p_bo4);
-      BOpi = exp(C34);
-    }
-    if (si.r_pi_pi > 0.0 && sj.r_pi_pi > 0.0) {
-      C56 = tw.p_bo5 * pow(dist / tw.r_pp, tw.p_bo6);
-      BOpi2 = exp(C56);
-    }
-    const double BO = BOs + BOpi + BOpi2;
-    if (BO >= C.bo_cut) {
-      isb = true;
+    if (isb) {
       const double r2 = dist * dist;
       Cs = tw.p_bo2 * C12 / r2;
       Cpi = tw.p_bo4 * C34 / r2;
@@ -394,6 +447,7 @@ __device__ __forceinline__ void bond_flush(const Dev &d, const Control &C, const
   nb += __popc(mb);
 }
 
+template <bool MIXED>
 __global__ void __launch_bounds__(NB_WARPS * 32) k_build_bonds(Dev d) {
   __shared__ BondQueue queues[NB_WARPS];
   const int lane = threadIdx.x & 31;
@@ -472,7 +526,7 @@ __global__ void __launch_bounds__(NB_WARPS * 32) k_build_bonds(Dev d) {
     }
     while (qn >= 32 || (base >= nn && qn > 0)) {
       const int cnt = min(qn, 32);
-      bond_flush(d, C, F, Q, cnt, lane, i, ti, nb, ddx, ddy, ddz, bsum);
+      bond_flush<MIXED>(d, C, F, Q, cnt, lane, i, ti, nb, ddx, ddy, ddz, bsum);
       __syncwarp();
       const int left = qn - cnt;
       uint32_t le = 0;
@@ -585,12 +639,16 @@ void launch_bin_sort(const Dev &d, cudaStream_t st) {
 void launch_build_nbrs(const Dev &d, cudaStream_t st) {
   const int B = NB_WARPS * 32;
   const long long threads = (long long)d.n * 32;
-  k_build_nbrs<<<(unsigned)((threads + B - 1) / B), B, 0, st>>>(d);
+  const unsigned G = (unsigned)((threads + B - 1) / B);
+  if (d.mixed) k_build_nbrs<true><<<G, B, 0, st>>>(d);
+  else k_build_nbrs<false><<<G, B, 0, st>>>(d);
 }
 
 void launch_build_bonds(const Dev &d, cudaStream_t st) {
   const long long threads = (long long)d.n * 32;
-  k_build_bonds<<<(unsigned)((threads + NB_WARPS * 32 - 1) / (NB_WARPS * 32)), NB_WARPS * 32, 0, st>>>(d);
+  const unsigned G = (unsigned)((threads + NB_WARPS * 32 - 1) / (NB_WARPS * 32));
+  if (d.mixed) k_build_bonds<true><<<G, NB_WARPS * 32, 0, st>>>(d);
+  else k_build_bonds<false><<<G, NB_WARPS * 32, 0, st>>>(d);
   const long long slots = (long long)d.n * d.bond_cap;
   k_bond_sym<<<(unsigned)((slots + 255) / 256), 256, 0, st>>>(d);
 }

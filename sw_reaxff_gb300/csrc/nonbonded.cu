@@ -8,6 +8,8 @@
 // reports in pvector (e_vdW, e_ele = twice the physical value) are recovered
 // by doubling, and eng_vdwl / eng_coul get the physical (half-tallied) sums
 // like ev_tally_full (reaxc_inlines_sw64.h:178-222).
+#include <type_traits>
+
 #include "rg_internal.h"
 
 namespace {
@@ -48,8 +50,41 @@ struct PairQueue {
   uint32_t e[QC];
 };
 
-// vdW + Coulomb of up to 32 queued pairs (one per lane); returns dE/dr / r
-// and the displacement in (c, dx, dy, dz), zero for idle lanes
+// real-type helpers of the two forms (FP64: the reference's expressions;
+// mixed: FP32 arithmetic)
+__device__ __forceinline__ double rs_(double x) { return rsqrt(x); }
+__device__ __forceinline__ float rs_(float x) { return rsqrtf(x); }
+
+// Tap(r) and (1/r) dTap/dr
+template <typename R>
+__device__ __forceinline__ void taper(const Control &C, R r, R rinv, R &Tp, R &dTap) {
+  if (std::is_same<R, float>::value && C.tap_factored) {
+    // (1-t)^4 (1 + 4t + 10t^2 + 20t^3), t = r/swb;  (1/r) d/dr = -140 t^2 (1-t)^3 / swb^2
+    const R is = (R)C.inv_swb_nb;
+    const R t = r * is, u = R(1) - t, u2 = u * u;
+    Tp = u2 * u2 * (R(1) + t * (R(4) + t * (R(10) + t * R(20))));
+    dTap = R(-140) * t * t * u2 * u * is * is;
+    return;
+  }
+  const double *Tap = C.Tap;
+  Tp = fma((R)Tap[7], r, (R)Tap[6]);
+  Tp = fma(Tp, r, (R)Tap[5]);
+  Tp = fma(Tp, r, (R)Tap[4]);
+  Tp = fma(Tp, r, (R)Tap[3]);
+  Tp = fma(Tp, r, (R)Tap[2]);
+  Tp = fma(Tp, r, (R)Tap[1]);
+  Tp = fma(Tp, r, (R)Tap[0]);
+  dTap = fma((R)(7 * Tap[7]), r, (R)(6 * Tap[6]));
+  dTap = fma(dTap, r, (R)(5 * Tap[5]));
+  dTap = fma(dTap, r, (R)(4 * Tap[4]));
+  dTap = fma(dTap, r, (R)(3 * Tap[3]));
+  dTap = fma(dTap, r, (R)(2 * Tap[2]));
+  dTap = fma((R)Tap[1], rinv, dTap);
+}
+
+// vdW + Coulomb of one queued pair; returns (1/r) dE/dr in c and the
+// displacement; energies are added in FP64
+template <typename R>
 __device__ __forceinline__ void pair_terms(const Dev &d, const ForceField &F, const Control &C,
                                           uint32_t e, bool act, const double4 &xi, int ti,
                                           double &evdw, double &eele, double &c, double &dx,
@@ -64,71 +99,65 @@ __device__ __forceinline__ void pair_terms(const Dev &d, const ForceField &F, co
   dx = __dsub_rn(__dadd_rn(xj.x, sx * d.L[0]), xi.x);
   dy = __dsub_rn(__dadd_rn(xj.y, sy * d.L[1]), xi.y);
   dz = __dsub_rn(__dadd_rn(xj.z, sz * d.L[2]), xi.z);
-  const double d2 = __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
-  if (d2 > C.nonb_cut2) { dx = dy = dz = 0.0; return; }
-  const double rinv = rsqrt(d2);
-  const double r = d2 * rinv;
+  const double d2x = __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
+  if (d2x > C.nonb_cut2) { dx = dy = dz = 0.0; return; }
+  const R d2 = (R)d2x;
+  const R rinv = rs_(d2);
+  const R r = d2 * rinv;
   const Tbp &tw = F.tbp[ti][d.ts[j]];
-  const double *Tap = C.Tap;
-  double Tp = fma(Tap[7], r, Tap[6]);
-  Tp = fma(Tp, r, Tap[5]);
-  Tp = fma(Tp, r, Tap[4]);
-  Tp = fma(Tp, r, Tap[3]);
-  Tp = fma(Tp, r, Tap[2]);
-  Tp = fma(Tp, r, Tap[1]);
-  Tp = fma(Tp, r, Tap[0]);
-  double dTap = fma(7 * Tap[7], r, 6 * Tap[6]);
-  dTap = fma(dTap, r, 5 * Tap[5]);
-  dTap = fma(dTap, r, 4 * Tap[4]);
-  dTap = fma(dTap, r, 3 * Tap[3]);
-  dTap = fma(dTap, r, 2 * Tap[2]);
-  dTap = fma(Tap[1], rinv, dTap);
-  const double p_vdW1 = F.gp[28];
+  R Tp, dTap;
+  taper<R>(C, r, rinv, Tp, dTap);
+  const R p_vdW1 = (R)F.gp[28];
   const int vdw_type = F.vdw_type;
-  const double ar = tw.alpha / tw.r_vdW;
-  double e_vdW, CEvd, e_core = 0.0, e_lg = 0.0;
+  const R alpha = (R)tw.alpha, r_vdW = (R)tw.r_vdW, D = (R)tw.D;
+  const R ar = alpha / r_vdW;
+  R e_vdW, CEvd, e_core = 0, e_lg = 0;
   if (vdw_type == 1 || vdw_type == 3) {
     // shielded Morse: fn13 = (r^p + gamma_w^-p)^(1/p)
-    const double powr = exp(p_vdW1 * log(r));                 // r^p
-    const double S = powr + tw.powgi_vdW1;
-    const double fn13 = exp(log(S) / p_vdW1);                 // S^(1/p)
-    const double exp2 = exp(0.5 * tw.alpha * (1.0 - fn13 / tw.r_vdW));
-    const double exp1 = exp2 * exp2;
-    e_vdW = tw.D * (exp1 - 2.0 * exp2);
-    const double dfn13 = (fn13 / S) * (powr / d2);            // S^(1/p-1) r^(p-2)
-    CEvd = dTap * e_vdW - Tp * tw.D * ar * (exp1 - exp2) * dfn13;
+    const R powr = exp(p_vdW1 * log(r));                      // r^p
+    const R S = powr + (R)tw.powgi_vdW1;
+    const R fn13 = exp(log(S) / p_vdW1);                      // S^(1/p)
+    const R exp2 = exp(R(0.5) * alpha * (R(1) - fn13 / r_vdW));
+    const R exp1 = exp2 * exp2;
+    e_vdW = D * (exp1 - R(2) * exp2);
+    const R dfn13 = (fn13 / S) * (powr / d2);                 // S^(1/p-1) r^(p-2)
+    CEvd = dTap * e_vdW - Tp * D * ar * (exp1 - exp2) * dfn13;
   } else {
-    const double exp2 = exp(0.5 * tw.alpha * (1.0 - r / tw.r_vdW));
-    const double exp1 = exp2 * exp2;
-    e_vdW = tw.D * (exp1 - 2.0 * exp2);
-    CEvd = dTap * e_vdW - Tp * tw.D * ar * (exp1 - exp2) * rinv;
+    const R exp2 = exp(R(0.5) * alpha * (R(1) - r / r_vdW));
+    const R exp1 = exp2 * exp2;
+    e_vdW = D * (exp1 - R(2) * exp2);
+    CEvd = dTap * e_vdW - Tp * D * ar * (exp1 - exp2) * rinv;
   }
   if (vdw_type == 2 || vdw_type == 3) {
-    e_core = tw.ecore * exp(tw.acore * (1.0 - (r / tw.rcore)));
-    const double de_core = -(tw.acore / tw.rcore) * e_core;
+    const R acore = (R)tw.acore, rcore = (R)tw.rcore;
+    e_core = (R)tw.ecore * exp(acore * (R(1) - (r / rcore)));
+    const R de_core = -(acore / rcore) * e_core;
     CEvd += dTap * e_core + Tp * de_core * rinv;
     if (C.lgflag) {
-      const double r5 = d2 * d2 * r, r6 = d2 * d2 * d2;
-      const double lg2 = tw.lgre * tw.lgre;
-      const double re6 = lg2 * lg2 * lg2;
-      e_lg = -(tw.lgcij / (r6 + re6));
-      const double de_lg = -6.0 * e_lg * r5 / (r6 + re6);
+      const R r5 = d2 * d2 * r, r6 = d2 * d2 * d2;
+      const R lg2 = (R)tw.lgre * (R)tw.lgre;
+      const R re6 = lg2 * lg2 * lg2;
+      e_lg = -((R)tw.lgcij / (r6 + re6));
+      const R de_lg = R(-6) * e_lg * r5 / (r6 + re6);
       CEvd += dTap * e_lg + Tp * de_lg * rinv;
     }
   }
   // shielded Coulomb: Tap qi qj / (r^3 + gamma)^c
-  const double dr3gamij_1 = fma(d2, r, tw.gamma);
-  const double inv3 = rpow_third(dr3gamij_1, RG_C3_ELE);
-  const double qq = C_ele * xi.w * xj.w;
-  const double e_ele = qq * Tp * inv3;
-  const double CEclmb = qq * (dTap - Tp * r / dr3gamij_1) * inv3;
-  evdw += Tp * (e_vdW + e_core + e_lg);
-  eele += e_ele;
-  c = CEvd + CEclmb;
+  const R dr3gamij_1 = fma(d2, r, (R)tw.gamma);
+  R inv3;
+  if (std::is_same<R, float>::value) inv3 = (R)rcbrtf((float)dr3gamij_1);
+  else inv3 = (R)rpow_third((double)dr3gamij_1, RG_C3_ELE);
+  const R qq = (R)(C_ele * xi.w * xj.w);
+  const R e_ele = qq * Tp * inv3;
+  const R CEclmb = qq * (dTap - Tp * r / dr3gamij_1) * inv3;
+  evdw += (double)(Tp * (e_vdW + e_core + e_lg));
+  eele += (double)e_ele;
+  c = (double)(CEvd + CEclmb);
 }
 
 // one warp per atom i; the pairs (i,j,image) with j > i, or j == i with the
 // "positive" image, are queued and evaluated 32 at a time
+template <typename R>
 __global__ void __launch_bounds__(NBW * 32) k_nonbonded(Dev d, int eflag) {
   __shared__ PairQueue queues[NBW];
   const int lane = threadIdx.x & 31;
@@ -171,7 +200,7 @@ __global__ void __launch_bounds__(NBW * 32) k_nonbonded(Dev d, int eflag) {
         const uint32_t e = act ? Q.e[lane] : 0u;
         double c, dx, dy, dz;
         int j;
-        pair_terms(d, F, C, e, act, xi, ti, evdw, eele, c, dx, dy, dz, j);
+        pair_terms<R>(d, F, C, e, act, xi, ti, evdw, eele, c, dx, dy, dz, j);
         if (act && c != 0.0) {
           fx -= c * dx;
           fy -= c * dy;
@@ -211,5 +240,7 @@ __global__ void __launch_bounds__(NBW * 32) k_nonbonded(Dev d, int eflag) {
 
 void launch_nonbonded(const Dev &d, cudaStream_t st, int eflag) {
   const long long threads = (long long)d.n * 32;
-  k_nonbonded<<<(unsigned)((threads + NBW * 32 - 1) / (NBW * 32)), NBW * 32, 0, st>>>(d, eflag);
+  const unsigned G = (unsigned)((threads + NBW * 32 - 1) / (NBW * 32));
+  if (d.mixed) k_nonbonded<float><<<G, NBW * 32, 0, st>>>(d, eflag);
+  else k_nonbonded<double><<<G, NBW * 32, 0, st>>>(d, eflag);
 }

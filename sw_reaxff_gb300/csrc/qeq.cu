@@ -64,7 +64,7 @@ __global__ void k_qeq_setup(Dev d) {
   d.qx[s] = make_double2(s0, t0);
 }
 
-// y = H x (+ eta x on the diagonal), one warp per row
+// y = H x (+ eta x on the diagonal), one warp per row; FP64 form
 __global__ void __launch_bounds__(256) k_spmv(Dev d, const double2 *__restrict__ x, double2 *__restrict__ y) {
   const int lane = threadIdx.x & 31;
   const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -87,6 +87,32 @@ __global__ void __launch_bounds__(256) k_spmv(Dev d, const double2 *__restrict__
     const double eta = d.ff->sbp[d.ts[i]].eta;
     const double2 xi = x[i];
     y[i] = make_double2(fma(eta, xi.x, as), fma(eta, xi.y, at));
+  }
+}
+
+// mixed form: FP32 H and FP32 products; per-lane partial sums in FP32,
+// the warp's total and the diagonal term in FP64
+__global__ void __launch_bounds__(256) k_spmv32(Dev d, const double2 *__restrict__ x, double2 *__restrict__ y) {
+  const int lane = threadIdx.x & 31;
+  const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (i >= d.n) return;
+  const long long row = (long long)i * d.nb_cap;
+  const int nn = d.n_near[i], nf = d.n_far[i], cap = d.nb_cap;
+  const int tot = min(nn + nf, cap);
+  float as = 0.f, at = 0.f;
+  for (int p = lane; p < tot; p += 32) {
+    const int slot = p < nn ? p : cap - 1 - (p - nn);
+    const uint32_t e = d.nbr[row + slot];
+    const float h = d.hval32[row + slot];
+    const double2 xj = x[e >> 8];
+    as = fmaf(h, (float)xj.x, as);
+    at = fmaf(h, (float)xj.y, at);
+  }
+  double ds = warp_sum((double)as), dt = warp_sum((double)at);
+  if (lane == 0) {
+    const double eta = d.ff->sbp[d.ts[i]].eta;
+    const double2 xi = x[i];
+    y[i] = make_double2(fma(eta, xi.x, ds), fma(eta, xi.y, dt));
   }
 }
 
@@ -273,7 +299,8 @@ void launch_qeq_setup(const Dev &d, cudaStream_t st) {
 
 void launch_qeq_spmv(const Dev &d, cudaStream_t st, const double2 *x, double2 *y) {
   const long long threads = (long long)d.n * 32;
-  k_spmv<<<(unsigned)((threads + 255) / 256), 256, 0, st>>>(d, x, y);
+  if (d.mixed) k_spmv32<<<(unsigned)((threads + 255) / 256), 256, 0, st>>>(d, x, y);
+  else k_spmv<<<(unsigned)((threads + 255) / 256), 256, 0, st>>>(d, x, y);
 }
 
 void launch_qeq_cg_init(const Dev &d, cudaStream_t st) {

@@ -221,7 +221,13 @@ int alloc_nbrs(rg_system *h) {
   const size_t S = (size_t)d.n * d.nb_cap;
   int r = 0;
   r |= dalloc(h, h->per_nb, &d.nbr, S);
-  r |= dalloc(h, h->per_nb, &d.hval, S);
+  if (d.mixed) {
+    r |= dalloc(h, h->per_nb, &d.hval32, S);
+    d.hval = nullptr;
+  } else {
+    r |= dalloc(h, h->per_nb, &d.hval, S);
+    d.hval32 = nullptr;
+  }
   return r;
 }
 
@@ -471,6 +477,15 @@ int rg_create(const char *ffield_path, const rg_params *pin, rg_system **out) {
   c.near_cut = std::max(c.bond_cut, c.hbond_cut);
   rg_init_taper(c.nonb_low, c.nonb_cut, c.Tap);
   rg_init_taper(h->p.qeq_swa, h->p.qeq_swb, c.qTap);
+  c.tap_factored = (c.nonb_low == 0.0);
+  c.qtap_factored = (h->p.qeq_swa == 0.0);
+  c.inv_swb_nb = 1.0 / c.nonb_cut;
+  c.inv_swb_q = 1.0 / h->p.qeq_swb;
+  if (h->p.precision != RG_PREC_FP64 && h->p.precision != RG_PREC_MIXED) {
+    delete h;
+    return RG_E_ARG;
+  }
+  h->d.mixed = (h->p.precision == RG_PREC_MIXED);
   if (c.near_cut > lc) {
     delete h;
     return RG_E_ARG;

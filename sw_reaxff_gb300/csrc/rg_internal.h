@@ -76,6 +76,11 @@ struct Control {
   double Tap[8];      // pair taper (swa = nonb_low, swb = nonb_cut)
   double qTap[8];     // QEq taper
   int enobondsflag, lgflag;
+  // mixed form: the taper in factored form (1-t)^4 (1+4t+10t^2+20t^3),
+  // t = r/swb, equal to the 7th-order polynomial when swa = 0; well
+  // conditioned in FP32 near the cutoff where the expanded form cancels
+  int tap_factored, qtap_factored;
+  double inv_swb_nb, inv_swb_q;
 };
 
 // Parse an ffield file (restates Read_Force_Field,
@@ -87,6 +92,7 @@ void rg_init_taper(double swa, double swb, double *Tap);
 // Device-side view of one system (sorted atom order unless noted).
 struct Dev {
   int n;              // atoms
+  int mixed;          // 1: FP32 arithmetic in the pair / bond kernels
   int nb_cap;         // neighbour row capacity (row-major rows)
   int bond_cap;       // bond slots per atom (slot-major: k*n + i)
   int hb_cap;         // H-bond partner slots per H atom (row-major)
@@ -117,7 +123,8 @@ struct Dev {
   // full pair list, row-major rows of nb_cap; near entries from the front,
   // far entries from the back
   uint32_t *nbr;      // (j << 8) | image
-  double *hval;       // QEq H_ij per entry
+  double *hval;       // QEq H_ij per entry (FP64 form)
+  float *hval32;      // QEq H_ij per entry (mixed form)
   int *n_near, *n_far;
 
   // bonds (slot-major, slot = k*n + i)

@@ -288,7 +288,6 @@ def gpu_arm(args):
                  "ms_per_step": tm * 1e3 / args.steps, "speedup_vs_fp64": tmax / tm,
                  "phases_ms_per_step": {k: round(v[0] / args.steps, 4)
                                         for k, v in pm.items() if v[1] > 0}}
-        gm.close()
 
     # end to end through the C ABI with host (pinned) buffers: per step the
     # state x, v, f goes host->device, the step runs, x, v, q, f come back
@@ -314,7 +313,25 @@ def gpu_arm(args):
                "h2d_bytes_per_step": int(hx.nbytes + hv.nbytes + hf.nbytes),
                "d2h_bytes_per_step": int(hx.nbytes + hv.nbytes + hq.nbytes + hf.nbytes)}
 
-    # roofline of the dominant kernel (FP64-ALU bound)
+    # errors of the mixed form against the FP64 form on the same state (the
+    # initial configuration, charges from zero initial guesses)
+    if mixed is not None:
+        g.set_system(s)
+        gm.set_system(s)
+        q64, _, _ = g.qeq()
+        f64, e64 = g.compute()
+        q32, its32, itt32 = gm.qeq()
+        f32, e32 = gm.compute()
+        mixed["errors_vs_fp64"] = {
+            "force_rel_rms": float(np.sqrt(((f32 - f64) ** 2).sum() / (f64 ** 2).sum())),
+            "charge_max_abs": float(np.abs(q32 - q64).max()),
+            "energy_rel": {k: float(abs(e32[k] - e64[k]) / abs(e64[k]))
+                           for k in e64 if e64[k] != 0.0},
+            "qeq_restarts": gm.stats()["qeq_restarts"],
+            "bars": {"force_rel_rms": 1e-4, "charge_max_abs": 1e-5}}
+        gm.close()
+
+    # roofline of the dominant kernel (bound by the FP64 units)
     fp64_peak = measure_fp64_peak(local)
     phases = {k: v for k, v in prof.items() if v[1] > 0}
     tot_ms = sum(v[0] for v in phases.values())

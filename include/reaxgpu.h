@@ -85,6 +85,8 @@ typedef struct {
   int max_nbrs, max_bonds, max_hbonds;
   int regrows;
   long long kernel_launches;   /* kernels launched by this handle so far */
+  int qeq_restarts;            /* mixed form: residual checks of the last
+                                  QEq (1 = converged at the first check) */
 } rg_stats;
 
 void rg_default_params(rg_params *p);
@@ -94,11 +96,24 @@ int rg_create(const char *ffield_path, const rg_params *p, rg_system **out);
 int rg_destroy(rg_system *h);
 const char *rg_last_error(const rg_system *h);
 
+/* Element names of a force-field file, read on the host without a device
+ * (what pair_coeff needs to map LAMMPS types to elements,
+ * pair_reaxc_sunway.cpp:305-340): *ntypes, and if names is not NULL ntypes
+ * names of len chars each (upper case).  RG_E_FILE if the file cannot be
+ * read; msg (msg_len chars, may be NULL) then gets the reason. */
+int rg_ffield_info(const char *path, int *ntypes, char *names, int len, char *msg,
+                   int msg_len);
+
 int rg_num_types(const rg_system *h);
 /* element name of ffield type t (0-based), upper case */
 int rg_element_name(const rg_system *h, int t, char *buf, int len);
 /* per-type "chi", "eta", "gamma" or "mass" into out[ntypes] */
 int rg_extract(const rg_system *h, const char *name, double *out);
+
+/* Per-type masses used by the integrator (g/mol, mass[ntypes] by ffield
+ * type): the LAMMPS data file's Masses, which fix nve/sunway reads from
+ * atom->mass (fix_nve_sunway.cpp:73-95).  Default: the force field's. */
+int rg_set_masses(rg_system *h, const double *mass);
 
 /* Orthogonal periodic box [0,L0)x[0,L1)x[0,L2). */
 int rg_set_box(rg_system *h, const double *L3);

@@ -29,7 +29,7 @@ EXPORTED = ["rg_default_params", "rg_create", "rg_destroy", "rg_last_error",
             "rg_get_atoms", "rg_device_arrays", "rg_get_stats", "rg_synchronize",
             "rg_dump_pairs", "rg_dump_bonds", "rg_dump_hbonds", "rg_set_state",
             "rg_stream", "rg_profile_enable", "rg_profile_get", "rg_measure_fp64_peak",
-            "rg_qeq_noalloc"]
+            "rg_qeq_noalloc", "rg_set_masses", "rg_ffield_info"]
 
 
 class Params(C.Structure):
@@ -47,7 +47,8 @@ class Stats(C.Structure):
                 ("n_H_entries", C.c_longlong), ("cg_iters_s", C.c_int),
                 ("cg_iters_t", C.c_int), ("max_nbrs", C.c_int),
                 ("max_bonds", C.c_int), ("max_hbonds", C.c_int),
-                ("regrows", C.c_int), ("kernel_launches", C.c_longlong)]
+                ("regrows", C.c_int), ("kernel_launches", C.c_longlong),
+                ("qeq_restarts", C.c_int)]
 
 
 class ReaxError(RuntimeError):
@@ -77,6 +78,8 @@ def load_library(path: str = LIBPATH):
     L.rg_element_name.argtypes = [C.c_void_p, C.c_int, C.c_char_p, C.c_int]
     L.rg_extract.argtypes = [C.c_void_p, C.c_char_p, dp]
     L.rg_set_box.argtypes = [C.c_void_p, dp]
+    L.rg_set_masses.argtypes = [C.c_void_p, dp]
+    L.rg_ffield_info.argtypes = [C.c_char_p, ip, C.c_char_p, C.c_int, C.c_char_p, C.c_int]
     L.rg_set_atoms.argtypes = [C.c_void_p, C.c_int, dp, ip, ip, dp, dp]
     L.rg_set_atoms_device.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p,
                                       C.c_void_p, C.c_void_p, C.c_void_p]
@@ -122,6 +125,18 @@ def measure_fp64_peak(device: int = 0) -> float:
     if L.rg_measure_fp64_peak(device, C.byref(t)) != 0:
         raise ReaxError("rg_measure_fp64_peak failed")
     return t.value
+
+
+def ffield_elements(path: str = None) -> list:
+    """Element names of a force-field file (host only, no device)."""
+    L = load_library()
+    n = C.c_int()
+    msg = C.create_string_buffer(256)
+    if L.rg_ffield_info((path or DEFAULT_FFIELD).encode(), C.byref(n), None, 0, msg, 256) != 0:
+        raise ReaxError(msg.value.decode())
+    buf = C.create_string_buffer(16 * n.value)
+    L.rg_ffield_info((path or DEFAULT_FFIELD).encode(), C.byref(n), buf, 16, None, 0)
+    return [buf.raw[16 * k:16 * (k + 1)].split(b"\0")[0].decode() for k in range(n.value)]
 
 
 def default_params(**kw) -> Params:
@@ -171,6 +186,13 @@ class ReaxGPU:
         out = np.zeros(len(self.elements))
         self._chk(self.L.rg_extract(self.h, name.encode(), _dp(out)), "rg_extract")
         return out
+
+    def set_masses(self, masses):
+        """Integrator masses per ffield type (default: the force field's)."""
+        m = np.ascontiguousarray(masses, np.float64)
+        if m.shape != (len(self.elements),):
+            raise ValueError("one mass per force-field type")
+        self._chk(self.L.rg_set_masses(self.h, _dp(m)), "rg_set_masses")
 
     def set_box(self, box):
         box = np.ascontiguousarray(box, np.float64)

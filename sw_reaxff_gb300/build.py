@@ -65,5 +65,32 @@ def build(force: bool = False, verbose_ptxas: bool = False) -> str:
     return OUT
 
 
+HOST = os.path.join(HERE, "host")
+REAX_MD = os.path.join(HERE, "reax_md")
+
+
+def build_host(force: bool = False) -> str:
+    """The C++ host styles (host/reax_styles.*) and the reax_md deck driver,
+    linked against libreaxgpu.so (g++, rpath to this directory)."""
+    lib = build()
+    srcs = [os.path.join(HOST, f) for f in ("reax_styles.cpp", "reax_md.cpp")]
+    deps = srcs + [os.path.join(HOST, "reax_styles.h"), lib,
+                   os.path.join(HERE, "..", "include", "reaxgpu.h")]
+    if not force and os.path.exists(REAX_MD) and \
+            all(os.path.getmtime(REAX_MD) >= os.path.getmtime(d) for d in deps):
+        return REAX_MD
+    cxx = os.environ.get("CXX") or shutil.which("g++") or "g++"
+    cmd = [cxx, "-O2", "-std=c++17", "-Wall", "-Wextra", "-o", REAX_MD, *srcs,
+           "-I", os.path.join(HERE, "..", "include"), "-L", HERE, "-lreaxgpu",
+           "-Wl,-rpath,$ORIGIN"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"g++ failed:\n{r.stdout}\n{r.stderr}")
+    if r.stderr.strip():
+        sys.stderr.write(r.stderr)
+    return REAX_MD
+
+
 if __name__ == "__main__":
     print(build(force="--force" in sys.argv, verbose_ptxas="--ptxas" in sys.argv))
+    print(build_host(force="--force" in sys.argv))

@@ -5,7 +5,7 @@
 //  k_atom_energy: bond energy, lone pair, over/under-coordination and
 //      polarisation, Merge_Bonds_Atom_Energy_C_New (reaxc_multi_body_sw64.c:21-333)
 //  k_hbonds: Hydrogen_Bonds_C (reaxc_hydrogen_bonds_sw64.c:146-248)
-//  k_valence_torsion: Merge_Torsion_Valence_Angles
+//  k_vt_* / k_valence / k_torsion: Merge_Torsion_Valence_Angles
 //      (reaxc_torsion_angles_sw64.c:813-1367) with Calculate_Omega (:21-102)
 //  k_dbond: Add_All_dBond_to_Forces_C (reaxc_forces_sw64.c:499-588)
 //
@@ -13,6 +13,8 @@
 // reference's ghost atoms become (atom, periodic image) pairs carried in the
 // bond entries, so forces and CdDelta land directly on the owning atoms.
 // Scattered accumulations use FP64 atomics.
+#include <type_traits>
+
 #include "rg_internal.h"
 
 namespace {
@@ -23,8 +25,10 @@ constexpr double KCALpMOL_to_EV = 23.02;        // reaxc_defs_sunway.h:69
 constexpr double HB_THRESHOLD = 1e-2;           // reaxc_defs_sunway.h:91
 constexpr double MIN_SINE = 1e-10;
 
-__device__ __forceinline__ double deg2rad(double a) { return a * constPI / 180.0; }
-__device__ __forceinline__ double sqr(double x) { return x * x; }
+template <typename R>
+__device__ __forceinline__ R deg2rad(R a) { return a * R(constPI) / R(180); }
+template <typename R>
+__device__ __forceinline__ R sqr(R x) { return x * x; }
 
 // per-block reduction of one value into dst (FP64 atomic)
 __device__ __forceinline__ void block_add(double v, double *dst) {
@@ -67,18 +71,19 @@ __device__ __forceinline__ bool tag_first(const Dev &d, int i, int j, uint32_t e
 }
 
 // Calculate_Theta / Calculate_dCos_Theta, reaxc_valence_angles_sunway.cpp:49-79
-__device__ __forceinline__ void theta_dcos(const double *dji, double d_ji, const double *djk,
-                                           double d_jk, double &theta, double &cos_theta,
-                                           double *di, double *dj, double *dk) {
-  const double dot = dji[0] * djk[0] + dji[1] * djk[1] + dji[2] * djk[2];
+// (R = double: the FP64 form; R = float: the mixed form)
+template <typename R>
+__device__ __forceinline__ void theta_dcos(const R *dji, R d_ji, const R *djk, R d_jk, R &theta,
+                                           R &cos_theta, R *di, R *dj, R *dk) {
+  const R dot = dji[0] * djk[0] + dji[1] * djk[1] + dji[2] * djk[2];
   cos_theta = dot / (d_ji * d_jk);
-  if (cos_theta > 1.) cos_theta = 1.0;
-  if (cos_theta < -1.) cos_theta = -1.0;
+  if (cos_theta > R(1)) cos_theta = R(1);
+  if (cos_theta < R(-1)) cos_theta = R(-1);
   theta = acos(cos_theta);
-  const double sqr_d_ji = d_ji * d_ji, sqr_d_jk = d_jk * d_jk;
-  const double inv_dists = 1.0 / (d_ji * d_jk);
-  const double inv_dists3 = inv_dists * inv_dists * inv_dists;
-  const double Cdot_inv3 = dot * inv_dists3;
+  const R sqr_d_ji = d_ji * d_ji, sqr_d_jk = d_jk * d_jk;
+  const R inv_dists = R(1) / (d_ji * d_jk);
+  const R inv_dists3 = inv_dists * inv_dists * inv_dists;
+  const R Cdot_inv3 = dot * inv_dists3;
 #pragma unroll
   for (int t = 0; t < 3; ++t) {
     di[t] = djk[t] * inv_dists - Cdot_inv3 * sqr_d_jk * dji[t];
@@ -357,6 +362,10 @@ __device__ __forceinline__ double warp_sum_d(double v) {
   return v;
 }
 
+// R = double: FP64 form; R = float (mixed form): the angle, the exponentials
+// and the force factors in FP32 from the FP64 displacement and bond order;
+// accumulation in FP64
+template <typename R>
 __global__ void __launch_bounds__(256) k_hbonds(Dev d, int eflag) {
   const int lane = threadIdx.x & 31;
   const int j = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -374,10 +383,11 @@ __global__ void __launch_bounds__(256) k_hbonds(Dev d, int eflag) {
       const long long s = (long long)q * n + j;
       const int i = nbr_of(d.b_nbr[s]);
       const int ti = d.ts[i];
-      const double BO = d.b_BO[s];
-      if (F.sbp[ti].p_hbond != 2 || !(BO >= HB_THRESHOLD)) continue;
-      const double dij[3] = {d.b_dx[s], d.b_dy[s], d.b_dz[s]};
-      const double r_ij = d.b_d[s];
+      const double BO64 = d.b_BO[s];
+      if (F.sbp[ti].p_hbond != 2 || !(BO64 >= HB_THRESHOLD)) continue;
+      const R BO = (R)BO64;
+      const R dij[3] = {(R)d.b_dx[s], (R)d.b_dy[s], (R)d.b_dz[s]};
+      const R r_ij = (R)d.b_d[s];
       const int tag_i = d.tags[i];
       double fix = 0, fiy = 0, fiz = 0, cdbo = 0;
       for (int pk = lane; pk < nh; pk += 32) {
@@ -389,34 +399,38 @@ __global__ void __launch_bounds__(256) k_hbonds(Dev d, int eflag) {
         int sx, sy, sz;
         img_unpack((int)(ek & 255u), &sx, &sy, &sz);
         const double4 xk = d.xs[k];
-        double djk[3];
-        djk[0] = __dsub_rn(__dadd_rn(xk.x, sx * d.L[0]), xj.x);
-        djk[1] = __dsub_rn(__dadd_rn(xk.y, sy * d.L[1]), xj.y);
-        djk[2] = __dsub_rn(__dadd_rn(xk.z, sz * d.L[2]), xj.z);
-        const double r_jk = __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(djk[0], djk[0]),
-                                                           __dmul_rn(djk[1], djk[1])),
-                                                 __dmul_rn(djk[2], djk[2])));
-        double theta, cos_theta, di[3], djv[3], dk[3];
-        theta_dcos(dij, r_ij, djk, r_jk, theta, cos_theta, di, djv, dk);
-        const double sin_theta2 = sin(theta / 2.0);
-        double sin_xhz4 = sqr(sin_theta2);
+        double dk64[3];
+        dk64[0] = __dsub_rn(__dadd_rn(xk.x, sx * d.L[0]), xj.x);
+        dk64[1] = __dsub_rn(__dadd_rn(xk.y, sy * d.L[1]), xj.y);
+        dk64[2] = __dsub_rn(__dadd_rn(xk.z, sz * d.L[2]), xj.z);
+        const double r64 = __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(dk64[0], dk64[0]),
+                                                          __dmul_rn(dk64[1], dk64[1])),
+                                                __dmul_rn(dk64[2], dk64[2])));
+        const R djk[3] = {(R)dk64[0], (R)dk64[1], (R)dk64[2]};
+        const R r_jk = (R)r64;
+        R theta, cos_theta, di[3], djv[3], dk[3];
+        theta_dcos<R>(dij, r_ij, djk, r_jk, theta, cos_theta, di, djv, dk);
+        const R sin_theta2 = sin(theta / R(2));
+        R sin_xhz4 = sqr(sin_theta2);
         sin_xhz4 *= sin_xhz4;
-        const double cos_xhz1 = 1.0 - cos_theta;
-        const double exp_hb2 = exp(-hbp.p_hb2 * BO);
-        const double exp_hb3 = exp(-hbp.p_hb3 * (hbp.r0_hb / r_jk + r_jk / hbp.r0_hb - 2.0));
-        const double e_hb = hbp.p_hb1 * (1.0 - exp_hb2) * exp_hb3 * sin_xhz4;
-        ehb += e_hb;
-        const double CEhb1 = hbp.p_hb1 * hbp.p_hb2 * exp_hb2 * exp_hb3 * sin_xhz4;
-        const double CEhb2 = -hbp.p_hb1 / 2.0 * (1.0 - exp_hb2) * exp_hb3 * cos_xhz1;
-        const double CEhb3 = -hbp.p_hb3 * (-hbp.r0_hb / sqr(r_jk) + 1.0 / hbp.r0_hb) * e_hb;
-        cdbo += CEhb1;
-        fix += CEhb2 * di[0]; fiy += CEhb2 * di[1]; fiz += CEhb2 * di[2];
-        const double c3 = CEhb3 / r_jk;
-        fjx += CEhb2 * djv[0] - c3 * djk[0];
-        fjy += CEhb2 * djv[1] - c3 * djk[1];
-        fjz += CEhb2 * djv[2] - c3 * djk[2];
-        add3(fC, n, k, 1.0, CEhb2 * dk[0] + c3 * djk[0], CEhb2 * dk[1] + c3 * djk[1],
-             CEhb2 * dk[2] + c3 * djk[2]);
+        const R cos_xhz1 = R(1) - cos_theta;
+        const R p_hb1 = (R)hbp.p_hb1, p_hb2 = (R)hbp.p_hb2, p_hb3 = (R)hbp.p_hb3;
+        const R r0_hb = (R)hbp.r0_hb;
+        const R exp_hb2 = exp(-p_hb2 * BO);
+        const R exp_hb3 = exp(-p_hb3 * (r0_hb / r_jk + r_jk / r0_hb - R(2)));
+        const R e_hb = p_hb1 * (R(1) - exp_hb2) * exp_hb3 * sin_xhz4;
+        ehb += (double)e_hb;
+        const R CEhb1 = p_hb1 * p_hb2 * exp_hb2 * exp_hb3 * sin_xhz4;
+        const R CEhb2 = -p_hb1 / R(2) * (R(1) - exp_hb2) * exp_hb3 * cos_xhz1;
+        const R CEhb3 = -p_hb3 * (-r0_hb / sqr(r_jk) + R(1) / r0_hb) * e_hb;
+        cdbo += (double)CEhb1;
+        fix += (double)(CEhb2 * di[0]); fiy += (double)(CEhb2 * di[1]); fiz += (double)(CEhb2 * di[2]);
+        const R c3 = CEhb3 / r_jk;
+        fjx += (double)(CEhb2 * djv[0] - c3 * djk[0]);
+        fjy += (double)(CEhb2 * djv[1] - c3 * djk[1]);
+        fjz += (double)(CEhb2 * djv[2] - c3 * djk[2]);
+        add3(fC, n, k, 1.0, (double)(CEhb2 * dk[0] + c3 * djk[0]), (double)(CEhb2 * dk[1] + c3 * djk[1]),
+             (double)(CEhb2 * dk[2] + c3 * djk[2]));
       }
       cdbo = warp_sum_d(cdbo);
       fix = warp_sum_d(fix);
@@ -440,50 +454,52 @@ __global__ void __launch_bounds__(256) k_hbonds(Dev d, int eflag) {
 
 // ------------------------------------------------------------------
 // Calculate_Omega, reaxc_torsion_angles_sw64.c:21-102
+template <typename R>
 struct Thb {
-  double theta, di[3], dj[3], dk[3];
+  R theta, di[3], dj[3], dk[3];
 };
 
-__device__ double calc_omega(const double *dvec_ij, double r_ij, const double *dvec_jk, double r_jk,
-                             const double *dvec_kl, double r_kl, const double *dvec_li, double r_li,
-                             const Thb &p_ijk, const Thb &p_jkl, double *doi, double *doj,
-                             double *dok, double *dol) {
-  double sin_ijk, cos_ijk, sin_jkl, cos_jkl;
+template <typename R>
+__device__ R calc_omega(const R *dvec_ij, R r_ij, const R *dvec_jk, R r_jk, const R *dvec_kl, R r_kl,
+                        const R *dvec_li, R r_li, const Thb<R> &p_ijk, const Thb<R> &p_jkl, R *doi,
+                        R *doj, R *dok, R *dol) {
+  R sin_ijk, cos_ijk, sin_jkl, cos_jkl;
   sincos(p_ijk.theta, &sin_ijk, &cos_ijk);
   sincos(p_jkl.theta, &sin_jkl, &cos_jkl);
-  const double dij_jk = dvec_ij[0] * dvec_jk[0] + dvec_ij[1] * dvec_jk[1] + dvec_ij[2] * dvec_jk[2];
-  const double djk_kl = dvec_jk[0] * dvec_kl[0] + dvec_jk[1] * dvec_kl[1] + dvec_jk[2] * dvec_kl[2];
-  const double dij_kl = dvec_ij[0] * dvec_kl[0] + dvec_ij[1] * dvec_kl[1] + dvec_ij[2] * dvec_kl[2];
-  const double unnorm_cos_omega = -dij_jk * djk_kl + sqr(r_jk) * dij_kl;
-  const double cr0 = dvec_jk[1] * dvec_kl[2] - dvec_jk[2] * dvec_kl[1];
-  const double cr1 = dvec_jk[2] * dvec_kl[0] - dvec_jk[0] * dvec_kl[2];
-  const double cr2 = dvec_jk[0] * dvec_kl[1] - dvec_jk[1] * dvec_kl[0];
-  const double unnorm_sin_omega = -r_jk * (dvec_ij[0] * cr0 + dvec_ij[1] * cr1 + dvec_ij[2] * cr2);
-  const double omega = atan2(unnorm_sin_omega, unnorm_cos_omega);
-  const double htra = r_ij + cos_ijk * (r_kl * cos_jkl - r_jk);
-  const double htrb = r_jk - r_ij * cos_ijk - r_kl * cos_jkl;
-  const double htrc = r_kl + cos_jkl * (r_ij * cos_ijk - r_jk);
-  const double hthd = r_ij * sin_ijk * (r_jk - r_kl * cos_jkl);
-  const double hthe = r_kl * sin_jkl * (r_jk - r_ij * cos_ijk);
-  const double hnra = r_kl * sin_ijk * sin_jkl;
-  const double hnrc = r_ij * sin_ijk * sin_jkl;
-  const double hnhd = r_ij * r_kl * cos_ijk * sin_jkl;
-  const double hnhe = r_ij * r_kl * sin_ijk * cos_jkl;
-  double poem = 2.0 * r_ij * r_kl * sin_ijk * sin_jkl;
-  if (poem < 1e-20) poem = 1e-20;
-  const double tel = sqr(r_ij) + sqr(r_jk) + sqr(r_kl) - sqr(r_li) -
-                     2.0 * (r_ij * r_jk * cos_ijk - r_ij * r_kl * cos_ijk * cos_jkl + r_jk * r_kl * cos_jkl);
-  double arg = tel / poem;
-  if (arg > 1.0) arg = 1.0;
-  if (arg < -1.0) arg = -1.0;
-  if (sin_ijk >= 0 && sin_ijk <= MIN_SINE) sin_ijk = MIN_SINE;
-  else if (sin_ijk <= 0 && sin_ijk >= -MIN_SINE) sin_ijk = -MIN_SINE;
-  if (sin_jkl >= 0 && sin_jkl <= MIN_SINE) sin_jkl = MIN_SINE;
-  else if (sin_jkl <= 0 && sin_jkl >= -MIN_SINE) sin_jkl = -MIN_SINE;
-  const double p2 = 2.0 / poem;
-  const double a1 = (htra - arg * hnra) / r_ij, a2 = (hthd - arg * hnhd) / sin_ijk;
-  const double a3 = (hthe - arg * hnhe) / sin_jkl, a4 = (htrc - arg * hnrc) / r_kl;
-  const double a5 = htrb / r_jk;
+  const R dij_jk = dvec_ij[0] * dvec_jk[0] + dvec_ij[1] * dvec_jk[1] + dvec_ij[2] * dvec_jk[2];
+  const R djk_kl = dvec_jk[0] * dvec_kl[0] + dvec_jk[1] * dvec_kl[1] + dvec_jk[2] * dvec_kl[2];
+  const R dij_kl = dvec_ij[0] * dvec_kl[0] + dvec_ij[1] * dvec_kl[1] + dvec_ij[2] * dvec_kl[2];
+  const R unnorm_cos_omega = -dij_jk * djk_kl + sqr(r_jk) * dij_kl;
+  const R cr0 = dvec_jk[1] * dvec_kl[2] - dvec_jk[2] * dvec_kl[1];
+  const R cr1 = dvec_jk[2] * dvec_kl[0] - dvec_jk[0] * dvec_kl[2];
+  const R cr2 = dvec_jk[0] * dvec_kl[1] - dvec_jk[1] * dvec_kl[0];
+  const R unnorm_sin_omega = -r_jk * (dvec_ij[0] * cr0 + dvec_ij[1] * cr1 + dvec_ij[2] * cr2);
+  const R omega = atan2(unnorm_sin_omega, unnorm_cos_omega);
+  const R htra = r_ij + cos_ijk * (r_kl * cos_jkl - r_jk);
+  const R htrb = r_jk - r_ij * cos_ijk - r_kl * cos_jkl;
+  const R htrc = r_kl + cos_jkl * (r_ij * cos_ijk - r_jk);
+  const R hthd = r_ij * sin_ijk * (r_jk - r_kl * cos_jkl);
+  const R hthe = r_kl * sin_jkl * (r_jk - r_ij * cos_ijk);
+  const R hnra = r_kl * sin_ijk * sin_jkl;
+  const R hnrc = r_ij * sin_ijk * sin_jkl;
+  const R hnhd = r_ij * r_kl * cos_ijk * sin_jkl;
+  const R hnhe = r_ij * r_kl * sin_ijk * cos_jkl;
+  R poem = R(2) * r_ij * r_kl * sin_ijk * sin_jkl;
+  if (poem < R(1e-20)) poem = R(1e-20);
+  const R tel = sqr(r_ij) + sqr(r_jk) + sqr(r_kl) - sqr(r_li) -
+                R(2) * (r_ij * r_jk * cos_ijk - r_ij * r_kl * cos_ijk * cos_jkl + r_jk * r_kl * cos_jkl);
+  R arg = tel / poem;
+  if (arg > R(1)) arg = R(1);
+  if (arg < R(-1)) arg = R(-1);
+  const R ms = (R)MIN_SINE;
+  if (sin_ijk >= R(0) && sin_ijk <= ms) sin_ijk = ms;
+  else if (sin_ijk <= R(0) && sin_ijk >= -ms) sin_ijk = -ms;
+  if (sin_jkl >= R(0) && sin_jkl <= ms) sin_jkl = ms;
+  else if (sin_jkl <= R(0) && sin_jkl >= -ms) sin_jkl = -ms;
+  const R p2 = R(2) / poem;
+  const R a1 = (htra - arg * hnra) / r_ij, a2 = (hthd - arg * hnhd) / sin_ijk;
+  const R a3 = (hthe - arg * hnhe) / sin_jkl, a4 = (htrc - arg * hnrc) / r_kl;
+  const R a5 = htrb / r_jk;
 #pragma unroll
   for (int t = 0; t < 3; ++t) {
     doi[t] = p2 * (a1 * dvec_ij[t] - dvec_li[t] - a2 * p_ijk.dk[t]);
@@ -492,293 +508,6 @@ __device__ double calc_omega(const double *dvec_ij, double r_ij, const double *d
     dol[t] = p2 * (a4 * dvec_kl[t] + dvec_li[t] - a3 * p_jkl.dk[t]);
   }
   return omega;
-}
-
-// ------------------------------------------------------------------
-// valence + penalty + coalition + torsion + conjugation:
-// one thread per (centre j, bond pk of j)
-
-__global__ void __launch_bounds__(128) k_valence_torsion(Dev d, int eflag) {
-  const int n = d.n;
-  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  const int j = (int)(t % n), kk = (int)(t / n);
-  double e_ang = 0, e_pen = 0, e_coa = 0, e_tor = 0, e_con = 0;
-  const bool active = (kk < d.bond_cap) && (j < n) && (kk < min(d.nbonds[j], d.bond_cap));
-  if (active) {
-    const ForceField &F = *d.ff;
-    const Control &C = *d.ctl;
-    const double p_tor2 = F.gp[23], p_tor3 = F.gp[24], p_tor4 = F.gp[25];
-    const double p_cot2 = F.gp[27], p_val6 = F.gp[14], p_val8 = F.gp[33];
-    const double p_val9 = F.gp[16], p_val10 = F.gp[17];
-    const double p_pen2 = F.gp[19], p_pen3 = F.gp[20], p_pen4 = F.gp[21];
-    const double p_coa2 = F.gp[2], p_coa3 = F.gp[38], p_coa4 = F.gp[30];
-    const double thb_cut = C.thb_cut, thb_cutsq = C.thb_cutsq;
-    double *fC = d.fC;
-    double *CdD = d.fC + 3 * (long long)n;
-    const int nbj = min(d.nbonds[j], d.bond_cap);
-    const int tj = d.ts[j];
-    const long long spk = (long long)kk * n + j;
-    const double BO_jk = d.b_BO[spk];
-    const double BOA_jk = BO_jk - thb_cut;
-    if (BOA_jk > 0.0 && d.b_sym[spk] >= 0) {
-      const uint32_t ejk = d.b_nbr[spk];
-      const int k = nbr_of(ejk), tk = d.ts[k];
-      const int nbk = min(d.nbonds[k], d.bond_cap);
-      const long long spj = d.b_sym[spk];  // j on k's list
-      // per-centre quantities (SBO etc.), recomputed per thread
-      const double Delta_j = d.Delta_boc[j];
-      const double p_val3 = F.sbp[tj].p_val3, p_val5 = F.sbp[tj].p_val5;
-      double SBOp = 0, prod_SBO = 1;
-      for (int q = 0; q < nbj; ++q) {
-        const long long sq = (long long)q * n + j;
-        SBOp += d.b_BOpi[sq] + d.b_BOpi2[sq];
-        double tmp = sqr(d.b_BO[sq]);
-        tmp *= tmp;
-        tmp *= tmp;
-        prod_SBO *= exp(-tmp);
-      }
-      double vlpadj, dSBO2;
-      if (d.vlpex[j] >= 0) {
-        vlpadj = 0;
-        dSBO2 = prod_SBO - 1;
-      } else {
-        vlpadj = d.nlp[j];
-        dSBO2 = (prod_SBO - 1) * (1 - p_val8 * d.dDelta_lp[j]);
-      }
-      const double SBO = SBOp + (1 - prod_SBO) * (-Delta_j - p_val8 * vlpadj);
-      const double dSBO1 = -8 * prod_SBO * (Delta_j + p_val8 * vlpadj);
-      double SBO2, CSBO2;
-      if (SBO <= 0) SBO2 = 0, CSBO2 = 0;
-      else if (SBO > 0 && SBO <= 1) {
-        SBO2 = pow(SBO, p_val9);
-        CSBO2 = p_val9 * pow(SBO, p_val9 - 1);
-      } else if (SBO > 1 && SBO < 2) {
-        SBO2 = 2 - pow(2 - SBO, p_val9);
-        CSBO2 = p_val9 * pow(2 - SBO, p_val9 - 1);
-      } else SBO2 = 2, CSBO2 = 0;
-      const double expval6 = exp(p_val6 * Delta_j);
-      const double Delta_k = d.Delta_boc[k];
-      const double r_jk = d.b_d[spk];
-      const double djk[3] = {d.b_dx[spk], d.b_dy[spk], d.b_dz[spk]};
-      const double exp_tor2_jk = exp(-p_tor2 * BOA_jk);
-      const double exp_cot2_jk = exp(-p_cot2 * sqr(BOA_jk - 1.5));
-      const double exp_tor3_DjDk = exp(-p_tor3 * (Delta_j + Delta_k));
-      const double exp_tor4_DjDk = exp(p_tor4 * (Delta_j + Delta_k));
-      const double exp_tor34_inv = 1.0 / (1.0 + exp_tor3_DjDk + exp_tor4_DjDk);
-      const double f11_DjDk = (2.0 + exp_tor3_DjDk) * exp_tor34_inv;
-      const bool do_tor = tag_first(d, j, k, ejk);
-      const double BOpi_jk = d.b_BOpi[spk];
-      int sjk[3];
-      img_unpack((int)(ejk & 255u), &sjk[0], &sjk[1], &sjk[2]);
-      const double dpj[3] = {d.b_dx[spj], d.b_dy[spj], d.b_dz[spj]};
-      const double r_pj = d.b_d[spj];
-      for (int ph = 0; ph < nbj; ++ph) {
-        if (ph == kk) continue;
-        const long long sph = (long long)ph * n + j;
-        const double BO_hj = d.b_BO[sph];
-        const double BOA_hj = BO_hj - thb_cut;
-        const uint32_t ehj = d.b_nbr[sph];
-        const int h = nbr_of(ehj), th = d.ts[h];
-        const double dhj[3] = {d.b_dx[sph], d.b_dy[sph], d.b_dz[sph]};
-        const double r_hj = d.b_d[sph];
-        Thb p_hjk;
-        double cos_theta_hjk;
-        theta_dcos(djk, r_jk, dhj, r_hj, p_hjk.theta, cos_theta_hjk, p_hjk.di, p_hjk.dj, p_hjk.dk);
-        const double theta_hjk = p_hjk.theta;
-        double sin_theta_hjk = sin(theta_hjk);
-        if (sin_theta_hjk < 1.0e-5) sin_theta_hjk = 1.0e-5;
-        // valence angle h-j-k, each unordered bond pair once
-        if (ph > kk && BO_jk > thb_cut && BO_hj > thb_cut && BO_jk * BO_hj > thb_cutsq) {
-          const Thbh &thbh = F.thbp[tk][tj][th];
-          for (int cnt = 0; cnt < thbh.cnt; ++cnt) {
-            const Thbp &tp = thbh.prm[cnt];
-            if (!(fabs(tp.p_val1) > 0.001)) continue;
-            const double p_val1 = tp.p_val1, p_val2 = tp.p_val2, p_val4 = tp.p_val4, p_val7 = tp.p_val7;
-            const double theta_00 = tp.theta_00;
-            const double exp3jk = exp(-p_val3 * pow(BOA_jk, p_val4));
-            const double f7_jk = 1.0 - exp3jk;
-            const double Cf7jk = p_val3 * p_val4 * pow(BOA_jk, p_val4 - 1.0) * exp3jk;
-            const double exp3hj = exp(-p_val3 * pow(BOA_hj, p_val4));
-            const double f7_hj = 1.0 - exp3hj;
-            const double Cf7hj = p_val3 * p_val4 * pow(BOA_hj, p_val4 - 1.0) * exp3hj;
-            const double expval7 = exp(-p_val7 * Delta_j);
-            const double trm8 = 1.0 + expval6 + expval7;
-            const double f8_Dj = p_val5 - ((p_val5 - 1.0) * (2.0 + expval6) / trm8);
-            const double Cf8j = ((1.0 - p_val5) / sqr(trm8)) *
-                                (p_val6 * expval6 * trm8 - (2.0 + expval6) * (p_val6 * expval6 - p_val7 * expval7));
-            double theta_0 = 180.0 - theta_00 * (1.0 - exp(-p_val10 * (2.0 - SBO2)));
-            theta_0 = deg2rad(theta_0);
-            const double expval2theta = exp(-p_val2 * sqr(theta_0 - theta_hjk));
-            const double expval12theta = (p_val1 >= 0) ? p_val1 * (1.0 - expval2theta) : p_val1 * -expval2theta;
-            const double CEval1 = Cf7jk * f7_hj * f8_Dj * expval12theta;
-            const double CEval2 = Cf7hj * f7_jk * f8_Dj * expval12theta;
-            const double CEval3 = Cf8j * f7_hj * f7_jk * expval12theta;
-            const double CEval4 = -2.0 * p_val1 * p_val2 * f7_jk * f7_hj * f8_Dj * expval2theta * (theta_0 - theta_hjk);
-            const double Ctheta_0 = p_val10 * deg2rad(theta_00) * exp(-p_val10 * (2.0 - SBO2));
-            const double CEval5 = -CEval4 * Ctheta_0 * CSBO2;
-            const double CEval6 = CEval5 * dSBO1;
-            const double CEval7 = CEval5 * dSBO2;
-            const double CEval8 = -CEval4 / sin_theta_hjk;
-            e_ang += f7_jk * f7_hj * f8_Dj * expval12theta;
-            const double p_pen1 = tp.p_pen1;
-            const double exp_pen2jk = exp(-p_pen2 * sqr(BOA_jk - 2.0));
-            const double exp_pen2hj = exp(-p_pen2 * sqr(BOA_hj - 2.0));
-            const double exp_pen3 = exp(-p_pen3 * d.Delta[j]);
-            const double exp_pen4 = exp(p_pen4 * d.Delta[j]);
-            const double trm_pen34 = 1.0 + exp_pen3 + exp_pen4;
-            const double f9_Dj = (2.0 + exp_pen3) / trm_pen34;
-            const double Cf9j = (-p_pen3 * exp_pen3 * trm_pen34 -
-                                 (2.0 + exp_pen3) * (-p_pen3 * exp_pen3 + p_pen4 * exp_pen4)) / sqr(trm_pen34);
-            const double epen = p_pen1 * f9_Dj * exp_pen2jk * exp_pen2hj;
-            e_pen += epen;
-            const double CEpen1 = epen * Cf9j / f9_Dj;
-            const double temp = -2.0 * p_pen2 * epen;
-            const double CEpen2 = temp * (BOA_jk - 2.0);
-            const double CEpen3 = temp * (BOA_hj - 2.0);
-            const double p_coa1 = tp.p_coa1;
-            const double exp_coa2 = exp(p_coa2 * d.Delta_val[j]);
-            const double bo0k = d.bo0[k], bo0h = d.bo0[h];
-            const double ecoa = p_coa1 / (1. + exp_coa2) * exp(-p_coa3 * sqr(bo0k - BOA_jk)) *
-                                exp(-p_coa3 * sqr(bo0h - BOA_hj)) * exp(-p_coa4 * sqr(BOA_jk - 1.5)) *
-                                exp(-p_coa4 * sqr(BOA_hj - 1.5));
-            e_coa += ecoa;
-            const double CEcoa1 = -2 * p_coa4 * (BOA_jk - 1.5) * ecoa;
-            const double CEcoa2 = -2 * p_coa4 * (BOA_hj - 1.5) * ecoa;
-            const double CEcoa3 = -p_coa2 * exp_coa2 * ecoa / (1 + exp_coa2);
-            const double CEcoa4 = -2 * p_coa3 * (bo0k - BOA_jk) * ecoa;
-            const double CEcoa5 = -2 * p_coa3 * (bo0h - BOA_hj) * ecoa;
-            atomicAdd(&d.b_Cdbo[spk], CEval1 + CEpen2 + (CEcoa1 - CEcoa4));
-            atomicAdd(&d.b_Cdbo[sph], CEval2 + CEpen3 + (CEcoa2 - CEcoa5));
-            atomicAdd(&CdD[j], (CEval3 + CEval7) + CEpen1 + CEcoa3);
-            atomicAdd(&CdD[k], CEcoa4);
-            atomicAdd(&CdD[h], CEcoa5);
-            for (int q = 0; q < nbj; ++q) {
-              const long long sq = (long long)q * n + j;
-              const double b = d.b_BO[sq];
-              const double b3 = b * b * b;
-              atomicAdd(&d.b_Cdbo[sq], CEval6 * (b3 * b3 * b));
-              atomicAdd(&d.b_Cdbopi[sq], CEval5);
-              atomicAdd(&d.b_Cdbopi2[sq], CEval5);
-            }
-            add3(fC, n, k, CEval8, p_hjk.di[0], p_hjk.di[1], p_hjk.di[2]);
-            add3(fC, n, j, CEval8, p_hjk.dj[0], p_hjk.dj[1], p_hjk.dj[2]);
-            add3(fC, n, h, CEval8, p_hjk.dk[0], p_hjk.dk[1], p_hjk.dk[2]);
-          }
-        }
-        // torsion h-j-k-l about the central bond j-k (counted at one end)
-        if (!do_tor) continue;
-        if (!(BO_hj > thb_cut) || nbk <= 0) continue;
-        const int i = h, ti = th;
-        const double r_ij = r_hj;
-        const double BOA_ij = BOA_hj;
-        const double theta_ijk = theta_hjk;
-        double sin_ijk, cos_ijk, tan_ijk_i;
-        sincos(theta_ijk, &sin_ijk, &cos_ijk);
-        if (sin_ijk >= 0 && sin_ijk <= MIN_SINE) tan_ijk_i = cos_ijk / MIN_SINE;
-        else if (sin_ijk <= 0 && sin_ijk >= -MIN_SINE) tan_ijk_i = cos_ijk / -MIN_SINE;
-        else tan_ijk_i = cos_ijk / sin_ijk;
-        const double exp_tor2_ij = exp(-p_tor2 * BOA_ij);
-        const double exp_cot2_ij = exp(-p_cot2 * sqr(BOA_ij - 1.5));
-        int shj[3];
-        img_unpack((int)(ehj & 255u), &shj[0], &shj[1], &shj[2]);
-        for (int pw = 0; pw < nbk; ++pw) {
-          const long long spw = (long long)pw * n + k;
-          if (spw == spj) continue;
-          const double BO_kl = d.b_BO[spw];
-          const uint32_t ekl = d.b_nbr[spw];
-          const int l = nbr_of(ekl), tl = d.ts[l];
-          // i and l are the same atom instance when owners and images agree
-          int skl[3];
-          img_unpack((int)(ekl & 255u), &skl[0], &skl[1], &skl[2]);
-          const bool same = (l == i) && (sjk[0] + skl[0] == shj[0]) && (sjk[1] + skl[1] == shj[1]) &&
-                            (sjk[2] + skl[2] == shj[2]);
-          const Fbh &fbh = F.fbp[ti][tj][tk][tl];
-          if (same || !fbh.cnt || !(BO_kl > thb_cut) || !(BO_hj * BO_jk * BO_kl > thb_cut)) continue;
-          const Fbp &fbp = fbh.prm;
-          const double dkl[3] = {d.b_dx[spw], d.b_dy[spw], d.b_dz[spw]};
-          const double r_kl = d.b_d[spw];
-          Thb p_jkl;
-          double cos_theta_jkl;
-          theta_dcos(dpj, r_pj, dkl, r_kl, p_jkl.theta, cos_theta_jkl, p_jkl.di, p_jkl.dj, p_jkl.dk);
-          const double BOA_kl = BO_kl - thb_cut;
-          double sin_jkl, cos_jkl, tan_jkl_i;
-          sincos(p_jkl.theta, &sin_jkl, &cos_jkl);
-          if (sin_jkl >= 0 && sin_jkl <= MIN_SINE) tan_jkl_i = cos_jkl / MIN_SINE;
-          else if (sin_jkl <= 0 && sin_jkl >= -MIN_SINE) tan_jkl_i = cos_jkl / -MIN_SINE;
-          else tan_jkl_i = cos_jkl / sin_jkl;
-          double dli[3];
-          dli[0] = dhj[0] - djk[0] - dkl[0];
-          dli[1] = dhj[1] - djk[1] - dkl[1];
-          dli[2] = dhj[2] - djk[2] - dkl[2];
-          const double r_li = sqrt(sqr(dli[0]) + sqr(dli[1]) + sqr(dli[2]));
-          double doi[3], doj[3], dok[3], dol[3];
-          const double omega = calc_omega(dhj, r_ij, djk, r_jk, dkl, r_kl, dli, r_li, p_hjk, p_jkl,
-                                          doi, doj, dok, dol);
-          const double cos_omega = cos(omega);
-          const double cos2omega = cos(2. * omega);
-          const double cos3omega = cos(3. * omega);
-          const double exp_tor1 = exp(fbp.p_tor1 * sqr(2.0 - BOpi_jk - f11_DjDk));
-          const double exp_tor2_kl = exp(-p_tor2 * BOA_kl);
-          const double exp_cot2_kl = exp(-p_cot2 * sqr(BOA_kl - 1.5));
-          const double fn10 = (1.0 - exp_tor2_ij) * (1.0 - exp_tor2_jk) * (1.0 - exp_tor2_kl);
-          const double CV = 0.5 * (fbp.V1 * (1.0 + cos_omega) + fbp.V2 * exp_tor1 * (1.0 - cos2omega) +
-                                   fbp.V3 * (1.0 + cos3omega));
-          e_tor += fn10 * sin_ijk * sin_jkl * CV;
-          const double dfn11 = (-p_tor3 * exp_tor3_DjDk +
-                                (p_tor3 * exp_tor3_DjDk - p_tor4 * exp_tor4_DjDk) * (2.0 + exp_tor3_DjDk) * exp_tor34_inv) *
-                               exp_tor34_inv;
-          const double CEtors1 = sin_ijk * sin_jkl * CV;
-          const double CEtors2 = -fn10 * 2.0 * fbp.p_tor1 * fbp.V2 * exp_tor1 * (2.0 - BOpi_jk - f11_DjDk) *
-                                 (1.0 - sqr(cos_omega)) * sin_ijk * sin_jkl;
-          const double CEtors3 = CEtors2 * dfn11;
-          const double CEtors4 = CEtors1 * p_tor2 * exp_tor2_ij * (1.0 - exp_tor2_jk) * (1.0 - exp_tor2_kl);
-          const double CEtors5 = CEtors1 * p_tor2 * (1.0 - exp_tor2_ij) * exp_tor2_jk * (1.0 - exp_tor2_kl);
-          const double CEtors6 = CEtors1 * p_tor2 * (1.0 - exp_tor2_ij) * (1.0 - exp_tor2_jk) * exp_tor2_kl;
-          const double cmn = -fn10 * CV;
-          const double CEtors7 = cmn * sin_jkl * tan_ijk_i;
-          const double CEtors8 = cmn * sin_ijk * tan_jkl_i;
-          const double CEtors9 = fn10 * sin_ijk * sin_jkl *
-                                 (0.5 * fbp.V1 - 2.0 * fbp.V2 * exp_tor1 * cos_omega +
-                                  1.5 * fbp.V3 * (cos2omega + 2.0 * sqr(cos_omega)));
-          const double fn12 = exp_cot2_ij * exp_cot2_jk * exp_cot2_kl;
-          const double econ = fbp.p_cot1 * fn12 * (1.0 + (sqr(cos_omega) - 1.0) * sin_ijk * sin_jkl);
-          e_con += econ;
-          const double Cconj = -2.0 * fn12 * fbp.p_cot1 * p_cot2 * (1.0 + (sqr(cos_omega) - 1.0) * sin_ijk * sin_jkl);
-          const double CEconj1 = Cconj * (BOA_ij - 1.5e0);
-          const double CEconj2 = Cconj * (BOA_jk - 1.5e0);
-          const double CEconj3 = Cconj * (BOA_kl - 1.5e0);
-          const double CEconj4 = -fbp.p_cot1 * fn12 * (sqr(cos_omega) - 1.0) * sin_jkl * tan_ijk_i;
-          const double CEconj5 = -fbp.p_cot1 * fn12 * (sqr(cos_omega) - 1.0) * sin_ijk * tan_jkl_i;
-          const double CEconj6 = 2.0 * fbp.p_cot1 * fn12 * cos_omega * sin_ijk * sin_jkl;
-          atomicAdd(&d.b_Cdbopi[spk], CEtors2);
-          atomicAdd(&CdD[j], CEtors3);
-          atomicAdd(&CdD[k], CEtors3);
-          atomicAdd(&d.b_Cdbo[sph], CEtors4 + CEconj1);
-          atomicAdd(&d.b_Cdbo[spk], CEtors5 + CEconj2);
-          atomicAdd(&d.b_Cdbo[spw], CEtors6 + CEconj3);
-          const double c78 = CEtors7 + CEconj4, c85 = CEtors8 + CEconj5, c96 = CEtors9 + CEconj6;
-          add3(fC, n, i, 1.0, c78 * p_hjk.dk[0] + c96 * doi[0], c78 * p_hjk.dk[1] + c96 * doi[1],
-               c78 * p_hjk.dk[2] + c96 * doi[2]);
-          add3(fC, n, j, 1.0, c78 * p_hjk.dj[0] + c85 * p_jkl.di[0] + c96 * doj[0],
-               c78 * p_hjk.dj[1] + c85 * p_jkl.di[1] + c96 * doj[1],
-               c78 * p_hjk.dj[2] + c85 * p_jkl.di[2] + c96 * doj[2]);
-          add3(fC, n, k, 1.0, c78 * p_hjk.di[0] + c85 * p_jkl.dj[0] + c96 * dok[0],
-               c78 * p_hjk.di[1] + c85 * p_jkl.dj[1] + c96 * dok[1],
-               c78 * p_hjk.di[2] + c85 * p_jkl.dj[2] + c96 * dok[2]);
-          add3(fC, n, l, 1.0, c85 * p_jkl.dk[0] + c96 * dol[0], c85 * p_jkl.dk[1] + c96 * dol[1],
-               c85 * p_jkl.dk[2] + c96 * dol[2]);
-        }
-      }
-    }
-  }
-  if (eflag) {
-    block_add(e_ang, &d.energy[E_ANG]);
-    block_add(e_pen, &d.energy[E_PEN]);
-    block_add(e_coa, &d.energy[E_COA]);
-    block_add(e_tor, &d.energy[E_TOR]);
-    block_add(e_con, &d.energy[E_CON]);
-    block_add(e_ang + e_pen + e_coa + e_tor + e_con, &d.energy[E_ENG_VDWL]);
-  }
 }
 
 // ------------------------------------------------------------------
@@ -935,112 +664,130 @@ __global__ void k_vt_fill(Dev d) {
   vt_enumerate<true>(d, (int)(t % n), (int)(t / n), cv, ct, d.w_off_v[t], d.w_off_t[t]);
 }
 
-// one valence angle h-j-k (with its penalty and coalition terms)
-__global__ void __launch_bounds__(128) k_valence(Dev d, int eflag, long long nitems) {
-  const long long w = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  double e_ang = 0, e_pen = 0, e_coa = 0;
-  if (w < nitems) {
-    const unsigned long long it = d.w_val[w];
+// one valence angle h-j-k (with its penalty and coalition terms); R as in
+// k_hbonds: the per-angle arithmetic in R from the FP64 per-bond and
+// per-centre quantities, accumulation in FP64
+template <typename R>
+__device__ __forceinline__ void valence_item(const Dev &d, unsigned long long it, double &e_ang,
+                                             double &e_pen, double &e_coa) {
+  {
     const int j = (int)(it >> 16), kk = (int)((it >> 8) & 255), ph = (int)(it & 255);
     const int n = d.n;
     const ForceField &F = *d.ff;
     const double thb_cut = d.ctl->thb_cut;
-    const double p_val6 = F.gp[14], p_val10 = F.gp[17];
-    const double p_pen2 = F.gp[19], p_pen3 = F.gp[20], p_pen4 = F.gp[21];
-    const double p_coa2 = F.gp[2], p_coa3 = F.gp[38], p_coa4 = F.gp[30];
+    const R p_val6 = (R)F.gp[14], p_val10 = (R)F.gp[17];
+    const R p_pen2 = (R)F.gp[19], p_pen3 = (R)F.gp[20], p_pen4 = (R)F.gp[21];
+    const R p_coa2 = (R)F.gp[2], p_coa3 = (R)F.gp[38], p_coa4 = (R)F.gp[30];
     double *fC = d.fC;
     double *CdD = d.fC + 3 * (long long)n;
     const int tj = d.ts[j];
-    const double p_val3 = F.sbp[tj].p_val3, p_val5 = F.sbp[tj].p_val5;
-    const double SBO2 = d.c_sbo[j], CSBO2 = d.c_sbo[n + j];
-    const double dSBO1 = d.c_sbo[2 * n + j], dSBO2 = d.c_sbo[3 * n + j];
-    const double expval6 = d.c_sbo[4 * n + j];
-    const double Delta_j = d.Delta_boc[j];
+    const R p_val3 = (R)F.sbp[tj].p_val3, p_val5 = (R)F.sbp[tj].p_val5;
+    const R SBO2 = (R)d.c_sbo[j], CSBO2 = (R)d.c_sbo[n + j];
+    const R dSBO1 = (R)d.c_sbo[2 * n + j], dSBO2 = (R)d.c_sbo[3 * n + j];
+    const R expval6 = (R)d.c_sbo[4 * n + j];
+    const R Delta_j = (R)d.Delta_boc[j];
     const long long spk = (long long)kk * n + j, sph = (long long)ph * n + j;
     const int k = nbr_of(d.b_nbr[spk]), h = nbr_of(d.b_nbr[sph]);
     const int tk = d.ts[k], th = d.ts[h];
-    const double BOA_jk = d.b_BO[spk] - thb_cut, BOA_hj = d.b_BO[sph] - thb_cut;
-    const double djk[3] = {d.b_dx[spk], d.b_dy[spk], d.b_dz[spk]};
-    const double dhj[3] = {d.b_dx[sph], d.b_dy[sph], d.b_dz[sph]};
-    double theta_hjk, cos_theta_hjk, di[3], dj[3], dk[3];
-    theta_dcos(djk, d.b_d[spk], dhj, d.b_d[sph], theta_hjk, cos_theta_hjk, di, dj, dk);
-    double sin_theta_hjk = sin(theta_hjk);
-    if (sin_theta_hjk < 1.0e-5) sin_theta_hjk = 1.0e-5;
+    const R BOA_jk = (R)(d.b_BO[spk] - thb_cut), BOA_hj = (R)(d.b_BO[sph] - thb_cut);
+    const R djk[3] = {(R)d.b_dx[spk], (R)d.b_dy[spk], (R)d.b_dz[spk]};
+    const R dhj[3] = {(R)d.b_dx[sph], (R)d.b_dy[sph], (R)d.b_dz[sph]};
+    R theta_hjk, cos_theta_hjk, di[3], dj[3], dk[3];
+    theta_dcos<R>(djk, (R)d.b_d[spk], dhj, (R)d.b_d[sph], theta_hjk, cos_theta_hjk, di, dj, dk);
+    R sin_theta_hjk = sin(theta_hjk);
+    if (sin_theta_hjk < R(1.0e-5)) sin_theta_hjk = R(1.0e-5);
     const Thbh &thbh = F.thbp[tk][tj][th];
     const int nbj = min(d.nbonds[j], d.bond_cap);
+    const R Dj = (R)d.Delta[j], Dval_j = (R)d.Delta_val[j];
+    const R bo0k = (R)d.bo0[k], bo0h = (R)d.bo0[h];
     for (int cnt = 0; cnt < thbh.cnt; ++cnt) {
       const Thbp &tp = thbh.prm[cnt];
       if (!(fabs(tp.p_val1) > 0.001)) continue;
-      const double p_val1 = tp.p_val1, p_val2 = tp.p_val2, p_val4 = tp.p_val4, p_val7 = tp.p_val7;
-      const double theta_00 = tp.theta_00;
-      const double exp3jk = exp(-p_val3 * pow(BOA_jk, p_val4));
-      const double f7_jk = 1.0 - exp3jk;
-      const double Cf7jk = p_val3 * p_val4 * pow(BOA_jk, p_val4 - 1.0) * exp3jk;
-      const double exp3hj = exp(-p_val3 * pow(BOA_hj, p_val4));
-      const double f7_hj = 1.0 - exp3hj;
-      const double Cf7hj = p_val3 * p_val4 * pow(BOA_hj, p_val4 - 1.0) * exp3hj;
-      const double expval7 = exp(-p_val7 * Delta_j);
-      const double trm8 = 1.0 + expval6 + expval7;
-      const double f8_Dj = p_val5 - ((p_val5 - 1.0) * (2.0 + expval6) / trm8);
-      const double Cf8j = ((1.0 - p_val5) / sqr(trm8)) *
-                          (p_val6 * expval6 * trm8 - (2.0 + expval6) * (p_val6 * expval6 - p_val7 * expval7));
-      double theta_0 = 180.0 - theta_00 * (1.0 - exp(-p_val10 * (2.0 - SBO2)));
+      const R p_val1 = (R)tp.p_val1, p_val2 = (R)tp.p_val2, p_val4 = (R)tp.p_val4, p_val7 = (R)tp.p_val7;
+      const R theta_00 = (R)tp.theta_00;
+      const R exp3jk = exp(-p_val3 * pow(BOA_jk, p_val4));
+      const R f7_jk = R(1) - exp3jk;
+      const R Cf7jk = p_val3 * p_val4 * pow(BOA_jk, p_val4 - R(1)) * exp3jk;
+      const R exp3hj = exp(-p_val3 * pow(BOA_hj, p_val4));
+      const R f7_hj = R(1) - exp3hj;
+      const R Cf7hj = p_val3 * p_val4 * pow(BOA_hj, p_val4 - R(1)) * exp3hj;
+      const R expval7 = exp(-p_val7 * Delta_j);
+      const R trm8 = R(1) + expval6 + expval7;
+      const R f8_Dj = p_val5 - ((p_val5 - R(1)) * (R(2) + expval6) / trm8);
+      const R Cf8j = ((R(1) - p_val5) / sqr(trm8)) *
+                     (p_val6 * expval6 * trm8 - (R(2) + expval6) * (p_val6 * expval6 - p_val7 * expval7));
+      R theta_0 = R(180) - theta_00 * (R(1) - exp(-p_val10 * (R(2) - SBO2)));
       theta_0 = deg2rad(theta_0);
-      const double expval2theta = exp(-p_val2 * sqr(theta_0 - theta_hjk));
-      const double expval12theta = (p_val1 >= 0) ? p_val1 * (1.0 - expval2theta) : p_val1 * -expval2theta;
-      const double CEval1 = Cf7jk * f7_hj * f8_Dj * expval12theta;
-      const double CEval2 = Cf7hj * f7_jk * f8_Dj * expval12theta;
-      const double CEval3 = Cf8j * f7_hj * f7_jk * expval12theta;
-      const double CEval4 = -2.0 * p_val1 * p_val2 * f7_jk * f7_hj * f8_Dj * expval2theta * (theta_0 - theta_hjk);
-      const double Ctheta_0 = p_val10 * deg2rad(theta_00) * exp(-p_val10 * (2.0 - SBO2));
-      const double CEval5 = -CEval4 * Ctheta_0 * CSBO2;
-      const double CEval6 = CEval5 * dSBO1;
-      const double CEval7 = CEval5 * dSBO2;
-      const double CEval8 = -CEval4 / sin_theta_hjk;
-      e_ang += f7_jk * f7_hj * f8_Dj * expval12theta;
-      const double exp_pen2jk = exp(-p_pen2 * sqr(BOA_jk - 2.0));
-      const double exp_pen2hj = exp(-p_pen2 * sqr(BOA_hj - 2.0));
-      const double exp_pen3 = exp(-p_pen3 * d.Delta[j]);
-      const double exp_pen4 = exp(p_pen4 * d.Delta[j]);
-      const double trm_pen34 = 1.0 + exp_pen3 + exp_pen4;
-      const double f9_Dj = (2.0 + exp_pen3) / trm_pen34;
-      const double Cf9j = (-p_pen3 * exp_pen3 * trm_pen34 -
-                           (2.0 + exp_pen3) * (-p_pen3 * exp_pen3 + p_pen4 * exp_pen4)) / sqr(trm_pen34);
-      const double epen = tp.p_pen1 * f9_Dj * exp_pen2jk * exp_pen2hj;
-      e_pen += epen;
-      const double CEpen1 = epen * Cf9j / f9_Dj;
-      const double temp = -2.0 * p_pen2 * epen;
-      const double CEpen2 = temp * (BOA_jk - 2.0);
-      const double CEpen3 = temp * (BOA_hj - 2.0);
-      const double exp_coa2 = exp(p_coa2 * d.Delta_val[j]);
-      const double bo0k = d.bo0[k], bo0h = d.bo0[h];
-      const double ecoa = tp.p_coa1 / (1. + exp_coa2) * exp(-p_coa3 * sqr(bo0k - BOA_jk)) *
-                          exp(-p_coa3 * sqr(bo0h - BOA_hj)) * exp(-p_coa4 * sqr(BOA_jk - 1.5)) *
-                          exp(-p_coa4 * sqr(BOA_hj - 1.5));
-      e_coa += ecoa;
-      const double CEcoa1 = -2 * p_coa4 * (BOA_jk - 1.5) * ecoa;
-      const double CEcoa2 = -2 * p_coa4 * (BOA_hj - 1.5) * ecoa;
-      const double CEcoa3 = -p_coa2 * exp_coa2 * ecoa / (1 + exp_coa2);
-      const double CEcoa4 = -2 * p_coa3 * (bo0k - BOA_jk) * ecoa;
-      const double CEcoa5 = -2 * p_coa3 * (bo0h - BOA_hj) * ecoa;
-      atomicAdd(&d.b_Cdbo[spk], CEval1 + CEpen2 + (CEcoa1 - CEcoa4));
-      atomicAdd(&d.b_Cdbo[sph], CEval2 + CEpen3 + (CEcoa2 - CEcoa5));
-      atomicAdd(&CdD[j], (CEval3 + CEval7) + CEpen1 + CEcoa3);
-      atomicAdd(&CdD[k], CEcoa4);
-      atomicAdd(&CdD[h], CEcoa5);
+      const R expval2theta = exp(-p_val2 * sqr(theta_0 - theta_hjk));
+      const R expval12theta = (p_val1 >= R(0)) ? p_val1 * (R(1) - expval2theta) : p_val1 * -expval2theta;
+      const R CEval1 = Cf7jk * f7_hj * f8_Dj * expval12theta;
+      const R CEval2 = Cf7hj * f7_jk * f8_Dj * expval12theta;
+      const R CEval3 = Cf8j * f7_hj * f7_jk * expval12theta;
+      const R CEval4 = R(-2) * p_val1 * p_val2 * f7_jk * f7_hj * f8_Dj * expval2theta * (theta_0 - theta_hjk);
+      const R Ctheta_0 = p_val10 * deg2rad(theta_00) * exp(-p_val10 * (R(2) - SBO2));
+      const R CEval5 = -CEval4 * Ctheta_0 * CSBO2;
+      const R CEval6 = CEval5 * dSBO1;
+      const R CEval7 = CEval5 * dSBO2;
+      const R CEval8 = -CEval4 / sin_theta_hjk;
+      e_ang += (double)(f7_jk * f7_hj * f8_Dj * expval12theta);
+      const R exp_pen2jk = exp(-p_pen2 * sqr(BOA_jk - R(2)));
+      const R exp_pen2hj = exp(-p_pen2 * sqr(BOA_hj - R(2)));
+      const R exp_pen3 = exp(-p_pen3 * Dj);
+      const R exp_pen4 = exp(p_pen4 * Dj);
+      const R trm_pen34 = R(1) + exp_pen3 + exp_pen4;
+      const R f9_Dj = (R(2) + exp_pen3) / trm_pen34;
+      const R Cf9j = (-p_pen3 * exp_pen3 * trm_pen34 -
+                      (R(2) + exp_pen3) * (-p_pen3 * exp_pen3 + p_pen4 * exp_pen4)) / sqr(trm_pen34);
+      const R epen = (R)tp.p_pen1 * f9_Dj * exp_pen2jk * exp_pen2hj;
+      e_pen += (double)epen;
+      const R CEpen1 = epen * Cf9j / f9_Dj;
+      const R temp = R(-2) * p_pen2 * epen;
+      const R CEpen2 = temp * (BOA_jk - R(2));
+      const R CEpen3 = temp * (BOA_hj - R(2));
+      const R exp_coa2 = exp(p_coa2 * Dval_j);
+      const R ecoa = (R)tp.p_coa1 / (R(1) + exp_coa2) * exp(-p_coa3 * sqr(bo0k - BOA_jk)) *
+                     exp(-p_coa3 * sqr(bo0h - BOA_hj)) * exp(-p_coa4 * sqr(BOA_jk - R(1.5))) *
+                     exp(-p_coa4 * sqr(BOA_hj - R(1.5)));
+      e_coa += (double)ecoa;
+      const R CEcoa1 = R(-2) * p_coa4 * (BOA_jk - R(1.5)) * ecoa;
+      const R CEcoa2 = R(-2) * p_coa4 * (BOA_hj - R(1.5)) * ecoa;
+      const R CEcoa3 = -p_coa2 * exp_coa2 * ecoa / (R(1) + exp_coa2);
+      const R CEcoa4 = R(-2) * p_coa3 * (bo0k - BOA_jk) * ecoa;
+      const R CEcoa5 = R(-2) * p_coa3 * (bo0h - BOA_hj) * ecoa;
+      atomicAdd(&d.b_Cdbo[spk], (double)(CEval1 + CEpen2 + (CEcoa1 - CEcoa4)));
+      atomicAdd(&d.b_Cdbo[sph], (double)(CEval2 + CEpen3 + (CEcoa2 - CEcoa5)));
+      atomicAdd(&CdD[j], (double)((CEval3 + CEval7) + CEpen1 + CEcoa3));
+      atomicAdd(&CdD[k], (double)CEcoa4);
+      atomicAdd(&CdD[h], (double)CEcoa5);
       for (int q = 0; q < nbj; ++q) {
         const long long sq = (long long)q * n + j;
         const double b = d.b_BO[sq];
         const double b3 = b * b * b;
-        atomicAdd(&d.b_Cdbo[sq], CEval6 * (b3 * b3 * b));
-        atomicAdd(&d.b_Cdbopi[sq], CEval5);
-        atomicAdd(&d.b_Cdbopi2[sq], CEval5);
+        atomicAdd(&d.b_Cdbo[sq], (double)CEval6 * (b3 * b3 * b));
+        atomicAdd(&d.b_Cdbopi[sq], (double)CEval5);
+        atomicAdd(&d.b_Cdbopi2[sq], (double)CEval5);
       }
-      add3(fC, n, k, CEval8, di[0], di[1], di[2]);
-      add3(fC, n, j, CEval8, dj[0], dj[1], dj[2]);
-      add3(fC, n, h, CEval8, dk[0], dk[1], dk[2]);
+      const double c8 = (double)CEval8;
+      add3(fC, n, k, c8, (double)di[0], (double)di[1], (double)di[2]);
+      add3(fC, n, j, c8, (double)dj[0], (double)dj[1], (double)dj[2]);
+      add3(fC, n, h, c8, (double)dk[0], (double)dk[1], (double)dk[2]);
     }
   }
+}
+
+// FP32 is not used for angles within about 1.1 degrees of 0 or 180 (sine
+// below 0.02): there the reference's 1/sin factors (MIN_SINE clamps at
+// 1e-10) overflow FP32 and its cancellations lose the result.  The FP32
+// kernels queue those items for an FP64 pass.
+__device__ __forceinline__ bool near_linear(const Dev &d, long long sa, long long sb) {
+  const float ax = (float)d.b_dx[sa], ay = (float)d.b_dy[sa], az = (float)d.b_dz[sa];
+  const float bx = (float)d.b_dx[sb], by = (float)d.b_dy[sb], bz = (float)d.b_dz[sb];
+  const float c = (ax * bx + ay * by + az * bz) / ((float)d.b_d[sa] * (float)d.b_d[sb]);
+  return fabsf(c) > 0.9998f;
+}
+
+__device__ __forceinline__ void valence_energies(const Dev &d, int eflag, double e_ang, double e_pen,
+                                                 double e_coa) {
   if (eflag) {
     block_add(e_ang, &d.energy[E_ANG]);
     block_add(e_pen, &d.energy[E_PEN]);
@@ -1049,18 +796,47 @@ __global__ void __launch_bounds__(128) k_valence(Dev d, int eflag, long long nit
   }
 }
 
-// one torsion h-j-k-l (with its 4-body conjugation term)
-__global__ void __launch_bounds__(128) k_torsion(Dev d, int eflag, long long nitems) {
+template <typename R>
+__global__ void __launch_bounds__(128) k_valence(Dev d, int eflag, long long nitems) {
   const long long w = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  double e_tor = 0, e_con = 0;
+  double e_ang = 0, e_pen = 0, e_coa = 0;
   if (w < nitems) {
-    const unsigned long long it = d.w_tor[w];
+    const unsigned long long it = d.w_val[w];
+    if (std::is_same<R, float>::value) {
+      const int j = (int)(it >> 16), kk = (int)((it >> 8) & 255), ph = (int)(it & 255);
+      if (near_linear(d, (long long)kk * d.n + j, (long long)ph * d.n + j))
+        d.w_fb_val[atomicAdd(&d.fb_cnt[0], 1)] = it;
+      else
+        valence_item<R>(d, it, e_ang, e_pen, e_coa);
+    } else {
+      valence_item<R>(d, it, e_ang, e_pen, e_coa);
+    }
+  }
+  valence_energies(d, eflag, e_ang, e_pen, e_coa);
+}
+
+// the FP64 pass over the queued near-linear angles (grid-stride over the
+// device-side count)
+__global__ void __launch_bounds__(128) k_valence_fb(Dev d, int eflag) {
+  double e_ang = 0, e_pen = 0, e_coa = 0;
+  const long long cnt = d.fb_cnt[0];
+  for (long long w = (long long)blockIdx.x * blockDim.x + threadIdx.x; w < cnt;
+       w += (long long)gridDim.x * blockDim.x)
+    valence_item<double>(d, d.w_fb_val[w], e_ang, e_pen, e_coa);
+  valence_energies(d, eflag, e_ang, e_pen, e_coa);
+}
+
+// one torsion h-j-k-l (with its 4-body conjugation term); R as in k_valence
+template <typename R>
+__device__ __forceinline__ void torsion_item(const Dev &d, unsigned long long it, double &e_tor,
+                                             double &e_con) {
+  {
     const int j = (int)(it >> 24), kk = (int)((it >> 16) & 255);
     const int ph = (int)((it >> 8) & 255), pw = (int)(it & 255);
     const int n = d.n;
     const ForceField &F = *d.ff;
     const double thb_cut = d.ctl->thb_cut;
-    const double p_tor2 = F.gp[23], p_tor3 = F.gp[24], p_tor4 = F.gp[25], p_cot2 = F.gp[27];
+    const R p_tor2 = (R)F.gp[23], p_tor3 = (R)F.gp[24], p_tor4 = (R)F.gp[25], p_cot2 = (R)F.gp[27];
     double *fC = d.fC;
     double *CdD = d.fC + 3 * (long long)n;
     const long long spk = (long long)kk * n + j, sph = (long long)ph * n + j;
@@ -1069,99 +845,138 @@ __global__ void __launch_bounds__(128) k_torsion(Dev d, int eflag, long long nit
     const long long spw = (long long)pw * n + k;
     const int l = nbr_of(d.b_nbr[spw]);
     const Fbp &fbp = F.fbp[d.ts[i]][d.ts[j]][d.ts[k]][d.ts[l]].prm;
-    const double BOA_jk = d.b_BO[spk] - thb_cut, BOA_ij = d.b_BO[sph] - thb_cut;
-    const double BOA_kl = d.b_BO[spw] - thb_cut;
-    const double Delta_j = d.Delta_boc[j], Delta_k = d.Delta_boc[k];
-    const double exp_tor3_DjDk = exp(-p_tor3 * (Delta_j + Delta_k));
-    const double exp_tor4_DjDk = exp(p_tor4 * (Delta_j + Delta_k));
-    const double exp_tor34_inv = 1.0 / (1.0 + exp_tor3_DjDk + exp_tor4_DjDk);
-    const double f11_DjDk = (2.0 + exp_tor3_DjDk) * exp_tor34_inv;
-    const double exp_tor2_jk = d.b_et2[spk], exp_cot2_jk = d.b_ec2[spk];
-    const double exp_tor2_ij = d.b_et2[sph], exp_cot2_ij = d.b_ec2[sph];
-    const double exp_tor2_kl = d.b_et2[spw], exp_cot2_kl = d.b_ec2[spw];
-    const double djk[3] = {d.b_dx[spk], d.b_dy[spk], d.b_dz[spk]};
-    const double dhj[3] = {d.b_dx[sph], d.b_dy[sph], d.b_dz[sph]};
-    const double dkl[3] = {d.b_dx[spw], d.b_dy[spw], d.b_dz[spw]};
-    const double dpj[3] = {d.b_dx[spj], d.b_dy[spj], d.b_dz[spj]};
-    const double r_jk = d.b_d[spk], r_ij = d.b_d[sph], r_kl = d.b_d[spw];
-    Thb p_ijk, p_jkl;
-    double cth;
-    theta_dcos(djk, r_jk, dhj, r_ij, p_ijk.theta, cth, p_ijk.di, p_ijk.dj, p_ijk.dk);
-    theta_dcos(dpj, d.b_d[spj], dkl, r_kl, p_jkl.theta, cth, p_jkl.di, p_jkl.dj, p_jkl.dk);
-    double sin_ijk, cos_ijk, tan_ijk_i, sin_jkl, cos_jkl, tan_jkl_i;
+    const R V1 = (R)fbp.V1, V2 = (R)fbp.V2, V3 = (R)fbp.V3;
+    const R p_tor1 = (R)fbp.p_tor1, p_cot1 = (R)fbp.p_cot1;
+    const R BOA_jk = (R)(d.b_BO[spk] - thb_cut), BOA_ij = (R)(d.b_BO[sph] - thb_cut);
+    const R BOA_kl = (R)(d.b_BO[spw] - thb_cut);
+    const R Delta_j = (R)d.Delta_boc[j], Delta_k = (R)d.Delta_boc[k];
+    const R exp_tor3_DjDk = exp(-p_tor3 * (Delta_j + Delta_k));
+    const R exp_tor4_DjDk = exp(p_tor4 * (Delta_j + Delta_k));
+    const R exp_tor34_inv = R(1) / (R(1) + exp_tor3_DjDk + exp_tor4_DjDk);
+    const R f11_DjDk = (R(2) + exp_tor3_DjDk) * exp_tor34_inv;
+    const R exp_tor2_jk = (R)d.b_et2[spk], exp_cot2_jk = (R)d.b_ec2[spk];
+    const R exp_tor2_ij = (R)d.b_et2[sph], exp_cot2_ij = (R)d.b_ec2[sph];
+    const R exp_tor2_kl = (R)d.b_et2[spw], exp_cot2_kl = (R)d.b_ec2[spw];
+    const R djk[3] = {(R)d.b_dx[spk], (R)d.b_dy[spk], (R)d.b_dz[spk]};
+    const R dhj[3] = {(R)d.b_dx[sph], (R)d.b_dy[sph], (R)d.b_dz[sph]};
+    const R dkl[3] = {(R)d.b_dx[spw], (R)d.b_dy[spw], (R)d.b_dz[spw]};
+    const R dpj[3] = {(R)d.b_dx[spj], (R)d.b_dy[spj], (R)d.b_dz[spj]};
+    const R r_jk = (R)d.b_d[spk], r_ij = (R)d.b_d[sph], r_kl = (R)d.b_d[spw];
+    Thb<R> p_ijk, p_jkl;
+    R cth;
+    theta_dcos<R>(djk, r_jk, dhj, r_ij, p_ijk.theta, cth, p_ijk.di, p_ijk.dj, p_ijk.dk);
+    theta_dcos<R>(dpj, (R)d.b_d[spj], dkl, r_kl, p_jkl.theta, cth, p_jkl.di, p_jkl.dj, p_jkl.dk);
+    const R ms = (R)MIN_SINE;
+    R sin_ijk, cos_ijk, tan_ijk_i, sin_jkl, cos_jkl, tan_jkl_i;
     sincos(p_ijk.theta, &sin_ijk, &cos_ijk);
-    if (sin_ijk >= 0 && sin_ijk <= MIN_SINE) tan_ijk_i = cos_ijk / MIN_SINE;
-    else if (sin_ijk <= 0 && sin_ijk >= -MIN_SINE) tan_ijk_i = cos_ijk / -MIN_SINE;
+    if (sin_ijk >= R(0) && sin_ijk <= ms) tan_ijk_i = cos_ijk / ms;
+    else if (sin_ijk <= R(0) && sin_ijk >= -ms) tan_ijk_i = cos_ijk / -ms;
     else tan_ijk_i = cos_ijk / sin_ijk;
     sincos(p_jkl.theta, &sin_jkl, &cos_jkl);
-    if (sin_jkl >= 0 && sin_jkl <= MIN_SINE) tan_jkl_i = cos_jkl / MIN_SINE;
-    else if (sin_jkl <= 0 && sin_jkl >= -MIN_SINE) tan_jkl_i = cos_jkl / -MIN_SINE;
+    if (sin_jkl >= R(0) && sin_jkl <= ms) tan_jkl_i = cos_jkl / ms;
+    else if (sin_jkl <= R(0) && sin_jkl >= -ms) tan_jkl_i = cos_jkl / -ms;
     else tan_jkl_i = cos_jkl / sin_jkl;
-    double dli[3];
+    R dli[3];
     dli[0] = dhj[0] - djk[0] - dkl[0];
     dli[1] = dhj[1] - djk[1] - dkl[1];
     dli[2] = dhj[2] - djk[2] - dkl[2];
-    const double r_li = sqrt(sqr(dli[0]) + sqr(dli[1]) + sqr(dli[2]));
-    double doi[3], doj[3], dok[3], dol[3];
-    const double omega = calc_omega(dhj, r_ij, djk, r_jk, dkl, r_kl, dli, r_li, p_ijk, p_jkl,
-                                    doi, doj, dok, dol);
-    const double cos_omega = cos(omega);
-    const double cos2omega = cos(2. * omega);
-    const double cos3omega = cos(3. * omega);
-    const double BOpi_jk = d.b_BOpi[spk];
-    const double exp_tor1 = exp(fbp.p_tor1 * sqr(2.0 - BOpi_jk - f11_DjDk));
-    const double fn10 = (1.0 - exp_tor2_ij) * (1.0 - exp_tor2_jk) * (1.0 - exp_tor2_kl);
-    const double CV = 0.5 * (fbp.V1 * (1.0 + cos_omega) + fbp.V2 * exp_tor1 * (1.0 - cos2omega) +
-                             fbp.V3 * (1.0 + cos3omega));
-    e_tor = fn10 * sin_ijk * sin_jkl * CV;
-    const double dfn11 = (-p_tor3 * exp_tor3_DjDk +
-                          (p_tor3 * exp_tor3_DjDk - p_tor4 * exp_tor4_DjDk) * (2.0 + exp_tor3_DjDk) * exp_tor34_inv) *
-                         exp_tor34_inv;
-    const double CEtors1 = sin_ijk * sin_jkl * CV;
-    const double CEtors2 = -fn10 * 2.0 * fbp.p_tor1 * fbp.V2 * exp_tor1 * (2.0 - BOpi_jk - f11_DjDk) *
-                           (1.0 - sqr(cos_omega)) * sin_ijk * sin_jkl;
-    const double CEtors3 = CEtors2 * dfn11;
-    const double CEtors4 = CEtors1 * p_tor2 * exp_tor2_ij * (1.0 - exp_tor2_jk) * (1.0 - exp_tor2_kl);
-    const double CEtors5 = CEtors1 * p_tor2 * (1.0 - exp_tor2_ij) * exp_tor2_jk * (1.0 - exp_tor2_kl);
-    const double CEtors6 = CEtors1 * p_tor2 * (1.0 - exp_tor2_ij) * (1.0 - exp_tor2_jk) * exp_tor2_kl;
-    const double cmn = -fn10 * CV;
-    const double CEtors7 = cmn * sin_jkl * tan_ijk_i;
-    const double CEtors8 = cmn * sin_ijk * tan_jkl_i;
-    const double CEtors9 = fn10 * sin_ijk * sin_jkl *
-                           (0.5 * fbp.V1 - 2.0 * fbp.V2 * exp_tor1 * cos_omega +
-                            1.5 * fbp.V3 * (cos2omega + 2.0 * sqr(cos_omega)));
-    const double fn12 = exp_cot2_ij * exp_cot2_jk * exp_cot2_kl;
-    e_con = fbp.p_cot1 * fn12 * (1.0 + (sqr(cos_omega) - 1.0) * sin_ijk * sin_jkl);
-    const double Cconj = -2.0 * fn12 * fbp.p_cot1 * p_cot2 * (1.0 + (sqr(cos_omega) - 1.0) * sin_ijk * sin_jkl);
-    const double CEconj1 = Cconj * (BOA_ij - 1.5e0);
-    const double CEconj2 = Cconj * (BOA_jk - 1.5e0);
-    const double CEconj3 = Cconj * (BOA_kl - 1.5e0);
-    const double CEconj4 = -fbp.p_cot1 * fn12 * (sqr(cos_omega) - 1.0) * sin_jkl * tan_ijk_i;
-    const double CEconj5 = -fbp.p_cot1 * fn12 * (sqr(cos_omega) - 1.0) * sin_ijk * tan_jkl_i;
-    const double CEconj6 = 2.0 * fbp.p_cot1 * fn12 * cos_omega * sin_ijk * sin_jkl;
-    atomicAdd(&d.b_Cdbopi[spk], CEtors2);
-    atomicAdd(&CdD[j], CEtors3);
-    atomicAdd(&CdD[k], CEtors3);
-    atomicAdd(&d.b_Cdbo[sph], CEtors4 + CEconj1);
-    atomicAdd(&d.b_Cdbo[spk], CEtors5 + CEconj2);
-    atomicAdd(&d.b_Cdbo[spw], CEtors6 + CEconj3);
-    const double c78 = CEtors7 + CEconj4, c85 = CEtors8 + CEconj5, c96 = CEtors9 + CEconj6;
-    add3(fC, n, i, 1.0, c78 * p_ijk.dk[0] + c96 * doi[0], c78 * p_ijk.dk[1] + c96 * doi[1],
-         c78 * p_ijk.dk[2] + c96 * doi[2]);
-    add3(fC, n, j, 1.0, c78 * p_ijk.dj[0] + c85 * p_jkl.di[0] + c96 * doj[0],
-         c78 * p_ijk.dj[1] + c85 * p_jkl.di[1] + c96 * doj[1],
-         c78 * p_ijk.dj[2] + c85 * p_jkl.di[2] + c96 * doj[2]);
-    add3(fC, n, k, 1.0, c78 * p_ijk.di[0] + c85 * p_jkl.dj[0] + c96 * dok[0],
-         c78 * p_ijk.di[1] + c85 * p_jkl.dj[1] + c96 * dok[1],
-         c78 * p_ijk.di[2] + c85 * p_jkl.dj[2] + c96 * dok[2]);
-    add3(fC, n, l, 1.0, c85 * p_jkl.dk[0] + c96 * dol[0], c85 * p_jkl.dk[1] + c96 * dol[1],
-         c85 * p_jkl.dk[2] + c96 * dol[2]);
+    const R r_li = sqrt(sqr(dli[0]) + sqr(dli[1]) + sqr(dli[2]));
+    R doi[3], doj[3], dok[3], dol[3];
+    const R omega = calc_omega<R>(dhj, r_ij, djk, r_jk, dkl, r_kl, dli, r_li, p_ijk, p_jkl,
+                                  doi, doj, dok, dol);
+    const R cos_omega = cos(omega);
+    const R cos2omega = cos(R(2) * omega);
+    const R cos3omega = cos(R(3) * omega);
+    const R BOpi_jk = (R)d.b_BOpi[spk];
+    const R exp_tor1 = exp(p_tor1 * sqr(R(2) - BOpi_jk - f11_DjDk));
+    const R fn10 = (R(1) - exp_tor2_ij) * (R(1) - exp_tor2_jk) * (R(1) - exp_tor2_kl);
+    const R CV = R(0.5) * (V1 * (R(1) + cos_omega) + V2 * exp_tor1 * (R(1) - cos2omega) +
+                           V3 * (R(1) + cos3omega));
+    e_tor = (double)(fn10 * sin_ijk * sin_jkl * CV);
+    const R dfn11 = (-p_tor3 * exp_tor3_DjDk +
+                     (p_tor3 * exp_tor3_DjDk - p_tor4 * exp_tor4_DjDk) * (R(2) + exp_tor3_DjDk) * exp_tor34_inv) *
+                    exp_tor34_inv;
+    const R CEtors1 = sin_ijk * sin_jkl * CV;
+    const R CEtors2 = -fn10 * R(2) * p_tor1 * V2 * exp_tor1 * (R(2) - BOpi_jk - f11_DjDk) *
+                      (R(1) - sqr(cos_omega)) * sin_ijk * sin_jkl;
+    const R CEtors3 = CEtors2 * dfn11;
+    const R CEtors4 = CEtors1 * p_tor2 * exp_tor2_ij * (R(1) - exp_tor2_jk) * (R(1) - exp_tor2_kl);
+    const R CEtors5 = CEtors1 * p_tor2 * (R(1) - exp_tor2_ij) * exp_tor2_jk * (R(1) - exp_tor2_kl);
+    const R CEtors6 = CEtors1 * p_tor2 * (R(1) - exp_tor2_ij) * (R(1) - exp_tor2_jk) * exp_tor2_kl;
+    const R cmn = -fn10 * CV;
+    const R CEtors7 = cmn * sin_jkl * tan_ijk_i;
+    const R CEtors8 = cmn * sin_ijk * tan_jkl_i;
+    const R CEtors9 = fn10 * sin_ijk * sin_jkl *
+                      (R(0.5) * V1 - R(2) * V2 * exp_tor1 * cos_omega +
+                       R(1.5) * V3 * (cos2omega + R(2) * sqr(cos_omega)));
+    const R fn12 = exp_cot2_ij * exp_cot2_jk * exp_cot2_kl;
+    e_con = (double)(p_cot1 * fn12 * (R(1) + (sqr(cos_omega) - R(1)) * sin_ijk * sin_jkl));
+    const R Cconj = R(-2) * fn12 * p_cot1 * p_cot2 * (R(1) + (sqr(cos_omega) - R(1)) * sin_ijk * sin_jkl);
+    const R CEconj1 = Cconj * (BOA_ij - R(1.5));
+    const R CEconj2 = Cconj * (BOA_jk - R(1.5));
+    const R CEconj3 = Cconj * (BOA_kl - R(1.5));
+    const R CEconj4 = -p_cot1 * fn12 * (sqr(cos_omega) - R(1)) * sin_jkl * tan_ijk_i;
+    const R CEconj5 = -p_cot1 * fn12 * (sqr(cos_omega) - R(1)) * sin_ijk * tan_jkl_i;
+    const R CEconj6 = R(2) * p_cot1 * fn12 * cos_omega * sin_ijk * sin_jkl;
+    atomicAdd(&d.b_Cdbopi[spk], (double)CEtors2);
+    atomicAdd(&CdD[j], (double)CEtors3);
+    atomicAdd(&CdD[k], (double)CEtors3);
+    atomicAdd(&d.b_Cdbo[sph], (double)(CEtors4 + CEconj1));
+    atomicAdd(&d.b_Cdbo[spk], (double)(CEtors5 + CEconj2));
+    atomicAdd(&d.b_Cdbo[spw], (double)(CEtors6 + CEconj3));
+    const R c78 = CEtors7 + CEconj4, c85 = CEtors8 + CEconj5, c96 = CEtors9 + CEconj6;
+    add3(fC, n, i, 1.0, (double)(c78 * p_ijk.dk[0] + c96 * doi[0]), (double)(c78 * p_ijk.dk[1] + c96 * doi[1]),
+         (double)(c78 * p_ijk.dk[2] + c96 * doi[2]));
+    add3(fC, n, j, 1.0, (double)(c78 * p_ijk.dj[0] + c85 * p_jkl.di[0] + c96 * doj[0]),
+         (double)(c78 * p_ijk.dj[1] + c85 * p_jkl.di[1] + c96 * doj[1]),
+         (double)(c78 * p_ijk.dj[2] + c85 * p_jkl.di[2] + c96 * doj[2]));
+    add3(fC, n, k, 1.0, (double)(c78 * p_ijk.di[0] + c85 * p_jkl.dj[0] + c96 * dok[0]),
+         (double)(c78 * p_ijk.di[1] + c85 * p_jkl.dj[1] + c96 * dok[1]),
+         (double)(c78 * p_ijk.di[2] + c85 * p_jkl.dj[2] + c96 * dok[2]));
+    add3(fC, n, l, 1.0, (double)(c85 * p_jkl.dk[0] + c96 * dol[0]), (double)(c85 * p_jkl.dk[1] + c96 * dol[1]),
+         (double)(c85 * p_jkl.dk[2] + c96 * dol[2]));
   }
+}
+
+__device__ __forceinline__ void torsion_energies(const Dev &d, int eflag, double e_tor, double e_con) {
   if (eflag) {
     block_add(e_tor, &d.energy[E_TOR]);
     block_add(e_con, &d.energy[E_CON]);
     block_add(e_tor + e_con, &d.energy[E_ENG_VDWL]);
   }
+}
+
+template <typename R>
+__global__ void __launch_bounds__(128) k_torsion(Dev d, int eflag, long long nitems) {
+  const long long w = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  double e_tor = 0, e_con = 0;
+  if (w < nitems) {
+    const unsigned long long it = d.w_tor[w];
+    if (std::is_same<R, float>::value) {
+      const int n = d.n;
+      const int j = (int)(it >> 24), kk = (int)((it >> 16) & 255);
+      const int ph = (int)((it >> 8) & 255), pw = (int)(it & 255);
+      const long long spk = (long long)kk * n + j, sph = (long long)ph * n + j;
+      const int k = nbr_of(d.b_nbr[spk]);
+      const long long spj = d.b_sym[spk], spw = (long long)pw * n + k;
+      if (near_linear(d, spk, sph) || near_linear(d, spj, spw))
+        d.w_fb_tor[atomicAdd(&d.fb_cnt[1], 1)] = it;
+      else
+        torsion_item<R>(d, it, e_tor, e_con);
+    } else {
+      torsion_item<R>(d, it, e_tor, e_con);
+    }
+  }
+  torsion_energies(d, eflag, e_tor, e_con);
+}
+
+__global__ void __launch_bounds__(128) k_torsion_fb(Dev d, int eflag) {
+  double e_tor = 0, e_con = 0;
+  const long long cnt = d.fb_cnt[1];
+  for (long long w = (long long)blockIdx.x * blockDim.x + threadIdx.x; w < cnt;
+       w += (long long)gridDim.x * blockDim.x)
+    torsion_item<double>(d, d.w_fb_tor[w], e_tor, e_con);
+  torsion_energies(d, eflag, e_tor, e_con);
 }
 
 // ------------------------------------------------------------------
@@ -1224,7 +1039,20 @@ __global__ void k_force_out(Dev d) {
   d.f_o[3 * i + 2] = fz;
 }
 
+// failure detection: sets *flag if any of a[0..count) is not finite
+__global__ void k_check_finite(const double *a, long long count, int *flag) {
+  bool bad = false;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < count;
+       i += (long long)gridDim.x * blockDim.x)
+    bad |= !isfinite(a[i]);
+  if (__any_sync(FULL, bad) && (threadIdx.x & 31) == 0) atomicOr(flag, 1);
+}
+
 }  // namespace
+
+void launch_check_finite(const double *a, long long count, int *flag, cudaStream_t st) {
+  k_check_finite<<<152 * 4, 256, 0, st>>>(a, count, flag);
+}
 
 void launch_bond_orders(const Dev &d, cudaStream_t st) {
   const int B = 256;
@@ -1240,12 +1068,9 @@ void launch_atom_energy(const Dev &d, cudaStream_t st, int eflag) {
 
 void launch_hbonds(const Dev &d, cudaStream_t st, int eflag) {
   const long long threads = (long long)d.n * 32;
-  k_hbonds<<<(unsigned)((threads + 255) / 256), 256, 0, st>>>(d, eflag);
-}
-
-void launch_valence_torsion(const Dev &d, cudaStream_t st, int eflag) {
-  const long long slots = (long long)d.n * d.bond_cap;
-  k_valence_torsion<<<(unsigned)((slots + 127) / 128), 128, 0, st>>>(d, eflag);
+  const unsigned G = (unsigned)((threads + 255) / 256);
+  if (d.mixed) k_hbonds<float><<<G, 256, 0, st>>>(d, eflag);
+  else k_hbonds<double><<<G, 256, 0, st>>>(d, eflag);
 }
 
 void launch_vt_count(const Dev &d, cudaStream_t st) {
@@ -1262,8 +1087,18 @@ void launch_vt_run(const Dev &d, cudaStream_t st, int eflag, long long nval, lon
   const int B = 256;
   const long long slots = (long long)d.n * d.bond_cap;
   k_vt_fill<<<(unsigned)((slots + B - 1) / B), B, 0, st>>>(d);
-  if (nval > 0) k_valence<<<(unsigned)((nval + 127) / 128), 128, 0, st>>>(d, eflag, nval);
-  if (ntor > 0) k_torsion<<<(unsigned)((ntor + 127) / 128), 128, 0, st>>>(d, eflag, ntor);
+  const unsigned gv = (unsigned)((nval + 127) / 128), gt = (unsigned)((ntor + 127) / 128);
+  if (d.mixed) {
+    cudaMemsetAsync(d.fb_cnt, 0, 2 * sizeof(int), st);
+    if (nval > 0) k_valence<float><<<gv, 128, 0, st>>>(d, eflag, nval);
+    if (ntor > 0) k_torsion<float><<<gt, 128, 0, st>>>(d, eflag, ntor);
+    // FP64 passes over the near-linear items (count read on the device)
+    k_valence_fb<<<152 * 2, 128, 0, st>>>(d, eflag);
+    k_torsion_fb<<<152 * 2, 128, 0, st>>>(d, eflag);
+  } else {
+    if (nval > 0) k_valence<double><<<gv, 128, 0, st>>>(d, eflag, nval);
+    if (ntor > 0) k_torsion<double><<<gt, 128, 0, st>>>(d, eflag, ntor);
+  }
 }
 
 void launch_dbond_forces(const Dev &d, cudaStream_t st) {

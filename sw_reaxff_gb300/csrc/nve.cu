@@ -1,6 +1,7 @@
 // Velocity-Verlet NVE integration (fix nve/sunway): the two half steps of
 // fix_nve_sw64.c:25-172 with dtf = 0.5 dt ftm2v (fix_nve_sunway.cpp:54-58),
-// per-type masses from the force field.  Arrays are in the original order.
+// per-type masses (the force field's unless the caller set the data
+// file's, rg_set_masses).  Arrays are in the original order.
 #include "rg_internal.h"
 
 namespace {
@@ -12,7 +13,7 @@ __global__ void k_nve_initial(Dev d, double dt) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= d.n) return;
   const double dtf = 0.5 * dt * FTM2V;
-  const double dtfm = dtf / d.ff->sbp[d.type_o[i]].mass;
+  const double dtfm = dtf / d.ff->nve_mass[d.type_o[i]];
 #pragma unroll
   for (int c = 0; c < 3; ++c) {
     double v = d.v_o[3 * i + c] + dtfm * d.f_o[3 * i + c];
@@ -25,7 +26,7 @@ __global__ void k_nve_final(Dev d, double dt) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= d.n) return;
   const double dtf = 0.5 * dt * FTM2V;
-  const double dtfm = dtf / d.ff->sbp[d.type_o[i]].mass;
+  const double dtfm = dtf / d.ff->nve_mass[d.type_o[i]];
 #pragma unroll
   for (int c = 0; c < 3; ++c) d.v_o[3 * i + c] += dtfm * d.f_o[3 * i + c];
 }

@@ -90,8 +90,44 @@ __global__ void __launch_bounds__(256) k_spmv(Dev d, const double2 *__restrict__
   }
 }
 
-// mixed form: FP32 H and FP32 products; per-lane partial sums in FP32,
-// the warp's total and the diagonal term in FP64
+// mixed form: the FP32 H with compensated FP32 arithmetic.  The vector is
+// read as FP32 (hi, lo) pairs (x = hi + lo to ~2^-48), each product is
+// formed exactly as p + e (fmaf) plus h*lo, and the row sum is carried as an
+// unevaluated FP32 pair with Knuth's TwoSum, across the warp too; the pair
+// becomes FP64 once per row.  The sums so carry ~46 significant bits: the
+// pipelined CG then follows the FP64 iterates (it stagnates with plain FP32
+// sums), while reading 8 bytes of H and index per entry and running on the
+// FP32 units.
+// (explicitly rounded operations: no contraction into FMAs may change them)
+__device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
+  s = __fadd_rn(a, b);
+  const float bb = __fsub_rn(s, a);
+  e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+
+// (sh, sl) += h * (xh + xl)
+__device__ __forceinline__ void df_fma(float h, float xh, float xl, float &sh, float &sl) {
+  const float p = __fmul_rn(h, xh);
+  float e = __fmaf_rn(h, xh, -p);   // exact: h*xh = p + e
+  e = __fmaf_rn(h, xl, e);
+  float s, err;
+  two_sum(sh, p, s, err);
+  sh = s;
+  sl = __fadd_rn(sl, __fadd_rn(err, e));
+}
+
+__device__ __forceinline__ void df_add(float &sh, float &sl, float oh, float ol) {
+  float s, err;
+  two_sum(sh, oh, s, err);
+  sh = s;
+  sl = __fadd_rn(sl, __fadd_rn(err, ol));
+}
+
+__device__ __forceinline__ float4 split4(double2 v) {
+  const float sh = __double2float_rn(v.x), th = __double2float_rn(v.y);
+  return make_float4(sh, __double2float_rn(v.x - (double)sh), th, __double2float_rn(v.y - (double)th));
+}
+
 __global__ void __launch_bounds__(256) k_spmv32(Dev d, const double2 *__restrict__ x, double2 *__restrict__ y) {
   const int lane = threadIdx.x & 31;
   const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -99,20 +135,55 @@ __global__ void __launch_bounds__(256) k_spmv32(Dev d, const double2 *__restrict
   const long long row = (long long)i * d.nb_cap;
   const int nn = d.n_near[i], nf = d.n_far[i], cap = d.nb_cap;
   const int tot = min(nn + nf, cap);
-  float as = 0.f, at = 0.f;
+  const float4 *__restrict__ x32 = d.qd32;
+  float sh = 0.f, sl = 0.f, th = 0.f, tl = 0.f;
   for (int p = lane; p < tot; p += 32) {
     const int slot = p < nn ? p : cap - 1 - (p - nn);
     const uint32_t e = d.nbr[row + slot];
     const float h = d.hval32[row + slot];
-    const double2 xj = x[e >> 8];
-    as = fmaf(h, (float)xj.x, as);
-    at = fmaf(h, (float)xj.y, at);
+    const float4 xj = x32[e >> 8];
+    df_fma(h, xj.x, xj.y, sh, sl);
+    df_fma(h, xj.z, xj.w, th, tl);
   }
-  double ds = warp_sum((double)as), dt = warp_sum((double)at);
+  for (int off = 16; off > 0; off >>= 1) {
+    const float a = __shfl_down_sync(FULL, sh, off), b = __shfl_down_sync(FULL, sl, off);
+    const float c = __shfl_down_sync(FULL, th, off), e = __shfl_down_sync(FULL, tl, off);
+    df_add(sh, sl, a, b);
+    df_add(th, tl, c, e);
+  }
   if (lane == 0) {
     const double eta = d.ff->sbp[d.ts[i]].eta;
     const double2 xi = x[i];
-    y[i] = make_double2(fma(eta, xi.x, ds), fma(eta, xi.y, dt));
+    y[i] = make_double2(fma(eta, xi.x, (double)sh + (double)sl),
+                        fma(eta, xi.y, (double)th + (double)tl));
+  }
+}
+
+// mixed form, residual of the refinement: the stored FP32 H with FP64
+// products and sums, so r = b - H x carries no FP32 rounding of x or of
+// the sums (the FP32 SpMV's rounding is what the inner CG iterations see)
+__global__ void __launch_bounds__(256) k_spmv_ref(Dev d, const double2 *__restrict__ x, double2 *__restrict__ y) {
+  const int lane = threadIdx.x & 31;
+  const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (i >= d.n) return;
+  const long long row = (long long)i * d.nb_cap;
+  const int nn = d.n_near[i], nf = d.n_far[i], cap = d.nb_cap;
+  const int tot = min(nn + nf, cap);
+  double as = 0.0, at = 0.0;
+  for (int p = lane; p < tot; p += 32) {
+    const int slot = p < nn ? p : cap - 1 - (p - nn);
+    const uint32_t e = d.nbr[row + slot];
+    const double h = (double)d.hval32[row + slot];
+    const double2 xj = x[e >> 8];
+    as = fma(h, xj.x, as);
+    at = fma(h, xj.y, at);
+  }
+  as = warp_sum(as);
+  at = warp_sum(at);
+  if (lane == 0) {
+    const double eta = d.ff->sbp[d.ts[i]].eta;
+    const double2 xi = x[i];
+    y[i] = make_double2(fma(eta, xi.x, as), fma(eta, xi.y, at));
   }
 }
 
@@ -127,6 +198,7 @@ __global__ void k_cg_init1(Dev d) {
   const double2 u = make_double2(r.x * hi, r.y * hi);
   d.qu[s] = u;
   d.qd[s] = u;
+  if (d.qd32) d.qd32[s] = split4(u);
 }
 
 // w = q; m = q*Hdia_inv; d = m
@@ -139,6 +211,7 @@ __global__ void k_cg_init2(Dev d) {
   const double2 m = make_double2(q.x * hi, q.y * hi);
   d.qm[s] = m;
   d.qd[s] = m;
+  if (d.qd32) d.qd32[s] = split4(m);
 }
 
 // p = u; s = w; v = m; z = q; sums b.b, u.r, u.w
@@ -200,6 +273,7 @@ __global__ void k_cg_A(Dev d) {
       dd.y = w.y * hi;
     }
     d.qr[s] = r; d.qu[s] = u; d.qw[s] = w; d.qd[s] = dd;
+    if (d.qd32) d.qd32[s] = split4(dd);
   }
   double all[4] = {v[0], v[1], v1[0], v1[1]};
   block_add_k<4>(all, d.red + R_ACC0);   // ACC0[2], ACC1[2] are contiguous
@@ -297,15 +371,26 @@ void launch_qeq_setup(const Dev &d, cudaStream_t st) {
   k_qeq_setup<<<(d.n + B - 1) / B, B, 0, st>>>(d);
 }
 
+// the mixed form's FP32 SpMV reads the split copy of qd; any other vector
+// goes through the FP64-sum kernel
 void launch_qeq_spmv(const Dev &d, cudaStream_t st, const double2 *x, double2 *y) {
   const long long threads = (long long)d.n * 32;
-  if (d.mixed) k_spmv32<<<(unsigned)((threads + 255) / 256), 256, 0, st>>>(d, x, y);
-  else k_spmv<<<(unsigned)((threads + 255) / 256), 256, 0, st>>>(d, x, y);
+  const unsigned G = (unsigned)((threads + 255) / 256);
+  if (!d.mixed) k_spmv<<<G, 256, 0, st>>>(d, x, y);
+  else if (x == d.qd) k_spmv32<<<G, 256, 0, st>>>(d, x, y);
+  else k_spmv_ref<<<G, 256, 0, st>>>(d, x, y);
 }
 
+// r = b - H x of the current iterate starts (or, in the mixed form,
+// restarts) the pipelined CG; the mixed form computes it with FP64 sums
 void launch_qeq_cg_init(const Dev &d, cudaStream_t st) {
   const int B = 256, G = (d.n + B - 1) / B;
-  launch_qeq_spmv(d, st, d.qx, d.qq);
+  if (d.mixed) {
+    const long long threads = (long long)d.n * 32;
+    k_spmv_ref<<<(unsigned)((threads + 255) / 256), 256, 0, st>>>(d, d.qx, d.qq);
+  } else {
+    launch_qeq_spmv(d, st, d.qx, d.qq);
+  }
   k_cg_init1<<<G, B, 0, st>>>(d);
   launch_qeq_spmv(d, st, d.qd, d.qq);
   k_cg_init2<<<G, B, 0, st>>>(d);

@@ -10,6 +10,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -92,6 +93,9 @@ struct rg_system {
   int ncell_alloc = 0;
   bool lists_valid = false;
   bool forces_valid = false;
+  // RG_CHECK_FINITE=1: test the force/CdDelta accumulators after every
+  // force phase and name the first phase that produced a non-finite value
+  bool check_finite = false;
   rg_stats stats{};
   double energy[RG_NE] = {0};
   Prof prof;
@@ -212,6 +216,12 @@ int alloc_items(rg_system *h, long long nval, long long ntor) {
   int r = 0;
   r |= dalloc(h, h->per_items, &d.w_val, (size_t)nval);
   r |= dalloc(h, h->per_items, &d.w_tor, (size_t)ntor);
+  if (d.mixed) {
+    r |= dalloc(h, h->per_items, &d.w_fb_val, (size_t)nval);
+    r |= dalloc(h, h->per_items, &d.w_fb_tor, (size_t)ntor);
+  } else {
+    d.w_fb_val = d.w_fb_tor = nullptr;
+  }
   return r;
 }
 
@@ -271,9 +281,12 @@ int alloc_atoms(rg_system *h, int n) {
   r |= dalloc(h, B, &d.c_sbo, 5 * (size_t)n);
   double2 **pv[] = {&d.qx, &d.qb, &d.qr, &d.qu, &d.qw, &d.qd, &d.qq, &d.qp, &d.qs, &d.qv, &d.qz, &d.qm};
   for (double2 **q : pv) r |= dalloc(h, B, q, (size_t)n);
+  if (d.mixed) r |= dalloc(h, B, &d.qd32, (size_t)n);
+  else d.qd32 = nullptr;
   r |= dalloc(h, B, &d.red, 128);
   r |= dalloc(h, B, &d.energy, RG_NE);
   r |= dalloc(h, B, &d.status, 8);
+  r |= dalloc(h, B, &d.fb_cnt, 2);
   if (r) return RG_E_CUDA;
   // capacity estimates from the mean density
   const double vol = h->L[0] * h->L[1] * h->L[2];
@@ -360,9 +373,20 @@ int do_compute(rg_system *h, int eflag) {
   if (!h->lists_valid && (rc = build_lists(h))) return rc;
   CK(cudaMemsetAsync(d.fC, 0, 4 * sizeof(double) * (size_t)d.n, h->st));
   CK(cudaMemsetAsync(d.energy, 0, RG_NE * sizeof(double), h->st));
+  auto finite_after = [&](const char *phase) -> int {
+    if (!h->check_finite) return 0;
+    int flag = 0;
+    CK(cudaMemsetAsync(d.status + ST_NAN, 0, sizeof(int), h->st));
+    launch_check_finite(d.fC, 4 * (long long)d.n, d.status + ST_NAN, h->st);
+    CK(cudaMemcpyAsync(&flag, d.status + ST_NAN, sizeof(int), cudaMemcpyDeviceToHost, h->st));
+    CK(cudaStreamSynchronize(h->st));
+    return flag ? fail(h, RG_E_NUMERIC, std::string("non-finite force after ") + phase) : 0;
+  };
   { Scope sc(h, PH_BO, 3); launch_bond_orders(d, h->st); }
   { Scope sc(h, PH_ATOM, 1); launch_atom_energy(d, h->st, eflag); }
+  if ((rc = finite_after("atom_energy"))) return rc;
   { Scope sc(h, PH_HB, 1); launch_hbonds(d, h->st, eflag); }
+  if ((rc = finite_after("hbonds"))) return rc;
   {
     Scope sc(h, PH_VALTOR, 9);
     launch_vt_count(d, h->st);
@@ -382,11 +406,14 @@ int do_compute(rg_system *h, int eflag) {
     }
     h->n_val = tot[0];
     h->n_tor = tot[1];
-    Scope sc(h, PH_VALTOR, 3);
+    Scope sc(h, PH_VALTOR, 1 + (tot[0] > 0) + (tot[1] > 0) + (d.mixed ? 2 : 0));
     launch_vt_run(d, h->st, eflag, tot[0], tot[1]);
   }
+  if ((rc = finite_after("valence_torsion"))) return rc;
   { Scope sc(h, PH_NONB, 1); launch_nonbonded(d, h->st, eflag); }
+  if ((rc = finite_after("nonbonded"))) return rc;
   { Scope sc(h, PH_DBOND, 1); launch_dbond_forces(d, h->st); }
+  if ((rc = finite_after("dbond_forces"))) return rc;
   { Scope sc(h, PH_FOUT, 1); launch_force_out(d, h->st); }
   CK(cudaGetLastError());
   h->forces_valid = true;
@@ -400,30 +427,49 @@ int do_qeq(rg_system *h, int *its, int *itt) {
   double hostred[2] = {h->p.qeq_tol, (double)h->p.qeq_imax};
   CK(cudaMemcpyAsync(d.red + 26, hostred, 2 * sizeof(double), cudaMemcpyHostToDevice, h->st));
   {
-    Scope sc(h, PH_QSETUP, 9);
+    Scope sc(h, PH_QSETUP, 8);
     launch_qeq_setup(d, h->st);
     launch_qeq_cg_init(d, h->st);
   }
-  // iterate; poll the activity flags every few iterations
+  // iterate; poll the activity flags every few iterations.  The mixed form
+  // then restarts the CG from its iterate with the residual recomputed with
+  // FP64 sums (iterative refinement) until that residual meets the
+  // tolerance: at most RG_MAX_REFINE restarts.
+  const int RG_MAX_REFINE = 3;
   double flags[4];
-  int done_iters = 0;
+  int tot_s = 0, tot_t = 0, refines = 0;
   const int chunk = 4;
   for (;;) {
-    CK(cudaMemcpyAsync(flags, d.red + 20, 4 * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+    int done_iters = 0;
+    for (;;) {
+      CK(cudaMemcpyAsync(flags, d.red + 20, 4 * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+      CK(cudaStreamSynchronize(h->st));
+      if (flags[0] == 0.0 && flags[1] == 0.0) break;
+      if (done_iters > h->p.qeq_imax + 8) return fail(h, RG_E_NUMERIC, "QEq iteration control lost");
+      for (int k = 0; k < chunk; ++k) {
+        { Scope sc(h, PH_QVEC, 1); launch_qeq_cg_A(d, h->st); }
+        { Scope sc(h, PH_QSPMV, 1); launch_qeq_spmv(d, h->st, d.qd, d.qq); }
+        { Scope sc(h, PH_QVEC, 3); launch_qeq_cg_C(d, h->st); }
+      }
+      done_iters += chunk;
+    }
+    // the initial pass counts its first (set-up) iteration like CG_v2;
+    // a restart that is not needed adds nothing
+    const int add_s = (int)flags[2] - (refines ? 1 : 0), add_t = (int)flags[3] - (refines ? 1 : 0);
+    tot_s += add_s > 0 ? add_s : 0;
+    tot_t += add_t > 0 ? add_t : 0;
+    if (!d.mixed || refines >= RG_MAX_REFINE) break;
+    { Scope sc(h, PH_QSETUP, 7); launch_qeq_cg_init(d, h->st); }
+    ++refines;
+    CK(cudaMemcpyAsync(flags, d.red + 20, 2 * sizeof(double), cudaMemcpyDeviceToHost, h->st));
     CK(cudaStreamSynchronize(h->st));
     if (flags[0] == 0.0 && flags[1] == 0.0) break;
-    if (done_iters > h->p.qeq_imax + 8) return fail(h, RG_E_NUMERIC, "QEq iteration control lost");
-    for (int k = 0; k < chunk; ++k) {
-      { Scope sc(h, PH_QVEC, 1); launch_qeq_cg_A(d, h->st); }
-      { Scope sc(h, PH_QSPMV, 1); launch_qeq_spmv(d, h->st, d.qd, d.qq); }
-      { Scope sc(h, PH_QVEC, 3); launch_qeq_cg_C(d, h->st); }
-    }
-    done_iters += chunk;
   }
-  h->stats.cg_iters_s = (int)flags[2];
-  h->stats.cg_iters_t = (int)flags[3];
-  if (its) *its = (int)flags[2];
-  if (itt) *itt = (int)flags[3];
+  h->stats.cg_iters_s = tot_s;
+  h->stats.cg_iters_t = tot_t;
+  h->stats.qeq_restarts = refines;
+  if (its) *its = tot_s;
+  if (itt) *itt = tot_t;
   { Scope sc(h, PH_QFIN, 2); launch_qeq_finish(d, h->st); }
   CK(cudaGetLastError());
   return 0;
@@ -486,6 +532,11 @@ int rg_create(const char *ffield_path, const rg_params *pin, rg_system **out) {
     return RG_E_ARG;
   }
   h->d.mixed = (h->p.precision == RG_PREC_MIXED);
+  {
+    const char *cf = std::getenv("RG_CHECK_FINITE");
+    h->check_finite = cf && cf[0] == '1';
+  }
+  for (int t = 0; t < RG_MAXT; ++t) h->ff.nve_mass[t] = h->ff.sbp[t].mass;
   if (c.near_cut > lc) {
     delete h;
     return RG_E_ARG;
@@ -505,6 +556,18 @@ int rg_create(const char *ffield_path, const rg_params *pin, rg_system **out) {
   h->d.ff = h->d_ff;
   h->d.ctl = h->d_ctl;
   *out = h;
+  return RG_OK;
+}
+
+int rg_set_masses(rg_system *h, const double *mass) {
+  if (!h || !mass) return RG_E_ARG;
+  for (int t = 0; t < h->ff.ntypes; ++t)
+    if (!(mass[t] > 0.0)) return fail(h, RG_E_ARG, "masses must be positive");
+  for (int t = 0; t < h->ff.ntypes; ++t) h->ff.nve_mass[t] = mass[t];
+  CK(cudaSetDevice(h->p.device));
+  CK(cudaMemcpyAsync(&h->d_ff->nve_mass[0], &h->ff.nve_mass[0], sizeof(h->ff.nve_mass),
+                     cudaMemcpyHostToDevice, h->st));
+  CK(cudaStreamSynchronize(h->st));
   return RG_OK;
 }
 
@@ -528,6 +591,22 @@ int rg_destroy(rg_system *h) {
 const char *rg_last_error(const rg_system *h) { return h ? h->err.c_str() : "null handle"; }
 
 int rg_num_types(const rg_system *h) { return h ? h->ff.ntypes : 0; }
+
+int rg_ffield_info(const char *path, int *ntypes, char *names, int len, char *msg, int msg_len) {
+  if (!path || !ntypes) return RG_E_ARG;
+  ForceField *ff = new ForceField();
+  const std::string e = rg_read_ffield(path, 0, ff);
+  if (!e.empty()) {
+    if (msg && msg_len > 0) std::snprintf(msg, msg_len, "%s", e.c_str());
+    delete ff;
+    return RG_E_FILE;
+  }
+  *ntypes = ff->ntypes;
+  if (names && len > 0)
+    for (int t = 0; t < ff->ntypes; ++t) std::snprintf(names + (size_t)t * len, len, "%s", ff->sbp[t].name);
+  delete ff;
+  return RG_OK;
+}
 
 int rg_element_name(const rg_system *h, int t, char *buf, int len) {
   if (!h || t < 0 || t >= h->ff.ntypes || !buf || len < 1) return RG_E_ARG;

@@ -65,6 +65,7 @@ struct ForceField {
   Thbh thbp[RG_MAXT][RG_MAXT][RG_MAXT];
   Hbp hbp[RG_MAXT][RG_MAXT][RG_MAXT];
   Fbh fbp[RG_MAXT][RG_MAXT][RG_MAXT][RG_MAXT];
+  double nve_mass[RG_MAXT];   // integrator masses (default: sbp mass)
 };
 
 // Scalar controls shared by all kernels.
@@ -151,6 +152,7 @@ struct Dev {
 
   // QEq vectors (sorted order), two solves s,t interleaved as double2
   double2 *qx, *qb, *qr, *qu, *qw, *qd, *qq, *qp, *qs, *qv, *qz, *qm;
+  float4 *qd32;   // mixed form: qd split into FP32 (hi, lo) pairs, s then t
   double *Hdia_inv;
   double *red;        // device scalars / reduction accumulators
   double *energy;     // [RG_NE]
@@ -163,6 +165,10 @@ struct Dev {
   int *w_bsum;             // scan block sums
   unsigned long long *w_val, *w_tor;   // packed items
   long long cap_val, cap_tor;
+  // mixed form: near-linear angles and torsions the FP32 kernels hand to
+  // an FP64 pass (fb_cnt[0] angles, fb_cnt[1] torsions)
+  unsigned long long *w_fb_val, *w_fb_tor;
+  int *fb_cnt;
 
   int *status;        // [8]: 0 overflow flags, 1 max nbrs, 2 max bonds, 3 max hb, 4 nonfinite,
                       //      5 pair entries, 6 bonds, 7 H-bond partners
@@ -206,7 +212,6 @@ void launch_count(const Dev &d, cudaStream_t st);
 void launch_bond_orders(const Dev &d, cudaStream_t st);
 void launch_atom_energy(const Dev &d, cudaStream_t st, int eflag);
 void launch_hbonds(const Dev &d, cudaStream_t st, int eflag);
-void launch_valence_torsion(const Dev &d, cudaStream_t st, int eflag);
 // work-list form: prep + count (then the host reads the totals), fill + run
 void launch_vt_count(const Dev &d, cudaStream_t st);
 void launch_vt_run(const Dev &d, cudaStream_t st, int eflag, long long nval, long long ntor);
@@ -214,6 +219,7 @@ void launch_scan(const int *in, int *out, int n, int *bsum, cudaStream_t st);
 void launch_nonbonded(const Dev &d, cudaStream_t st, int eflag);
 void launch_dbond_forces(const Dev &d, cudaStream_t st);
 void launch_force_out(const Dev &d, cudaStream_t st);
+void launch_check_finite(const double *a, long long count, int *flag, cudaStream_t st);
 
 // QEq
 void launch_qeq_setup(const Dev &d, cudaStream_t st);

@@ -1,0 +1,380 @@
+// Host-side C++ styles over the reaxgpu C ABI (see reax_styles.h for the
+// reference classes each one mirrors).
+#include "reax_styles.h"
+
+#include <cerrno>
+#include <cmath>
+#include <cstdlib>
+#include <cstring>
+#include <strings.h>
+
+namespace reaxgb {
+
+namespace {
+
+// LAMMPS force->numeric / inumeric: the whole string must be a number
+double numeric(const char *s) {
+  char *end = nullptr;
+  errno = 0;
+  const double v = std::strtod(s, &end);
+  if (!s[0] || *end || errno)
+    throw Error(std::string("Expected floating point parameter instead of ") + s +
+                " in input script or data file");
+  return v;
+}
+
+long inumeric(const char *s) {
+  char *end = nullptr;
+  errno = 0;
+  const long v = std::strtol(s, &end, 10);
+  if (!s[0] || *end || errno)
+    throw Error(std::string("Expected integer parameter instead of ") + s +
+                " in input script or data file");
+  return v;
+}
+
+bool yes_no(const char *s, const char *illegal) {
+  if (!std::strcmp(s, "yes")) return true;
+  if (!std::strcmp(s, "no")) return false;
+  throw Error(illegal);
+}
+
+// LAMMPS real units: ftm2v = 1 / 48.88821291^2, mvv2e = 48.88821291^2
+constexpr double FTM2V = 1.0 / 48.88821291 / 48.88821291;
+constexpr double MVV2E = 48.88821291 * 48.88821291;
+
+}  // namespace
+
+// ---------------------------------------------------------------- pair
+
+PairReaxCGB300::PairReaxCGB300(Atom *atom) : atom_(atom) { rg_default_params(&params_); }
+
+PairReaxCGB300::~PairReaxCGB300() {
+  if (h_) rg_destroy(h_);
+}
+
+void PairReaxCGB300::settings(int narg, char **arg) {
+  if (narg < 1) throw Error("Illegal pair_style command");
+  // a control file (pair_reaxc_sunway.cpp:231 Read_Control_File) is not
+  // supported: its cutoffs are the NULL defaults' keywords here
+  if (std::strcmp(arg[0], "NULL") != 0)
+    throw Error("pair_style reax/c/gb300 supports only NULL control (default controls)");
+  rg_default_params(&params_);
+  qeqflag = 1;
+  const char *illegal = "Illegal pair_style reax/c command";
+  int iarg = 1;
+  while (iarg < narg) {
+    if (iarg + 2 > narg) throw Error(illegal);
+    const char *key = arg[iarg], *val = arg[iarg + 1];
+    if (!std::strcmp(key, "checkqeq")) {
+      qeqflag = yes_no(val, illegal) ? 1 : 0;
+    } else if (!std::strcmp(key, "enobonds")) {
+      params_.enobondsflag = yes_no(val, illegal) ? 1 : 0;
+    } else if (!std::strcmp(key, "lgvdw")) {
+      params_.lgflag = yes_no(val, illegal) ? 1 : 0;
+    } else if (!std::strcmp(key, "safezone")) {
+      // list capacities grow on the device as needed: accepted, not used
+      if (numeric(val) < 0.0) throw Error("Illegal pair_style reax/c safezone command");
+    } else if (!std::strcmp(key, "mincap")) {
+      if (inumeric(val) < 0) throw Error("Illegal pair_style reax/c mincap command");
+    } else if (!std::strcmp(key, "maxfar")) {
+      if (inumeric(val) < 0) throw Error("Illegal pair_style reax/c maxfar command");
+    } else if (!std::strcmp(key, "precision")) {
+      if (!std::strcmp(val, "fp64")) params_.precision = RG_PREC_FP64;
+      else if (!std::strcmp(val, "mixed")) params_.precision = RG_PREC_MIXED;
+      else throw Error(illegal);
+    } else if (!std::strcmp(key, "device")) {
+      params_.device = (int)inumeric(val);
+    } else {
+      throw Error(illegal);
+    }
+    iarg += 2;
+  }
+}
+
+void PairReaxCGB300::coeff(int narg, char **arg) {
+  if (narg != 3 + atom_->ntypes) throw Error("Incorrect args for pair coefficients");
+  if (std::strcmp(arg[0], "*") != 0 || std::strcmp(arg[1], "*") != 0)
+    throw Error("Incorrect args for pair coefficients");
+  int nt = 0;
+  char msg[256] = {0};
+  if (rg_ffield_info(arg[2], &nt, nullptr, 0, msg, sizeof msg) != RG_OK)
+    throw Error(std::string("Cannot open ReaxFF potential file ") + arg[2]);
+  std::vector<char> names((size_t)nt * 16);
+  rg_ffield_info(arg[2], &nt, names.data(), 16, nullptr, 0);
+  elements_.clear();
+  for (int t = 0; t < nt; ++t) elements_.emplace_back(&names[(size_t)t * 16]);
+  ffield_ = arg[2];
+  // map[i] = ffield type of LAMMPS type i, -1 for NULL
+  map_.assign(atom_->ntypes + 1, -1);
+  int itmp = 0;
+  for (int i = 3; i < narg; ++i) {
+    if (!std::strcmp(arg[i], "NULL")) {
+      ++itmp;
+      continue;
+    }
+    for (int j = 0; j < nt; ++j)
+      if (!strcasecmp(arg[i], elements_[j].c_str())) {
+        map_[i - 2] = j;
+        ++itmp;
+      }
+  }
+  if (itmp != atom_->ntypes) throw Error("Non-existent ReaxFF type");
+  int count = 0;
+  for (int i = 1; i <= atom_->ntypes; ++i)
+    if (map_[i] >= 0) ++count;
+  if (count == 0) throw Error("Incorrect args for pair coefficients");
+}
+
+void PairReaxCGB300::init_style() {
+  if (!atom_->q_flag) throw Error("Pair style reax/c requires atom attribute q");
+  if (!fix_qeq_ && qeqflag == 1) throw Error("Pair reax/c requires use of fix qeq/reax");
+  if (atom_->tag_enable == 0) throw Error("Pair style reax/c requires atom IDs");
+  if (map_.empty()) throw Error("All pair coeffs are not set");
+  for (int i = 0; i < atom_->nlocal; ++i)
+    if (map_[atom_->type[i]] < 0)
+      throw Error("reax/c/gb300 computes every atom: NULL-mapped types are not supported");
+  // the device context is created at the first device call (setup), after
+  // every style's init has checked its arguments
+  if (h_) {
+    rg_destroy(h_);
+    h_ = nullptr;
+  }
+  chi_.assign(atom_->ntypes + 1, 0.0);
+  eta_.assign(atom_->ntypes + 1, 0.0);
+  gamma_.assign(atom_->ntypes + 1, 0.0);
+  uploaded_ = false;
+  host_dirty_ = true;
+  device_dirty_ = false;
+  have_forces_ = false;
+}
+
+void PairReaxCGB300::create_device() {
+  if (fix_qeq_) {
+    params_.qeq_swa = fix_qeq_->swa;
+    params_.qeq_swb = fix_qeq_->swb;
+    params_.qeq_tol = fix_qeq_->tolerance;
+    params_.qeq_imax = fix_qeq_->imax;
+  }
+  if (rg_create(ffield_.c_str(), &params_, &h_) != RG_OK || !h_)
+    throw Error("reax/c/gb300: cannot create the device context for " + ffield_);
+  const int nt = (int)elements_.size();
+  // integrator masses per ffield type from the data file's per-type masses
+  std::vector<double> m(nt, 0.0);
+  check(rg_extract(h_, "mass", m.data()), "rg_extract");
+  std::vector<int> seen(nt, 0);
+  for (int i = 1; i <= atom_->ntypes; ++i) {
+    const int t = map_[i];
+    if (t < 0 || (int)atom_->mass.size() <= i || !(atom_->mass[i] > 0.0)) continue;
+    if (seen[t] && m[t] != atom_->mass[i])
+      throw Error("reax/c/gb300: types mapped to one element need one mass");
+    m[t] = atom_->mass[i];
+    seen[t] = 1;
+  }
+  check(rg_set_masses(h_, m.data()), "rg_set_masses");
+  const double L[3] = {atom_->boxhi[0] - atom_->boxlo[0], atom_->boxhi[1] - atom_->boxlo[1],
+                       atom_->boxhi[2] - atom_->boxlo[2]};
+  check(rg_set_box(h_, L), "rg_set_box");
+}
+
+rg_system *PairReaxCGB300::handle() {
+  if (map_.empty() || chi_.empty()) throw Error("reax/c/gb300: init_style has not been called");
+  if (!h_) create_device();
+  return h_;
+}
+
+void PairReaxCGB300::check(int rc, const char *what) {
+  if (rc != RG_OK)
+    throw Error(std::string(what) + ": " + (h_ ? rg_last_error(h_) : "no device context"));
+}
+
+void PairReaxCGB300::sync_device() {
+  if (!host_dirty_) return;
+  if (device_dirty_)
+    throw Error("reax/c/gb300: host atom arrays modified while the device copy is newer "
+                "(call sync_host before editing them)");
+  rg_system *h = handle();
+  const int n = atom_->nlocal;
+  // positions wrapped into the box (LAMMPS keeps them there between
+  // re-neighbourings; the library's periodic images need [0, L))
+  std::vector<double> x(3 * (size_t)n);
+  for (int i = 0; i < n; ++i)
+    for (int c = 0; c < 3; ++c) {
+      const double lo = atom_->boxlo[c], L = atom_->boxhi[c] - atom_->boxlo[c];
+      double u = atom_->x[3 * i + c] - lo;
+      u -= L * std::floor(u / L);
+      if (u >= L) u -= L;
+      x[3 * i + c] = u;
+    }
+  if (!uploaded_) {
+    std::vector<int> t(n);
+    for (int i = 0; i < n; ++i) t[i] = map_[atom_->type[i]];
+    check(rg_set_atoms(h, n, x.data(), t.data(), atom_->tag.data(),
+                       atom_->q.empty() ? nullptr : atom_->q.data(),
+                       atom_->v.empty() ? nullptr : atom_->v.data()),
+          "rg_set_atoms");
+    uploaded_ = true;
+  } else {
+    // forces of edited positions are recomputed by the next force call
+    check(rg_set_state(h, x.data(), atom_->v.data(), nullptr), "rg_set_state");
+    have_forces_ = false;
+  }
+  host_dirty_ = false;
+}
+
+void PairReaxCGB300::sync_host() {
+  if (!device_dirty_) return;
+  rg_system *h = handle();
+  const int n = atom_->nlocal;
+  atom_->x.resize(3 * (size_t)n);
+  atom_->v.resize(3 * (size_t)n);
+  atom_->f.resize(3 * (size_t)n);
+  atom_->q.resize(n);
+  check(rg_get_atoms(h, atom_->x.data(), atom_->v.data(), atom_->q.data(), atom_->f.data()),
+        "rg_get_atoms");
+  // back to the LAMMPS box origin
+  for (int i = 0; i < n; ++i)
+    for (int c = 0; c < 3; ++c) atom_->x[3 * i + c] += atom_->boxlo[c];
+  device_dirty_ = false;
+}
+
+void PairReaxCGB300::compute(int eflag, int vflag) {
+  rg_system *h = handle();
+  sync_device();
+  double e[RG_NENERGY];
+  check(rg_compute(h, eflag, vflag, nullptr, eflag ? e : nullptr), "rg_compute");
+  have_forces_ = true;
+  modified_device();
+  if (eflag) {
+    // pvector order of pair_reaxc_sunway.cpp:657-670 and the tallied sums
+    for (int k = 0; k < 14; ++k) pvector[k] = e[k];
+    eng_vdwl = e[14];
+    eng_coul = e[15];
+  }
+}
+
+void *PairReaxCGB300::extract(const char *str, int &dim) {
+  dim = 1;
+  std::vector<double> *dst = nullptr;
+  if (!std::strcmp(str, "chi")) dst = &chi_;
+  else if (!std::strcmp(str, "eta")) dst = &eta_;
+  else if (!std::strcmp(str, "gamma")) dst = &gamma_;
+  if (!dst || !h_) return nullptr;
+  std::vector<double> per(elements_.size());
+  check(rg_extract(h_, str, per.data()), "rg_extract");
+  dst->assign(atom_->ntypes + 1, 0.0);
+  for (int i = 1; i <= atom_->ntypes; ++i) (*dst)[i] = map_[i] >= 0 ? per[map_[i]] : 0.0;
+  return dst->data();
+}
+
+// ---------------------------------------------------------------- fix qeq
+
+FixQEqReaxGB300::FixQEqReaxGB300(PairReaxCGB300 *pair, Update *update, int narg, char **arg)
+    : pair_(pair), update_(update) {
+  const char *illegal = "Illegal fix qeq/reax command";
+  if (narg < 8 || narg > 9) throw Error(illegal);
+  nevery = (int)inumeric(arg[3]);
+  if (nevery <= 0) throw Error(illegal);
+  swa = numeric(arg[4]);
+  swb = numeric(arg[5]);
+  tolerance = numeric(arg[6]);
+  // per-type chi/eta/gamma from the pair (extract); a parameter file is not
+  // supported (fix_qeq_reax_sunway.cpp:198-247)
+  if (std::strcmp(arg[7], "reax/c") != 0)
+    throw Error("fix qeq/reax/gb300 takes its parameters from pair reax/c/gb300 (reax/c)");
+  // the s and t systems are always solved together on the device
+  if (narg == 9 && std::strcmp(arg[8], "dual") != 0) throw Error(illegal);
+  if (!pair_) throw Error("No pair reax/c for fix qeq/reax");
+  pair_->attach_qeq(this);
+}
+
+void FixQEqReaxGB300::init() {
+  if (!pair_->atom_->q_flag) throw Error("Fix qeq/reax requires atom attribute q");
+  if (pair_->atom_->nlocal == 0) throw Error("Fix qeq/reax group has no atoms");
+  // init_taper (fix_qeq_reax_sunway.cpp:458-486) rejects these two
+  if (swb < 0) throw Error("Fix qeq/reax has negative upper Taper radius cutoff");
+  if (swa < 0) throw Error("Fix qeq/reax has negative lower Taper radius cutoff");
+}
+
+void FixQEqReaxGB300::setup_pre_force(int vflag) { pre_force(vflag); }
+
+void FixQEqReaxGB300::pre_force(int /*vflag*/) {
+  if (update_->ntimestep % nevery) return;
+  rg_system *h = pair_->handle();
+  pair_->sync_device();
+  int its = 0, itt = 0;
+  pair_->check(rg_qeq(h, nullptr, &its, &itt), "rg_qeq");
+  matvecs_s = its;
+  matvecs_t = itt;
+  matvecs = its + itt;
+  pair_->modified_device();
+}
+
+// ---------------------------------------------------------------- fix nve
+
+FixNVEGB300::FixNVEGB300(PairReaxCGB300 *pair, Update *update, int narg, char ** /*arg*/)
+    : pair_(pair), update_(update) {
+  if (narg < 3) throw Error("Illegal fix nve command");
+  if (!pair_) throw Error("fix nve/gb300 requires pair reax/c/gb300");
+}
+
+void FixNVEGB300::init() {
+  dtv = update_->dt;
+  dtf = 0.5 * update_->dt * FTM2V;
+}
+
+void FixNVEGB300::reset_dt() { init(); }
+
+void FixNVEGB300::initial_integrate(int /*vflag*/) {
+  pair_->sync_device();
+  pair_->check(rg_nve_initial(pair_->handle(), dtv), "rg_nve_initial");
+  pair_->modified_device();
+}
+
+void FixNVEGB300::final_integrate() {
+  pair_->sync_device();
+  pair_->check(rg_nve_final(pair_->handle(), dtv), "rg_nve_final");
+  pair_->modified_device();
+}
+
+// ---------------------------------------------------------------- Verlet
+
+void Verlet::setup() {
+  pair_->init_style();
+  if (qeq_) qeq_->init();
+  if (nve_) nve_->init();
+  if (qeq_) qeq_->setup_pre_force(0);
+  pair_->compute(1, 0);
+}
+
+void Verlet::run(long long nsteps, int thermo_every, void (*thermo)(const Verlet &, void *),
+                 void *ctx) {
+  for (long long s = 0; s < nsteps; ++s) {
+    ++update_->ntimestep;
+    const bool th = thermo_every > 0 &&
+                    (update_->ntimestep % thermo_every == 0 || s == nsteps - 1);
+    if (nve_) nve_->initial_integrate(0);
+    if (qeq_) qeq_->pre_force(0);
+    pair_->compute(th ? 1 : 0, 0);
+    if (nve_) nve_->final_integrate();
+    if (th) {
+      pair_->sync_host();
+      if (thermo) thermo(*this, ctx);
+    }
+  }
+  pair_->sync_host();
+}
+
+double Verlet::kinetic_energy() const {
+  // 0.5 m v^2 in kcal/mol (LAMMPS real: mvv2e)
+  double ke = 0.0;
+  if ((int)atom_->mass.size() <= atom_->ntypes) throw Error("Not all per-type masses are set");
+  for (int i = 0; i < atom_->nlocal; ++i) {
+    const double m = atom_->mass[atom_->type[i]];
+    const double *v = &atom_->v[3 * (size_t)i];
+    ke += m * (v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+  }
+  return 0.5 * MVV2E * ke;
+}
+
+}  // namespace reaxgb

@@ -279,3 +279,32 @@ def small_pack(n_atoms_target: int, density: float, seed: int) -> System:
         n += len(MOLECULES[k][0])
     counts = {k: v for k, v in counts.items() if v}
     return pack_molecules(counts, density, seed + 1)
+
+
+def write_lammps_data(system: System, path: str, elements=None, q=None) -> list:
+    """Write a LAMMPS data file (atom_style charge: Masses, Atoms with
+    "id type q x y z", Velocities) of an orthogonal periodic system, the input
+    format of the reference's decks (read_data).  LAMMPS type k is
+    elements[k-1] (default: the elements present, sorted).  Returns the
+    element order for pair_coeff."""
+    els = list(elements) if elements is not None else sorted(set(system.elem))
+    tidx = {e: k + 1 for k, e in enumerate(els)}
+    q = np.zeros(system.n) if q is None else np.asarray(q, np.float64)
+    with open(path, "w") as fp:
+        fp.write("ReaxFF system written by sw_reaxff_gb300.systems\n\n")
+        fp.write(f"{system.n} atoms\n{len(els)} atom types\n\n")
+        for c, nm in enumerate(("x", "y", "z")):
+            fp.write(f"0.0 {float(system.box[c])!r} {nm}lo {nm}hi\n")
+        fp.write("\nMasses\n\n")
+        for e in els:
+            fp.write(f"{tidx[e]} {float(MASS[e])!r}\n")
+        fp.write("\nAtoms # charge\n\n")
+        for i in range(system.n):
+            x = system.x[i]
+            fp.write(f"{int(system.tag[i])} {tidx[system.elem[i]]} {float(q[i])!r} "
+                     f"{float(x[0])!r} {float(x[1])!r} {float(x[2])!r}\n")
+        fp.write("\nVelocities\n\n")
+        for i in range(system.n):
+            v = system.v[i]
+            fp.write(f"{int(system.tag[i])} {float(v[0])!r} {float(v[1])!r} {float(v[2])!r}\n")
+    return els

@@ -118,6 +118,21 @@ int rg_set_masses(rg_system *h, const double *mass);
 /* Orthogonal periodic box [0,L0)x[0,L1)x[0,L2). */
 int rg_set_box(rg_system *h, const double *L3);
 
+/* Independent systems in one handle ("segments", for batched evaluation
+ * of many small systems): nseg orthogonal periodic boxes (boxes[3*nseg]),
+ * segment k holding counts[k] consecutive atoms of the arrays given to
+ * rg_set_atoms (whose n must be the sum).  Every call then works on all
+ * segments at once: lists, QEq (each segment's own CG scalars and
+ * convergence, fix_qeq_reax_sunway.cpp:983-1167 per system), forces and
+ * NVE.  rg_set_box is the one-segment case.  rg_compute's energies are the
+ * sums over segments; rg_get_energies gives them per segment
+ * (e[nseg][RG_NENERGY]) and rg_get_segment_iters the s and t CG iterations
+ * of the last QEq per segment (iters[2*nseg]). */
+int rg_set_segments(rg_system *h, int nseg, const int *counts, const double *boxes);
+int rg_num_segments(const rg_system *h);
+int rg_get_energies(rg_system *h, double *e);
+int rg_get_segment_iters(rg_system *h, int *iters);
+
 /* Host arrays of n atoms: x[3n] (wrapped into the box), type[n] (0-based
  * ffield type), tag[n] (1-based global id; NULL -> 1..n), q[n] (NULL -> 0),
  * v[3n] (NULL -> 0).  Resets the QEq histories. */

@@ -29,7 +29,8 @@ EXPORTED = ["rg_default_params", "rg_create", "rg_destroy", "rg_last_error",
             "rg_get_atoms", "rg_device_arrays", "rg_get_stats", "rg_synchronize",
             "rg_dump_pairs", "rg_dump_bonds", "rg_dump_hbonds", "rg_set_state",
             "rg_stream", "rg_profile_enable", "rg_profile_get", "rg_measure_fp64_peak",
-            "rg_qeq_noalloc", "rg_set_masses", "rg_ffield_info"]
+            "rg_qeq_noalloc", "rg_set_masses", "rg_ffield_info", "rg_set_segments",
+            "rg_num_segments", "rg_get_energies", "rg_get_segment_iters"]
 
 
 class Params(C.Structure):
@@ -79,6 +80,10 @@ def load_library(path: str = LIBPATH):
     L.rg_extract.argtypes = [C.c_void_p, C.c_char_p, dp]
     L.rg_set_box.argtypes = [C.c_void_p, dp]
     L.rg_set_masses.argtypes = [C.c_void_p, dp]
+    L.rg_set_segments.argtypes = [C.c_void_p, C.c_int, ip, dp]
+    L.rg_num_segments.argtypes = [C.c_void_p]
+    L.rg_get_energies.argtypes = [C.c_void_p, dp]
+    L.rg_get_segment_iters.argtypes = [C.c_void_p, ip]
     L.rg_ffield_info.argtypes = [C.c_char_p, ip, C.c_char_p, C.c_int, C.c_char_p, C.c_int]
     L.rg_set_atoms.argtypes = [C.c_void_p, C.c_int, dp, ip, ip, dp, dp]
     L.rg_set_atoms_device.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p,
@@ -213,6 +218,36 @@ class ReaxGPU:
         """Load a sw_reaxff_gb300.systems.System."""
         self.set_box(system.box)
         self.set_atoms(system.x, system.types(self.elements), system.tag, None, system.v)
+
+    def set_systems(self, systems_list):
+        """Load several independent systems as segments of one handle
+        (batched evaluation): every call then works on all of them.
+        Returns the atom offset of each system in the concatenated arrays."""
+        counts = np.array([s.n for s in systems_list], np.int32)
+        boxes = np.ascontiguousarray(np.stack([s.box for s in systems_list]), np.float64)
+        self._chk(self.L.rg_set_segments(self.h, len(systems_list), _ip(counts), _dp(boxes)),
+                  "rg_set_segments")
+        x = np.concatenate([s.x for s in systems_list])
+        types = np.concatenate([s.types(self.elements) for s in systems_list])
+        tags = np.concatenate([s.tag for s in systems_list])
+        v = np.concatenate([s.v for s in systems_list])
+        self.set_atoms(x, types, tags, None, v)
+        self.nseg = len(systems_list)
+        return np.concatenate([[0], np.cumsum(counts)[:-1]])
+
+    def energies(self):
+        """Per-segment energy vectors of the last force step (dicts)."""
+        ns = self.L.rg_num_segments(self.h)
+        e = np.zeros((ns, NENERGY))
+        self._chk(self.L.rg_get_energies(self.h, _dp(e)), "rg_get_energies")
+        return [dict(zip(ENERGY_NAMES, row)) for row in e]
+
+    def segment_iters(self):
+        """(s, t) CG iterations of the last QEq per segment."""
+        ns = self.L.rg_num_segments(self.h)
+        it = np.zeros(2 * ns, np.int32)
+        self._chk(self.L.rg_get_segment_iters(self.h, _ip(it)), "rg_get_segment_iters")
+        return it.reshape(ns, 2)
 
     def set_positions(self, x):
         x = np.ascontiguousarray(x, np.float64)

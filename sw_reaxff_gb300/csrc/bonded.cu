@@ -30,19 +30,9 @@ __device__ __forceinline__ R deg2rad(R a) { return a * R(constPI) / R(180); }
 template <typename R>
 __device__ __forceinline__ R sqr(R x) { return x * x; }
 
-// per-block reduction of one value into dst (FP64 atomic)
-__device__ __forceinline__ void block_add(double v, double *dst) {
-  __shared__ double red[32];
-  for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(FULL, v, off);
-  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
-  __syncthreads();
-  if (l == 0) red[w] = v;
-  __syncthreads();
-  if (w == 0) {
-    v = (l < (int)(blockDim.x >> 5)) ? red[l] : 0.0;
-    for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(FULL, v, off);
-    if (l == 0 && v != 0.0) atomicAdd(dst, v);
-  }
+// per-block reduction of one energy term into segment seg's entry E
+__device__ __forceinline__ void energy_add(const Dev &d, double v, int seg, int E) {
+  seg_block_add<1>(&v, seg, d.energy + E, RG_NE);
 }
 
 __device__ __forceinline__ void add3(double *fC, int n, int a, double s, double x, double y, double z) {
@@ -53,6 +43,14 @@ __device__ __forceinline__ void add3(double *fC, int n, int a, double s, double 
 
 __device__ __forceinline__ int nbr_of(uint32_t e) { return (int)(e >> 8); }
 
+// diagnostics: keeps the first non-finite term (kind 1 angle, 2 torsion)
+__device__ void debug_record(const Dev &d, int kind, int a, int b, int c, int e, const double *v,
+                             int nv) {
+  if (atomicCAS(d.dbg_flag, 0, 1) != 0) return;
+  d.dbg[0] = kind; d.dbg[1] = a; d.dbg[2] = b; d.dbg[3] = c; d.dbg[4] = e;
+  for (int k = 0; k < nv && k < 35; ++k) d.dbg[5 + k] = v[k];
+}
+
 // (tag, position) order deciding which end of a bond / central torsion
 // bond carries the term, reaxc_multi_body_sw64.c:256-267
 __device__ __forceinline__ bool tag_first(const Dev &d, int i, int j, uint32_t e) {
@@ -62,7 +60,8 @@ __device__ __forceinline__ bool tag_first(const Dev &d, int i, int j, uint32_t e
     int sx, sy, sz;
     img_unpack((int)(e & 255u), &sx, &sy, &sz);
     const double4 xi = d.xs[i], xj0 = d.xs[j];
-    const double xj = xj0.x + sx * d.L[0], yj = xj0.y + sy * d.L[1], zj = xj0.z + sz * d.L[2];
+    const double *L = d.seg[d.seg_s[i]].L;
+    const double xj = xj0.x + sx * L[0], yj = xj0.y + sy * L[1], zj = xj0.z + sz * L[2];
     if (zj < xi.z) return false;
     if (zj == xi.z && yj < xi.y) return false;
     if (zj == xi.z && yj == xi.y && xj < xi.x) return false;
@@ -230,10 +229,11 @@ __global__ void k_atom_energy(Dev d, int eflag) {
     const int nb = min(d.nbonds[i], d.bond_cap);
     // polarisation (Compute_Polarization_Energy inlined at :93-104); the
     // reference's pvector value is the running sum, = sum_k pol_k*(n-k) over
-    // the original atom order
+    // the original atom order of the segment
     const double q = d.xs[i].w;
     pol = KCALpMOL_to_EV * (si.chi * q + (si.eta / 2.) * sqr(q));
-    pol_w = pol * (double)(n - d.perm[i]);
+    const SegGeom &g = d.seg[d.seg_s[i]];
+    pol_w = pol * (double)(g.atom0 + g.natoms - d.perm[i]);
     const double p_lp2 = si.p_lp2;
     const double Dlp_i = d.Delta_lp[i];
     const double expvd2 = exp(-75 * Dlp_i);
@@ -343,13 +343,14 @@ __global__ void k_atom_energy(Dev d, int eflag) {
     atomicAdd(&CdD[i], cd_i);
   }
   if (eflag) {
-    block_add(ebond + estriph, &d.energy[E_BOND]);
-    block_add(e_ov + e_un, &d.energy[E_OVUN]);
-    block_add(e_lp + e_lph, &d.energy[E_LP]);
-    block_add(e_lph + e_lp + e_ov + ebond + estriph + e_un, &d.energy[E_ENG_VDWL]);
-    block_add(pol, &d.energy[E_ENG_COUL]);
-    block_add(pol, &d.energy[E_POL_PHYS]);
-    block_add(pol_w, &d.energy[E_POL]);
+    const int sg = i < n ? d.seg_s[i] : -1;
+    energy_add(d, ebond + estriph, sg, E_BOND);
+    energy_add(d, e_ov + e_un, sg, E_OVUN);
+    energy_add(d, e_lp + e_lph, sg, E_LP);
+    energy_add(d, e_lph + e_lp + e_ov + ebond + estriph + e_un, sg, E_ENG_VDWL);
+    energy_add(d, pol, sg, E_ENG_COUL);
+    energy_add(d, pol, sg, E_POL_PHYS);
+    energy_add(d, pol_w, sg, E_POL);
   }
 }
 
@@ -377,6 +378,7 @@ __global__ void __launch_bounds__(256) k_hbonds(Dev d, int eflag) {
     const int nb = min(d.nbonds[j], d.bond_cap);
     const int nh = min(d.nhb[j], d.hb_cap);
     const double4 xj = d.xs[j];
+    const double *L = d.seg[d.seg_s[j]].L;
     double *fC = d.fC;
     double fjx = 0, fjy = 0, fjz = 0;
     for (int q = 0; q < nb; ++q) {
@@ -400,9 +402,9 @@ __global__ void __launch_bounds__(256) k_hbonds(Dev d, int eflag) {
         img_unpack((int)(ek & 255u), &sx, &sy, &sz);
         const double4 xk = d.xs[k];
         double dk64[3];
-        dk64[0] = __dsub_rn(__dadd_rn(xk.x, sx * d.L[0]), xj.x);
-        dk64[1] = __dsub_rn(__dadd_rn(xk.y, sy * d.L[1]), xj.y);
-        dk64[2] = __dsub_rn(__dadd_rn(xk.z, sz * d.L[2]), xj.z);
+        dk64[0] = __dsub_rn(__dadd_rn(xk.x, sx * L[0]), xj.x);
+        dk64[1] = __dsub_rn(__dadd_rn(xk.y, sy * L[1]), xj.y);
+        dk64[2] = __dsub_rn(__dadd_rn(xk.z, sz * L[2]), xj.z);
         const double r64 = __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(dk64[0], dk64[0]),
                                                           __dmul_rn(dk64[1], dk64[1])),
                                                 __dmul_rn(dk64[2], dk64[2])));
@@ -447,8 +449,9 @@ __global__ void __launch_bounds__(256) k_hbonds(Dev d, int eflag) {
     if (lane == 0 && (fjx != 0.0 || fjy != 0.0 || fjz != 0.0)) add3(fC, n, j, 1.0, fjx, fjy, fjz);
   }
   if (eflag) {
-    block_add(ehb, &d.energy[E_HB]);
-    block_add(ehb, &d.energy[E_ENG_VDWL]);
+    const int sg = j < n ? d.seg_s[j] : -1;
+    energy_add(d, ehb, sg, E_HB);
+    energy_add(d, ehb, sg, E_ENG_VDWL);
   }
 }
 
@@ -767,6 +770,15 @@ __device__ __forceinline__ void valence_item(const Dev &d, unsigned long long it
         atomicAdd(&d.b_Cdbopi[sq], (double)CEval5);
         atomicAdd(&d.b_Cdbopi2[sq], (double)CEval5);
       }
+      if (d.debug) {
+        const double v[] = {BOA_jk, BOA_hj, theta_hjk, sin_theta_hjk, SBO2, CSBO2, dSBO1, dSBO2,
+                            expval6, Delta_j, f7_jk, f7_hj, f8_Dj, expval2theta, theta_0, CEval1,
+                            CEval2, CEval3, CEval4, CEval5, CEval8, epen, ecoa, exp_coa2, Cf7jk,
+                            Cf7hj, Cf8j, CEpen1, CEcoa3, (double)cnt};
+        double sum = 0.0;
+        for (double x : v) sum += x;
+        if (!isfinite(sum)) debug_record(d, 1, j, kk, ph, 0, v, (int)(sizeof(v) / sizeof(v[0])));
+      }
       const double c8 = (double)CEval8;
       add3(fC, n, k, c8, (double)di[0], (double)di[1], (double)di[2]);
       add3(fC, n, j, c8, (double)dj[0], (double)dj[1], (double)dj[2]);
@@ -786,13 +798,13 @@ __device__ __forceinline__ bool near_linear(const Dev &d, long long sa, long lon
   return fabsf(c) > 0.9998f;
 }
 
-__device__ __forceinline__ void valence_energies(const Dev &d, int eflag, double e_ang, double e_pen,
-                                                 double e_coa) {
+__device__ __forceinline__ void valence_energies(const Dev &d, int eflag, int sg, double e_ang,
+                                                 double e_pen, double e_coa) {
   if (eflag) {
-    block_add(e_ang, &d.energy[E_ANG]);
-    block_add(e_pen, &d.energy[E_PEN]);
-    block_add(e_coa, &d.energy[E_COA]);
-    block_add(e_ang + e_pen + e_coa, &d.energy[E_ENG_VDWL]);
+    energy_add(d, e_ang, sg, E_ANG);
+    energy_add(d, e_pen, sg, E_PEN);
+    energy_add(d, e_coa, sg, E_COA);
+    energy_add(d, e_ang + e_pen + e_coa, sg, E_ENG_VDWL);
   }
 }
 
@@ -800,8 +812,10 @@ template <typename R>
 __global__ void __launch_bounds__(128) k_valence(Dev d, int eflag, long long nitems) {
   const long long w = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   double e_ang = 0, e_pen = 0, e_coa = 0;
+  int sg = -1;
   if (w < nitems) {
     const unsigned long long it = d.w_val[w];
+    sg = d.seg_s[(int)(it >> 16)];
     if (std::is_same<R, float>::value) {
       const int j = (int)(it >> 16), kk = (int)((it >> 8) & 255), ph = (int)(it & 255);
       if (near_linear(d, (long long)kk * d.n + j, (long long)ph * d.n + j))
@@ -812,18 +826,26 @@ __global__ void __launch_bounds__(128) k_valence(Dev d, int eflag, long long nit
       valence_item<R>(d, it, e_ang, e_pen, e_coa);
     }
   }
-  valence_energies(d, eflag, e_ang, e_pen, e_coa);
+  valence_energies(d, eflag, sg, e_ang, e_pen, e_coa);
 }
 
 // the FP64 pass over the queued near-linear angles (grid-stride over the
-// device-side count)
+// device-side count; few items, so energies go straight to their segment)
 __global__ void __launch_bounds__(128) k_valence_fb(Dev d, int eflag) {
-  double e_ang = 0, e_pen = 0, e_coa = 0;
   const long long cnt = d.fb_cnt[0];
   for (long long w = (long long)blockIdx.x * blockDim.x + threadIdx.x; w < cnt;
-       w += (long long)gridDim.x * blockDim.x)
-    valence_item<double>(d, d.w_fb_val[w], e_ang, e_pen, e_coa);
-  valence_energies(d, eflag, e_ang, e_pen, e_coa);
+       w += (long long)gridDim.x * blockDim.x) {
+    double e_ang = 0, e_pen = 0, e_coa = 0;
+    const unsigned long long it = d.w_fb_val[w];
+    valence_item<double>(d, it, e_ang, e_pen, e_coa);
+    if (eflag) {
+      double *E = d.energy + (long long)d.seg_s[(int)(it >> 16)] * RG_NE;
+      atomicAdd(&E[E_ANG], e_ang);
+      atomicAdd(&E[E_PEN], e_pen);
+      atomicAdd(&E[E_COA], e_coa);
+      atomicAdd(&E[E_ENG_VDWL], e_ang + e_pen + e_coa);
+    }
+  }
 }
 
 // one torsion h-j-k-l (with its 4-body conjugation term); R as in k_valence
@@ -925,6 +947,15 @@ __device__ __forceinline__ void torsion_item(const Dev &d, unsigned long long it
     atomicAdd(&d.b_Cdbo[spk], (double)(CEtors5 + CEconj2));
     atomicAdd(&d.b_Cdbo[spw], (double)(CEtors6 + CEconj3));
     const R c78 = CEtors7 + CEconj4, c85 = CEtors8 + CEconj5, c96 = CEtors9 + CEconj6;
+    if (d.debug) {
+      const double v[] = {BOA_ij, BOA_jk, BOA_kl, p_ijk.theta, p_jkl.theta, sin_ijk, sin_jkl,
+                          tan_ijk_i, tan_jkl_i, omega, r_li, exp_tor1, fn10, CV, c78, c85, c96,
+                          CEtors2, CEtors3, CEtors4, CEtors5, CEtors6, doi[0], doj[0], dok[0],
+                          dol[0], f11_DjDk, dfn11, Delta_j, Delta_k};
+      double sum = 0.0;
+      for (double x : v) sum += x;
+      if (!isfinite(sum)) debug_record(d, 2, j, kk, ph, pw, v, (int)(sizeof(v) / sizeof(v[0])));
+    }
     add3(fC, n, i, 1.0, (double)(c78 * p_ijk.dk[0] + c96 * doi[0]), (double)(c78 * p_ijk.dk[1] + c96 * doi[1]),
          (double)(c78 * p_ijk.dk[2] + c96 * doi[2]));
     add3(fC, n, j, 1.0, (double)(c78 * p_ijk.dj[0] + c85 * p_jkl.di[0] + c96 * doj[0]),
@@ -938,11 +969,12 @@ __device__ __forceinline__ void torsion_item(const Dev &d, unsigned long long it
   }
 }
 
-__device__ __forceinline__ void torsion_energies(const Dev &d, int eflag, double e_tor, double e_con) {
+__device__ __forceinline__ void torsion_energies(const Dev &d, int eflag, int sg, double e_tor,
+                                                 double e_con) {
   if (eflag) {
-    block_add(e_tor, &d.energy[E_TOR]);
-    block_add(e_con, &d.energy[E_CON]);
-    block_add(e_tor + e_con, &d.energy[E_ENG_VDWL]);
+    energy_add(d, e_tor, sg, E_TOR);
+    energy_add(d, e_con, sg, E_CON);
+    energy_add(d, e_tor + e_con, sg, E_ENG_VDWL);
   }
 }
 
@@ -950,8 +982,10 @@ template <typename R>
 __global__ void __launch_bounds__(128) k_torsion(Dev d, int eflag, long long nitems) {
   const long long w = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   double e_tor = 0, e_con = 0;
+  int sg = -1;
   if (w < nitems) {
     const unsigned long long it = d.w_tor[w];
+    sg = d.seg_s[(int)(it >> 24)];
     if (std::is_same<R, float>::value) {
       const int n = d.n;
       const int j = (int)(it >> 24), kk = (int)((it >> 16) & 255);
@@ -967,16 +1001,23 @@ __global__ void __launch_bounds__(128) k_torsion(Dev d, int eflag, long long nit
       torsion_item<R>(d, it, e_tor, e_con);
     }
   }
-  torsion_energies(d, eflag, e_tor, e_con);
+  torsion_energies(d, eflag, sg, e_tor, e_con);
 }
 
 __global__ void __launch_bounds__(128) k_torsion_fb(Dev d, int eflag) {
-  double e_tor = 0, e_con = 0;
   const long long cnt = d.fb_cnt[1];
   for (long long w = (long long)blockIdx.x * blockDim.x + threadIdx.x; w < cnt;
-       w += (long long)gridDim.x * blockDim.x)
-    torsion_item<double>(d, d.w_fb_tor[w], e_tor, e_con);
-  torsion_energies(d, eflag, e_tor, e_con);
+       w += (long long)gridDim.x * blockDim.x) {
+    double e_tor = 0, e_con = 0;
+    const unsigned long long it = d.w_fb_tor[w];
+    torsion_item<double>(d, it, e_tor, e_con);
+    if (eflag) {
+      double *E = d.energy + (long long)d.seg_s[(int)(it >> 24)] * RG_NE;
+      atomicAdd(&E[E_TOR], e_tor);
+      atomicAdd(&E[E_CON], e_con);
+      atomicAdd(&E[E_ENG_VDWL], e_tor + e_con);
+    }
+  }
 }
 
 // ------------------------------------------------------------------

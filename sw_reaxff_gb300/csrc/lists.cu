@@ -50,16 +50,17 @@ __device__ __forceinline__ int cell_of(double x, double w, int nc) {
 __global__ void k_cell_assign(Dev d) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= d.n) return;
-  double x = wrap1(d.x_o[3 * i + 0], d.L[0]);
-  double y = wrap1(d.x_o[3 * i + 1], d.L[1]);
-  double z = wrap1(d.x_o[3 * i + 2], d.L[2]);
+  const SegGeom &g = d.seg[d.seg_o[i]];
+  double x = wrap1(d.x_o[3 * i + 0], g.L[0]);
+  double y = wrap1(d.x_o[3 * i + 1], g.L[1]);
+  double z = wrap1(d.x_o[3 * i + 2], g.L[2]);
   d.x_o[3 * i + 0] = x;
   d.x_o[3 * i + 1] = y;
   d.x_o[3 * i + 2] = z;
-  int cx = cell_of(x, d.cellw[0], d.nc[0]);
-  int cy = cell_of(y, d.cellw[1], d.nc[1]);
-  int cz = cell_of(z, d.cellw[2], d.nc[2]);
-  int c = (cz * d.nc[1] + cy) * d.nc[0] + cx;
+  int cx = cell_of(x, g.cellw[0], g.nc[0]);
+  int cy = cell_of(y, g.cellw[1], g.nc[1]);
+  int cz = cell_of(z, g.cellw[2], g.nc[2]);
+  int c = g.cell0 + (cz * g.nc[1] + cy) * g.nc[0] + cx;
   d.cell_o[i] = c;
   atomicAdd(&d.cell_count[c], 1);
 }
@@ -143,6 +144,7 @@ __global__ void k_gather(Dev d) {
   d.xf[s] = make_float4((float)x, (float)y, (float)z, __int_as_float(t));
   d.ts[s] = t;
   d.tags[s] = d.tag_o[i];
+  d.seg_s[s] = d.seg_o[i];
   d.iperm[i] = s;
 }
 
@@ -171,7 +173,7 @@ template <bool MIXED>
 __device__ __forceinline__ void nbr_flush(const Dev &d, const Control &C, const ForceField &F,
                                           const NbrQueue &Q, int cnt, int lane, int i,
                                           const double4 &xi, int ti, long long row, int cap,
-                                          int &cntN, int &cntF) {
+                                          const double *L, int &cntN, int &cntF) {
   bool in = false, near = false;
   double d2 = 0.0;
   int j = 0, img = 0;
@@ -181,9 +183,9 @@ __device__ __forceinline__ void nbr_flush(const Dev &d, const Control &C, const 
     int sx, sy, sz;
     img_unpack(img, &sx, &sy, &sz);
     const double4 xj = d.xs[j];
-    const double dx = __dsub_rn(__dadd_rn(xj.x, sx * d.L[0]), xi.x);
-    const double dy = __dsub_rn(__dadd_rn(xj.y, sy * d.L[1]), xi.y);
-    const double dz = __dsub_rn(__dadd_rn(xj.z, sz * d.L[2]), xi.z);
+    const double dx = __dsub_rn(__dadd_rn(xj.x, sx * L[0]), xi.x);
+    const double dy = __dsub_rn(__dadd_rn(xj.y, sy * L[1]), xi.y);
+    const double dz = __dsub_rn(__dadd_rn(xj.z, sz * L[2]), xi.z);
     d2 = __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
     in = d2 <= C.list_cut2;
     if (in) {
@@ -263,36 +265,39 @@ __global__ void __launch_bounds__(NB_WARPS * 32) k_build_nbrs(Dev d) {
   const float4 xif = d.xf[i];
   const int ti = d.ts[i];
   const float cut2f = (float)(C.list_cut2 * (1.0 + 1e-5) + 0.05);
-  const int cx = cell_of(xi.x, d.cellw[0], d.nc[0]);
-  const int cy = cell_of(xi.y, d.cellw[1], d.nc[1]);
-  const int cz = cell_of(xi.z, d.cellw[2], d.nc[2]);
+  const SegGeom &g = d.seg[d.seg_s[i]];
+  const double L[3] = {g.L[0], g.L[1], g.L[2]};
+  const int ncx = g.nc[0], ncy = g.nc[1], ncz = g.nc[2], S = g.S;
+  const int cx = cell_of(xi.x, g.cellw[0], ncx);
+  const int cy = cell_of(xi.y, g.cellw[1], ncy);
+  const int cz = cell_of(xi.z, g.cellw[2], ncz);
   const long long row = (long long)i * d.nb_cap;
   const int cap = d.nb_cap;
-  const int nx = d.nc[0];
+  const int nx = ncx;
   int cntN = 0, cntF = 0, qn = 0;
-  for (int oz = -d.S; oz <= d.S; ++oz) {
+  for (int oz = -S; oz <= S; ++oz) {
     int rz = cz + oz, sz = 0;
-    while (rz < 0) { rz += d.nc[2]; --sz; }
-    while (rz >= d.nc[2]) { rz -= d.nc[2]; ++sz; }
-    for (int oy = -d.S; oy <= d.S; ++oy) {
+    while (rz < 0) { rz += ncz; --sz; }
+    while (rz >= ncz) { rz -= ncz; ++sz; }
+    for (int oy = -S; oy <= S; ++oy) {
       int ry = cy + oy, sy = 0;
-      while (ry < 0) { ry += d.nc[1]; --sy; }
-      while (ry >= d.nc[1]) { ry -= d.nc[1]; ++sy; }
-      const int rowcell = (rz * d.nc[1] + ry) * nx;
+      while (ry < 0) { ry += ncy; --sy; }
+      while (ry >= ncy) { ry -= ncy; ++sy; }
+      const int rowcell = g.cell0 + (rz * ncy + ry) * nx;
       // runs of consecutive cells with one x image each
-      int ox = -d.S;
-      while (ox <= d.S) {
+      int ox = -S;
+      while (ox <= S) {
         int rx = cx + ox, sx = 0;
         while (rx < 0) { rx += nx; --sx; }
         while (rx >= nx) { rx -= nx; ++sx; }
         int len = 1;
-        while (ox + len <= d.S && rx + len < nx) ++len;
+        while (ox + len <= S && rx + len < nx) ++len;
         const int beg = d.cell_start[rowcell + rx];
         const int end = d.cell_start[rowcell + rx + len];
         ox += len;
-        const float shxf = (float)(sx * d.L[0]);
-        const float shyf = (float)(sy * d.L[1]);
-        const float shzf = (float)(sz * d.L[2]);
+        const float shxf = (float)(sx * L[0]);
+        const float shyf = (float)(sy * L[1]);
+        const float shzf = (float)(sz * L[2]);
         const bool self_img = (sx == 0 && sy == 0 && sz == 0);
         const int img = img_pack(sx, sy, sz);
         for (int base = beg; base < end; base += 32) {
@@ -314,7 +319,7 @@ __global__ void __launch_bounds__(NB_WARPS * 32) k_build_nbrs(Dev d) {
           qn += __popc(mc);
           __syncwarp();
           if (qn >= 32) {
-            nbr_flush<MIXED>(d, C, F, Q, 32, lane, i, xi, ti, row, cap, cntN, cntF);
+            nbr_flush<MIXED>(d, C, F, Q, 32, lane, i, xi, ti, row, cap, L, cntN, cntF);
             __syncwarp();
             // move the leftover (< 32) to the front of the queue
             const int left = qn - 32;
@@ -335,7 +340,7 @@ __global__ void __launch_bounds__(NB_WARPS * 32) k_build_nbrs(Dev d) {
       }
     }
   }
-  if (qn > 0) nbr_flush<MIXED>(d, C, F, Q, qn, lane, i, xi, ti, row, cap, cntN, cntF);
+  if (qn > 0) nbr_flush<MIXED>(d, C, F, Q, qn, lane, i, xi, ti, row, cap, L, cntN, cntF);
   if (lane == 0) {
     d.n_near[i] = cntN;
     d.n_far[i] = cntF;
@@ -464,6 +469,8 @@ __global__ void __launch_bounds__(NB_WARPS * 32) k_build_bonds(Dev d) {
   const long long row = (long long)i * d.nb_cap;
   const int nn = d.n_near[i] < d.nb_cap ? d.n_near[i] : d.nb_cap;
   const int n = d.n;
+  const SegGeom &g = d.seg[d.seg_s[i]];
+  const double L[3] = {g.L[0], g.L[1], g.L[2]};
   // FP32 prefilter radius: anything that could be within bond_cut, and for
   // H atoms within hbond_cut
   const float rpre = (float)((ihb ? fmax(C.bond_cut, C.hbond_cut) : C.bond_cut) + 0.01);
@@ -483,14 +490,14 @@ __global__ void __launch_bounds__(NB_WARPS * 32) k_build_bonds(Dev d) {
         int sx, sy, sz;
         img_unpack((int)(e & 255u), &sx, &sy, &sz);
         const float4 xjf = d.xf[j];
-        const float fx = xjf.x + (float)(sx * d.L[0]) - xif.x;
-        const float fy = xjf.y + (float)(sy * d.L[1]) - xif.y;
-        const float fz = xjf.z + (float)(sz * d.L[2]) - xif.z;
+        const float fx = xjf.x + (float)(sx * L[0]) - xif.x;
+        const float fy = xjf.y + (float)(sy * L[1]) - xif.y;
+        const float fz = xjf.z + (float)(sz * L[2]) - xif.z;
         if (fx * fx + fy * fy + fz * fz <= rpre2) {
           const double4 xj = d.xs[j];
-          dx = __dsub_rn(__dadd_rn(xj.x, sx * d.L[0]), xi.x);
-          dy = __dsub_rn(__dadd_rn(xj.y, sy * d.L[1]), xi.y);
-          dz = __dsub_rn(__dadd_rn(xj.z, sz * d.L[2]), xi.z);
+          dx = __dsub_rn(__dadd_rn(xj.x, sx * L[0]), xi.x);
+          dy = __dsub_rn(__dadd_rn(xj.y, sy * L[1]), xi.y);
+          dz = __dsub_rn(__dadd_rn(xj.z, sz * L[2]), xi.z);
           const double d2 = __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
           dist = __dsqrt_rn(d2);
           const int tj = __float_as_int(xjf.w);
@@ -620,7 +627,7 @@ void launch_count(const Dev &d, cudaStream_t st) {
 }
 
 void launch_bin_sort(const Dev &d, cudaStream_t st) {
-  const int ncell = d.nc[0] * d.nc[1] * d.nc[2];
+  const int ncell = d.ncell;
   cudaMemsetAsync(d.cell_count, 0, sizeof(int) * (ncell + 1), st);
   cudaMemsetAsync(d.cell_fill, 0, sizeof(int) * (ncell + 1), st);
   const int B = 256;

@@ -23,20 +23,6 @@ __device__ __forceinline__ double warp_sum(double v) {
   return v;
 }
 
-__device__ __forceinline__ void block_add(double v, double *dst) {
-  __shared__ double red[32];
-  v = warp_sum(v);
-  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
-  __syncthreads();
-  if (l == 0) red[w] = v;
-  __syncthreads();
-  if (w == 0) {
-    v = (l < (int)(blockDim.x >> 5)) ? red[l] : 0.0;
-    v = warp_sum(v);
-    if (l == 0 && v != 0.0) atomicAdd(dst, v);
-  }
-}
-
 constexpr int NBW = 8;     // warps per block
 constexpr int QC = 64;     // queue slots per warp
 
@@ -87,8 +73,8 @@ __device__ __forceinline__ void taper(const Control &C, R r, R rinv, R &Tp, R &d
 template <typename R>
 __device__ __forceinline__ void pair_terms(const Dev &d, const ForceField &F, const Control &C,
                                           uint32_t e, bool act, const double4 &xi, int ti,
-                                          double &evdw, double &eele, double &c, double &dx,
-                                          double &dy, double &dz, int &j) {
+                                          const double *L, double &evdw, double &eele, double &c,
+                                          double &dx, double &dy, double &dz, int &j) {
   c = 0.0; dx = dy = dz = 0.0;
   j = (int)(e >> 8);
   if (!act) return;
@@ -96,9 +82,9 @@ __device__ __forceinline__ void pair_terms(const Dev &d, const ForceField &F, co
   img_unpack((int)(e & 255u), &sx, &sy, &sz);
   const double4 xj = d.xs[j];
   // same rounding as the pair-list membership test
-  dx = __dsub_rn(__dadd_rn(xj.x, sx * d.L[0]), xi.x);
-  dy = __dsub_rn(__dadd_rn(xj.y, sy * d.L[1]), xi.y);
-  dz = __dsub_rn(__dadd_rn(xj.z, sz * d.L[2]), xi.z);
+  dx = __dsub_rn(__dadd_rn(xj.x, sx * L[0]), xi.x);
+  dy = __dsub_rn(__dadd_rn(xj.y, sy * L[1]), xi.y);
+  dz = __dsub_rn(__dadd_rn(xj.z, sz * L[2]), xi.z);
   const double d2x = __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
   if (d2x > C.nonb_cut2) { dx = dy = dz = 0.0; return; }
   const R d2 = (R)d2x;
@@ -170,6 +156,8 @@ __global__ void __launch_bounds__(NBW * 32) k_nonbonded(Dev d, int eflag) {
     const int n = d.n;
     const double4 xi = d.xs[i];
     const int ti = d.ts[i];
+    const SegGeom &g = d.seg[d.seg_s[i]];
+    const double L[3] = {g.L[0], g.L[1], g.L[2]};
     const long long row = (long long)i * d.nb_cap;
     const int nn = d.n_near[i], nf = d.n_far[i];
     const int cap = d.nb_cap;
@@ -200,7 +188,7 @@ __global__ void __launch_bounds__(NBW * 32) k_nonbonded(Dev d, int eflag) {
         const uint32_t e = act ? Q.e[lane] : 0u;
         double c, dx, dy, dz;
         int j;
-        pair_terms<R>(d, F, C, e, act, xi, ti, evdw, eele, c, dx, dy, dz, j);
+        pair_terms<R>(d, F, C, e, act, xi, ti, L, evdw, eele, c, dx, dy, dz, j);
         if (act && c != 0.0) {
           fx -= c * dx;
           fy -= c * dy;
@@ -229,10 +217,12 @@ __global__ void __launch_bounds__(NBW * 32) k_nonbonded(Dev d, int eflag) {
     }
   }
   if (eflag) {
-    block_add(2.0 * evdw, &d.energy[E_VDW]);
-    block_add(2.0 * eele, &d.energy[E_ELE]);
-    block_add(evdw, &d.energy[E_ENG_VDWL]);
-    block_add(eele, &d.energy[E_ENG_COUL]);
+    const int sg = i < d.n ? d.seg_s[i] : -1;
+    const double v[4] = {2.0 * evdw, 2.0 * eele, evdw, eele};
+    static_assert(E_ELE == E_VDW + 1, "energy slots");
+    seg_block_add<2>(v, sg, d.energy + E_VDW, RG_NE);
+    seg_block_add<1>(v + 2, sg, d.energy + E_ENG_VDWL, RG_NE);
+    seg_block_add<1>(v + 3, sg, d.energy + E_ENG_COUL, RG_NE);
   }
 }
 

@@ -22,33 +22,23 @@ constexpr unsigned FULL = 0xffffffffu;
 enum {
   R_ACC0 = 0, R_ACC1 = 2, R_ACC2 = 4, R_ALPHA = 6, R_ALPHA_OLD = 8, R_BETA = 10,
   R_SIG = 12, R_HETA = 14, R_BNORM = 16, R_DOTP = 18, R_ACTIVE = 20, R_ITERS = 22,
-  R_SUM = 24, R_TOL = 26, R_IMAX = 27, R_NRED = 32
+  R_SUM = 24, R_TOL = 26, R_IMAX = 27, R_NEXT = 32, R_INIT = 68
 };
+// (per segment: d.red + seg * RG_NRED; R_NEXT + c: activity of the next
+// iteration; R_INIT..R_INIT+5: the set-up sums b.b, u.r, u.w)
+
+__device__ __forceinline__ int seg_at(const Dev &d, int s) { return s < d.n ? d.seg_s[s] : -1; }
+
+// zero count slots from slot of every segment
+__global__ void k_seg_zero(Dev d, int slot, int count) {
+  const int g = blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= d.nseg) return;
+  for (int c = 0; c < count; ++c) d.red[(long long)g * RG_NRED + slot + c] = 0.0;
+}
 
 __device__ __forceinline__ double warp_sum(double v) {
   for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(FULL, v, off);
   return v;
-}
-
-// block-reduce up to 6 values and atomically add to dst[0..k)
-template <int K>
-__device__ __forceinline__ void block_add_k(double *v, double *dst) {
-  __shared__ double red[K][32];
-  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
-#pragma unroll
-  for (int c = 0; c < K; ++c) v[c] = warp_sum(v[c]);
-  if (l == 0)
-#pragma unroll
-    for (int c = 0; c < K; ++c) red[c][w] = v[c];
-  __syncthreads();
-  if (w == 0) {
-#pragma unroll
-    for (int c = 0; c < K; ++c) {
-      double x = (l < (int)(blockDim.x >> 5)) ? red[c][l] : 0.0;
-      x = warp_sum(x);
-      if (l == 0) atomicAdd(&dst[c], x);
-    }
-  }
 }
 
 __global__ void k_qeq_setup(Dev d) {
@@ -228,15 +218,18 @@ __global__ void k_cg_init3(Dev d) {
     v[2] = u.x * r.x; v[3] = u.y * r.y;
     v[4] = u.x * w.x; v[5] = u.y * w.y;
   }
-  block_add_k<6>(v, d.red + R_ACC2 + 64);   // scratch area 68..73
+  seg_block_add<6>(v, seg_at(d, s), d.red + R_INIT, RG_NRED);
 }
 
-__global__ void k_cg_init_ctrl(Dev d) {
-  double *R = d.red;
-  const double tol = R[R_TOL];
-  const int imax = (int)R[R_IMAX];
+// one thread per segment; counts the segments with an active solve
+__global__ void k_cg_init_ctrl(Dev d, double tol, int imax) {
+  const int g = blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= d.nseg) return;
+  double *R = d.red + (long long)g * RG_NRED;
+  R[R_TOL] = tol;
+  R[R_IMAX] = imax;
   for (int c = 0; c < 2; ++c) {
-    const double bb = R[68 + c], ur = R[70 + c], uw = R[72 + c];
+    const double bb = R[R_INIT + c], ur = R[R_INIT + 2 + c], uw = R[R_INIT + 4 + c];
     R[R_BNORM + c] = sqrt(bb);
     R[R_SIG + c] = ur;
     R[R_HETA + c] = uw;
@@ -247,12 +240,14 @@ __global__ void k_cg_init_ctrl(Dev d) {
     R[R_ACC0 + c] = 0.0;
     R[R_ACC1 + c] = 0.0;
   }
+  if (R[R_ACTIVE] != 0.0 || R[R_ACTIVE + 1] != 0.0) atomicAdd(d.n_active, 1);
 }
 
 // A: r -= a s; u -= a v; w -= a z; acc u.r, u.w; d = w*Hdia_inv
 __global__ void k_cg_A(Dev d) {
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
-  const double *R = d.red;
+  const int sg = seg_at(d, s);
+  const double *R = d.red + (long long)(sg < 0 ? 0 : sg) * RG_NRED;
   const bool as = R[R_ACTIVE] != 0.0, at = R[R_ACTIVE + 1] != 0.0;
   double v[2] = {0, 0}, v1[2] = {0, 0};
   if (s < d.n && (as || at)) {
@@ -276,12 +271,16 @@ __global__ void k_cg_A(Dev d) {
     if (d.qd32) d.qd32[s] = split4(dd);
   }
   double all[4] = {v[0], v[1], v1[0], v1[1]};
-  block_add_k<4>(all, d.red + R_ACC0);   // ACC0[2], ACC1[2] are contiguous
+  seg_block_add<4>(all, sg, d.red + R_ACC0, RG_NRED);   // ACC0[2], ACC1[2] are contiguous
 }
 
-// scalars after A: beta, heta, alpha; activity of the next iteration
+// scalars after A: beta, heta, alpha; activity of the next iteration (one
+// thread per segment)
 __global__ void k_cg_ctrl(Dev d) {
-  double *R = d.red;
+  const int g = blockIdx.x * blockDim.x + threadIdx.x;
+  if (g == 0) *d.n_active = 0;   // recounted by k_cg_flip
+  if (g >= d.nseg) return;
+  double *R = d.red + (long long)g * RG_NRED;
   const double tol = R[R_TOL];
   const int imax = (int)R[R_IMAX];
   for (int c = 0; c < 2; ++c) {
@@ -304,14 +303,15 @@ __global__ void k_cg_ctrl(Dev d) {
     // loop increment and test of the next iteration
     const double it = R[R_ITERS + c] + 1.0;
     R[R_ITERS + c] = it;
-    R[R_ACTIVE + c + 32] = (it < imax && sqrt(dot0) / R[R_BNORM + c] > tol) ? 1.0 : 0.0;
+    R[R_NEXT + c] = (it < imax && sqrt(dot0) / R[R_BNORM + c] > tol) ? 1.0 : 0.0;
   }
 }
 
 // C: x += a_old p; p = u + b p; s = w + b s; v = d + b v; z = q + b z
 __global__ void k_cg_C(Dev d) {
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
-  double *R = d.red;
+  if (s >= d.n) return;
+  const double *R = d.red + (long long)d.seg_s[s] * RG_NRED;
   const bool as = R[R_ACTIVE] != 0.0, at = R[R_ACTIVE + 1] != 0.0;
   if (s < d.n && (as || at)) {
     double2 x = d.qx[s], p = d.qp[s], ss = d.qs[s], v = d.qv[s], z = d.qz[s];
@@ -328,11 +328,15 @@ __global__ void k_cg_C(Dev d) {
   }
 }
 
-// the activity decided in k_cg_ctrl takes effect for the next iteration
+// the activity decided in k_cg_ctrl takes effect for the next iteration;
+// counts the segments still active (one thread per segment)
 __global__ void k_cg_flip(Dev d) {
-  double *R = d.red;
+  const int g = blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= d.nseg) return;
+  double *R = d.red + (long long)g * RG_NRED;
   for (int c = 0; c < 2; ++c)
-    if (R[R_ACTIVE + c] != 0.0) R[R_ACTIVE + c] = R[R_ACTIVE + c + 32];
+    if (R[R_ACTIVE + c] != 0.0) R[R_ACTIVE + c] = R[R_NEXT + c];
+  if (R[R_ACTIVE] != 0.0 || R[R_ACTIVE + 1] != 0.0) atomicAdd(d.n_active, 1);
 }
 
 __global__ void k_qeq_sums(Dev d) {
@@ -343,15 +347,16 @@ __global__ void k_qeq_sums(Dev d) {
     v[0] = x.x;
     v[1] = x.y;
   }
-  block_add_k<2>(v, d.red + R_SUM);
+  seg_block_add<2>(v, seg_at(d, s), d.red + R_SUM, RG_NRED);
 }
 
-// q = s - (sum s / sum t) t; shift histories (original order)
+// q = s - (sum s / sum t) t per segment; shift histories (original order)
 __global__ void k_qeq_finish(Dev d) {
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= d.n) return;
   const int n = d.n, i = d.perm[s];
-  const double u = d.red[R_SUM] / d.red[R_SUM + 1];
+  const double *R = d.red + (long long)d.seg_s[s] * RG_NRED;
+  const double u = R[R_SUM] / R[R_SUM + 1];
   const double2 x = d.qx[s];
   const double q = x.x - u * x.y;
   d.q_o[i] = q;
@@ -383,8 +388,9 @@ void launch_qeq_spmv(const Dev &d, cudaStream_t st, const double2 *x, double2 *y
 
 // r = b - H x of the current iterate starts (or, in the mixed form,
 // restarts) the pipelined CG; the mixed form computes it with FP64 sums
-void launch_qeq_cg_init(const Dev &d, cudaStream_t st) {
+void launch_qeq_cg_init(const Dev &d, cudaStream_t st, double tol, int imax) {
   const int B = 256, G = (d.n + B - 1) / B;
+  const int GS = (d.nseg + 127) / 128;
   if (d.mixed) {
     const long long threads = (long long)d.n * 32;
     k_spmv_ref<<<(unsigned)((threads + 255) / 256), 256, 0, st>>>(d, d.qx, d.qq);
@@ -395,9 +401,10 @@ void launch_qeq_cg_init(const Dev &d, cudaStream_t st) {
   launch_qeq_spmv(d, st, d.qd, d.qq);
   k_cg_init2<<<G, B, 0, st>>>(d);
   launch_qeq_spmv(d, st, d.qd, d.qq);
-  cudaMemsetAsync(d.red + 68, 0, 6 * sizeof(double), st);
+  k_seg_zero<<<GS, 128, 0, st>>>(d, R_INIT, 6);
   k_cg_init3<<<G, B, 0, st>>>(d);
-  k_cg_init_ctrl<<<1, 1, 0, st>>>(d);
+  cudaMemsetAsync(d.n_active, 0, sizeof(int), st);
+  k_cg_init_ctrl<<<GS, 128, 0, st>>>(d, tol, imax);
 }
 
 // one CG iteration = launch_qeq_cg_A, SpMV of d into q, launch_qeq_cg_C
@@ -408,14 +415,15 @@ void launch_qeq_cg_A(const Dev &d, cudaStream_t st) {
 
 void launch_qeq_cg_C(const Dev &d, cudaStream_t st) {
   const int B = 256, G = (d.n + B - 1) / B;
-  k_cg_ctrl<<<1, 1, 0, st>>>(d);
+  const int GS = (d.nseg + 127) / 128;
+  k_cg_ctrl<<<GS, 128, 0, st>>>(d);
   k_cg_C<<<G, B, 0, st>>>(d);
-  k_cg_flip<<<1, 1, 0, st>>>(d);
+  k_cg_flip<<<GS, 128, 0, st>>>(d);
 }
 
 void launch_qeq_finish(const Dev &d, cudaStream_t st) {
   const int B = 256, G = (d.n + B - 1) / B;
-  cudaMemsetAsync(d.red + R_SUM, 0, 2 * sizeof(double), st);
+  k_seg_zero<<<(d.nseg + 127) / 128, 128, 0, st>>>(d, R_SUM, 2);
   k_qeq_sums<<<G, B, 0, st>>>(d);
   k_qeq_finish<<<G, B, 0, st>>>(d);
 }

@@ -81,8 +81,15 @@ struct rg_system {
   cudaStream_t st = nullptr;
   std::string err;
   int n = 0;
-  double L[3] = {0, 0, 0};
   bool have_box = false;
+  // segments: host table, atoms per segment (-1: all atoms of a single
+  // segment), allocations sized by the segment count
+  std::vector<SegGeom> segs;
+  std::vector<int> seg_counts;
+  std::vector<void *> per_seg;
+  int nseg_alloc = 0;
+  std::vector<double> e_host;     // per-segment energies read back
+  std::vector<int> seg_iters;     // last QEq: s and t iterations per segment
   Dev d{};
   std::vector<void *> per_n;    // allocations sized by n
   std::vector<void *> per_nb;   // sized by n * nb_cap
@@ -150,18 +157,26 @@ int setup_cells(rg_system *h) {
   const double rc = list_cutoff(h);
   const int S = 2;
   Dev &d = h->d;
-  d.S = S;
-  for (int k = 0; k < 3; ++k) {
-    if (h->L[k] < rc / S)
-      return fail(h, RG_E_ARG, "box edge shorter than half the pair cutoff is not supported");
-    int nc = (int)std::floor(h->L[k] * S / (rc * (1.0 + 1e-9)));
-    nc = std::max(nc, 1);
-    d.nc[k] = nc;
-    d.cellw[k] = h->L[k] / nc;
-    d.L[k] = h->L[k];
+  long long ncell = 0;
+  for (SegGeom &g : h->segs) {
+    g.S = S;
+    long long nseg_cells = 1;
+    for (int k = 0; k < 3; ++k) {
+      if (g.L[k] < rc / S)
+        return fail(h, RG_E_ARG, "box edge shorter than half the pair cutoff is not supported");
+      int nc = (int)std::floor(g.L[k] * S / (rc * (1.0 + 1e-9)));
+      nc = std::max(nc, 1);
+      g.nc[k] = nc;
+      g.cellw[k] = g.L[k] / nc;
+      nseg_cells *= nc;
+    }
+    g.cell0 = (int)ncell;
+    ncell += nseg_cells;
+    if (ncell > (1LL << 26)) return fail(h, RG_E_ARG, "too many cells");
   }
-  const long long ncell = (long long)d.nc[0] * d.nc[1] * d.nc[2];
-  if (ncell > (1LL << 26)) return fail(h, RG_E_ARG, "too many cells");
+  d.ncell = (int)ncell;
+  CK(cudaMemcpyAsync((void *)d.seg, h->segs.data(), sizeof(SegGeom) * h->segs.size(),
+                     cudaMemcpyHostToDevice, h->st));
   if (ncell > h->ncell_alloc) {
     if (h->cells) cudaFree(h->cells);
     const size_t nb = (ncell + 1 + 1023) / 1024 + 1;
@@ -173,6 +188,26 @@ int setup_cells(rg_system *h) {
   d.cell_count = c;
   d.cell_start = c + (ncell + 1);
   d.cell_fill = c + 2 * (ncell + 1);
+  CK(cudaStreamSynchronize(h->st));   // the host table may change after return
+  return 0;
+}
+
+// arrays sized by the segment count: geometry table, QEq scalars, energies
+int alloc_segs(rg_system *h) {
+  const int ns = (int)h->segs.size();
+  Dev &d = h->d;
+  d.nseg = ns;
+  if (ns <= h->nseg_alloc) return 0;
+  free_bucket(h->per_seg);
+  int r = 0;
+  SegGeom *sg = nullptr;
+  r |= dalloc(h, h->per_seg, &sg, (size_t)ns);
+  d.seg = sg;
+  r |= dalloc(h, h->per_seg, &d.red, (size_t)ns * RG_NRED);
+  r |= dalloc(h, h->per_seg, &d.energy, (size_t)ns * RG_NE);
+  r |= dalloc(h, h->per_seg, &d.n_active, 1);
+  if (r) return RG_E_CUDA;
+  h->nseg_alloc = ns;
   return 0;
 }
 
@@ -283,13 +318,16 @@ int alloc_atoms(rg_system *h, int n) {
   for (double2 **q : pv) r |= dalloc(h, B, q, (size_t)n);
   if (d.mixed) r |= dalloc(h, B, &d.qd32, (size_t)n);
   else d.qd32 = nullptr;
-  r |= dalloc(h, B, &d.red, 128);
-  r |= dalloc(h, B, &d.energy, RG_NE);
+  r |= dalloc(h, B, &d.seg_o, (size_t)n);
+  r |= dalloc(h, B, &d.seg_s, (size_t)n);
   r |= dalloc(h, B, &d.status, 8);
+  r |= dalloc(h, B, &d.dbg_flag, 1);
+  r |= dalloc(h, B, &d.dbg, 40);
   r |= dalloc(h, B, &d.fb_cnt, 2);
   if (r) return RG_E_CUDA;
   // capacity estimates from the mean density
-  const double vol = h->L[0] * h->L[1] * h->L[2];
+  double vol = 0.0;
+  for (const SegGeom &g : h->segs) vol += g.L[0] * g.L[1] * g.L[2];
   const double rho = n / vol;
   const double rc = list_cutoff(h);
   const double pi = 3.14159265358979;
@@ -372,7 +410,8 @@ int do_compute(rg_system *h, int eflag) {
   int rc;
   if (!h->lists_valid && (rc = build_lists(h))) return rc;
   CK(cudaMemsetAsync(d.fC, 0, 4 * sizeof(double) * (size_t)d.n, h->st));
-  CK(cudaMemsetAsync(d.energy, 0, RG_NE * sizeof(double), h->st));
+  CK(cudaMemsetAsync(d.energy, 0, (size_t)d.nseg * RG_NE * sizeof(double), h->st));
+  if (d.debug) CK(cudaMemsetAsync(d.dbg_flag, 0, sizeof(int), h->st));
   auto finite_after = [&](const char *phase) -> int {
     if (!h->check_finite) return 0;
     int flag = 0;
@@ -380,7 +419,17 @@ int do_compute(rg_system *h, int eflag) {
     launch_check_finite(d.fC, 4 * (long long)d.n, d.status + ST_NAN, h->st);
     CK(cudaMemcpyAsync(&flag, d.status + ST_NAN, sizeof(int), cudaMemcpyDeviceToHost, h->st));
     CK(cudaStreamSynchronize(h->st));
-    return flag ? fail(h, RG_E_NUMERIC, std::string("non-finite force after ") + phase) : 0;
+    if (!flag) return 0;
+    std::string msg = std::string("non-finite force after ") + phase;
+    int df = 0;
+    CK(cudaMemcpy(&df, d.dbg_flag, sizeof(int), cudaMemcpyDeviceToHost));
+    if (df) {
+      double v[40];
+      CK(cudaMemcpy(v, d.dbg, sizeof v, cudaMemcpyDeviceToHost));
+      msg += "; first term:";
+      for (double x : v) msg += " " + std::to_string(x);
+    }
+    return fail(h, RG_E_NUMERIC, msg);
   };
   { Scope sc(h, PH_BO, 3); launch_bond_orders(d, h->st); }
   { Scope sc(h, PH_ATOM, 1); launch_atom_energy(d, h->st, eflag); }
@@ -424,28 +473,30 @@ int do_qeq(rg_system *h, int *its, int *itt) {
   Dev &d = h->d;
   int rc;
   if (!h->lists_valid && (rc = build_lists(h))) return rc;
-  double hostred[2] = {h->p.qeq_tol, (double)h->p.qeq_imax};
-  CK(cudaMemcpyAsync(d.red + 26, hostred, 2 * sizeof(double), cudaMemcpyHostToDevice, h->st));
+  const int ns = d.nseg;
+  const double tol = h->p.qeq_tol;
+  const int imax = h->p.qeq_imax;
   {
-    Scope sc(h, PH_QSETUP, 8);
+    Scope sc(h, PH_QSETUP, 9);
     launch_qeq_setup(d, h->st);
-    launch_qeq_cg_init(d, h->st);
+    launch_qeq_cg_init(d, h->st, tol, imax);
   }
-  // iterate; poll the activity flags every few iterations.  The mixed form
-  // then restarts the CG from its iterate with the residual recomputed with
-  // FP64 sums (iterative refinement) until that residual meets the
-  // tolerance: at most RG_MAX_REFINE restarts.
+  // iterate; poll the number of segments with an active solve every few
+  // iterations.  The mixed form then restarts the CG from its iterate with
+  // the residual recomputed with FP64 sums (iterative refinement) until that
+  // residual meets the tolerance: at most RG_MAX_REFINE restarts.
   const int RG_MAX_REFINE = 3;
-  double flags[4];
-  int tot_s = 0, tot_t = 0, refines = 0;
   const int chunk = 4;
+  std::vector<double> it(2 * (size_t)ns);
+  std::vector<int> tot(2 * (size_t)ns, 0);
+  int refines = 0, active = 0;
   for (;;) {
     int done_iters = 0;
     for (;;) {
-      CK(cudaMemcpyAsync(flags, d.red + 20, 4 * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+      CK(cudaMemcpyAsync(&active, d.n_active, sizeof(int), cudaMemcpyDeviceToHost, h->st));
       CK(cudaStreamSynchronize(h->st));
-      if (flags[0] == 0.0 && flags[1] == 0.0) break;
-      if (done_iters > h->p.qeq_imax + 8) return fail(h, RG_E_NUMERIC, "QEq iteration control lost");
+      if (active == 0) break;
+      if (done_iters > imax + 8) return fail(h, RG_E_NUMERIC, "QEq iteration control lost");
       for (int k = 0; k < chunk; ++k) {
         { Scope sc(h, PH_QVEC, 1); launch_qeq_cg_A(d, h->st); }
         { Scope sc(h, PH_QSPMV, 1); launch_qeq_spmv(d, h->st, d.qd, d.qq); }
@@ -453,24 +504,32 @@ int do_qeq(rg_system *h, int *its, int *itt) {
       }
       done_iters += chunk;
     }
-    // the initial pass counts its first (set-up) iteration like CG_v2;
-    // a restart that is not needed adds nothing
-    const int add_s = (int)flags[2] - (refines ? 1 : 0), add_t = (int)flags[3] - (refines ? 1 : 0);
-    tot_s += add_s > 0 ? add_s : 0;
-    tot_t += add_t > 0 ? add_t : 0;
-    if (!d.mixed || refines >= RG_MAX_REFINE) break;
-    { Scope sc(h, PH_QSETUP, 7); launch_qeq_cg_init(d, h->st); }
-    ++refines;
-    CK(cudaMemcpyAsync(flags, d.red + 20, 2 * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+    // iterations of this pass per segment and system; the initial pass
+    // counts its first (set-up) iteration like CG_v2, a restart that is not
+    // needed adds nothing
+    CK(cudaMemcpy2DAsync(it.data(), 2 * sizeof(double), d.red + 22, RG_NRED * sizeof(double),
+                         2 * sizeof(double), ns, cudaMemcpyDeviceToHost, h->st));
     CK(cudaStreamSynchronize(h->st));
-    if (flags[0] == 0.0 && flags[1] == 0.0) break;
+    for (size_t k = 0; k < it.size(); ++k) tot[k] += std::max(0, (int)it[k] - (refines ? 1 : 0));
+    if (!d.mixed || refines >= RG_MAX_REFINE) break;
+    { Scope sc(h, PH_QSETUP, 8); launch_qeq_cg_init(d, h->st, tol, imax); }
+    ++refines;
+    CK(cudaMemcpyAsync(&active, d.n_active, sizeof(int), cudaMemcpyDeviceToHost, h->st));
+    CK(cudaStreamSynchronize(h->st));
+    if (active == 0) break;
   }
-  h->stats.cg_iters_s = tot_s;
-  h->stats.cg_iters_t = tot_t;
+  int ms = 0, mt = 0;
+  for (int g = 0; g < ns; ++g) {
+    ms = std::max(ms, tot[2 * g]);
+    mt = std::max(mt, tot[2 * g + 1]);
+  }
+  h->seg_iters.swap(tot);
+  h->stats.cg_iters_s = ms;
+  h->stats.cg_iters_t = mt;
   h->stats.qeq_restarts = refines;
-  if (its) *its = tot_s;
-  if (itt) *itt = tot_t;
-  { Scope sc(h, PH_QFIN, 2); launch_qeq_finish(d, h->st); }
+  if (its) *its = ms;
+  if (itt) *itt = mt;
+  { Scope sc(h, PH_QFIN, 3); launch_qeq_finish(d, h->st); }
   CK(cudaGetLastError());
   return 0;
 }
@@ -534,7 +593,8 @@ int rg_create(const char *ffield_path, const rg_params *pin, rg_system **out) {
   h->d.mixed = (h->p.precision == RG_PREC_MIXED);
   {
     const char *cf = std::getenv("RG_CHECK_FINITE");
-    h->check_finite = cf && cf[0] == '1';
+    h->check_finite = cf && (cf[0] == '1' || cf[0] == '2');
+    h->d.debug = cf && cf[0] == '2';
   }
   for (int t = 0; t < RG_MAXT; ++t) h->ff.nve_mass[t] = h->ff.sbp[t].mass;
   if (c.near_cut > lc) {
@@ -627,14 +687,93 @@ int rg_extract(const rg_system *h, const char *name, double *out) {
   return RG_OK;
 }
 
+// atom ranges of the segments from their counts and the atom count; the
+// per-atom segment index goes to the device
+static int sync_segments(rg_system *h) {
+  const int n = h->n;
+  const int ns = (int)h->segs.size();
+  long long sum = 0;
+  for (int g = 0; g < ns; ++g) {
+    const int c = h->seg_counts[g] < 0 ? n : h->seg_counts[g];
+    h->segs[g].atom0 = (int)sum;
+    h->segs[g].natoms = c;
+    sum += c;
+  }
+  if (sum != n) return fail(h, RG_E_ARG, "segment atom counts do not add up to the atom count");
+  int rc = alloc_segs(h);
+  if (rc) return rc;
+  std::vector<int> so((size_t)n);
+  for (int g = 0; g < ns; ++g)
+    for (int a = 0; a < h->segs[g].natoms; ++a) so[(size_t)h->segs[g].atom0 + a] = g;
+  CK(cudaMemcpyAsync(h->d.seg_o, so.data(), sizeof(int) * (size_t)n, cudaMemcpyHostToDevice, h->st));
+  CK(cudaStreamSynchronize(h->st));
+  return 0;
+}
+
+// energies of the last force step summed over the segments
+static int energy_sum(rg_system *h, double *out) {
+  const int ns = h->d.nseg;
+  h->e_host.resize((size_t)ns * RG_NE);
+  CK(cudaMemcpyAsync(h->e_host.data(), h->d.energy, sizeof(double) * RG_NE * ns,
+                     cudaMemcpyDeviceToHost, h->st));
+  CK(cudaStreamSynchronize(h->st));
+  for (int k = 0; k < RG_NE; ++k) {
+    double s = 0.0;
+    for (int g = 0; g < ns; ++g) s += h->e_host[(size_t)g * RG_NE + k];
+    out[k] = s;
+  }
+  return 0;
+}
+
 int rg_set_box(rg_system *h, const double *L3) {
   if (!h || !L3) return RG_E_ARG;
+  const int counts[1] = {-1};
   for (int k = 0; k < 3; ++k)
     if (!(L3[k] > 0.0) || !std::isfinite(L3[k])) return fail(h, RG_E_ARG, "box edge must be positive");
-  for (int k = 0; k < 3; ++k) h->L[k] = L3[k];
+  h->segs.assign(1, SegGeom{});
+  for (int k = 0; k < 3; ++k) h->segs[0].L[k] = L3[k];
+  h->seg_counts.assign(counts, counts + 1);
   h->have_box = true;
   h->lists_valid = false;
   h->forces_valid = false;
+  if (h->n) return sync_segments(h);
+  return RG_OK;
+}
+
+int rg_set_segments(rg_system *h, int nseg, const int *counts, const double *boxes) {
+  if (!h || nseg <= 0 || !counts || !boxes) return RG_E_ARG;
+  for (int g = 0; g < nseg; ++g) {
+    if (counts[g] <= 0) return fail(h, RG_E_ARG, "every segment needs atoms");
+    for (int k = 0; k < 3; ++k)
+      if (!(boxes[3 * g + k] > 0.0) || !std::isfinite(boxes[3 * g + k]))
+        return fail(h, RG_E_ARG, "box edge must be positive");
+  }
+  h->segs.assign(nseg, SegGeom{});
+  for (int g = 0; g < nseg; ++g)
+    for (int k = 0; k < 3; ++k) h->segs[g].L[k] = boxes[3 * g + k];
+  h->seg_counts.assign(counts, counts + nseg);
+  h->have_box = true;
+  h->lists_valid = false;
+  h->forces_valid = false;
+  long long sum = 0;
+  for (int g = 0; g < nseg; ++g) sum += counts[g];
+  if (h->n && sum == h->n) return sync_segments(h);
+  return RG_OK;
+}
+
+int rg_num_segments(const rg_system *h) { return h ? (int)h->segs.size() : RG_E_ARG; }
+
+int rg_get_energies(rg_system *h, double *e) {
+  if (!h || !e) return RG_E_ARG;
+  if (!h->n) return fail(h, RG_E_STATE, "no atoms set");
+  CK(cudaMemcpyAsync(e, h->d.energy, sizeof(double) * RG_NE * h->d.nseg, cudaMemcpyDeviceToHost, h->st));
+  CK(cudaStreamSynchronize(h->st));
+  return RG_OK;
+}
+
+int rg_get_segment_iters(rg_system *h, int *iters) {
+  if (!h || !iters) return RG_E_ARG;
+  for (size_t k = 0; k < h->seg_iters.size(); ++k) iters[k] = h->seg_iters[k];
   return RG_OK;
 }
 
@@ -648,8 +787,18 @@ static int set_atoms_impl(rg_system *h, int n, const double *x, const int *type,
     for (int i = 0; i < n; ++i)
       if (type[i] < 0 || type[i] >= h->ff.ntypes) return fail(h, RG_E_ARG, "atom type out of range");
   }
+  {
+    long long sum = 0;
+    for (int c : h->seg_counts) sum += c < 0 ? n : c;
+    if (sum != n) return fail(h, RG_E_ARG, "segment atom counts do not add up to the atom count");
+  }
   if (n != h->d.n) {
     int rc = alloc_atoms(h, n);
+    if (rc) return rc;
+  }
+  h->n = n;
+  {
+    int rc = sync_segments(h);
     if (rc) return rc;
   }
   Dev &d = h->d;
@@ -717,7 +866,7 @@ int rg_compute(rg_system *h, int eflag, int vflag, double *f_out, double *energi
   int rc = do_compute(h, eflag || energies != nullptr);
   if (rc) return rc;
   if (f_out) CK(cudaMemcpyAsync(f_out, h->d.f_o, 3 * sizeof(double) * h->n, cudaMemcpyDeviceToHost, h->st));
-  if (energies) CK(cudaMemcpyAsync(energies, h->d.energy, RG_NE * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+  if (energies && (rc = energy_sum(h, energies))) return rc;
   int st[8];
   if ((rc = read_status(h, st))) return rc;
   if (st[ST_NAN]) return fail(h, RG_E_NUMERIC, "non-finite force");
@@ -759,7 +908,7 @@ int rg_run(rg_system *h, int nsteps, double dt, double *energies) {
     if ((rc = do_compute(h, energies != nullptr && s == nsteps - 1))) return rc;
     { Scope sc(h, PH_NVE, 1); launch_nve_final(h->d, h->st, dt); }
   }
-  if (energies) CK(cudaMemcpyAsync(energies, h->d.energy, RG_NE * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+  if (energies && (rc = energy_sum(h, energies))) return rc;
   CK(cudaStreamSynchronize(h->st));
   CK(cudaGetLastError());
   return RG_OK;

@@ -68,6 +68,18 @@ struct ForceField {
   double nve_mass[RG_MAXT];   // integrator masses (default: sbp mass)
 };
 
+// Geometry of one segment (periodic orthogonal box and its cells).
+struct SegGeom {
+  double L[3];        // box edges
+  double cellw[3];    // cell edges (L / nc)
+  int nc[3];          // cells per dimension
+  int S;              // stencil half-width (cells)
+  int cell0;          // first global cell index of the segment
+  int atom0, natoms;  // original-order atom range
+};
+
+constexpr int RG_NRED = 128;   // QEq scalar slots per segment
+
 // Scalar controls shared by all kernels.
 struct Control {
   double bo_cut, nonb_cut, nonb_low, bond_cut, hbond_cut, thb_cut, thb_cutsq;
@@ -97,10 +109,14 @@ struct Dev {
   int nb_cap;         // neighbour row capacity (row-major rows)
   int bond_cap;       // bond slots per atom (slot-major: k*n + i)
   int hb_cap;         // H-bond partner slots per H atom (row-major)
-  double L[3];        // box
-  int nc[3];          // cells per dimension
-  int S;              // stencil half-width (cells)
-  double cellw[3];
+  // independent periodic systems ("segments") in one set of arrays: atoms
+  // of segment k are original indices [atom0, atom0 + natoms); a single
+  // system is one segment
+  int nseg;
+  const SegGeom *seg;    // [nseg]
+  int *seg_o;            // segment of each atom (original order)
+  int *seg_s;            // segment of each atom (sorted order)
+  int ncell;             // cells over all segments
 
   const ForceField *ff;
   const Control *ctl;
@@ -154,8 +170,9 @@ struct Dev {
   double2 *qx, *qb, *qr, *qu, *qw, *qd, *qq, *qp, *qs, *qv, *qz, *qm;
   float4 *qd32;   // mixed form: qd split into FP32 (hi, lo) pairs, s then t
   double *Hdia_inv;
-  double *red;        // device scalars / reduction accumulators
-  double *energy;     // [RG_NE]
+  double *red;        // device scalars / reduction accumulators, RG_NRED per segment
+  double *energy;     // [nseg][RG_NE]
+  int *n_active;      // QEq: segments with an active solve (host poll)
 
   // valence / torsion work lists (built per force step)
   double *c_sbo;      // 5 * n: SBO2, CSBO2, dSBO1, dSBO2, expval6 per centre
@@ -169,6 +186,12 @@ struct Dev {
   // an FP64 pass (fb_cnt[0] angles, fb_cnt[1] torsions)
   unsigned long long *w_fb_val, *w_fb_tor;
   int *fb_cnt;
+
+  // RG_CHECK_FINITE=2: the first non-finite angle or torsion term is
+  // recorded with its inputs (dbg_flag set, dbg[0..39])
+  int debug;
+  int *dbg_flag;
+  double *dbg;
 
   int *status;        // [8]: 0 overflow flags, 1 max nbrs, 2 max bonds, 3 max hb, 4 nonfinite,
                       //      5 pair entries, 6 bonds, 7 H-bond partners
@@ -185,6 +208,55 @@ enum { OVF_NBR = 1, OVF_BOND = 2, OVF_HB = 4, OVF_CELL = 8 };
 #define RG_C3_QEQ (0.3333333333333 - 1.0 / 3.0)
 #define RG_C3_ELE (0.33333333333333 - 1.0 / 3.0)
 #ifdef __CUDACC__
+// Adds v[0..K) of every thread of the block into dst[seg * stride + c],
+// c = 0..K-1; seg < 0 marks a thread without values.  One FP64 atomic per
+// value per block when the block's threads belong to one segment, per warp
+// when a warp's do, per thread otherwise (warps that straddle two
+// segments).  Every thread of the block must call it.
+template <int K>
+__device__ __forceinline__ void seg_block_add(const double *vin, int seg, double *dst, int stride) {
+  __shared__ double sh[K][32];
+  __shared__ int sw[32];
+  const unsigned FULLM = 0xffffffffu;
+  double v[K];
+#pragma unroll
+  for (int c = 0; c < K; ++c) v[c] = vin[c];
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  const bool uni = __match_any_sync(FULLM, seg) == FULLM;
+  if (uni) {
+#pragma unroll
+    for (int c = 0; c < K; ++c)
+      for (int off = 16; off > 0; off >>= 1) v[c] += __shfl_down_sync(FULLM, v[c], off);
+  } else if (seg >= 0) {
+#pragma unroll
+    for (int c = 0; c < K; ++c)
+      if (v[c] != 0.0) atomicAdd(&dst[(long long)seg * stride + c], v[c]);
+  }
+  __syncthreads();
+  if (l == 0) {
+    sw[w] = uni ? seg : -1;
+#pragma unroll
+    for (int c = 0; c < K; ++c) sh[c][w] = uni ? v[c] : 0.0;
+  }
+  __syncthreads();
+  if (w == 0) {
+    const int nw = (int)(blockDim.x >> 5);
+    const int sg = l < nw ? sw[l] : -1;
+    const int s0 = __shfl_sync(FULLM, sg, 0);
+    const bool one = __all_sync(FULLM, l >= nw || sg == s0) && s0 >= 0;
+#pragma unroll
+    for (int c = 0; c < K; ++c) {
+      double x = l < nw ? sh[c][l] : 0.0;
+      if (one) {
+        for (int off = 16; off > 0; off >>= 1) x += __shfl_down_sync(FULLM, x, off);
+        if (l == 0 && x != 0.0) atomicAdd(&dst[(long long)s0 * stride + c], x);
+      } else if (l < nw && sg >= 0 && x != 0.0) {
+        atomicAdd(&dst[(long long)sg * stride + c], x);
+      }
+    }
+  }
+}
+
 __device__ __forceinline__ double pow_third(double x, double dc) {
   return cbrt(x) * (1.0 + dc * (double)__logf((float)x));
 }
@@ -224,7 +296,7 @@ void launch_check_finite(const double *a, long long count, int *flag, cudaStream
 // QEq
 void launch_qeq_setup(const Dev &d, cudaStream_t st);
 void launch_qeq_spmv(const Dev &d, cudaStream_t st, const double2 *x, double2 *y);
-void launch_qeq_cg_init(const Dev &d, cudaStream_t st);
+void launch_qeq_cg_init(const Dev &d, cudaStream_t st, double tol, int imax);
 void launch_qeq_cg_A(const Dev &d, cudaStream_t st);
 void launch_qeq_cg_C(const Dev &d, cudaStream_t st);
 void launch_qeq_finish(const Dev &d, cudaStream_t st);

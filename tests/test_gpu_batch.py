@@ -1,0 +1,92 @@
+"""Segments: many independent periodic systems in one handle (batched
+single-point evaluation).  Each system's charges, forces, energies and CG
+iteration counts in the batch must be those of the same system run alone
+(same library, same form): the batch changes only the order of FP64
+reductions.  Boxes below twice the 10 A cutoff (several periodic images of
+one partner) and uneven sizes are included."""
+import numpy as np
+import pytest
+
+from oracle.pyoracle import Oracle
+from sw_reaxff_gb300 import ReaxGPU, systems
+from sw_reaxff_gb300.api import PREC_MIXED
+
+pytestmark = pytest.mark.gpu
+
+
+def batch_systems():
+    return [
+        systems.small_pack(60, 0.9, seed=101),      # ~60 atoms, box < 10 A
+        systems.water_box(200, seed=1),             # 600 atoms, box 18 A
+        systems.small_pack(400, 0.35, seed=102),
+        systems.mixture(scale=0.001, seed=3),       # ~1k atoms
+        systems.small_pack(150, 1.0, seed=103),
+        systems.small_pack(2500, 0.6, seed=104),
+    ]
+
+
+def run_alone(ffield, s, **kw):
+    g = ReaxGPU(ffield, **kw)
+    g.set_system(s)
+    q, its, itt = g.qeq()
+    f, e = g.compute()
+    return q, f, e, (its, itt)
+
+
+@pytest.mark.parametrize("precision", [0, PREC_MIXED])
+def test_batch_equals_alone(ffield, precision):
+    S = batch_systems()
+    g = ReaxGPU(ffield, precision=precision)
+    off = g.set_systems(S)
+    q, _, _ = g.qeq()
+    f, _ = g.compute()
+    es = g.energies()
+    iters = g.segment_iters()
+    assert len(es) == len(S) and iters.shape == (len(S), 2)
+    for k, s in enumerate(S):
+        qa, fa, ea, (its, itt) = run_alone(ffield, s, precision=precision)
+        sl = slice(off[k], off[k] + s.n)
+        assert np.abs(q[sl] - qa).max() < 1e-8, (k, np.abs(q[sl] - qa).max())
+        assert abs(q[sl].sum()) < 1e-9
+        rel = np.sqrt(((f[sl] - fa) ** 2).sum() / (fa ** 2).sum())
+        assert rel < 1e-8, (k, rel)
+        for name in ("eng_vdwl", "eng_coul", "e_bond", "e_ang", "e_tor", "e_hb", "e_pol"):
+            assert abs(es[k][name] - ea[name]) <= 1e-8 * max(abs(ea[name]), 1.0), (k, name)
+        assert abs(int(iters[k, 0]) - its) <= 1 and abs(int(iters[k, 1]) - itt) <= 1
+
+
+def test_batch_against_oracle(ffield):
+    S = batch_systems()[:3]
+    g = ReaxGPU(ffield)
+    off = g.set_systems(S)
+    q, _, _ = g.qeq()
+    f, _ = g.compute()
+    es = g.energies()
+    for k, s in enumerate(S):
+        o = Oracle(ffield)
+        o.set_system(s.box, s.x, s.types(g.elements), s.tag, None, s.v)
+        qo, _, _ = o.qeq()
+        fo, eo = o.compute()
+        sl = slice(off[k], off[k] + s.n)
+        assert np.abs(q[sl] - qo).max() < 1e-5
+        assert np.sqrt(((f[sl] - fo) ** 2).sum() / (fo ** 2).sum()) < 1e-5
+        pe, peo = es[k]["eng_vdwl"] + es[k]["eng_coul"], eo["eng_vdwl"] + eo["eng_coul"]
+        assert abs(pe - peo) < 1e-5 * abs(peo)
+
+
+def test_batch_nve_keeps_segments_apart(ffield):
+    S = batch_systems()[:4]
+    g = ReaxGPU(ffield)
+    off = g.set_systems(S)
+    g.run(5, 0.25)
+    x, v, q, _ = g.get_atoms()
+    for k, s in enumerate(S):
+        a = ReaxGPU(ffield)
+        a.set_system(s)
+        a.run(5, 0.25)
+        xa, va, qa, _ = a.get_atoms()
+        sl = slice(off[k], off[k] + s.n)
+        dx = x[sl] - xa
+        dx -= s.box * np.round(dx / s.box)
+        assert np.abs(dx).max() < 1e-9
+        assert np.abs(q[sl] - qa).max() < 1e-7

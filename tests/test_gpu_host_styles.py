@@ -91,7 +91,7 @@ def test_deck_nve_follows_rg_run(tmp_path, ffield):
     # the CG charges move by ~1e-7 when FP64 atomics reorder (see the
     # parity tests), which moves velocities by ~1e-9 over these steps
     assert np.abs(st["v"] - v[order]).max() < 1e-7
-    assert np.abs(st["q"] - q[order]).max() < 1e-7
+    assert np.abs(st["q"] - q[order]).max() < 1e-6
     lines = [ln for ln in out.splitlines() if ln.strip() and ln.split()[0].isdigit()]
     assert [int(ln.split()[0]) for ln in lines] == [0, 5, 10]
     etot = [float(ln.split()[3]) for ln in lines]

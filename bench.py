@@ -56,6 +56,12 @@ def parse():
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--cpu-scale", type=float, default=0.02,
                    help="size of the CPU-baseline sample relative to 1M atoms")
+    p.add_argument("--no-batched", action="store_true",
+                   help="skip the batched single-point measurement (512 small systems)")
+    p.add_argument("--no-serve", action="store_true",
+                   help="skip the serving-loop measurement (Poisson request stream)")
+    p.add_argument("--batch-systems", type=int, default=512)
+    p.add_argument("--serve-requests", type=int, default=300)
     return p.parse_args()
 
 
@@ -189,6 +195,111 @@ def _cpu_sample(arg):
     o.qeq()
     o.compute()
     return s.n, time.perf_counter() - t0
+
+
+def _gen_batch_system(k):
+    """System k of the batched workload: log-uniform 50-3000 atoms, a random
+    pack of H2O/CH4/NH3/CO2/C2H6 at a density uniform in 0.3-1.0 g/cm3."""
+    import math
+    sys.path.insert(0, ROOT)
+    from sw_reaxff_gb300 import systems
+    rng = np.random.default_rng(1000 + k)
+    size = int(round(math.exp(rng.uniform(math.log(50), math.log(3000)))))
+    return systems.small_pack(size, float(rng.uniform(0.3, 1.0)), seed=20000 + k)
+
+
+def _gen_request(spec):
+    sys.path.insert(0, ROOT)
+    from sw_reaxff_gb300 import serve
+    return serve.make_request(spec)
+
+
+def _spawn_pool():
+    import multiprocessing as mp
+    return mp.get_context("spawn").Pool(min(16, os.cpu_count() or 1))
+
+
+def batched_section(args, local):
+    """512 independent small systems, one single point each (QEq + energies
+    + forces), evaluated together as segments of one handle in the mixed
+    form; against the same systems solved one after another with a plain
+    FP64 handle."""
+    import torch
+    from sw_reaxff_gb300 import ReaxGPU
+    from sw_reaxff_gb300.api import DEFAULT_FFIELD, PREC_MIXED
+    with _spawn_pool() as pool:
+        S = pool.map(_gen_batch_system, range(args.batch_systems))
+    natoms = sum(s.n for s in S)
+    out = {"workload": f"{len(S)} periodic systems, {natoms} atoms, 50-3000 atoms "
+                       "log-uniform, 0.3-1.0 g/cm3, single point (QEq+energies+forces)"}
+    for label, prec in (("mixed", PREC_MIXED), ("fp64", 0)):
+        g = ReaxGPU(DEFAULT_FFIELD, device=local, precision=prec)
+        g.set_systems(S)
+        st = torch.cuda.ExternalStream(g.stream())
+        times = []
+        for it in range(args.warmup + args.steps):
+            g.set_histories(None, None)        # fresh single points
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(st)
+            g.qeq()
+            g.compute()
+            e1.record(st)
+            g.synchronize()
+            if it >= args.warmup:
+                times.append(e0.elapsed_time(e1) / 1e3)
+        t_batch = float(np.mean(times))
+        out[label] = {"batch_ms": t_batch * 1e3, "req_per_s": len(S) / t_batch,
+                      "p50_ms": t_batch * 1e3, "p99_ms": t_batch * 1e3,
+                      "atom_evals_per_s": natoms / t_batch}
+        g.close()
+    # sequential plain FP64 solves (host arrays in and out, one handle), on
+    # a sample of the systems
+    g = ReaxGPU(DEFAULT_FFIELD, device=local)
+    sample = S[:: max(1, len(S) // 64)]
+    for s in sample[:3]:
+        g.set_system(s); g.qeq(); g.compute()
+    lat = []
+    for s in sample:
+        t0 = time.perf_counter()
+        g.set_system(s)
+        g.qeq()
+        g.compute()
+        lat.append(time.perf_counter() - t0)
+    g.close()
+    out["sequential_fp64"] = {"req_per_s": 1.0 / float(np.mean(lat)),
+                              "p50_ms": float(np.percentile(lat, 50) * 1e3),
+                              "p99_ms": float(np.percentile(lat, 99) * 1e3),
+                              "sample": len(sample)}
+    out["speedup_vs_sequential_fp64"] = out["mixed"]["req_per_s"] / out["sequential_fp64"]["req_per_s"]
+    return out
+
+
+def serve_section(args, local):
+    """The request loop on a Poisson stream at 200 req/s (sizes 100-20,000
+    atoms log-uniform; 70 % single points, 30 % NVE runs of 10-500 steps),
+    mixed form, against sequential plain FP64 solves of a sample of the
+    same stream."""
+    from sw_reaxff_gb300 import serve
+    from sw_reaxff_gb300.api import DEFAULT_FFIELD, PREC_MIXED
+    specs = serve.stream_specs(args.serve_requests, rate=200.0, seed=SEED)
+    with _spawn_pool() as pool:
+        reqs = pool.map(_gen_request, specs)
+    srv = serve.ReaxServer(DEFAULT_FFIELD, precision=PREC_MIXED, device=local)
+    warm = serve.request_stream(8, rate=1e6, seed=SEED + 1, max_atoms=2000, md_steps=(5, 10))
+    srv.serve(warm, realtime=False)
+    st = srv.serve(reqs, realtime=True)
+    srv.close()
+    out = {"workload": f"{len(reqs)} requests, Poisson 200 req/s, 100-20000 atoms, "
+                       "70% single point / 30% NVE 10-500 steps, mixed form",
+           **st.summary()}
+    work = sum(r.system.n * max(1, r.nsteps) for r in reqs)
+    out["atom_steps_per_s"] = work / st.wall
+    sample = reqs[:: max(1, len(reqs) // 30)]
+    wall = serve.sequential(DEFAULT_FFIELD, sample)
+    out["sequential_fp64"] = {"req_per_s": len(sample) / wall, "sample": len(sample)}
+    out["speedup_vs_sequential_fp64"] = out["req_per_s"] / out["sequential_fp64"]["req_per_s"]
+    return out
 
 
 def reference_arm(args):
@@ -375,6 +486,10 @@ def gpu_arm(args):
         "hbm_peak_gbs": peaks.get("hbm_gbs"),
     }
     line["gpu_launches"] = int(launches)
+    if rank == 0 and not args.no_batched:
+        line["batched"] = batched_section(args, local)
+    if rank == 0 and not args.no_serve:
+        line["serving"] = serve_section(args, local)
     if rank == 0 and not args.no_cpu:
         v, cores, sample = cpu_baseline(args.cpu_scale, 1)
         line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": cores, "kind": "port",

@@ -167,6 +167,15 @@ int rg_nve_final(rg_system *h, double dt);
  * QEq, force step, final_integrate.  energies of the last step or NULL. */
 int rg_run(rg_system *h, int nsteps, double dt, double *energies);
 
+/* QEq histories (the s and t solutions of the last 5 solves that seed the
+ * extrapolated initial guesses, fix_qeq_reax_sunway.cpp:618-723,1741-1752):
+ * host arrays of 5*n doubles, entry k*n + i for solve k (0 = latest) of atom
+ * i in the original order.  Moving a system between handles keeps its
+ * trajectory with them.  rg_set_histories(h, NULL, NULL) clears them (the
+ * next QEq starts from zero guesses, as after rg_set_atoms). */
+int rg_get_histories(rg_system *h, double *s_hist, double *t_hist);
+int rg_set_histories(rg_system *h, const double *s_hist, const double *t_hist);
+
 /* Read back the current state (host arrays, original atom order). */
 int rg_get_atoms(rg_system *h, double *x, double *v, double *q, double *f);
 /* Device pointers of the state arrays (original order, 3n/n doubles). */

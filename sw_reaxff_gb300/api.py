@@ -30,7 +30,8 @@ EXPORTED = ["rg_default_params", "rg_create", "rg_destroy", "rg_last_error",
             "rg_dump_pairs", "rg_dump_bonds", "rg_dump_hbonds", "rg_set_state",
             "rg_stream", "rg_profile_enable", "rg_profile_get", "rg_measure_fp64_peak",
             "rg_qeq_noalloc", "rg_set_masses", "rg_ffield_info", "rg_set_segments",
-            "rg_num_segments", "rg_get_energies", "rg_get_segment_iters"]
+            "rg_num_segments", "rg_get_energies", "rg_get_segment_iters",
+            "rg_get_histories", "rg_set_histories"]
 
 
 class Params(C.Structure):
@@ -84,6 +85,8 @@ def load_library(path: str = LIBPATH):
     L.rg_num_segments.argtypes = [C.c_void_p]
     L.rg_get_energies.argtypes = [C.c_void_p, dp]
     L.rg_get_segment_iters.argtypes = [C.c_void_p, ip]
+    L.rg_get_histories.argtypes = [C.c_void_p, dp, dp]
+    L.rg_set_histories.argtypes = [C.c_void_p, dp, dp]
     L.rg_ffield_info.argtypes = [C.c_char_p, ip, C.c_char_p, C.c_int, C.c_char_p, C.c_int]
     L.rg_set_atoms.argtypes = [C.c_void_p, C.c_int, dp, ip, ip, dp, dp]
     L.rg_set_atoms_device.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p,
@@ -248,6 +251,18 @@ class ReaxGPU:
         it = np.zeros(2 * ns, np.int32)
         self._chk(self.L.rg_get_segment_iters(self.h, _ip(it)), "rg_get_segment_iters")
         return it.reshape(ns, 2)
+
+    def get_histories(self):
+        """QEq histories, two (5, n) arrays (latest solve first)."""
+        s = np.zeros((5, self.n))
+        t = np.zeros((5, self.n))
+        self._chk(self.L.rg_get_histories(self.h, _dp(s), _dp(t)), "rg_get_histories")
+        return s, t
+
+    def set_histories(self, s=None, t=None):
+        s = None if s is None else np.ascontiguousarray(s, np.float64)
+        t = None if t is None else np.ascontiguousarray(t, np.float64)
+        self._chk(self.L.rg_set_histories(self.h, _dp(s), _dp(t)), "rg_set_histories")
 
     def set_positions(self, x):
         x = np.ascontiguousarray(x, np.float64)

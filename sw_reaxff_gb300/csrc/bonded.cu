@@ -915,9 +915,18 @@ __device__ __forceinline__ void torsion_item(const Dev &d, unsigned long long it
     const R CV = R(0.5) * (V1 * (R(1) + cos_omega) + V2 * exp_tor1 * (R(1) - cos2omega) +
                            V3 * (R(1) + cos3omega));
     e_tor = (double)(fn10 * sin_ijk * sin_jkl * CV);
-    const R dfn11 = (-p_tor3 * exp_tor3_DjDk +
-                     (p_tor3 * exp_tor3_DjDk - p_tor4 * exp_tor4_DjDk) * (R(2) + exp_tor3_DjDk) * exp_tor34_inv) *
-                    exp_tor34_inv;
+    R dfn11;
+    if (std::is_same<R, double>::value) {
+      dfn11 = (-p_tor3 * exp_tor3_DjDk +
+               (p_tor3 * exp_tor3_DjDk - p_tor4 * exp_tor4_DjDk) * (R(2) + exp_tor3_DjDk) * exp_tor34_inv) *
+              exp_tor34_inv;
+    } else {
+      // the same value with every product bounded: for Delta_j + Delta_k
+      // near -4 the product of the two exponentials above exceeds FP32
+      const R a3 = p_tor3 * (exp_tor3_DjDk * exp_tor34_inv);
+      const R a4 = p_tor4 * (exp_tor4_DjDk * exp_tor34_inv);
+      dfn11 = -a3 + (a3 - a4) * f11_DjDk;
+    }
     const R CEtors1 = sin_ijk * sin_jkl * CV;
     const R CEtors2 = -fn10 * R(2) * p_tor1 * V2 * exp_tor1 * (R(2) - BOpi_jk - f11_DjDk) *
                       (R(1) - sqr(cos_omega)) * sin_ijk * sin_jkl;

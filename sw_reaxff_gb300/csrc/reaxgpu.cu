@@ -88,6 +88,7 @@ struct rg_system {
   std::vector<int> seg_counts;
   std::vector<void *> per_seg;
   int nseg_alloc = 0;
+  int n_cap = 0;                  // atoms the per-atom arrays and lists hold
   std::vector<double> e_host;     // per-segment energies read back
   std::vector<int> seg_iters;     // last QEq: s and t iterations per segment
   Dev d{};
@@ -199,22 +200,23 @@ int alloc_segs(rg_system *h) {
   d.nseg = ns;
   if (ns <= h->nseg_alloc) return 0;
   free_bucket(h->per_seg);
+  const int cap = ns == 1 ? 1 : ns + ns / 2;
   int r = 0;
   SegGeom *sg = nullptr;
-  r |= dalloc(h, h->per_seg, &sg, (size_t)ns);
+  r |= dalloc(h, h->per_seg, &sg, (size_t)cap);
   d.seg = sg;
-  r |= dalloc(h, h->per_seg, &d.red, (size_t)ns * RG_NRED);
-  r |= dalloc(h, h->per_seg, &d.energy, (size_t)ns * RG_NE);
+  r |= dalloc(h, h->per_seg, &d.red, (size_t)cap * RG_NRED);
+  r |= dalloc(h, h->per_seg, &d.energy, (size_t)cap * RG_NE);
   r |= dalloc(h, h->per_seg, &d.n_active, 1);
   if (r) return RG_E_CUDA;
-  h->nseg_alloc = ns;
+  h->nseg_alloc = cap;
   return 0;
 }
 
 int alloc_bonds(rg_system *h) {
   free_bucket(h->per_b);
   Dev &d = h->d;
-  const size_t S = (size_t)d.n * d.bond_cap;
+  const size_t S = (size_t)h->n_cap * d.bond_cap;
   int r = 0;
   r |= dalloc(h, h->per_b, &d.b_nbr, S);
   r |= dalloc(h, h->per_b, &d.b_sym, S);
@@ -263,7 +265,7 @@ int alloc_items(rg_system *h, long long nval, long long ntor) {
 int alloc_nbrs(rg_system *h) {
   free_bucket(h->per_nb);
   Dev &d = h->d;
-  const size_t S = (size_t)d.n * d.nb_cap;
+  const size_t S = (size_t)h->n_cap * d.nb_cap;
   int r = 0;
   r |= dalloc(h, h->per_nb, &d.nbr, S);
   if (d.mixed) {
@@ -279,12 +281,20 @@ int alloc_nbrs(rg_system *h) {
 int alloc_hb(rg_system *h) {
   free_bucket(h->per_hb);
   Dev &d = h->d;
-  return dalloc(h, h->per_hb, &d.hb_nbr, (size_t)d.n * d.hb_cap);
+  return dalloc(h, h->per_hb, &d.hb_nbr, (size_t)h->n_cap * d.hb_cap);
 }
 
+// Per-atom arrays and the lists sized for n_cap >= n atoms.  A handle whose
+// atom count shrinks (or grows within its capacity) keeps its arrays: no
+// cudaFree, which would wait for other streams' work, on the way.
 int alloc_atoms(rg_system *h, int n) {
-  free_bucket(h->per_n);
   Dev &d = h->d;
+  if (n <= h->n_cap) {
+    d.n = n;
+    return 0;
+  }
+  free_bucket(h->per_n);
+  h->n_cap = n;
   d.n = n;
   int r = 0;
   auto &B = h->per_n;
@@ -792,7 +802,7 @@ static int set_atoms_impl(rg_system *h, int n, const double *x, const int *type,
     for (int c : h->seg_counts) sum += c < 0 ? n : c;
     if (sum != n) return fail(h, RG_E_ARG, "segment atom counts do not add up to the atom count");
   }
-  if (n != h->d.n) {
+  {
     int rc = alloc_atoms(h, n);
     if (rc) return rc;
   }
@@ -922,6 +932,28 @@ int rg_set_state(rg_system *h, const double *x, const double *v, const double *f
   if (f) CK(cudaMemcpyAsync(h->d.f_o, f, 3 * sizeof(double) * h->n, cudaMemcpyHostToDevice, h->st));
   h->lists_valid = false;
   h->forces_valid = f != nullptr;
+  return RG_OK;
+}
+
+int rg_get_histories(rg_system *h, double *s_hist, double *t_hist) {
+  if (!h || !s_hist || !t_hist) return RG_E_ARG;
+  if (!h->n) return fail(h, RG_E_STATE, "no atoms set");
+  const size_t b = 5 * sizeof(double) * h->n;
+  CK(cudaMemcpyAsync(s_hist, h->d.s_hist, b, cudaMemcpyDeviceToHost, h->st));
+  CK(cudaMemcpyAsync(t_hist, h->d.t_hist, b, cudaMemcpyDeviceToHost, h->st));
+  CK(cudaStreamSynchronize(h->st));
+  return RG_OK;
+}
+
+int rg_set_histories(rg_system *h, const double *s_hist, const double *t_hist) {
+  if (!h) return RG_E_ARG;
+  if (!h->n) return fail(h, RG_E_STATE, "no atoms set");
+  const size_t b = 5 * sizeof(double) * h->n;
+  if (s_hist) CK(cudaMemcpyAsync(h->d.s_hist, s_hist, b, cudaMemcpyHostToDevice, h->st));
+  else CK(cudaMemsetAsync(h->d.s_hist, 0, b, h->st));
+  if (t_hist) CK(cudaMemcpyAsync(h->d.t_hist, t_hist, b, cudaMemcpyHostToDevice, h->st));
+  else CK(cudaMemsetAsync(h->d.t_hist, 0, b, h->st));
+  CK(cudaStreamSynchronize(h->st));
   return RG_OK;
 }
 

@@ -141,7 +141,11 @@ __global__ void k_gather(Dev d) {
   double x = d.x_o[3 * i], y = d.x_o[3 * i + 1], z = d.x_o[3 * i + 2];
   d.xs[s] = make_double4(x, y, z, d.q_o[i]);
   int t = d.type_o[i];
-  d.xf[s] = make_float4((float)x, (float)y, (float)z, __int_as_float(t));
+  const float hx = __double2float_rn(x), hy = __double2float_rn(y), hz = __double2float_rn(z);
+  d.xf[s] = make_float4(hx, hy, hz, __int_as_float(t));
+  if (d.xl)
+    d.xl[s] = make_float4(__double2float_rn(x - (double)hx), __double2float_rn(y - (double)hy),
+                          __double2float_rn(z - (double)hz), (float)d.q_o[i]);
   d.ts[s] = t;
   d.tags[s] = d.tag_o[i];
   d.seg_s[s] = d.seg_o[i];
@@ -169,30 +173,58 @@ struct NbrQueue {
 };
 
 // finish 32 queued candidates (lanes with q < cnt hold one each)
+// exact (FP64, explicitly rounded) squared distance of a queued entry
+__device__ __forceinline__ double exact_d2(const Dev &d, int j, int sx, int sy, int sz,
+                                          const double4 &xi, const double *L) {
+  const double4 xj = d.xs[j];
+  const double dx = __dsub_rn(__dadd_rn(xj.x, sx * L[0]), xi.x);
+  const double dy = __dsub_rn(__dadd_rn(xj.y, sy * L[1]), xi.y);
+  const double dz = __dsub_rn(__dadd_rn(xj.z, sz * L[2]), xi.z);
+  return __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
+}
+
+// FP32 tests in the mixed form are taken only when d^2 is more than this
+// relative distance from the cutoff; the FP32 d^2 from df_disp is good to a
+// few 1e-7, so the outcome is the FP64 one
+constexpr float MARGIN32 = 1e-5f;
+
 template <bool MIXED>
 __device__ __forceinline__ void nbr_flush(const Dev &d, const Control &C, const ForceField &F,
                                           const NbrQueue &Q, int cnt, int lane, int i,
-                                          const double4 &xi, int ti, long long row, int cap,
-                                          const double *L, int &cntN, int &cntF) {
+                                          const double4 &xi, const float4 &xif, const float4 &xil,
+                                          int ti, long long row, int cap, const double *L,
+                                          const SegGeom &g, int &cntN, int &cntF) {
   bool in = false, near = false;
   double d2 = 0.0;
+  float d2f = 0.f;
   int j = 0, img = 0;
   if (lane < cnt) {
     j = Q.j[lane];
     img = Q.img[lane];
     int sx, sy, sz;
     img_unpack(img, &sx, &sy, &sz);
-    const double4 xj = d.xs[j];
-    const double dx = __dsub_rn(__dadd_rn(xj.x, sx * L[0]), xi.x);
-    const double dy = __dsub_rn(__dadd_rn(xj.y, sy * L[1]), xi.y);
-    const double dz = __dsub_rn(__dadd_rn(xj.z, sz * L[2]), xi.z);
-    d2 = __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
-    in = d2 <= C.list_cut2;
-    if (in) {
-      const double nc2 = C.near_cut * C.near_cut;
-      if (d2 <= nc2 * (1.0 - 1e-12)) near = true;
-      else if (d2 > nc2 * (1.0 + 1e-12)) near = false;
-      else near = __dsqrt_rn(d2) <= C.near_cut;
+    if (MIXED) {
+      const float4 hj = d.xf[j], lj = d.xl[j];
+      const float dx = df_disp(hj.x, lj.x, xif.x, xil.x, sx, g.Lh[0], g.Ll[0]);
+      const float dy = df_disp(hj.y, lj.y, xif.y, xil.y, sy, g.Lh[1], g.Ll[1]);
+      const float dz = df_disp(hj.z, lj.z, xif.z, xil.z, sz, g.Lh[2], g.Ll[2]);
+      d2f = dx * dx + dy * dy + dz * dz;
+      const float lc2 = (float)C.list_cut2;
+      if (d2f <= lc2 * (1.f - MARGIN32)) in = true;
+      else if (d2f > lc2 * (1.f + MARGIN32)) in = false;
+      else in = exact_d2(d, j, sx, sy, sz, xi, L) <= C.list_cut2;
+      // near part: conservative (the bond pass tests its own cutoffs)
+      const float nc = (float)C.near_cut;
+      near = d2f <= nc * nc * (1.f + MARGIN32);
+    } else {
+      d2 = exact_d2(d, j, sx, sy, sz, xi, L);
+      in = d2 <= C.list_cut2;
+      if (in) {
+        const double nc2 = C.near_cut * C.near_cut;
+        if (d2 <= nc2 * (1.0 - 1e-12)) near = true;
+        else if (d2 > nc2 * (1.0 + 1e-12)) near = false;
+        else near = __dsqrt_rn(d2) <= C.near_cut;
+      }
     }
   }
   const unsigned mn = __ballot_sync(FULL, in && near);
@@ -202,10 +234,9 @@ __device__ __forceinline__ void nbr_flush(const Dev &d, const Control &C, const 
     const int pos = near ? cntN + __popc(mn & lanemask_lt())
                          : cap - 1 - (cntF + __popc(mf & lanemask_lt()));
     double h = 0.0;
-    if (MIXED && d2 <= C.swb2) {
+    if (MIXED && d2f <= (float)C.swb2) {
       // FP32: factored taper when swa = 0
       const int tj = __float_as_int(d.xf[j].w);
-      const float d2f = (float)d2;
       const float r = d2f * rsqrtf(d2f);
       float tp;
       if (C.qtap_factored) {
@@ -263,6 +294,7 @@ __global__ void __launch_bounds__(NB_WARPS * 32) k_build_nbrs(Dev d) {
   const ForceField &F = *d.ff;
   const double4 xi = d.xs[i];
   const float4 xif = d.xf[i];
+  const float4 xil = MIXED ? d.xl[i] : make_float4(0.f, 0.f, 0.f, 0.f);
   const int ti = d.ts[i];
   const float cut2f = (float)(C.list_cut2 * (1.0 + 1e-5) + 0.05);
   const SegGeom &g = d.seg[d.seg_s[i]];
@@ -319,7 +351,7 @@ __global__ void __launch_bounds__(NB_WARPS * 32) k_build_nbrs(Dev d) {
           qn += __popc(mc);
           __syncwarp();
           if (qn >= 32) {
-            nbr_flush<MIXED>(d, C, F, Q, 32, lane, i, xi, ti, row, cap, L, cntN, cntF);
+            nbr_flush<MIXED>(d, C, F, Q, 32, lane, i, xi, xif, xil, ti, row, cap, L, g, cntN, cntF);
             __syncwarp();
             // move the leftover (< 32) to the front of the queue
             const int left = qn - 32;
@@ -340,7 +372,7 @@ __global__ void __launch_bounds__(NB_WARPS * 32) k_build_nbrs(Dev d) {
       }
     }
   }
-  if (qn > 0) nbr_flush<MIXED>(d, C, F, Q, qn, lane, i, xi, ti, row, cap, L, cntN, cntF);
+  if (qn > 0) nbr_flush<MIXED>(d, C, F, Q, qn, lane, i, xi, xif, xil, ti, row, cap, L, g, cntN, cntF);
   if (lane == 0) {
     d.n_near[i] = cntN;
     d.n_far[i] = cntF;
@@ -471,6 +503,7 @@ __global__ void __launch_bounds__(NB_WARPS * 32) k_build_bonds(Dev d) {
   const int n = d.n;
   const SegGeom &g = d.seg[d.seg_s[i]];
   const double L[3] = {g.L[0], g.L[1], g.L[2]};
+  const float4 xil = MIXED ? d.xl[i] : make_float4(0.f, 0.f, 0.f, 0.f);
   // FP32 prefilter radius: anything that could be within bond_cut, and for
   // H atoms within hbond_cut
   const float rpre = (float)((ihb ? fmax(C.bond_cut, C.hbond_cut) : C.bond_cut) + 0.01);
@@ -494,12 +527,26 @@ __global__ void __launch_bounds__(NB_WARPS * 32) k_build_bonds(Dev d) {
         const float fy = xjf.y + (float)(sy * L[1]) - xif.y;
         const float fz = xjf.z + (float)(sz * L[2]) - xif.z;
         if (fx * fx + fy * fy + fz * fz <= rpre2) {
-          const double4 xj = d.xs[j];
-          dx = __dsub_rn(__dadd_rn(xj.x, sx * L[0]), xi.x);
-          dy = __dsub_rn(__dadd_rn(xj.y, sy * L[1]), xi.y);
-          dz = __dsub_rn(__dadd_rn(xj.z, sz * L[2]), xi.z);
-          const double d2 = __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
-          dist = __dsqrt_rn(d2);
+          bool exact = true;
+          if (MIXED) {
+            // FP32 displacement; FP64 only within MARGIN32 of a cutoff
+            const float4 lj = d.xl[j];
+            const float ex = df_disp(xjf.x, lj.x, xif.x, xil.x, sx, g.Lh[0], g.Ll[0]);
+            const float ey = df_disp(xjf.y, lj.y, xif.y, xil.y, sy, g.Lh[1], g.Ll[1]);
+            const float ez = df_disp(xjf.z, lj.z, xif.z, xil.z, sz, g.Lh[2], g.Ll[2]);
+            const float df = sqrtf(ex * ex + ey * ey + ez * ez);
+            const float bc = (float)C.bond_cut, hc = (float)C.hbond_cut;
+            exact = fabsf(df - bc) <= MARGIN32 * bc || (ihb && fabsf(df - hc) <= MARGIN32 * hc);
+            dx = ex; dy = ey; dz = ez; dist = df;
+          }
+          if (exact) {
+            const double4 xj = d.xs[j];
+            dx = __dsub_rn(__dadd_rn(xj.x, sx * L[0]), xi.x);
+            dy = __dsub_rn(__dadd_rn(xj.y, sy * L[1]), xi.y);
+            dz = __dsub_rn(__dadd_rn(xj.z, sz * L[2]), xi.z);
+            const double d2 = __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
+            dist = __dsqrt_rn(d2);
+          }
           const int tj = __float_as_int(xjf.w);
           const Sbp &sj = F.sbp[tj];
           if (ihb && dist <= C.hbond_cut && sj.p_hbond == 2) ish = true;

@@ -72,22 +72,55 @@ __device__ __forceinline__ void taper(const Control &C, R r, R rinv, R &Tp, R &d
 // displacement; energies are added in FP64
 template <typename R>
 __device__ __forceinline__ void pair_terms(const Dev &d, const ForceField &F, const Control &C,
-                                          uint32_t e, bool act, const double4 &xi, int ti,
-                                          const double *L, double &evdw, double &eele, double &c,
-                                          double &dx, double &dy, double &dz, int &j) {
+                                          uint32_t e, bool act, const double4 &xi,
+                                          const float4 &xif, const float4 &xil, int ti,
+                                          const double *L, const SegGeom &g, double &evdw,
+                                          double &eele, double &c, double &dx, double &dy,
+                                          double &dz, int &j) {
   c = 0.0; dx = dy = dz = 0.0;
   j = (int)(e >> 8);
   if (!act) return;
   int sx, sy, sz;
   img_unpack((int)(e & 255u), &sx, &sy, &sz);
-  const double4 xj = d.xs[j];
-  // same rounding as the pair-list membership test
-  dx = __dsub_rn(__dadd_rn(xj.x, sx * L[0]), xi.x);
-  dy = __dsub_rn(__dadd_rn(xj.y, sy * L[1]), xi.y);
-  dz = __dsub_rn(__dadd_rn(xj.z, sz * L[2]), xi.z);
-  const double d2x = __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
-  if (d2x > C.nonb_cut2) { dx = dy = dz = 0.0; return; }
-  const R d2 = (R)d2x;
+  R d2;
+  double qj;
+  if (std::is_same<R, float>::value) {
+    // mixed form: FP32 displacement from the (hi, lo) positions; the list
+    // holds exactly the pairs within max(nonb_cut, swb), so only a QEq
+    // taper radius above nonb_cut needs a test here (FP64 near the cutoff)
+    const float4 hj = d.xf[j], lj = d.xl[j];
+    const float fx = df_disp(hj.x, lj.x, xif.x, xil.x, sx, g.Lh[0], g.Ll[0]);
+    const float fy = df_disp(hj.y, lj.y, xif.y, xil.y, sy, g.Lh[1], g.Ll[1]);
+    const float fz = df_disp(hj.z, lj.z, xif.z, xil.z, sz, g.Lh[2], g.Ll[2]);
+    const float d2f = fx * fx + fy * fy + fz * fz;
+    if (!C.nonb_all_listed) {
+      const float nc2 = (float)C.nonb_cut2;
+      bool out;
+      if (d2f <= nc2 * (1.f - 1e-5f)) out = false;
+      else if (d2f > nc2 * (1.f + 1e-5f)) out = true;
+      else {
+        const double4 xj = d.xs[j];
+        const double ex = __dsub_rn(__dadd_rn(xj.x, sx * L[0]), xi.x);
+        const double ey = __dsub_rn(__dadd_rn(xj.y, sy * L[1]), xi.y);
+        const double ez = __dsub_rn(__dadd_rn(xj.z, sz * L[2]), xi.z);
+        out = __dadd_rn(__dadd_rn(__dmul_rn(ex, ex), __dmul_rn(ey, ey)), __dmul_rn(ez, ez)) > C.nonb_cut2;
+      }
+      if (out) return;
+    }
+    dx = fx; dy = fy; dz = fz;
+    d2 = (R)d2f;
+    qj = lj.w;                 // charge (FP32 copy)
+  } else {
+    // same rounding as the pair-list membership test
+    const double4 xj = d.xs[j];
+    qj = xj.w;
+    dx = __dsub_rn(__dadd_rn(xj.x, sx * L[0]), xi.x);
+    dy = __dsub_rn(__dadd_rn(xj.y, sy * L[1]), xi.y);
+    dz = __dsub_rn(__dadd_rn(xj.z, sz * L[2]), xi.z);
+    const double d2x = __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
+    if (d2x > C.nonb_cut2) { dx = dy = dz = 0.0; return; }
+    d2 = (R)d2x;
+  }
   const R rinv = rs_(d2);
   const R r = d2 * rinv;
   const Tbp &tw = F.tbp[ti][d.ts[j]];
@@ -133,7 +166,7 @@ __device__ __forceinline__ void pair_terms(const Dev &d, const ForceField &F, co
   R inv3;
   if (std::is_same<R, float>::value) inv3 = (R)rcbrtf((float)dr3gamij_1);
   else inv3 = (R)rpow_third((double)dr3gamij_1, RG_C3_ELE);
-  const R qq = (R)(C_ele * xi.w * xj.w);
+  const R qq = std::is_same<R, float>::value ? (R)C_ele * xil.w * (R)qj : (R)(C_ele * xi.w * qj);
   const R e_ele = qq * Tp * inv3;
   const R CEclmb = qq * (dTap - Tp * r / dr3gamij_1) * inv3;
   evdw += (double)(Tp * (e_vdW + e_core + e_lg));
@@ -155,6 +188,8 @@ __global__ void __launch_bounds__(NBW * 32) k_nonbonded(Dev d, int eflag) {
     const Control &C = *d.ctl;
     const int n = d.n;
     const double4 xi = d.xs[i];
+    const float4 xif = d.xf[i];
+    const float4 xil = d.mixed ? d.xl[i] : make_float4(0.f, 0.f, 0.f, 0.f);
     const int ti = d.ts[i];
     const SegGeom &g = d.seg[d.seg_s[i]];
     const double L[3] = {g.L[0], g.L[1], g.L[2]};
@@ -188,7 +223,7 @@ __global__ void __launch_bounds__(NBW * 32) k_nonbonded(Dev d, int eflag) {
         const uint32_t e = act ? Q.e[lane] : 0u;
         double c, dx, dy, dz;
         int j;
-        pair_terms<R>(d, F, C, e, act, xi, ti, L, evdw, eele, c, dx, dy, dz, j);
+        pair_terms<R>(d, F, C, e, act, xi, xif, xil, ti, L, g, evdw, eele, c, dx, dy, dz, j);
         if (act && c != 0.0) {
           fx -= c * dx;
           fy -= c * dy;

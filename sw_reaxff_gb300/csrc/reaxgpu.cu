@@ -163,6 +163,8 @@ int setup_cells(rg_system *h) {
     g.S = S;
     long long nseg_cells = 1;
     for (int k = 0; k < 3; ++k) {
+      g.Lh[k] = (float)g.L[k];
+      g.Ll[k] = (float)(g.L[k] - (double)g.Lh[k]);
       if (g.L[k] < rc / S)
         return fail(h, RG_E_ARG, "box edge shorter than half the pair cutoff is not supported");
       int nc = (int)std::floor(g.L[k] * S / (rc * (1.0 + 1e-9)));
@@ -311,6 +313,8 @@ int alloc_atoms(rg_system *h, int n) {
   r |= dalloc(h, B, &d.iperm, (size_t)n);
   r |= dalloc(h, B, &d.xs, (size_t)n);
   r |= dalloc(h, B, &d.xf, (size_t)n);
+  if (d.mixed) r |= dalloc(h, B, &d.xl, (size_t)n);
+  else d.xl = nullptr;
   r |= dalloc(h, B, &d.ts, (size_t)n);
   r |= dalloc(h, B, &d.tags, (size_t)n);
   r |= dalloc(h, B, &d.n_near, (size_t)n);
@@ -596,6 +600,7 @@ int rg_create(const char *ffield_path, const rg_params *pin, rg_system **out) {
   c.qtap_factored = (h->p.qeq_swa == 0.0);
   c.inv_swb_nb = 1.0 / c.nonb_cut;
   c.inv_swb_q = 1.0 / h->p.qeq_swb;
+  c.nonb_all_listed = c.nonb_cut2 >= c.list_cut2;
   if (h->p.precision != RG_PREC_FP64 && h->p.precision != RG_PREC_MIXED) {
     delete h;
     return RG_E_ARG;

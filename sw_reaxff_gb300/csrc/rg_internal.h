@@ -71,6 +71,7 @@ struct ForceField {
 // Geometry of one segment (periodic orthogonal box and its cells).
 struct SegGeom {
   double L[3];        // box edges
+  float Lh[3], Ll[3]; // L as an unevaluated FP32 pair (hi + lo)
   double cellw[3];    // cell edges (L / nc)
   int nc[3];          // cells per dimension
   int S;              // stencil half-width (cells)
@@ -94,6 +95,7 @@ struct Control {
   // conditioned in FP32 near the cutoff where the expanded form cancels
   int tap_factored, qtap_factored;
   double inv_swb_nb, inv_swb_q;
+  int nonb_all_listed;   // nonb_cut >= list cutoff: every list entry is a vdW/Coulomb pair
 };
 
 // Parse an ffield file (restates Read_Force_Field,
@@ -135,6 +137,8 @@ struct Dev {
   // sorted atoms
   double4 *xs;        // x, y, z, q
   float4 *xf;         // fp32 x, y, z, (type as float)
+  float4 *xl;         // mixed form: x - xf (FP32), so x = xf + xl to ~2^-48;
+                      // w: the charge (FP32)
   int *ts, *tags;
 
   // full pair list, row-major rows of nb_cap; near entries from the front,
@@ -255,6 +259,17 @@ __device__ __forceinline__ void seg_block_add(const double *vin, int seg, double
       }
     }
   }
+}
+
+// Mixed form: displacement x_j + s L - x_i from positions and box edges
+// held as FP32 (hi, lo) pairs.  The hi parts combine first (exact or
+// rounded once at the result's magnitude), so the error is a few FP32 ulps
+// of the displacement itself, not of the coordinates.
+__device__ __forceinline__ float df_disp(float hj, float lj, float hi, float li, int s, float Lh,
+                                         float Ll) {
+  const float a = __fsub_rn(__fmaf_rn((float)s, Lh, hj), hi);
+  const float b = __fsub_rn(__fmaf_rn((float)s, Ll, lj), li);
+  return __fadd_rn(a, b);
 }
 
 __device__ __forceinline__ double pow_third(double x, double dc) {

@@ -11,7 +11,7 @@ from sw_reaxff_gb300.api import PREC_MIXED
 
 pytestmark = pytest.mark.gpu
 
-TOL_Q, TOL_F, TOL_X, TOL_V = 1e-6, 1e-6, 1e-6, 1e-6
+TOL_Q, TOL_F, TOL_X, TOL_V = 1e-5, 1e-5, 1e-5, 1e-5
 
 
 def stream():

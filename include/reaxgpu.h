@@ -68,6 +68,14 @@ typedef struct {
   int qeq_imax;         /* 200   CG iteration limit                     */
   int precision;        /* RG_PREC_FP64 or RG_PREC_MIXED               */
   int device;           /* CUDA device ordinal                          */
+  int tabulate;         /* FP64 form: vdW+Coulomb and QEq H from cubic
+                           Hermite tables in r^2 with this many intervals
+                           per type pair (the reference's control
+                           "tabulate_long_range", off in its NULL control);
+                           0 = analytic.  Default 65536: ~1e-10 of the
+                           analytic pair functions (rg_table_check). */
+  int tabulate_check;   /* 1: measure the tables' error at rg_create
+                           (rg_table_info); 0 (default): skip */
 } rg_params;
 
 /* Energy vector of rg_compute: entries 0..13 are the pair's pvector in the
@@ -103,6 +111,14 @@ const char *rg_last_error(const rg_system *h);
  * read; msg (msg_len chars, may be NULL) then gets the reason. */
 int rg_ffield_info(const char *path, int *ntypes, char *names, int len, char *msg,
                    int msg_len);
+
+/* FP64 tables: intervals per type pair (0: analytic) and the largest
+ * relative deviation of the interpolants from the analytic pair functions,
+ * measured when the tables were built. */
+int rg_table_info(const rg_system *h, int *intervals, double *max_rel_err);
+/* The same check without a device: builds the tables of p->tabulate
+ * intervals (p NULL: defaults) for a force field on the host. */
+int rg_table_check(const char *ffield_path, const rg_params *p, double *max_rel_err);
 
 int rg_num_types(const rg_system *h);
 /* element name of ffield type t (0-based), upper case */

@@ -31,7 +31,7 @@ EXPORTED = ["rg_default_params", "rg_create", "rg_destroy", "rg_last_error",
             "rg_stream", "rg_profile_enable", "rg_profile_get", "rg_measure_fp64_peak",
             "rg_qeq_noalloc", "rg_set_masses", "rg_ffield_info", "rg_set_segments",
             "rg_num_segments", "rg_get_energies", "rg_get_segment_iters",
-            "rg_get_histories", "rg_set_histories"]
+            "rg_get_histories", "rg_set_histories", "rg_table_info", "rg_table_check"]
 
 
 class Params(C.Structure):
@@ -40,7 +40,8 @@ class Params(C.Structure):
                 ("enobondsflag", C.c_int), ("lgflag", C.c_int),
                 ("qeq_swa", C.c_double), ("qeq_swb", C.c_double),
                 ("qeq_tol", C.c_double), ("qeq_imax", C.c_int),
-                ("precision", C.c_int), ("device", C.c_int)]
+                ("precision", C.c_int), ("device", C.c_int), ("tabulate", C.c_int),
+                ("tabulate_check", C.c_int)]
 
 
 class Stats(C.Structure):
@@ -86,6 +87,8 @@ def load_library(path: str = LIBPATH):
     L.rg_get_energies.argtypes = [C.c_void_p, dp]
     L.rg_get_segment_iters.argtypes = [C.c_void_p, ip]
     L.rg_get_histories.argtypes = [C.c_void_p, dp, dp]
+    L.rg_table_info.argtypes = [C.c_void_p, ip, dp]
+    L.rg_table_check.argtypes = [C.c_char_p, P(Params), dp]
     L.rg_set_histories.argtypes = [C.c_void_p, dp, dp]
     L.rg_ffield_info.argtypes = [C.c_char_p, ip, C.c_char_p, C.c_int, C.c_char_p, C.c_int]
     L.rg_set_atoms.argtypes = [C.c_void_p, C.c_int, dp, ip, ip, dp, dp]
@@ -263,6 +266,14 @@ class ReaxGPU:
         s = None if s is None else np.ascontiguousarray(s, np.float64)
         t = None if t is None else np.ascontiguousarray(t, np.float64)
         self._chk(self.L.rg_set_histories(self.h, _dp(s), _dp(t)), "rg_set_histories")
+
+    def table_info(self):
+        """(intervals per type pair, largest relative error) of the FP64
+        pair-function tables; (0, 0.0) for analytic pair functions."""
+        n = C.c_int()
+        e = C.c_double()
+        self._chk(self.L.rg_table_info(self.h, C.byref(n), C.byref(e)), "rg_table_info")
+        return n.value, e.value
 
     def set_positions(self, x):
         x = np.ascontiguousarray(x, np.float64)

@@ -15,7 +15,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "libreaxgpu.so")
 BUILD = os.path.join(HERE, "_build")
-SOURCES = ["ffield.cpp", "lists.cu", "bonded.cu", "nonbonded.cu", "qeq.cu",
+SOURCES = ["ffield.cpp", "tables.cpp", "lists.cu", "bonded.cu", "nonbonded.cu", "qeq.cu",
            "nve.cu", "peak.cu", "noalloc.cu", "reaxgpu.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
@@ -58,7 +58,7 @@ def build(force: bool = False, verbose_ptxas: bool = False) -> str:
     if os.path.exists(OUT) and not force and \
             all(os.path.getmtime(OUT) >= os.path.getmtime(o) for o in objs):
         return OUT
-    cmd = [nvcc(), "-shared", "-o", OUT, *objs, *ARCH, "-lcudart"]
+    cmd = [nvcc(), "-shared", "-o", OUT, *objs, *ARCH, "-lcudart", "-lpthread"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")

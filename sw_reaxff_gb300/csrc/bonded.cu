@@ -790,7 +790,8 @@ __device__ __forceinline__ void valence_item(const Dev &d, unsigned long long it
 // FP32 is not used for angles within about 1.1 degrees of 0 or 180 (sine
 // below 0.02): there the reference's 1/sin factors (MIN_SINE clamps at
 // 1e-10) overflow FP32 and its cancellations lose the result.  The FP32
-// kernels queue those items for an FP64 pass.
+// kernels queue those items (and the over-coordination cases below) for an
+// FP64 pass.
 __device__ __forceinline__ bool near_linear(const Dev &d, long long sa, long long sb) {
   const float ax = (float)d.b_dx[sa], ay = (float)d.b_dy[sa], az = (float)d.b_dz[sa];
   const float bx = (float)d.b_dx[sb], by = (float)d.b_dy[sb], bz = (float)d.b_dz[sb];
@@ -818,7 +819,11 @@ __global__ void __launch_bounds__(128) k_valence(Dev d, int eflag, long long nit
     sg = d.seg_s[(int)(it >> 16)];
     if (std::is_same<R, float>::value) {
       const int j = (int)(it >> 16), kk = (int)((it >> 8) & 255), ph = (int)(it & 255);
-      if (near_linear(d, (long long)kk * d.n + j, (long long)ph * d.n + j))
+      // FP64 as well for strongly over-coordinated centres, where
+      // exp(p_val6 Delta) (p_val6 ~ 34) and exp(p_coa2 Delta_val) and their
+      // products leave the FP32 range
+      if (near_linear(d, (long long)kk * d.n + j, (long long)ph * d.n + j) ||
+          d.Delta_boc[j] > 1.0 || d.Delta_val[j] > 2.0)
         d.w_fb_val[atomicAdd(&d.fb_cnt[0], 1)] = it;
       else
         valence_item<R>(d, it, e_ang, e_pen, e_coa);

@@ -258,6 +258,13 @@ __device__ __forceinline__ void nbr_flush(const Dev &d, const Control &C, const 
     } else if (MIXED) {
       d.nbr[row + pos] = ((uint32_t)j << 8) | (uint32_t)img;
       d.hval32[row + pos] = 0.f;
+    } else if (d2 <= C.swb2 && C.tab_n && d2 >= C.tab_s0) {
+      // FP64 table of H_ij (cubic Hermite in r^2)
+      double h00, h01, h10, h11;
+      const int k = tab_weights(C, d2, h00, h01, h10, h11);
+      const int tj = __float_as_int(d.xf[j].w);
+      const double *T = d.tab_h + ((long long)C.tab_pair[ti][tj] * (C.tab_n + 1) + k) * 2;
+      h = h00 * T[0] + h01 * T[2] + h10 * T[1] + h11 * T[3];
     } else if (d2 <= C.swb2) {
       // H_ij = Tap(r) * 14.4 / (r^3 + shld)^c, c = 0.3333333333333
       const double r = d2 * rsqrt(d2);

@@ -120,6 +120,21 @@ __device__ __forceinline__ void pair_terms(const Dev &d, const ForceField &F, co
     const double d2x = __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
     if (d2x > C.nonb_cut2) { dx = dy = dz = 0.0; return; }
     d2 = (R)d2x;
+    if (C.tab_n && d2x >= C.tab_s0) {
+      // FP64 tables: energies and (1/r) dE/dr = 2 dE/ds by cubic Hermite
+      double h00, h01, h10, h11;
+      const int k = tab_weights(C, d2x, h00, h01, h10, h11);
+      const double *T = d.tab_nb + ((long long)C.tab_pair[ti][d.ts[j]] * (C.tab_n + 1) + k) * 6;
+      const double ev = h00 * T[0] + h01 * T[6] + h10 * T[1] + h11 * T[7];
+      const double dv = h00 * T[1] + h01 * T[7] + h10 * T[2] + h11 * T[8];
+      const double ec = h00 * T[3] + h01 * T[9] + h10 * T[4] + h11 * T[10];
+      const double dcl = h00 * T[4] + h01 * T[10] + h10 * T[5] + h11 * T[11];
+      const double qq = C_ele * xi.w * qj;
+      evdw += ev;
+      eele += qq * ec;
+      c = 2.0 * (dv + qq * dcl);
+      return;
+    }
   }
   const R rinv = rs_(d2);
   const R r = d2 * rinv;

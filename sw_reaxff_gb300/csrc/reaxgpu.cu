@@ -78,6 +78,8 @@ struct rg_system {
   Control ctl{};
   ForceField *d_ff = nullptr;
   Control *d_ctl = nullptr;
+  double *d_tab = nullptr;        // FP64 tables (nb then H)
+  double tab_err = 0.0;
   cudaStream_t st = nullptr;
   std::string err;
   int n = 0;
@@ -548,6 +550,32 @@ int do_qeq(rg_system *h, int *its, int *itt) {
   return 0;
 }
 
+// scalar controls from the run parameters and the force field
+// (reaxc_ffield_sunway.cpp:86-88 and the pair_style defaults)
+void init_control(const rg_params &p, const ForceField &ff, Control &c) {
+  c.bo_cut = 0.01 * ff.gp[29];
+  c.nonb_low = ff.gp[11];
+  c.nonb_cut = ff.gp[12];
+  c.bond_cut = p.bond_cut;
+  c.hbond_cut = p.hbond_cut;
+  c.thb_cut = p.thb_cut;
+  c.thb_cutsq = p.thb_cutsq;
+  c.enobondsflag = p.enobondsflag;
+  c.lgflag = p.lgflag;
+  const double lc = std::max(c.nonb_cut, p.qeq_swb);
+  c.list_cut2 = lc * lc;
+  c.nonb_cut2 = c.nonb_cut * c.nonb_cut;
+  c.swb2 = p.qeq_swb * p.qeq_swb;
+  c.near_cut = std::max(c.bond_cut, c.hbond_cut);
+  rg_init_taper(c.nonb_low, c.nonb_cut, c.Tap);
+  rg_init_taper(p.qeq_swa, p.qeq_swb, c.qTap);
+  c.tap_factored = (c.nonb_low == 0.0);
+  c.qtap_factored = (p.qeq_swa == 0.0);
+  c.inv_swb_nb = 1.0 / c.nonb_cut;
+  c.inv_swb_q = 1.0 / p.qeq_swb;
+  c.nonb_all_listed = c.nonb_cut2 >= c.list_cut2;
+}
+
 }  // namespace
 
 extern "C" {
@@ -565,6 +593,8 @@ void rg_default_params(rg_params *p) {
   p->qeq_imax = 200;
   p->precision = RG_PREC_FP64;
   p->device = 0;
+  p->tabulate = 65536;
+  p->tabulate_check = 0;
 }
 
 int rg_create(const char *ffield_path, const rg_params *pin, rg_system **out) {
@@ -579,28 +609,8 @@ int rg_create(const char *ffield_path, const rg_params *pin, rg_system **out) {
     return RG_E_FILE;
   }
   Control &c = h->ctl;
-  // reaxc_ffield_sunway.cpp:86-88 and the pair_style defaults
-  c.bo_cut = 0.01 * h->ff.gp[29];
-  c.nonb_low = h->ff.gp[11];
-  c.nonb_cut = h->ff.gp[12];
-  c.bond_cut = h->p.bond_cut;
-  c.hbond_cut = h->p.hbond_cut;
-  c.thb_cut = h->p.thb_cut;
-  c.thb_cutsq = h->p.thb_cutsq;
-  c.enobondsflag = h->p.enobondsflag;
-  c.lgflag = h->p.lgflag;
-  const double lc = std::max(c.nonb_cut, h->p.qeq_swb);
-  c.list_cut2 = lc * lc;
-  c.nonb_cut2 = c.nonb_cut * c.nonb_cut;
-  c.swb2 = h->p.qeq_swb * h->p.qeq_swb;
-  c.near_cut = std::max(c.bond_cut, c.hbond_cut);
-  rg_init_taper(c.nonb_low, c.nonb_cut, c.Tap);
-  rg_init_taper(h->p.qeq_swa, h->p.qeq_swb, c.qTap);
-  c.tap_factored = (c.nonb_low == 0.0);
-  c.qtap_factored = (h->p.qeq_swa == 0.0);
-  c.inv_swb_nb = 1.0 / c.nonb_cut;
-  c.inv_swb_q = 1.0 / h->p.qeq_swb;
-  c.nonb_all_listed = c.nonb_cut2 >= c.list_cut2;
+  init_control(h->p, h->ff, c);
+  const double lc = std::sqrt(c.list_cut2);
   if (h->p.precision != RG_PREC_FP64 && h->p.precision != RG_PREC_MIXED) {
     delete h;
     return RG_E_ARG;
@@ -616,20 +626,45 @@ int rg_create(const char *ffield_path, const rg_params *pin, rg_system **out) {
     delete h;
     return RG_E_ARG;
   }
+  // FP64 tables of the pair functions (tables.cpp)
+  std::vector<double> tab_nb, tab_h;
+  c.tab_n = 0;
+  if (!h->d.mixed && h->p.tabulate > 0) {
+    const int nt = h->ff.ntypes;
+    for (int a = 0; a < nt; ++a)
+      for (int b = 0; b < nt; ++b) c.tab_pair[a][b] = rg_pair_index(a, b, nt);
+    const double s0 = 0.25, s1 = c.list_cut2 * (1.0 + 1e-9);
+    c.tab_n = h->p.tabulate;
+    c.tab_s0 = s0;
+    c.tab_ds = (s1 - s0) / c.tab_n;
+    c.tab_inv_ds = 1.0 / c.tab_ds;
+    h->tab_err = rg_build_tables(h->ff, c, c.tab_n, s0, s1, tab_nb, tab_h, h->p.tabulate_check != 0);
+  }
   cudaError_t ce = cudaSetDevice(h->p.device);
   if (ce == cudaSuccess) ce = cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking);
   if (ce == cudaSuccess) ce = cudaMalloc(&h->d_ff, sizeof(ForceField));
   if (ce == cudaSuccess) ce = cudaMalloc(&h->d_ctl, sizeof(Control));
   if (ce == cudaSuccess) ce = cudaMemcpy(h->d_ff, &h->ff, sizeof(ForceField), cudaMemcpyHostToDevice);
   if (ce == cudaSuccess) ce = cudaMemcpy(h->d_ctl, &h->ctl, sizeof(Control), cudaMemcpyHostToDevice);
+  if (ce == cudaSuccess && c.tab_n) {
+    ce = cudaMalloc(&h->d_tab, sizeof(double) * (tab_nb.size() + tab_h.size()));
+    if (ce == cudaSuccess)
+      ce = cudaMemcpy(h->d_tab, tab_nb.data(), sizeof(double) * tab_nb.size(), cudaMemcpyHostToDevice);
+    if (ce == cudaSuccess)
+      ce = cudaMemcpy(h->d_tab + tab_nb.size(), tab_h.data(), sizeof(double) * tab_h.size(),
+                      cudaMemcpyHostToDevice);
+  }
   if (ce != cudaSuccess) {
     if (h->d_ff) cudaFree(h->d_ff);
     if (h->d_ctl) cudaFree(h->d_ctl);
+    if (h->d_tab) cudaFree(h->d_tab);
     delete h;
     return RG_E_CUDA;
   }
   h->d.ff = h->d_ff;
   h->d.ctl = h->d_ctl;
+  h->d.tab_nb = h->d_tab;
+  h->d.tab_h = h->d_tab ? h->d_tab + tab_nb.size() : nullptr;
   *out = h;
   return RG_OK;
 }
@@ -658,6 +693,7 @@ int rg_destroy(rg_system *h) {
   if (h->cells) cudaFree(h->cells);
   cudaFree(h->d_ff);
   cudaFree(h->d_ctl);
+  if (h->d_tab) cudaFree(h->d_tab);
   cudaStreamDestroy(h->st);
   delete h;
   return RG_OK;
@@ -680,6 +716,33 @@ int rg_ffield_info(const char *path, int *ntypes, char *names, int len, char *ms
   if (names && len > 0)
     for (int t = 0; t < ff->ntypes; ++t) std::snprintf(names + (size_t)t * len, len, "%s", ff->sbp[t].name);
   delete ff;
+  return RG_OK;
+}
+
+int rg_table_check(const char *ffield_path, const rg_params *pin, double *max_rel_err) {
+  if (!ffield_path || !max_rel_err) return RG_E_ARG;
+  rg_params p;
+  if (pin) p = *pin;
+  else rg_default_params(&p);
+  if (p.tabulate <= 0) return RG_E_ARG;
+  ForceField *ff = new ForceField();
+  if (!rg_read_ffield(ffield_path, p.lgflag, ff).empty()) {
+    delete ff;
+    return RG_E_FILE;
+  }
+  Control *c = new Control();
+  init_control(p, *ff, *c);
+  std::vector<double> nb, hq;
+  *max_rel_err = rg_build_tables(*ff, *c, p.tabulate, 0.25, c->list_cut2 * (1.0 + 1e-9), nb, hq, true);
+  delete c;
+  delete ff;
+  return RG_OK;
+}
+
+int rg_table_info(const rg_system *h, int *intervals, double *max_rel_err) {
+  if (!h) return RG_E_ARG;
+  if (intervals) *intervals = h->ctl.tab_n;
+  if (max_rel_err) *max_rel_err = h->tab_err;
   return RG_OK;
 }
 

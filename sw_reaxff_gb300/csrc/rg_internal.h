@@ -96,11 +96,19 @@ struct Control {
   int tap_factored, qtap_factored;
   double inv_swb_nb, inv_swb_q;
   int nonb_all_listed;   // nonb_cut >= list cutoff: every list entry is a vdW/Coulomb pair
+  // FP64 tables (tables.cpp): tab_n intervals of width tab_ds over
+  // s = r^2 in [tab_s0, ...]; 0 = analytic pair functions
+  int tab_n;
+  double tab_s0, tab_ds, tab_inv_ds;
+  int tab_pair[RG_MAXT][RG_MAXT];   // unordered type pair -> table index
 };
 
 // Parse an ffield file (restates Read_Force_Field,
 // reaxc_ffield_sunway.cpp:35-714).  Returns empty string or an error.
 std::string rg_read_ffield(const char *path, int lgflag, ForceField *ff);
+int rg_pair_index(int ti, int tj, int nt);
+double rg_build_tables(const ForceField &F, const Control &C, int n, double s0, double s1,
+                       std::vector<double> &nb, std::vector<double> &hq, bool check);
 void rg_init_taper(double swa, double swb, double *Tap);
 
 // ---------------------------------------------------------------------
@@ -122,6 +130,8 @@ struct Dev {
 
   const ForceField *ff;
   const Control *ctl;
+  const double *tab_nb;  // [pair][node][6]: Ev, dEv/ds, d2Ev/ds2, Ec, dEc/ds, d2Ec/ds2
+  const double *tab_h;   // [pair][node][2]: H, dH/ds
 
   // original order (persistent state)
   double *x_o, *v_o, *q_o, *f_o;
@@ -270,6 +280,21 @@ __device__ __forceinline__ float df_disp(float hj, float lj, float hi, float li,
   const float a = __fsub_rn(__fmaf_rn((float)s, Lh, hj), hi);
   const float b = __fsub_rn(__fmaf_rn((float)s, Ll, lj), li);
   return __fadd_rn(a, b);
+}
+
+// cubic Hermite weights of s in the FP64 tables (h10, h11 carry the node
+// spacing, so they multiply the stored s-derivatives directly)
+__device__ __forceinline__ int tab_weights(const Control &C, double s, double &h00, double &h01,
+                                           double &h10, double &h11) {
+  const double x = (s - C.tab_s0) * C.tab_inv_ds;
+  int k = (int)x;
+  if (k > C.tab_n - 1) k = C.tab_n - 1;
+  const double u = x - (double)k, u2 = u * u, w = 1.0 - u;
+  h01 = u2 * (3.0 - 2.0 * u);
+  h00 = 1.0 - h01;
+  h10 = C.tab_ds * u * w * w;
+  h11 = -C.tab_ds * u2 * w;
+  return k;
 }
 
 __device__ __forceinline__ double pow_third(double x, double dc) {

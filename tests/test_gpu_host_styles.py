@@ -89,12 +89,12 @@ def test_deck_nve_follows_rg_run(tmp_path, ffield):
     L = s.box
     dx = st["x"] - x[order]
     dx -= L * np.round(dx / L)        # either side may have wrapped
-    # the CG charges move by up to a few 1e-6 when FP64 atomics reorder,
-    # which moves positions by ~1e-7 A and velocities by ~1e-8 over these
-    # steps
+    # the CG charges move by up to a few 1e-6 per solve when FP64 atomics
+    # reorder; over 10 steps of extrapolated solves that reaches ~1e-5 in
+    # the charges, ~1e-7 A in the positions and ~1e-8 A/fs in the velocities
     assert np.abs(dx).max() < 1e-5
     assert np.abs(st["v"] - v[order]).max() < 1e-5
-    assert np.abs(st["q"] - q[order]).max() < 1e-5
+    assert np.abs(st["q"] - q[order]).max() < 5e-5
     lines = [ln for ln in out.splitlines() if ln.strip() and ln.split()[0].isdigit()]
     assert [int(ln.split()[0]) for ln in lines] == [0, 5, 10]
     etot = [float(ln.split()[3]) for ln in lines]

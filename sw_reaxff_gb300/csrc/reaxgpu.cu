@@ -106,6 +106,12 @@ struct rg_system {
   // RG_CHECK_FINITE=1: test the force/CdDelta accumulators after every
   // force phase and name the first phase that produced a non-finite value
   bool check_finite = false;
+  // the CG iterations of a poll interval as one captured CUDA graph,
+  // replayed while any system's solve is active; recaptured whenever the
+  // device arrays or sizes change (RG_NO_GRAPHS=1: plain launches)
+  cudaGraphExec_t cg_exec = nullptr;
+  Dev cg_dev{};
+  bool use_graphs = true;
   rg_stats stats{};
   double energy[RG_NE] = {0};
   Prof prof;
@@ -485,6 +491,31 @@ int do_compute(rg_system *h, int eflag) {
   return 0;
 }
 
+// capture `chunk` CG iterations (A, SpMV, ctrl/C/flip) as a graph
+int capture_cg(rg_system *h, int chunk) {
+  Dev &d = h->d;
+  if (h->cg_exec) {
+    cudaGraphExecDestroy(h->cg_exec);
+    h->cg_exec = nullptr;
+  }
+  cudaGraph_t g = nullptr;
+  CK(cudaStreamBeginCapture(h->st, cudaStreamCaptureModeThreadLocal));
+  for (int k = 0; k < chunk; ++k) {
+    launch_qeq_cg_A(d, h->st);
+    launch_qeq_spmv(d, h->st, d.qd, d.qq);
+    launch_qeq_cg_C(d, h->st);
+  }
+  cudaError_t e = cudaStreamEndCapture(h->st, &g);
+  if (e == cudaSuccess) e = cudaGraphInstantiate(&h->cg_exec, g, 0);
+  if (g) cudaGraphDestroy(g);
+  if (e != cudaSuccess) {
+    h->cg_exec = nullptr;
+    return fail(h, RG_E_CUDA, std::string("CG graph capture: ") + cudaGetErrorString(e));
+  }
+  h->cg_dev = d;
+  return 0;
+}
+
 int do_qeq(rg_system *h, int *its, int *itt) {
   Dev &d = h->d;
   int rc;
@@ -513,10 +544,20 @@ int do_qeq(rg_system *h, int *its, int *itt) {
       CK(cudaStreamSynchronize(h->st));
       if (active == 0) break;
       if (done_iters > imax + 8) return fail(h, RG_E_NUMERIC, "QEq iteration control lost");
-      for (int k = 0; k < chunk; ++k) {
-        { Scope sc(h, PH_QVEC, 1); launch_qeq_cg_A(d, h->st); }
-        { Scope sc(h, PH_QSPMV, 1); launch_qeq_spmv(d, h->st, d.qd, d.qq); }
-        { Scope sc(h, PH_QVEC, 3); launch_qeq_cg_C(d, h->st); }
+      if (h->use_graphs && !h->prof.on) {
+        // phase profiling needs the per-kernel event marks: plain launches
+        if (!h->cg_exec || std::memcmp(&h->cg_dev, &d, sizeof(Dev)) != 0) {
+          int rc2 = capture_cg(h, chunk);
+          if (rc2) return rc2;
+        }
+        CK(cudaGraphLaunch(h->cg_exec, h->st));
+        h->launches += 5 * chunk;
+      } else {
+        for (int k = 0; k < chunk; ++k) {
+          { Scope sc(h, PH_QVEC, 1); launch_qeq_cg_A(d, h->st); }
+          { Scope sc(h, PH_QSPMV, 1); launch_qeq_spmv(d, h->st, d.qd, d.qq); }
+          { Scope sc(h, PH_QVEC, 3); launch_qeq_cg_C(d, h->st); }
+        }
       }
       done_iters += chunk;
     }
@@ -619,6 +660,8 @@ int rg_create(const char *ffield_path, const rg_params *pin, rg_system **out) {
   {
     const char *cf = std::getenv("RG_CHECK_FINITE");
     h->check_finite = cf && (cf[0] == '1' || cf[0] == '2');
+    const char *ng = std::getenv("RG_NO_GRAPHS");
+    h->use_graphs = !(ng && ng[0] == '1');
     h->d.debug = cf && cf[0] == '2';
   }
   for (int t = 0; t < RG_MAXT; ++t) h->ff.nve_mass[t] = h->ff.sbp[t].mass;
@@ -658,6 +701,7 @@ int rg_create(const char *ffield_path, const rg_params *pin, rg_system **out) {
     if (h->d_ff) cudaFree(h->d_ff);
     if (h->d_ctl) cudaFree(h->d_ctl);
     if (h->d_tab) cudaFree(h->d_tab);
+  if (h->cg_exec) cudaGraphExecDestroy(h->cg_exec);
     delete h;
     return RG_E_CUDA;
   }
@@ -690,10 +734,12 @@ int rg_destroy(rg_system *h) {
   free_bucket(h->per_b);
   free_bucket(h->per_hb);
   free_bucket(h->per_items);
+  free_bucket(h->per_seg);
   if (h->cells) cudaFree(h->cells);
   cudaFree(h->d_ff);
   cudaFree(h->d_ctl);
   if (h->d_tab) cudaFree(h->d_tab);
+  if (h->cg_exec) cudaGraphExecDestroy(h->cg_exec);
   cudaStreamDestroy(h->st);
   delete h;
   return RG_OK;

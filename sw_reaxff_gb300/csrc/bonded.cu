@@ -402,9 +402,9 @@ __global__ void __launch_bounds__(256) k_hbonds(Dev d, int eflag) {
         img_unpack((int)(ek & 255u), &sx, &sy, &sz);
         const double4 xk = d.xs[k];
         double dk64[3];
-        dk64[0] = __dsub_rn(__dadd_rn(xk.x, sx * L[0]), xj.x);
-        dk64[1] = __dsub_rn(__dadd_rn(xk.y, sy * L[1]), xj.y);
-        dk64[2] = __dsub_rn(__dadd_rn(xk.z, sz * L[2]), xj.z);
+        dk64[0] = __dsub_rn(img_shift(xk.x, sx, L[0]), xj.x);
+        dk64[1] = __dsub_rn(img_shift(xk.y, sy, L[1]), xj.y);
+        dk64[2] = __dsub_rn(img_shift(xk.z, sz, L[2]), xj.z);
         const double r64 = __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(dk64[0], dk64[0]),
                                                           __dmul_rn(dk64[1], dk64[1])),
                                                 __dmul_rn(dk64[2], dk64[2])));

@@ -177,9 +177,9 @@ struct NbrQueue {
 __device__ __forceinline__ double exact_d2(const Dev &d, int j, int sx, int sy, int sz,
                                           const double4 &xi, const double *L) {
   const double4 xj = d.xs[j];
-  const double dx = __dsub_rn(__dadd_rn(xj.x, sx * L[0]), xi.x);
-  const double dy = __dsub_rn(__dadd_rn(xj.y, sy * L[1]), xi.y);
-  const double dz = __dsub_rn(__dadd_rn(xj.z, sz * L[2]), xi.z);
+  const double dx = __dsub_rn(img_shift(xj.x, sx, L[0]), xi.x);
+  const double dy = __dsub_rn(img_shift(xj.y, sy, L[1]), xi.y);
+  const double dz = __dsub_rn(img_shift(xj.z, sz, L[2]), xi.z);
   return __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
 }
 
@@ -260,11 +260,11 @@ __device__ __forceinline__ void nbr_flush(const Dev &d, const Control &C, const 
       d.hval32[row + pos] = 0.f;
     } else if (d2 <= C.swb2 && C.tab_n && d2 >= C.tab_s0) {
       // FP64 table of H_ij (cubic Hermite in r^2)
-      double h00, h01, h10, h11;
-      const int k = tab_weights(C, d2, h00, h01, h10, h11);
+      double h01, t10, t11;
+      const int k = tab_weights(C, d2, h01, t10, t11);
       const int tj = __float_as_int(d.xf[j].w);
       const double *T = d.tab_h + ((long long)C.tab_pair[ti][tj] * (C.tab_n + 1) + k) * 2;
-      h = h00 * T[0] + h01 * T[2] + h10 * T[1] + h11 * T[3];
+      h = tab_interp(T[0], T[2], T[1], T[3], h01, t10, t11);
     } else if (d2 <= C.swb2) {
       // H_ij = Tap(r) * 14.4 / (r^3 + shld)^c, c = 0.3333333333333
       const double r = d2 * rsqrt(d2);
@@ -510,7 +510,7 @@ __global__ void __launch_bounds__(NB_WARPS * 32) k_build_bonds(Dev d) {
   const int n = d.n;
   const SegGeom &g = d.seg[d.seg_s[i]];
   const double L[3] = {g.L[0], g.L[1], g.L[2]};
-  const float4 xil = MIXED ? d.xl[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+  const float4 xil = d.xl[i];
   // FP32 prefilter radius: anything that could be within bond_cut, and for
   // H atoms within hbond_cut
   const float rpre = (float)((ihb ? fmax(C.bond_cut, C.hbond_cut) : C.bond_cut) + 0.01);
@@ -530,43 +530,46 @@ __global__ void __launch_bounds__(NB_WARPS * 32) k_build_bonds(Dev d) {
         int sx, sy, sz;
         img_unpack((int)(e & 255u), &sx, &sy, &sz);
         const float4 xjf = d.xf[j];
-        const float fx = xjf.x + (float)(sx * L[0]) - xif.x;
-        const float fy = xjf.y + (float)(sy * L[1]) - xif.y;
-        const float fz = xjf.z + (float)(sz * L[2]) - xif.z;
+        const float fx = xjf.x + (float)sx * g.Lh[0] - xif.x;
+        const float fy = xjf.y + (float)sy * g.Lh[1] - xif.y;
+        const float fz = xjf.z + (float)sz * g.Lh[2] - xif.z;
         if (fx * fx + fy * fy + fz * fz <= rpre2) {
-          bool exact = true;
-          if (MIXED) {
-            // FP32 displacement; FP64 only within MARGIN32 of a cutoff
-            const float4 lj = d.xl[j];
-            const float ex = df_disp(xjf.x, lj.x, xif.x, xil.x, sx, g.Lh[0], g.Ll[0]);
-            const float ey = df_disp(xjf.y, lj.y, xif.y, xil.y, sy, g.Lh[1], g.Ll[1]);
-            const float ez = df_disp(xjf.z, lj.z, xif.z, xil.z, sz, g.Lh[2], g.Ll[2]);
-            const float df = sqrtf(ex * ex + ey * ey + ez * ez);
-            const float bc = (float)C.bond_cut, hc = (float)C.hbond_cut;
-            exact = fabsf(df - bc) <= MARGIN32 * bc || (ihb && fabsf(df - hc) <= MARGIN32 * hc);
-            dx = ex; dy = ey; dz = ez; dist = df;
-          }
+          const int tj = __float_as_int(xjf.w);
+          const Sbp &sj = F.sbp[tj];
+          const bool hb_rel = ihb && sj.p_hbond == 2;
+          // FP32 distance from the (hi, lo) positions decides away from the
+          // cutoffs; the FP64 form takes the exact distance for every
+          // possible bond (its value is stored), the mixed form only within
+          // MARGIN32 of a cutoff
+          const float4 lj = d.xl[j];
+          const float ex = df_disp(xjf.x, lj.x, xif.x, xil.x, sx, g.Lh[0], g.Ll[0]);
+          const float ey = df_disp(xjf.y, lj.y, xif.y, xil.y, sy, g.Lh[1], g.Ll[1]);
+          const float ez = df_disp(xjf.z, lj.z, xif.z, xil.z, sz, g.Lh[2], g.Ll[2]);
+          const float df = sqrtf(ex * ex + ey * ey + ez * ez);
+          const float bc = (float)C.bond_cut, hc = (float)C.hbond_cut;
+          const bool near_b = fabsf(df - bc) <= MARGIN32 * bc;
+          const bool near_h = hb_rel && fabsf(df - hc) <= MARGIN32 * hc;
+          const bool exact = MIXED ? (near_b || near_h) : (df <= bc * (1.f + MARGIN32) || near_h);
+          dx = ex; dy = ey; dz = ez; dist = df;
           if (exact) {
             const double4 xj = d.xs[j];
-            dx = __dsub_rn(__dadd_rn(xj.x, sx * L[0]), xi.x);
-            dy = __dsub_rn(__dadd_rn(xj.y, sy * L[1]), xi.y);
-            dz = __dsub_rn(__dadd_rn(xj.z, sz * L[2]), xi.z);
+            dx = __dsub_rn(img_shift(xj.x, sx, L[0]), xi.x);
+            dy = __dsub_rn(img_shift(xj.y, sy, L[1]), xi.y);
+            dz = __dsub_rn(img_shift(xj.z, sz, L[2]), xi.z);
             const double d2 = __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
             dist = __dsqrt_rn(d2);
           }
-          const int tj = __float_as_int(xjf.w);
-          const Sbp &sj = F.sbp[tj];
-          if (ihb && dist <= C.hbond_cut && sj.p_hbond == 2) ish = true;
+          if (hb_rel && dist <= C.hbond_cut) ish = true;
           if (dist <= C.bond_cut) {
             const Tbp &tw = F.tbp[ti][tj];
-            const float df = (float)dist;
+            const float dd = (float)dist;
             float est = 0.f;
             if (si.r_s > 0.0 && sj.r_s > 0.0)
-              est += (float)(1.0 + C.bo_cut) * expf((float)tw.p_bo1 * powf(df / (float)tw.r_s, (float)tw.p_bo2));
+              est += (float)(1.0 + C.bo_cut) * expf((float)tw.p_bo1 * powf(dd / (float)tw.r_s, (float)tw.p_bo2));
             if (si.r_pi > 0.0 && sj.r_pi > 0.0)
-              est += expf((float)tw.p_bo3 * powf(df / (float)tw.r_p, (float)tw.p_bo4));
+              est += expf((float)tw.p_bo3 * powf(dd / (float)tw.r_p, (float)tw.p_bo4));
             if (si.r_pi_pi > 0.0 && sj.r_pi_pi > 0.0)
-              est += expf((float)tw.p_bo5 * powf(df / (float)tw.r_pp, (float)tw.p_bo6));
+              est += expf((float)tw.p_bo5 * powf(dd / (float)tw.r_pp, (float)tw.p_bo6));
             cand = est >= bo_half;
           }
         }

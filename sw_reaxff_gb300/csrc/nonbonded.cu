@@ -100,9 +100,9 @@ __device__ __forceinline__ void pair_terms(const Dev &d, const ForceField &F, co
       else if (d2f > nc2 * (1.f + 1e-5f)) out = true;
       else {
         const double4 xj = d.xs[j];
-        const double ex = __dsub_rn(__dadd_rn(xj.x, sx * L[0]), xi.x);
-        const double ey = __dsub_rn(__dadd_rn(xj.y, sy * L[1]), xi.y);
-        const double ez = __dsub_rn(__dadd_rn(xj.z, sz * L[2]), xi.z);
+        const double ex = __dsub_rn(img_shift(xj.x, sx, L[0]), xi.x);
+        const double ey = __dsub_rn(img_shift(xj.y, sy, L[1]), xi.y);
+        const double ez = __dsub_rn(img_shift(xj.z, sz, L[2]), xi.z);
         out = __dadd_rn(__dadd_rn(__dmul_rn(ex, ex), __dmul_rn(ey, ey)), __dmul_rn(ez, ez)) > C.nonb_cut2;
       }
       if (out) return;
@@ -114,21 +114,22 @@ __device__ __forceinline__ void pair_terms(const Dev &d, const ForceField &F, co
     // same rounding as the pair-list membership test
     const double4 xj = d.xs[j];
     qj = xj.w;
-    dx = __dsub_rn(__dadd_rn(xj.x, sx * L[0]), xi.x);
-    dy = __dsub_rn(__dadd_rn(xj.y, sy * L[1]), xi.y);
-    dz = __dsub_rn(__dadd_rn(xj.z, sz * L[2]), xi.z);
+    dx = __dsub_rn(img_shift(xj.x, sx, L[0]), xi.x);
+    dy = __dsub_rn(img_shift(xj.y, sy, L[1]), xi.y);
+    dz = __dsub_rn(img_shift(xj.z, sz, L[2]), xi.z);
     const double d2x = __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
     if (d2x > C.nonb_cut2) { dx = dy = dz = 0.0; return; }
     d2 = (R)d2x;
     if (C.tab_n && d2x >= C.tab_s0) {
       // FP64 tables: energies and (1/r) dE/dr = 2 dE/ds by cubic Hermite
-      double h00, h01, h10, h11;
-      const int k = tab_weights(C, d2x, h00, h01, h10, h11);
+      double h01, t10, t11;
+      const int k = tab_weights(C, d2x, h01, t10, t11);
       const double *T = d.tab_nb + ((long long)C.tab_pair[ti][d.ts[j]] * (C.tab_n + 1) + k) * 6;
-      const double ev = h00 * T[0] + h01 * T[6] + h10 * T[1] + h11 * T[7];
-      const double dv = h00 * T[1] + h01 * T[7] + h10 * T[2] + h11 * T[8];
-      const double ec = h00 * T[3] + h01 * T[9] + h10 * T[4] + h11 * T[10];
-      const double dcl = h00 * T[4] + h01 * T[10] + h10 * T[5] + h11 * T[11];
+      const double ds = C.tab_ds;
+      const double ev = tab_interp(T[0], T[6], ds * T[1], ds * T[7], h01, t10, t11);
+      const double dv = tab_interp(T[1], T[7], T[2], T[8], h01, t10, t11);
+      const double ec = tab_interp(T[3], T[9], ds * T[4], ds * T[10], h01, t10, t11);
+      const double dcl = tab_interp(T[4], T[10], T[5], T[11], h01, t10, t11);
       const double qq = C_ele * xi.w * qj;
       evdw += ev;
       eele += qq * ec;

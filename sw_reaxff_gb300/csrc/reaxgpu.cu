@@ -321,8 +321,7 @@ int alloc_atoms(rg_system *h, int n) {
   r |= dalloc(h, B, &d.iperm, (size_t)n);
   r |= dalloc(h, B, &d.xs, (size_t)n);
   r |= dalloc(h, B, &d.xf, (size_t)n);
-  if (d.mixed) r |= dalloc(h, B, &d.xl, (size_t)n);
-  else d.xl = nullptr;
+  r |= dalloc(h, B, &d.xl, (size_t)n);
   r |= dalloc(h, B, &d.ts, (size_t)n);
   r |= dalloc(h, B, &d.tags, (size_t)n);
   r |= dalloc(h, B, &d.n_near, (size_t)n);
@@ -681,6 +680,7 @@ int rg_create(const char *ffield_path, const rg_params *pin, rg_system **out) {
     c.tab_s0 = s0;
     c.tab_ds = (s1 - s0) / c.tab_n;
     c.tab_inv_ds = 1.0 / c.tab_ds;
+    c.tab_x0 = -s0 * c.tab_inv_ds;
     h->tab_err = rg_build_tables(h->ff, c, c.tab_n, s0, s1, tab_nb, tab_h, h->p.tabulate_check != 0);
   }
   cudaError_t ce = cudaSetDevice(h->p.device);

@@ -99,7 +99,7 @@ struct Control {
   // FP64 tables (tables.cpp): tab_n intervals of width tab_ds over
   // s = r^2 in [tab_s0, ...]; 0 = analytic pair functions
   int tab_n;
-  double tab_s0, tab_ds, tab_inv_ds;
+  double tab_s0, tab_ds, tab_inv_ds, tab_x0;   // tab_x0 = -tab_s0 / tab_ds
   int tab_pair[RG_MAXT][RG_MAXT];   // unordered type pair -> table index
 };
 
@@ -271,6 +271,12 @@ __device__ __forceinline__ void seg_block_add(const double *vin, int seg, double
   }
 }
 
+// x + s L with the reference's rounding; the image-free case (most pairs)
+// skips the product and the add, which leave x unchanged anyway
+__device__ __forceinline__ double img_shift(double x, int s, double L) {
+  return s ? __dadd_rn(x, s * L) : x;
+}
+
 // Mixed form: displacement x_j + s L - x_i from positions and box edges
 // held as FP32 (hi, lo) pairs.  The hi parts combine first (exact or
 // rounded once at the result's magnitude), so the error is a few FP32 ulps
@@ -282,19 +288,26 @@ __device__ __forceinline__ float df_disp(float hj, float lj, float hi, float li,
   return __fadd_rn(a, b);
 }
 
-// cubic Hermite weights of s in the FP64 tables (h10, h11 carry the node
-// spacing, so they multiply the stored s-derivatives directly)
-__device__ __forceinline__ int tab_weights(const Control &C, double s, double &h00, double &h01,
-                                           double &h10, double &h11) {
-  const double x = (s - C.tab_s0) * C.tab_inv_ds;
+// cubic Hermite interpolation in the FP64 tables: for s, the interval k,
+// the weight h01 of the right node value and the weights t10, t11 of the
+// node derivatives in units of the spacing; with y0, y1 the node values and
+// p0, p1 the derivatives times the spacing:
+//   y(s) = y0 + h01 (y1 - y0) + t10 p0 + t11 p1
+__device__ __forceinline__ int tab_weights(const Control &C, double s, double &h01, double &t10,
+                                           double &t11) {
+  const double x = fma(s, C.tab_inv_ds, C.tab_x0);
   int k = (int)x;
   if (k > C.tab_n - 1) k = C.tab_n - 1;
   const double u = x - (double)k, u2 = u * u, w = 1.0 - u;
-  h01 = u2 * (3.0 - 2.0 * u);
-  h00 = 1.0 - h01;
-  h10 = C.tab_ds * u * w * w;
-  h11 = -C.tab_ds * u2 * w;
+  h01 = u2 * fma(-2.0, u, 3.0);
+  t10 = u * w * w;
+  t11 = -u2 * w;
   return k;
+}
+
+__device__ __forceinline__ double tab_interp(double y0, double y1, double p0, double p1, double h01,
+                                             double t10, double t11) {
+  return fma(t11, p1, fma(t10, p0, fma(h01, y1 - y0, y0)));
 }
 
 __device__ __forceinline__ double pow_third(double x, double dc) {

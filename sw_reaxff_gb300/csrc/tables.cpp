@@ -109,8 +109,9 @@ int rg_pair_index(int ti, int tj, int nt) {
   return ti * nt - ti * (ti - 1) / 2 + (tj - ti);
 }
 
-// Fills nb[npair][n+1][6] = {Ev, Dv, Dv', Ec, Dc, Dc'} (D = dE/ds, ' = d/ds)
-// and hq[npair][n+1][2] = {H, H'}, over s in [s0, s1] with n intervals; with
+// Fills nb[npair][n+1][6] = {Ev, Dv, ds Dv', Ec, Dc, ds Dc'} (D = dE/ds,
+// ' = d/ds, ds the node spacing) and hq[npair][n+1][2] = {H, ds H'}, over s
+// in [s0, s1] with n intervals; with
 // check, returns the largest deviation of the interpolants from the
 // analytic functions at 5 interior points of every interval (else 0).
 double rg_build_tables(const ForceField &F, const Control &C, int n, double s0, double s1,
@@ -141,13 +142,13 @@ double rg_build_tables(const ForceField &F, const Control &C, int n, double s0, 
         double *e = &nb[((size_t)p * (n + 1) + k) * 6];
         e[0] = ev(s);
         e[1] = dv(s);
-        e[2] = deriv(dv, s, h);
+        e[2] = ds * deriv(dv, s, h);
         e[3] = ecf(s);
         e[4] = dc(s);
-        e[5] = deriv(dc, s, h);
+        e[5] = ds * deriv(dc, s, h);
         double *q = &hq[((size_t)p * (n + 1) + k) * 2];
         q[0] = hf(s);
-        q[1] = deriv(hf, s, h);
+        q[1] = ds * deriv(hf, s, h);
       }
       if (!check) return;
       // accuracy of the interpolants against the analytic functions:
@@ -172,14 +173,14 @@ double rg_build_tables(const ForceField &F, const Control &C, int n, double s0, 
           double x[4];
           pair_funcs(F, C, ti, tj, std::sqrt(s), &x[0], &x[1], &x[2], &x[3]);
           const double iv[4] = {hermite(a[0], a[1], b[0], b[1], u, ds),
-                                2.0 * hermite(a[1], a[2], b[1], b[2], u, ds),
+                                2.0 * hermite(a[1], a[2], b[1], b[2], u, 1.0),
                                 hermite(a[3], a[4], b[3], b[4], u, ds),
-                                2.0 * hermite(a[4], a[5], b[4], b[5], u, ds)};
+                                2.0 * hermite(a[4], a[5], b[4], b[5], u, 1.0)};
           for (int c = 0; c < 4; ++c) {
             const double scale = std::max(std::fabs(x[c]), 1e-4 * M[c]);
             if (scale > 0.0) worst = std::max(worst, std::fabs(iv[c] - x[c]) / scale);
           }
-          const double hv = hermite(qa[0], qa[1], qb[0], qb[1], u, ds), hx = hf(s);
+          const double hv = hermite(qa[0], qa[1], qb[0], qb[1], u, 1.0), hx = hf(s);
           const double hs = std::max(std::fabs(hx), 1e-4 * M[4]);
           if (hs > 0.0) worst = std::max(worst, std::fabs(hv - hx) / hs);
         }

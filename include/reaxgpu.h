@@ -171,9 +171,15 @@ int rg_set_state(rg_system *h, const double *x, const double *v,
 int rg_qeq(rg_system *h, double *q_out, int *iters_s, int *iters_t);
 
 /* Force step.  f_out[3n] host or NULL (forces, kcal/mol/A), energies
- * [RG_NENERGY] host or NULL; eflag = 0 skips the energy reductions. */
+ * [RG_NENERGY] host or NULL; eflag = 0 skips the energy reductions;
+ * vflag != 0 also accumulates the virial (rg_get_virial). */
 int rg_compute(rg_system *h, int eflag, int vflag, double *f_out,
                double *energies);
+/* Virial of the last force step computed with vflag, per segment
+ * (v[6*nseg]): sum over atoms of r (x) f in the order xx yy zz xy xz yz,
+ * kcal/mol, the quantity LAMMPS's virial[6] holds (virial_fdotr_compute
+ * over local + ghost atoms, pair_reaxc_sunway.cpp:674-763). */
+int rg_get_virial(rg_system *h, double *v);
 
 /* Velocity-Verlet halves (dt in fs). */
 int rg_nve_initial(rg_system *h, double dt);

@@ -31,7 +31,8 @@ EXPORTED = ["rg_default_params", "rg_create", "rg_destroy", "rg_last_error",
             "rg_stream", "rg_profile_enable", "rg_profile_get", "rg_measure_fp64_peak",
             "rg_qeq_noalloc", "rg_set_masses", "rg_ffield_info", "rg_set_segments",
             "rg_num_segments", "rg_get_energies", "rg_get_segment_iters",
-            "rg_get_histories", "rg_set_histories", "rg_table_info", "rg_table_check"]
+            "rg_get_histories", "rg_set_histories", "rg_table_info", "rg_table_check",
+            "rg_get_virial"]
 
 
 class Params(C.Structure):
@@ -88,6 +89,7 @@ def load_library(path: str = LIBPATH):
     L.rg_get_segment_iters.argtypes = [C.c_void_p, ip]
     L.rg_get_histories.argtypes = [C.c_void_p, dp, dp]
     L.rg_table_info.argtypes = [C.c_void_p, ip, dp]
+    L.rg_get_virial.argtypes = [C.c_void_p, dp]
     L.rg_table_check.argtypes = [C.c_char_p, P(Params), dp]
     L.rg_set_histories.argtypes = [C.c_void_p, dp, dp]
     L.rg_ffield_info.argtypes = [C.c_char_p, ip, C.c_char_p, C.c_int, C.c_char_p, C.c_int]
@@ -285,11 +287,19 @@ class ReaxGPU:
         self._chk(self.L.rg_qeq(self.h, _dp(q), C.byref(a), C.byref(b)), "rg_qeq")
         return q, a.value, b.value
 
-    def compute(self, eflag=1):
+    def compute(self, eflag=1, vflag=0):
         f = np.zeros((self.n, 3))
         e = np.zeros(NENERGY)
-        self._chk(self.L.rg_compute(self.h, eflag, 0, _dp(f), _dp(e)), "rg_compute")
+        self._chk(self.L.rg_compute(self.h, eflag, vflag, _dp(f), _dp(e)), "rg_compute")
         return f, dict(zip(ENERGY_NAMES, e))
+
+    def virial(self):
+        """Virial (xx, yy, zz, xy, xz, yz of sum r x f, kcal/mol) of the last
+        force step computed with vflag, one row per segment."""
+        ns = self.L.rg_num_segments(self.h)
+        v = np.zeros((ns, 6))
+        self._chk(self.L.rg_get_virial(self.h, _dp(v)), "rg_get_virial")
+        return v
 
     def nve_initial(self, dt):
         self._chk(self.L.rg_nve_initial(self.h, dt), "rg_nve_initial")

@@ -372,6 +372,7 @@ __global__ void __launch_bounds__(256) k_hbonds(Dev d, int eflag) {
   const int j = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int n = d.n;
   double ehb = 0.0;
+  double w[6] = {0, 0, 0, 0, 0, 0};
   if (j < n && d.ff->sbp[d.ts[j]].p_hbond == 1) {
     const ForceField &F = *d.ff;
     const int tj = d.ts[j];
@@ -433,7 +434,11 @@ __global__ void __launch_bounds__(256) k_hbonds(Dev d, int eflag) {
         fjz += (double)(CEhb2 * djv[2] - c3 * djk[2]);
         add3(fC, n, k, 1.0, (double)(CEhb2 * dk[0] + c3 * djk[0]), (double)(CEhb2 * dk[1] + c3 * djk[1]),
              (double)(CEhb2 * dk[2] + c3 * djk[2]));
+        if (d.vflag)
+          vir_acc(w, dk64[0], dk64[1], dk64[2], (double)(CEhb2 * dk[0] + c3 * djk[0]),
+                  (double)(CEhb2 * dk[1] + c3 * djk[1]), (double)(CEhb2 * dk[2] + c3 * djk[2]));
       }
+      if (d.vflag) vir_acc(w, d.b_dx[s], d.b_dy[s], d.b_dz[s], fix, fiy, fiz);
       cdbo = warp_sum_d(cdbo);
       fix = warp_sum_d(fix);
       fiy = warp_sum_d(fiy);
@@ -453,6 +458,7 @@ __global__ void __launch_bounds__(256) k_hbonds(Dev d, int eflag) {
     energy_add(d, ehb, sg, E_HB);
     energy_add(d, ehb, sg, E_ENG_VDWL);
   }
+  if (d.vflag) seg_block_add<6>(w, j < n ? d.seg_s[j] : -1, d.virial, 6);
 }
 
 // ------------------------------------------------------------------
@@ -672,7 +678,7 @@ __global__ void k_vt_fill(Dev d) {
 // per-centre quantities, accumulation in FP64
 template <typename R>
 __device__ __forceinline__ void valence_item(const Dev &d, unsigned long long it, double &e_ang,
-                                             double &e_pen, double &e_coa) {
+                                             double &e_pen, double &e_coa, double *w) {
   {
     const int j = (int)(it >> 16), kk = (int)((it >> 8) & 255), ph = (int)(it & 255);
     const int n = d.n;
@@ -783,6 +789,10 @@ __device__ __forceinline__ void valence_item(const Dev &d, unsigned long long it
       add3(fC, n, k, c8, (double)di[0], (double)di[1], (double)di[2]);
       add3(fC, n, j, c8, (double)dj[0], (double)dj[1], (double)dj[2]);
       add3(fC, n, h, c8, (double)dk[0], (double)dk[1], (double)dk[2]);
+      if (d.vflag) {
+        vir_acc(w, d.b_dx[spk], d.b_dy[spk], d.b_dz[spk], c8 * di[0], c8 * di[1], c8 * di[2]);
+        vir_acc(w, d.b_dx[sph], d.b_dy[sph], d.b_dz[sph], c8 * dk[0], c8 * dk[1], c8 * dk[2]);
+      }
     }
   }
 }
@@ -813,6 +823,7 @@ template <typename R>
 __global__ void __launch_bounds__(128) k_valence(Dev d, int eflag, long long nitems) {
   const long long w = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   double e_ang = 0, e_pen = 0, e_coa = 0;
+  double vw[6] = {0, 0, 0, 0, 0, 0};
   int sg = -1;
   if (w < nitems) {
     const unsigned long long it = d.w_val[w];
@@ -826,12 +837,13 @@ __global__ void __launch_bounds__(128) k_valence(Dev d, int eflag, long long nit
           d.Delta_boc[j] > 1.0 || d.Delta_val[j] > 2.0)
         d.w_fb_val[atomicAdd(&d.fb_cnt[0], 1)] = it;
       else
-        valence_item<R>(d, it, e_ang, e_pen, e_coa);
+        valence_item<R>(d, it, e_ang, e_pen, e_coa, vw);
     } else {
-      valence_item<R>(d, it, e_ang, e_pen, e_coa);
+      valence_item<R>(d, it, e_ang, e_pen, e_coa, vw);
     }
   }
   valence_energies(d, eflag, sg, e_ang, e_pen, e_coa);
+  if (d.vflag) seg_block_add<6>(vw, sg, d.virial, 6);
 }
 
 // the FP64 pass over the queued near-linear angles (grid-stride over the
@@ -841,22 +853,26 @@ __global__ void __launch_bounds__(128) k_valence_fb(Dev d, int eflag) {
   for (long long w = (long long)blockIdx.x * blockDim.x + threadIdx.x; w < cnt;
        w += (long long)gridDim.x * blockDim.x) {
     double e_ang = 0, e_pen = 0, e_coa = 0;
+    double vw[6] = {0, 0, 0, 0, 0, 0};
     const unsigned long long it = d.w_fb_val[w];
-    valence_item<double>(d, it, e_ang, e_pen, e_coa);
+    valence_item<double>(d, it, e_ang, e_pen, e_coa, vw);
+    const int sg = d.seg_s[(int)(it >> 16)];
     if (eflag) {
-      double *E = d.energy + (long long)d.seg_s[(int)(it >> 16)] * RG_NE;
+      double *E = d.energy + (long long)sg * RG_NE;
       atomicAdd(&E[E_ANG], e_ang);
       atomicAdd(&E[E_PEN], e_pen);
       atomicAdd(&E[E_COA], e_coa);
       atomicAdd(&E[E_ENG_VDWL], e_ang + e_pen + e_coa);
     }
+    if (d.vflag)
+      for (int c = 0; c < 6; ++c) atomicAdd(&d.virial[(long long)sg * 6 + c], vw[c]);
   }
 }
 
 // one torsion h-j-k-l (with its 4-body conjugation term); R as in k_valence
 template <typename R>
 __device__ __forceinline__ void torsion_item(const Dev &d, unsigned long long it, double &e_tor,
-                                             double &e_con) {
+                                             double &e_con, double *w) {
   {
     const int j = (int)(it >> 24), kk = (int)((it >> 16) & 255);
     const int ph = (int)((it >> 8) & 255), pw = (int)(it & 255);
@@ -980,6 +996,19 @@ __device__ __forceinline__ void torsion_item(const Dev &d, unsigned long long it
          (double)(c78 * p_ijk.di[2] + c85 * p_jkl.dj[2] + c96 * dok[2]));
     add3(fC, n, l, 1.0, (double)(c85 * p_jkl.dk[0] + c96 * dol[0]), (double)(c85 * p_jkl.dk[1] + c96 * dol[1]),
          (double)(c85 * p_jkl.dk[2] + c96 * dol[2]));
+    if (d.vflag) {
+      // positions relative to j: i = j + d(j->i), k = j + d(j->k), l = k + d(k->l)
+      const double ax = d.b_dx[sph], ay = d.b_dy[sph], az = d.b_dz[sph];
+      const double bx = d.b_dx[spk], by = d.b_dy[spk], bz = d.b_dz[spk];
+      const double lx = bx + d.b_dx[spw], ly = by + d.b_dy[spw], lz = bz + d.b_dz[spw];
+      vir_acc(w, ax, ay, az, (double)(c78 * p_ijk.dk[0] + c96 * doi[0]),
+              (double)(c78 * p_ijk.dk[1] + c96 * doi[1]), (double)(c78 * p_ijk.dk[2] + c96 * doi[2]));
+      vir_acc(w, bx, by, bz, (double)(c78 * p_ijk.di[0] + c85 * p_jkl.dj[0] + c96 * dok[0]),
+              (double)(c78 * p_ijk.di[1] + c85 * p_jkl.dj[1] + c96 * dok[1]),
+              (double)(c78 * p_ijk.di[2] + c85 * p_jkl.dj[2] + c96 * dok[2]));
+      vir_acc(w, lx, ly, lz, (double)(c85 * p_jkl.dk[0] + c96 * dol[0]),
+              (double)(c85 * p_jkl.dk[1] + c96 * dol[1]), (double)(c85 * p_jkl.dk[2] + c96 * dol[2]));
+    }
   }
 }
 
@@ -996,6 +1025,7 @@ template <typename R>
 __global__ void __launch_bounds__(128) k_torsion(Dev d, int eflag, long long nitems) {
   const long long w = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   double e_tor = 0, e_con = 0;
+  double vw[6] = {0, 0, 0, 0, 0, 0};
   int sg = -1;
   if (w < nitems) {
     const unsigned long long it = d.w_tor[w];
@@ -1010,12 +1040,13 @@ __global__ void __launch_bounds__(128) k_torsion(Dev d, int eflag, long long nit
       if (near_linear(d, spk, sph) || near_linear(d, spj, spw))
         d.w_fb_tor[atomicAdd(&d.fb_cnt[1], 1)] = it;
       else
-        torsion_item<R>(d, it, e_tor, e_con);
+        torsion_item<R>(d, it, e_tor, e_con, vw);
     } else {
-      torsion_item<R>(d, it, e_tor, e_con);
+      torsion_item<R>(d, it, e_tor, e_con, vw);
     }
   }
   torsion_energies(d, eflag, sg, e_tor, e_con);
+  if (d.vflag) seg_block_add<6>(vw, sg, d.virial, 6);
 }
 
 __global__ void __launch_bounds__(128) k_torsion_fb(Dev d, int eflag) {
@@ -1023,14 +1054,18 @@ __global__ void __launch_bounds__(128) k_torsion_fb(Dev d, int eflag) {
   for (long long w = (long long)blockIdx.x * blockDim.x + threadIdx.x; w < cnt;
        w += (long long)gridDim.x * blockDim.x) {
     double e_tor = 0, e_con = 0;
+    double vw[6] = {0, 0, 0, 0, 0, 0};
     const unsigned long long it = d.w_fb_tor[w];
-    torsion_item<double>(d, it, e_tor, e_con);
+    torsion_item<double>(d, it, e_tor, e_con, vw);
+    const int sg = d.seg_s[(int)(it >> 24)];
     if (eflag) {
-      double *E = d.energy + (long long)d.seg_s[(int)(it >> 24)] * RG_NE;
+      double *E = d.energy + (long long)sg * RG_NE;
       atomicAdd(&E[E_TOR], e_tor);
       atomicAdd(&E[E_CON], e_con);
       atomicAdd(&E[E_ENG_VDWL], e_tor + e_con);
     }
+    if (d.vflag)
+      for (int c = 0; c < 6; ++c) atomicAdd(&d.virial[(long long)sg * 6 + c], vw[c]);
   }
 }
 
@@ -1040,46 +1075,58 @@ __global__ void __launch_bounds__(128) k_torsion_fb(Dev d, int eflag) {
 __global__ void k_dbond(Dev d) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int n = d.n;
-  if (i >= n) return;
-  const long long S = (long long)d.bond_cap * n;
-  const int nb = min(d.nbonds[i], d.bond_cap);
-  const double *CdD = d.fC + 3 * (long long)n;
-  const double Ddx = d.dDeltap[i], Ddy = d.dDeltap[n + i], Ddz = d.dDeltap[2 * n + i];
-  const double cdi = CdD[i];
-  double fx = 0, fy = 0, fz = 0, buf_c = 0;
-  for (int k = 0; k < nb; ++k) {
-    const long long s = (long long)k * n + i;
-    const int j = nbr_of(d.b_nbr[s]);
-    const long long sy = d.b_sym[s];
-    double cdbo = d.b_Cdbo[s], cdbopi = d.b_Cdbopi[s], cdbopi2 = d.b_Cdbopi2[s];
-    if (sy >= 0) {
-      cdbo += d.b_Cdbo[sy];
-      cdbopi += d.b_Cdbopi[sy];
-      cdbopi2 += d.b_Cdbopi2[sy];
-    }
-    const double C1dbo = d.b_C[0 * S + s], C2dbo = d.b_C[1 * S + s];
-    const double C1pi = d.b_C[3 * S + s], C2pi = d.b_C[4 * S + s], C3pi = d.b_C[5 * S + s];
-    const double C1pi2 = d.b_C[7 * S + s], C2pi2 = d.b_C[8 * S + s], C3pi2 = d.b_C[9 * S + s];
-    const double cdd = cdi + CdD[j];
-    const double a = C1dbo * cdbo + C1dbo * cdd + C2pi * cdbopi + C2pi2 * cdbopi2;  // along dBOp
-    const double b = C2dbo * cdbo + C2dbo * cdd + C3pi * cdbopi + C3pi2 * cdbopi2;  // along dDeltap_i
-    const double cpi = C1pi * cdbopi, cpi2 = C1pi2 * cdbopi2;
-    const double gx = d.b_dBOp[s], gy = d.b_dBOp[S + s], gz = d.b_dBOp[2 * S + s];
-    fx += a * gx + b * Ddx + cpi * d.b_dlnpi[s] + cpi2 * d.b_dlnpi2[s];
-    fy += a * gy + b * Ddy + cpi * d.b_dlnpi[S + s] + cpi2 * d.b_dlnpi2[S + s];
-    fz += a * gz + b * Ddz + cpi * d.b_dlnpi[2 * S + s] + cpi2 * d.b_dlnpi2[2 * S + s];
-    buf_c -= b;
-  }
-  double *fC = d.fC;
-  atomicAdd(&fC[i], fx);
-  atomicAdd(&fC[n + i], fy);
-  atomicAdd(&fC[2 * n + i], fz);
-  if (buf_c != 0.0)
+  // virial: the pieces along a bond i-k that act on i here and on k in k's
+  // pass count half each; the Delta' pieces (on i and on all of i's
+  // neighbours m, both here) count whole
+  double w[6] = {0, 0, 0, 0, 0, 0};
+  if (i < n) {
+    const long long S = (long long)d.bond_cap * n;
+    const int nb = min(d.nbonds[i], d.bond_cap);
+    const double *CdD = d.fC + 3 * (long long)n;
+    const double Ddx = d.dDeltap[i], Ddy = d.dDeltap[n + i], Ddz = d.dDeltap[2 * n + i];
+    const double cdi = CdD[i];
+    double fx = 0, fy = 0, fz = 0, buf_c = 0;
     for (int k = 0; k < nb; ++k) {
       const long long s = (long long)k * n + i;
       const int j = nbr_of(d.b_nbr[s]);
-      add3(fC, n, j, buf_c, d.b_dBOp[s], d.b_dBOp[S + s], d.b_dBOp[2 * S + s]);
+      const long long sy = d.b_sym[s];
+      double cdbo = d.b_Cdbo[s], cdbopi = d.b_Cdbopi[s], cdbopi2 = d.b_Cdbopi2[s];
+      if (sy >= 0) {
+        cdbo += d.b_Cdbo[sy];
+        cdbopi += d.b_Cdbopi[sy];
+        cdbopi2 += d.b_Cdbopi2[sy];
+      }
+      const double C1dbo = d.b_C[0 * S + s], C2dbo = d.b_C[1 * S + s];
+      const double C1pi = d.b_C[3 * S + s], C2pi = d.b_C[4 * S + s], C3pi = d.b_C[5 * S + s];
+      const double C1pi2 = d.b_C[7 * S + s], C2pi2 = d.b_C[8 * S + s], C3pi2 = d.b_C[9 * S + s];
+      const double cdd = cdi + CdD[j];
+      const double a = C1dbo * cdbo + C1dbo * cdd + C2pi * cdbopi + C2pi2 * cdbopi2;  // along dBOp
+      const double b = C2dbo * cdbo + C2dbo * cdd + C3pi * cdbopi + C3pi2 * cdbopi2;  // along dDeltap_i
+      const double cpi = C1pi * cdbopi, cpi2 = C1pi2 * cdbopi2;
+      const double gx = d.b_dBOp[s], gy = d.b_dBOp[S + s], gz = d.b_dBOp[2 * S + s];
+      const double px = a * gx + cpi * d.b_dlnpi[s] + cpi2 * d.b_dlnpi2[s];
+      const double py = a * gy + cpi * d.b_dlnpi[S + s] + cpi2 * d.b_dlnpi2[S + s];
+      const double pz = a * gz + cpi * d.b_dlnpi[2 * S + s] + cpi2 * d.b_dlnpi2[2 * S + s];
+      fx += px + b * Ddx;
+      fy += py + b * Ddy;
+      fz += pz + b * Ddz;
+      buf_c -= b;
+      if (d.vflag) vir_acc(w, d.b_dx[s], d.b_dy[s], d.b_dz[s], -0.5 * px, -0.5 * py, -0.5 * pz);
     }
+    double *fC = d.fC;
+    atomicAdd(&fC[i], fx);
+    atomicAdd(&fC[n + i], fy);
+    atomicAdd(&fC[2 * n + i], fz);
+    if (buf_c != 0.0)
+      for (int k = 0; k < nb; ++k) {
+        const long long s = (long long)k * n + i;
+        const int j = nbr_of(d.b_nbr[s]);
+        const double gx = d.b_dBOp[s], gy = d.b_dBOp[S + s], gz = d.b_dBOp[2 * S + s];
+        add3(fC, n, j, buf_c, gx, gy, gz);
+        if (d.vflag) vir_acc(w, d.b_dx[s], d.b_dy[s], d.b_dz[s], buf_c * gx, buf_c * gy, buf_c * gz);
+      }
+  }
+  if (d.vflag) seg_block_add<6>(w, i < n ? d.seg_s[i] : -1, d.virial, 6);
 }
 
 // forces back to the original atom order: f = -dE/dx

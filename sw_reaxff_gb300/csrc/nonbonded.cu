@@ -198,6 +198,7 @@ __global__ void __launch_bounds__(NBW * 32) k_nonbonded(Dev d, int eflag) {
   const int lane = threadIdx.x & 31;
   const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   double evdw = 0.0, eele = 0.0;
+  double w[6] = {0, 0, 0, 0, 0, 0};
   if (i < d.n) {
     PairQueue &Q = queues[threadIdx.x >> 5];
     const ForceField &F = *d.ff;
@@ -247,6 +248,7 @@ __global__ void __launch_bounds__(NBW * 32) k_nonbonded(Dev d, int eflag) {
           atomicAdd(&fC[j], c * dx);
           atomicAdd(&fC[n + j], c * dy);
           atomicAdd(&fC[2 * n + j], c * dz);
+          if (d.vflag) vir_acc(w, dx, dy, dz, c * dx, c * dy, c * dz);
         }
         __syncwarp();
         const int left = qn - cnt;
@@ -275,6 +277,7 @@ __global__ void __launch_bounds__(NBW * 32) k_nonbonded(Dev d, int eflag) {
     seg_block_add<1>(v + 2, sg, d.energy + E_ENG_VDWL, RG_NE);
     seg_block_add<1>(v + 3, sg, d.energy + E_ENG_COUL, RG_NE);
   }
+  if (d.vflag) seg_block_add<6>(w, i < d.n ? d.seg_s[i] : -1, d.virial, 6);
 }
 
 }  // namespace

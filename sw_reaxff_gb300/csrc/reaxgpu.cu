@@ -217,6 +217,7 @@ int alloc_segs(rg_system *h) {
   d.seg = sg;
   r |= dalloc(h, h->per_seg, &d.red, (size_t)cap * RG_NRED);
   r |= dalloc(h, h->per_seg, &d.energy, (size_t)cap * RG_NE);
+  r |= dalloc(h, h->per_seg, &d.virial, (size_t)cap * 6);
   r |= dalloc(h, h->per_seg, &d.n_active, 1);
   if (r) return RG_E_CUDA;
   h->nseg_alloc = cap;
@@ -426,12 +427,14 @@ int build_lists(rg_system *h) {
   return 0;
 }
 
-int do_compute(rg_system *h, int eflag) {
+int do_compute(rg_system *h, int eflag, int vflag = 0) {
   Dev &d = h->d;
   int rc;
   if (!h->lists_valid && (rc = build_lists(h))) return rc;
   CK(cudaMemsetAsync(d.fC, 0, 4 * sizeof(double) * (size_t)d.n, h->st));
   CK(cudaMemsetAsync(d.energy, 0, (size_t)d.nseg * RG_NE * sizeof(double), h->st));
+  d.vflag = vflag ? 1 : 0;
+  if (vflag) CK(cudaMemsetAsync(d.virial, 0, (size_t)d.nseg * 6 * sizeof(double), h->st));
   if (d.debug) CK(cudaMemsetAsync(d.dbg_flag, 0, sizeof(int), h->st));
   auto finite_after = [&](const char *phase) -> int {
     if (!h->check_finite) return 0;
@@ -895,6 +898,14 @@ int rg_get_energies(rg_system *h, double *e) {
   return RG_OK;
 }
 
+int rg_get_virial(rg_system *h, double *v) {
+  if (!h || !v) return RG_E_ARG;
+  if (!h->n) return fail(h, RG_E_STATE, "no atoms set");
+  CK(cudaMemcpyAsync(v, h->d.virial, sizeof(double) * 6 * h->d.nseg, cudaMemcpyDeviceToHost, h->st));
+  CK(cudaStreamSynchronize(h->st));
+  return RG_OK;
+}
+
 int rg_get_segment_iters(rg_system *h, int *iters) {
   if (!h || !iters) return RG_E_ARG;
   for (size_t k = 0; k < h->seg_iters.size(); ++k) iters[k] = h->seg_iters[k];
@@ -983,11 +994,10 @@ int rg_qeq(rg_system *h, double *q_out, int *iters_s, int *iters_t) {
 }
 
 int rg_compute(rg_system *h, int eflag, int vflag, double *f_out, double *energies) {
-  (void)vflag;
   if (!h) return RG_E_ARG;
   if (!h->n) return fail(h, RG_E_STATE, "no atoms set");
   CK(cudaSetDevice(h->p.device));
-  int rc = do_compute(h, eflag || energies != nullptr);
+  int rc = do_compute(h, eflag || energies != nullptr, vflag);
   if (rc) return rc;
   if (f_out) CK(cudaMemcpyAsync(f_out, h->d.f_o, 3 * sizeof(double) * h->n, cudaMemcpyDeviceToHost, h->st));
   if (energies && (rc = energy_sum(h, energies))) return rc;

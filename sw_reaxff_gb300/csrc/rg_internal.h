@@ -186,6 +186,8 @@ struct Dev {
   double *Hdia_inv;
   double *red;        // device scalars / reduction accumulators, RG_NRED per segment
   double *energy;     // [nseg][RG_NE]
+  double *virial;     // [nseg][6]: xx yy zz xy xz yz of sum r (x) f (LAMMPS order)
+  int vflag;          // accumulate the virial in this force step
   int *n_active;      // QEq: segments with an active solve (host poll)
 
   // valence / torsion work lists (built per force step)
@@ -269,6 +271,21 @@ __device__ __forceinline__ void seg_block_add(const double *vin, int seg, double
       }
     }
   }
+}
+
+// virial of one term: w -= d (x) g for an atom at displacement d from the
+// term's reference atom receiving the energy gradient g (forces are -g; the
+// gradients of a term sum to zero, so W = sum_atoms r (x) f needs only the
+// displacements within the term, never the periodic images' absolute
+// positions)
+__device__ __forceinline__ void vir_acc(double *w, double dx, double dy, double dz, double gx,
+                                        double gy, double gz) {
+  w[0] -= dx * gx;
+  w[1] -= dy * gy;
+  w[2] -= dz * gz;
+  w[3] -= dx * gy;
+  w[4] -= dx * gz;
+  w[5] -= dy * gz;
 }
 
 // x + s L with the reference's rounding; the image-free case (most pairs)

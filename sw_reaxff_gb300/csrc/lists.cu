@@ -220,9 +220,8 @@ __device__ __forceinline__ void nbr_flush(const Dev &d, const Control &C, const 
       d2 = exact_d2(d, j, sx, sy, sz, xi, L);
       in = d2 <= C.list_cut2;
       if (in) {
-        const double nc2 = C.near_cut * C.near_cut;
-        if (d2 <= nc2 * (1.0 - 1e-12)) near = true;
-        else if (d2 > nc2 * (1.0 + 1e-12)) near = false;
+        if (d2 <= C.near_cut2_lo) near = true;
+        else if (d2 > C.near_cut2_hi) near = false;
         else near = __dsqrt_rn(d2) <= C.near_cut;
       }
     }
@@ -546,11 +545,11 @@ __global__ void __launch_bounds__(NB_WARPS * 32) k_build_bonds(Dev d) {
           const float ey = df_disp(xjf.y, lj.y, xif.y, xil.y, sy, g.Lh[1], g.Ll[1]);
           const float ez = df_disp(xjf.z, lj.z, xif.z, xil.z, sz, g.Lh[2], g.Ll[2]);
           const float df = sqrtf(ex * ex + ey * ey + ez * ez);
-          const float bc = (float)C.bond_cut, hc = (float)C.hbond_cut;
+          const float bc = C.bond_cut_f, hc = C.hbond_cut_f;
           const bool near_b = fabsf(df - bc) <= MARGIN32 * bc;
           const bool near_h = hb_rel && fabsf(df - hc) <= MARGIN32 * hc;
           const bool exact = MIXED ? (near_b || near_h) : (df <= bc * (1.f + MARGIN32) || near_h);
-          dx = ex; dy = ey; dz = ez; dist = df;
+          bool isb;
           if (exact) {
             const double4 xj = d.xs[j];
             dx = __dsub_rn(img_shift(xj.x, sx, L[0]), xi.x);
@@ -558,9 +557,15 @@ __global__ void __launch_bounds__(NB_WARPS * 32) k_build_bonds(Dev d) {
             dz = __dsub_rn(img_shift(xj.z, sz, L[2]), xi.z);
             const double d2 = __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
             dist = __dsqrt_rn(d2);
+            ish = hb_rel && dist <= C.hbond_cut;
+            isb = dist <= C.bond_cut;
+          } else {
+            // decided in FP32; values kept only for the (mixed-form) bonds
+            ish = hb_rel && df <= hc;
+            isb = df <= bc;
+            if (isb) { dx = ex; dy = ey; dz = ez; dist = df; }
           }
-          if (hb_rel && dist <= C.hbond_cut) ish = true;
-          if (dist <= C.bond_cut) {
+          if (isb) {
             const Tbp &tw = F.tbp[ti][tj];
             const float dd = (float)dist;
             float est = 0.f;

@@ -54,22 +54,45 @@ __global__ void k_qeq_setup(Dev d) {
   d.qx[s] = make_double2(s0, t0);
 }
 
-// y = H x (+ eta x on the diagonal), one warp per row; FP64 form
-__global__ void __launch_bounds__(256) k_spmv(Dev d, const double2 *__restrict__ x, double2 *__restrict__ y) {
+// y = H x (+ eta x on the diagonal), one warp per row; FP64 form.  In the
+// CG iterations (use_act) a system whose solve has converged is skipped:
+// its half of y is not read again
+__global__ void __launch_bounds__(256) k_spmv(Dev d, const double2 *__restrict__ x, double2 *__restrict__ y,
+                                              int use_act) {
   const int lane = threadIdx.x & 31;
   const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   if (i >= d.n) return;
   const long long row = (long long)i * d.nb_cap;
   const int nn = d.n_near[i], nf = d.n_far[i], cap = d.nb_cap;
   const int tot = min(nn + nf, cap);
+  bool on_s = true, on_t = true;
+  if (use_act) {
+    const double *R = d.red + (long long)d.seg_s[i] * RG_NRED;
+    on_s = R[R_ACTIVE] != 0.0;
+    on_t = R[R_ACTIVE + 1] != 0.0;
+  }
   double as = 0.0, at = 0.0;
-  for (int p = lane; p < tot; p += 32) {
-    const int slot = p < nn ? p : cap - 1 - (p - nn);
-    const uint32_t e = d.nbr[row + slot];
-    const double h = d.hval[row + slot];
-    const double2 xj = x[e >> 8];
-    as = fma(h, xj.x, as);
-    at = fma(h, xj.y, at);
+  if (on_s && on_t) {
+    for (int p = lane; p < tot; p += 32) {
+      const int slot = p < nn ? p : cap - 1 - (p - nn);
+      const uint32_t e = d.nbr[row + slot];
+      const double h = d.hval[row + slot];
+      const double2 xj = x[e >> 8];
+      as = fma(h, xj.x, as);
+      at = fma(h, xj.y, at);
+    }
+  } else if (on_s || on_t) {
+    for (int p = lane; p < tot; p += 32) {
+      const int slot = p < nn ? p : cap - 1 - (p - nn);
+      const uint32_t e = d.nbr[row + slot];
+      const double h = d.hval[row + slot];
+      const double2 xj = x[e >> 8];
+      as = fma(h, on_s ? xj.x : xj.y, as);
+    }
+    if (on_t) {
+      at = as;
+      as = 0.0;
+    }
   }
   as = warp_sum(as);
   at = warp_sum(at);
@@ -118,7 +141,8 @@ __device__ __forceinline__ float4 split4(double2 v) {
   return make_float4(sh, __double2float_rn(v.x - (double)sh), th, __double2float_rn(v.y - (double)th));
 }
 
-__global__ void __launch_bounds__(256) k_spmv32(Dev d, const double2 *__restrict__ x, double2 *__restrict__ y) {
+__global__ void __launch_bounds__(256) k_spmv32(Dev d, const double2 *__restrict__ x, double2 *__restrict__ y,
+                                                int use_act) {
   const int lane = threadIdx.x & 31;
   const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   if (i >= d.n) return;
@@ -126,14 +150,36 @@ __global__ void __launch_bounds__(256) k_spmv32(Dev d, const double2 *__restrict
   const int nn = d.n_near[i], nf = d.n_far[i], cap = d.nb_cap;
   const int tot = min(nn + nf, cap);
   const float4 *__restrict__ x32 = d.qd32;
+  bool on_s = true, on_t = true;
+  if (use_act) {
+    const double *R = d.red + (long long)d.seg_s[i] * RG_NRED;
+    on_s = R[R_ACTIVE] != 0.0;
+    on_t = R[R_ACTIVE + 1] != 0.0;
+  }
   float sh = 0.f, sl = 0.f, th = 0.f, tl = 0.f;
-  for (int p = lane; p < tot; p += 32) {
-    const int slot = p < nn ? p : cap - 1 - (p - nn);
-    const uint32_t e = d.nbr[row + slot];
-    const float h = d.hval32[row + slot];
-    const float4 xj = x32[e >> 8];
-    df_fma(h, xj.x, xj.y, sh, sl);
-    df_fma(h, xj.z, xj.w, th, tl);
+  if (on_s && on_t) {
+    for (int p = lane; p < tot; p += 32) {
+      const int slot = p < nn ? p : cap - 1 - (p - nn);
+      const uint32_t e = d.nbr[row + slot];
+      const float h = d.hval32[row + slot];
+      const float4 xj = x32[e >> 8];
+      df_fma(h, xj.x, xj.y, sh, sl);
+      df_fma(h, xj.z, xj.w, th, tl);
+    }
+  } else if (on_s) {
+    for (int p = lane; p < tot; p += 32) {
+      const int slot = p < nn ? p : cap - 1 - (p - nn);
+      const float h = d.hval32[row + slot];
+      const float4 xj = x32[d.nbr[row + slot] >> 8];
+      df_fma(h, xj.x, xj.y, sh, sl);
+    }
+  } else if (on_t) {
+    for (int p = lane; p < tot; p += 32) {
+      const int slot = p < nn ? p : cap - 1 - (p - nn);
+      const float h = d.hval32[row + slot];
+      const float4 xj = x32[d.nbr[row + slot] >> 8];
+      df_fma(h, xj.z, xj.w, th, tl);
+    }
   }
   for (int off = 16; off > 0; off >>= 1) {
     const float a = __shfl_down_sync(FULL, sh, off), b = __shfl_down_sync(FULL, sl, off);
@@ -379,11 +425,11 @@ void launch_qeq_setup(const Dev &d, cudaStream_t st) {
 
 // the mixed form's FP32 SpMV reads the split copy of qd; any other vector
 // goes through the FP64-sum kernel
-void launch_qeq_spmv(const Dev &d, cudaStream_t st, const double2 *x, double2 *y) {
+void launch_qeq_spmv(const Dev &d, cudaStream_t st, const double2 *x, double2 *y, int use_act) {
   const long long threads = (long long)d.n * 32;
   const unsigned G = (unsigned)((threads + 255) / 256);
-  if (!d.mixed) k_spmv<<<G, 256, 0, st>>>(d, x, y);
-  else if (x == d.qd) k_spmv32<<<G, 256, 0, st>>>(d, x, y);
+  if (!d.mixed) k_spmv<<<G, 256, 0, st>>>(d, x, y, use_act);
+  else if (x == d.qd) k_spmv32<<<G, 256, 0, st>>>(d, x, y, use_act);
   else k_spmv_ref<<<G, 256, 0, st>>>(d, x, y);
 }
 
@@ -396,12 +442,12 @@ void launch_qeq_cg_init(const Dev &d, cudaStream_t st, double tol, int imax) {
     const long long threads = (long long)d.n * 32;
     k_spmv_ref<<<(unsigned)((threads + 255) / 256), 256, 0, st>>>(d, d.qx, d.qq);
   } else {
-    launch_qeq_spmv(d, st, d.qx, d.qq);
+    launch_qeq_spmv(d, st, d.qx, d.qq, 0);
   }
   k_cg_init1<<<G, B, 0, st>>>(d);
-  launch_qeq_spmv(d, st, d.qd, d.qq);
+  launch_qeq_spmv(d, st, d.qd, d.qq, 0);
   k_cg_init2<<<G, B, 0, st>>>(d);
-  launch_qeq_spmv(d, st, d.qd, d.qq);
+  launch_qeq_spmv(d, st, d.qd, d.qq, 0);
   k_seg_zero<<<GS, 128, 0, st>>>(d, R_INIT, 6);
   k_cg_init3<<<G, B, 0, st>>>(d);
   cudaMemsetAsync(d.n_active, 0, sizeof(int), st);

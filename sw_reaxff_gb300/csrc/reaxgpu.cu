@@ -504,7 +504,7 @@ int capture_cg(rg_system *h, int chunk) {
   CK(cudaStreamBeginCapture(h->st, cudaStreamCaptureModeThreadLocal));
   for (int k = 0; k < chunk; ++k) {
     launch_qeq_cg_A(d, h->st);
-    launch_qeq_spmv(d, h->st, d.qd, d.qq);
+    launch_qeq_spmv(d, h->st, d.qd, d.qq, 1);
     launch_qeq_cg_C(d, h->st);
   }
   cudaError_t e = cudaStreamEndCapture(h->st, &g);
@@ -557,7 +557,7 @@ int do_qeq(rg_system *h, int *its, int *itt) {
       } else {
         for (int k = 0; k < chunk; ++k) {
           { Scope sc(h, PH_QVEC, 1); launch_qeq_cg_A(d, h->st); }
-          { Scope sc(h, PH_QSPMV, 1); launch_qeq_spmv(d, h->st, d.qd, d.qq); }
+          { Scope sc(h, PH_QSPMV, 1); launch_qeq_spmv(d, h->st, d.qd, d.qq, 1); }
           { Scope sc(h, PH_QVEC, 3); launch_qeq_cg_C(d, h->st); }
         }
       }
@@ -610,6 +610,10 @@ void init_control(const rg_params &p, const ForceField &ff, Control &c) {
   c.nonb_cut2 = c.nonb_cut * c.nonb_cut;
   c.swb2 = p.qeq_swb * p.qeq_swb;
   c.near_cut = std::max(c.bond_cut, c.hbond_cut);
+  c.near_cut2_lo = c.near_cut * c.near_cut * (1.0 - 1e-12);
+  c.near_cut2_hi = c.near_cut * c.near_cut * (1.0 + 1e-12);
+  c.bond_cut_f = (float)c.bond_cut;
+  c.hbond_cut_f = (float)c.hbond_cut;
   rg_init_taper(c.nonb_low, c.nonb_cut, c.Tap);
   rg_init_taper(p.qeq_swa, p.qeq_swb, c.qTap);
   c.tap_factored = (c.nonb_low == 0.0);

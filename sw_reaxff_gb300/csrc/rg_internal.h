@@ -87,6 +87,8 @@ struct Control {
   double list_cut2;   // squared pair-list cutoff max(nonb_cut, qeq_swb)^2
   double nonb_cut2, swb2;
   double near_cut;    // max(bond_cut, hbond_cut): "near" part of a row
+  double near_cut2_lo, near_cut2_hi;   // near_cut^2 (1 -/+ 1e-12)
+  float bond_cut_f, hbond_cut_f;        // FP32 copies for FP32-first tests
   double Tap[8];      // pair taper (swa = nonb_low, swb = nonb_cut)
   double qTap[8];     // QEq taper
   int enobondsflag, lgflag;
@@ -365,7 +367,7 @@ void launch_check_finite(const double *a, long long count, int *flag, cudaStream
 
 // QEq
 void launch_qeq_setup(const Dev &d, cudaStream_t st);
-void launch_qeq_spmv(const Dev &d, cudaStream_t st, const double2 *x, double2 *y);
+void launch_qeq_spmv(const Dev &d, cudaStream_t st, const double2 *x, double2 *y, int use_act);
 void launch_qeq_cg_init(const Dev &d, cudaStream_t st, double tol, int imax);
 void launch_qeq_cg_A(const Dev &d, cudaStream_t st);
 void launch_qeq_cg_C(const Dev &d, cudaStream_t st);

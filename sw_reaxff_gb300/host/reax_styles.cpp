@@ -251,6 +251,7 @@ void PairReaxCGB300::compute(int eflag, int vflag) {
     eng_vdwl = e[14];
     eng_coul = e[15];
   }
+  if (vflag) check(rg_get_virial(h, virial), "rg_get_virial");
 }
 
 void *PairReaxCGB300::extract(const char *str, int &dim) {

@@ -366,7 +366,7 @@ __device__ __forceinline__ double warp_sum_d(double v) {
 // R = double: FP64 form; R = float (mixed form): the angle, the exponentials
 // and the force factors in FP32 from the FP64 displacement and bond order;
 // accumulation in FP64
-template <typename R>
+template <typename R, bool VIR>
 __global__ void __launch_bounds__(256) k_hbonds(Dev d, int eflag) {
   const int lane = threadIdx.x & 31;
   const int j = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -434,11 +434,11 @@ __global__ void __launch_bounds__(256) k_hbonds(Dev d, int eflag) {
         fjz += (double)(CEhb2 * djv[2] - c3 * djk[2]);
         add3(fC, n, k, 1.0, (double)(CEhb2 * dk[0] + c3 * djk[0]), (double)(CEhb2 * dk[1] + c3 * djk[1]),
              (double)(CEhb2 * dk[2] + c3 * djk[2]));
-        if (d.vflag)
+        if (VIR)
           vir_acc(w, dk64[0], dk64[1], dk64[2], (double)(CEhb2 * dk[0] + c3 * djk[0]),
                   (double)(CEhb2 * dk[1] + c3 * djk[1]), (double)(CEhb2 * dk[2] + c3 * djk[2]));
       }
-      if (d.vflag) vir_acc(w, d.b_dx[s], d.b_dy[s], d.b_dz[s], fix, fiy, fiz);
+      if (VIR) vir_acc(w, d.b_dx[s], d.b_dy[s], d.b_dz[s], fix, fiy, fiz);
       cdbo = warp_sum_d(cdbo);
       fix = warp_sum_d(fix);
       fiy = warp_sum_d(fiy);
@@ -458,7 +458,7 @@ __global__ void __launch_bounds__(256) k_hbonds(Dev d, int eflag) {
     energy_add(d, ehb, sg, E_HB);
     energy_add(d, ehb, sg, E_ENG_VDWL);
   }
-  if (d.vflag) seg_block_add<6>(w, j < n ? d.seg_s[j] : -1, d.virial, 6);
+  if (VIR) seg_block_add<6>(w, j < n ? d.seg_s[j] : -1, d.virial, 6);
 }
 
 // ------------------------------------------------------------------
@@ -676,7 +676,7 @@ __global__ void k_vt_fill(Dev d) {
 // one valence angle h-j-k (with its penalty and coalition terms); R as in
 // k_hbonds: the per-angle arithmetic in R from the FP64 per-bond and
 // per-centre quantities, accumulation in FP64
-template <typename R>
+template <typename R, bool VIR>
 __device__ __forceinline__ void valence_item(const Dev &d, unsigned long long it, double &e_ang,
                                              double &e_pen, double &e_coa, double *w) {
   {
@@ -789,7 +789,7 @@ __device__ __forceinline__ void valence_item(const Dev &d, unsigned long long it
       add3(fC, n, k, c8, (double)di[0], (double)di[1], (double)di[2]);
       add3(fC, n, j, c8, (double)dj[0], (double)dj[1], (double)dj[2]);
       add3(fC, n, h, c8, (double)dk[0], (double)dk[1], (double)dk[2]);
-      if (d.vflag) {
+      if (VIR) {
         vir_acc(w, d.b_dx[spk], d.b_dy[spk], d.b_dz[spk], c8 * di[0], c8 * di[1], c8 * di[2]);
         vir_acc(w, d.b_dx[sph], d.b_dy[sph], d.b_dz[sph], c8 * dk[0], c8 * dk[1], c8 * dk[2]);
       }
@@ -819,7 +819,7 @@ __device__ __forceinline__ void valence_energies(const Dev &d, int eflag, int sg
   }
 }
 
-template <typename R>
+template <typename R, bool VIR>
 __global__ void __launch_bounds__(128) k_valence(Dev d, int eflag, long long nitems) {
   const long long w = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   double e_ang = 0, e_pen = 0, e_coa = 0;
@@ -837,17 +837,18 @@ __global__ void __launch_bounds__(128) k_valence(Dev d, int eflag, long long nit
           d.Delta_boc[j] > 1.0 || d.Delta_val[j] > 2.0)
         d.w_fb_val[atomicAdd(&d.fb_cnt[0], 1)] = it;
       else
-        valence_item<R>(d, it, e_ang, e_pen, e_coa, vw);
+        valence_item<R, VIR>(d, it, e_ang, e_pen, e_coa, vw);
     } else {
-      valence_item<R>(d, it, e_ang, e_pen, e_coa, vw);
+      valence_item<R, VIR>(d, it, e_ang, e_pen, e_coa, vw);
     }
   }
   valence_energies(d, eflag, sg, e_ang, e_pen, e_coa);
-  if (d.vflag) seg_block_add<6>(vw, sg, d.virial, 6);
+  if (VIR) seg_block_add<6>(vw, sg, d.virial, 6);
 }
 
 // the FP64 pass over the queued near-linear angles (grid-stride over the
 // device-side count; few items, so energies go straight to their segment)
+template <bool VIR>
 __global__ void __launch_bounds__(128) k_valence_fb(Dev d, int eflag) {
   const long long cnt = d.fb_cnt[0];
   for (long long w = (long long)blockIdx.x * blockDim.x + threadIdx.x; w < cnt;
@@ -855,7 +856,7 @@ __global__ void __launch_bounds__(128) k_valence_fb(Dev d, int eflag) {
     double e_ang = 0, e_pen = 0, e_coa = 0;
     double vw[6] = {0, 0, 0, 0, 0, 0};
     const unsigned long long it = d.w_fb_val[w];
-    valence_item<double>(d, it, e_ang, e_pen, e_coa, vw);
+    valence_item<double, VIR>(d, it, e_ang, e_pen, e_coa, vw);
     const int sg = d.seg_s[(int)(it >> 16)];
     if (eflag) {
       double *E = d.energy + (long long)sg * RG_NE;
@@ -864,13 +865,13 @@ __global__ void __launch_bounds__(128) k_valence_fb(Dev d, int eflag) {
       atomicAdd(&E[E_COA], e_coa);
       atomicAdd(&E[E_ENG_VDWL], e_ang + e_pen + e_coa);
     }
-    if (d.vflag)
+    if (VIR)
       for (int c = 0; c < 6; ++c) atomicAdd(&d.virial[(long long)sg * 6 + c], vw[c]);
   }
 }
 
 // one torsion h-j-k-l (with its 4-body conjugation term); R as in k_valence
-template <typename R>
+template <typename R, bool VIR>
 __device__ __forceinline__ void torsion_item(const Dev &d, unsigned long long it, double &e_tor,
                                              double &e_con, double *w) {
   {
@@ -996,7 +997,7 @@ __device__ __forceinline__ void torsion_item(const Dev &d, unsigned long long it
          (double)(c78 * p_ijk.di[2] + c85 * p_jkl.dj[2] + c96 * dok[2]));
     add3(fC, n, l, 1.0, (double)(c85 * p_jkl.dk[0] + c96 * dol[0]), (double)(c85 * p_jkl.dk[1] + c96 * dol[1]),
          (double)(c85 * p_jkl.dk[2] + c96 * dol[2]));
-    if (d.vflag) {
+    if (VIR) {
       // positions relative to j: i = j + d(j->i), k = j + d(j->k), l = k + d(k->l)
       const double ax = d.b_dx[sph], ay = d.b_dy[sph], az = d.b_dz[sph];
       const double bx = d.b_dx[spk], by = d.b_dy[spk], bz = d.b_dz[spk];
@@ -1021,7 +1022,7 @@ __device__ __forceinline__ void torsion_energies(const Dev &d, int eflag, int sg
   }
 }
 
-template <typename R>
+template <typename R, bool VIR>
 __global__ void __launch_bounds__(128) k_torsion(Dev d, int eflag, long long nitems) {
   const long long w = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   double e_tor = 0, e_con = 0;
@@ -1040,15 +1041,16 @@ __global__ void __launch_bounds__(128) k_torsion(Dev d, int eflag, long long nit
       if (near_linear(d, spk, sph) || near_linear(d, spj, spw))
         d.w_fb_tor[atomicAdd(&d.fb_cnt[1], 1)] = it;
       else
-        torsion_item<R>(d, it, e_tor, e_con, vw);
+        torsion_item<R, VIR>(d, it, e_tor, e_con, vw);
     } else {
-      torsion_item<R>(d, it, e_tor, e_con, vw);
+      torsion_item<R, VIR>(d, it, e_tor, e_con, vw);
     }
   }
   torsion_energies(d, eflag, sg, e_tor, e_con);
-  if (d.vflag) seg_block_add<6>(vw, sg, d.virial, 6);
+  if (VIR) seg_block_add<6>(vw, sg, d.virial, 6);
 }
 
+template <bool VIR>
 __global__ void __launch_bounds__(128) k_torsion_fb(Dev d, int eflag) {
   const long long cnt = d.fb_cnt[1];
   for (long long w = (long long)blockIdx.x * blockDim.x + threadIdx.x; w < cnt;
@@ -1056,7 +1058,7 @@ __global__ void __launch_bounds__(128) k_torsion_fb(Dev d, int eflag) {
     double e_tor = 0, e_con = 0;
     double vw[6] = {0, 0, 0, 0, 0, 0};
     const unsigned long long it = d.w_fb_tor[w];
-    torsion_item<double>(d, it, e_tor, e_con, vw);
+    torsion_item<double, VIR>(d, it, e_tor, e_con, vw);
     const int sg = d.seg_s[(int)(it >> 24)];
     if (eflag) {
       double *E = d.energy + (long long)sg * RG_NE;
@@ -1064,7 +1066,7 @@ __global__ void __launch_bounds__(128) k_torsion_fb(Dev d, int eflag) {
       atomicAdd(&E[E_CON], e_con);
       atomicAdd(&E[E_ENG_VDWL], e_tor + e_con);
     }
-    if (d.vflag)
+    if (VIR)
       for (int c = 0; c < 6; ++c) atomicAdd(&d.virial[(long long)sg * 6 + c], vw[c]);
   }
 }
@@ -1072,6 +1074,7 @@ __global__ void __launch_bounds__(128) k_torsion_fb(Dev d, int eflag) {
 // ------------------------------------------------------------------
 // bond-order derivative forces: one thread per atom i over its bonds
 
+template <bool VIR>
 __global__ void k_dbond(Dev d) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int n = d.n;
@@ -1111,7 +1114,7 @@ __global__ void k_dbond(Dev d) {
       fy += py + b * Ddy;
       fz += pz + b * Ddz;
       buf_c -= b;
-      if (d.vflag) vir_acc(w, d.b_dx[s], d.b_dy[s], d.b_dz[s], -0.5 * px, -0.5 * py, -0.5 * pz);
+      if (VIR) vir_acc(w, d.b_dx[s], d.b_dy[s], d.b_dz[s], -0.5 * px, -0.5 * py, -0.5 * pz);
     }
     double *fC = d.fC;
     atomicAdd(&fC[i], fx);
@@ -1123,10 +1126,10 @@ __global__ void k_dbond(Dev d) {
         const int j = nbr_of(d.b_nbr[s]);
         const double gx = d.b_dBOp[s], gy = d.b_dBOp[S + s], gz = d.b_dBOp[2 * S + s];
         add3(fC, n, j, buf_c, gx, gy, gz);
-        if (d.vflag) vir_acc(w, d.b_dx[s], d.b_dy[s], d.b_dz[s], buf_c * gx, buf_c * gy, buf_c * gz);
+        if (VIR) vir_acc(w, d.b_dx[s], d.b_dy[s], d.b_dz[s], buf_c * gx, buf_c * gy, buf_c * gz);
       }
   }
-  if (d.vflag) seg_block_add<6>(w, i < n ? d.seg_s[i] : -1, d.virial, 6);
+  if (VIR) seg_block_add<6>(w, i < n ? d.seg_s[i] : -1, d.virial, 6);
 }
 
 // forces back to the original atom order: f = -dE/dx
@@ -1171,8 +1174,13 @@ void launch_atom_energy(const Dev &d, cudaStream_t st, int eflag) {
 void launch_hbonds(const Dev &d, cudaStream_t st, int eflag) {
   const long long threads = (long long)d.n * 32;
   const unsigned G = (unsigned)((threads + 255) / 256);
-  if (d.mixed) k_hbonds<float><<<G, 256, 0, st>>>(d, eflag);
-  else k_hbonds<double><<<G, 256, 0, st>>>(d, eflag);
+  if (d.vflag) {
+    if (d.mixed) k_hbonds<float, true><<<G, 256, 0, st>>>(d, eflag);
+    else k_hbonds<double, true><<<G, 256, 0, st>>>(d, eflag);
+  } else {
+    if (d.mixed) k_hbonds<float, false><<<G, 256, 0, st>>>(d, eflag);
+    else k_hbonds<double, false><<<G, 256, 0, st>>>(d, eflag);
+  }
 }
 
 void launch_vt_count(const Dev &d, cudaStream_t st) {
@@ -1185,27 +1193,35 @@ void launch_vt_count(const Dev &d, cudaStream_t st) {
   launch_scan(d.w_cnt_t, d.w_off_t, (int)(slots + 1), d.w_bsum, st);
 }
 
+template <bool VIR>
+static void vt_kernels(const Dev &d, cudaStream_t st, int eflag, long long nval, long long ntor,
+                       unsigned gv, unsigned gt) {
+  if (d.mixed) {
+    cudaMemsetAsync(d.fb_cnt, 0, 2 * sizeof(int), st);
+    if (nval > 0) k_valence<float, VIR><<<gv, 128, 0, st>>>(d, eflag, nval);
+    if (ntor > 0) k_torsion<float, VIR><<<gt, 128, 0, st>>>(d, eflag, ntor);
+    // FP64 passes over the near-linear items (count read on the device)
+    k_valence_fb<VIR><<<152 * 2, 128, 0, st>>>(d, eflag);
+    k_torsion_fb<VIR><<<152 * 2, 128, 0, st>>>(d, eflag);
+  } else {
+    if (nval > 0) k_valence<double, VIR><<<gv, 128, 0, st>>>(d, eflag, nval);
+    if (ntor > 0) k_torsion<double, VIR><<<gt, 128, 0, st>>>(d, eflag, ntor);
+  }
+}
+
 void launch_vt_run(const Dev &d, cudaStream_t st, int eflag, long long nval, long long ntor) {
   const int B = 256;
   const long long slots = (long long)d.n * d.bond_cap;
   k_vt_fill<<<(unsigned)((slots + B - 1) / B), B, 0, st>>>(d);
   const unsigned gv = (unsigned)((nval + 127) / 128), gt = (unsigned)((ntor + 127) / 128);
-  if (d.mixed) {
-    cudaMemsetAsync(d.fb_cnt, 0, 2 * sizeof(int), st);
-    if (nval > 0) k_valence<float><<<gv, 128, 0, st>>>(d, eflag, nval);
-    if (ntor > 0) k_torsion<float><<<gt, 128, 0, st>>>(d, eflag, ntor);
-    // FP64 passes over the near-linear items (count read on the device)
-    k_valence_fb<<<152 * 2, 128, 0, st>>>(d, eflag);
-    k_torsion_fb<<<152 * 2, 128, 0, st>>>(d, eflag);
-  } else {
-    if (nval > 0) k_valence<double><<<gv, 128, 0, st>>>(d, eflag, nval);
-    if (ntor > 0) k_torsion<double><<<gt, 128, 0, st>>>(d, eflag, ntor);
-  }
+  if (d.vflag) vt_kernels<true>(d, st, eflag, nval, ntor, gv, gt);
+  else vt_kernels<false>(d, st, eflag, nval, ntor, gv, gt);
 }
 
 void launch_dbond_forces(const Dev &d, cudaStream_t st) {
   const int B = 256;
-  k_dbond<<<(d.n + B - 1) / B, B, 0, st>>>(d);
+  if (d.vflag) k_dbond<true><<<(d.n + B - 1) / B, B, 0, st>>>(d);
+  else k_dbond<false><<<(d.n + B - 1) / B, B, 0, st>>>(d);
 }
 
 void launch_force_out(const Dev &d, cudaStream_t st) {

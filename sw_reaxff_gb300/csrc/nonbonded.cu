@@ -192,7 +192,7 @@ __device__ __forceinline__ void pair_terms(const Dev &d, const ForceField &F, co
 
 // one warp per atom i; the pairs (i,j,image) with j > i, or j == i with the
 // "positive" image, are queued and evaluated 32 at a time
-template <typename R>
+template <typename R, bool VIR>
 __global__ void __launch_bounds__(NBW * 32) k_nonbonded(Dev d, int eflag) {
   __shared__ PairQueue queues[NBW];
   const int lane = threadIdx.x & 31;
@@ -248,7 +248,7 @@ __global__ void __launch_bounds__(NBW * 32) k_nonbonded(Dev d, int eflag) {
           atomicAdd(&fC[j], c * dx);
           atomicAdd(&fC[n + j], c * dy);
           atomicAdd(&fC[2 * n + j], c * dz);
-          if (d.vflag) vir_acc(w, dx, dy, dz, c * dx, c * dy, c * dz);
+          if (VIR) vir_acc(w, dx, dy, dz, c * dx, c * dy, c * dz);
         }
         __syncwarp();
         const int left = qn - cnt;
@@ -277,7 +277,7 @@ __global__ void __launch_bounds__(NBW * 32) k_nonbonded(Dev d, int eflag) {
     seg_block_add<1>(v + 2, sg, d.energy + E_ENG_VDWL, RG_NE);
     seg_block_add<1>(v + 3, sg, d.energy + E_ENG_COUL, RG_NE);
   }
-  if (d.vflag) seg_block_add<6>(w, i < d.n ? d.seg_s[i] : -1, d.virial, 6);
+  if (VIR) seg_block_add<6>(w, i < d.n ? d.seg_s[i] : -1, d.virial, 6);
 }
 
 }  // namespace
@@ -285,6 +285,11 @@ __global__ void __launch_bounds__(NBW * 32) k_nonbonded(Dev d, int eflag) {
 void launch_nonbonded(const Dev &d, cudaStream_t st, int eflag) {
   const long long threads = (long long)d.n * 32;
   const unsigned G = (unsigned)((threads + NBW * 32 - 1) / (NBW * 32));
-  if (d.mixed) k_nonbonded<float><<<G, NBW * 32, 0, st>>>(d, eflag);
-  else k_nonbonded<double><<<G, NBW * 32, 0, st>>>(d, eflag);
+  if (d.vflag) {
+    if (d.mixed) k_nonbonded<float, true><<<G, NBW * 32, 0, st>>>(d, eflag);
+    else k_nonbonded<double, true><<<G, NBW * 32, 0, st>>>(d, eflag);
+  } else {
+    if (d.mixed) k_nonbonded<float, false><<<G, NBW * 32, 0, st>>>(d, eflag);
+    else k_nonbonded<double, false><<<G, NBW * 32, 0, st>>>(d, eflag);
+  }
 }

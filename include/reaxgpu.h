@@ -241,6 +241,16 @@ int rg_qeq_noalloc(rg_system *h, int n, const double *x, const int *type,
  * denominator of the FP64 form, whose kernels are bound by the FP64 units. */
 int rg_measure_fp64_peak(int device, double *tflops);
 
+/* Bond table of the last force step (fix reax/c/bonds, FindBond,
+ * fix_reaxc_bonds_sunway.cpp:196-255), per atom in the original order:
+ * nbond[n] partners with corrected bond order > bo_cut (at most
+ * max_per_atom listed), their tags nbr_tag[n*max_per_atom] and bond orders
+ * bo[n*max_per_atom], the total bond order total_bo[n] and the lone pairs
+ * nlp[n] (any array may be NULL).  Returns the largest partner count (which
+ * may exceed max_per_atom) or a negative error code. */
+int rg_bond_table(rg_system *h, double bo_cut, int max_per_atom, int *nbond, int *nbr_tag,
+                  double *bo, double *total_bo, double *nlp);
+
 /* List dumps for parity checks, from the last force step.  Each entry is
  * (tag_i, tag_j, image) with image = (sx+8) | (sy+8)<<4 | (sz+8)<<8 the
  * periodic image of j relative to i.  Pass NULL arrays to get the count.

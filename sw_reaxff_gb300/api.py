@@ -32,7 +32,7 @@ EXPORTED = ["rg_default_params", "rg_create", "rg_destroy", "rg_last_error",
             "rg_qeq_noalloc", "rg_set_masses", "rg_ffield_info", "rg_set_segments",
             "rg_num_segments", "rg_get_energies", "rg_get_segment_iters",
             "rg_get_histories", "rg_set_histories", "rg_table_info", "rg_table_check",
-            "rg_get_virial"]
+            "rg_get_virial", "rg_bond_table"]
 
 
 class Params(C.Structure):
@@ -90,6 +90,7 @@ def load_library(path: str = LIBPATH):
     L.rg_get_histories.argtypes = [C.c_void_p, dp, dp]
     L.rg_table_info.argtypes = [C.c_void_p, ip, dp]
     L.rg_get_virial.argtypes = [C.c_void_p, dp]
+    L.rg_bond_table.argtypes = [C.c_void_p, C.c_double, C.c_int, ip, ip, dp, dp, dp]
     L.rg_table_check.argtypes = [C.c_char_p, P(Params), dp]
     L.rg_set_histories.argtypes = [C.c_void_p, dp, dp]
     L.rg_ffield_info.argtypes = [C.c_char_p, ip, C.c_char_p, C.c_int, C.c_char_p, C.c_int]
@@ -276,6 +277,20 @@ class ReaxGPU:
         e = C.c_double()
         self._chk(self.L.rg_table_info(self.h, C.byref(n), C.byref(e)), "rg_table_info")
         return n.value, e.value
+
+    def bond_table(self, bo_cut=0.3, max_per_atom=12):
+        """Per-atom bonds with corrected BO > bo_cut (fix reax/c/bonds):
+        (nbond[n], partner tags[n, max], bond orders[n, max], total BO[n],
+        lone pairs[n]) in the original atom order."""
+        nb = np.zeros(self.n, np.int32)
+        tg = np.zeros((self.n, max_per_atom), np.int32)
+        bo = np.zeros((self.n, max_per_atom))
+        tot = np.zeros(self.n)
+        nlp = np.zeros(self.n)
+        rc = self.L.rg_bond_table(self.h, bo_cut, max_per_atom, _ip(nb), _ip(tg), _dp(bo),
+                                  _dp(tot), _dp(nlp))
+        self._chk(min(rc, 0), "rg_bond_table")
+        return nb, tg, bo, tot, nlp
 
     def set_positions(self, x):
         x = np.ascontiguousarray(x, np.float64)

@@ -1232,6 +1232,47 @@ extern "C" long long rg_dump_bonds(rg_system *h, int *ti, int *tj, int *img, dou
   return k;
 }
 
+// FindBond (fix_reaxc_bonds_sunway.cpp:196-223) and PassBuffer (:226-255):
+// per atom (original order) the partners with corrected BO > bo_cut, their
+// bond orders, the total bond order (bo_dboc[i][0]) and the lone pairs.
+extern "C" int rg_bond_table(rg_system *h, double bo_cut, int max_per_atom, int *nbond,
+                             int *nbr_tag, double *bo, double *total_bo, double *nlp) {
+  if (!h || max_per_atom <= 0) return RG_E_ARG;
+  // bond orders belong to the positions of the last force step
+  if (!h->forces_valid || !h->lists_valid)
+    return fail(h, RG_E_STATE, "no force step since the last state change");
+  const Dev &d = h->d;
+  const int n = d.n;
+  auto nb = fetch(h, d.nbonds, n);
+  auto tags = fetch(h, d.tags, n);
+  auto perm = fetch(h, d.perm, n);
+  const size_t S = (size_t)n * d.bond_cap;
+  auto bn = fetch(h, d.b_nbr, S);
+  auto BO = fetch(h, d.b_BO, S);
+  auto tb = fetch(h, d.bo0, n);
+  auto lp = fetch(h, d.nlp, n);
+  int most = 0;
+  for (int i = 0; i < n; ++i) {
+    const int o = perm[i];
+    int c = 0;
+    for (int q = 0; q < std::min(nb[i], d.bond_cap); ++q) {
+      const size_t s = (size_t)q * n + i;
+      if (BO[s] > bo_cut) {
+        if (c < max_per_atom) {
+          if (nbr_tag) nbr_tag[(size_t)o * max_per_atom + c] = tags[bn[s] >> 8];
+          if (bo) bo[(size_t)o * max_per_atom + c] = BO[s];
+        }
+        ++c;
+      }
+    }
+    if (nbond) nbond[o] = std::min(c, max_per_atom);
+    if (total_bo) total_bo[o] = tb[i];
+    if (nlp) nlp[o] = lp[i];
+    most = std::max(most, c);
+  }
+  return most;
+}
+
 extern "C" long long rg_dump_hbonds(rg_system *h, int *ti, int *tj, int *img) {
   if (!h || !h->lists_valid) return -1;
   const Dev &d = h->d;

@@ -10,6 +10,7 @@
 //
 //   units real | atom_style charge | boundary p p p | read_data FILE |
 //   mass I M | pair_style ... | pair_coeff ... | fix ID all STYLE ... |
+//   (STYLE: qeq/reax, nve, reax/c/bonds and their /sunway, /gb300 names)
 //   timestep DT | thermo N | run N |
 //   write_dump all custom FILE COLS (id type q x y z vx vy vz fx fy fz)
 //   neighbor / neigh_modify / thermo_style / thermo_modify: accepted, no effect
@@ -209,6 +210,7 @@ int run_deck(std::istream &in) {
   std::unique_ptr<reaxgb::FixQEqReaxGB300> qeq;
   std::unique_ptr<reaxgb::FixNVEGB300> nve;
   std::unique_ptr<reaxgb::Verlet> verlet;
+  std::vector<std::unique_ptr<reaxgb::FixReaxCBondsGB300>> bonds;
   bool have_data = false, setup_done = false;
   int thermo_every = 0;
   std::string line;
@@ -254,6 +256,8 @@ int run_deck(std::istream &in) {
         qeq.reset(new reaxgb::FixQEqReaxGB300(pair.get(), &update, a.n(), a.v()));
       } else if (is_style(w[3], {"nve", "nve/sunway", "nve/gb300"})) {
         nve.reset(new reaxgb::FixNVEGB300(pair.get(), &update, a.n(), a.v()));
+      } else if (is_style(w[3], {"reax/c/bonds", "reax/c/bonds/sunway", "reax/c/bonds/gb300"})) {
+        bonds.emplace_back(new reaxgb::FixReaxCBondsGB300(pair.get(), &atom, &update, a.n(), a.v()));
       } else {
         throw Error("Unrecognized fix style " + w[3]);
       }
@@ -271,7 +275,10 @@ int run_deck(std::istream &in) {
       if (w.size() < 2) throw Error("Illegal run command");
       if (!pair) throw Error("Run command before pair style is defined");
       const long long n = std::stoll(w[1]);
-      if (!verlet) verlet.reset(new reaxgb::Verlet(&atom, &update, pair.get(), qeq.get(), nve.get()));
+      if (!verlet) {
+        verlet.reset(new reaxgb::Verlet(&atom, &update, pair.get(), qeq.get(), nve.get()));
+        for (auto &b : bonds) verlet->end_of_step_fixes.push_back(b.get());
+      }
       Thermo T{pair.get(), qeq.get()};
       if (!setup_done) {
         verlet->setup();

@@ -338,6 +338,57 @@ void FixNVEGB300::final_integrate() {
   pair_->modified_device();
 }
 
+// ---------------------------------------------------------------- fix bonds
+
+FixReaxCBondsGB300::FixReaxCBondsGB300(PairReaxCGB300 *pair, Atom *atom, Update *update, int narg,
+                                       char **arg)
+    : pair_(pair), atom_(atom), update_(update) {
+  if (narg != 5) throw Error("Illegal fix reax/c/bonds command");
+  nevery = (int)inumeric(arg[3]);
+  if (nevery <= 0) throw Error("Illegal fix reax/c/bonds command");
+  if (!pair_) throw Error("Cannot use fix reax/c/bonds without pair_style reax/c");
+  fp_ = std::fopen(arg[4], "w");
+  if (!fp_) throw Error(std::string("Cannot open fix reax/c/bonds file ") + arg[4]);
+}
+
+FixReaxCBondsGB300::~FixReaxCBondsGB300() {
+  if (fp_) std::fclose(fp_);
+}
+
+void FixReaxCBondsGB300::setup() { output(); }
+
+void FixReaxCBondsGB300::end_of_step() {
+  if (update_->ntimestep % nevery == 0) output();
+}
+
+void FixReaxCBondsGB300::output() {
+  const int n = atom_->nlocal;
+  const int cap = 24;
+  std::vector<int> nb(n), tags((size_t)n * cap);
+  std::vector<double> bo((size_t)n * cap), tot(n), nlp(n);
+  const int most = rg_bond_table(pair_->handle(), bg_cut, cap, nb.data(), tags.data(), bo.data(),
+                                 tot.data(), nlp.data());
+  pair_->check(most < 0 ? most : RG_OK, "rg_bond_table");
+  pair_->sync_host();
+  std::fprintf(fp_, "# Timestep %lld \n", update_->ntimestep);
+  std::fprintf(fp_, "# \n");
+  std::fprintf(fp_, "# Number of particles %d \n", n);
+  std::fprintf(fp_, "# \n");
+  std::fprintf(fp_, "# Max number of bonds per atom %d with coarse bond order cutoff %5.3f \n",
+               most, bg_cut);
+  std::fprintf(fp_, "# Particle connection table and bond orders \n");
+  std::fprintf(fp_, "# id type nb id_1...id_nb mol bo_1...bo_nb abo nlp q \n");
+  for (int i = 0; i < n; ++i) {
+    std::fprintf(fp_, " %d %d %d", atom_->tag[i], atom_->type[i], nb[i]);
+    for (int k = 0; k < nb[i]; ++k) std::fprintf(fp_, " %d", tags[(size_t)i * cap + k]);
+    std::fprintf(fp_, " %d", 0);   // molecule id (atom_style charge has none)
+    for (int k = 0; k < nb[i]; ++k) std::fprintf(fp_, "%14.3f", bo[(size_t)i * cap + k]);
+    std::fprintf(fp_, "%14.3f%14.3f%14.3f\n", tot[i], nlp[i], atom_->q[i]);
+  }
+  std::fprintf(fp_, "# \n");
+  std::fflush(fp_);
+}
+
 // ---------------------------------------------------------------- Verlet
 
 void Verlet::setup() {
@@ -346,6 +397,7 @@ void Verlet::setup() {
   if (nve_) nve_->init();
   if (qeq_) qeq_->setup_pre_force(0);
   pair_->compute(1, 0);
+  for (auto *f : end_of_step_fixes) f->setup();
 }
 
 void Verlet::run(long long nsteps, int thermo_every, void (*thermo)(const Verlet &, void *),
@@ -358,6 +410,7 @@ void Verlet::run(long long nsteps, int thermo_every, void (*thermo)(const Verlet
     if (qeq_) qeq_->pre_force(0);
     pair_->compute(th ? 1 : 0, 0);
     if (nve_) nve_->final_integrate();
+    for (auto *f : end_of_step_fixes) f->end_of_step();
     if (th) {
       pair_->sync_host();
       if (thermo) thermo(*this, ctx);

@@ -23,6 +23,7 @@
 #ifndef REAX_STYLES_H
 #define REAX_STYLES_H
 
+#include <cstdio>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -86,6 +87,30 @@ class FixNVEGB300 {
   Update *update_;
 };
 
+// fix ID group reax/c/bonds Nevery file (FixReaxCBondsSunway,
+// fix_reaxc_bonds_sunway.cpp:45-330): every Nevery steps, the connection
+// table with bond orders above the coarse cutoff bg_cut = 0.3, the total
+// bond order, lone pairs and charge of every atom, in the reference's file
+// format.
+class FixReaxCBondsGB300 {
+ public:
+  FixReaxCBondsGB300(PairReaxCGB300 *pair, Atom *atom, Update *update, int narg, char **arg);
+  ~FixReaxCBondsGB300();
+  FixReaxCBondsGB300(const FixReaxCBondsGB300 &) = delete;
+  FixReaxCBondsGB300 &operator=(const FixReaxCBondsGB300 &) = delete;
+  void setup();
+  void end_of_step();
+  int nevery = 1;
+  double bg_cut = 0.3;
+
+ private:
+  void output();
+  PairReaxCGB300 *pair_;
+  Atom *atom_;
+  Update *update_;
+  std::FILE *fp_ = nullptr;
+};
+
 class PairReaxCGB300 {
  public:
   explicit PairReaxCGB300(Atom *atom);
@@ -131,6 +156,7 @@ class PairReaxCGB300 {
   bool have_forces_ = false;
   friend class FixQEqReaxGB300;
   friend class FixNVEGB300;
+  friend class FixReaxCBondsGB300;
 };
 
 // LAMMPS's Verlet order: setup (pre_force, force) then per step
@@ -145,6 +171,7 @@ class Verlet {
   void run(long long nsteps, int thermo_every,
            void (*thermo)(const Verlet &, void *) = nullptr, void *ctx = nullptr);
   double kinetic_energy() const;   // kcal/mol from the host velocities
+  std::vector<FixReaxCBondsGB300 *> end_of_step_fixes;
   Atom *atom_;
   Update *update_;
   PairReaxCGB300 *pair_;

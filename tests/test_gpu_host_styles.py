@@ -100,3 +100,87 @@ def test_deck_nve_follows_rg_run(tmp_path, ffield):
     etot = [float(ln.split()[3]) for ln in lines]
     # NVE: total energy drifts by far less than the kinetic energy
     assert abs(etot[-1] - etot[0]) < 0.05 * abs(float(lines[0].split()[2]))
+
+
+def read_bonds(path):
+    """One frame of a fix reax/c/bonds file: {tag: (type, partner tags, bond
+    orders, abo, nlp, q)} and the header's max bond count."""
+    rows, most = {}, None
+    for line in open(path):
+        if line.startswith("# Max number of bonds"):
+            most = int(line.split()[6])
+        elif not line.startswith("#"):
+            w = line.split()
+            tag, typ, nb = int(w[0]), int(w[1]), int(w[2])
+            ids = [int(v) for v in w[3:3 + nb]]
+            bo = [float(v) for v in w[4 + nb:4 + 2 * nb]]
+            abo, nlp, q = (float(v) for v in w[4 + 2 * nb:7 + 2 * nb])
+            rows[tag] = (typ, ids, bo, abo, nlp, q)
+    return rows, most
+
+
+def test_bond_table_matches_oracle(ffield):
+    """rg_bond_table (fix reax/c/bonds, FindBond with bg_cut = 0.3) against
+    the oracle's corrected bond orders, total bond order and lone pairs."""
+    s = systems.water_box(300, seed=4)
+    g = ReaxGPU(ffield)
+    g.set_system(s)
+    g.qeq()
+    g.compute()
+    nb, tg, bo, tot, nlp = g.bond_table(0.3, 12)
+    o = Oracle(ffield)
+    o.set_system(s.box, s.x, s.types(g.elements), s.tag, None, s.v)
+    o.qeq()
+    o.compute()
+    ti, tj, _, obo = o.bond_list()
+    at = o.atom_terms()
+    idx = {t: k for k, t in enumerate(s.tag)}
+    for a in range(s.n):
+        sel = (ti == s.tag[a]) & (obo[:, 0] > 0.3)
+        want = sorted(zip(tj[sel], obo[sel, 0]))
+        got = sorted(zip(tg[a, :nb[a]], bo[a, :nb[a]]))
+        assert [w[0] for w in want] == [x[0] for x in got]
+        assert np.allclose([w[1] for w in want], [x[1] for x in got], rtol=1e-9, atol=1e-12)
+        k = idx[s.tag[a]]
+        assert abs(tot[a] - obo[ti == s.tag[a], 0].sum()) < 1e-9
+        assert abs(nlp[a] - at[k, 6]) < 1e-9
+    assert nb.max() >= 2
+
+
+def test_deck_bonds_file(tmp_path, ffield):
+    """fix reax/c/bonds in a deck writes the reference's file format, one
+    frame per Nevery steps, with the library's bond table."""
+    s = systems.water_box(150, seed=2)
+    data = tmp_path / "sys.data"
+    els = systems.write_lammps_data(s, str(data), ["H", "O"])
+    deck = [
+        "units real", "atom_style charge", "boundary p p p", f"read_data {data}",
+        "pair_style reax/c/sunway NULL", f"pair_coeff * * {ffield} {' '.join(els)}",
+        "fix 1 all nve/sunway", "fix 2 all qeq/reax/sunway 1 0.0 10.0 1.0e-6 reax/c",
+        "fix 3 all reax/c/bonds 5 bonds.reaxc", "timestep 0.25", "run 10",
+        f"write_dump all custom out.dump {COLS}",
+    ]
+    (tmp_path / "in.deck").write_text("\n".join(deck) + "\n")
+    r = subprocess.run([B.build_host(), "in.deck"], cwd=str(tmp_path), capture_output=True,
+                       text=True, timeout=300)
+    assert r.returncode == 0, r.stdout + r.stderr
+    text = (tmp_path / "bonds.reaxc").read_text()
+    assert [int(l.split()[2]) for l in text.splitlines() if l.startswith("# Timestep")] == [0, 5, 10]
+    last = text[text.rindex("# Timestep"):]
+    (tmp_path / "last.reaxc").write_text(last)
+    rows, most = read_bonds(str(tmp_path / "last.reaxc"))
+    assert len(rows) == s.n and most == max(len(v[1]) for v in rows.values())
+    meta, st = read_dump(str(tmp_path / "out.dump"))
+    # the last frame is the final state: its charges are the dump's
+    for t, qv in zip(st["tag"], st["q"]):
+        assert abs(rows[t][5] - qv) < 1e-3
+    # every bond listed from both ends with the same order (to the printed 3 decimals)
+    for t, (_, ids, bo, _, _, _) in rows.items():
+        for j, b in zip(ids, bo):
+            back = rows[j][1].index(t)
+            assert abs(rows[j][2][back] - b) < 1.5e-3
+        assert all(b > 0.3 - 5e-4 for b in bo)
+    # O has two H partners in intact water
+    types = {t: v[0] for t, v in rows.items()}
+    o_type = els.index("O") + 1
+    assert np.mean([len(v[1]) == 2 for t, v in rows.items() if types[t] == o_type]) > 0.9

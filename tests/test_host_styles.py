@@ -2,7 +2,8 @@
 nve over the C ABI, with the reference's argument lists and error messages
 (PairReaxCSunway::settings/coeff/init_style, pair_reaxc_sunway.cpp:202-424;
 FixQEqReaxSunway constructor, fix_qeq_reax_sunway.cpp:64-90; FixNVESunway
-constructor, fix_nve_sunway.cpp:29-36), driven by the reax_md deck
+constructor, fix_nve_sunway.cpp:29-36; FixReaxCBondsSunway constructor,
+fix_reaxc_bonds_sunway.cpp:45-60, 125), driven by the reax_md deck
 interpreter.  Every deck here fails before the first device call, so these
 run without a GPU; the device runs are in test_gpu_host_styles.py."""
 import os
@@ -73,6 +74,12 @@ CASES = {
                      "Pair reax/c requires use of fix qeq/reax"),
     "qeq_taper": (["pair_style reax/c NULL", PAIR, "fix 2 all qeq/reax 1 0.0 -10.0 1e-6 reax/c",
                    "run 1"], "Fix qeq/reax has negative upper Taper radius cutoff"),
+    "bonds_args": (["pair_style reax/c NULL", PAIR, "fix 3 all reax/c/bonds 5"],
+                   "Illegal fix reax/c/bonds command"),
+    "bonds_nevery": (["pair_style reax/c NULL", PAIR, "fix 3 all reax/c/bonds 0 bonds.out"],
+                     "Illegal fix reax/c/bonds command"),
+    "bonds_no_pair": (["fix 3 all reax/c/bonds 5 bonds.out"],
+                      "Cannot use fix reax/c/bonds without pair_style reax/c"),
     "unknown": (["pair_style reax/c NULL", "compute 1 all pe"], "Unknown command"),
     "units": (["pair_style reax/c NULL"], "requires units real"),
 }

@@ -258,12 +258,16 @@ __device__ __forceinline__ void nbr_flush(const Dev &d, const Control &C, const 
       d.nbr[row + pos] = ((uint32_t)j << 8) | (uint32_t)img;
       d.hval32[row + pos] = 0.f;
     } else if (d2 <= C.swb2 && C.tab_n && d2 >= C.tab_s0) {
-      // FP64 table of H_ij (cubic Hermite in r^2)
-      double h01, t10, t11;
-      const int k = tab_weights(C, d2, h01, t10, t11);
+      // FP64 table of H_ij (cubic Hermite in r^2, power basis per interval)
+      const double x = fma(d2, C.tab_inv_ds, C.tab_x0);
+      int k = (int)x;
+      if (k > C.tab_n - 1) k = C.tab_n - 1;
+      const double u = x - (double)k;
       const int tj = __float_as_int(d.xf[j].w);
-      const double *T = d.tab_h + ((long long)C.tab_pair[ti][tj] * (C.tab_n + 1) + k) * 2;
-      h = tab_interp(T[0], T[2], T[1], T[3], h01, t10, t11);
+      const double2 *T =
+          reinterpret_cast<const double2 *>(d.tab_h + ((long long)C.tab_pair[ti][tj] * C.tab_n + k) * 4);
+      const double2 c01 = T[0], c23 = T[1];
+      h = fma(fma(fma(c23.y, u, c23.x), u, c01.y), u, c01.x);
     } else if (d2 <= C.swb2) {
       // H_ij = Tap(r) * 14.4 / (r^3 + shld)^c, c = 0.3333333333333
       const double r = d2 * rsqrt(d2);
@@ -302,7 +306,7 @@ __global__ void __launch_bounds__(NB_WARPS * 32) k_build_nbrs(Dev d) {
   const float4 xif = d.xf[i];
   const float4 xil = MIXED ? d.xl[i] : make_float4(0.f, 0.f, 0.f, 0.f);
   const int ti = d.ts[i];
-  const float cut2f = (float)(C.list_cut2 * (1.0 + 1e-5) + 0.05);
+  const float cut2f = C.list_pre2_f;
   const SegGeom &g = d.seg[d.seg_s[i]];
   const double L[3] = {g.L[0], g.L[1], g.L[2]};
   const int ncx = g.nc[0], ncy = g.nc[1], ncz = g.nc[2], S = g.S;
@@ -333,9 +337,10 @@ __global__ void __launch_bounds__(NB_WARPS * 32) k_build_nbrs(Dev d) {
         const int beg = d.cell_start[rowcell + rx];
         const int end = d.cell_start[rowcell + rx + len];
         ox += len;
-        const float shxf = (float)(sx * L[0]);
-        const float shyf = (float)(sy * L[1]);
-        const float shzf = (float)(sz * L[2]);
+        // (float)(s L) exactly: |s| <= 2 scales the rounded edge exactly
+        const float shxf = (float)sx * g.Lh[0];
+        const float shyf = (float)sy * g.Lh[1];
+        const float shzf = (float)sz * g.Lh[2];
         const bool self_img = (sx == 0 && sy == 0 && sz == 0);
         const int img = img_pack(sx, sy, sz);
         for (int base = beg; base < end; base += 32) {
@@ -393,15 +398,12 @@ __global__ void __launch_bounds__(NB_WARPS * 32) k_build_nbrs(Dev d) {
 // One warp per atom i over the near part of its row.  H-bond partners are
 // decided from the exact distance directly.  Bond candidates (d <= bond_cut)
 // whose FP32 estimate of BO' is above half of bo_cut (FP32 errors are ~1e-4
-// relative here) are queued; full batches of 32 then get the FP64 BO' and
-// the exact BO' >= bo_cut decision with all lanes busy.
+// relative here) are written to the bond slots of i; k_bond_prime then
+// evaluates BO' and the exact BO' >= bo_cut decision one thread per
+// candidate (a row has only a few candidates, so a per-row warp would run
+// the FP64 pow/exp with most lanes idle), and k_bond_finish compacts the
+// rows and sums dDeltap and the total bond order.
 
-struct BondQueue {
-  uint32_t e[QCAP];
-  double dist[QCAP], dx[QCAP], dy[QCAP], dz[QCAP];
-};
-
-// uncorrected bond order terms of one pair in arithmetic R
 template <typename R>
 __device__ __forceinline__ void bo_prime(const Sbp &si, const Sbp &sj, const Tbp &tw, R dist, R bo_cut,
                                          R &BOs, R &BOpi, R &BOpi2, R &C12, R &C34, R &C56) {
@@ -420,83 +422,117 @@ __device__ __forceinline__ void bo_prime(const Sbp &si, const Sbp &sj, const Tbp
   }
 }
 
+// BO' of the bond candidates: one thread per candidate slot (blockIdx.y =
+// slot), so the FP64 pow/exp run with full warps instead of the few lanes a
+// per-atom warp has candidates for.  Accepted entries get their bond
+// orders and dBO' terms; rejected ones (BO' < bo_cut) are marked with a
+// negative distance and removed by k_bond_finish.
 template <bool MIXED>
-__device__ __forceinline__ void bond_flush(const Dev &d, const Control &C, const ForceField &F,
-                                           const BondQueue &Q, int cnt, int lane, int i, int ti,
-                                           int &nb, double &ddx, double &ddy, double &ddz,
-                                           double &bsum) {
-  bool isb = false;
-  double dist = 0, dx = 0, dy = 0, dz = 0, BOs = 0, BOpi = 0, BOpi2 = 0, Cs = 0, Cpi = 0, Cpi2 = 0;
-  uint32_t e = 0;
-  if (lane < cnt) {
-    e = Q.e[lane];
-    dist = Q.dist[lane];
-    dx = Q.dx[lane]; dy = Q.dy[lane]; dz = Q.dz[lane];
-    const int tj = d.ts[(int)(e >> 8)];
-    const Sbp &si = F.sbp[ti], &sj = F.sbp[tj];
-    const Tbp &tw = F.tbp[ti][tj];
-    double C12, C34, C56;
-    if (MIXED) {
-      // FP32 bond orders; the exact FP64 decision only within 1e-4 of
-      // the threshold, so the bond list equals the FP64 form's
-      float a, b, c, c12, c34, c56;
-      bo_prime<float>(si, sj, tw, (float)dist, (float)C.bo_cut, a, b, c, c12, c34, c56);
-      BOs = a; BOpi = b; BOpi2 = c; C12 = c12; C34 = c34; C56 = c56;
-      const double BO32 = (double)(a + b + c);
-      if (fabs(BO32 - C.bo_cut) <= 1e-4 * C.bo_cut) {
-        double x0, x1, x2, y0, y1, y2;
-        bo_prime<double>(si, sj, tw, dist, C.bo_cut, x0, x1, x2, y0, y1, y2);
-        isb = (x0 + x1 + x2) >= C.bo_cut;
-      } else {
-        isb = BO32 >= C.bo_cut;
-      }
+__global__ void k_bond_prime(Dev d) {
+  const int n = d.n;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int k = blockIdx.y;
+  if (i >= n) return;
+  if (k >= min(d.nbonds[i], d.bond_cap)) return;
+  const Control &C = *d.ctl;
+  const ForceField &F = *d.ff;
+  const long long s = (long long)k * n + i;
+  const long long S3 = (long long)d.bond_cap * n;
+  const uint32_t e = d.b_nbr[s];
+  const double dist = d.b_d[s];
+  const int ti = d.ts[i], tj = d.ts[(int)(e >> 8)];
+  const Sbp &si = F.sbp[ti], &sj = F.sbp[tj];
+  const Tbp &tw = F.tbp[ti][tj];
+  double BOs, BOpi, BOpi2, C12, C34, C56;
+  bool isb;
+  if (MIXED) {
+    // FP32 bond orders; the exact FP64 decision only within 1e-4 of the
+    // threshold, so the bond list equals the FP64 form's
+    float a, b, c, c12, c34, c56;
+    bo_prime<float>(si, sj, tw, (float)dist, (float)C.bo_cut, a, b, c, c12, c34, c56);
+    BOs = a; BOpi = b; BOpi2 = c; C12 = c12; C34 = c34; C56 = c56;
+    const double BO32 = (double)(a + b + c);
+    if (fabs(BO32 - C.bo_cut) <= 1e-4 * C.bo_cut) {
+      double x0, x1, x2, y0, y1, y2;
+      bo_prime<double>(si, sj, tw, dist, C.bo_cut, x0, x1, x2, y0, y1, y2);
+      isb = (x0 + x1 + x2) >= C.bo_cut;
     } else {
-      bo_prime<double>(si, sj, tw, dist, C.bo_cut, BOs, BOpi, BOpi2, C12, C34, C56);
-      isb = (BOs + BOpi + BOpi2) >= C.bo_cut;
+      isb = BO32 >= C.bo_cut;
     }
-    if (isb) {
-      const double r2 = dist * dist;
-      Cs = tw.p_bo2 * C12 / r2;
-      Cpi = tw.p_bo4 * C34 / r2;
-      Cpi2 = tw.p_bo6 * C56 / r2;
-    }
+  } else {
+    bo_prime<double>(si, sj, tw, dist, C.bo_cut, BOs, BOpi, BOpi2, C12, C34, C56);
+    isb = (BOs + BOpi + BOpi2) >= C.bo_cut;
   }
-  const unsigned mb = __ballot_sync(FULL, isb);
-  if (isb) {
-    const int n = d.n;
-    const int k = nb + __popc(mb & lanemask_lt());
-    const double g = -(BOs * Cs + BOpi * Cpi + BOpi2 * Cpi2);
-    const double gx = g * dx, gy = g * dy, gz = g * dz;
-    ddx += gx; ddy += gy; ddz += gz;
-    const double BOc = BOs + BOpi + BOpi2 - C.bo_cut;
-    bsum += BOc;
-    if (k < d.bond_cap) {
-      const long long s = (long long)k * n + i;
-      const long long S3 = (long long)d.bond_cap * n;
-      d.b_nbr[s] = e;
-      d.b_d[s] = dist;
-      d.b_dx[s] = dx; d.b_dy[s] = dy; d.b_dz[s] = dz;
-      d.b_BO[s] = BOc;
-      d.b_BOs[s] = BOs - C.bo_cut;
-      d.b_BOpi[s] = BOpi;
-      d.b_BOpi2[s] = BOpi2;
-      d.b_dBOp[s] = gx; d.b_dBOp[S3 + s] = gy; d.b_dBOp[2 * S3 + s] = gz;
-      const double api = -BOpi * Cpi, api2 = -BOpi2 * Cpi2;
-      d.b_dlnpi[s] = api * dx; d.b_dlnpi[S3 + s] = api * dy; d.b_dlnpi[2 * S3 + s] = api * dz;
-      d.b_dlnpi2[s] = api2 * dx; d.b_dlnpi2[S3 + s] = api2 * dy; d.b_dlnpi2[2 * S3 + s] = api2 * dz;
-      d.b_Cdbo[s] = 0.0; d.b_Cdbopi[s] = 0.0; d.b_Cdbopi2[s] = 0.0;
-    }
+  if (!isb) {
+    d.b_d[s] = -1.0;
+    return;
   }
-  nb += __popc(mb);
+  const double r2 = dist * dist;
+  const double Cs = tw.p_bo2 * C12 / r2;
+  const double Cpi = tw.p_bo4 * C34 / r2;
+  const double Cpi2 = tw.p_bo6 * C56 / r2;
+  const double dx = d.b_dx[s], dy = d.b_dy[s], dz = d.b_dz[s];
+  const double g = -(BOs * Cs + BOpi * Cpi + BOpi2 * Cpi2);
+  d.b_BO[s] = BOs + BOpi + BOpi2 - C.bo_cut;
+  d.b_BOs[s] = BOs - C.bo_cut;
+  d.b_BOpi[s] = BOpi;
+  d.b_BOpi2[s] = BOpi2;
+  d.b_dBOp[s] = g * dx; d.b_dBOp[S3 + s] = g * dy; d.b_dBOp[2 * S3 + s] = g * dz;
+  const double api = -BOpi * Cpi, api2 = -BOpi2 * Cpi2;
+  d.b_dlnpi[s] = api * dx; d.b_dlnpi[S3 + s] = api * dy; d.b_dlnpi[2 * S3 + s] = api * dz;
+  d.b_dlnpi2[s] = api2 * dx; d.b_dlnpi2[S3 + s] = api2 * dy; d.b_dlnpi2[2 * S3 + s] = api2 * dz;
+  d.b_Cdbo[s] = 0.0; d.b_Cdbopi[s] = 0.0; d.b_Cdbopi2[s] = 0.0;
+}
+
+// per atom: drop rejected candidates (keeping the order of the rest), then
+// the bond count, sum_j dBO'_ij (dDeltap) and the total bond order, summed
+// in slot order
+__global__ void k_bond_finish(Dev d) {
+  const int n = d.n;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int nc = min(d.nbonds[i], d.bond_cap);
+  const long long S3 = (long long)d.bond_cap * n;
+  double ddx = 0.0, ddy = 0.0, ddz = 0.0, bsum = 0.0;
+  int w = 0;
+  for (int k = 0; k < nc; ++k) {
+    const long long s = (long long)k * n + i;
+    if (d.b_d[s] < 0.0) continue;
+    if (w != k) {
+      const long long t = (long long)w * n + i;
+      d.b_nbr[t] = d.b_nbr[s];
+      d.b_d[t] = d.b_d[s];
+      d.b_dx[t] = d.b_dx[s]; d.b_dy[t] = d.b_dy[s]; d.b_dz[t] = d.b_dz[s];
+      d.b_BO[t] = d.b_BO[s]; d.b_BOs[t] = d.b_BOs[s];
+      d.b_BOpi[t] = d.b_BOpi[s]; d.b_BOpi2[t] = d.b_BOpi2[s];
+      for (int c = 0; c < 3; ++c) {
+        d.b_dBOp[c * S3 + t] = d.b_dBOp[c * S3 + s];
+        d.b_dlnpi[c * S3 + t] = d.b_dlnpi[c * S3 + s];
+        d.b_dlnpi2[c * S3 + t] = d.b_dlnpi2[c * S3 + s];
+      }
+      d.b_Cdbo[t] = 0.0; d.b_Cdbopi[t] = 0.0; d.b_Cdbopi2[t] = 0.0;
+    }
+    const long long t = (long long)w * n + i;
+    ddx += d.b_dBOp[t];
+    ddy += d.b_dBOp[S3 + t];
+    ddz += d.b_dBOp[2 * S3 + t];
+    bsum += d.b_BO[t];
+    ++w;
+  }
+  // an overflowed row (more candidates than slots) keeps its candidate
+  // count, so the host sees the overflow and rebuilds with more slots
+  if (d.nbonds[i] <= d.bond_cap) d.nbonds[i] = w;
+  d.dDeltap[i] = ddx;
+  d.dDeltap[n + i] = ddy;
+  d.dDeltap[2 * n + i] = ddz;
+  d.bo0[i] = bsum;
 }
 
 template <bool MIXED>
 __global__ void __launch_bounds__(NB_WARPS * 32) k_build_bonds(Dev d) {
-  __shared__ BondQueue queues[NB_WARPS];
   const int lane = threadIdx.x & 31;
   const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   if (i >= d.n) return;
-  BondQueue &Q = queues[threadIdx.x >> 5];
   const Control &C = *d.ctl;
   const ForceField &F = *d.ff;
   const double4 xi = d.xs[i];
@@ -514,11 +550,10 @@ __global__ void __launch_bounds__(NB_WARPS * 32) k_build_bonds(Dev d) {
   // H atoms within hbond_cut
   const float rpre = (float)((ihb ? fmax(C.bond_cut, C.hbond_cut) : C.bond_cut) + 0.01);
   const float rpre2 = rpre * rpre;
-  const float bo_half = (float)(0.5 * C.bo_cut);
-  int nb = 0, nh = 0, qn = 0;
-  double ddx = 0.0, ddy = 0.0, ddz = 0.0, bsum = 0.0;
-  for (int base = 0; base < nn + 32; base += 32) {
-    if (base < nn) {
+  const float bo_half = C.bo_half_f;
+  int nb = 0, nh = 0;
+  for (int base = 0; base < nn; base += 32) {
+    {
       const int p = base + lane;
       bool ish = false, cand = false;
       uint32_t e = 0;
@@ -566,15 +601,12 @@ __global__ void __launch_bounds__(NB_WARPS * 32) k_build_bonds(Dev d) {
             if (isb) { dx = ex; dy = ey; dz = ez; dist = df; }
           }
           if (isb) {
-            const Tbp &tw = F.tbp[ti][tj];
-            const float dd = (float)dist;
+            const Control::BoEst &be = C.bo_est[ti][tj];
+            const float dd = exact ? (float)dist : df;
             float est = 0.f;
-            if (si.r_s > 0.0 && sj.r_s > 0.0)
-              est += (float)(1.0 + C.bo_cut) * expf((float)tw.p_bo1 * powf(dd / (float)tw.r_s, (float)tw.p_bo2));
-            if (si.r_pi > 0.0 && sj.r_pi > 0.0)
-              est += expf((float)tw.p_bo3 * powf(dd / (float)tw.r_p, (float)tw.p_bo4));
-            if (si.r_pi_pi > 0.0 && sj.r_pi_pi > 0.0)
-              est += expf((float)tw.p_bo5 * powf(dd / (float)tw.r_pp, (float)tw.p_bo6));
+            if (be.mask & 1) est += C.bo_scale_f * expf(be.p_bo1 * powf(dd / be.r_s, be.p_bo2));
+            if (be.mask & 2) est += expf(be.p_bo3 * powf(dd / be.r_p, be.p_bo4));
+            if (be.mask & 4) est += expf(be.p_bo5 * powf(dd / be.r_pp, be.p_bo6));
             cand = est >= bo_half;
           }
         }
@@ -585,47 +617,24 @@ __global__ void __launch_bounds__(NB_WARPS * 32) k_build_bonds(Dev d) {
         if (k < d.hb_cap) d.hb_nbr[(long long)i * d.hb_cap + k] = e;
       }
       nh += __popc(mh);
+      // candidates go to the bond slots in row order; k_bond_prime gives
+      // them their FP64 (or FP32) BO' and k_bond_finish drops the rejected
       const unsigned mc = __ballot_sync(FULL, cand);
       if (cand) {
-        const int q = qn + __popc(mc & lanemask_lt());
-        Q.e[q] = e; Q.dist[q] = dist; Q.dx[q] = dx; Q.dy[q] = dy; Q.dz[q] = dz;
+        const int k = nb + __popc(mc & lanemask_lt());
+        if (k < d.bond_cap) {
+          const long long s = (long long)k * n + i;
+          d.b_nbr[s] = e;
+          d.b_d[s] = dist;
+          d.b_dx[s] = dx; d.b_dy[s] = dy; d.b_dz[s] = dz;
+        }
       }
-      qn += __popc(mc);
-      __syncwarp();
+      nb += __popc(mc);
     }
-    while (qn >= 32 || (base >= nn && qn > 0)) {
-      const int cnt = min(qn, 32);
-      bond_flush<MIXED>(d, C, F, Q, cnt, lane, i, ti, nb, ddx, ddy, ddz, bsum);
-      __syncwarp();
-      const int left = qn - cnt;
-      uint32_t le = 0;
-      double l0 = 0, l1 = 0, l2 = 0, l3 = 0;
-      if (lane < left) {
-        le = Q.e[cnt + lane]; l0 = Q.dist[cnt + lane];
-        l1 = Q.dx[cnt + lane]; l2 = Q.dy[cnt + lane]; l3 = Q.dz[cnt + lane];
-      }
-      __syncwarp();
-      if (lane < left) {
-        Q.e[lane] = le; Q.dist[lane] = l0; Q.dx[lane] = l1; Q.dy[lane] = l2; Q.dz[lane] = l3;
-      }
-      qn = left;
-      __syncwarp();
-    }
-  }
-  // warp sums in lane order (deterministic)
-  for (int off = 16; off > 0; off >>= 1) {
-    ddx += __shfl_down_sync(FULL, ddx, off);
-    ddy += __shfl_down_sync(FULL, ddy, off);
-    ddz += __shfl_down_sync(FULL, ddz, off);
-    bsum += __shfl_down_sync(FULL, bsum, off);
   }
   if (lane == 0) {
     d.nbonds[i] = nb;
     d.nhb[i] = nh;
-    d.dDeltap[i] = ddx;
-    d.dDeltap[n + i] = ddy;
-    d.dDeltap[2 * n + i] = ddz;
-    d.bo0[i] = bsum;
     if (nb > d.bond_cap) atomicOr(&d.status[ST_OVF], OVF_BOND);
     if (nh > d.hb_cap) atomicOr(&d.status[ST_OVF], OVF_HB);
     atomicMax(&d.status[ST_MAXB], nb);
@@ -718,6 +727,10 @@ void launch_build_bonds(const Dev &d, cudaStream_t st) {
   const unsigned G = (unsigned)((threads + NB_WARPS * 32 - 1) / (NB_WARPS * 32));
   if (d.mixed) k_build_bonds<true><<<G, NB_WARPS * 32, 0, st>>>(d);
   else k_build_bonds<false><<<G, NB_WARPS * 32, 0, st>>>(d);
+  const dim3 gp((unsigned)((d.n + 127) / 128), (unsigned)d.bond_cap);
+  if (d.mixed) k_bond_prime<true><<<gp, 128, 0, st>>>(d);
+  else k_bond_prime<false><<<gp, 128, 0, st>>>(d);
+  k_bond_finish<<<(d.n + 255) / 256, 256, 0, st>>>(d);
   const long long slots = (long long)d.n * d.bond_cap;
   k_bond_sym<<<(unsigned)((slots + 255) / 256), 256, 0, st>>>(d);
 }

@@ -57,23 +57,39 @@ __global__ void k_qeq_setup(Dev d) {
 // y = H x (+ eta x on the diagonal), one warp per row; FP64 form.  In the
 // CG iterations (use_act) a system whose solve has converged is skipped:
 // its half of y is not read again
+// Half a warp per row (rows average several hundred entries): each lane
+// keeps the s and t partial sums of its entries; the two sums are reduced
+// together (the first exchange swaps halves, so every later level is one
+// add per lane for both systems), and lanes 0 and 1 of the row group write
+// y_s and y_t.
+constexpr int SPMV_RW = 16;
+
+__device__ __forceinline__ double pair_sum(double a, double b, int gl) {
+  const bool odd = gl & 1;
+  double v = odd ? b : a;
+  v += __shfl_xor_sync(0xffffffffu, odd ? a : b, 1);
+  for (int off = 2; off < SPMV_RW; off <<= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+  return v;   // group lane 0: sum of a; group lane 1: sum of b
+}
+
 __global__ void __launch_bounds__(256) k_spmv(Dev d, const double2 *__restrict__ x, double2 *__restrict__ y,
                                               int use_act) {
-  const int lane = threadIdx.x & 31;
-  const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  if (i >= d.n) return;
+  const long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const int gl = (int)(tid & (SPMV_RW - 1));
+  const int i = (int)(tid / SPMV_RW);
+  const bool valid = i < d.n;     // no early return: the row group shuffles
   const long long row = (long long)i * d.nb_cap;
-  const int nn = d.n_near[i], nf = d.n_far[i], cap = d.nb_cap;
+  const int nn = valid ? d.n_near[i] : 0, nf = valid ? d.n_far[i] : 0, cap = d.nb_cap;
   const int tot = min(nn + nf, cap);
-  bool on_s = true, on_t = true;
-  if (use_act) {
+  bool on_s = valid, on_t = valid;
+  if (use_act && valid) {
     const double *R = d.red + (long long)d.seg_s[i] * RG_NRED;
     on_s = R[R_ACTIVE] != 0.0;
     on_t = R[R_ACTIVE + 1] != 0.0;
   }
   double as = 0.0, at = 0.0;
   if (on_s && on_t) {
-    for (int p = lane; p < tot; p += 32) {
+    for (int p = gl; p < tot; p += SPMV_RW) {
       const int slot = p < nn ? p : cap - 1 - (p - nn);
       const uint32_t e = d.nbr[row + slot];
       const double h = d.hval[row + slot];
@@ -82,7 +98,7 @@ __global__ void __launch_bounds__(256) k_spmv(Dev d, const double2 *__restrict__
       at = fma(h, xj.y, at);
     }
   } else if (on_s || on_t) {
-    for (int p = lane; p < tot; p += 32) {
+    for (int p = gl; p < tot; p += SPMV_RW) {
       const int slot = p < nn ? p : cap - 1 - (p - nn);
       const uint32_t e = d.nbr[row + slot];
       const double h = d.hval[row + slot];
@@ -94,12 +110,11 @@ __global__ void __launch_bounds__(256) k_spmv(Dev d, const double2 *__restrict__
       as = 0.0;
     }
   }
-  as = warp_sum(as);
-  at = warp_sum(at);
-  if (lane == 0) {
+  const double v = pair_sum(as, at, gl);
+  if (valid && gl < 2) {
     const double eta = d.ff->sbp[d.ts[i]].eta;
-    const double2 xi = x[i];
-    y[i] = make_double2(fma(eta, xi.x, as), fma(eta, xi.y, at));
+    const double *xi = reinterpret_cast<const double *>(x) + 2 * (long long)i;
+    reinterpret_cast<double *>(y)[2 * (long long)i + gl] = fma(eta, xi[gl], v);
   }
 }
 
@@ -199,14 +214,15 @@ __global__ void __launch_bounds__(256) k_spmv32(Dev d, const double2 *__restrict
 // products and sums, so r = b - H x carries no FP32 rounding of x or of
 // the sums (the FP32 SpMV's rounding is what the inner CG iterations see)
 __global__ void __launch_bounds__(256) k_spmv_ref(Dev d, const double2 *__restrict__ x, double2 *__restrict__ y) {
-  const int lane = threadIdx.x & 31;
-  const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  if (i >= d.n) return;
+  const long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const int gl = (int)(tid & (SPMV_RW - 1));
+  const int i = (int)(tid / SPMV_RW);
+  const bool valid = i < d.n;
   const long long row = (long long)i * d.nb_cap;
-  const int nn = d.n_near[i], nf = d.n_far[i], cap = d.nb_cap;
+  const int nn = valid ? d.n_near[i] : 0, nf = valid ? d.n_far[i] : 0, cap = d.nb_cap;
   const int tot = min(nn + nf, cap);
   double as = 0.0, at = 0.0;
-  for (int p = lane; p < tot; p += 32) {
+  for (int p = gl; p < tot; p += SPMV_RW) {
     const int slot = p < nn ? p : cap - 1 - (p - nn);
     const uint32_t e = d.nbr[row + slot];
     const double h = (double)d.hval32[row + slot];
@@ -214,12 +230,11 @@ __global__ void __launch_bounds__(256) k_spmv_ref(Dev d, const double2 *__restri
     as = fma(h, xj.x, as);
     at = fma(h, xj.y, at);
   }
-  as = warp_sum(as);
-  at = warp_sum(at);
-  if (lane == 0) {
+  const double v = pair_sum(as, at, gl);
+  if (valid && gl < 2) {
     const double eta = d.ff->sbp[d.ts[i]].eta;
-    const double2 xi = x[i];
-    y[i] = make_double2(fma(eta, xi.x, as), fma(eta, xi.y, at));
+    const double *xi = reinterpret_cast<const double *>(x) + 2 * (long long)i;
+    reinterpret_cast<double *>(y)[2 * (long long)i + gl] = fma(eta, xi[gl], v);
   }
 }
 
@@ -428,9 +443,10 @@ void launch_qeq_setup(const Dev &d, cudaStream_t st) {
 void launch_qeq_spmv(const Dev &d, cudaStream_t st, const double2 *x, double2 *y, int use_act) {
   const long long threads = (long long)d.n * 32;
   const unsigned G = (unsigned)((threads + 255) / 256);
-  if (!d.mixed) k_spmv<<<G, 256, 0, st>>>(d, x, y, use_act);
+  const unsigned G16 = (unsigned)(((long long)d.n * SPMV_RW + 255) / 256);
+  if (!d.mixed) k_spmv<<<G16, 256, 0, st>>>(d, x, y, use_act);
   else if (x == d.qd) k_spmv32<<<G, 256, 0, st>>>(d, x, y, use_act);
-  else k_spmv_ref<<<G, 256, 0, st>>>(d, x, y);
+  else k_spmv_ref<<<G16, 256, 0, st>>>(d, x, y);
 }
 
 // r = b - H x of the current iterate starts (or, in the mixed form,
@@ -439,7 +455,7 @@ void launch_qeq_cg_init(const Dev &d, cudaStream_t st, double tol, int imax) {
   const int B = 256, G = (d.n + B - 1) / B;
   const int GS = (d.nseg + 127) / 128;
   if (d.mixed) {
-    const long long threads = (long long)d.n * 32;
+    const long long threads = (long long)d.n * SPMV_RW;
     k_spmv_ref<<<(unsigned)((threads + 255) / 256), 256, 0, st>>>(d, d.qx, d.qq);
   } else {
     launch_qeq_spmv(d, st, d.qx, d.qq, 0);

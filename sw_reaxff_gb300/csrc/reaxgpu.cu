@@ -621,6 +621,22 @@ void init_control(const rg_params &p, const ForceField &ff, Control &c) {
   c.inv_swb_nb = 1.0 / c.nonb_cut;
   c.inv_swb_q = 1.0 / p.qeq_swb;
   c.nonb_all_listed = c.nonb_cut2 >= c.list_cut2;
+  c.list_pre2_f = (float)(c.list_cut2 * (1.0 + 1e-5) + 0.05);
+  c.bo_scale_f = (float)(1.0 + c.bo_cut);
+  c.bo_half_f = (float)(0.5 * c.bo_cut);
+  for (int a = 0; a < RG_MAXT; ++a)
+    for (int b = 0; b < RG_MAXT; ++b) {
+      const Tbp &tw = ff.tbp[a][b];
+      Control::BoEst &e = c.bo_est[a][b];
+      e.p_bo1 = (float)tw.p_bo1; e.p_bo2 = (float)tw.p_bo2;
+      e.p_bo3 = (float)tw.p_bo3; e.p_bo4 = (float)tw.p_bo4;
+      e.p_bo5 = (float)tw.p_bo5; e.p_bo6 = (float)tw.p_bo6;
+      e.r_s = (float)tw.r_s; e.r_p = (float)tw.r_p; e.r_pp = (float)tw.r_pp;
+      const Sbp &sa = ff.sbp[a], &sb = ff.sbp[b];
+      e.mask = ((sa.r_s > 0.0 && sb.r_s > 0.0) ? 1 : 0) |
+               ((sa.r_pi > 0.0 && sb.r_pi > 0.0) ? 2 : 0) |
+               ((sa.r_pi_pi > 0.0 && sb.r_pi_pi > 0.0) ? 4 : 0);
+    }
 }
 
 }  // namespace

@@ -103,6 +103,15 @@ struct Control {
   int tab_n;
   double tab_s0, tab_ds, tab_inv_ds, tab_x0;   // tab_x0 = -tab_s0 / tab_ds
   int tab_pair[RG_MAXT][RG_MAXT];   // unordered type pair -> table index
+  // FP32 copies for the prefilters (no FP64 conversions per entry; GB300
+  // runs FP64 at 1/64 of the FP32 rate)
+  float list_pre2_f;   // FP32 pair-list prefilter radius^2: list_cut2 (1 + 1e-5) + 0.05
+  float bo_scale_f;    // 1 + bo_cut (FP32 estimate of BO')
+  float bo_half_f;     // bo_cut / 2
+  struct BoEst {
+    float p_bo1, p_bo2, p_bo3, p_bo4, p_bo5, p_bo6, r_s, r_p, r_pp;
+    int mask;          // 1: sigma, 2: pi, 4: pi-pi bond order terms present
+  } bo_est[RG_MAXT][RG_MAXT];
 };
 
 // Parse an ffield file (restates Read_Force_Field,

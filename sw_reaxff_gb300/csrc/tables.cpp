@@ -12,7 +12,7 @@
 // square root, and (1/r) dE/dr = 2 dE/ds.  Each node holds the function
 // and its s-derivative (the reference's own force expression, halved), and
 // for the force factor its s-derivative by a fourth-order central
-// difference; with 32768 intervals on [0.25, rc^2] A^2 the interpolants
+// difference; with 65536 intervals on [0.25, rc^2] A^2 the interpolants
 // agree with the analytic expressions to ~1e-10 (relative to
 // max(|f|, 1e-4 max|f|); checked here, rg_table_info), inside the 1e-9
 // parity bars.
@@ -110,8 +110,11 @@ int rg_pair_index(int ti, int tj, int nt) {
 }
 
 // Fills nb[npair][n+1][6] = {Ev, Dv, ds Dv', Ec, Dc, ds Dc'} (D = dE/ds,
-// ' = d/ds, ds the node spacing) and hq[npair][n+1][2] = {H, ds H'}, over s
-// in [s0, s1] with n intervals; with
+// ' = d/ds, ds the node spacing) per node and hq[npair][n][4] = the Hermite
+// cubic of H (nodes H, ds H') per interval in the power basis
+// c0 + u (c1 + u (c2 + u c3)), u in [0, 1] (three FMAs and no weights on the
+// device; the same 32 bytes per evaluation), over s in [s0, s1] with n
+// intervals; with
 // check, returns the largest deviation of the interpolants from the
 // analytic functions at 5 interior points of every interval (else 0).
 double rg_build_tables(const ForceField &F, const Control &C, int n, double s0, double s1,
@@ -120,7 +123,7 @@ double rg_build_tables(const ForceField &F, const Control &C, int n, double s0, 
   const int np = nt * (nt + 1) / 2;
   const double ds = (s1 - s0) / n;
   nb.assign((size_t)np * (n + 1) * 6, 0.0);
-  hq.assign((size_t)np * (n + 1) * 2, 0.0);
+  hq.assign((size_t)np * n * 4, 0.0);
   std::vector<std::pair<int, int>> pairs;
   for (int ti = 0; ti < nt; ++ti)
     for (int tj = ti; tj < nt; ++tj) pairs.emplace_back(ti, tj);
@@ -137,6 +140,7 @@ double rg_build_tables(const ForceField &F, const Control &C, int n, double s0, 
       auto dc = [&](double s) { double a, b, c, d; pair_funcs(F, C, ti, tj, std::sqrt(s), &a, &b, &c, &d); return 0.5 * d; };
       auto hf = [&](double s) { return h_func(F, C, ti, tj, std::sqrt(s)); };
       const double h = 1e-4;
+      double hy0 = 0.0, hp0 = 0.0;
       for (int k = 0; k <= n; ++k) {
         const double s = s0 + k * ds;
         double *e = &nb[((size_t)p * (n + 1) + k) * 6];
@@ -146,9 +150,17 @@ double rg_build_tables(const ForceField &F, const Control &C, int n, double s0, 
         e[3] = ecf(s);
         e[4] = dc(s);
         e[5] = ds * deriv(dc, s, h);
-        double *q = &hq[((size_t)p * (n + 1) + k) * 2];
-        q[0] = hf(s);
-        q[1] = ds * deriv(hf, s, h);
+        // H: the Hermite cubic of each interval in the power basis of u
+        const double hy1 = hf(s), hp1 = ds * deriv(hf, s, h);
+        if (k > 0) {
+          double *q = &hq[((size_t)p * n + (k - 1)) * 4];
+          q[0] = hy0;
+          q[1] = hp0;
+          q[2] = 3.0 * (hy1 - hy0) - 2.0 * hp0 - hp1;
+          q[3] = 2.0 * (hy0 - hy1) + hp0 + hp1;
+        }
+        hy0 = hy1;
+        hp0 = hp1;
       }
       if (!check) return;
       // accuracy of the interpolants against the analytic functions:
@@ -158,16 +170,15 @@ double rg_build_tables(const ForceField &F, const Control &C, int n, double s0, 
       double M[5] = {0, 0, 0, 0, 0};
       for (int k = 0; k <= n; ++k) {
         const double *e = &nb[((size_t)p * (n + 1) + k) * 6];
-        const double *q = &hq[((size_t)p * (n + 1) + k) * 2];
         M[0] = std::max(M[0], std::fabs(e[0]));
         M[1] = std::max(M[1], std::fabs(2.0 * e[1]));
         M[2] = std::max(M[2], std::fabs(e[3]));
         M[3] = std::max(M[3], std::fabs(2.0 * e[4]));
-        M[4] = std::max(M[4], std::fabs(q[0]));
+        if (k < n) M[4] = std::max(M[4], std::fabs(hq[((size_t)p * n + k) * 4]));
       }
       for (int k = 0; k < n; ++k) {
         const double *a = &nb[((size_t)p * (n + 1) + k) * 6], *b = a + 6;
-        const double *qa = &hq[((size_t)p * (n + 1) + k) * 2], *qb = qa + 2;
+        const double *qc = &hq[((size_t)p * n + k) * 4];
         for (int m = 1; m <= 5; ++m) {
           const double u = m / 6.0, s = s0 + (k + u) * ds;
           double x[4];
@@ -180,7 +191,7 @@ double rg_build_tables(const ForceField &F, const Control &C, int n, double s0, 
             const double scale = std::max(std::fabs(x[c]), 1e-4 * M[c]);
             if (scale > 0.0) worst = std::max(worst, std::fabs(iv[c] - x[c]) / scale);
           }
-          const double hv = hermite(qa[0], qa[1], qb[0], qb[1], u, 1.0), hx = hf(s);
+          const double hv = ((qc[3] * u + qc[2]) * u + qc[1]) * u + qc[0], hx = hf(s);
           const double hs = std::max(std::fabs(hx), 1e-4 * M[4]);
           if (hs > 0.0) worst = std::max(worst, std::fabs(hv - hx) / hs);
         }

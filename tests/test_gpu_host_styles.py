@@ -108,7 +108,7 @@ def read_bonds(path):
     rows, most = {}, None
     for line in open(path):
         if line.startswith("# Max number of bonds"):
-            most = int(line.split()[6])
+            most = int(line.split()[7])
         elif not line.startswith("#"):
             w = line.split()
             tag, typ, nb = int(w[0]), int(w[1]), int(w[2])

@@ -35,11 +35,20 @@ UNIT = "atom-steps/s"
 DT = 0.25          # fs
 SEED = 7
 
-# FP64 operations per unit of the dominant kernels (per half pair for the
-# nonbonded kernel, per (centre, bond) slot for valence/torsion), counted
-# from ncu's SASS instruction counters on a small case of the same workload
-# (2*dfma + dmul + dadd per unit); profiles/ holds the capture summary.
-FP64_OPS_PER_UNIT = {"nonbonded": None, "valence_torsion": None}
+# Per-unit FP64 FLOP (2*dfma + dmul + dadd, SASS thread-instruction counts)
+# and DRAM bytes (dram__bytes_read + write) of the kernels that can dominate
+# the FP64 step, from one ncu capture of the 52,428-atom case of the same
+# mixture (profiles/fp64_kernels_tabulated_mixture52k.md): per directed pair
+# for the pair-list build, per unordered pair for the nonbonded kernel, per
+# list entry for one QEq SpMV (two systems).  bench.py multiplies them by
+# the units of the measured workload; traffic scales with the units because
+# every kernel streams its list once.
+FP64_PER_UNIT = {
+    # phase: (kernel, unit, FLOP per unit, DRAM bytes per unit)
+    "pair_list+H": ("k_build_nbrs", "directed pair", 26.2, 11.25),
+    "nonbonded": ("k_nonbonded", "unordered pair", 75.7, 11.7),
+    "qeq_spmv": ("k_spmv", "list entry", 4.13, 12.75),
+}
 
 
 def parse():
@@ -348,6 +357,17 @@ def gpu_arm(args):
     g = ReaxGPU(DEFAULT_FFIELD, device=local)
     g.set_system(s)
     g.run(max(args.warmup, 1), DT, energies=False)          # setup + warm-up steps
+    # phase breakdown from a separate, profiled run (events around every
+    # kernel group; the CG iterations then run as plain launches)
+    psteps = max(1, min(args.steps, 2))
+    g.profile(True)
+    g.run(psteps, DT, energies=False)
+    g.synchronize()
+    prof = g.profile_get()
+    g.profile(False)
+    # the roofline kernel: the larger of the two force-step kernels with
+    # ncu-counted FP64 work; the timed steps carry events around it alone
+    dom = max(("pair_list+H", "nonbonded"), key=lambda k: prof[k][0])
     stream = torch.cuda.ExternalStream(g.stream())
     ev0 = torch.cuda.Event(enable_timing=True)
     ev1 = torch.cuda.Event(enable_timing=True)
@@ -357,6 +377,7 @@ def gpu_arm(args):
     torch.cuda.synchronize()
     clocks.start()
     launches0 = g.stats()["kernel_launches"]
+    g.profile(True, phases=[dom])
     ev0.record(stream)
     g.run(args.steps, DT, energies=False)
     ev1.record(stream)
@@ -364,19 +385,13 @@ def gpu_arm(args):
     torch.cuda.synchronize()
     dist.barrier()
     ck = clocks.stop()
+    live = g.profile_get()[dom]
+    g.profile(False)
     st = g.stats()
     launches = st["kernel_launches"] - launches0
     ms = ev0.elapsed_time(ev1)
     tmax = dist.max(ms / 1e3)
     value = n * args.steps * world / tmax
-    # phase breakdown from a separate, profiled run: the event marks between
-    # kernels replace the captured CG graph by plain launches
-    psteps = max(1, min(args.steps, 2))
-    g.profile(True)
-    g.run(psteps, DT, energies=False)
-    g.synchronize()
-    prof = g.profile_get()
-    g.profile(False)
 
     # the mixed-precision form on the same workload (FP32 pair/bond arithmetic
     # and QEq SpMV, FP64 accumulation), timed the same way
@@ -449,28 +464,23 @@ def gpu_arm(args):
             "bars": {"force_rel_rms": 1e-4, "charge_max_abs": 1e-5}}
         gm.close()
 
-    # roofline of the dominant kernel (bound by the FP64 units)
+    # roofline of the dominant force-step kernel (bound by the FP64 units),
+    # its launch time measured with CUDA events in the timed steps
     fp64_peak = measure_fp64_peak(local)
     phases = {k: v for k, v in prof.items() if v[1] > 0}
     tot_ms = sum(v[0] for v in phases.values())
-    dom = max(phases, key=lambda k: phases[k][0])
-    roof = {"kernel": dom, "share": phases[dom][0] / tot_ms if tot_ms else None}
-    avg_ms = phases[dom][0] / phases[dom][1]
-    units = None
-    if dom == "nonbonded":
-        units = st["n_pairs"] / 2
-    elif dom == "valence_torsion":
-        units = st["n_bonds"]
-    ops = FP64_OPS_PER_UNIT.get(dom)
-    if ops and units:
-        ach = ops * units / (avg_ms * 1e-3) / 1e12
-        roof.update({"bound": "fp64", "achieved": ach, "peak": fp64_peak,
-                     "unit": "TFLOP/s", "frac": ach / fp64_peak, "traffic": None,
-                     "peak_source": "FP64 FMA probe measured in this run"})
-    else:
-        roof.update({"bound": "fp64", "achieved": None, "peak": fp64_peak, "unit": "TFLOP/s",
-                     "frac": None, "traffic": None,
-                     "peak_source": "FP64 FMA probe measured in this run"})
+    kname, uname, flop_u, bytes_u = FP64_PER_UNIT[dom]
+    units = st["n_pairs"] / 2 if dom == "nonbonded" else st["n_pairs"]
+    avg_ms = live[0] / max(live[1], 1)
+    ach = flop_u * units / (avg_ms * 1e-3) / 1e12
+    roof = {"kernel": kname, "phase": dom, "share": phases[dom][0] / tot_ms if tot_ms else None,
+            "bound": "fp64", "achieved": ach, "peak": fp64_peak, "unit": "TFLOP/s",
+            "frac": ach / fp64_peak, "traffic": bytes_u * units,
+            "units_per_launch": units, "unit_of_work": uname, "flop_per_unit": flop_u,
+            "avg_launch_ms": avg_ms, "launches_timed": live[1],
+            "peak_source": "FP64 FMA probe measured in this run (MEASURED_PEAKS.json has "
+                           "no FP64 figure); traffic scaled from the 52,428-atom ncu capture",
+            "hbm_gbs_achieved": bytes_u * units / (avg_ms * 1e-3) / 1e9}
     peaks = measured_peaks()
 
     line = {

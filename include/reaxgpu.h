@@ -134,6 +134,18 @@ int rg_set_masses(rg_system *h, const double *mass);
 /* Orthogonal periodic box [0,L0)x[0,L1)x[0,L2). */
 int rg_set_box(rg_system *h, const double *L3);
 
+/* Triclinic boxes (LAMMPS's restricted form, the shipped TATB deck's
+ * `region prism` / data-file `xy xz yz` line): edge vectors a = (lx,0,0),
+ * b = (xy,ly,0), c = (xz,yz,lz) with L = (lx,ly,lz) from rg_set_box or
+ * rg_set_segments and tilt[3*nseg] = (xy, xz, yz) per segment (zeros: back
+ * to orthogonal).  Positions are wrapped into the cell by its fractional
+ * coordinates.  Every width of the cell between opposite faces must be at
+ * least half the pair cutoff.  Replaces the triclinic ghost images that
+ * LAMMPS's Domain/Comm give the reference (outside its tree; the reference
+ * sees them as ghost atoms, pair_reaxc_sunway.cpp:797-831), as the shipped
+ * TATB deck's prism box needs (in.reaxc.lattice). */
+int rg_set_tilt(rg_system *h, const double *tilt);
+
 /* Independent systems in one handle ("segments", for batched evaluation
  * of many small systems): nseg orthogonal periodic boxes (boxes[3*nseg]),
  * segment k holding counts[k] consecutive atoms of the arrays given to
@@ -217,6 +229,12 @@ void *rg_stream(rg_system *h);
 int rg_profile_enable(rg_system *h, int on);
 int rg_profile_get(rg_system *h, int max, char *names, double *ms,
                    long long *count);
+/* Restrict the events to the phases in mask (bit k = phase k of
+ * rg_profile_get's order; default all).  Timing one force-step phase this
+ * way adds two event records per step and keeps the QEq iterations in their
+ * captured CUDA graph (the QEq iteration phases are timed only with plain
+ * launches). */
+int rg_profile_phases(rg_system *h, unsigned mask);
 
 /* Allocation-free QEq (no counterpart in the reference).  For callers that
  * cannot call cudaMalloc when they need charges -- code running under a host

@@ -81,6 +81,7 @@ def _declare(L):
         L.ro_type_param.argtypes = [C.c_void_p, C.c_int, C.c_char_p]
         L.ro_set_system.argtypes = [C.c_void_p, C.c_int, P(C.c_double), P(C.c_double),
                                     P(C.c_int), P(C.c_int), P(C.c_double), P(C.c_double)]
+        L.ro_set_tilt.argtypes = [C.c_void_p, P(C.c_double)]
         L.ro_qeq.argtypes = [C.c_void_p, P(C.c_double), P(C.c_int), P(C.c_int)]
         L.ro_compute.argtypes = [C.c_void_p, P(C.c_double), P(C.c_double)]
         L.ro_run_nve.argtypes = [C.c_void_p, C.c_int, C.c_double, P(C.c_double)]
@@ -112,6 +113,7 @@ class Oracle:
     def __init__(self, ffield: str, reference: bool = False, **control):
         """reference=True loads the build that also carries the reference's
         own host-side code (ref_compute)."""
+        self.h = None
         L = lib(REF_LIB if reference else None)
         ctl = Control()
         L.ro_default_control(C.byref(ctl))
@@ -134,7 +136,10 @@ class Oracle:
     def type_param(self, t, what):
         return self.L.ro_type_param(self.h, t, what.encode())
 
-    def set_system(self, box, x, types, tags=None, q=None, v=None):
+    def set_system(self, box, x, types, tags=None, q=None, v=None, tilt=None):
+        """tilt: (xy, xz, yz) of a triclinic cell, None for orthogonal."""
+        self.L.ro_set_tilt(self.h, None if tilt is None else
+                           _dp(np.ascontiguousarray(tilt, np.float64)))
         x = np.ascontiguousarray(x, np.float64)
         types = np.ascontiguousarray(types, np.int32)
         n = x.shape[0]

@@ -101,6 +101,8 @@ struct ro_ctx {
   double Tap[8];     /* pair taper, Init_Taper reaxc_init_md_sunway.cpp:100 */
   double qTap[8];    /* QEq taper, init_taper fix_qeq_reax_sunway.cpp:458 */
   double L[3];
+  double T[3];       /* tilts xy, xz, yz (0: orthogonal) */
+  int tri;
   /* local atoms */
   int n;
   double *x, *v, *q, *f;
@@ -510,6 +512,55 @@ static double wrap1(double x, double L) {
   return y;
 }
 
+/* Triclinic cell (LAMMPS's restricted form: a = (lx,0,0), b = (xy,ly,0),
+ * c = (xz,yz,lz)); LAMMPS's Domain/Comm give the reference these images as
+ * ghost atoms.  Fractional coordinates by back-substitution and the wrap by
+ * the lattice translation floor(fractional), each operation rounded once
+ * (the device code does the same). */
+static void frac3(const ro_ctx *c, const double *x, double *u) {
+  u[2] = x[2] / c->L[2];
+  u[1] = (x[1] - u[2] * c->T[2]) / c->L[1];
+  u[0] = ((x[0] - u[1] * c->T[0]) - u[2] * c->T[1]) / c->L[0];
+}
+
+static void img_vec(const ro_ctx *c, int sx, int sy, int sz, double *v) {
+  v[0] = ((double)sx * c->L[0] + (double)sy * c->T[0]) + (double)sz * c->T[1];
+  v[1] = (double)sy * c->L[1] + (double)sz * c->T[2];
+  v[2] = (double)sz * c->L[2];
+}
+
+static void wrap_pos(const ro_ctx *c, double *x) {
+  int d;
+  if (!c->tri) {
+    for (d = 0; d < 3; d++) x[d] = wrap1(x[d], c->L[d]);
+    return;
+  }
+  double u[3];
+  frac3(c, x, u);
+  const double kx = floor(u[0]), ky = floor(u[1]), kz = floor(u[2]);
+  x[0] = x[0] - ((kx * c->L[0] + ky * c->T[0]) + kz * c->T[1]);
+  x[1] = x[1] - (ky * c->L[1] + kz * c->T[2]);
+  x[2] = x[2] - kz * c->L[2];
+}
+
+/* widths of the cell between opposite faces */
+static void cell_widths(const ro_ctx *c, double *w) {
+  const double lx = c->L[0], ly = c->L[1], lz = c->L[2];
+  const double xy = c->T[0], xz = c->T[1], yz = c->T[2];
+  w[0] = lx; w[1] = ly; w[2] = lz;
+  if (c->tri) {
+    const double V = lx * ly * lz;
+    w[0] = V / sqrt(ly * lz * ly * lz + xy * lz * xy * lz + (xy * yz - ly * xz) * (xy * yz - ly * xz));
+    w[1] = ly * lz / sqrt(lz * lz + yz * yz);
+  }
+}
+
+void ro_set_tilt(ro_ctx *c, const double *tilt3) {
+  int d;
+  for (d = 0; d < 3; d++) c->T[d] = tilt3 ? tilt3[d] : 0.0;
+  c->tri = c->T[0] != 0.0 || c->T[1] != 0.0 || c->T[2] != 0.0;
+}
+
 int ro_set_system(ro_ctx *c, int n, const double *box3, const double *x,
                   const int *type, const int *tag, const double *q,
                   const double *v) {
@@ -537,7 +588,8 @@ int ro_set_system(ro_ctx *c, int n, const double *box3, const double *x,
   for (d = 0; d < 3; d++) c->L[d] = box3[d];
   for (i = 0; i < n; i++) {
     if (type[i] < 0 || type[i] >= c->ff.ntypes) return -1;
-    for (d = 0; d < 3; d++) c->x[3 * i + d] = wrap1(x[3 * i + d], c->L[d]);
+    for (d = 0; d < 3; d++) c->x[3 * i + d] = x[3 * i + d];
+    wrap_pos(c, c->x + 3 * i);
     c->type[i] = type[i];
     c->tag[i] = tag ? tag[i] : i + 1;
     c->q[i] = q ? q[i] : 0.0;
@@ -586,7 +638,9 @@ static void build_ghosts(ro_ctx *c) {
       fmax(fmax(c->nonb_cut, c->ctl.hbond_cut), 2.0 * c->ctl.bond_cut);
   const double rc = cutmax + c->ctl.skin;
   int kmax[3], d, i, sx, sy, sz, N;
-  for (d = 0; d < 3; d++) kmax[d] = (int)ceil(rc / c->L[d]);
+  double w[3];
+  cell_widths(c, w);
+  for (d = 0; d < 3; d++) kmax[d] = (int)ceil(rc / w[d]);
   ensure_N(c, c->n);
   for (i = 0; i < c->n; i++) {
     for (d = 0; d < 3; d++) c->xe[3 * i + d] = c->x[3 * i + d];
@@ -599,14 +653,27 @@ static void build_ghosts(ro_ctx *c) {
     for (sy = -kmax[1]; sy <= kmax[1]; sy++)
       for (sx = -kmax[0]; sx <= kmax[0]; sx++) {
         if (!sx && !sy && !sz) continue;
+        double iv[3];
+        const int s3[3] = {sx, sy, sz};
+        img_vec(c, sx, sy, sz, iv);
         for (i = 0; i < c->n; i++) {
           double p[3];
-          p[0] = c->x[3 * i + 0] + sx * c->L[0];
-          p[1] = c->x[3 * i + 1] + sy * c->L[1];
-          p[2] = c->x[3 * i + 2] + sz * c->L[2];
           int ok = 1;
-          for (d = 0; d < 3; d++)
-            if (p[d] < -rc || p[d] >= c->L[d] + rc) ok = 0;
+          if (!c->tri) {
+            p[0] = c->x[3 * i + 0] + sx * c->L[0];
+            p[1] = c->x[3 * i + 1] + sy * c->L[1];
+            p[2] = c->x[3 * i + 2] + sz * c->L[2];
+            for (d = 0; d < 3; d++)
+              if (p[d] < -rc || p[d] >= c->L[d] + rc) ok = 0;
+          } else {
+            /* within rc of the cell across each pair of faces */
+            double u[3];
+            frac3(c, c->x + 3 * i, u);
+            for (d = 0; d < 3; d++) {
+              p[d] = c->x[3 * i + d] + iv[d];
+              if (u[d] + s3[d] < -rc / w[d] || u[d] + s3[d] >= 1.0 + rc / w[d]) ok = 0;
+            }
+          }
           if (!ok) continue;
           ensure_N(c, N + 1);
           for (d = 0; d < 3; d++) c->xe[3 * N + d] = p[d];
@@ -1939,7 +2006,7 @@ int ro_run_nve(ro_ctx *c, int nsteps, double dt, double *energies_last) {
         c->v[3 * i + d] += dtfm * c->f[3 * i + d];
         c->x[3 * i + d] += dt * c->v[3 * i + d];
       }
-      for (d = 0; d < 3; d++) c->x[3 * i + d] = wrap1(c->x[3 * i + d], c->L[d]);
+      wrap_pos(c, c->x + 3 * i);
     }
     c->tphase[5] += now_s() - t0;
     ro_qeq(c, NULL, NULL, NULL);

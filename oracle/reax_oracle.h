@@ -61,6 +61,9 @@ double ro_global_param(const ro_ctx *c, int idx);
 /* Set the periodic orthogonal box [0,L) and the local atoms.  type is the
  * 0-based ffield element index, tag the 1-based global id.  Positions are
  * wrapped into the box. */
+/* Tilts (xy, xz, yz) of a triclinic cell for the next ro_set_system (NULL:
+ * orthogonal). */
+void ro_set_tilt(ro_ctx *c, const double *tilt3);
 int ro_set_system(ro_ctx *c, int n, const double *box3, const double *x,
                   const int *type, const int *tag, const double *q,
                   const double *v);

@@ -23,12 +23,13 @@ NENERGY = len(ENERGY_NAMES)
 PREC_FP64, PREC_MIXED = 0, 1
 
 EXPORTED = ["rg_default_params", "rg_create", "rg_destroy", "rg_last_error",
-            "rg_num_types", "rg_element_name", "rg_extract", "rg_set_box",
+            "rg_num_types", "rg_element_name", "rg_extract", "rg_set_box", "rg_set_tilt",
             "rg_set_atoms", "rg_set_atoms_device", "rg_set_positions", "rg_qeq",
             "rg_compute", "rg_nve_initial", "rg_nve_final", "rg_run",
             "rg_get_atoms", "rg_device_arrays", "rg_get_stats", "rg_synchronize",
             "rg_dump_pairs", "rg_dump_bonds", "rg_dump_hbonds", "rg_set_state",
-            "rg_stream", "rg_profile_enable", "rg_profile_get", "rg_measure_fp64_peak",
+            "rg_stream", "rg_profile_enable", "rg_profile_get", "rg_profile_phases",
+            "rg_measure_fp64_peak",
             "rg_qeq_noalloc", "rg_set_masses", "rg_ffield_info", "rg_set_segments",
             "rg_num_segments", "rg_get_energies", "rg_get_segment_iters",
             "rg_get_histories", "rg_set_histories", "rg_table_info", "rg_table_check",
@@ -82,6 +83,7 @@ def load_library(path: str = LIBPATH):
     L.rg_element_name.argtypes = [C.c_void_p, C.c_int, C.c_char_p, C.c_int]
     L.rg_extract.argtypes = [C.c_void_p, C.c_char_p, dp]
     L.rg_set_box.argtypes = [C.c_void_p, dp]
+    L.rg_set_tilt.argtypes = [C.c_void_p, dp]
     L.rg_set_masses.argtypes = [C.c_void_p, dp]
     L.rg_set_segments.argtypes = [C.c_void_p, C.c_int, ip, dp]
     L.rg_num_segments.argtypes = [C.c_void_p]
@@ -116,6 +118,7 @@ def load_library(path: str = LIBPATH):
     L.rg_stream.restype = C.c_void_p
     L.rg_stream.argtypes = [C.c_void_p]
     L.rg_profile_enable.argtypes = [C.c_void_p, C.c_int]
+    L.rg_profile_phases.argtypes = [C.c_void_p, C.c_uint]
     L.rg_profile_get.argtypes = [C.c_void_p, C.c_int, C.c_char_p, dp, P(C.c_longlong)]
     L.rg_measure_fp64_peak.argtypes = [C.c_int, dp]
     L.rg_qeq_noalloc.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, dp,
@@ -223,9 +226,16 @@ class ReaxGPU:
                   "rg_set_atoms")
         self.n = n
 
+    def set_tilt(self, tilt):
+        """Tilts (xy, xz, yz) of a triclinic box, one row per segment."""
+        tl = np.ascontiguousarray(tilt, np.float64).reshape(-1)
+        self._chk(self.L.rg_set_tilt(self.h, _dp(tl)), "rg_set_tilt")
+
     def set_system(self, system):
         """Load a sw_reaxff_gb300.systems.System."""
         self.set_box(system.box)
+        if system.triclinic:
+            self.set_tilt(system.tilt)
         self.set_atoms(system.x, system.types(self.elements), system.tag, None, system.v)
 
     def set_systems(self, systems_list):
@@ -236,6 +246,9 @@ class ReaxGPU:
         boxes = np.ascontiguousarray(np.stack([s.box for s in systems_list]), np.float64)
         self._chk(self.L.rg_set_segments(self.h, len(systems_list), _ip(counts), _dp(boxes)),
                   "rg_set_segments")
+        if any(s.triclinic for s in systems_list):
+            self.set_tilt(np.stack([np.zeros(3) if s.tilt is None else np.asarray(s.tilt, float)
+                                    for s in systems_list]))
         x = np.concatenate([s.x for s in systems_list])
         types = np.concatenate([s.types(self.elements) for s in systems_list])
         tags = np.concatenate([s.tag for s in systems_list])
@@ -341,7 +354,15 @@ class ReaxGPU:
     def stream(self) -> int:
         return self.L.rg_stream(self.h)
 
-    def profile(self, on: bool):
+    PHASES = ("bin_sort", "pair_list+H", "bond_list", "bond_orders", "atom_energy", "hbonds",
+              "valence_torsion", "nonbonded", "dbond_forces", "force_out", "qeq_setup",
+              "qeq_spmv", "qeq_vector", "qeq_finish", "nve")
+
+    def profile(self, on: bool, phases=None):
+        """Phase timing with CUDA events; phases (names of PHASES) limits
+        the events to those phases (None: all)."""
+        mask = 0xFFFFFFFF if phases is None else sum(1 << self.PHASES.index(p) for p in phases)
+        self._chk(self.L.rg_profile_phases(self.h, mask), "rg_profile_phases")
         self._chk(self.L.rg_profile_enable(self.h, 1 if on else 0), "rg_profile_enable")
 
     def profile_get(self) -> dict:

@@ -379,7 +379,7 @@ __global__ void __launch_bounds__(256) k_hbonds(Dev d, int eflag) {
     const int nb = min(d.nbonds[j], d.bond_cap);
     const int nh = min(d.nhb[j], d.hb_cap);
     const double4 xj = d.xs[j];
-    const double *L = d.seg[d.seg_s[j]].L;
+    const SegGeom &g = d.seg[d.seg_s[j]];
     double *fC = d.fC;
     double fjx = 0, fjy = 0, fjz = 0;
     for (int q = 0; q < nb; ++q) {
@@ -403,9 +403,7 @@ __global__ void __launch_bounds__(256) k_hbonds(Dev d, int eflag) {
         img_unpack((int)(ek & 255u), &sx, &sy, &sz);
         const double4 xk = d.xs[k];
         double dk64[3];
-        dk64[0] = __dsub_rn(img_shift(xk.x, sx, L[0]), xj.x);
-        dk64[1] = __dsub_rn(img_shift(xk.y, sy, L[1]), xj.y);
-        dk64[2] = __dsub_rn(img_shift(xk.z, sz, L[2]), xj.z);
+        disp64(g, xk, xj, sx, sy, sz, dk64[0], dk64[1], dk64[2]);
         const double r64 = __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(dk64[0], dk64[0]),
                                                           __dmul_rn(dk64[1], dk64[1])),
                                                 __dmul_rn(dk64[2], dk64[2])));

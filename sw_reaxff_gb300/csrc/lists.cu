@@ -44,6 +44,40 @@ __device__ __forceinline__ int cell_of(double x, double w, int nc) {
   return c < 0 ? 0 : (c >= nc ? nc - 1 : c);
 }
 
+__device__ __forceinline__ int frac_cell(double u, int nc) {
+  int c = (int)floor(u * nc);
+  return c < 0 ? 0 : (c >= nc ? nc - 1 : c);
+}
+
+// cell of a wrapped position: Cartesian cells of an orthogonal segment,
+// cells of the fractional coordinates of a triclinic one
+__device__ __forceinline__ void cell3(const SegGeom &g, double x, double y, double z, int &cx,
+                                      int &cy, int &cz) {
+  if (!g.tri) {
+    cx = cell_of(x, g.cellw[0], g.nc[0]);
+    cy = cell_of(y, g.cellw[1], g.nc[1]);
+    cz = cell_of(z, g.cellw[2], g.nc[2]);
+  } else {
+    double u, v, w;
+    frac3(g, x, y, z, u, v, w);
+    cx = frac_cell(u, g.nc[0]);
+    cy = frac_cell(v, g.nc[1]);
+    cz = frac_cell(w, g.nc[2]);
+  }
+}
+
+// triclinic wrap: subtract the lattice translation floor(fractional
+// coordinates), rounded per operation like the oracle
+__device__ __forceinline__ void wrap_tri(const SegGeom &g, double &x, double &y, double &z) {
+  double u, v, w;
+  frac3(g, x, y, z, u, v, w);
+  const double kx = floor(u), ky = floor(v), kz = floor(w);
+  x = __dsub_rn(x, __dadd_rn(__dadd_rn(__dmul_rn(kx, g.L[0]), __dmul_rn(ky, g.tilt[0])),
+                             __dmul_rn(kz, g.tilt[1])));
+  y = __dsub_rn(y, __dadd_rn(__dmul_rn(ky, g.L[1]), __dmul_rn(kz, g.tilt[2])));
+  z = __dsub_rn(z, __dmul_rn(kz, g.L[2]));
+}
+
 // -------------------------------------------------------------------
 // binning and sort
 
@@ -51,15 +85,19 @@ __global__ void k_cell_assign(Dev d) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= d.n) return;
   const SegGeom &g = d.seg[d.seg_o[i]];
-  double x = wrap1(d.x_o[3 * i + 0], g.L[0]);
-  double y = wrap1(d.x_o[3 * i + 1], g.L[1]);
-  double z = wrap1(d.x_o[3 * i + 2], g.L[2]);
+  double x = d.x_o[3 * i + 0], y = d.x_o[3 * i + 1], z = d.x_o[3 * i + 2];
+  if (!g.tri) {
+    x = wrap1(x, g.L[0]);
+    y = wrap1(y, g.L[1]);
+    z = wrap1(z, g.L[2]);
+  } else {
+    wrap_tri(g, x, y, z);
+  }
   d.x_o[3 * i + 0] = x;
   d.x_o[3 * i + 1] = y;
   d.x_o[3 * i + 2] = z;
-  int cx = cell_of(x, g.cellw[0], g.nc[0]);
-  int cy = cell_of(y, g.cellw[1], g.nc[1]);
-  int cz = cell_of(z, g.cellw[2], g.nc[2]);
+  int cx, cy, cz;
+  cell3(g, x, y, z, cx, cy, cz);
   int c = g.cell0 + (cz * g.nc[1] + cy) * g.nc[0] + cx;
   d.cell_o[i] = c;
   atomicAdd(&d.cell_count[c], 1);
@@ -175,11 +213,9 @@ struct NbrQueue {
 // finish 32 queued candidates (lanes with q < cnt hold one each)
 // exact (FP64, explicitly rounded) squared distance of a queued entry
 __device__ __forceinline__ double exact_d2(const Dev &d, int j, int sx, int sy, int sz,
-                                          const double4 &xi, const double *L) {
-  const double4 xj = d.xs[j];
-  const double dx = __dsub_rn(img_shift(xj.x, sx, L[0]), xi.x);
-  const double dy = __dsub_rn(img_shift(xj.y, sy, L[1]), xi.y);
-  const double dz = __dsub_rn(img_shift(xj.z, sz, L[2]), xi.z);
+                                          const double4 &xi, const SegGeom &g) {
+  double dx, dy, dz;
+  disp64(g, d.xs[j], xi, sx, sy, sz, dx, dy, dz);
   return __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
 }
 
@@ -205,19 +241,18 @@ __device__ __forceinline__ void nbr_flush(const Dev &d, const Control &C, const 
     img_unpack(img, &sx, &sy, &sz);
     if (MIXED) {
       const float4 hj = d.xf[j], lj = d.xl[j];
-      const float dx = df_disp(hj.x, lj.x, xif.x, xil.x, sx, g.Lh[0], g.Ll[0]);
-      const float dy = df_disp(hj.y, lj.y, xif.y, xil.y, sy, g.Lh[1], g.Ll[1]);
-      const float dz = df_disp(hj.z, lj.z, xif.z, xil.z, sz, g.Lh[2], g.Ll[2]);
+      float dx, dy, dz;
+      disp32(g, hj, lj, xif, xil, sx, sy, sz, dx, dy, dz);
       d2f = dx * dx + dy * dy + dz * dz;
       const float lc2 = (float)C.list_cut2;
       if (d2f <= lc2 * (1.f - MARGIN32)) in = true;
       else if (d2f > lc2 * (1.f + MARGIN32)) in = false;
-      else in = exact_d2(d, j, sx, sy, sz, xi, L) <= C.list_cut2;
+      else in = exact_d2(d, j, sx, sy, sz, xi, g) <= C.list_cut2;
       // near part: conservative (the bond pass tests its own cutoffs)
       const float nc = (float)C.near_cut;
       near = d2f <= nc * nc * (1.f + MARGIN32);
     } else {
-      d2 = exact_d2(d, j, sx, sy, sz, xi, L);
+      d2 = exact_d2(d, j, sx, sy, sz, xi, g);
       in = d2 <= C.list_cut2;
       if (in) {
         if (d2 <= C.near_cut2_lo) near = true;
@@ -310,9 +345,8 @@ __global__ void __launch_bounds__(NB_WARPS * 32) k_build_nbrs(Dev d) {
   const SegGeom &g = d.seg[d.seg_s[i]];
   const double L[3] = {g.L[0], g.L[1], g.L[2]};
   const int ncx = g.nc[0], ncy = g.nc[1], ncz = g.nc[2], S = g.S;
-  const int cx = cell_of(xi.x, g.cellw[0], ncx);
-  const int cy = cell_of(xi.y, g.cellw[1], ncy);
-  const int cz = cell_of(xi.z, g.cellw[2], ncz);
+  int cx, cy, cz;
+  cell3(g, xi.x, xi.y, xi.z, cx, cy, cz);
   const long long row = (long long)i * d.nb_cap;
   const int cap = d.nb_cap;
   const int nx = ncx;
@@ -337,10 +371,10 @@ __global__ void __launch_bounds__(NB_WARPS * 32) k_build_nbrs(Dev d) {
         const int beg = d.cell_start[rowcell + rx];
         const int end = d.cell_start[rowcell + rx + len];
         ox += len;
-        // (float)(s L) exactly: |s| <= 2 scales the rounded edge exactly
-        const float shxf = (float)sx * g.Lh[0];
-        const float shyf = (float)sy * g.Lh[1];
-        const float shzf = (float)sz * g.Lh[2];
+        // orthogonal: (float)(s L) exactly (|s| <= 2 scales the rounded edge
+        // exactly); triclinic: the FP32 translation
+        float shxf, shyf, shzf;
+        img_vec32(g, sx, sy, sz, shxf, shyf, shzf);
         const bool self_img = (sx == 0 && sy == 0 && sz == 0);
         const int img = img_pack(sx, sy, sz);
         for (int base = beg; base < end; base += 32) {
@@ -396,7 +430,8 @@ __global__ void __launch_bounds__(NB_WARPS * 32) k_build_nbrs(Dev d) {
 // bond list with uncorrected bond orders, and H-bond partners
 //
 // One warp per atom i over the near part of its row.  H-bond partners are
-// decided from the exact distance directly.  Bond candidates (d <= bond_cut)
+// decided from the FP32 (hi, lo) distance away from hbond_cut and from the
+// exact distance near it.  Bond candidates (d <= bond_cut)
 // whose FP32 estimate of BO' is above half of bo_cut (FP32 errors are ~1e-4
 // relative here) are written to the bond slots of i; k_bond_prime then
 // evaluates BO' and the exact BO' >= bo_cut decision one thread per
@@ -422,6 +457,31 @@ __device__ __forceinline__ void bo_prime(const Sbp &si, const Sbp &sj, const Tbp
   }
 }
 
+// FP64 form: (d / r)^p as exp(p (log d - log r)) with log d once per bond
+// and log r from the control block (a few 1e-16 relative from pow, far
+// inside the 1e-10 bond-order bars; the reference's live form is a
+// polynomial pow/exp on the CPEs)
+__device__ __forceinline__ void bo_prime64(const Control &C, int ti, int tj, const Sbp &si,
+                                           const Sbp &sj, const Tbp &tw, double dist,
+                                           double &BOs, double &BOpi, double &BOpi2,
+                                           double &C12, double &C34, double &C56) {
+  BOs = BOpi = BOpi2 = C12 = C34 = C56 = 0;
+  const double ld = log(dist);
+  const double *lr = C.ln_r[ti][tj];
+  if (si.r_s > 0.0 && sj.r_s > 0.0) {
+    C12 = tw.p_bo1 * exp(tw.p_bo2 * (ld - lr[0]));
+    BOs = (1.0 + C.bo_cut) * exp(C12);
+  }
+  if (si.r_pi > 0.0 && sj.r_pi > 0.0) {
+    C34 = tw.p_bo3 * exp(tw.p_bo4 * (ld - lr[1]));
+    BOpi = exp(C34);
+  }
+  if (si.r_pi_pi > 0.0 && sj.r_pi_pi > 0.0) {
+    C56 = tw.p_bo5 * exp(tw.p_bo6 * (ld - lr[2]));
+    BOpi2 = exp(C56);
+  }
+}
+
 // BO' of the bond candidates: one thread per candidate slot (blockIdx.y =
 // slot), so the FP64 pow/exp run with full warps instead of the few lanes a
 // per-atom warp has candidates for.  Accepted entries get their bond
@@ -439,8 +499,37 @@ __global__ void k_bond_prime(Dev d) {
   const long long s = (long long)k * n + i;
   const long long S3 = (long long)d.bond_cap * n;
   const uint32_t e = d.b_nbr[s];
-  const double dist = d.b_d[s];
-  const int ti = d.ts[i], tj = d.ts[(int)(e >> 8)];
+  const int j = (int)(e >> 8);
+  int sx, sy, sz;
+  img_unpack((int)(e & 255u), &sx, &sy, &sz);
+  const SegGeom &g = d.seg[d.seg_s[i]];
+  // the bond distance: exact FP64 (FP64 form; the mixed form within
+  // MARGIN32 of bond_cut), else the FP32 (hi, lo) displacement
+  double dist, dx, dy, dz;
+  bool exact = !MIXED;
+  if (MIXED) {
+    const float4 hi = d.xf[i], li = d.xl[i], hj = d.xf[j], lj = d.xl[j];
+    float ex, ey, ez;
+    disp32(g, hj, lj, hi, li, sx, sy, sz, ex, ey, ez);
+    const float df = sqrtf(ex * ex + ey * ey + ez * ez);
+    if (fabsf(df - C.bond_cut_f) <= MARGIN32 * C.bond_cut_f) {
+      exact = true;
+    } else if (df > C.bond_cut_f) {
+      d.b_d[s] = -1.0;
+      return;
+    } else {
+      dx = ex; dy = ey; dz = ez; dist = df;
+    }
+  }
+  if (exact) {
+    disp64(g, d.xs[j], d.xs[i], sx, sy, sz, dx, dy, dz);
+    dist = __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz)));
+    if (!(dist <= C.bond_cut)) {
+      d.b_d[s] = -1.0;
+      return;
+    }
+  }
+  const int ti = d.ts[i], tj = d.ts[j];
   const Sbp &si = F.sbp[ti], &sj = F.sbp[tj];
   const Tbp &tw = F.tbp[ti][tj];
   double BOs, BOpi, BOpi2, C12, C34, C56;
@@ -454,13 +543,13 @@ __global__ void k_bond_prime(Dev d) {
     const double BO32 = (double)(a + b + c);
     if (fabs(BO32 - C.bo_cut) <= 1e-4 * C.bo_cut) {
       double x0, x1, x2, y0, y1, y2;
-      bo_prime<double>(si, sj, tw, dist, C.bo_cut, x0, x1, x2, y0, y1, y2);
+      bo_prime64(C, ti, tj, si, sj, tw, dist, x0, x1, x2, y0, y1, y2);
       isb = (x0 + x1 + x2) >= C.bo_cut;
     } else {
       isb = BO32 >= C.bo_cut;
     }
   } else {
-    bo_prime<double>(si, sj, tw, dist, C.bo_cut, BOs, BOpi, BOpi2, C12, C34, C56);
+    bo_prime64(C, ti, tj, si, sj, tw, dist, BOs, BOpi, BOpi2, C12, C34, C56);
     isb = (BOs + BOpi + BOpi2) >= C.bo_cut;
   }
   if (!isb) {
@@ -471,13 +560,14 @@ __global__ void k_bond_prime(Dev d) {
   const double Cs = tw.p_bo2 * C12 / r2;
   const double Cpi = tw.p_bo4 * C34 / r2;
   const double Cpi2 = tw.p_bo6 * C56 / r2;
-  const double dx = d.b_dx[s], dy = d.b_dy[s], dz = d.b_dz[s];
-  const double g = -(BOs * Cs + BOpi * Cpi + BOpi2 * Cpi2);
+  d.b_d[s] = dist;
+  d.b_dx[s] = dx; d.b_dy[s] = dy; d.b_dz[s] = dz;
+  const double gb = -(BOs * Cs + BOpi * Cpi + BOpi2 * Cpi2);
   d.b_BO[s] = BOs + BOpi + BOpi2 - C.bo_cut;
   d.b_BOs[s] = BOs - C.bo_cut;
   d.b_BOpi[s] = BOpi;
   d.b_BOpi2[s] = BOpi2;
-  d.b_dBOp[s] = g * dx; d.b_dBOp[S3 + s] = g * dy; d.b_dBOp[2 * S3 + s] = g * dz;
+  d.b_dBOp[s] = gb * dx; d.b_dBOp[S3 + s] = gb * dy; d.b_dBOp[2 * S3 + s] = gb * dz;
   const double api = -BOpi * Cpi, api2 = -BOpi2 * Cpi2;
   d.b_dlnpi[s] = api * dx; d.b_dlnpi[S3 + s] = api * dy; d.b_dlnpi[2 * S3 + s] = api * dz;
   d.b_dlnpi2[s] = api2 * dx; d.b_dlnpi2[S3 + s] = api2 * dy; d.b_dlnpi2[2 * S3 + s] = api2 * dz;
@@ -557,56 +647,45 @@ __global__ void __launch_bounds__(NB_WARPS * 32) k_build_bonds(Dev d) {
       const int p = base + lane;
       bool ish = false, cand = false;
       uint32_t e = 0;
-      double dist = 0, dx = 0, dy = 0, dz = 0;
       if (p < nn) {
         e = d.nbr[row + p];
         const int j = (int)(e >> 8);
         int sx, sy, sz;
         img_unpack((int)(e & 255u), &sx, &sy, &sz);
         const float4 xjf = d.xf[j];
-        const float fx = xjf.x + (float)sx * g.Lh[0] - xif.x;
-        const float fy = xjf.y + (float)sy * g.Lh[1] - xif.y;
-        const float fz = xjf.z + (float)sz * g.Lh[2] - xif.z;
+        float vx, vy, vz;
+        img_vec32(g, sx, sy, sz, vx, vy, vz);
+        const float fx = xjf.x + vx - xif.x;
+        const float fy = xjf.y + vy - xif.y;
+        const float fz = xjf.z + vz - xif.z;
         if (fx * fx + fy * fy + fz * fz <= rpre2) {
           const int tj = __float_as_int(xjf.w);
           const Sbp &sj = F.sbp[tj];
           const bool hb_rel = ihb && sj.p_hbond == 2;
-          // FP32 distance from the (hi, lo) positions decides away from the
-          // cutoffs; the FP64 form takes the exact distance for every
-          // possible bond (its value is stored), the mixed form only within
-          // MARGIN32 of a cutoff
+          // FP32 distance from the (hi, lo) positions (a few FP32 ulps of
+          // the displacement) decides away from the cutoffs; the exact
+          // distance only within MARGIN32 of the H-bond cutoff.  Possible
+          // bonds are decided exactly (and their values computed) by
+          // k_bond_prime.
           const float4 lj = d.xl[j];
-          const float ex = df_disp(xjf.x, lj.x, xif.x, xil.x, sx, g.Lh[0], g.Ll[0]);
-          const float ey = df_disp(xjf.y, lj.y, xif.y, xil.y, sy, g.Lh[1], g.Ll[1]);
-          const float ez = df_disp(xjf.z, lj.z, xif.z, xil.z, sz, g.Lh[2], g.Ll[2]);
+          float ex, ey, ez;
+          disp32(g, xjf, lj, xif, xil, sx, sy, sz, ex, ey, ez);
           const float df = sqrtf(ex * ex + ey * ey + ez * ez);
           const float bc = C.bond_cut_f, hc = C.hbond_cut_f;
-          const bool near_b = fabsf(df - bc) <= MARGIN32 * bc;
-          const bool near_h = hb_rel && fabsf(df - hc) <= MARGIN32 * hc;
-          const bool exact = MIXED ? (near_b || near_h) : (df <= bc * (1.f + MARGIN32) || near_h);
-          bool isb;
-          if (exact) {
-            const double4 xj = d.xs[j];
-            dx = __dsub_rn(img_shift(xj.x, sx, L[0]), xi.x);
-            dy = __dsub_rn(img_shift(xj.y, sy, L[1]), xi.y);
-            dz = __dsub_rn(img_shift(xj.z, sz, L[2]), xi.z);
-            const double d2 = __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
-            dist = __dsqrt_rn(d2);
-            ish = hb_rel && dist <= C.hbond_cut;
-            isb = dist <= C.bond_cut;
+          if (hb_rel && fabsf(df - hc) <= MARGIN32 * hc) {
+            double ax, ay, az;
+            disp64(g, d.xs[j], xi, sx, sy, sz, ax, ay, az);
+            const double d2 = __dadd_rn(__dadd_rn(__dmul_rn(ax, ax), __dmul_rn(ay, ay)), __dmul_rn(az, az));
+            ish = __dsqrt_rn(d2) <= C.hbond_cut;
           } else {
-            // decided in FP32; values kept only for the (mixed-form) bonds
             ish = hb_rel && df <= hc;
-            isb = df <= bc;
-            if (isb) { dx = ex; dy = ey; dz = ez; dist = df; }
           }
-          if (isb) {
+          if (df <= bc * (1.f + MARGIN32)) {
             const Control::BoEst &be = C.bo_est[ti][tj];
-            const float dd = exact ? (float)dist : df;
             float est = 0.f;
-            if (be.mask & 1) est += C.bo_scale_f * expf(be.p_bo1 * powf(dd / be.r_s, be.p_bo2));
-            if (be.mask & 2) est += expf(be.p_bo3 * powf(dd / be.r_p, be.p_bo4));
-            if (be.mask & 4) est += expf(be.p_bo5 * powf(dd / be.r_pp, be.p_bo6));
+            if (be.mask & 1) est += C.bo_scale_f * expf(be.p_bo1 * powf(df / be.r_s, be.p_bo2));
+            if (be.mask & 2) est += expf(be.p_bo3 * powf(df / be.r_p, be.p_bo4));
+            if (be.mask & 4) est += expf(be.p_bo5 * powf(df / be.r_pp, be.p_bo6));
             cand = est >= bo_half;
           }
         }
@@ -622,12 +701,7 @@ __global__ void __launch_bounds__(NB_WARPS * 32) k_build_bonds(Dev d) {
       const unsigned mc = __ballot_sync(FULL, cand);
       if (cand) {
         const int k = nb + __popc(mc & lanemask_lt());
-        if (k < d.bond_cap) {
-          const long long s = (long long)k * n + i;
-          d.b_nbr[s] = e;
-          d.b_d[s] = dist;
-          d.b_dx[s] = dx; d.b_dy[s] = dy; d.b_dz[s] = dz;
-        }
+        if (k < d.bond_cap) d.b_nbr[(long long)k * n + i] = e;
       }
       nb += __popc(mc);
     }

@@ -89,9 +89,8 @@ __device__ __forceinline__ void pair_terms(const Dev &d, const ForceField &F, co
     // holds exactly the pairs within max(nonb_cut, swb), so only a QEq
     // taper radius above nonb_cut needs a test here (FP64 near the cutoff)
     const float4 hj = d.xf[j], lj = d.xl[j];
-    const float fx = df_disp(hj.x, lj.x, xif.x, xil.x, sx, g.Lh[0], g.Ll[0]);
-    const float fy = df_disp(hj.y, lj.y, xif.y, xil.y, sy, g.Lh[1], g.Ll[1]);
-    const float fz = df_disp(hj.z, lj.z, xif.z, xil.z, sz, g.Lh[2], g.Ll[2]);
+    float fx, fy, fz;
+    disp32(g, hj, lj, xif, xil, sx, sy, sz, fx, fy, fz);
     const float d2f = fx * fx + fy * fy + fz * fz;
     if (!C.nonb_all_listed) {
       const float nc2 = (float)C.nonb_cut2;
@@ -99,10 +98,8 @@ __device__ __forceinline__ void pair_terms(const Dev &d, const ForceField &F, co
       if (d2f <= nc2 * (1.f - 1e-5f)) out = false;
       else if (d2f > nc2 * (1.f + 1e-5f)) out = true;
       else {
-        const double4 xj = d.xs[j];
-        const double ex = __dsub_rn(img_shift(xj.x, sx, L[0]), xi.x);
-        const double ey = __dsub_rn(img_shift(xj.y, sy, L[1]), xi.y);
-        const double ez = __dsub_rn(img_shift(xj.z, sz, L[2]), xi.z);
+        double ex, ey, ez;
+        disp64(g, d.xs[j], xi, sx, sy, sz, ex, ey, ez);
         out = __dadd_rn(__dadd_rn(__dmul_rn(ex, ex), __dmul_rn(ey, ey)), __dmul_rn(ez, ez)) > C.nonb_cut2;
       }
       if (out) return;
@@ -114,9 +111,7 @@ __device__ __forceinline__ void pair_terms(const Dev &d, const ForceField &F, co
     // same rounding as the pair-list membership test
     const double4 xj = d.xs[j];
     qj = xj.w;
-    dx = __dsub_rn(img_shift(xj.x, sx, L[0]), xi.x);
-    dy = __dsub_rn(img_shift(xj.y, sy, L[1]), xi.y);
-    dz = __dsub_rn(img_shift(xj.z, sz, L[2]), xi.z);
+    disp64(g, xj, xi, sx, sy, sz, dx, dy, dz);
     const double d2x = __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
     if (d2x > C.nonb_cut2) { dx = dy = dz = 0.0; return; }
     d2 = (R)d2x;

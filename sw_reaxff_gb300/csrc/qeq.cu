@@ -449,14 +449,27 @@ void launch_qeq_spmv(const Dev &d, cudaStream_t st, const double2 *x, double2 *y
   else k_spmv_ref<<<G16, 256, 0, st>>>(d, x, y);
 }
 
+// the split FP32 pair copy of x that k_spmv32 reads
+__global__ void k_split_x(Dev d, const double2 *__restrict__ x) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < d.n) d.qd32[i] = split4(x[i]);
+}
+
 // r = b - H x of the current iterate starts (or, in the mixed form,
-// restarts) the pipelined CG; the mixed form computes it with FP64 sums
-void launch_qeq_cg_init(const Dev &d, cudaStream_t st, double tol, int imax) {
+// restarts) the pipelined CG.  The mixed form's restarts (refine) take the
+// residual with FP64 products and sums (iterative refinement); its first
+// pass, whose iterate the refinement checks anyway, the compensated FP32
+// SpMV of the iterations.
+void launch_qeq_cg_init(const Dev &d, cudaStream_t st, double tol, int imax, bool refine) {
   const int B = 256, G = (d.n + B - 1) / B;
   const int GS = (d.nseg + 127) / 128;
-  if (d.mixed) {
+  if (d.mixed && refine) {
     const long long threads = (long long)d.n * SPMV_RW;
     k_spmv_ref<<<(unsigned)((threads + 255) / 256), 256, 0, st>>>(d, d.qx, d.qq);
+  } else if (d.mixed) {
+    k_split_x<<<G, B, 0, st>>>(d, d.qx);
+    const unsigned G32 = (unsigned)(((long long)d.n * 32 + 255) / 256);
+    k_spmv32<<<G32, 256, 0, st>>>(d, d.qx, d.qq, 0);
   } else {
     launch_qeq_spmv(d, st, d.qx, d.qq, 0);
   }

@@ -31,6 +31,7 @@ static const char *kPhaseNames[PH_N] = {
 
 struct Prof {
   bool on = false;
+  unsigned mask = ~0u;       // phases that get events (bit k: phase k)
   std::vector<cudaEvent_t> pool;
   std::vector<int> phase;   // phase of each recorded event (-1 = gap)
   size_t used = 0;
@@ -123,12 +124,18 @@ namespace {
 
 struct Scope {
   rg_system *h;
-  Scope(rg_system *hh, int ph, int kernels) : h(hh) {
-    h->prof.mark(h->st, ph);
+  bool timed;
+  Scope(rg_system *hh, int ph, int kernels) : h(hh), timed((hh->prof.mask >> ph) & 1u) {
+    if (timed) h->prof.mark(h->st, ph);
     h->launches += kernels;
   }
-  ~Scope() { h->prof.mark(h->st, -1); }
+  ~Scope() {
+    if (timed) h->prof.mark(h->st, -1);
+  }
 };
+
+// the CG iterations run as plain launches only when their phases are timed
+constexpr unsigned kCgPhases = (1u << PH_QSPMV) | (1u << PH_QVEC);
 
 int fail(rg_system *h, int code, const std::string &msg) {
   if (h) h->err = msg;
@@ -169,13 +176,29 @@ int setup_cells(rg_system *h) {
   long long ncell = 0;
   for (SegGeom &g : h->segs) {
     g.S = S;
+    g.tri = (g.tilt[0] != 0.0 || g.tilt[1] != 0.0 || g.tilt[2] != 0.0);
+    // widths of the cell between opposite faces: the box edges, or for a
+    // triclinic cell V / |b x c|, V / |c x a|, V / |a x b|.  Cells (in
+    // fractional coordinates when triclinic) at least rc/S wide across
+    // make the +-S stencil reach every partner within rc.
+    const double lx = g.L[0], ly = g.L[1], lz = g.L[2];
+    const double xy = g.tilt[0], xz = g.tilt[1], yz = g.tilt[2];
+    double w[3] = {lx, ly, lz};
+    if (g.tri) {
+      const double V = lx * ly * lz;
+      w[0] = V / std::sqrt(ly * lz * ly * lz + xy * lz * xy * lz +
+                           (xy * yz - ly * xz) * (xy * yz - ly * xz));
+      w[1] = ly * lz / std::sqrt(lz * lz + yz * yz);
+      w[2] = lz;
+    }
     long long nseg_cells = 1;
     for (int k = 0; k < 3; ++k) {
       g.Lh[k] = (float)g.L[k];
       g.Ll[k] = (float)(g.L[k] - (double)g.Lh[k]);
-      if (g.L[k] < rc / S)
-        return fail(h, RG_E_ARG, "box edge shorter than half the pair cutoff is not supported");
-      int nc = (int)std::floor(g.L[k] * S / (rc * (1.0 + 1e-9)));
+      g.Th[k] = (float)g.tilt[k];
+      if (w[k] < rc / S)
+        return fail(h, RG_E_ARG, "box width shorter than half the pair cutoff is not supported");
+      int nc = (int)std::floor(w[k] * S / (rc * (1.0 + 1e-9)));
       nc = std::max(nc, 1);
       g.nc[k] = nc;
       g.cellw[k] = g.L[k] / nc;
@@ -526,9 +549,9 @@ int do_qeq(rg_system *h, int *its, int *itt) {
   const double tol = h->p.qeq_tol;
   const int imax = h->p.qeq_imax;
   {
-    Scope sc(h, PH_QSETUP, 9);
+    Scope sc(h, PH_QSETUP, 9 + (d.mixed ? 1 : 0));
     launch_qeq_setup(d, h->st);
-    launch_qeq_cg_init(d, h->st, tol, imax);
+    launch_qeq_cg_init(d, h->st, tol, imax, false);
   }
   // iterate; poll the number of segments with an active solve every few
   // iterations.  The mixed form then restarts the CG from its iterate with
@@ -546,8 +569,8 @@ int do_qeq(rg_system *h, int *its, int *itt) {
       CK(cudaStreamSynchronize(h->st));
       if (active == 0) break;
       if (done_iters > imax + 8) return fail(h, RG_E_NUMERIC, "QEq iteration control lost");
-      if (h->use_graphs && !h->prof.on) {
-        // phase profiling needs the per-kernel event marks: plain launches
+      if (h->use_graphs && !(h->prof.on && (h->prof.mask & kCgPhases))) {
+        // timing the CG phases needs the per-kernel event marks: plain launches
         if (!h->cg_exec || std::memcmp(&h->cg_dev, &d, sizeof(Dev)) != 0) {
           int rc2 = capture_cg(h, chunk);
           if (rc2) return rc2;
@@ -571,7 +594,7 @@ int do_qeq(rg_system *h, int *its, int *itt) {
     CK(cudaStreamSynchronize(h->st));
     for (size_t k = 0; k < it.size(); ++k) tot[k] += std::max(0, (int)it[k] - (refines ? 1 : 0));
     if (!d.mixed || refines >= RG_MAX_REFINE) break;
-    { Scope sc(h, PH_QSETUP, 8); launch_qeq_cg_init(d, h->st, tol, imax); }
+    { Scope sc(h, PH_QSETUP, 8); launch_qeq_cg_init(d, h->st, tol, imax, true); }
     ++refines;
     CK(cudaMemcpyAsync(&active, d.n_active, sizeof(int), cudaMemcpyDeviceToHost, h->st));
     CK(cudaStreamSynchronize(h->st));
@@ -632,6 +655,9 @@ void init_control(const rg_params &p, const ForceField &ff, Control &c) {
       e.p_bo3 = (float)tw.p_bo3; e.p_bo4 = (float)tw.p_bo4;
       e.p_bo5 = (float)tw.p_bo5; e.p_bo6 = (float)tw.p_bo6;
       e.r_s = (float)tw.r_s; e.r_p = (float)tw.r_p; e.r_pp = (float)tw.r_pp;
+      c.ln_r[a][b][0] = tw.r_s > 0.0 ? std::log(tw.r_s) : 0.0;
+      c.ln_r[a][b][1] = tw.r_p > 0.0 ? std::log(tw.r_p) : 0.0;
+      c.ln_r[a][b][2] = tw.r_pp > 0.0 ? std::log(tw.r_pp) : 0.0;
       const Sbp &sa = ff.sbp[a], &sb = ff.sbp[b];
       e.mask = ((sa.r_s > 0.0 && sb.r_s > 0.0) ? 1 : 0) |
                ((sa.r_pi > 0.0 && sb.r_pi > 0.0) ? 2 : 0) |
@@ -908,6 +934,19 @@ int rg_set_segments(rg_system *h, int nseg, const int *counts, const double *box
   return RG_OK;
 }
 
+int rg_set_tilt(rg_system *h, const double *tilt) {
+  if (!h || !tilt) return RG_E_ARG;
+  if (!h->have_box) return fail(h, RG_E_STATE, "set the box or the segments first");
+  for (size_t g = 0; g < h->segs.size(); ++g)
+    for (int k = 0; k < 3; ++k) {
+      if (!std::isfinite(tilt[3 * g + k])) return fail(h, RG_E_ARG, "tilt must be finite");
+      h->segs[g].tilt[k] = tilt[3 * g + k];
+    }
+  h->lists_valid = false;
+  h->forces_valid = false;
+  return RG_OK;
+}
+
 int rg_num_segments(const rg_system *h) { return h ? (int)h->segs.size() : RG_E_ARG; }
 
 int rg_get_energies(rg_system *h, double *e) {
@@ -1108,6 +1147,13 @@ int rg_profile_enable(rg_system *h, int on) {
   if (on) h->prof.reset();
   else h->prof.resolve();
   h->prof.on = on != 0;
+  return RG_OK;
+}
+
+int rg_profile_phases(rg_system *h, unsigned mask) {
+  if (!h) return RG_E_ARG;
+  h->prof.resolve();
+  h->prof.mask = mask;
   return RG_OK;
 }
 

@@ -68,12 +68,17 @@ struct ForceField {
   double nve_mass[RG_MAXT];   // integrator masses (default: sbp mass)
 };
 
-// Geometry of one segment (periodic orthogonal box and its cells).
+// Geometry of one segment: a periodic box with edge vectors a = (lx, 0, 0),
+// b = (xy, ly, 0), c = (xz, yz, lz) (LAMMPS's restricted triclinic form;
+// orthogonal when the tilts are zero) and its cells.
 struct SegGeom {
-  double L[3];        // box edges
+  double L[3];        // lx, ly, lz
+  double tilt[3];     // xy, xz, yz
+  int tri;            // a tilt is nonzero: fractional binning and wrap
   float Lh[3], Ll[3]; // L as an unevaluated FP32 pair (hi + lo)
-  double cellw[3];    // cell edges (L / nc)
-  int nc[3];          // cells per dimension
+  float Th[3];        // tilts in FP32 (prefilter shifts only)
+  double cellw[3];    // orthogonal: cell edges (L / nc)
+  int nc[3];          // cells per dimension (fractional axes when tri)
   int S;              // stencil half-width (cells)
   int cell0;          // first global cell index of the segment
   int atom0, natoms;  // original-order atom range
@@ -108,6 +113,9 @@ struct Control {
   float list_pre2_f;   // FP32 pair-list prefilter radius^2: list_cut2 (1 + 1e-5) + 0.05
   float bo_scale_f;    // 1 + bo_cut (FP32 estimate of BO')
   float bo_half_f;     // bo_cut / 2
+  // log r_s, log r_pi, log r_pipi per type pair: the FP64 BO' powers as
+  // exp(p (log d - log r)) with one log per bond
+  double ln_r[RG_MAXT][RG_MAXT][3];
   struct BoEst {
     float p_bo1, p_bo2, p_bo3, p_bo4, p_bo5, p_bo6, r_s, r_p, r_pp;
     int mask;          // 1: sigma, 2: pi, 4: pi-pi bond order terms present
@@ -305,6 +313,50 @@ __device__ __forceinline__ double img_shift(double x, int s, double L) {
   return s ? __dadd_rn(x, s * L) : x;
 }
 
+// Lattice translation sx a + sy b + sz c of a segment, rounded per
+// operation in this order (the oracle builds its periodic images the same
+// way); for an orthogonal box it is (sx lx, sy ly, sz lz) exactly.
+__device__ __forceinline__ void img_vec(const SegGeom &g, int sx, int sy, int sz, double &vx,
+                                        double &vy, double &vz) {
+  vx = __dadd_rn(__dadd_rn(__dmul_rn((double)sx, g.L[0]), __dmul_rn((double)sy, g.tilt[0])),
+                 __dmul_rn((double)sz, g.tilt[1]));
+  vy = __dadd_rn(__dmul_rn((double)sy, g.L[1]), __dmul_rn((double)sz, g.tilt[2]));
+  vz = __dmul_rn((double)sz, g.L[2]);
+}
+
+// exact displacement (x_j + image) - x_i of the membership tests
+__device__ __forceinline__ void disp64(const SegGeom &g, const double4 &xj, const double4 &xi,
+                                       int sx, int sy, int sz, double &dx, double &dy,
+                                       double &dz) {
+  if (!g.tri) {
+    dx = __dsub_rn(img_shift(xj.x, sx, g.L[0]), xi.x);
+    dy = __dsub_rn(img_shift(xj.y, sy, g.L[1]), xi.y);
+    dz = __dsub_rn(img_shift(xj.z, sz, g.L[2]), xi.z);
+  } else if (sx | sy | sz) {
+    double vx, vy, vz;
+    img_vec(g, sx, sy, sz, vx, vy, vz);
+    dx = __dsub_rn(__dadd_rn(xj.x, vx), xi.x);
+    dy = __dsub_rn(__dadd_rn(xj.y, vy), xi.y);
+    dz = __dsub_rn(__dadd_rn(xj.z, vz), xi.z);
+  } else {
+    dx = __dsub_rn(xj.x, xi.x);
+    dy = __dsub_rn(xj.y, xi.y);
+    dz = __dsub_rn(xj.z, xi.z);
+  }
+}
+
+// FP32 image shift for the distance prefilters (which carry a margin)
+__device__ __forceinline__ void img_vec32(const SegGeom &g, int sx, int sy, int sz, float &vx,
+                                          float &vy, float &vz) {
+  vx = (float)sx * g.Lh[0];
+  vy = (float)sy * g.Lh[1];
+  vz = (float)sz * g.Lh[2];
+  if (g.tri) {
+    vx += (float)sy * g.Th[0] + (float)sz * g.Th[1];
+    vy += (float)sz * g.Th[2];
+  }
+}
+
 // Mixed form: displacement x_j + s L - x_i from positions and box edges
 // held as FP32 (hi, lo) pairs.  The hi parts combine first (exact or
 // rounded once at the result's magnitude), so the error is a few FP32 ulps
@@ -314,6 +366,42 @@ __device__ __forceinline__ float df_disp(float hj, float lj, float hi, float li,
   const float a = __fsub_rn(__fmaf_rn((float)s, Lh, hj), hi);
   const float b = __fsub_rn(__fmaf_rn((float)s, Ll, lj), li);
   return __fadd_rn(a, b);
+}
+
+// the same with a shift given as an FP32 pair (triclinic images)
+__device__ __forceinline__ float df_disp2(float hj, float lj, float hi, float li, float vh,
+                                          float vl) {
+  const float a = __fsub_rn(__fadd_rn(hj, vh), hi);
+  const float b = __fsub_rn(__fadd_rn(lj, vl), li);
+  return __fadd_rn(a, b);
+}
+
+// mixed-form displacement (x_j + image) - x_i; a triclinic image is formed
+// in FP64 and split into an FP32 pair
+__device__ __forceinline__ void disp32(const SegGeom &g, const float4 &hj, const float4 &lj,
+                                       const float4 &hi, const float4 &li, int sx, int sy,
+                                       int sz, float &ex, float &ey, float &ez) {
+  if (!g.tri || !(sx | sy | sz)) {
+    ex = df_disp(hj.x, lj.x, hi.x, li.x, sx, g.Lh[0], g.Ll[0]);
+    ey = df_disp(hj.y, lj.y, hi.y, li.y, sy, g.Lh[1], g.Ll[1]);
+    ez = df_disp(hj.z, lj.z, hi.z, li.z, sz, g.Lh[2], g.Ll[2]);
+  } else {
+    double vx, vy, vz;
+    img_vec(g, sx, sy, sz, vx, vy, vz);
+    const float hx = __double2float_rn(vx), hy = __double2float_rn(vy), hz = __double2float_rn(vz);
+    ex = df_disp2(hj.x, lj.x, hi.x, li.x, hx, __double2float_rn(vx - (double)hx));
+    ey = df_disp2(hj.y, lj.y, hi.y, li.y, hy, __double2float_rn(vy - (double)hy));
+    ez = df_disp2(hj.z, lj.z, hi.z, li.z, hz, __double2float_rn(vz - (double)hz));
+  }
+}
+
+// fractional coordinates of a position in a triclinic segment by
+// back-substitution (no precomputed inverse), rounded per operation
+__device__ __forceinline__ void frac3(const SegGeom &g, double x, double y, double z, double &u,
+                                      double &v, double &w) {
+  w = __ddiv_rn(z, g.L[2]);
+  v = __ddiv_rn(__dsub_rn(y, __dmul_rn(w, g.tilt[2])), g.L[1]);
+  u = __ddiv_rn(__dsub_rn(__dsub_rn(x, __dmul_rn(v, g.tilt[0])), __dmul_rn(w, g.tilt[1])), g.L[0]);
 }
 
 // cubic Hermite interpolation in the FP64 tables: for s, the interval k,
@@ -377,7 +465,7 @@ void launch_check_finite(const double *a, long long count, int *flag, cudaStream
 // QEq
 void launch_qeq_setup(const Dev &d, cudaStream_t st);
 void launch_qeq_spmv(const Dev &d, cudaStream_t st, const double2 *x, double2 *y, int use_act);
-void launch_qeq_cg_init(const Dev &d, cudaStream_t st, double tol, int imax);
+void launch_qeq_cg_init(const Dev &d, cudaStream_t st, double tol, int imax, bool refine);
 void launch_qeq_cg_A(const Dev &d, cudaStream_t st);
 void launch_qeq_cg_C(const Dev &d, cudaStream_t st);
 void launch_qeq_finish(const Dev &d, cudaStream_t st);

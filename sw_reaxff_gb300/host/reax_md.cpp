@@ -10,13 +10,24 @@
 //
 //   units real | atom_style charge | boundary p p p | read_data FILE |
 //   mass I M | pair_style ... | pair_coeff ... | fix ID all STYLE ... |
-//   (STYLE: qeq/reax, nve, reax/c/bonds and their /sunway, /gb300 names)
+//   (STYLE: qeq/reax, nve, reax/c/bonds, reax/c/species and their
+//   /sunway, /gb300 names)
 //   timestep DT | thermo N | run N |
 //   write_dump all custom FILE COLS (id type q x y z vx vy vz fx fy fz)
 //   neighbor / neigh_modify / thermo_style / thermo_modify: accepted, no effect
 //
+// and what the shipped TATB deck (in.reaxc.lattice) builds its crystal
+// with: variable NAME index|equal ..., $x / ${name} substitution, "&" line
+// continuation, lattice custom SCALE a1 .. a2 .. a3 .. basis .., region ID
+// prism|block ... [units box], create_box N REGION, create_atoms TYPE box
+// [basis I T ...]; read_data also takes the "xy xz yz" tilt line.  Index
+// variables can be set on the command line: reax_md -var S 2 -in deck.
+//
 // Errors print "ERROR: <message>" and exit 1, as LAMMPS does.
 #include <algorithm>
+#include <array>
+#include <cmath>
+#include <cstdlib>
 #include <cctype>
 #include <cstdio>
 #include <cstring>
@@ -86,8 +97,10 @@ void read_data(const std::string &path, reaxgb::Atom &A) {
     } else if (w.size() >= 4 && w[2] == "ylo" && w[3] == "yhi") {
       A.boxlo[1] = std::stod(w[0]); A.boxhi[1] = std::stod(w[1]); have_box[1] = true;
     } else if (w.size() >= 6 && w[3] == "xy") {
-      if (std::stod(w[0]) != 0.0 || std::stod(w[1]) != 0.0 || std::stod(w[2]) != 0.0)
-        throw Error("reax_md: triclinic boxes are not supported");
+      A.xy = std::stod(w[0]);
+      A.xz = std::stod(w[1]);
+      A.yz = std::stod(w[2]);
+      A.triclinic = 1;
     } else if (w.size() >= 4 && w[2] == "zlo" && w[3] == "zhi") {
       A.boxlo[2] = std::stod(w[0]); A.boxhi[2] = std::stod(w[1]); have_box[2] = true;
     } else if (w.size() >= 3 && (w[1] == "bonds" || w[1] == "angles" || w[1] == "dihedrals" ||
@@ -158,13 +171,303 @@ void read_data(const std::string &path, reaxgb::Atom &A) {
   if (!have_atoms) throw Error("No Atoms section in data file");
 }
 
+// ---------------------------------------------------------------- input
+// LAMMPS input-script mechanics (input.cpp, variable.cpp): "&" joins lines,
+// "#" starts a comment, $x and ${name} are replaced by the variable's value
+// before the command is parsed; index variables hold a string, equal
+// variables a formula evaluated when referenced.
+struct Variables {
+  std::map<std::string, std::pair<std::string, std::string>> v;   // name -> (style, text)
+  std::map<std::string, std::string> cmdline;                      // -var NAME VALUE
+
+  double eval(const std::string &f) const {
+    size_t pos = 0;
+    const double r = expr(f, pos);
+    skip(f, pos);
+    if (pos != f.size()) throw Error("Invalid syntax in variable formula: " + f);
+    return r;
+  }
+  std::string value(const std::string &name) const {
+    auto it = v.find(name);
+    if (it == v.end()) throw Error("Substitution for illegal variable " + name);
+    if (it->second.first == "index") return it->second.second;
+    char buf[64];
+    std::snprintf(buf, sizeof buf, "%.15g", eval(it->second.second));
+    return buf;
+  }
+  std::string substitute(const std::string &line) const {
+    std::string out;
+    for (size_t i = 0; i < line.size(); ++i) {
+      if (line[i] != '$' || i + 1 >= line.size()) {
+        out += line[i];
+        continue;
+      }
+      std::string name;
+      if (line[i + 1] == '{') {
+        const size_t e = line.find('}', i + 2);
+        if (e == std::string::npos) throw Error("Invalid variable name in: " + line);
+        name = line.substr(i + 2, e - i - 2);
+        i = e;
+      } else {
+        name = line.substr(i + 1, 1);
+        i += 1;
+      }
+      out += value(name);
+    }
+    return out;
+  }
+
+ private:
+  static void skip(const std::string &f, size_t &p) {
+    while (p < f.size() && std::isspace((unsigned char)f[p])) ++p;
+  }
+  double expr(const std::string &f, size_t &p) const {
+    double a = term(f, p);
+    for (;;) {
+      skip(f, p);
+      if (p < f.size() && (f[p] == '+' || f[p] == '-')) {
+        const char op = f[p++];
+        const double b = term(f, p);
+        a = op == '+' ? a + b : a - b;
+      } else {
+        return a;
+      }
+    }
+  }
+  double term(const std::string &f, size_t &p) const {
+    double a = power(f, p);
+    for (;;) {
+      skip(f, p);
+      if (p < f.size() && (f[p] == '*' || f[p] == '/')) {
+        const char op = f[p++];
+        const double b = power(f, p);
+        if (op == '/' && b == 0.0) throw Error("Divide by 0 in variable formula");
+        a = op == '*' ? a * b : a / b;
+      } else {
+        return a;
+      }
+    }
+  }
+  double power(const std::string &f, size_t &p) const {
+    const double a = unary(f, p);
+    skip(f, p);
+    if (p < f.size() && f[p] == '^') {
+      ++p;
+      return std::pow(a, power(f, p));
+    }
+    return a;
+  }
+  double unary(const std::string &f, size_t &p) const {
+    skip(f, p);
+    if (p < f.size() && (f[p] == '-' || f[p] == '+')) {
+      const char op = f[p++];
+      const double a = unary(f, p);
+      return op == '-' ? -a : a;
+    }
+    if (p < f.size() && f[p] == '(') {
+      ++p;
+      const double a = expr(f, p);
+      skip(f, p);
+      if (p >= f.size() || f[p] != ')') throw Error("Invalid syntax in variable formula: " + f);
+      ++p;
+      return a;
+    }
+    if (f.compare(p, 2, "v_") == 0) {
+      size_t e = p + 2;
+      while (e < f.size() && (std::isalnum((unsigned char)f[e]) || f[e] == '_')) ++e;
+      const std::string name = f.substr(p + 2, e - p - 2);
+      p = e;
+      return std::stod(value(name));
+    }
+    const char *s = f.c_str() + p;
+    char *end = nullptr;
+    const double a = std::strtod(s, &end);
+    if (end == s) throw Error("Invalid syntax in variable formula: " + f);
+    p += (size_t)(end - s);
+    return a;
+  }
+};
+
+// lattice custom SCALE a1 x y z a2 x y z a3 x y z basis u v w ... (lattice.cpp)
+struct Lattice {
+  double scale = 1.0;
+  double a[3][3] = {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
+  std::vector<std::array<double, 3>> basis;
+};
+
+// region ID prism xlo xhi ylo yhi zlo zhi xy xz yz | block xlo xhi ylo yhi zlo zhi
+struct Region {
+  double lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
+  double xy = 0, xz = 0, yz = 0;
+  bool prism = false;
+};
+
+double num(const std::string &s) {
+  char *end = nullptr;
+  const double v = std::strtod(s.c_str(), &end);
+  if (end == s.c_str()) throw Error("Expected floating point parameter instead of " + s);
+  return v;
+}
+
+Lattice make_lattice(const std::vector<std::string> &w) {
+  if (w.size() < 3 || w[1] != "custom") throw Error("reax_md supports lattice custom only");
+  Lattice L;
+  L.scale = num(w[2]);
+  for (size_t k = 3; k < w.size();) {
+    if ((w[k] == "a1" || w[k] == "a2" || w[k] == "a3") && k + 3 < w.size()) {
+      const int r = w[k][1] - '1';
+      for (int c = 0; c < 3; ++c) L.a[r][c] = num(w[k + 1 + c]);
+      k += 4;
+    } else if (w[k] == "basis" && k + 3 < w.size()) {
+      L.basis.push_back({num(w[k + 1]), num(w[k + 2]), num(w[k + 3])});
+      k += 4;
+    } else {
+      throw Error("Illegal lattice command");
+    }
+  }
+  if (L.basis.empty()) throw Error("No basis atoms in lattice");
+  return L;
+}
+
+Region make_region(const std::vector<std::string> &w) {
+  Region R;
+  if (w.size() >= 9 && w[2] == "prism") {
+    for (int c = 0; c < 3; ++c) {
+      R.lo[c] = num(w[3 + 2 * c]);
+      R.hi[c] = num(w[4 + 2 * c]);
+    }
+    if (w.size() < 12) throw Error("Illegal region prism command");
+    R.xy = num(w[9]);
+    R.xz = num(w[10]);
+    R.yz = num(w[11]);
+    R.prism = true;
+  } else if (w.size() >= 9 && w[2] == "block") {
+    for (int c = 0; c < 3; ++c) {
+      R.lo[c] = num(w[3 + 2 * c]);
+      R.hi[c] = num(w[4 + 2 * c]);
+    }
+  } else {
+    throw Error("reax_md supports region prism|block with units box");
+  }
+  for (size_t k = R.prism ? 12 : 9; k < w.size(); k += 2)
+    if (w[k] != "units" || k + 1 >= w.size() || w[k + 1] != "box")
+      throw Error("reax_md supports region ... units box only");
+  return R;
+}
+
+void create_box(const std::vector<std::string> &w, const std::map<std::string, Region> &regions,
+                reaxgb::Atom &A) {
+  if (w.size() < 3) throw Error("Illegal create_box command");
+  auto it = regions.find(w[2]);
+  if (it == regions.end()) throw Error("Create_box region ID does not exist");
+  const Region &R = it->second;
+  A.ntypes = std::stoi(w[1]);
+  if (A.ntypes <= 0) throw Error("Illegal create_box command");
+  for (int c = 0; c < 3; ++c) {
+    A.boxlo[c] = R.lo[c];
+    A.boxhi[c] = R.hi[c];
+  }
+  A.triclinic = R.prism ? 1 : 0;
+  A.xy = R.xy;
+  A.xz = R.xz;
+  A.yz = R.yz;
+  A.nlocal = 0;
+  A.x.clear(); A.v.clear(); A.f.clear(); A.q.clear(); A.type.clear(); A.tag.clear();
+  A.mass.assign(A.ntypes + 1, 0.0);
+}
+
+// create_atoms TYPE box [basis I T ...] on a lattice (CreateAtoms::
+// add_lattice in LAMMPS): lattice points i + b over the lattice-coordinate
+// bounding box of the simulation box, kept when their fractional box
+// coordinates lie in [-eps, 1 - 2 eps) (eps = 1e-6, the periodic-edge rule
+// of one process), in k, j, i, basis order; tags continue from the last.
+void create_atoms(const std::vector<std::string> &w, const Lattice *lat, reaxgb::Atom &A) {
+  if (w.size() < 3 || w[2] != "box") throw Error("reax_md supports create_atoms TYPE box");
+  if (!lat) throw Error("Cannot create atoms with undefined lattice");
+  if (A.ntypes <= 0) throw Error("Create_atoms command before simulation box is defined");
+  const int deftype = std::stoi(w[1]);
+  std::vector<int> btype(lat->basis.size(), deftype);
+  for (size_t k = 3; k < w.size(); k += 3) {
+    if (w[k] != "basis" || k + 2 >= w.size()) throw Error("Illegal create_atoms command");
+    const int b = std::stoi(w[k + 1]), t = std::stoi(w[k + 2]);
+    if (b < 1 || b > (int)btype.size() || t < 1 || t > A.ntypes)
+      throw Error("Illegal create_atoms command");
+    btype[b - 1] = t;
+  }
+  if (deftype < 1 || deftype > A.ntypes) throw Error("Invalid atom type in create_atoms command");
+  const double lx = A.boxhi[0] - A.boxlo[0], ly = A.boxhi[1] - A.boxlo[1],
+               lz = A.boxhi[2] - A.boxlo[2];
+  const double xy = A.xy, xz = A.xz, yz = A.yz;
+  // lattice matrix (columns a1, a2, a3 times the scale) and its inverse
+  double M[3][3];
+  for (int r = 0; r < 3; ++r)
+    for (int c = 0; c < 3; ++c) M[r][c] = lat->scale * lat->a[c][r];
+  const double det = M[0][0] * (M[1][1] * M[2][2] - M[1][2] * M[2][1]) -
+                     M[0][1] * (M[1][0] * M[2][2] - M[1][2] * M[2][0]) +
+                     M[0][2] * (M[1][0] * M[2][1] - M[1][1] * M[2][0]);
+  if (det == 0.0) throw Error("Degenerate lattice primitive vectors");
+  double Mi[3][3];
+  Mi[0][0] = (M[1][1] * M[2][2] - M[1][2] * M[2][1]) / det;
+  Mi[0][1] = (M[0][2] * M[2][1] - M[0][1] * M[2][2]) / det;
+  Mi[0][2] = (M[0][1] * M[1][2] - M[0][2] * M[1][1]) / det;
+  Mi[1][0] = (M[1][2] * M[2][0] - M[1][0] * M[2][2]) / det;
+  Mi[1][1] = (M[0][0] * M[2][2] - M[0][2] * M[2][0]) / det;
+  Mi[1][2] = (M[0][2] * M[1][0] - M[0][0] * M[1][2]) / det;
+  Mi[2][0] = (M[1][0] * M[2][1] - M[1][1] * M[2][0]) / det;
+  Mi[2][1] = (M[0][1] * M[2][0] - M[0][0] * M[2][1]) / det;
+  Mi[2][2] = (M[0][0] * M[1][1] - M[0][1] * M[1][0]) / det;
+  // lattice-coordinate range of the box's eight corners
+  double lmin[3] = {1e300, 1e300, 1e300}, lmax[3] = {-1e300, -1e300, -1e300};
+  for (int cz = 0; cz < 2; ++cz)
+    for (int cy = 0; cy < 2; ++cy)
+      for (int cx = 0; cx < 2; ++cx) {
+        const double p[3] = {cx * lx + cy * xy + cz * xz, cy * ly + cz * yz, cz * lz};
+        for (int r = 0; r < 3; ++r) {
+          const double u = Mi[r][0] * p[0] + Mi[r][1] * p[1] + Mi[r][2] * p[2];
+          lmin[r] = std::min(lmin[r], u);
+          lmax[r] = std::max(lmax[r], u);
+        }
+      }
+  int lo[3], hi[3];
+  for (int r = 0; r < 3; ++r) {
+    lo[r] = (int)std::floor(lmin[r]) - 1;
+    hi[r] = (int)std::ceil(lmax[r]) + 1;
+  }
+  const double eps = 1e-6;
+  int next_tag = 0;
+  for (int t : A.tag) next_tag = std::max(next_tag, t);
+  for (int k = lo[2]; k <= hi[2]; ++k)
+    for (int j = lo[1]; j <= hi[1]; ++j)
+      for (int i = lo[0]; i <= hi[0]; ++i)
+        for (size_t m = 0; m < lat->basis.size(); ++m) {
+          const double u[3] = {i + lat->basis[m][0], j + lat->basis[m][1], k + lat->basis[m][2]};
+          double p[3];
+          for (int r = 0; r < 3; ++r) p[r] = M[r][0] * u[0] + M[r][1] * u[1] + M[r][2] * u[2];
+          // fractional coordinates in the box (origin boxlo)
+          const double fz = p[2] / lz;
+          const double fy = (p[1] - fz * yz) / ly;
+          const double fx = (p[0] - fy * xy - fz * xz) / lx;
+          if (fx < -eps || fx >= 1.0 - 2 * eps || fy < -eps || fy >= 1.0 - 2 * eps ||
+              fz < -eps || fz >= 1.0 - 2 * eps)
+            continue;
+          for (int r = 0; r < 3; ++r) A.x.push_back(p[r] + A.boxlo[r]);
+          for (int r = 0; r < 3; ++r) A.v.push_back(0.0);
+          for (int r = 0; r < 3; ++r) A.f.push_back(0.0);
+          A.q.push_back(0.0);
+          A.type.push_back(btype[m]);
+          A.tag.push_back(++next_tag);
+          ++A.nlocal;
+        }
+}
+
 void write_dump(const std::string &path, const std::vector<std::string> &cols,
-                const reaxgb::Atom &A, const reaxgb::PairReaxCGB300 &pair, long long step) {
+                const reaxgb::Atom &A, const reaxgb::PairReaxCGB300 *pair, long long step) {
   std::FILE *fp = std::fopen(path.c_str(), "w");
   if (!fp) throw Error("Cannot open dump file " + path);
   std::fprintf(fp, "# step %lld\n# pvector", step);
-  for (double e : pair.pvector) std::fprintf(fp, " %.17g", e);
-  std::fprintf(fp, "\n# eng_vdwl %.17g eng_coul %.17g\n#", pair.eng_vdwl, pair.eng_coul);
+  for (int k = 0; k < 14; ++k) std::fprintf(fp, " %.17g", pair ? pair->pvector[k] : 0.0);
+  std::fprintf(fp, "\n# eng_vdwl %.17g eng_coul %.17g\n#", pair ? pair->eng_vdwl : 0.0,
+               pair ? pair->eng_coul : 0.0);
   for (auto &c : cols) std::fprintf(fp, " %s", c.c_str());
   std::fprintf(fp, "\n");
   std::vector<int> order(A.nlocal);
@@ -203,24 +506,65 @@ void print_thermo(const reaxgb::Verlet &V, void *ctx) {
               T.qeq ? T.qeq->matvecs : 0);
 }
 
-int run_deck(std::istream &in) {
+int run_deck(std::istream &in, const std::map<std::string, std::string> &cmdvars) {
+  Variables vars;
+  vars.cmdline = cmdvars;
+  for (auto &kv : cmdvars) vars.v[kv.first] = {"index", kv.second};
+  std::unique_ptr<Lattice> lattice;
+  std::map<std::string, Region> regions;
   reaxgb::Atom atom;
   reaxgb::Update update;
   std::unique_ptr<reaxgb::PairReaxCGB300> pair;
   std::unique_ptr<reaxgb::FixQEqReaxGB300> qeq;
   std::unique_ptr<reaxgb::FixNVEGB300> nve;
   std::unique_ptr<reaxgb::Verlet> verlet;
-  std::vector<std::unique_ptr<reaxgb::FixReaxCBondsGB300>> bonds;
+  std::vector<std::unique_ptr<reaxgb::StepFix>> bonds;   // bond and species output
   bool have_data = false, setup_done = false;
   int thermo_every = 0;
-  std::string line;
+  std::string line, raw;
   int lineno = 0;
-  while (std::getline(in, line)) {
+  while (std::getline(in, raw)) {
     ++lineno;
+    // "&" at the end continues the command on the next line
+    line = raw;
+    while (true) {
+      size_t e = line.find_last_not_of(" \t\r");
+      if (e == std::string::npos || line[e] != '&') break;
+      line.erase(e);
+      if (!std::getline(in, raw)) break;
+      ++lineno;
+      line += " " + raw;
+    }
+    const size_t hash = line.find('#');
+    if (hash != std::string::npos) line.erase(hash);
+    line = vars.substitute(line);
     const auto w = split(line);
     if (w.empty()) continue;
     const std::string &cmd = w[0];
-    if (cmd == "units") {
+    if (cmd == "variable") {
+      if (w.size() < 4) throw Error("Illegal variable command");
+      if (w[2] == "index") {
+        // a command-line value wins (LAMMPS -var)
+        if (!vars.cmdline.count(w[1])) vars.v[w[1]] = {"index", w[3]};
+      } else if (w[2] == "equal") {
+        std::string f;
+        for (size_t k = 3; k < w.size(); ++k) f += w[k];
+        vars.v[w[1]] = {"equal", f};
+      } else {
+        throw Error("reax_md supports index and equal variables");
+      }
+    } else if (cmd == "lattice") {
+      lattice.reset(new Lattice(make_lattice(w)));
+    } else if (cmd == "region") {
+      if (w.size() < 3) throw Error("Illegal region command");
+      regions[w[1]] = make_region(w);
+    } else if (cmd == "create_box") {
+      if (have_data) throw Error("Cannot create_box after simulation box is defined");
+      create_box(w, regions, atom);
+      have_data = true;
+    } else if (cmd == "create_atoms") {
+      create_atoms(w, lattice.get(), atom);
+    } else if (cmd == "units") {
       if (w.size() != 2 || w[1] != "real") throw Error("reax/c/gb300 requires units real");
     } else if (cmd == "atom_style") {
       if (w.size() != 2 || w[1] != "charge") throw Error("reax_md supports atom_style charge");
@@ -258,6 +602,9 @@ int run_deck(std::istream &in) {
         nve.reset(new reaxgb::FixNVEGB300(pair.get(), &update, a.n(), a.v()));
       } else if (is_style(w[3], {"reax/c/bonds", "reax/c/bonds/sunway", "reax/c/bonds/gb300"})) {
         bonds.emplace_back(new reaxgb::FixReaxCBondsGB300(pair.get(), &atom, &update, a.n(), a.v()));
+      } else if (is_style(w[3], {"reax/c/species", "reax/c/species/sunway",
+                                 "reax/c/species/gb300"})) {
+        bonds.emplace_back(new reaxgb::FixReaxCSpeciesGB300(pair.get(), &atom, &update, a.n(), a.v()));
       } else {
         throw Error("Unrecognized fix style " + w[3]);
       }
@@ -291,13 +638,14 @@ int run_deck(std::istream &in) {
                   print_thermo, &T);
     } else if (cmd == "write_dump") {
       if (w.size() < 5 || w[1] != "all" || w[2] != "custom") throw Error("Illegal write_dump command");
-      if (!pair || !setup_done) throw Error("write_dump before a run");
+      if (!have_data) throw Error("Write_dump command before simulation box is defined");
       std::vector<std::string> cols(w.begin() + 4, w.end());
       for (auto &c : cols)
         if (!is_style(c, {"id", "type", "q", "x", "y", "z", "vx", "vy", "vz", "fx", "fy", "fz"}))
           throw Error("Invalid attribute " + c + " in dump custom command");
-      pair->sync_host();
-      write_dump(w[3], cols, atom, *pair, update.ntimestep);
+      // before the first run: the host arrays (no forces, energies zero)
+      if (pair && setup_done) pair->sync_host();
+      write_dump(w[3], cols, atom, pair.get(), update.ntimestep);
     } else {
       throw Error("Unknown command: " + line);
     }
@@ -309,12 +657,26 @@ int run_deck(std::istream &in) {
 
 int main(int argc, char **argv) {
   try {
-    if (argc > 1 && std::strcmp(argv[1], "-") != 0) {
-      std::ifstream in(argv[1]);
-      if (!in) throw Error(std::string("Cannot open input script ") + argv[1]);
-      return run_deck(in);
+    // reax_md [-var NAME VALUE ...] [-in] [FILE | -]
+    std::map<std::string, std::string> cmdvars;
+    std::string file;
+    for (int k = 1; k < argc; ++k) {
+      const std::string a = argv[k];
+      if ((a == "-var" || a == "-v") && k + 2 < argc) {
+        cmdvars[argv[k + 1]] = argv[k + 2];
+        k += 2;
+      } else if ((a == "-in" || a == "-i") && k + 1 < argc) {
+        file = argv[++k];
+      } else {
+        file = a;
+      }
     }
-    return run_deck(std::cin);
+    if (!file.empty() && file != "-") {
+      std::ifstream in(file);
+      if (!in) throw Error("Cannot open input script " + file);
+      return run_deck(in, cmdvars);
+    }
+    return run_deck(std::cin, cmdvars);
   } catch (const Error &e) {
     std::fprintf(stdout, "ERROR: %s\n", e.what());
     std::fflush(stdout);

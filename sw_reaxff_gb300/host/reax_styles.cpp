@@ -2,6 +2,8 @@
 // reference classes each one mirrors).
 #include "reax_styles.h"
 
+#include <algorithm>
+#include <array>
 #include <cerrno>
 #include <cmath>
 #include <cstdlib>
@@ -55,11 +57,11 @@ PairReaxCGB300::~PairReaxCGB300() {
 
 void PairReaxCGB300::settings(int narg, char **arg) {
   if (narg < 1) throw Error("Illegal pair_style command");
-  // a control file (pair_reaxc_sunway.cpp:231 Read_Control_File) is not
-  // supported: its cutoffs are the NULL defaults' keywords here
-  if (std::strcmp(arg[0], "NULL") != 0)
-    throw Error("pair_style reax/c/gb300 supports only NULL control (default controls)");
+  // NULL: the reference's default controls (pair_reaxc_sunway.cpp:208-242);
+  // else a control file (pair_reaxc_sunway.cpp:231, Read_Control_File)
   rg_default_params(&params_);
+  bg_cut = 0.3;
+  if (std::strcmp(arg[0], "NULL") != 0) read_control_file(arg[0]);
   qeqflag = 1;
   const char *illegal = "Illegal pair_style reax/c command";
   int iarg = 1;
@@ -90,6 +92,47 @@ void PairReaxCGB300::settings(int narg, char **arg) {
     }
     iarg += 2;
   }
+}
+
+void PairReaxCGB300::read_control_file(const char *path) {
+  std::FILE *fp = std::fopen(path, "r");
+  if (!fp) throw Error(std::string("Cannot open control file ") + path);
+  // keywords of Read_Control_File that do not touch the force step
+  static const char *other[] = {
+      "simulation_name", "ensemble_type", "nsteps", "dt", "proc_by_dim", "random_vel",
+      "restart_format", "restart_freq", "reposition_atoms", "restrict_bonds", "remove_CoM_vel",
+      "debug_level", "energy_update_freq", "reneighbor", "vlist_buffer", "ghost_cutoff",
+      "qeq_freq", "q_err", "ilu_refactor", "ilu_droptol", "temp_init", "temp_final", "t_mass",
+      "t_mode", "t_rate", "t_freq", "pressure", "p_mass", "pt_mass", "compress", "press_mode",
+      "geo_format", "write_freq", "traj_compress", "traj_method", "traj_title", "atom_info",
+      "atom_velocities", "atom_forces", "bond_info", "angle_info", "molecular_analysis",
+      "ignore", "dipole_anal", "freq_dipole_anal", "diffusion_coef", "freq_diffusion_coef",
+      "restrict_type"};
+  char line[1024];
+  std::string bad;
+  while (std::fgets(line, sizeof line, fp)) {
+    char key[256] = {0}, val[256] = {0};
+    const int k = std::sscanf(line, "%255s %255s", key, val);
+    if (k < 1) continue;   // blank line
+    const double v = std::atof(val);
+    if (!std::strcmp(key, "nbrhood_cutoff")) params_.bond_cut = v;
+    else if (!std::strcmp(key, "hbond_cutoff")) params_.hbond_cut = v;
+    else if (!std::strcmp(key, "thb_cutoff")) params_.thb_cut = v;
+    else if (!std::strcmp(key, "thb_cutoff_sq")) params_.thb_cutsq = v;
+    else if (!std::strcmp(key, "bond_graph_cutoff")) bg_cut = v;
+    else if (!std::strcmp(key, "tabulate_long_range")) {
+      // the reference's long-range table switch: 0 = analytic pair
+      // functions; any other value selects the FP64 tables here
+      if (std::atoi(val) == 0) params_.tabulate = 0;
+    } else {
+      bool known = false;
+      for (const char *o : other) known = known || !std::strcmp(key, o);
+      if (!known && bad.empty()) bad = key;
+    }
+  }
+  std::fclose(fp);
+  // the reference prints "WARNING: unknown parameter" and aborts
+  if (!bad.empty()) throw Error("Unknown parameter " + bad + " in control file " + path);
 }
 
 void PairReaxCGB300::coeff(int narg, char **arg) {
@@ -175,6 +218,10 @@ void PairReaxCGB300::create_device() {
   const double L[3] = {atom_->boxhi[0] - atom_->boxlo[0], atom_->boxhi[1] - atom_->boxlo[1],
                        atom_->boxhi[2] - atom_->boxlo[2]};
   check(rg_set_box(h_, L), "rg_set_box");
+  if (atom_->triclinic) {
+    const double tilt[3] = {atom_->xy, atom_->xz, atom_->yz};
+    check(rg_set_tilt(h_, tilt), "rg_set_tilt");
+  }
 }
 
 rg_system *PairReaxCGB300::handle() {
@@ -195,15 +242,18 @@ void PairReaxCGB300::sync_device() {
                 "(call sync_host before editing them)");
   rg_system *h = handle();
   const int n = atom_->nlocal;
-  // positions wrapped into the box (LAMMPS keeps them there between
-  // re-neighbourings; the library's periodic images need [0, L))
+  // positions relative to the box origin, wrapped into an orthogonal box
+  // (LAMMPS keeps them there between re-neighbourings); the library wraps
+  // a triclinic cell's positions by their fractional coordinates itself
   std::vector<double> x(3 * (size_t)n);
   for (int i = 0; i < n; ++i)
     for (int c = 0; c < 3; ++c) {
       const double lo = atom_->boxlo[c], L = atom_->boxhi[c] - atom_->boxlo[c];
       double u = atom_->x[3 * i + c] - lo;
-      u -= L * std::floor(u / L);
-      if (u >= L) u -= L;
+      if (!atom_->triclinic) {
+        u -= L * std::floor(u / L);
+        if (u >= L) u -= L;
+      }
       x[3 * i + c] = u;
     }
   if (!uploaded_) {
@@ -366,6 +416,7 @@ void FixReaxCBondsGB300::output() {
   const int cap = 24;
   std::vector<int> nb(n), tags((size_t)n * cap);
   std::vector<double> bo((size_t)n * cap), tot(n), nlp(n);
+  bg_cut = pair_->bg_cut;
   const int most = rg_bond_table(pair_->handle(), bg_cut, cap, nb.data(), tags.data(), bo.data(),
                                  tot.data(), nlp.data());
   pair_->check(most < 0 ? most : RG_OK, "rg_bond_table");
@@ -387,6 +438,262 @@ void FixReaxCBondsGB300::output() {
   }
   std::fprintf(fp_, "# \n");
   std::fflush(fp_);
+}
+
+// ---------------------------------------------------------------- fix species
+
+FixReaxCSpeciesGB300::FixReaxCSpeciesGB300(PairReaxCGB300 *pair, Atom *atom, Update *update,
+                                           int narg, char **arg)
+    : pair_(pair), atom_(atom), update_(update) {
+  const char *illegal = "Illegal fix reax/c/species command";
+  if (narg < 7) throw Error(illegal);
+  nevery = (int)inumeric(arg[3]);
+  nrepeat = (int)inumeric(arg[4]);
+  nfreq = (int)inumeric(arg[5]);
+  if (nevery <= 0 || nrepeat <= 0 || nfreq <= 0) throw Error(illegal);
+  if (nfreq % nevery || nrepeat * nevery > nfreq) throw Error(illegal);
+  if (!pair_) throw Error("Cannot use fix reax/c/species without pair_style reax/c");
+  const int nt = atom_->ntypes;
+  bocut_.assign(nt + 1, std::vector<double>(nt + 1, 0.30));
+  static const char *dflt[] = {"C", "H", "O", "N"};
+  ele_.assign(nt, "");
+  for (int k = 0; k < nt && k < 4; ++k) ele_[k] = dflt[k];
+  int iarg = 7;
+  while (iarg < narg) {
+    if (!std::strcmp(arg[iarg], "cutoff")) {
+      if (iarg + 4 > narg) throw Error(illegal);
+      const int it = (int)inumeric(arg[iarg + 1]), jt = (int)inumeric(arg[iarg + 2]);
+      const double bo = numeric(arg[iarg + 3]);
+      if (it > nt || jt > nt || it <= 0 || jt <= 0 || bo > 1.0 || bo < 0.0) throw Error(illegal);
+      bocut_[it][jt] = bocut_[jt][it] = bo;
+      iarg += 4;
+    } else if (!std::strcmp(arg[iarg], "element")) {
+      if (iarg + nt + 1 > narg) throw Error(illegal);
+      for (int k = 0; k < nt; ++k) ele_[k] = arg[iarg + 1 + k];
+      iarg += nt + 1;
+    } else if (!std::strcmp(arg[iarg], "position")) {
+      if (iarg + 3 > narg) throw Error(illegal);
+      posfreq_ = (int)inumeric(arg[iarg + 1]);
+      if (posfreq_ < nfreq || posfreq_ % nfreq != 0) throw Error(illegal);
+      posfile_ = arg[iarg + 2];
+      multipos_ = posfile_.find('*') != std::string::npos;
+      if (!multipos_) {
+        pos_ = std::fopen(posfile_.c_str(), "w");
+        if (!pos_) throw Error("Cannot open fix reax/c/species position file");
+      }
+      iarg += 3;
+    } else {
+      throw Error(illegal);
+    }
+  }
+  const std::string file = arg[6];
+  if (file.size() > 3 && file.compare(file.size() - 3, 3, ".gz") == 0)
+    throw Error("Cannot open gzipped file");
+  fp_ = std::fopen(file.c_str(), "w");
+  if (!fp_) throw Error("Cannot open fix reax/c/species file " + file);
+}
+
+FixReaxCSpeciesGB300::~FixReaxCSpeciesGB300() {
+  if (fp_) std::fclose(fp_);
+  if (pos_) std::fclose(pos_);
+}
+
+void FixReaxCSpeciesGB300::setup() {
+  // first output Nfreq steps on (FixReaxCSpeciesSunway::init)
+  nvalid_ = update_->ntimestep + nfreq;
+  nsamples_ = 0;
+  xsum_.clear();
+  qsum_.clear();
+  bosum_.clear();
+}
+
+void FixReaxCSpeciesGB300::end_of_step() {
+  const long long t = update_->ntimestep;
+  const long long first = nvalid_ - (long long)(nrepeat - 1) * nevery;
+  if (t >= first && t <= nvalid_ && (nvalid_ - t) % nevery == 0) sample();
+  if (t == nvalid_) {
+    output();
+    nvalid_ += nfreq;
+    nsamples_ = 0;
+    xsum_.clear();
+    qsum_.clear();
+    bosum_.clear();
+  }
+}
+
+// one sample: positions, charges and the bond orders >= 0.10 of every pair
+// (the pre-cut of PairReaxCSunway::FindBond, pair_reaxc_sunway.cpp:1170-1198)
+void FixReaxCSpeciesGB300::sample() {
+  const int n = atom_->nlocal;
+  const int cap = 24;
+  std::vector<int> nb(n), tags((size_t)n * cap);
+  std::vector<double> bo((size_t)n * cap), tot(n), nlp(n);
+  const int most = rg_bond_table(pair_->handle(), 0.10, cap, nb.data(), tags.data(), bo.data(),
+                                 tot.data(), nlp.data());
+  pair_->check(most < 0 ? most : RG_OK, "rg_bond_table");
+  if (most > cap) throw Error("Increase MAXSPECBOND: an atom has more than 24 bonds");
+  pair_->sync_host();
+  if (xsum_.empty()) {
+    xsum_.assign(3 * (size_t)n, 0.0);
+    qsum_.assign(n, 0.0);
+  }
+  for (int i = 0; i < n; ++i) {
+    for (int c = 0; c < 3; ++c) xsum_[3 * (size_t)i + c] += atom_->x[3 * (size_t)i + c];
+    qsum_[i] += atom_->q[i];
+  }
+  // the largest order per atom pair (periodic images of one pair in small
+  // boxes count once)
+  std::map<std::pair<int, int>, double> s;
+  for (int i = 0; i < n; ++i)
+    for (int k = 0; k < nb[i]; ++k) {
+      const int a = atom_->tag[i], b = tags[(size_t)i * cap + k];
+      if (a >= b) continue;
+      double &v = s[{a, b}];
+      v = std::max(v, bo[(size_t)i * cap + k]);
+    }
+  for (auto &kv : s) bosum_[kv.first] += kv.second;
+  ++nsamples_;
+}
+
+std::string FixReaxCSpeciesGB300::formula(const std::vector<int> &count) const {
+  std::string f;
+  for (size_t j = 0; j < count.size(); ++j)
+    if (count[j]) {
+      f += ele_[j];
+      if (count[j] != 1) f += std::to_string(count[j]);
+    }
+  return f;
+}
+
+void FixReaxCSpeciesGB300::output() {
+  const int n = atom_->nlocal;
+  const int nt = atom_->ntypes;
+  if (nsamples_ == 0) sample();
+  std::map<int, int> slot;   // tag -> Atoms index
+  for (int i = 0; i < n; ++i) slot[atom_->tag[i]] = i;
+  // union-find over the averaged bonds above their cutoff
+  std::vector<int> parent(n);
+  for (int i = 0; i < n; ++i) parent[i] = i;
+  auto find = [&](int i) {
+    while (parent[i] != i) i = parent[i] = parent[parent[i]];
+    return i;
+  };
+  for (auto &kv : bosum_) {
+    const int i = slot[kv.first.first], j = slot[kv.first.second];
+    const double avg = kv.second / nsamples_;
+    if (avg > bocut_[atom_->type[i]][atom_->type[j]]) parent[find(i)] = find(j);
+  }
+  // molecules numbered 1.. in the order of their smallest atom ID
+  // (SortMolecule), species in the order of first appearance (FindSpecies)
+  std::map<int, int> root_min;
+  for (int i = 0; i < n; ++i) {
+    const int r = find(i);
+    auto it = root_min.find(r);
+    if (it == root_min.end() || atom_->tag[i] < it->second) root_min[r] = atom_->tag[i];
+  }
+  std::vector<std::pair<int, int>> order;   // (min tag, root)
+  for (auto &kv : root_min) order.push_back({kv.second, kv.first});
+  std::sort(order.begin(), order.end());
+  std::map<int, int> molid;
+  for (size_t m = 0; m < order.size(); ++m) molid[order[m].second] = (int)m + 1;
+  nmole = (int)order.size();
+  std::vector<int> mol(n);
+  std::vector<std::vector<int>> counts(nmole, std::vector<int>(nt, 0));
+  for (int i = 0; i < n; ++i) {
+    mol[i] = molid[find(i)];
+    counts[mol[i] - 1][atom_->type[i] - 1]++;
+  }
+  std::vector<std::vector<int>> species;
+  std::vector<int> nmol;
+  for (int m = 0; m < nmole; ++m) {
+    size_t k = 0;
+    while (k < species.size() && species[k] != counts[m]) ++k;
+    if (k == species.size()) {
+      species.push_back(counts[m]);
+      nmol.push_back(1);
+    } else {
+      nmol[k]++;
+    }
+  }
+  nspec = (int)species.size();
+  std::fprintf(fp_, "# Timestep     No_Moles     No_Specs     ");
+  for (auto &sp : species) std::fprintf(fp_, "%s\t", formula(sp).c_str());
+  std::fprintf(fp_, "\n");
+  std::fprintf(fp_, "%lld", update_->ntimestep);
+  std::fprintf(fp_, "%11d%11d\t", nmole, nspec);
+  for (int c : nmol) std::fprintf(fp_, " %d\t", c);
+  std::fprintf(fp_, "\n");
+  std::fflush(fp_);
+  if (posfreq_ > 0 && update_->ntimestep % posfreq_ == 0) write_pos(mol, nmole, nspec);
+}
+
+// molecule sizes, formulas, mean charges and centres (WritePos,
+// fix_reaxc_species_sunway.cpp:814-935): atoms unwrapped to the half-box
+// image nearest the molecule's anchor (its lexicographically smallest
+// averaged position), the centre wrapped into the box and given as a
+// fraction of the box edges
+void FixReaxCSpeciesGB300::write_pos(const std::vector<int> &mol, int nmole_, int nspec_) {
+  std::FILE *fp = pos_;
+  if (multipos_) {
+    std::string f = posfile_;
+    f.replace(f.find('*'), 1, std::to_string(update_->ntimestep));
+    fp = std::fopen(f.c_str(), "w");
+    if (!fp) throw Error("Cannot open fix reax/c/species position file");
+  }
+  const int n = atom_->nlocal, nt = atom_->ntypes;
+  const double *lo = atom_->boxlo, *hi = atom_->boxhi;
+  double box[3], half[3];
+  for (int c = 0; c < 3; ++c) {
+    box[c] = hi[c] - lo[c];
+    half[c] = box[c] / 2;
+  }
+  std::fprintf(fp, "Timestep %lld NMole %d  NSpec %d  xlo %f  xhi %f  ylo %f  yhi %f  zlo %f  zhi %f\n",
+               update_->ntimestep, nmole_, nspec_, lo[0], hi[0], lo[1], hi[1], lo[2], hi[2]);
+  std::fprintf(fp, "ID\tAtom_Count\tType\tAve_q\t\tCoM_x\t\tCoM_y\t\tCoM_z\n");
+  const double w = 1.0 / nsamples_;
+  std::vector<std::array<double, 3>> anchor(nmole_ + 1);
+  std::vector<int> have(nmole_ + 1, 0);
+  for (int i = 0; i < n; ++i) {
+    const std::array<double, 3> x = {xsum_[3 * (size_t)i] * w, xsum_[3 * (size_t)i + 1] * w,
+                                     xsum_[3 * (size_t)i + 2] * w};
+    const int m = mol[i];
+    if (!have[m] || x < anchor[m]) anchor[m] = x;
+    have[m] = 1;
+  }
+  for (int m = 1; m <= nmole_; ++m) {
+    int count = 0;
+    double avq = 0.0, avx[3] = {0, 0, 0};
+    std::vector<int> name(nt, 0);
+    for (int i = 0; i < n; ++i) {
+      if (mol[i] != m) continue;
+      name[atom_->type[i] - 1]++;
+      ++count;
+      avq += qsum_[i] * w;
+      for (int c = 0; c < 3; ++c) {
+        double x = xsum_[3 * (size_t)i + c] * w;
+        if (anchor[m][c] - x > half[c]) x += box[c];
+        if (x - anchor[m][c] > half[c]) x -= box[c];
+        avx[c] += x;
+      }
+    }
+    std::fprintf(fp, "%d\t%d\t%s", m, count, formula(name).c_str());
+    if (count > 0) {
+      avq /= count;
+      for (int c = 0; c < 3; ++c) {
+        avx[c] /= count;
+        if (avx[c] >= hi[c]) avx[c] -= box[c];
+        if (avx[c] < lo[c]) avx[c] += box[c];
+        avx[c] = (avx[c] - lo[c]) / box[c];
+      }
+      std::fprintf(fp, "\t%.8f \t%.8f \t%.8f \t%.8f", avq, avx[0], avx[1], avx[2]);
+    }
+    std::fprintf(fp, "\n");
+  }
+  if (multipos_) std::fclose(fp);
+  else {
+    std::fprintf(fp, "#\n");
+    std::fflush(fp);
+  }
 }
 
 // ---------------------------------------------------------------- Verlet

@@ -24,6 +24,7 @@
 #define REAX_STYLES_H
 
 #include <cstdio>
+#include <map>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -36,7 +37,8 @@ struct Error : std::runtime_error {
   using std::runtime_error::runtime_error;
 };
 
-// The part of LAMMPS's Atom the three styles use (orthogonal periodic box).
+// The part of LAMMPS's Atom and Domain the styles use: a periodic box,
+// orthogonal or triclinic (edge vectors (lx,0,0), (xy,ly,0), (xz,yz,lz)).
 struct Atom {
   int nlocal = 0;
   int ntypes = 0;
@@ -46,6 +48,8 @@ struct Atom {
   std::vector<int> type, tag;      // type 1..ntypes, tag 1..natoms
   std::vector<double> mass;        // [ntypes + 1], mass[0] unused
   double boxlo[3] = {0, 0, 0}, boxhi[3] = {0, 0, 0};
+  int triclinic = 0;
+  double xy = 0.0, xz = 0.0, yz = 0.0;
 };
 
 struct Update {
@@ -87,19 +91,26 @@ class FixNVEGB300 {
   Update *update_;
 };
 
+// A fix called by the Verlet loop after setup and at the end of every step.
+struct StepFix {
+  virtual ~StepFix() = default;
+  virtual void setup() = 0;
+  virtual void end_of_step() = 0;
+};
+
 // fix ID group reax/c/bonds Nevery file (FixReaxCBondsSunway,
 // fix_reaxc_bonds_sunway.cpp:45-330): every Nevery steps, the connection
 // table with bond orders above the coarse cutoff bg_cut = 0.3, the total
 // bond order, lone pairs and charge of every atom, in the reference's file
 // format.
-class FixReaxCBondsGB300 {
+class FixReaxCBondsGB300 : public StepFix {
  public:
   FixReaxCBondsGB300(PairReaxCGB300 *pair, Atom *atom, Update *update, int narg, char **arg);
-  ~FixReaxCBondsGB300();
+  ~FixReaxCBondsGB300() override;
   FixReaxCBondsGB300(const FixReaxCBondsGB300 &) = delete;
   FixReaxCBondsGB300 &operator=(const FixReaxCBondsGB300 &) = delete;
-  void setup();
-  void end_of_step();
+  void setup() override;
+  void end_of_step() override;
   int nevery = 1;
   double bg_cut = 0.3;
 
@@ -111,6 +122,49 @@ class FixReaxCBondsGB300 {
   std::FILE *fp_ = nullptr;
 };
 
+// fix ID group reax/c/species Nevery Nrepeat Nfreq file [cutoff I J BO]
+//   [element E1 .. En] [position Nposfreq file]  (FixReaxCSpeciesSunway,
+// fix_reaxc_species_sunway.cpp:49-945): molecules are the connected
+// components of the bonds whose bond order, averaged over Nrepeat samples
+// Nevery steps apart ending at every Nfreq-th step, is above the type pair's
+// cutoff (default 0.3); every Nfreq steps the species (element formulas)
+// and their molecule counts are written in the reference's format, and
+// with "position" each molecule's size, formula, mean charge and centre in
+// fractional box coordinates.  The reference samples in post_integrate,
+// where its bond orders are those of the previous step's positions; here the
+// samples are taken at the end of the step, positions, charges and bond
+// orders of one step together.
+class FixReaxCSpeciesGB300 : public StepFix {
+ public:
+  FixReaxCSpeciesGB300(PairReaxCGB300 *pair, Atom *atom, Update *update, int narg, char **arg);
+  ~FixReaxCSpeciesGB300() override;
+  FixReaxCSpeciesGB300(const FixReaxCSpeciesGB300 &) = delete;
+  FixReaxCSpeciesGB300 &operator=(const FixReaxCSpeciesGB300 &) = delete;
+  void setup() override;
+  void end_of_step() override;
+  int nevery = 1, nrepeat = 1, nfreq = 1;
+  int nmole = 0, nspec = 0;   // of the last output (the fix's vector)
+
+ private:
+  void sample();
+  void output();
+  void write_pos(const std::vector<int> &mol, int nmole, int nspec);
+  std::string formula(const std::vector<int> &count) const;
+  PairReaxCGB300 *pair_;
+  Atom *atom_;
+  Update *update_;
+  std::FILE *fp_ = nullptr, *pos_ = nullptr;
+  std::vector<std::vector<double>> bocut_;   // [ntypes+1][ntypes+1]
+  std::vector<std::string> ele_;             // element name per LAMMPS type
+  int posfreq_ = 0;
+  std::string posfile_;
+  bool multipos_ = false;
+  long long nvalid_ = -1;
+  int nsamples_ = 0;
+  std::vector<double> xsum_, qsum_;                    // per atom (Atoms order)
+  std::map<std::pair<int, int>, double> bosum_;        // (tag_i < tag_j) -> sum of BO
+};
+
 class PairReaxCGB300 {
  public:
   explicit PairReaxCGB300(Atom *atom);
@@ -118,9 +172,14 @@ class PairReaxCGB300 {
   PairReaxCGB300(const PairReaxCGB300 &) = delete;
   PairReaxCGB300 &operator=(const PairReaxCGB300 &) = delete;
 
-  // pair_style reax/c/gb300 NULL [checkqeq yes/no] [enobonds yes/no]
+  // pair_style reax/c/gb300 NULL|control_file [checkqeq yes/no] [enobonds yes/no]
   //   [lgvdw yes/no] [safezone f] [mincap i] [maxfar i] [precision fp64/mixed]
   void settings(int narg, char **arg);
+  // the reference's control file (Read_Control_File,
+  // reaxc_control_sunway.cpp:33-380): its force-step keywords set the
+  // cutoffs; the others are accepted and have no effect here
+  void read_control_file(const char *path);
+  double bg_cut = 0.3;   // bond_graph_cutoff (fix reax/c/bonds)
   // pair_coeff * * ffield.reax E1 E2 ... (one element or NULL per type)
   void coeff(int narg, char **arg);
   void init_style();
@@ -157,6 +216,7 @@ class PairReaxCGB300 {
   friend class FixQEqReaxGB300;
   friend class FixNVEGB300;
   friend class FixReaxCBondsGB300;
+  friend class FixReaxCSpeciesGB300;
 };
 
 // LAMMPS's Verlet order: setup (pre_force, force) then per step
@@ -171,7 +231,7 @@ class Verlet {
   void run(long long nsteps, int thermo_every,
            void (*thermo)(const Verlet &, void *) = nullptr, void *ctx = nullptr);
   double kinetic_energy() const;   // kcal/mol from the host velocities
-  std::vector<FixReaxCBondsGB300 *> end_of_step_fixes;
+  std::vector<StepFix *> end_of_step_fixes;
   Atom *atom_;
   Update *update_;
   PairReaxCGB300 *pair_;

@@ -14,6 +14,9 @@ from __future__ import annotations
 import math
 from dataclasses import dataclass, field
 
+import os
+import re
+
 import numpy as np
 
 AVOGADRO = 6.0221367e23
@@ -78,14 +81,21 @@ MOLECULES = {"H2O": _water(), "CH4": _methane(), "NH3": _ammonia(),
 
 @dataclass
 class System:
-    """A periodic orthogonal box of atoms (positions in [0, L))."""
-    box: np.ndarray            # (3,) edge lengths
+    """A periodic box of atoms: orthogonal (positions in [0, L)), or
+    triclinic with tilt = (xy, xz, yz) (edge vectors (lx,0,0), (xy,ly,0),
+    (xz,yz,lz), LAMMPS's restricted form)."""
+    box: np.ndarray            # (3,) edge lengths lx, ly, lz
     x: np.ndarray              # (n, 3) float64
     elem: list                 # element symbol per atom
     tag: np.ndarray            # (n,) int32, 1-based
     v: np.ndarray              # (n, 3) float64, A/fs
     mol: np.ndarray            # (n,) molecule index
     meta: dict = field(default_factory=dict)
+    tilt: np.ndarray = None    # (3,) xy, xz, yz or None (orthogonal)
+
+    @property
+    def triclinic(self) -> bool:
+        return self.tilt is not None and bool(np.any(np.asarray(self.tilt) != 0.0))
 
     @property
     def n(self) -> int:
@@ -279,6 +289,99 @@ def small_pack(n_atoms_target: int, density: float, seed: int) -> System:
         n += len(MOLECULES[k][0])
     counts = {k: v for k, v in counts.items() if v}
     return pack_molecules(counts, density, seed + 1)
+
+
+_NUM = re.compile(r"[+-]?(\d+\.?\d*|\.\d+)([eE][+-]?\d+)?")
+
+
+def _num(tok: str) -> float:
+    """The longest numeric prefix of a token, as C's strtod reads it (the
+    shipped TATB data file writes "15.1826391451E zlo zhi")."""
+    m = _NUM.match(tok)
+    if not m:
+        raise ValueError(f"not a number: {tok!r}")
+    return float(m.group(0))
+
+
+def read_lammps_data(path: str, elements) -> System:
+    """Read a LAMMPS data file of atom_style charge (header counts, box
+    bounds, an optional "xy xz yz" tilt line, Masses, Atoms "id type q x y
+    z", optional Velocities), the format of the reference's data.tatb.
+    LAMMPS type k is elements[k-1].  Positions are taken relative to the
+    box origin (xlo, ylo, zlo); velocities default to zero."""
+    lines = [ln.split("#")[0].strip() for ln in open(path)]
+    n = None
+    lo, hi = [0.0] * 3, [0.0] * 3
+    tilt = None
+    k = 1
+    while k < len(lines):
+        w = lines[k].split()
+        if not w:
+            k += 1
+            continue
+        if w[-1] == "atoms" and len(w) == 2:
+            n = int(w[0])
+        elif w[-2:] in (["xlo", "xhi"], ["ylo", "yhi"], ["zlo", "zhi"]):
+            c = "xyz".index(w[-2][0])
+            lo[c], hi[c] = _num(w[0]), _num(w[1])
+        elif w[-3:] == ["xy", "xz", "yz"]:
+            tilt = np.array([_num(w[0]), _num(w[1]), _num(w[2])])
+        elif w[0] in ("Masses", "Atoms", "Velocities"):
+            break
+        k += 1
+    if n is None:
+        raise ValueError("data file has no atom count")
+    x = np.zeros((n, 3))
+    v = np.zeros((n, 3))
+    tag = np.zeros(n, np.int32)
+    typ = np.zeros(n, np.int32)
+    row = {}
+    while k < len(lines):
+        sec = lines[k].split()
+        k += 1
+        if not sec:
+            continue
+        name = sec[0]
+        body = []
+        while k < len(lines) and (not lines[k] or lines[k].split()[0][0] in "+-.0123456789"):
+            if lines[k]:
+                body.append(lines[k].split())
+            k += 1
+        if name == "Atoms":
+            if len(body) != n:
+                raise ValueError("Atoms section does not hold every atom")
+            for a, w in enumerate(body):
+                tag[a], typ[a] = int(w[0]), int(w[1])
+                x[a] = [_num(w[3]) - lo[0], _num(w[4]) - lo[1], _num(w[5]) - lo[2]]
+                row[tag[a]] = a
+        elif name == "Velocities":
+            for w in body:
+                v[row[int(w[0])]] = [_num(w[1]), _num(w[2]), _num(w[3])]
+    box = np.array([hi[c] - lo[c] for c in range(3)])
+    elem = [elements[t - 1] for t in typ]
+    return System(box=box, x=x, elem=elem, tag=tag, v=v, mol=np.zeros(n, np.int32),
+                  meta={"source": os.path.basename(path)}, tilt=tilt)
+
+
+def replicate(system: System, reps) -> System:
+    """The system repeated reps = (na, nb, nc) times along its edge vectors
+    (what scaling the TATB deck's box and lattice by S does)."""
+    na, nb, nc = reps
+    lx, ly, lz = system.box
+    xy, xz, yz = system.tilt if system.tilt is not None else (0.0, 0.0, 0.0)
+    a, b, c = np.array([lx, 0, 0]), np.array([xy, ly, 0]), np.array([xz, yz, lz])
+    xs, els, vs = [], [], []
+    for k in range(nc):
+        for j in range(nb):
+            for i in range(na):
+                xs.append(system.x + i * a + j * b + k * c)
+                els += list(system.elem)
+                vs.append(system.v)
+    n = len(els)
+    tilt = None if system.tilt is None else np.array([nb * xy, nc * xz, nc * yz])
+    return System(box=np.array([na * lx, nb * ly, nc * lz]), x=np.concatenate(xs), elem=els,
+                  tag=np.arange(1, n + 1, dtype=np.int32), v=np.concatenate(vs),
+                  mol=np.zeros(n, np.int32), meta=dict(system.meta, reps=reps), tilt=tilt)
 
 
 def write_lammps_data(system: System, path: str, elements=None, q=None) -> list:

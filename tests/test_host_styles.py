@@ -3,7 +3,8 @@ nve over the C ABI, with the reference's argument lists and error messages
 (PairReaxCSunway::settings/coeff/init_style, pair_reaxc_sunway.cpp:202-424;
 FixQEqReaxSunway constructor, fix_qeq_reax_sunway.cpp:64-90; FixNVESunway
 constructor, fix_nve_sunway.cpp:29-36; FixReaxCBondsSunway constructor,
-fix_reaxc_bonds_sunway.cpp:45-60, 125), driven by the reax_md deck
+fix_reaxc_bonds_sunway.cpp:45-60, 125; FixReaxCSpeciesSunway constructor,
+fix_reaxc_species_sunway.cpp:49-238), driven by the reax_md deck
 interpreter.  Every deck here fails before the first device call, so these
 run without a GPU; the device runs are in test_gpu_host_styles.py."""
 import os
@@ -80,6 +81,18 @@ CASES = {
                      "Illegal fix reax/c/bonds command"),
     "bonds_no_pair": (["fix 3 all reax/c/bonds 5 bonds.out"],
                       "Cannot use fix reax/c/bonds without pair_style reax/c"),
+    "species_args": (["pair_style reax/c NULL", PAIR, "fix 4 all reax/c/species 1 1"],
+                     "Illegal fix reax/c/species command"),
+    "species_freq": (["pair_style reax/c NULL", PAIR, "fix 4 all reax/c/species 2 3 5 sp.out"],
+                     "Illegal fix reax/c/species command"),
+    "species_cutoff": (["pair_style reax/c NULL", PAIR,
+                        "fix 4 all reax/c/species 1 1 1 sp.out cutoff 1 5 0.3"],
+                       "Illegal fix reax/c/species command"),
+    "species_pos": (["pair_style reax/c NULL", PAIR,
+                     "fix 4 all reax/c/species 1 1 10 sp.out position 5 pos.out"],
+                    "Illegal fix reax/c/species command"),
+    "species_gz": (["pair_style reax/c NULL", PAIR, "fix 4 all reax/c/species 1 1 1 sp.gz"],
+                   "Cannot open gzipped file"),
     "unknown": (["pair_style reax/c NULL", "compute 1 all pe"], "Unknown command"),
     "units": (["pair_style reax/c NULL"], "requires units real"),
 }

@@ -459,6 +459,112 @@ __global__ void __launch_bounds__(256) k_hbonds(Dev d, int eflag) {
   if (VIR) seg_block_add<6>(w, j < n ? d.seg_s[j] : -1, d.virial, 6);
 }
 
+// Mixed form: the same terms entirely in FP32 per (H, acceptor bond,
+// partner) triple: the H...Z displacement from the FP32 (hi, lo) positions,
+// parameters from the control block's FP32 copies, forces summed in FP32
+// (the atoms' into the FP32 force array), energies and the bond's Cdbo in
+// FP64 once per lane and bond.
+template <bool VIR>
+__global__ void __launch_bounds__(256) k_hbonds32(Dev d, int eflag) {
+  const int lane = threadIdx.x & 31;
+  const int j = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int n = d.n;
+  double ehb = 0.0;
+  double w[6] = {0, 0, 0, 0, 0, 0};
+  if (j < n && d.ff->sbp[d.ts[j]].p_hbond == 1) {
+    const ForceField &F = *d.ff;
+    const Control &C = *d.ctl;
+    const int tj = d.ts[j];
+    const int nb = min(d.nbonds[j], d.bond_cap);
+    const int nh = min(d.nhb[j], d.hb_cap);
+    const float4 hjf = d.xf[j], ljf = d.xl[j];
+    const SegGeom &g = d.seg[d.seg_s[j]];
+    float *f32 = d.fC32;
+    float fjx = 0.f, fjy = 0.f, fjz = 0.f;
+    for (int q = 0; q < nb; ++q) {
+      const long long s = (long long)q * n + j;
+      const int i = nbr_of(d.b_nbr[s]);
+      const int ti = d.ts[i];
+      const double BO64 = d.b_BO[s];
+      if (F.sbp[ti].p_hbond != 2 || !(BO64 >= HB_THRESHOLD)) continue;
+      const float BO = (float)BO64;
+      const float dij[3] = {(float)d.b_dx[s], (float)d.b_dy[s], (float)d.b_dz[s]};
+      const float r_ij = (float)d.b_d[s];
+      const int tag_i = d.tags[i];
+      float fix = 0.f, fiy = 0.f, fiz = 0.f, cdbo = 0.f, el = 0.f;
+      for (int pk = lane; pk < nh; pk += 32) {
+        const uint32_t ek = d.hb_nbr[(long long)j * d.hb_cap + pk];
+        const int k = nbr_of(ek), tk = d.ts[k];
+        if (d.tags[k] == tag_i) continue;
+        const Control::HbF &hp = C.hb32[ti][tj][tk];
+        if (hp.r0_hb <= 0.f) continue;
+        int sx, sy, sz;
+        img_unpack((int)(ek & 255u), &sx, &sy, &sz);
+        float djk[3];
+        disp32(g, d.xf[k], d.xl[k], hjf, ljf, sx, sy, sz, djk[0], djk[1], djk[2]);
+        const float r_jk = sqrtf(djk[0] * djk[0] + djk[1] * djk[1] + djk[2] * djk[2]);
+        float theta, cos_theta, di[3], djv[3], dk[3];
+        theta_dcos<float>(dij, r_ij, djk, r_jk, theta, cos_theta, di, djv, dk);
+        const float sin_theta2 = sinf(theta / 2.f);
+        float sin_xhz4 = sin_theta2 * sin_theta2;
+        sin_xhz4 *= sin_xhz4;
+        const float cos_xhz1 = 1.f - cos_theta;
+        const float exp_hb2 = expf(-hp.p_hb2 * BO);
+        const float exp_hb3 = expf(-hp.p_hb3 * (hp.r0_hb / r_jk + r_jk / hp.r0_hb - 2.f));
+        const float e_hb = hp.p_hb1 * (1.f - exp_hb2) * exp_hb3 * sin_xhz4;
+        el += e_hb;
+        const float CEhb1 = hp.p_hb1 * hp.p_hb2 * exp_hb2 * exp_hb3 * sin_xhz4;
+        const float CEhb2 = -hp.p_hb1 / 2.f * (1.f - exp_hb2) * exp_hb3 * cos_xhz1;
+        const float CEhb3 = -hp.p_hb3 * (-hp.r0_hb / (r_jk * r_jk) + 1.f / hp.r0_hb) * e_hb;
+        cdbo += CEhb1;
+        fix += CEhb2 * di[0]; fiy += CEhb2 * di[1]; fiz += CEhb2 * di[2];
+        const float c3 = CEhb3 / r_jk;
+        fjx += CEhb2 * djv[0] - c3 * djk[0];
+        fjy += CEhb2 * djv[1] - c3 * djk[1];
+        fjz += CEhb2 * djv[2] - c3 * djk[2];
+        const float fkx = CEhb2 * dk[0] + c3 * djk[0], fky = CEhb2 * dk[1] + c3 * djk[1],
+                    fkz = CEhb2 * dk[2] + c3 * djk[2];
+        atomicAdd(&f32[k], fkx);
+        atomicAdd(&f32[n + k], fky);
+        atomicAdd(&f32[2 * n + k], fkz);
+        if (VIR) vir_acc(w, djk[0], djk[1], djk[2], fkx, fky, fkz);
+      }
+      if (eflag) ehb += (double)el;
+      if (VIR) vir_acc(w, d.b_dx[s], d.b_dy[s], d.b_dz[s], fix, fiy, fiz);
+      for (int off = 16; off > 0; off >>= 1) {
+        cdbo += __shfl_down_sync(FULL, cdbo, off);
+        fix += __shfl_down_sync(FULL, fix, off);
+        fiy += __shfl_down_sync(FULL, fiy, off);
+        fiz += __shfl_down_sync(FULL, fiz, off);
+      }
+      if (lane == 0) {
+        d.b_Cdbo[s] += (double)cdbo;
+        if (fix != 0.f || fiy != 0.f || fiz != 0.f) {
+          atomicAdd(&f32[i], fix);
+          atomicAdd(&f32[n + i], fiy);
+          atomicAdd(&f32[2 * n + i], fiz);
+        }
+      }
+    }
+    for (int off = 16; off > 0; off >>= 1) {
+      fjx += __shfl_down_sync(FULL, fjx, off);
+      fjy += __shfl_down_sync(FULL, fjy, off);
+      fjz += __shfl_down_sync(FULL, fjz, off);
+    }
+    if (lane == 0 && (fjx != 0.f || fjy != 0.f || fjz != 0.f)) {
+      atomicAdd(&f32[j], fjx);
+      atomicAdd(&f32[n + j], fjy);
+      atomicAdd(&f32[2 * n + j], fjz);
+    }
+  }
+  if (eflag) {
+    const int sg = j < n ? d.seg_s[j] : -1;
+    energy_add(d, ehb, sg, E_HB);
+    energy_add(d, ehb, sg, E_ENG_VDWL);
+  }
+  if (VIR) seg_block_add<6>(w, j < n ? d.seg_s[j] : -1, d.virial, 6);
+}
+
 // ------------------------------------------------------------------
 // Calculate_Omega, reaxc_torsion_angles_sw64.c:21-102
 template <typename R>
@@ -1135,7 +1241,12 @@ __global__ void k_force_out(Dev d) {
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= d.n) return;
   const int n = d.n, i = d.perm[s];
-  const double fx = -d.fC[s], fy = -d.fC[n + s], fz = -d.fC[2 * n + s];
+  double fx = -d.fC[s], fy = -d.fC[n + s], fz = -d.fC[2 * n + s];
+  if (d.fC32) {   // mixed form: the FP32 pair terms' forces
+    fx -= (double)d.fC32[s];
+    fy -= (double)d.fC32[n + s];
+    fz -= (double)d.fC32[2 * n + s];
+  }
   if (!(isfinite(fx) && isfinite(fy) && isfinite(fz))) atomicOr(&d.status[ST_NAN], 1);
   d.f_o[3 * i + 0] = fx;
   d.f_o[3 * i + 1] = fy;
@@ -1173,10 +1284,10 @@ void launch_hbonds(const Dev &d, cudaStream_t st, int eflag) {
   const long long threads = (long long)d.n * 32;
   const unsigned G = (unsigned)((threads + 255) / 256);
   if (d.vflag) {
-    if (d.mixed) k_hbonds<float, true><<<G, 256, 0, st>>>(d, eflag);
+    if (d.mixed) k_hbonds32<true><<<G, 256, 0, st>>>(d, eflag);
     else k_hbonds<double, true><<<G, 256, 0, st>>>(d, eflag);
   } else {
-    if (d.mixed) k_hbonds<float, false><<<G, 256, 0, st>>>(d, eflag);
+    if (d.mixed) k_hbonds32<false><<<G, 256, 0, st>>>(d, eflag);
     else k_hbonds<double, false><<<G, 256, 0, st>>>(d, eflag);
   }
 }
@@ -1198,9 +1309,10 @@ static void vt_kernels(const Dev &d, cudaStream_t st, int eflag, long long nval,
     cudaMemsetAsync(d.fb_cnt, 0, 2 * sizeof(int), st);
     if (nval > 0) k_valence<float, VIR><<<gv, 128, 0, st>>>(d, eflag, nval);
     if (ntor > 0) k_torsion<float, VIR><<<gt, 128, 0, st>>>(d, eflag, ntor);
-    // FP64 passes over the near-linear items (count read on the device)
-    k_valence_fb<VIR><<<152 * 2, 128, 0, st>>>(d, eflag);
-    k_torsion_fb<VIR><<<152 * 2, 128, 0, st>>>(d, eflag);
+    // FP64 passes over the near-linear items (count read on the device;
+    // usually none or a few, so a small grid that strides)
+    k_valence_fb<VIR><<<16, 128, 0, st>>>(d, eflag);
+    k_torsion_fb<VIR><<<16, 128, 0, st>>>(d, eflag);
   } else {
     if (nval > 0) k_valence<double, VIR><<<gv, 128, 0, st>>>(d, eflag, nval);
     if (ntor > 0) k_torsion<double, VIR><<<gt, 128, 0, st>>>(d, eflag, ntor);

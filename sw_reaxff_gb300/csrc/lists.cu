@@ -244,12 +244,12 @@ __device__ __forceinline__ void nbr_flush(const Dev &d, const Control &C, const 
       float dx, dy, dz;
       disp32(g, hj, lj, xif, xil, sx, sy, sz, dx, dy, dz);
       d2f = dx * dx + dy * dy + dz * dz;
-      const float lc2 = (float)C.list_cut2;
+      const float lc2 = C.list_cut2_f;
       if (d2f <= lc2 * (1.f - MARGIN32)) in = true;
       else if (d2f > lc2 * (1.f + MARGIN32)) in = false;
       else in = exact_d2(d, j, sx, sy, sz, xi, g) <= C.list_cut2;
       // near part: conservative (the bond pass tests its own cutoffs)
-      const float nc = (float)C.near_cut;
+      const float nc = C.near_cut_f;
       near = d2f <= nc * nc * (1.f + MARGIN32);
     } else {
       d2 = exact_d2(d, j, sx, sy, sz, xi, g);
@@ -268,25 +268,25 @@ __device__ __forceinline__ void nbr_flush(const Dev &d, const Control &C, const 
     const int pos = near ? cntN + __popc(mn & lanemask_lt())
                          : cap - 1 - (cntF + __popc(mf & lanemask_lt()));
     double h = 0.0;
-    if (MIXED && d2f <= (float)C.swb2) {
+    if (MIXED && d2f <= C.swb2_f) {
       // FP32: factored taper when swa = 0
       const int tj = __float_as_int(d.xf[j].w);
       const float r = d2f * rsqrtf(d2f);
       float tp;
       if (C.qtap_factored) {
-        const float t = r * (float)C.inv_swb_q, u = 1.f - t, u2 = u * u;
+        const float t = r * C.inv_swb_q_f, u = 1.f - t, u2 = u * u;
         tp = u2 * u2 * (1.f + t * (4.f + t * (10.f + t * 20.f)));
       } else {
-        const double *T = C.qTap;
-        tp = fmaf((float)T[7], r, (float)T[6]);
-        tp = fmaf(tp, r, (float)T[5]);
-        tp = fmaf(tp, r, (float)T[4]);
-        tp = fmaf(tp, r, (float)T[3]);
-        tp = fmaf(tp, r, (float)T[2]);
-        tp = fmaf(tp, r, (float)T[1]);
-        tp = fmaf(tp, r, (float)T[0]);
+        const float *T = C.qTap_f;
+        tp = fmaf(T[7], r, T[6]);
+        tp = fmaf(tp, r, T[5]);
+        tp = fmaf(tp, r, T[4]);
+        tp = fmaf(tp, r, T[3]);
+        tp = fmaf(tp, r, T[2]);
+        tp = fmaf(tp, r, T[1]);
+        tp = fmaf(tp, r, T[0]);
       }
-      const float x = fmaf(d2f, r, (float)F.tbp[ti][tj].gamma);
+      const float x = fmaf(d2f, r, C.nb32[ti][tj].gamma);
       d.nbr[row + pos] = ((uint32_t)j << 8) | (uint32_t)img;
       d.hval32[row + pos] = tp * 14.4f * rcbrtf(x);
     } else if (MIXED) {
@@ -345,8 +345,9 @@ __global__ void __launch_bounds__(NB_WARPS * 32) k_build_nbrs(Dev d) {
   const SegGeom &g = d.seg[d.seg_s[i]];
   const double L[3] = {g.L[0], g.L[1], g.L[2]};
   const int ncx = g.nc[0], ncy = g.nc[1], ncz = g.nc[2], S = g.S;
-  int cx, cy, cz;
-  cell3(g, xi.x, xi.y, xi.z, cx, cy, cz);
+  // the cell the binning put atom i in (integer decomposition, no FP64)
+  const int cl = d.cell_o[d.perm[i]] - g.cell0;
+  const int cx = cl % ncx, cy = (cl / ncx) % ncy, cz = cl / (ncx * ncy);
   const long long row = (long long)i * d.nb_cap;
   const int cap = d.nb_cap;
   const int nx = ncx;
@@ -439,27 +440,9 @@ __global__ void __launch_bounds__(NB_WARPS * 32) k_build_nbrs(Dev d) {
 // the FP64 pow/exp with most lanes idle), and k_bond_finish compacts the
 // rows and sums dDeltap and the total bond order.
 
-template <typename R>
-__device__ __forceinline__ void bo_prime(const Sbp &si, const Sbp &sj, const Tbp &tw, R dist, R bo_cut,
-                                         R &BOs, R &BOpi, R &BOpi2, R &C12, R &C34, R &C56) {
-  BOs = BOpi = BOpi2 = C12 = C34 = C56 = 0;
-  if (si.r_s > 0.0 && sj.r_s > 0.0) {
-    C12 = (R)tw.p_bo1 * pow(dist / (R)tw.r_s, (R)tw.p_bo2);
-    BOs = (R(1) + bo_cut) * exp(C12);
-  }
-  if (si.r_pi > 0.0 && sj.r_pi > 0.0) {
-    C34 = (R)tw.p_bo3 * pow(dist / (R)tw.r_p, (R)tw.p_bo4);
-    BOpi = exp(C34);
-  }
-  if (si.r_pi_pi > 0.0 && sj.r_pi_pi > 0.0) {
-    C56 = (R)tw.p_bo5 * pow(dist / (R)tw.r_pp, (R)tw.p_bo6);
-    BOpi2 = exp(C56);
-  }
-}
-
-// FP64 form: (d / r)^p as exp(p (log d - log r)) with log d once per bond
-// and log r from the control block (a few 1e-16 relative from pow, far
-// inside the 1e-10 bond-order bars; the reference's live form is a
+// BO' terms in FP64: (d / r)^p as exp(p (log d - log r)) with log d once
+// per bond and log r from the control block (a few 1e-16 relative from pow,
+// far inside the 1e-10 bond-order bars; the reference's live form is a
 // polynomial pow/exp on the CPEs)
 __device__ __forceinline__ void bo_prime64(const Control &C, int ti, int tj, const Sbp &si,
                                            const Sbp &sj, const Tbp &tw, double dist,
@@ -483,11 +466,15 @@ __device__ __forceinline__ void bo_prime64(const Control &C, int ti, int tj, con
 }
 
 // BO' of the bond candidates: one thread per candidate slot (blockIdx.y =
-// slot), so the FP64 pow/exp run with full warps instead of the few lanes a
-// per-atom warp has candidates for.  Accepted entries get their bond
-// orders and dBO' terms; rejected ones (BO' < bo_cut) are marked with a
-// negative distance and removed by k_bond_finish.
-template <bool MIXED>
+// slot), so the FP64 log/exp run with full warps instead of the few lanes a
+// per-atom warp has candidates for.  Accepted entries get their exact
+// distance, bond orders and dBO' terms; rejected ones (d > bond_cut or
+// BO' < bo_cut) are marked with a negative distance and removed by
+// k_bond_finish.  Both forms take the exact FP64 distance and FP64 BO':
+// BO' = exp(p_bo1 (d/r)^p_bo2) amplifies relative errors of d by
+// |p_bo1 p_bo2 (d/r)^p_bo2| (up to ~10 for C-C and C-N bonds), and in FP32
+// that left the mixed form's forces on the TATB crystal 1.7e-4 (relative
+// RMS) from the FP64 forces, against 1e-5 with FP64 BO'.
 __global__ void k_bond_prime(Dev d) {
   const int n = d.n;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -503,56 +490,20 @@ __global__ void k_bond_prime(Dev d) {
   int sx, sy, sz;
   img_unpack((int)(e & 255u), &sx, &sy, &sz);
   const SegGeom &g = d.seg[d.seg_s[i]];
-  // the bond distance: exact FP64 (FP64 form; the mixed form within
-  // MARGIN32 of bond_cut), else the FP32 (hi, lo) displacement
-  double dist, dx, dy, dz;
-  bool exact = !MIXED;
-  if (MIXED) {
-    const float4 hi = d.xf[i], li = d.xl[i], hj = d.xf[j], lj = d.xl[j];
-    float ex, ey, ez;
-    disp32(g, hj, lj, hi, li, sx, sy, sz, ex, ey, ez);
-    const float df = sqrtf(ex * ex + ey * ey + ez * ez);
-    if (fabsf(df - C.bond_cut_f) <= MARGIN32 * C.bond_cut_f) {
-      exact = true;
-    } else if (df > C.bond_cut_f) {
-      d.b_d[s] = -1.0;
-      return;
-    } else {
-      dx = ex; dy = ey; dz = ez; dist = df;
-    }
-  }
-  if (exact) {
-    disp64(g, d.xs[j], d.xs[i], sx, sy, sz, dx, dy, dz);
-    dist = __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz)));
-    if (!(dist <= C.bond_cut)) {
-      d.b_d[s] = -1.0;
-      return;
-    }
+  double dx, dy, dz;
+  disp64(g, d.xs[j], d.xs[i], sx, sy, sz, dx, dy, dz);
+  const double dist =
+      __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz)));
+  if (!(dist <= C.bond_cut)) {
+    d.b_d[s] = -1.0;
+    return;
   }
   const int ti = d.ts[i], tj = d.ts[j];
   const Sbp &si = F.sbp[ti], &sj = F.sbp[tj];
   const Tbp &tw = F.tbp[ti][tj];
   double BOs, BOpi, BOpi2, C12, C34, C56;
-  bool isb;
-  if (MIXED) {
-    // FP32 bond orders; the exact FP64 decision only within 1e-4 of the
-    // threshold, so the bond list equals the FP64 form's
-    float a, b, c, c12, c34, c56;
-    bo_prime<float>(si, sj, tw, (float)dist, (float)C.bo_cut, a, b, c, c12, c34, c56);
-    BOs = a; BOpi = b; BOpi2 = c; C12 = c12; C34 = c34; C56 = c56;
-    const double BO32 = (double)(a + b + c);
-    if (fabs(BO32 - C.bo_cut) <= 1e-4 * C.bo_cut) {
-      double x0, x1, x2, y0, y1, y2;
-      bo_prime64(C, ti, tj, si, sj, tw, dist, x0, x1, x2, y0, y1, y2);
-      isb = (x0 + x1 + x2) >= C.bo_cut;
-    } else {
-      isb = BO32 >= C.bo_cut;
-    }
-  } else {
-    bo_prime64(C, ti, tj, si, sj, tw, dist, BOs, BOpi, BOpi2, C12, C34, C56);
-    isb = (BOs + BOpi + BOpi2) >= C.bo_cut;
-  }
-  if (!isb) {
+  bo_prime64(C, ti, tj, si, sj, tw, dist, BOs, BOpi, BOpi2, C12, C34, C56);
+  if (!((BOs + BOpi + BOpi2) >= C.bo_cut)) {
     d.b_d[s] = -1.0;
     return;
   }
@@ -697,7 +648,7 @@ __global__ void __launch_bounds__(NB_WARPS * 32) k_build_bonds(Dev d) {
       }
       nh += __popc(mh);
       // candidates go to the bond slots in row order; k_bond_prime gives
-      // them their FP64 (or FP32) BO' and k_bond_finish drops the rejected
+      // them their FP64 BO' and k_bond_finish drops the rejected
       const unsigned mc = __ballot_sync(FULL, cand);
       if (cand) {
         const int k = nb + __popc(mc & lanemask_lt());
@@ -802,8 +753,7 @@ void launch_build_bonds(const Dev &d, cudaStream_t st) {
   if (d.mixed) k_build_bonds<true><<<G, NB_WARPS * 32, 0, st>>>(d);
   else k_build_bonds<false><<<G, NB_WARPS * 32, 0, st>>>(d);
   const dim3 gp((unsigned)((d.n + 127) / 128), (unsigned)d.bond_cap);
-  if (d.mixed) k_bond_prime<true><<<gp, 128, 0, st>>>(d);
-  else k_bond_prime<false><<<gp, 128, 0, st>>>(d);
+  k_bond_prime<<<gp, 128, 0, st>>>(d);
   k_bond_finish<<<(d.n + 255) / 256, 256, 0, st>>>(d);
   const long long slots = (long long)d.n * d.bond_cap;
   k_bond_sym<<<(unsigned)((slots + 255) / 256), 256, 0, st>>>(d);

@@ -185,6 +185,94 @@ __device__ __forceinline__ void pair_terms(const Dev &d, const ForceField &F, co
   c = (double)(CEvd + CEclmb);
 }
 
+// Mixed form: vdW + Coulomb of one pair entirely in FP32, parameters from
+// the control block's FP32 copies (no double is read or converted per
+// pair); returns (1/r) dE/dr in c, the displacement and the two energies.
+__device__ __forceinline__ void pair32(const Dev &d, const Control &C, int vdw_type, uint32_t e,
+                                       bool act, const double4 &xi, const float4 &xif,
+                                       const float4 &xil, int ti, const SegGeom &g, float &ev,
+                                       float &ee, float &c, float &dx, float &dy, float &dz,
+                                       int &j) {
+  c = 0.f; dx = dy = dz = 0.f; ev = ee = 0.f;
+  j = (int)(e >> 8);
+  if (!act) return;
+  int sx, sy, sz;
+  img_unpack((int)(e & 255u), &sx, &sy, &sz);
+  const float4 hj = d.xf[j], lj = d.xl[j];
+  disp32(g, hj, lj, xif, xil, sx, sy, sz, dx, dy, dz);
+  const float d2 = dx * dx + dy * dy + dz * dz;
+  if (!C.nonb_all_listed) {
+    // the list reaches the QEq taper radius beyond nonb_cut: FP64 only near
+    // the cutoff
+    const float nc2 = C.nonb_cut2_f;
+    bool out;
+    if (d2 <= nc2 * (1.f - 1e-5f)) out = false;
+    else if (d2 > nc2 * (1.f + 1e-5f)) out = true;
+    else {
+      double ex, ey, ez;
+      disp64(g, d.xs[j], xi, sx, sy, sz, ex, ey, ez);
+      out = __dadd_rn(__dadd_rn(__dmul_rn(ex, ex), __dmul_rn(ey, ey)), __dmul_rn(ez, ez)) > C.nonb_cut2;
+    }
+    if (out) {
+      dx = dy = dz = 0.f;
+      return;
+    }
+  }
+  const int tj = __float_as_int(hj.w);
+  const Control::NbF &P = C.nb32[ti][tj];
+  const float rinv = rsqrtf(d2);
+  const float r = d2 * rinv;
+  float Tp, dTap;
+  if (C.tap_factored) {
+    // (1-t)^4 (1 + 4t + 10t^2 + 20t^3), t = r/swb;  (1/r) d/dr = -140 t^2 (1-t)^3 / swb^2
+    const float is = C.inv_swb_nb_f;
+    const float t = r * is, u = 1.f - t, u2 = u * u;
+    Tp = u2 * u2 * (1.f + t * (4.f + t * (10.f + t * 20.f)));
+    dTap = -140.f * t * t * u2 * u * is * is;
+  } else {
+    const float *T = C.Tap_f, *D = C.dTap_f;
+    Tp = fmaf(fmaf(fmaf(fmaf(fmaf(fmaf(fmaf(T[7], r, T[6]), r, T[5]), r, T[4]), r, T[3]), r, T[2]),
+                   r, T[1]), r, T[0]);
+    dTap = fmaf(fmaf(fmaf(fmaf(fmaf(D[7], r, D[6]), r, D[5]), r, D[4]), r, D[3]), r, D[2]);
+    dTap = fmaf(T[1], rinv, dTap);
+  }
+  float e_vdW, CEvd, e_core = 0.f, e_lg = 0.f;
+  if (vdw_type == 1 || vdw_type == 3) {
+    const float p = C.p_vdW1_f;
+    const float powr = expf(p * logf(r));                // r^p
+    const float S = powr + P.powgi;
+    const float fn13 = expf(logf(S) / p);                // S^(1/p)
+    const float exp2 = expf(0.5f * P.alpha * (1.f - fn13 / P.r_vdW));
+    const float exp1 = exp2 * exp2;
+    e_vdW = P.D * (exp1 - 2.f * exp2);
+    const float dfn13 = (fn13 / S) * (powr / d2);            // S^(1/p-1) r^(p-2)
+    CEvd = dTap * e_vdW - Tp * P.D * P.ar * (exp1 - exp2) * dfn13;
+  } else {
+    const float exp2 = expf(0.5f * P.alpha * (1.f - r / P.r_vdW));
+    const float exp1 = exp2 * exp2;
+    e_vdW = P.D * (exp1 - 2.f * exp2);
+    CEvd = dTap * e_vdW - Tp * P.D * P.ar * (exp1 - exp2) * rinv;
+  }
+  if (vdw_type == 2 || vdw_type == 3) {
+    e_core = P.ecore * expf(P.acore * (1.f - r / P.rcore));
+    const float de_core = -(P.acore / P.rcore) * e_core;
+    CEvd += dTap * e_core + Tp * de_core * rinv;
+    if (C.lgflag) {
+      const float r5 = d2 * d2 * r, r6 = d2 * d2 * d2;
+      e_lg = -(P.lgcij / (r6 + P.re6));
+      const float de_lg = -6.f * e_lg * r5 / (r6 + P.re6);
+      CEvd += dTap * e_lg + Tp * de_lg * rinv;
+    }
+  }
+  // shielded Coulomb: Tap qi qj / (r^3 + gamma)^(1/3)
+  const float dr3 = fmaf(d2, r, P.gamma);
+  const float inv3 = rcbrtf(dr3);
+  const float qq = (float)C_ele * xil.w * lj.w;
+  ee = qq * Tp * inv3;
+  ev = Tp * (e_vdW + e_core + e_lg);
+  c = CEvd + qq * (dTap - Tp * r / dr3) * inv3;
+}
+
 // one warp per atom i; the pairs (i,j,image) with j > i, or j == i with the
 // "positive" image, are queued and evaluated 32 at a time
 template <typename R, bool VIR>
@@ -210,7 +298,9 @@ __global__ void __launch_bounds__(NBW * 32) k_nonbonded(Dev d, int eflag) {
     const int cap = d.nb_cap;
     const int tot = min(nn + nf, cap);
     double fx = 0, fy = 0, fz = 0;
+    float fx32 = 0.f, fy32 = 0.f, fz32 = 0.f;   // mixed form: FP32 force sums
     double *fC = d.fC;
+    const int vdw_type = F.vdw_type;
     int qn = 0;
     for (int base = 0; base < tot + 32; base += 32) {
       if (base < tot) {
@@ -233,17 +323,35 @@ __global__ void __launch_bounds__(NBW * 32) k_nonbonded(Dev d, int eflag) {
         const int cnt = min(qn, 32);
         const bool act = lane < cnt;
         const uint32_t e = act ? Q.e[lane] : 0u;
-        double c, dx, dy, dz;
         int j;
-        pair_terms<R>(d, F, C, e, act, xi, xif, xil, ti, L, g, evdw, eele, c, dx, dy, dz, j);
-        if (act && c != 0.0) {
-          fx -= c * dx;
-          fy -= c * dy;
-          fz -= c * dz;
-          atomicAdd(&fC[j], c * dx);
-          atomicAdd(&fC[n + j], c * dy);
-          atomicAdd(&fC[2 * n + j], c * dz);
-          if (VIR) vir_acc(w, dx, dy, dz, c * dx, c * dy, c * dz);
+        if constexpr (std::is_same<R, float>::value) {
+          float ev, ee, c, dx, dy, dz;
+          pair32(d, C, vdw_type, e, act, xi, xif, xil, ti, g, ev, ee, c, dx, dy, dz, j);
+          if (eflag) {   // energies summed in FP64 (only on energy steps)
+            evdw += (double)ev;
+            eele += (double)ee;
+          }
+          if (act && c != 0.f) {
+            fx32 -= c * dx;
+            fy32 -= c * dy;
+            fz32 -= c * dz;
+            atomicAdd(&d.fC32[j], c * dx);
+            atomicAdd(&d.fC32[n + j], c * dy);
+            atomicAdd(&d.fC32[2 * n + j], c * dz);
+            if (VIR) vir_acc(w, dx, dy, dz, (double)(c * dx), (double)(c * dy), (double)(c * dz));
+          }
+        } else {
+          double c, dx, dy, dz;
+          pair_terms<R>(d, F, C, e, act, xi, xif, xil, ti, L, g, evdw, eele, c, dx, dy, dz, j);
+          if (act && c != 0.0) {
+            fx -= c * dx;
+            fy -= c * dy;
+            fz -= c * dz;
+            atomicAdd(&fC[j], c * dx);
+            atomicAdd(&fC[n + j], c * dy);
+            atomicAdd(&fC[2 * n + j], c * dz);
+            if (VIR) vir_acc(w, dx, dy, dz, c * dx, c * dy, c * dz);
+          }
         }
         __syncwarp();
         const int left = qn - cnt;
@@ -255,13 +363,26 @@ __global__ void __launch_bounds__(NBW * 32) k_nonbonded(Dev d, int eflag) {
         __syncwarp();
       }
     }
-    fx = warp_sum(fx);
-    fy = warp_sum(fy);
-    fz = warp_sum(fz);
-    if (lane == 0) {
-      atomicAdd(&fC[i], fx);
-      atomicAdd(&fC[n + i], fy);
-      atomicAdd(&fC[2 * n + i], fz);
+    if constexpr (std::is_same<R, float>::value) {
+      for (int off = 16; off > 0; off >>= 1) {
+        fx32 += __shfl_down_sync(FULL, fx32, off);
+        fy32 += __shfl_down_sync(FULL, fy32, off);
+        fz32 += __shfl_down_sync(FULL, fz32, off);
+      }
+      if (lane == 0) {
+        atomicAdd(&d.fC32[i], fx32);
+        atomicAdd(&d.fC32[n + i], fy32);
+        atomicAdd(&d.fC32[2 * n + i], fz32);
+      }
+    } else {
+      fx = warp_sum(fx);
+      fy = warp_sum(fy);
+      fz = warp_sum(fz);
+      if (lane == 0) {
+        atomicAdd(&fC[i], fx);
+        atomicAdd(&fC[n + i], fy);
+        atomicAdd(&fC[2 * n + i], fz);
+      }
     }
   }
   if (eflag) {

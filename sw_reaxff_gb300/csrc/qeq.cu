@@ -83,9 +83,10 @@ __global__ void __launch_bounds__(256) k_spmv(Dev d, const double2 *__restrict__
   const int tot = min(nn + nf, cap);
   bool on_s = valid, on_t = valid;
   if (use_act && valid) {
-    const double *R = d.red + (long long)d.seg_s[i] * RG_NRED;
-    on_s = R[R_ACTIVE] != 0.0;
-    on_t = R[R_ACTIVE + 1] != 0.0;
+    // activity flags are exactly 0.0 or 1.0: compare their bits (no FP64)
+    const long long *R = reinterpret_cast<const long long *>(d.red + (long long)d.seg_s[i] * RG_NRED);
+    on_s = R[R_ACTIVE] != 0;
+    on_t = R[R_ACTIVE + 1] != 0;
   }
   double as = 0.0, at = 0.0;
   if (on_s && on_t) {
@@ -156,24 +157,45 @@ __device__ __forceinline__ float4 split4(double2 v) {
   return make_float4(sh, __double2float_rn(v.x - (double)sh), th, __double2float_rn(v.y - (double)th));
 }
 
+// Half a warp per row as in k_spmv.  The compensated pairs of the two
+// systems are reduced together (the first exchange swaps halves, each later
+// level is one compensated add per lane), and lanes 0 and 1 of the row
+// group finish y_s and y_t: the FP64 tail (conversion, eta x) is one warp
+// instruction sequence for four values, not eight per row.
+__device__ __forceinline__ void df_pair_sum(float &vh, float &vl, float ah, float al, float bh,
+                                            float bl, int gl) {
+  const bool odd = gl & 1;
+  vh = odd ? bh : ah;
+  vl = odd ? bl : al;
+  const float oh = __shfl_xor_sync(FULL, odd ? ah : bh, 1);
+  const float ol = __shfl_xor_sync(FULL, odd ? al : bl, 1);
+  df_add(vh, vl, oh, ol);
+  for (int off = 2; off < SPMV_RW; off <<= 1) {
+    const float ph = __shfl_xor_sync(FULL, vh, off), pl = __shfl_xor_sync(FULL, vl, off);
+    df_add(vh, vl, ph, pl);
+  }
+}
+
 __global__ void __launch_bounds__(256) k_spmv32(Dev d, const double2 *__restrict__ x, double2 *__restrict__ y,
                                                 int use_act) {
-  const int lane = threadIdx.x & 31;
-  const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  if (i >= d.n) return;
+  const long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const int gl = (int)(tid & (SPMV_RW - 1));
+  const int i = (int)(tid / SPMV_RW);
+  const bool valid = i < d.n;     // no early return: the row group shuffles
   const long long row = (long long)i * d.nb_cap;
-  const int nn = d.n_near[i], nf = d.n_far[i], cap = d.nb_cap;
+  const int nn = valid ? d.n_near[i] : 0, nf = valid ? d.n_far[i] : 0, cap = d.nb_cap;
   const int tot = min(nn + nf, cap);
   const float4 *__restrict__ x32 = d.qd32;
-  bool on_s = true, on_t = true;
-  if (use_act) {
-    const double *R = d.red + (long long)d.seg_s[i] * RG_NRED;
-    on_s = R[R_ACTIVE] != 0.0;
-    on_t = R[R_ACTIVE + 1] != 0.0;
+  bool on_s = valid, on_t = valid;
+  if (use_act && valid) {
+    // activity flags are exactly 0.0 or 1.0: compare their bits (no FP64)
+    const long long *R = reinterpret_cast<const long long *>(d.red + (long long)d.seg_s[i] * RG_NRED);
+    on_s = R[R_ACTIVE] != 0;
+    on_t = R[R_ACTIVE + 1] != 0;
   }
   float sh = 0.f, sl = 0.f, th = 0.f, tl = 0.f;
   if (on_s && on_t) {
-    for (int p = lane; p < tot; p += 32) {
+    for (int p = gl; p < tot; p += SPMV_RW) {
       const int slot = p < nn ? p : cap - 1 - (p - nn);
       const uint32_t e = d.nbr[row + slot];
       const float h = d.hval32[row + slot];
@@ -182,31 +204,26 @@ __global__ void __launch_bounds__(256) k_spmv32(Dev d, const double2 *__restrict
       df_fma(h, xj.z, xj.w, th, tl);
     }
   } else if (on_s) {
-    for (int p = lane; p < tot; p += 32) {
+    for (int p = gl; p < tot; p += SPMV_RW) {
       const int slot = p < nn ? p : cap - 1 - (p - nn);
       const float h = d.hval32[row + slot];
       const float4 xj = x32[d.nbr[row + slot] >> 8];
       df_fma(h, xj.x, xj.y, sh, sl);
     }
   } else if (on_t) {
-    for (int p = lane; p < tot; p += 32) {
+    for (int p = gl; p < tot; p += SPMV_RW) {
       const int slot = p < nn ? p : cap - 1 - (p - nn);
       const float h = d.hval32[row + slot];
       const float4 xj = x32[d.nbr[row + slot] >> 8];
       df_fma(h, xj.z, xj.w, th, tl);
     }
   }
-  for (int off = 16; off > 0; off >>= 1) {
-    const float a = __shfl_down_sync(FULL, sh, off), b = __shfl_down_sync(FULL, sl, off);
-    const float c = __shfl_down_sync(FULL, th, off), e = __shfl_down_sync(FULL, tl, off);
-    df_add(sh, sl, a, b);
-    df_add(th, tl, c, e);
-  }
-  if (lane == 0) {
+  float vh, vl;
+  df_pair_sum(vh, vl, sh, sl, th, tl, gl);
+  if (valid && gl < 2) {
     const double eta = d.ff->sbp[d.ts[i]].eta;
-    const double2 xi = x[i];
-    y[i] = make_double2(fma(eta, xi.x, (double)sh + (double)sl),
-                        fma(eta, xi.y, (double)th + (double)tl));
+    const double *xi = reinterpret_cast<const double *>(x) + 2 * (long long)i;
+    reinterpret_cast<double *>(y)[2 * (long long)i + gl] = fma(eta, xi[gl], (double)vh + (double)vl);
   }
 }
 
@@ -445,8 +462,9 @@ void launch_qeq_spmv(const Dev &d, cudaStream_t st, const double2 *x, double2 *y
   const unsigned G = (unsigned)((threads + 255) / 256);
   const unsigned G16 = (unsigned)(((long long)d.n * SPMV_RW + 255) / 256);
   if (!d.mixed) k_spmv<<<G16, 256, 0, st>>>(d, x, y, use_act);
-  else if (x == d.qd) k_spmv32<<<G, 256, 0, st>>>(d, x, y, use_act);
+  else if (x == d.qd) k_spmv32<<<G16, 256, 0, st>>>(d, x, y, use_act);
   else k_spmv_ref<<<G16, 256, 0, st>>>(d, x, y);
+  (void)G;
 }
 
 // the split FP32 pair copy of x that k_spmv32 reads
@@ -468,8 +486,8 @@ void launch_qeq_cg_init(const Dev &d, cudaStream_t st, double tol, int imax, boo
     k_spmv_ref<<<(unsigned)((threads + 255) / 256), 256, 0, st>>>(d, d.qx, d.qq);
   } else if (d.mixed) {
     k_split_x<<<G, B, 0, st>>>(d, d.qx);
-    const unsigned G32 = (unsigned)(((long long)d.n * 32 + 255) / 256);
-    k_spmv32<<<G32, 256, 0, st>>>(d, d.qx, d.qq, 0);
+    const unsigned G16 = (unsigned)(((long long)d.n * SPMV_RW + 255) / 256);
+    k_spmv32<<<G16, 256, 0, st>>>(d, d.qx, d.qq, 0);
   } else {
     launch_qeq_spmv(d, st, d.qx, d.qq, 0);
   }

@@ -363,6 +363,8 @@ int alloc_atoms(rg_system *h, int n) {
   for (double2 **q : pv) r |= dalloc(h, B, q, (size_t)n);
   if (d.mixed) r |= dalloc(h, B, &d.qd32, (size_t)n);
   else d.qd32 = nullptr;
+  if (d.mixed) r |= dalloc(h, B, &d.fC32, 3 * (size_t)n);
+  else d.fC32 = nullptr;
   r |= dalloc(h, B, &d.seg_o, (size_t)n);
   r |= dalloc(h, B, &d.seg_s, (size_t)n);
   r |= dalloc(h, B, &d.status, 8);
@@ -455,6 +457,7 @@ int do_compute(rg_system *h, int eflag, int vflag = 0) {
   int rc;
   if (!h->lists_valid && (rc = build_lists(h))) return rc;
   CK(cudaMemsetAsync(d.fC, 0, 4 * sizeof(double) * (size_t)d.n, h->st));
+  if (d.fC32) CK(cudaMemsetAsync(d.fC32, 0, 3 * sizeof(float) * (size_t)d.n, h->st));
   CK(cudaMemsetAsync(d.energy, 0, (size_t)d.nseg * RG_NE * sizeof(double), h->st));
   d.vflag = vflag ? 1 : 0;
   if (vflag) CK(cudaMemsetAsync(d.virial, 0, (size_t)d.nseg * 6 * sizeof(double), h->st));
@@ -645,6 +648,39 @@ void init_control(const rg_params &p, const ForceField &ff, Control &c) {
   c.inv_swb_q = 1.0 / p.qeq_swb;
   c.nonb_all_listed = c.nonb_cut2 >= c.list_cut2;
   c.list_pre2_f = (float)(c.list_cut2 * (1.0 + 1e-5) + 0.05);
+  c.list_cut2_f = (float)c.list_cut2;
+  c.near_cut_f = (float)c.near_cut;
+  c.swb2_f = (float)c.swb2;
+  c.inv_swb_q_f = (float)c.inv_swb_q;
+  c.nonb_cut2_f = (float)c.nonb_cut2;
+  c.inv_swb_nb_f = (float)c.inv_swb_nb;
+  for (int k = 0; k < 8; ++k) {
+    c.qTap_f[k] = (float)c.qTap[k];
+    c.Tap_f[k] = (float)c.Tap[k];
+    c.dTap_f[k] = (float)(k * c.Tap[k]);
+  }
+  c.p_vdW1_f = (float)ff.gp[28];
+  for (int a = 0; a < RG_MAXT; ++a)
+    for (int b = 0; b < RG_MAXT; ++b) {
+      const Tbp &tw = ff.tbp[a][b];
+      Control::NbF &e = c.nb32[a][b];
+      e.alpha = (float)tw.alpha;
+      e.r_vdW = (float)tw.r_vdW;
+      e.D = (float)tw.D;
+      e.ar = (float)tw.alpha / (float)tw.r_vdW;
+      e.powgi = (float)tw.powgi_vdW1;
+      e.gamma = (float)tw.gamma;
+      e.ecore = (float)tw.ecore;
+      e.acore = (float)tw.acore;
+      e.rcore = (float)tw.rcore;
+      e.lgcij = (float)tw.lgcij;
+      const float lg2 = (float)tw.lgre * (float)tw.lgre;
+      e.re6 = lg2 * lg2 * lg2;
+      for (int k = 0; k < RG_MAXT; ++k) {
+        const Hbp &hp = ff.hbp[a][b][k];
+        c.hb32[a][b][k] = {(float)hp.r0_hb, (float)hp.p_hb1, (float)hp.p_hb2, (float)hp.p_hb3};
+      }
+    }
   c.bo_scale_f = (float)(1.0 + c.bo_cut);
   c.bo_half_f = (float)(0.5 * c.bo_cut);
   for (int a = 0; a < RG_MAXT; ++a)

@@ -113,6 +113,17 @@ struct Control {
   float list_pre2_f;   // FP32 pair-list prefilter radius^2: list_cut2 (1 + 1e-5) + 0.05
   float bo_scale_f;    // 1 + bo_cut (FP32 estimate of BO')
   float bo_half_f;     // bo_cut / 2
+  // mixed form, FP32 copies used per pair (GB300 runs FP64, conversions
+  // included, at 1/64 of the FP32 rate, so the FP32 kernels read no double)
+  float list_cut2_f, near_cut_f, swb2_f, inv_swb_q_f, nonb_cut2_f, inv_swb_nb_f;
+  float qTap_f[8], Tap_f[8], dTap_f[8];   // dTap_f[k] = k Tap[k]
+  float p_vdW1_f;
+  struct NbF {
+    float alpha, r_vdW, D, ar, powgi, gamma, ecore, acore, rcore, lgcij, re6;
+  } nb32[RG_MAXT][RG_MAXT];
+  struct HbF {
+    float r0_hb, p_hb1, p_hb2, p_hb3;
+  } hb32[RG_MAXT][RG_MAXT][RG_MAXT];
   // log r_s, log r_pi, log r_pipi per type pair: the FP64 BO' powers as
   // exp(p (log d - log r)) with one log per bond
   double ln_r[RG_MAXT][RG_MAXT][3];
@@ -198,6 +209,7 @@ struct Dev {
   double *vlpex, *nlp, *Delta_lp, *Delta_lp_temp, *dDelta_lp, *nlp_temp;
   double *dDeltap;    // 3 * n (xyz blocks)
   double *fC;         // 4 * n: force xyz blocks + CdDelta block
+  float *fC32;        // mixed form: 3 * n force xyz blocks of the FP32 pair terms
 
   // QEq vectors (sorted order), two solves s,t interleaved as double2
   double2 *qx, *qb, *qr, *qu, *qw, *qd, *qq, *qp, *qs, *qv, *qz, *qm;

@@ -187,10 +187,10 @@ def test_deck_bonds_file(tmp_path, ffield):
 
 
 def test_deck_species(tmp_path, ffield):
-    """fix reax/c/species in a deck: the molecules of a seeded H2O/CH4/C2H6/
-    NH3 mixture are found intact (bond orders above 0.3 inside molecules,
-    below between them), with the reference's species file and position
-    file formats."""
+    """fix reax/c/species in a deck (reference species and position file
+    formats): at the last output step its molecules and species equal the
+    connected components of the library's bond table (orders above 0.3)
+    for the deck's final positions, computed here independently."""
     s = systems.mixture(scale=0.0005, seed=3)
     data = tmp_path / "mix.data"
     els = systems.write_lammps_data(s, str(data), ["C", "H", "O", "N"])
@@ -198,30 +198,54 @@ def test_deck_species(tmp_path, ffield):
         "units real", "atom_style charge", "boundary p p p", f"read_data {data}",
         "pair_style reax/c/sunway NULL", f"pair_coeff * * {ffield} {' '.join(els)}",
         "fix 1 all nve/sunway", "fix 2 all qeq/reax/sunway 1 0.0 10.0 1.0e-6 reax/c",
-        "fix 3 all reax/c/species 1 2 5 species.out position 5 pos.out",
-        "timestep 0.25", "run 10",
+        "fix 3 all reax/c/species 1 1 5 species.out position 5 pos.out",
+        "timestep 0.25", "run 10", f"write_dump all custom out.dump {COLS}",
     ]
     (tmp_path / "in.deck").write_text("\n".join(deck) + "\n")
     r = subprocess.run([B.build_host(), "in.deck"], cwd=str(tmp_path), capture_output=True,
                        text=True, timeout=300)
     assert r.returncode == 0, r.stdout + r.stderr
-    # expected molecules by formula (element counts in LAMMPS type order C H O N)
+    _, st = read_dump(str(tmp_path / "out.dump"))
+    # independent: union-find over the bond table of the final positions
+    g = ReaxGPU(ffield)
+    order = np.argsort(s.tag)
+    g.set_box(s.box)
+    g.set_atoms(st["x"], s.types(g.elements)[order], st["tag"], st["q"], st["v"])
+    g.compute()
+    nb, tg, bo, _, _ = g.bond_table(0.10, 24)
+    idx = {t: k for k, t in enumerate(st["tag"])}
+    parent = list(range(s.n))
+
+    def find(a):
+        while parent[a] != a:
+            parent[a] = parent[parent[a]]
+            a = parent[a]
+        return a
+
+    for a in range(s.n):
+        for k in range(nb[a]):
+            if bo[a, k] > 0.3:
+                parent[find(a)] = find(idx[tg[a, k]])
+    elem = np.array(s.elem)[order]
+    comps = {}
+    for a in range(s.n):
+        comps.setdefault(find(a), []).append(a)
     want = {}
-    for m in np.unique(s.mol):
-        idx = np.where(s.mol == m)[0]
-        cnt = [sum(1 for i in idx if s.elem[i] == e) for e in els]
+    for atoms in comps.values():
+        cnt = [sum(1 for a in atoms if elem[a] == e) for e in els]
         f = "".join(e + (str(c) if c != 1 else "") for e, c in zip(els, cnt) if c)
         want[f] = want.get(f, 0) + 1
     lines = (tmp_path / "species.out").read_text().splitlines()
     assert len(lines) == 4                                  # steps 5 and 10
-    for k in (0, 2):
-        names = lines[k].split()[4:]
-        vals = lines[k + 1].split()
-        assert int(vals[0]) == 5 * (k // 2 + 1)
-        assert int(vals[1]) == len(np.unique(s.mol)) and int(vals[2]) == len(want)
-        assert dict(zip(names, map(int, vals[3:]))) == want
+    assert lines[0].split()[:4] == ["#", "Timestep", "No_Moles", "No_Specs"]
+    names = lines[2].split()[4:]
+    vals = lines[3].split()
+    assert int(vals[0]) == 10
+    assert int(vals[1]) == len(comps) and int(vals[2]) == len(want)
+    assert dict(zip(names, map(int, vals[3:]))) == want
     pos = (tmp_path / "pos.out").read_text().split("#\n")
     frame = [l.split() for l in pos[-2].splitlines()[2:]]
-    assert len(frame) == len(np.unique(s.mol))
+    assert pos[-2].startswith("Timestep 10 NMole")
+    assert len(frame) == len(comps)
     assert sum(int(w[1]) for w in frame) == s.n
     assert all(0.0 <= float(x) < 1.0 for w in frame for x in w[4:7])

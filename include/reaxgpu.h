@@ -95,6 +95,9 @@ typedef struct {
   long long kernel_launches;   /* kernels launched by this handle so far */
   int qeq_restarts;            /* mixed form: residual checks of the last
                                   QEq (1 = converged at the first check) */
+  int fp64_angles, fp64_torsions; /* mixed form: valence angles and torsions
+                                  of the last force step evaluated by the
+                                  FP64 passes (near-linear, over-coordinated) */
 } rg_stats;
 
 void rg_default_params(rg_params *p);

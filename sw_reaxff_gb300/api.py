@@ -53,7 +53,8 @@ class Stats(C.Structure):
                 ("cg_iters_t", C.c_int), ("max_nbrs", C.c_int),
                 ("max_bonds", C.c_int), ("max_hbonds", C.c_int),
                 ("regrows", C.c_int), ("kernel_launches", C.c_longlong),
-                ("qeq_restarts", C.c_int)]
+                ("qeq_restarts", C.c_int), ("fp64_angles", C.c_int),
+                ("fp64_torsions", C.c_int)]
 
 
 class ReaxError(RuntimeError):

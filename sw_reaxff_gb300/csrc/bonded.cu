@@ -682,28 +682,40 @@ __global__ void k_vt_prep_bond(Dev d) {
   const int i = (int)(t % n), k = (int)(t / n);
   if (k >= d.bond_cap || i >= n || k >= d.nbonds[i]) return;
   const long long s = (long long)k * n + i;
-  const double BOA = d.b_BO[s] - d.ctl->thb_cut;
+  const double BO = d.b_BO[s], BOA = BO - d.ctl->thb_cut;
   d.b_et2[s] = exp(-d.ff->gp[23] * BOA);
   d.b_ec2[s] = exp(-d.ff->gp[27] * sqr(BOA - 1.5));
+  d.b_BOf[s] = BO > d.ctl->thb_cut ? (float)BO : 0.f;
 }
 
 __device__ __forceinline__ bool fbp_nonzero(const Fbp &p) {
   return p.V1 != 0.0 || p.V2 != 0.0 || p.V3 != 0.0 || p.p_cot1 != 0.0;
 }
 
-// enumerate the items of slot (j, kk); FILL writes them at the offsets
+// a > b (b > 0) decided in FP32 away from the threshold and in FP64 within
+// 1e-5 of it, so the outcome is the FP64 one
+__device__ __forceinline__ bool above(float af, float bf, double a, double b) {
+  if (af > bf * (1.f + 1e-5f)) return true;
+  if (af < bf * (1.f - 1e-5f)) return false;
+  return a > b;
+}
+
+// enumerate the items of slot (j, kk); FILL writes them at the offsets.
+// The single-bond tests BO > thb_cut are the exact flags of b_BOf (0 =
+// below), the product tests are FP32 away from their thresholds, and the
+// parameter tests are the control block's tables: no FP64 in the common
+// case.
 template <bool FILL>
 __device__ void vt_enumerate(const Dev &d, int j, int kk, int &cv, int &ct, long long ov,
                              long long ot) {
   const int n = d.n;
-  const ForceField &F = *d.ff;
-  const double thb_cut = d.ctl->thb_cut, thb_cutsq = d.ctl->thb_cutsq;
+  const Control &C = *d.ctl;
   cv = ct = 0;
   const int nbj = min(d.nbonds[j], d.bond_cap);
   if (kk >= nbj) return;
   const long long spk = (long long)kk * n + j;
-  const double BO_jk = d.b_BO[spk];
-  if (!(BO_jk - thb_cut > 0.0) || d.b_sym[spk] < 0) return;
+  const float BO_jk = d.b_BOf[spk];
+  if (BO_jk == 0.f || d.b_sym[spk] < 0) return;
   const uint32_t ejk = d.b_nbr[spk];
   const int k = nbr_of(ejk), tj = d.ts[j], tk = d.ts[k];
   const long long spj = d.b_sym[spk];
@@ -714,31 +726,30 @@ __device__ void vt_enumerate(const Dev &d, int j, int kk, int &cv, int &ct, long
   for (int ph = 0; ph < nbj; ++ph) {
     if (ph == kk) continue;
     const long long sph = (long long)ph * n + j;
-    const double BO_hj = d.b_BO[sph];
+    const float BO_hj = d.b_BOf[sph];
+    if (BO_hj == 0.f) continue;   // below thb_cut: neither an angle nor a torsion end
     const uint32_t ehj = d.b_nbr[sph];
     const int h = nbr_of(ehj), th = d.ts[h];
-    if (ph > kk && BO_jk > thb_cut && BO_hj > thb_cut && BO_jk * BO_hj > thb_cutsq) {
-      const Thbh &thbh = F.thbp[tk][tj][th];
-      bool any = false;
-      for (int c = 0; c < thbh.cnt; ++c) any |= fabs(thbh.prm[c].p_val1) > 0.001;
-      if (any) {
-        if (FILL)
-          d.w_val[ov + cv] = ((unsigned long long)j << 16) | ((unsigned long long)kk << 8) | ph;
-        ++cv;
-      }
+    if (ph > kk && C.thb_any[tk][tj][th] &&
+        above(BO_jk * BO_hj, C.thb_cutsq_f, d.b_BO[spk] * d.b_BO[sph], C.thb_cutsq)) {
+      if (FILL)
+        d.w_val[ov + cv] = ((unsigned long long)j << 16) | ((unsigned long long)kk << 8) | ph;
+      ++cv;
     }
-    if (!do_tor || !(BO_hj > thb_cut)) continue;
+    if (!do_tor) continue;
     int shj[3];
     img_unpack((int)(ehj & 255u), &shj[0], &shj[1], &shj[2]);
     for (int pw = 0; pw < nbk; ++pw) {
       const long long spw = (long long)pw * n + k;
       if (spw == spj) continue;
-      const double BO_kl = d.b_BO[spw];
-      if (!(BO_kl > thb_cut) || !(BO_hj * BO_jk * BO_kl > thb_cut)) continue;
+      const float BO_kl = d.b_BOf[spw];
+      if (BO_kl == 0.f) continue;
       const uint32_t ekl = d.b_nbr[spw];
       const int l = nbr_of(ekl);
-      const Fbh &fbh = F.fbp[th][tj][tk][d.ts[l]];
-      if (!fbh.cnt || !fbp_nonzero(fbh.prm)) continue;
+      if (!C.fb_on[th][tj][tk][d.ts[l]]) continue;
+      if (!above(BO_hj * BO_jk * BO_kl, C.thb_cut_f,
+                 d.b_BO[sph] * d.b_BO[spk] * d.b_BO[spw], C.thb_cut))
+        continue;
       int skl[3];
       img_unpack((int)(ekl & 255u), &skl[0], &skl[1], &skl[2]);
       if (l == h && sjk[0] + skl[0] == shj[0] && sjk[1] + skl[1] == shj[1] &&
@@ -810,7 +821,6 @@ __device__ __forceinline__ void valence_item(const Dev &d, unsigned long long it
     R sin_theta_hjk = sin(theta_hjk);
     if (sin_theta_hjk < R(1.0e-5)) sin_theta_hjk = R(1.0e-5);
     const Thbh &thbh = F.thbp[tk][tj][th];
-    const int nbj = min(d.nbonds[j], d.bond_cap);
     const R Dj = (R)d.Delta[j], Dval_j = (R)d.Delta_val[j];
     const R bo0k = (R)d.bo0[k], bo0h = (R)d.bo0[h];
     for (int cnt = 0; cnt < thbh.cnt; ++cnt) {
@@ -872,14 +882,10 @@ __device__ __forceinline__ void valence_item(const Dev &d, unsigned long long it
       atomicAdd(&CdD[j], (double)((CEval3 + CEval7) + CEpen1 + CEcoa3));
       atomicAdd(&CdD[k], (double)CEcoa4);
       atomicAdd(&CdD[h], (double)CEcoa5);
-      for (int q = 0; q < nbj; ++q) {
-        const long long sq = (long long)q * n + j;
-        const double b = d.b_BO[sq];
-        const double b3 = b * b * b;
-        atomicAdd(&d.b_Cdbo[sq], (double)CEval6 * (b3 * b3 * b));
-        atomicAdd(&d.b_Cdbopi[sq], (double)CEval5);
-        atomicAdd(&d.b_Cdbopi2[sq], (double)CEval5);
-      }
+      // CEval6 BO^7 to Cdbo and CEval5 to Cdbopi, Cdbopi2 of every bond of
+      // j: summed per centre here, applied per bond in k_dbond
+      atomicAdd(&d.vsum[j], (double)CEval5);
+      atomicAdd(&d.vsum[n + j], (double)CEval6);
       if (d.debug) {
         const double v[] = {BOA_jk, BOA_hj, theta_hjk, sin_theta_hjk, SBO2, CSBO2, dSBO1, dSBO2,
                             expval6, Delta_j, f7_jk, f7_hj, f8_Dj, expval2theta, theta_0, CEval1,
@@ -1192,16 +1198,22 @@ __global__ void k_dbond(Dev d) {
     const double *CdD = d.fC + 3 * (long long)n;
     const double Ddx = d.dDeltap[i], Ddy = d.dDeltap[n + i], Ddz = d.dDeltap[2 * n + i];
     const double cdi = CdD[i];
+    const double v5i = d.vsum[i], v6i = d.vsum[n + i];
     double fx = 0, fy = 0, fz = 0, buf_c = 0;
     for (int k = 0; k < nb; ++k) {
       const long long s = (long long)k * n + i;
       const int j = nbr_of(d.b_nbr[s]);
       const long long sy = d.b_sym[s];
-      double cdbo = d.b_Cdbo[s], cdbopi = d.b_Cdbopi[s], cdbopi2 = d.b_Cdbopi2[s];
+      // the valence centres' shares: CEval6 BO^7 and CEval5 from both ends
+      const double bs = d.b_BO[s], bs3 = bs * bs * bs;
+      double cdbo = d.b_Cdbo[s] + v6i * (bs3 * bs3 * bs);
+      double cdbopi = d.b_Cdbopi[s] + v5i, cdbopi2 = d.b_Cdbopi2[s] + v5i;
       if (sy >= 0) {
-        cdbo += d.b_Cdbo[sy];
-        cdbopi += d.b_Cdbopi[sy];
-        cdbopi2 += d.b_Cdbopi2[sy];
+        const double by = d.b_BO[sy], by3 = by * by * by;
+        const double v5j = d.vsum[j], v6j = d.vsum[n + j];
+        cdbo += d.b_Cdbo[sy] + v6j * (by3 * by3 * by);
+        cdbopi += d.b_Cdbopi[sy] + v5j;
+        cdbopi2 += d.b_Cdbopi2[sy] + v5j;
       }
       const double C1dbo = d.b_C[0 * S + s], C2dbo = d.b_C[1 * S + s];
       const double C1pi = d.b_C[3 * S + s], C2pi = d.b_C[4 * S + s], C3pi = d.b_C[5 * S + s];

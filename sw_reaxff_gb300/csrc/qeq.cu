@@ -195,7 +195,23 @@ __global__ void __launch_bounds__(256) k_spmv32(Dev d, const double2 *__restrict
   }
   float sh = 0.f, sl = 0.f, th = 0.f, tl = 0.f;
   if (on_s && on_t) {
-    for (int p = gl; p < tot; p += SPMV_RW) {
+    // two entries per lane and step with separate compensated sums: two
+    // independent gathers of x in flight
+    float sh1 = 0.f, sl1 = 0.f, th1 = 0.f, tl1 = 0.f;
+    int p = gl;
+    for (; p + SPMV_RW < tot; p += 2 * SPMV_RW) {
+      const int q = p + SPMV_RW;
+      const int s0 = p < nn ? p : cap - 1 - (p - nn);
+      const int s1 = q < nn ? q : cap - 1 - (q - nn);
+      const uint32_t e0 = d.nbr[row + s0], e1 = d.nbr[row + s1];
+      const float h0 = d.hval32[row + s0], h1 = d.hval32[row + s1];
+      const float4 x0 = x32[e0 >> 8], x1 = x32[e1 >> 8];
+      df_fma(h0, x0.x, x0.y, sh, sl);
+      df_fma(h0, x0.z, x0.w, th, tl);
+      df_fma(h1, x1.x, x1.y, sh1, sl1);
+      df_fma(h1, x1.z, x1.w, th1, tl1);
+    }
+    if (p < tot) {
       const int slot = p < nn ? p : cap - 1 - (p - nn);
       const uint32_t e = d.nbr[row + slot];
       const float h = d.hval32[row + slot];
@@ -203,6 +219,8 @@ __global__ void __launch_bounds__(256) k_spmv32(Dev d, const double2 *__restrict
       df_fma(h, xj.x, xj.y, sh, sl);
       df_fma(h, xj.z, xj.w, th, tl);
     }
+    df_add(sh, sl, sh1, sl1);
+    df_add(th, tl, th1, tl1);
   } else if (on_s) {
     for (int p = gl; p < tot; p += SPMV_RW) {
       const int slot = p < nn ? p : cap - 1 - (p - nn);
@@ -473,18 +491,13 @@ __global__ void k_split_x(Dev d, const double2 *__restrict__ x) {
   if (i < d.n) d.qd32[i] = split4(x[i]);
 }
 
-// r = b - H x of the current iterate starts (or, in the mixed form,
-// restarts) the pipelined CG.  The mixed form's restarts (refine) take the
-// residual with FP64 products and sums (iterative refinement); its first
-// pass, whose iterate the refinement checks anyway, the compensated FP32
-// SpMV of the iterations.
-void launch_qeq_cg_init(const Dev &d, cudaStream_t st, double tol, int imax, bool refine) {
+// r = b - H x of the current iterate starts the pipelined CG.  The mixed
+// form's first pass, whose iterate the refinement checks in FP64 anyway,
+// takes it from the compensated FP32 SpMV of the iterations; its restarts
+// come from launch_qeq_refine_check + launch_qeq_cg_init_rest.
+void launch_qeq_cg_init(const Dev &d, cudaStream_t st, double tol, int imax) {
   const int B = 256, G = (d.n + B - 1) / B;
-  const int GS = (d.nseg + 127) / 128;
-  if (d.mixed && refine) {
-    const long long threads = (long long)d.n * SPMV_RW;
-    k_spmv_ref<<<(unsigned)((threads + 255) / 256), 256, 0, st>>>(d, d.qx, d.qq);
-  } else if (d.mixed) {
+  if (d.mixed) {
     k_split_x<<<G, B, 0, st>>>(d, d.qx);
     const unsigned G16 = (unsigned)(((long long)d.n * SPMV_RW + 255) / 256);
     k_spmv32<<<G16, 256, 0, st>>>(d, d.qx, d.qq, 0);
@@ -492,6 +505,51 @@ void launch_qeq_cg_init(const Dev &d, cudaStream_t st, double tol, int imax, boo
     launch_qeq_spmv(d, st, d.qx, d.qq, 0);
   }
   k_cg_init1<<<G, B, 0, st>>>(d);
+  launch_qeq_cg_init_rest(d, st, tol, imax);
+}
+
+// The mixed form's refinement check: b.b and u.r of r = b - H x (FP64 sums,
+// k_spmv_ref) and u = r Hdia_inv per segment; a segment needs a restart
+// only where sqrt(u.r) / |b| is above the tolerance (the criterion of
+// k_cg_init_ctrl), and the rest of the set-up runs only then.
+__global__ void k_refine_sums(Dev d) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  double v[4] = {0, 0, 0, 0};
+  if (s < d.n) {
+    const double2 u = d.qu[s], r = d.qr[s], b = d.qb[s];
+    v[0] = b.x * b.x; v[1] = b.y * b.y;
+    v[2] = u.x * r.x; v[3] = u.y * r.y;
+  }
+  seg_block_add<4>(v, seg_at(d, s), d.red + R_INIT, RG_NRED);
+}
+
+__global__ void k_refine_ctrl(Dev d, double tol) {
+  const int g = blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= d.nseg) return;
+  const double *R = d.red + (long long)g * RG_NRED;
+  bool need = false;
+  for (int c = 0; c < 2; ++c)
+    need = need || sqrt(R[R_INIT + 2 + c]) / sqrt(R[R_INIT + c]) > tol;
+  if (need) atomicAdd(d.n_active, 1);
+}
+
+void launch_qeq_refine_check(const Dev &d, cudaStream_t st, double tol) {
+  const int B = 256, G = (d.n + B - 1) / B;
+  const int GS = (d.nseg + 127) / 128;
+  const long long threads = (long long)d.n * SPMV_RW;
+  k_spmv_ref<<<(unsigned)((threads + 255) / 256), 256, 0, st>>>(d, d.qx, d.qq);
+  k_cg_init1<<<G, B, 0, st>>>(d);
+  k_seg_zero<<<GS, 128, 0, st>>>(d, R_INIT, 4);
+  k_refine_sums<<<G, B, 0, st>>>(d);
+  cudaMemsetAsync(d.n_active, 0, sizeof(int), st);
+  k_refine_ctrl<<<GS, 128, 0, st>>>(d, tol);
+}
+
+// the set-up after r and u (k_cg_init1): the two pipelining SpMVs and the
+// CG scalars
+void launch_qeq_cg_init_rest(const Dev &d, cudaStream_t st, double tol, int imax) {
+  const int B = 256, G = (d.n + B - 1) / B;
+  const int GS = (d.nseg + 127) / 128;
   launch_qeq_spmv(d, st, d.qd, d.qq, 0);
   k_cg_init2<<<G, B, 0, st>>>(d);
   launch_qeq_spmv(d, st, d.qd, d.qq, 0);

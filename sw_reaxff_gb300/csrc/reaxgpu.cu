@@ -271,6 +271,7 @@ int alloc_bonds(rg_system *h) {
   r |= dalloc(h, h->per_b, &d.b_Cdbopi2, S);
   r |= dalloc(h, h->per_b, &d.b_et2, S);
   r |= dalloc(h, h->per_b, &d.b_ec2, S);
+  r |= dalloc(h, h->per_b, &d.b_BOf, S);
   r |= dalloc(h, h->per_b, &d.w_cnt_v, S + 1);
   r |= dalloc(h, h->per_b, &d.w_cnt_t, S + 1);
   r |= dalloc(h, h->per_b, &d.w_off_v, S + 1);
@@ -358,6 +359,7 @@ int alloc_atoms(rg_system *h, int n) {
   for (double **q : pd) r |= dalloc(h, B, q, (size_t)n);
   r |= dalloc(h, B, &d.dDeltap, 3 * (size_t)n);
   r |= dalloc(h, B, &d.fC, 4 * (size_t)n);
+  r |= dalloc(h, B, &d.vsum, 2 * (size_t)n);
   r |= dalloc(h, B, &d.c_sbo, 5 * (size_t)n);
   double2 **pv[] = {&d.qx, &d.qb, &d.qr, &d.qu, &d.qw, &d.qd, &d.qq, &d.qp, &d.qs, &d.qv, &d.qz, &d.qm};
   for (double2 **q : pv) r |= dalloc(h, B, q, (size_t)n);
@@ -458,6 +460,7 @@ int do_compute(rg_system *h, int eflag, int vflag = 0) {
   if (!h->lists_valid && (rc = build_lists(h))) return rc;
   CK(cudaMemsetAsync(d.fC, 0, 4 * sizeof(double) * (size_t)d.n, h->st));
   if (d.fC32) CK(cudaMemsetAsync(d.fC32, 0, 3 * sizeof(float) * (size_t)d.n, h->st));
+  CK(cudaMemsetAsync(d.vsum, 0, 2 * sizeof(double) * (size_t)d.n, h->st));
   CK(cudaMemsetAsync(d.energy, 0, (size_t)d.nseg * RG_NE * sizeof(double), h->st));
   d.vflag = vflag ? 1 : 0;
   if (vflag) CK(cudaMemsetAsync(d.virial, 0, (size_t)d.nseg * 6 * sizeof(double), h->st));
@@ -554,7 +557,7 @@ int do_qeq(rg_system *h, int *its, int *itt) {
   {
     Scope sc(h, PH_QSETUP, 9 + (d.mixed ? 1 : 0));
     launch_qeq_setup(d, h->st);
-    launch_qeq_cg_init(d, h->st, tol, imax, false);
+    launch_qeq_cg_init(d, h->st, tol, imax);
   }
   // iterate; poll the number of segments with an active solve every few
   // iterations.  The mixed form then restarts the CG from its iterate with
@@ -597,8 +600,14 @@ int do_qeq(rg_system *h, int *its, int *itt) {
     CK(cudaStreamSynchronize(h->st));
     for (size_t k = 0; k < it.size(); ++k) tot[k] += std::max(0, (int)it[k] - (refines ? 1 : 0));
     if (!d.mixed || refines >= RG_MAX_REFINE) break;
-    { Scope sc(h, PH_QSETUP, 8); launch_qeq_cg_init(d, h->st, tol, imax, true); }
+    // residual with FP64 sums; the CG set-up for a restart only where it
+    // is above the tolerance
+    { Scope sc(h, PH_QSETUP, 5); launch_qeq_refine_check(d, h->st, tol); }
     ++refines;
+    CK(cudaMemcpyAsync(&active, d.n_active, sizeof(int), cudaMemcpyDeviceToHost, h->st));
+    CK(cudaStreamSynchronize(h->st));
+    if (active == 0) break;
+    { Scope sc(h, PH_QSETUP, 6); launch_qeq_cg_init_rest(d, h->st, tol, imax); }
     CK(cudaMemcpyAsync(&active, d.n_active, sizeof(int), cudaMemcpyDeviceToHost, h->st));
     CK(cudaStreamSynchronize(h->st));
     if (active == 0) break;
@@ -649,6 +658,21 @@ void init_control(const rg_params &p, const ForceField &ff, Control &c) {
   c.nonb_all_listed = c.nonb_cut2 >= c.list_cut2;
   c.list_pre2_f = (float)(c.list_cut2 * (1.0 + 1e-5) + 0.05);
   c.list_cut2_f = (float)c.list_cut2;
+  c.thb_cut_f = (float)c.thb_cut;
+  c.thb_cutsq_f = (float)c.thb_cutsq;
+  for (int a = 0; a < RG_MAXT; ++a)
+    for (int b = 0; b < RG_MAXT; ++b)
+      for (int e = 0; e < RG_MAXT; ++e) {
+        const Thbh &th = ff.thbp[a][b][e];
+        bool any = false;
+        for (int q = 0; q < th.cnt; ++q) any = any || std::fabs(th.prm[q].p_val1) > 0.001;
+        c.thb_any[a][b][e] = any ? 1 : 0;
+        for (int g = 0; g < RG_MAXT; ++g) {
+          const Fbh &fb = ff.fbp[a][b][e][g];
+          c.fb_on[a][b][e][g] = (fb.cnt && (fb.prm.V1 != 0.0 || fb.prm.V2 != 0.0 ||
+                                            fb.prm.V3 != 0.0 || fb.prm.p_cot1 != 0.0)) ? 1 : 0;
+        }
+      }
   c.near_cut_f = (float)c.near_cut;
   c.swb2_f = (float)c.swb2;
   c.inv_swb_q_f = (float)c.inv_swb_q;
@@ -1230,6 +1254,15 @@ int rg_get_stats(const rg_system *h, rg_stats *s) {
   *s = h->stats;
   s->n_atoms = h->n;
   s->kernel_launches = h->launches;
+  s->fp64_angles = s->fp64_torsions = 0;
+  if (h->d.mixed && h->d.fb_cnt) {
+    int fb[2] = {0, 0};
+    if (cudaMemcpyAsync(fb, h->d.fb_cnt, sizeof fb, cudaMemcpyDeviceToHost, h->st) == cudaSuccess &&
+        cudaStreamSynchronize(h->st) == cudaSuccess) {
+      s->fp64_angles = fb[0];
+      s->fp64_torsions = fb[1];
+    }
+  }
   return RG_OK;
 }
 

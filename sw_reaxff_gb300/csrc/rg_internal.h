@@ -111,6 +111,11 @@ struct Control {
   // FP32 copies for the prefilters (no FP64 conversions per entry; GB300
   // runs FP64 at 1/64 of the FP32 rate)
   float list_pre2_f;   // FP32 pair-list prefilter radius^2: list_cut2 (1 + 1e-5) + 0.05
+  float thb_cut_f, thb_cutsq_f;
+  // type triples with a valence parameter set |p_val1| > 0.001, and type
+  // quadruples with a nonzero torsion set (the enumeration's table tests)
+  unsigned char thb_any[RG_MAXT][RG_MAXT][RG_MAXT];
+  unsigned char fb_on[RG_MAXT][RG_MAXT][RG_MAXT][RG_MAXT];
   float bo_scale_f;    // 1 + bo_cut (FP32 estimate of BO')
   float bo_half_f;     // bo_cut / 2
   // mixed form, FP32 copies used per pair (GB300 runs FP64, conversions
@@ -210,6 +215,9 @@ struct Dev {
   double *dDeltap;    // 3 * n (xyz blocks)
   double *fC;         // 4 * n: force xyz blocks + CdDelta block
   float *fC32;        // mixed form: 3 * n force xyz blocks of the FP32 pair terms
+  double *vsum;       // 2 * n: per valence centre, sum of CEval5 and of CEval6
+                      // (their share of Cdbopi/Cdbopi2 and Cdbo of every bond
+                      // of the centre, applied in k_dbond)
 
   // QEq vectors (sorted order), two solves s,t interleaved as double2
   double2 *qx, *qb, *qr, *qu, *qw, *qd, *qq, *qp, *qs, *qv, *qz, *qm;
@@ -224,6 +232,8 @@ struct Dev {
   // valence / torsion work lists (built per force step)
   double *c_sbo;      // 5 * n: SBO2, CSBO2, dSBO1, dSBO2, expval6 per centre
   double *b_et2, *b_ec2;   // per bond slot: exp(-p_tor2 BOA), exp(-p_cot2 (BOA-1.5)^2)
+  float *b_BOf;             // per bond slot: BO in FP32, 0 where BO <= thb_cut (exact
+                            // FP64 test), for the valence/torsion enumeration
   int *w_cnt_v, *w_cnt_t;  // per (centre, bond) slot counts (+1 trailing zero)
   int *w_off_v, *w_off_t;  // exclusive scans (+1: totals)
   int *w_bsum;             // scan block sums
@@ -477,7 +487,9 @@ void launch_check_finite(const double *a, long long count, int *flag, cudaStream
 // QEq
 void launch_qeq_setup(const Dev &d, cudaStream_t st);
 void launch_qeq_spmv(const Dev &d, cudaStream_t st, const double2 *x, double2 *y, int use_act);
-void launch_qeq_cg_init(const Dev &d, cudaStream_t st, double tol, int imax, bool refine);
+void launch_qeq_cg_init(const Dev &d, cudaStream_t st, double tol, int imax);
+void launch_qeq_refine_check(const Dev &d, cudaStream_t st, double tol);
+void launch_qeq_cg_init_rest(const Dev &d, cudaStream_t st, double tol, int imax);
 void launch_qeq_cg_A(const Dev &d, cudaStream_t st);
 void launch_qeq_cg_C(const Dev &d, cudaStream_t st);
 void launch_qeq_finish(const Dev &d, cudaStream_t st);

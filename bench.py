@@ -45,9 +45,9 @@ SEED = 7
 # every kernel streams its list once.
 FP64_PER_UNIT = {
     # phase: (kernel, unit, FLOP per unit, DRAM bytes per unit)
-    "pair_list+H": ("k_build_nbrs", "directed pair", 26.2, 11.25),
+    "pair_list+H": ("k_build_nbrs", "directed pair", 17.29, 11.15),
     "nonbonded": ("k_nonbonded", "unordered pair", 75.7, 11.7),
-    "qeq_spmv": ("k_spmv", "list entry", 4.13, 12.75),
+    "qeq_spmv": ("k_spmv", "list entry", 4.12, 12.76),
 }
 
 

@@ -417,10 +417,14 @@ def gpu_arm(args):
         gm.synchronize()
         pm = gm.profile_get()
         gm.profile(False)
+        smx = gm.stats()
         mixed = {"value": n * args.steps * world / tm, "unit": UNIT,
                  "ms_per_step": tm * 1e3 / args.steps, "speedup_vs_fp64": tmax / tm,
                  "phases_ms_per_step": {k: round(v[0] / psteps, 4)
-                                        for k, v in pm.items() if v[1] > 0}}
+                                        for k, v in pm.items() if v[1] > 0},
+                 "autotuned": {"cell_div": smx["cell_div"], "spmv_lanes_per_row": smx["spmv_rows"]},
+                 "fp64_fallback_items": {"angles": smx["fp64_angles"],
+                                         "torsions": smx["fp64_torsions"]}}
 
     # end to end through the C ABI with host (pinned) buffers: per step the
     # state x, v, f goes host->device, the step runs, x, v, q, f come back
@@ -500,6 +504,7 @@ def gpu_arm(args):
         "phases_ms_per_step": {k: round(v[0] / psteps, 4) for k, v in phases.items()},
         "counts": {"pairs": st["n_pairs"], "bonds": st["n_bonds"], "hbond_pairs": st["n_hbond_pairs"],
                    "cg_iters_s": st["cg_iters_s"], "cg_iters_t": st["cg_iters_t"]},
+        "autotuned": {"cell_div": st["cell_div"], "spmv_lanes_per_row": st["spmv_rows"]},
         "hbm_peak_gbs": peaks.get("hbm_gbs"),
     }
     line["gpu_launches"] = int(launches)

@@ -76,6 +76,15 @@ typedef struct {
                            analytic pair functions (rg_table_check). */
   int tabulate_check;   /* 1: measure the tables' error at rg_create
                            (rg_table_info); 0 (default): skip */
+  int autotune;         /* 1 (default): at the first list build of a handle
+                           (and when its atom count changes by 4x) time the
+                           cell division (cells of cutoff/2 or cutoff/3) and
+                           the QEq SpMV's lanes per row (8, 16, 32) on the
+                           system and keep the fastest; 0: cutoff/2 and 16 */
+  int cell_div;         /* 0 (default): as above; 2 or 3: cells of cutoff/2
+                           or cutoff/3 (3 only where every cell width is at
+                           least the cutoff), not tuned */
+  int spmv_rows;        /* 0 (default): as above; 8, 16 or 32: fixed */
 } rg_params;
 
 /* Energy vector of rg_compute: entries 0..13 are the pair's pvector in the
@@ -98,6 +107,8 @@ typedef struct {
   int fp64_angles, fp64_torsions; /* mixed form: valence angles and torsions
                                   of the last force step evaluated by the
                                   FP64 passes (near-linear, over-coordinated) */
+  int cell_div, spmv_rows;     /* the configuration in use (autotuned): cells
+                                  of cutoff/cell_div, SpMV lanes per row */
 } rg_stats;
 
 void rg_default_params(rg_params *p);

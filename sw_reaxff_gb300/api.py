@@ -43,7 +43,8 @@ class Params(C.Structure):
                 ("qeq_swa", C.c_double), ("qeq_swb", C.c_double),
                 ("qeq_tol", C.c_double), ("qeq_imax", C.c_int),
                 ("precision", C.c_int), ("device", C.c_int), ("tabulate", C.c_int),
-                ("tabulate_check", C.c_int)]
+                ("tabulate_check", C.c_int), ("autotune", C.c_int), ("cell_div", C.c_int),
+                ("spmv_rows", C.c_int)]
 
 
 class Stats(C.Structure):
@@ -54,7 +55,7 @@ class Stats(C.Structure):
                 ("max_bonds", C.c_int), ("max_hbonds", C.c_int),
                 ("regrows", C.c_int), ("kernel_launches", C.c_longlong),
                 ("qeq_restarts", C.c_int), ("fp64_angles", C.c_int),
-                ("fp64_torsions", C.c_int)]
+                ("fp64_torsions", C.c_int), ("cell_div", C.c_int), ("spmv_rows", C.c_int)]
 
 
 class ReaxError(RuntimeError):

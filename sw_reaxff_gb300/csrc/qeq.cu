@@ -62,21 +62,21 @@ __global__ void k_qeq_setup(Dev d) {
 // together (the first exchange swaps halves, so every later level is one
 // add per lane for both systems), and lanes 0 and 1 of the row group write
 // y_s and y_t.
-constexpr int SPMV_RW = 16;
-
+template <int RW>
 __device__ __forceinline__ double pair_sum(double a, double b, int gl) {
   const bool odd = gl & 1;
   double v = odd ? b : a;
   v += __shfl_xor_sync(0xffffffffu, odd ? a : b, 1);
-  for (int off = 2; off < SPMV_RW; off <<= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+  for (int off = 2; off < RW; off <<= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
   return v;   // group lane 0: sum of a; group lane 1: sum of b
 }
 
+template <int RW>
 __global__ void __launch_bounds__(256) k_spmv(Dev d, const double2 *__restrict__ x, double2 *__restrict__ y,
                                               int use_act) {
   const long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  const int gl = (int)(tid & (SPMV_RW - 1));
-  const int i = (int)(tid / SPMV_RW);
+  const int gl = (int)(tid & (RW - 1));
+  const int i = (int)(tid / RW);
   const bool valid = i < d.n;     // no early return: the row group shuffles
   const long long row = (long long)i * d.nb_cap;
   const int nn = valid ? d.n_near[i] : 0, nf = valid ? d.n_far[i] : 0, cap = d.nb_cap;
@@ -90,7 +90,7 @@ __global__ void __launch_bounds__(256) k_spmv(Dev d, const double2 *__restrict__
   }
   double as = 0.0, at = 0.0;
   if (on_s && on_t) {
-    for (int p = gl; p < tot; p += SPMV_RW) {
+    for (int p = gl; p < tot; p += RW) {
       const int slot = p < nn ? p : cap - 1 - (p - nn);
       const uint32_t e = d.nbr[row + slot];
       const double h = d.hval[row + slot];
@@ -99,7 +99,7 @@ __global__ void __launch_bounds__(256) k_spmv(Dev d, const double2 *__restrict__
       at = fma(h, xj.y, at);
     }
   } else if (on_s || on_t) {
-    for (int p = gl; p < tot; p += SPMV_RW) {
+    for (int p = gl; p < tot; p += RW) {
       const int slot = p < nn ? p : cap - 1 - (p - nn);
       const uint32_t e = d.nbr[row + slot];
       const double h = d.hval[row + slot];
@@ -111,7 +111,7 @@ __global__ void __launch_bounds__(256) k_spmv(Dev d, const double2 *__restrict__
       as = 0.0;
     }
   }
-  const double v = pair_sum(as, at, gl);
+  const double v = pair_sum<RW>(as, at, gl);
   if (valid && gl < 2) {
     const double eta = d.ff->sbp[d.ts[i]].eta;
     const double *xi = reinterpret_cast<const double *>(x) + 2 * (long long)i;
@@ -162,6 +162,7 @@ __device__ __forceinline__ float4 split4(double2 v) {
 // level is one compensated add per lane), and lanes 0 and 1 of the row
 // group finish y_s and y_t: the FP64 tail (conversion, eta x) is one warp
 // instruction sequence for four values, not eight per row.
+template <int RW>
 __device__ __forceinline__ void df_pair_sum(float &vh, float &vl, float ah, float al, float bh,
                                             float bl, int gl) {
   const bool odd = gl & 1;
@@ -170,17 +171,18 @@ __device__ __forceinline__ void df_pair_sum(float &vh, float &vl, float ah, floa
   const float oh = __shfl_xor_sync(FULL, odd ? ah : bh, 1);
   const float ol = __shfl_xor_sync(FULL, odd ? al : bl, 1);
   df_add(vh, vl, oh, ol);
-  for (int off = 2; off < SPMV_RW; off <<= 1) {
+  for (int off = 2; off < RW; off <<= 1) {
     const float ph = __shfl_xor_sync(FULL, vh, off), pl = __shfl_xor_sync(FULL, vl, off);
     df_add(vh, vl, ph, pl);
   }
 }
 
+template <int RW>
 __global__ void __launch_bounds__(256) k_spmv32(Dev d, const double2 *__restrict__ x, double2 *__restrict__ y,
                                                 int use_act) {
   const long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  const int gl = (int)(tid & (SPMV_RW - 1));
-  const int i = (int)(tid / SPMV_RW);
+  const int gl = (int)(tid & (RW - 1));
+  const int i = (int)(tid / RW);
   const bool valid = i < d.n;     // no early return: the row group shuffles
   const long long row = (long long)i * d.nb_cap;
   const int nn = valid ? d.n_near[i] : 0, nf = valid ? d.n_far[i] : 0, cap = d.nb_cap;
@@ -199,8 +201,8 @@ __global__ void __launch_bounds__(256) k_spmv32(Dev d, const double2 *__restrict
     // independent gathers of x in flight
     float sh1 = 0.f, sl1 = 0.f, th1 = 0.f, tl1 = 0.f;
     int p = gl;
-    for (; p + SPMV_RW < tot; p += 2 * SPMV_RW) {
-      const int q = p + SPMV_RW;
+    for (; p + RW < tot; p += 2 * RW) {
+      const int q = p + RW;
       const int s0 = p < nn ? p : cap - 1 - (p - nn);
       const int s1 = q < nn ? q : cap - 1 - (q - nn);
       const uint32_t e0 = d.nbr[row + s0], e1 = d.nbr[row + s1];
@@ -222,14 +224,14 @@ __global__ void __launch_bounds__(256) k_spmv32(Dev d, const double2 *__restrict
     df_add(sh, sl, sh1, sl1);
     df_add(th, tl, th1, tl1);
   } else if (on_s) {
-    for (int p = gl; p < tot; p += SPMV_RW) {
+    for (int p = gl; p < tot; p += RW) {
       const int slot = p < nn ? p : cap - 1 - (p - nn);
       const float h = d.hval32[row + slot];
       const float4 xj = x32[d.nbr[row + slot] >> 8];
       df_fma(h, xj.x, xj.y, sh, sl);
     }
   } else if (on_t) {
-    for (int p = gl; p < tot; p += SPMV_RW) {
+    for (int p = gl; p < tot; p += RW) {
       const int slot = p < nn ? p : cap - 1 - (p - nn);
       const float h = d.hval32[row + slot];
       const float4 xj = x32[d.nbr[row + slot] >> 8];
@@ -237,7 +239,7 @@ __global__ void __launch_bounds__(256) k_spmv32(Dev d, const double2 *__restrict
     }
   }
   float vh, vl;
-  df_pair_sum(vh, vl, sh, sl, th, tl, gl);
+  df_pair_sum<RW>(vh, vl, sh, sl, th, tl, gl);
   if (valid && gl < 2) {
     const double eta = d.ff->sbp[d.ts[i]].eta;
     const double *xi = reinterpret_cast<const double *>(x) + 2 * (long long)i;
@@ -248,16 +250,17 @@ __global__ void __launch_bounds__(256) k_spmv32(Dev d, const double2 *__restrict
 // mixed form, residual of the refinement: the stored FP32 H with FP64
 // products and sums, so r = b - H x carries no FP32 rounding of x or of
 // the sums (the FP32 SpMV's rounding is what the inner CG iterations see)
+template <int RW>
 __global__ void __launch_bounds__(256) k_spmv_ref(Dev d, const double2 *__restrict__ x, double2 *__restrict__ y) {
   const long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  const int gl = (int)(tid & (SPMV_RW - 1));
-  const int i = (int)(tid / SPMV_RW);
+  const int gl = (int)(tid & (RW - 1));
+  const int i = (int)(tid / RW);
   const bool valid = i < d.n;
   const long long row = (long long)i * d.nb_cap;
   const int nn = valid ? d.n_near[i] : 0, nf = valid ? d.n_far[i] : 0, cap = d.nb_cap;
   const int tot = min(nn + nf, cap);
   double as = 0.0, at = 0.0;
-  for (int p = gl; p < tot; p += SPMV_RW) {
+  for (int p = gl; p < tot; p += RW) {
     const int slot = p < nn ? p : cap - 1 - (p - nn);
     const uint32_t e = d.nbr[row + slot];
     const double h = (double)d.hval32[row + slot];
@@ -265,7 +268,7 @@ __global__ void __launch_bounds__(256) k_spmv_ref(Dev d, const double2 *__restri
     as = fma(h, xj.x, as);
     at = fma(h, xj.y, at);
   }
-  const double v = pair_sum(as, at, gl);
+  const double v = pair_sum<RW>(as, at, gl);
   if (valid && gl < 2) {
     const double eta = d.ff->sbp[d.ts[i]].eta;
     const double *xi = reinterpret_cast<const double *>(x) + 2 * (long long)i;
@@ -473,16 +476,27 @@ void launch_qeq_setup(const Dev &d, cudaStream_t st) {
   k_qeq_setup<<<(d.n + B - 1) / B, B, 0, st>>>(d);
 }
 
-// the mixed form's FP32 SpMV reads the split copy of qd; any other vector
-// goes through the FP64-sum kernel
+// the row-group width (lanes per row) chosen by the autotuner, d.spmv_rw
+template <int RW>
+static void spmv_rw(const Dev &d, cudaStream_t st, const double2 *x, double2 *y, int use_act,
+                    int kind) {
+  const unsigned G = (unsigned)(((long long)d.n * RW + 255) / 256);
+  if (kind == 0) k_spmv<RW><<<G, 256, 0, st>>>(d, x, y, use_act);
+  else if (kind == 1) k_spmv32<RW><<<G, 256, 0, st>>>(d, x, y, use_act);
+  else k_spmv_ref<RW><<<G, 256, 0, st>>>(d, x, y);
+}
+
+static void spmv_kind(const Dev &d, cudaStream_t st, const double2 *x, double2 *y, int use_act,
+                      int kind) {
+  if (d.spmv_rw == 8) spmv_rw<8>(d, st, x, y, use_act, kind);
+  else if (d.spmv_rw == 32) spmv_rw<32>(d, st, x, y, use_act, kind);
+  else spmv_rw<16>(d, st, x, y, use_act, kind);
+}
+
+// FP64 form: the FP64 SpMV; mixed form: the compensated SpMV of the split
+// copy of qd, and the FP64-sum kernel for any other vector
 void launch_qeq_spmv(const Dev &d, cudaStream_t st, const double2 *x, double2 *y, int use_act) {
-  const long long threads = (long long)d.n * 32;
-  const unsigned G = (unsigned)((threads + 255) / 256);
-  const unsigned G16 = (unsigned)(((long long)d.n * SPMV_RW + 255) / 256);
-  if (!d.mixed) k_spmv<<<G16, 256, 0, st>>>(d, x, y, use_act);
-  else if (x == d.qd) k_spmv32<<<G16, 256, 0, st>>>(d, x, y, use_act);
-  else k_spmv_ref<<<G16, 256, 0, st>>>(d, x, y);
-  (void)G;
+  spmv_kind(d, st, x, y, use_act, !d.mixed ? 0 : (x == d.qd ? 1 : 2));
 }
 
 // the split FP32 pair copy of x that k_spmv32 reads
@@ -499,8 +513,7 @@ void launch_qeq_cg_init(const Dev &d, cudaStream_t st, double tol, int imax) {
   const int B = 256, G = (d.n + B - 1) / B;
   if (d.mixed) {
     k_split_x<<<G, B, 0, st>>>(d, d.qx);
-    const unsigned G16 = (unsigned)(((long long)d.n * SPMV_RW + 255) / 256);
-    k_spmv32<<<G16, 256, 0, st>>>(d, d.qx, d.qq, 0);
+    spmv_kind(d, st, d.qx, d.qq, 0, 1);
   } else {
     launch_qeq_spmv(d, st, d.qx, d.qq, 0);
   }
@@ -536,8 +549,7 @@ __global__ void k_refine_ctrl(Dev d, double tol) {
 void launch_qeq_refine_check(const Dev &d, cudaStream_t st, double tol) {
   const int B = 256, G = (d.n + B - 1) / B;
   const int GS = (d.nseg + 127) / 128;
-  const long long threads = (long long)d.n * SPMV_RW;
-  k_spmv_ref<<<(unsigned)((threads + 255) / 256), 256, 0, st>>>(d, d.qx, d.qq);
+  spmv_kind(d, st, d.qx, d.qq, 0, 2);
   k_cg_init1<<<G, B, 0, st>>>(d);
   k_seg_zero<<<GS, 128, 0, st>>>(d, R_INIT, 4);
   k_refine_sums<<<G, B, 0, st>>>(d);

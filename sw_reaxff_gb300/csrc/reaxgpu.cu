@@ -104,6 +104,11 @@ struct rg_system {
   int ncell_alloc = 0;
   bool lists_valid = false;
   bool forces_valid = false;
+  // autotuned configuration: cells of cutoff/cell_div (2 or 3) and the SpMV
+  // lanes per row (d.spmv_rw); tuned_n = atom count it was tuned for
+  int cell_div = 2;
+  int tuned_n = 0;
+  bool tuning = false;
   // RG_CHECK_FINITE=1: test the force/CdDelta accumulators after every
   // force phase and name the first phase that produced a non-finite value
   bool check_finite = false;
@@ -169,28 +174,45 @@ double list_cutoff(const rg_system *h) {
   return std::max(h->ctl.nonb_cut, h->p.qeq_swb);
 }
 
+// widths of a segment's cell between opposite faces: the box edges, or for
+// a triclinic cell V / |b x c|, V / |c x a|, V / |a x b|
+void cell_widths(const SegGeom &g, double *w) {
+  const double lx = g.L[0], ly = g.L[1], lz = g.L[2];
+  const double xy = g.tilt[0], xz = g.tilt[1], yz = g.tilt[2];
+  w[0] = lx; w[1] = ly; w[2] = lz;
+  if (xy != 0.0 || xz != 0.0 || yz != 0.0) {
+    const double V = lx * ly * lz;
+    w[0] = V / std::sqrt(ly * lz * ly * lz + xy * lz * xy * lz +
+                         (xy * yz - ly * xz) * (xy * yz - ly * xz));
+    w[1] = ly * lz / std::sqrt(lz * lz + yz * yz);
+  }
+}
+
+// cells of cutoff/3 (stencil +-3) only where every width is at least the
+// cutoff: then a partner is at most one image away and the 5x5x5 image
+// codes hold
+bool div3_ok(const rg_system *h) {
+  const double rc = list_cutoff(h);
+  for (const SegGeom &g : h->segs) {
+    double w[3];
+    cell_widths(g, w);
+    if (w[0] < rc || w[1] < rc || w[2] < rc) return false;
+  }
+  return true;
+}
+
 int setup_cells(rg_system *h) {
   const double rc = list_cutoff(h);
-  const int S = 2;
+  const int S = (h->cell_div == 3 && div3_ok(h)) ? 3 : 2;
   Dev &d = h->d;
   long long ncell = 0;
   for (SegGeom &g : h->segs) {
     g.S = S;
     g.tri = (g.tilt[0] != 0.0 || g.tilt[1] != 0.0 || g.tilt[2] != 0.0);
-    // widths of the cell between opposite faces: the box edges, or for a
-    // triclinic cell V / |b x c|, V / |c x a|, V / |a x b|.  Cells (in
-    // fractional coordinates when triclinic) at least rc/S wide across
-    // make the +-S stencil reach every partner within rc.
-    const double lx = g.L[0], ly = g.L[1], lz = g.L[2];
-    const double xy = g.tilt[0], xz = g.tilt[1], yz = g.tilt[2];
-    double w[3] = {lx, ly, lz};
-    if (g.tri) {
-      const double V = lx * ly * lz;
-      w[0] = V / std::sqrt(ly * lz * ly * lz + xy * lz * xy * lz +
-                           (xy * yz - ly * xz) * (xy * yz - ly * xz));
-      w[1] = ly * lz / std::sqrt(lz * lz + yz * yz);
-      w[2] = lz;
-    }
+    // cells (in fractional coordinates when triclinic) at least rc/S wide
+    // across make the +-S stencil reach every partner within rc
+    double w[3];
+    cell_widths(g, w);
     long long nseg_cells = 1;
     for (int k = 0; k < 3; ++k) {
       g.Lh[k] = (float)g.L[k];
@@ -399,9 +421,72 @@ int read_status(rg_system *h, int *st) {
   return 0;
 }
 
+int build_lists(rg_system *h);
+
+// The autotuner: on the system at hand, the pair-list build (bin sort +
+// pair list, the FP32 candidate walk depends on the cell size) with cells
+// of cutoff/2 and cutoff/3, and the QEq SpMV with 8, 16 and 32 lanes per
+// row, each timed with CUDA events; the fastest stays.  Results are the
+// same up to the order of floating-point sums.
+int autotune(rg_system *h) {
+  Dev &d = h->d;
+  h->tuning = true;
+  cudaEvent_t e0, e1;
+  CK(cudaEventCreate(&e0));
+  CK(cudaEventCreate(&e1));
+  auto timed = [&](auto &&work, int reps, float &ms) -> int {
+    CK(cudaEventRecord(e0, h->st));
+    for (int r = 0; r < reps; ++r) work();
+    CK(cudaEventRecord(e1, h->st));
+    CK(cudaEventSynchronize(e1));
+    CK(cudaEventElapsedTime(&ms, e0, e1));
+    ms /= reps;
+    return 0;
+  };
+  int rc = 0;
+  float best = 1e30f;
+  int best_div = h->p.cell_div ? h->p.cell_div : 2;
+  for (int div : {2, 3}) {
+    if (h->p.cell_div) break;                 // fixed by the caller
+    if (div == 3 && !div3_ok(h)) continue;
+    h->cell_div = div;
+    if ((rc = build_lists(h))) break;   // capacities for this cell size
+    float ms = 0.f;
+    if ((rc = timed([&] { launch_bin_sort(d, h->st); launch_build_nbrs(d, h->st); }, 2, ms))) break;
+    if (ms < best) best = ms, best_div = div;
+  }
+  h->cell_div = best_div;
+  if (!rc) rc = build_lists(h);
+  if (!rc && !h->p.spmv_rows) {
+    // SpMV lanes per row on the list just built (a zero vector: timing only)
+    CK(cudaMemsetAsync(d.qd, 0, sizeof(double2) * (size_t)d.n, h->st));
+    if (d.qd32) CK(cudaMemsetAsync(d.qd32, 0, sizeof(float4) * (size_t)d.n, h->st));
+    best = 1e30f;
+    int best_rw = 16;
+    for (int rw : {8, 16, 32}) {
+      d.spmv_rw = rw;
+      float ms = 0.f;
+      if ((rc = timed([&] { launch_qeq_spmv(d, h->st, d.qd, d.qq, 0); }, 3, ms))) break;
+      if (ms < best) best = ms, best_rw = rw;
+    }
+    d.spmv_rw = best_rw;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  h->tuned_n = d.n;
+  h->tuning = false;
+  return rc;
+}
+
 int build_lists(rg_system *h) {
   Dev &d = h->d;
   if (!d.n) return fail(h, RG_E_STATE, "no atoms set");
+  if (h->p.autotune && !h->tuning &&
+      (h->tuned_n == 0 || d.n > 4 * h->tuned_n || 4 * d.n < h->tuned_n)) {
+    int r = autotune(h);
+    if (r) return r;
+    return 0;   // autotune left the lists of the chosen configuration
+  }
   int rc = setup_cells(h);
   if (rc) return rc;
   CK(cudaMemsetAsync(d.status, 0, 8 * sizeof(int), h->st));
@@ -744,6 +829,9 @@ void rg_default_params(rg_params *p) {
   p->device = 0;
   p->tabulate = 65536;
   p->tabulate_check = 0;
+  p->autotune = 1;
+  p->cell_div = 0;
+  p->spmv_rows = 0;
 }
 
 int rg_create(const char *ffield_path, const rg_params *pin, rg_system **out) {
@@ -765,6 +853,17 @@ int rg_create(const char *ffield_path, const rg_params *pin, rg_system **out) {
     return RG_E_ARG;
   }
   h->d.mixed = (h->p.precision == RG_PREC_MIXED);
+  h->d.spmv_rw = 16;
+  if (h->p.cell_div != 0 && h->p.cell_div != 2 && h->p.cell_div != 3) {
+    delete h;
+    return RG_E_ARG;
+  }
+  if (h->p.spmv_rows != 0 && h->p.spmv_rows != 8 && h->p.spmv_rows != 16 && h->p.spmv_rows != 32) {
+    delete h;
+    return RG_E_ARG;
+  }
+  if (h->p.cell_div) h->cell_div = h->p.cell_div;
+  if (h->p.spmv_rows) h->d.spmv_rw = h->p.spmv_rows;
   {
     const char *cf = std::getenv("RG_CHECK_FINITE");
     h->check_finite = cf && (cf[0] == '1' || cf[0] == '2');
@@ -1255,6 +1354,8 @@ int rg_get_stats(const rg_system *h, rg_stats *s) {
   s->n_atoms = h->n;
   s->kernel_launches = h->launches;
   s->fp64_angles = s->fp64_torsions = 0;
+  s->cell_div = h->cell_div;
+  s->spmv_rows = h->d.spmv_rw;
   if (h->d.mixed && h->d.fb_cnt) {
     int fb[2] = {0, 0};
     if (cudaMemcpyAsync(fb, h->d.fb_cnt, sizeof fb, cudaMemcpyDeviceToHost, h->st) == cudaSuccess &&

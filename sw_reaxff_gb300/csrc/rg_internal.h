@@ -159,6 +159,7 @@ struct Dev {
   // system is one segment
   int nseg;
   const SegGeom *seg;    // [nseg]
+  int spmv_rw;           // lanes per row in the QEq SpMVs (8, 16, 32; autotuned)
   int *seg_o;            // segment of each atom (original order)
   int *seg_s;            // segment of each atom (sorted order)
   int ncell;             // cells over all segments

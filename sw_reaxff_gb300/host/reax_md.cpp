@@ -498,12 +498,23 @@ struct Thermo {
   reaxgb::FixQEqReaxGB300 *qeq;
 };
 
+// thermo columns of LAMMPS's default style in real units: temperature
+// from 3N - 3 degrees of freedom (compute temp), pressure in atm from the
+// kinetic energy and the pair virial (compute pressure: (2 KE + W_xx +
+// W_yy + W_zz) / 3V times nktv2p)
 void print_thermo(const reaxgb::Verlet &V, void *ctx) {
   const Thermo &T = *(const Thermo *)ctx;
+  const reaxgb::Atom &A = *V.atom_;
+  const double boltz = 0.0019872067, nktv2p = 68568.415;
   const double pe = T.pair->eng_vdwl + T.pair->eng_coul;
   const double ke = V.kinetic_energy();
-  std::printf("%10lld %20.10f %20.10f %20.10f %8d\n", V.update_->ntimestep, pe, ke, pe + ke,
-              T.qeq ? T.qeq->matvecs : 0);
+  const int dof = 3 * A.nlocal - 3;
+  const double temp = dof > 0 ? 2.0 * ke / (dof * boltz) : 0.0;
+  const double vol = (A.boxhi[0] - A.boxlo[0]) * (A.boxhi[1] - A.boxlo[1]) * (A.boxhi[2] - A.boxlo[2]);
+  const double *w = T.pair->virial;
+  const double press = (2.0 * ke + w[0] + w[1] + w[2]) / (3.0 * vol) * nktv2p;
+  std::printf("%10lld %14.6f %20.10f %20.10f %20.10f %14.4f %8d\n", V.update_->ntimestep, temp, pe,
+              ke, pe + ke, press, T.qeq ? T.qeq->matvecs : 0);
 }
 
 int run_deck(std::istream &in, const std::map<std::string, std::string> &cmdvars) {
@@ -630,7 +641,8 @@ int run_deck(std::istream &in, const std::map<std::string, std::string> &cmdvars
       if (!setup_done) {
         verlet->setup();
         pair->sync_host();
-        std::printf("%10s %20s %20s %20s %8s\n", "Step", "PotEng", "KinEng", "TotEng", "Matvecs");
+        std::printf("%10s %14s %20s %20s %20s %14s %8s\n", "Step", "Temp", "PotEng", "KinEng",
+                    "TotEng", "Press", "Matvecs");
         print_thermo(*verlet, &T);
         setup_done = true;
       }

@@ -703,7 +703,7 @@ void Verlet::setup() {
   if (qeq_) qeq_->init();
   if (nve_) nve_->init();
   if (qeq_) qeq_->setup_pre_force(0);
-  pair_->compute(1, 0);
+  pair_->compute(1, 1);
   for (auto *f : end_of_step_fixes) f->setup();
 }
 
@@ -715,7 +715,7 @@ void Verlet::run(long long nsteps, int thermo_every, void (*thermo)(const Verlet
                     (update_->ntimestep % thermo_every == 0 || s == nsteps - 1);
     if (nve_) nve_->initial_integrate(0);
     if (qeq_) qeq_->pre_force(0);
-    pair_->compute(th ? 1 : 0, 0);
+    pair_->compute(th ? 1 : 0, th ? 1 : 0);   // energies and virial on thermo steps
     if (nve_) nve_->final_integrate();
     for (auto *f : end_of_step_fixes) f->end_of_step();
     if (th) {

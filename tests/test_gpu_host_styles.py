@@ -249,3 +249,25 @@ def test_deck_species(tmp_path, ffield):
     assert len(frame) == len(comps)
     assert sum(int(w[1]) for w in frame) == s.n
     assert all(0.0 <= float(x) < 1.0 for w in frame for x in w[4:7])
+
+
+def test_deck_thermo_pressure(tmp_path, ffield):
+    """The deck's thermo pressure is LAMMPS's compute pressure in real
+    units: (2 KE + W_xx + W_yy + W_zz) / 3V * nktv2p with the pair virial
+    (rg_get_virial), and its temperature 2 KE / ((3N - 3) k_B)."""
+    s = systems.water_box(300, seed=3)
+    (meta, st), out = run_deck(tmp_path, s, 0)
+    head = [l.split() for l in out.splitlines() if l.split()[:2] == ["Step", "Temp"]]
+    row = [l.split() for l in out.splitlines() if l.split() and l.split()[0] == "0"][0]
+    cols = dict(zip(head[0], row))
+    ke, temp, press = float(cols["KinEng"]), float(cols["Temp"]), float(cols["Press"])
+    assert abs(temp - 2 * ke / ((3 * s.n - 3) * 0.0019872067)) < 1e-6 * temp
+    g = ReaxGPU(ffield)
+    g.set_system(s)
+    g.qeq()
+    g.compute(vflag=1)
+    w = g.virial()[0]
+    vol = float(np.prod(s.box))
+    want = (2 * ke + w[0] + w[1] + w[2]) / (3 * vol) * 68568.415
+    # charges of the deck's and this handle's QEq agree to ~1e-6 e
+    assert abs(press - want) < 1e-4 * (abs(want) + 2 * ke / (3 * vol) * 68568.415)

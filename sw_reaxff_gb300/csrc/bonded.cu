@@ -71,14 +71,14 @@ __device__ __forceinline__ bool tag_first(const Dev &d, int i, int j, uint32_t e
 
 // Calculate_Theta / Calculate_dCos_Theta, reaxc_valence_angles_sunway.cpp:49-79
 // (R = double: the FP64 form; R = float: the mixed form)
-template <typename R>
+template <typename R, bool THETA = true>
 __device__ __forceinline__ void theta_dcos(const R *dji, R d_ji, const R *djk, R d_jk, R &theta,
                                            R &cos_theta, R *di, R *dj, R *dk) {
   const R dot = dji[0] * djk[0] + dji[1] * djk[1] + dji[2] * djk[2];
   cos_theta = dot / (d_ji * d_jk);
   if (cos_theta > R(1)) cos_theta = R(1);
   if (cos_theta < R(-1)) cos_theta = R(-1);
-  theta = acos(cos_theta);
+  if (THETA) theta = acos(cos_theta);
   const R sqr_d_ji = d_ji * d_ji, sqr_d_jk = d_jk * d_jk;
   const R inv_dists = R(1) / (d_ji * d_jk);
   const R inv_dists3 = inv_dists * inv_dists * inv_dists;
@@ -99,8 +99,13 @@ __global__ void k_bo_deltap(Dev d) {
   if (i >= d.n) return;
   const Sbp &s = d.ff->sbp[d.ts[i]];
   const double b = d.bo0[i];
-  d.Deltap[i] = b - s.valency;
+  const double Dp = b - s.valency;
+  d.Deltap[i] = Dp;
   d.Deltap_boc[i] = b - s.valency_val;
+  // the per-atom exponentials of the f1 correction, once per atom instead
+  // of once per bond end
+  d.exp_boc[i] = exp(-d.ff->gp[0] * Dp);
+  d.exp_boc[d.n + i] = exp(-d.ff->gp[1] * Dp);
 }
 
 __global__ void k_bo_correct(Dev d) {
@@ -122,12 +127,11 @@ __global__ void k_bo_correct(Dev d) {
   } else {
     const double p_boc1 = F.gp[0], p_boc2 = F.gp[1];
     const double val_i = F.sbp[ti].valency, val_j = F.sbp[tj].valency;
-    const double Deltap_i = d.Deltap[i], Deltap_j = d.Deltap[j];
     const double Dboc_i = d.Deltap_boc[i], Dboc_j = d.Deltap_boc[j];
     double f1, Cf1_ij, Cf1_ji, f4, f5, f4f5, Cf45_ij, Cf45_ji;
     if (tw.ovc >= 0.001) {
-      const double exp_p1i = exp(-p_boc1 * Deltap_i), exp_p2i = exp(-p_boc2 * Deltap_i);
-      const double exp_p1j = exp(-p_boc1 * Deltap_j), exp_p2j = exp(-p_boc2 * Deltap_j);
+      const double exp_p1i = d.exp_boc[i], exp_p2i = d.exp_boc[n + i];
+      const double exp_p1j = d.exp_boc[j], exp_p2j = d.exp_boc[n + j];
       const double f2 = exp_p1i + exp_p1j;
       const double f3 = -1.0 / p_boc2 * log(0.5 * (exp_p2i + exp_p2j));
       f1 = 0.5 * ((val_i + f2) / (val_i + f2 + f3) + (val_j + f2) / (val_j + f2 + f3));
@@ -363,9 +367,7 @@ __device__ __forceinline__ double warp_sum_d(double v) {
   return v;
 }
 
-// R = double: FP64 form; R = float (mixed form): the angle, the exponentials
-// and the force factors in FP32 from the FP64 displacement and bond order;
-// accumulation in FP64
+// FP64 form (R = double; the mixed form runs k_hbonds32 below)
 template <typename R, bool VIR>
 __global__ void __launch_bounds__(256) k_hbonds(Dev d, int eflag) {
   const int lane = threadIdx.x & 31;
@@ -410,9 +412,10 @@ __global__ void __launch_bounds__(256) k_hbonds(Dev d, int eflag) {
         const R djk[3] = {(R)dk64[0], (R)dk64[1], (R)dk64[2]};
         const R r_jk = (R)r64;
         R theta, cos_theta, di[3], djv[3], dk[3];
-        theta_dcos<R>(dij, r_ij, djk, r_jk, theta, cos_theta, di, djv, dk);
-        const R sin_theta2 = sin(theta / R(2));
-        R sin_xhz4 = sqr(sin_theta2);
+        theta_dcos<R, false>(dij, r_ij, djk, r_jk, theta, cos_theta, di, djv, dk);
+        // sin^4(theta/2) = ((1 - cos theta) / 2)^2: the reference's
+        // sin(acos(c) / 2) without the two transcendentals
+        R sin_xhz4 = (R(1) - cos_theta) / R(2);
         sin_xhz4 *= sin_xhz4;
         const R cos_xhz1 = R(1) - cos_theta;
         const R p_hb1 = (R)hbp.p_hb1, p_hb2 = (R)hbp.p_hb2, p_hb3 = (R)hbp.p_hb3;
@@ -504,9 +507,8 @@ __global__ void __launch_bounds__(256) k_hbonds32(Dev d, int eflag) {
         disp32(g, d.xf[k], d.xl[k], hjf, ljf, sx, sy, sz, djk[0], djk[1], djk[2]);
         const float r_jk = sqrtf(djk[0] * djk[0] + djk[1] * djk[1] + djk[2] * djk[2]);
         float theta, cos_theta, di[3], djv[3], dk[3];
-        theta_dcos<float>(dij, r_ij, djk, r_jk, theta, cos_theta, di, djv, dk);
-        const float sin_theta2 = sinf(theta / 2.f);
-        float sin_xhz4 = sin_theta2 * sin_theta2;
+        theta_dcos<float, false>(dij, r_ij, djk, r_jk, theta, cos_theta, di, djv, dk);
+        float sin_xhz4 = (1.f - cos_theta) * 0.5f;   // sin^2(theta/2)
         sin_xhz4 *= sin_xhz4;
         const float cos_xhz1 = 1.f - cos_theta;
         const float exp_hb2 = expf(-hp.p_hb2 * BO);
@@ -959,10 +961,9 @@ __global__ void __launch_bounds__(128) k_valence(Dev d, int eflag, long long nit
 // the FP64 pass over the queued near-linear angles (grid-stride over the
 // device-side count; few items, so energies go straight to their segment)
 template <bool VIR>
-__global__ void __launch_bounds__(128) k_valence_fb(Dev d, int eflag) {
+__device__ void valence_fb(const Dev &d, int eflag, long long first, long long stride) {
   const long long cnt = d.fb_cnt[0];
-  for (long long w = (long long)blockIdx.x * blockDim.x + threadIdx.x; w < cnt;
-       w += (long long)gridDim.x * blockDim.x) {
+  for (long long w = first; w < cnt; w += stride) {
     double e_ang = 0, e_pen = 0, e_coa = 0;
     double vw[6] = {0, 0, 0, 0, 0, 0};
     const unsigned long long it = d.w_fb_val[w];
@@ -1161,10 +1162,9 @@ __global__ void __launch_bounds__(128) k_torsion(Dev d, int eflag, long long nit
 }
 
 template <bool VIR>
-__global__ void __launch_bounds__(128) k_torsion_fb(Dev d, int eflag) {
+__device__ void torsion_fb(const Dev &d, int eflag, long long first, long long stride) {
   const long long cnt = d.fb_cnt[1];
-  for (long long w = (long long)blockIdx.x * blockDim.x + threadIdx.x; w < cnt;
-       w += (long long)gridDim.x * blockDim.x) {
+  for (long long w = first; w < cnt; w += stride) {
     double e_tor = 0, e_con = 0;
     double vw[6] = {0, 0, 0, 0, 0, 0};
     const unsigned long long it = d.w_fb_tor[w];
@@ -1179,6 +1179,18 @@ __global__ void __launch_bounds__(128) k_torsion_fb(Dev d, int eflag) {
     if (VIR)
       for (int c = 0; c < 6; ++c) atomicAdd(&d.virial[(long long)sg * 6 + c], vw[c]);
   }
+}
+
+// the FP64 passes over the queued angles (first half of the blocks) and
+// torsions (second half) in one launch, so their latencies overlap
+template <bool VIR>
+__global__ void __launch_bounds__(128) k_vt_fb(Dev d, int eflag) {
+  const int half = gridDim.x / 2;
+  const bool val = (int)blockIdx.x < half;
+  const long long first = (long long)(val ? blockIdx.x : blockIdx.x - half) * blockDim.x + threadIdx.x;
+  const long long stride = (long long)half * blockDim.x;
+  if (val) valence_fb<VIR>(d, eflag, first, stride);
+  else torsion_fb<VIR>(d, eflag, first, stride);
 }
 
 // ------------------------------------------------------------------
@@ -1323,8 +1335,7 @@ static void vt_kernels(const Dev &d, cudaStream_t st, int eflag, long long nval,
     if (ntor > 0) k_torsion<float, VIR><<<gt, 128, 0, st>>>(d, eflag, ntor);
     // FP64 passes over the near-linear items (count read on the device;
     // usually none or a few, so a small grid that strides)
-    k_valence_fb<VIR><<<16, 128, 0, st>>>(d, eflag);
-    k_torsion_fb<VIR><<<16, 128, 0, st>>>(d, eflag);
+    k_vt_fb<VIR><<<32, 128, 0, st>>>(d, eflag);
   } else {
     if (nval > 0) k_valence<double, VIR><<<gv, 128, 0, st>>>(d, eflag, nval);
     if (ntor > 0) k_torsion<double, VIR><<<gt, 128, 0, st>>>(d, eflag, ntor);

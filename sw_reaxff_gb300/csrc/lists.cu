@@ -228,8 +228,8 @@ template <bool MIXED>
 __device__ __forceinline__ void nbr_flush(const Dev &d, const Control &C, const ForceField &F,
                                           const NbrQueue &Q, int cnt, int lane, int i,
                                           const double4 &xi, const float4 &xif, const float4 &xil,
-                                          int ti, long long row, int cap, const double *L,
-                                          const SegGeom &g, int &cntN, int &cntF) {
+                                          int ti, long long row, int cap, const SegGeom &g,
+                                          int &cntN, int &cntF) {
   bool in = false, near = false;
   double d2 = 0.0;
   float d2f = 0.f;
@@ -343,7 +343,6 @@ __global__ void __launch_bounds__(NB_WARPS * 32) k_build_nbrs(Dev d) {
   const int ti = d.ts[i];
   const float cut2f = C.list_pre2_f;
   const SegGeom &g = d.seg[d.seg_s[i]];
-  const double L[3] = {g.L[0], g.L[1], g.L[2]};
   const int ncx = g.nc[0], ncy = g.nc[1], ncz = g.nc[2], S = g.S;
   // the cell the binning put atom i in (integer decomposition, no FP64)
   const int cl = d.cell_o[d.perm[i]] - g.cell0;
@@ -397,7 +396,7 @@ __global__ void __launch_bounds__(NB_WARPS * 32) k_build_nbrs(Dev d) {
           qn += __popc(mc);
           __syncwarp();
           if (qn >= 32) {
-            nbr_flush<MIXED>(d, C, F, Q, 32, lane, i, xi, xif, xil, ti, row, cap, L, g, cntN, cntF);
+            nbr_flush<MIXED>(d, C, F, Q, 32, lane, i, xi, xif, xil, ti, row, cap, g, cntN, cntF);
             __syncwarp();
             // move the leftover (< 32) to the front of the queue
             const int left = qn - 32;
@@ -418,7 +417,7 @@ __global__ void __launch_bounds__(NB_WARPS * 32) k_build_nbrs(Dev d) {
       }
     }
   }
-  if (qn > 0) nbr_flush<MIXED>(d, C, F, Q, qn, lane, i, xi, xif, xil, ti, row, cap, L, g, cntN, cntF);
+  if (qn > 0) nbr_flush<MIXED>(d, C, F, Q, qn, lane, i, xi, xif, xil, ti, row, cap, g, cntN, cntF);
   if (lane == 0) {
     d.n_near[i] = cntN;
     d.n_far[i] = cntF;
@@ -585,7 +584,6 @@ __global__ void __launch_bounds__(NB_WARPS * 32) k_build_bonds(Dev d) {
   const int nn = d.n_near[i] < d.nb_cap ? d.n_near[i] : d.nb_cap;
   const int n = d.n;
   const SegGeom &g = d.seg[d.seg_s[i]];
-  const double L[3] = {g.L[0], g.L[1], g.L[2]};
   const float4 xil = d.xl[i];
   // FP32 prefilter radius: anything that could be within bond_cut, and for
   // H atoms within hbond_cut

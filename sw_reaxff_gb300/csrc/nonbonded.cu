@@ -36,153 +36,109 @@ struct PairQueue {
   uint32_t e[QC];
 };
 
-// real-type helpers of the two forms (FP64: the reference's expressions;
-// mixed: FP32 arithmetic)
-__device__ __forceinline__ double rs_(double x) { return rsqrt(x); }
-__device__ __forceinline__ float rs_(float x) { return rsqrtf(x); }
-
-// Tap(r) and (1/r) dTap/dr
-template <typename R>
-__device__ __forceinline__ void taper(const Control &C, R r, R rinv, R &Tp, R &dTap) {
-  if (std::is_same<R, float>::value && C.tap_factored) {
-    // (1-t)^4 (1 + 4t + 10t^2 + 20t^3), t = r/swb;  (1/r) d/dr = -140 t^2 (1-t)^3 / swb^2
-    const R is = (R)C.inv_swb_nb;
-    const R t = r * is, u = R(1) - t, u2 = u * u;
-    Tp = u2 * u2 * (R(1) + t * (R(4) + t * (R(10) + t * R(20))));
-    dTap = R(-140) * t * t * u2 * u * is * is;
-    return;
-  }
+// Tap(r) and (1/r) dTap/dr (FP64 form)
+__device__ __forceinline__ void taper(const Control &C, double r, double rinv, double &Tp,
+                                      double &dTap) {
   const double *Tap = C.Tap;
-  Tp = fma((R)Tap[7], r, (R)Tap[6]);
-  Tp = fma(Tp, r, (R)Tap[5]);
-  Tp = fma(Tp, r, (R)Tap[4]);
-  Tp = fma(Tp, r, (R)Tap[3]);
-  Tp = fma(Tp, r, (R)Tap[2]);
-  Tp = fma(Tp, r, (R)Tap[1]);
-  Tp = fma(Tp, r, (R)Tap[0]);
-  dTap = fma((R)(7 * Tap[7]), r, (R)(6 * Tap[6]));
-  dTap = fma(dTap, r, (R)(5 * Tap[5]));
-  dTap = fma(dTap, r, (R)(4 * Tap[4]));
-  dTap = fma(dTap, r, (R)(3 * Tap[3]));
-  dTap = fma(dTap, r, (R)(2 * Tap[2]));
-  dTap = fma((R)Tap[1], rinv, dTap);
+  Tp = fma(Tap[7], r, Tap[6]);
+  Tp = fma(Tp, r, Tap[5]);
+  Tp = fma(Tp, r, Tap[4]);
+  Tp = fma(Tp, r, Tap[3]);
+  Tp = fma(Tp, r, Tap[2]);
+  Tp = fma(Tp, r, Tap[1]);
+  Tp = fma(Tp, r, Tap[0]);
+  dTap = fma(7 * Tap[7], r, 6 * Tap[6]);
+  dTap = fma(dTap, r, 5 * Tap[5]);
+  dTap = fma(dTap, r, 4 * Tap[4]);
+  dTap = fma(dTap, r, 3 * Tap[3]);
+  dTap = fma(dTap, r, 2 * Tap[2]);
+  dTap = fma(Tap[1], rinv, dTap);
 }
 
-// vdW + Coulomb of one queued pair; returns (1/r) dE/dr in c and the
-// displacement; energies are added in FP64
-template <typename R>
+// FP64 form: vdW + Coulomb of one queued pair, from the pair-function
+// tables (tabulate > 0) or the reference's expressions; returns (1/r) dE/dr
+// in c and the displacement; energies are added to evdw and eele
 __device__ __forceinline__ void pair_terms(const Dev &d, const ForceField &F, const Control &C,
-                                          uint32_t e, bool act, const double4 &xi,
-                                          const float4 &xif, const float4 &xil, int ti,
-                                          const double *L, const SegGeom &g, double &evdw,
-                                          double &eele, double &c, double &dx, double &dy,
-                                          double &dz, int &j) {
+                                          uint32_t e, bool act, const double4 &xi, int ti,
+                                          const SegGeom &g, double &evdw, double &eele,
+                                          double &c, double &dx, double &dy, double &dz,
+                                          int &j) {
   c = 0.0; dx = dy = dz = 0.0;
   j = (int)(e >> 8);
   if (!act) return;
   int sx, sy, sz;
   img_unpack((int)(e & 255u), &sx, &sy, &sz);
-  R d2;
-  double qj;
-  if (std::is_same<R, float>::value) {
-    // mixed form: FP32 displacement from the (hi, lo) positions; the list
-    // holds exactly the pairs within max(nonb_cut, swb), so only a QEq
-    // taper radius above nonb_cut needs a test here (FP64 near the cutoff)
-    const float4 hj = d.xf[j], lj = d.xl[j];
-    float fx, fy, fz;
-    disp32(g, hj, lj, xif, xil, sx, sy, sz, fx, fy, fz);
-    const float d2f = fx * fx + fy * fy + fz * fz;
-    if (!C.nonb_all_listed) {
-      const float nc2 = (float)C.nonb_cut2;
-      bool out;
-      if (d2f <= nc2 * (1.f - 1e-5f)) out = false;
-      else if (d2f > nc2 * (1.f + 1e-5f)) out = true;
-      else {
-        double ex, ey, ez;
-        disp64(g, d.xs[j], xi, sx, sy, sz, ex, ey, ez);
-        out = __dadd_rn(__dadd_rn(__dmul_rn(ex, ex), __dmul_rn(ey, ey)), __dmul_rn(ez, ez)) > C.nonb_cut2;
-      }
-      if (out) return;
-    }
-    dx = fx; dy = fy; dz = fz;
-    d2 = (R)d2f;
-    qj = lj.w;                 // charge (FP32 copy)
-  } else {
-    // same rounding as the pair-list membership test
-    const double4 xj = d.xs[j];
-    qj = xj.w;
-    disp64(g, xj, xi, sx, sy, sz, dx, dy, dz);
-    const double d2x = __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
-    if (d2x > C.nonb_cut2) { dx = dy = dz = 0.0; return; }
-    d2 = (R)d2x;
-    if (C.tab_n && d2x >= C.tab_s0) {
-      // FP64 tables: energies and (1/r) dE/dr = 2 dE/ds by cubic Hermite
-      double h01, t10, t11;
-      const int k = tab_weights(C, d2x, h01, t10, t11);
-      const double *T = d.tab_nb + ((long long)C.tab_pair[ti][d.ts[j]] * (C.tab_n + 1) + k) * 6;
-      const double ds = C.tab_ds;
-      const double ev = tab_interp(T[0], T[6], ds * T[1], ds * T[7], h01, t10, t11);
-      const double dv = tab_interp(T[1], T[7], T[2], T[8], h01, t10, t11);
-      const double ec = tab_interp(T[3], T[9], ds * T[4], ds * T[10], h01, t10, t11);
-      const double dcl = tab_interp(T[4], T[10], T[5], T[11], h01, t10, t11);
-      const double qq = C_ele * xi.w * qj;
-      evdw += ev;
-      eele += qq * ec;
-      c = 2.0 * (dv + qq * dcl);
-      return;
-    }
+  // same rounding as the pair-list membership test
+  const double4 xj = d.xs[j];
+  const double qj = xj.w;
+  disp64(g, xj, xi, sx, sy, sz, dx, dy, dz);
+  const double d2 = __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
+  if (d2 > C.nonb_cut2) { dx = dy = dz = 0.0; return; }
+  if (C.tab_n && d2 >= C.tab_s0) {
+    // FP64 tables: energies and (1/r) dE/dr = 2 dE/ds by cubic Hermite
+    double h01, t10, t11;
+    const int k = tab_weights(C, d2, h01, t10, t11);
+    const double *T = d.tab_nb + ((long long)C.tab_pair[ti][d.ts[j]] * (C.tab_n + 1) + k) * 6;
+    const double ds = C.tab_ds;
+    const double ev = tab_interp(T[0], T[6], ds * T[1], ds * T[7], h01, t10, t11);
+    const double dv = tab_interp(T[1], T[7], T[2], T[8], h01, t10, t11);
+    const double ec = tab_interp(T[3], T[9], ds * T[4], ds * T[10], h01, t10, t11);
+    const double dcl = tab_interp(T[4], T[10], T[5], T[11], h01, t10, t11);
+    const double qq = C_ele * xi.w * qj;
+    evdw += ev;
+    eele += qq * ec;
+    c = 2.0 * (dv + qq * dcl);
+    return;
   }
-  const R rinv = rs_(d2);
-  const R r = d2 * rinv;
+  const double rinv = rsqrt(d2);
+  const double r = d2 * rinv;
   const Tbp &tw = F.tbp[ti][d.ts[j]];
-  R Tp, dTap;
-  taper<R>(C, r, rinv, Tp, dTap);
-  const R p_vdW1 = (R)F.gp[28];
+  double Tp, dTap;
+  taper(C, r, rinv, Tp, dTap);
+  const double p_vdW1 = F.gp[28];
   const int vdw_type = F.vdw_type;
-  const R alpha = (R)tw.alpha, r_vdW = (R)tw.r_vdW, D = (R)tw.D;
-  const R ar = alpha / r_vdW;
-  R e_vdW, CEvd, e_core = 0, e_lg = 0;
+  const double alpha = tw.alpha, r_vdW = tw.r_vdW, D = tw.D;
+  const double ar = alpha / r_vdW;
+  double e_vdW, CEvd, e_core = 0, e_lg = 0;
   if (vdw_type == 1 || vdw_type == 3) {
     // shielded Morse: fn13 = (r^p + gamma_w^-p)^(1/p)
-    const R powr = exp(p_vdW1 * log(r));                      // r^p
-    const R S = powr + (R)tw.powgi_vdW1;
-    const R fn13 = exp(log(S) / p_vdW1);                      // S^(1/p)
-    const R exp2 = exp(R(0.5) * alpha * (R(1) - fn13 / r_vdW));
-    const R exp1 = exp2 * exp2;
-    e_vdW = D * (exp1 - R(2) * exp2);
-    const R dfn13 = (fn13 / S) * (powr / d2);                 // S^(1/p-1) r^(p-2)
+    const double powr = exp(p_vdW1 * log(r));                 // r^p
+    const double S = powr + tw.powgi_vdW1;
+    const double fn13 = exp(log(S) / p_vdW1);                 // S^(1/p)
+    const double exp2 = exp(0.5 * alpha * (1.0 - fn13 / r_vdW));
+    const double exp1 = exp2 * exp2;
+    e_vdW = D * (exp1 - 2.0 * exp2);
+    const double dfn13 = (fn13 / S) * (powr / d2);            // S^(1/p-1) r^(p-2)
     CEvd = dTap * e_vdW - Tp * D * ar * (exp1 - exp2) * dfn13;
   } else {
-    const R exp2 = exp(R(0.5) * alpha * (R(1) - r / r_vdW));
-    const R exp1 = exp2 * exp2;
-    e_vdW = D * (exp1 - R(2) * exp2);
+    const double exp2 = exp(0.5 * alpha * (1.0 - r / r_vdW));
+    const double exp1 = exp2 * exp2;
+    e_vdW = D * (exp1 - 2.0 * exp2);
     CEvd = dTap * e_vdW - Tp * D * ar * (exp1 - exp2) * rinv;
   }
   if (vdw_type == 2 || vdw_type == 3) {
-    const R acore = (R)tw.acore, rcore = (R)tw.rcore;
-    e_core = (R)tw.ecore * exp(acore * (R(1) - (r / rcore)));
-    const R de_core = -(acore / rcore) * e_core;
+    const double acore = tw.acore, rcore = tw.rcore;
+    e_core = tw.ecore * exp(acore * (1.0 - (r / rcore)));
+    const double de_core = -(acore / rcore) * e_core;
     CEvd += dTap * e_core + Tp * de_core * rinv;
     if (C.lgflag) {
-      const R r5 = d2 * d2 * r, r6 = d2 * d2 * d2;
-      const R lg2 = (R)tw.lgre * (R)tw.lgre;
-      const R re6 = lg2 * lg2 * lg2;
-      e_lg = -((R)tw.lgcij / (r6 + re6));
-      const R de_lg = R(-6) * e_lg * r5 / (r6 + re6);
+      const double r5 = d2 * d2 * r, r6 = d2 * d2 * d2;
+      const double lg2 = tw.lgre * tw.lgre;
+      const double re6 = lg2 * lg2 * lg2;
+      e_lg = -(tw.lgcij / (r6 + re6));
+      const double de_lg = -6.0 * e_lg * r5 / (r6 + re6);
       CEvd += dTap * e_lg + Tp * de_lg * rinv;
     }
   }
   // shielded Coulomb: Tap qi qj / (r^3 + gamma)^c
-  const R dr3gamij_1 = fma(d2, r, (R)tw.gamma);
-  R inv3;
-  if (std::is_same<R, float>::value) inv3 = (R)rcbrtf((float)dr3gamij_1);
-  else inv3 = (R)rpow_third((double)dr3gamij_1, RG_C3_ELE);
-  const R qq = std::is_same<R, float>::value ? (R)C_ele * xil.w * (R)qj : (R)(C_ele * xi.w * qj);
-  const R e_ele = qq * Tp * inv3;
-  const R CEclmb = qq * (dTap - Tp * r / dr3gamij_1) * inv3;
-  evdw += (double)(Tp * (e_vdW + e_core + e_lg));
-  eele += (double)e_ele;
-  c = (double)(CEvd + CEclmb);
+  const double dr3gamij_1 = fma(d2, r, tw.gamma);
+  const double inv3 = rpow_third(dr3gamij_1, RG_C3_ELE);
+  const double qq = C_ele * xi.w * qj;
+  const double e_ele = qq * Tp * inv3;
+  const double CEclmb = qq * (dTap - Tp * r / dr3gamij_1) * inv3;
+  evdw += Tp * (e_vdW + e_core + e_lg);
+  eele += e_ele;
+  c = CEvd + CEclmb;
 }
 
 // Mixed form: vdW + Coulomb of one pair entirely in FP32, parameters from
@@ -292,7 +248,6 @@ __global__ void __launch_bounds__(NBW * 32) k_nonbonded(Dev d, int eflag) {
     const float4 xil = d.mixed ? d.xl[i] : make_float4(0.f, 0.f, 0.f, 0.f);
     const int ti = d.ts[i];
     const SegGeom &g = d.seg[d.seg_s[i]];
-    const double L[3] = {g.L[0], g.L[1], g.L[2]};
     const long long row = (long long)i * d.nb_cap;
     const int nn = d.n_near[i], nf = d.n_far[i];
     const int cap = d.nb_cap;
@@ -342,7 +297,7 @@ __global__ void __launch_bounds__(NBW * 32) k_nonbonded(Dev d, int eflag) {
           }
         } else {
           double c, dx, dy, dz;
-          pair_terms<R>(d, F, C, e, act, xi, xif, xil, ti, L, g, evdw, eele, c, dx, dy, dz, j);
+          pair_terms(d, F, C, e, act, xi, ti, g, evdw, eele, c, dx, dy, dz, j);
           if (act && c != 0.0) {
             fx -= c * dx;
             fy -= c * dy;

@@ -382,6 +382,7 @@ int alloc_atoms(rg_system *h, int n) {
   r |= dalloc(h, B, &d.dDeltap, 3 * (size_t)n);
   r |= dalloc(h, B, &d.fC, 4 * (size_t)n);
   r |= dalloc(h, B, &d.vsum, 2 * (size_t)n);
+  r |= dalloc(h, B, &d.exp_boc, 2 * (size_t)n);
   r |= dalloc(h, B, &d.c_sbo, 5 * (size_t)n);
   double2 **pv[] = {&d.qx, &d.qb, &d.qr, &d.qu, &d.qw, &d.qd, &d.qq, &d.qp, &d.qs, &d.qv, &d.qz, &d.qm};
   for (double2 **q : pv) r |= dalloc(h, B, q, (size_t)n);
@@ -593,7 +594,7 @@ int do_compute(rg_system *h, int eflag, int vflag = 0) {
     }
     h->n_val = tot[0];
     h->n_tor = tot[1];
-    Scope sc(h, PH_VALTOR, 1 + (tot[0] > 0) + (tot[1] > 0) + (d.mixed ? 2 : 0));
+    Scope sc(h, PH_VALTOR, 1 + (tot[0] > 0) + (tot[1] > 0) + (d.mixed ? 1 : 0));
     launch_vt_run(d, h->st, eflag, tot[0], tot[1]);
   }
   if ((rc = finite_after("valence_torsion"))) return rc;
@@ -1139,6 +1140,8 @@ static int set_atoms_impl(rg_system *h, int n, const double *x, const int *type,
   if (kind == cudaMemcpyHostToDevice) {
     for (int i = 0; i < n; ++i)
       if (type[i] < 0 || type[i] >= h->ff.ntypes) return fail(h, RG_E_ARG, "atom type out of range");
+    for (long long k = 0; k < 3LL * n; ++k)
+      if (!std::isfinite(x[k])) return fail(h, RG_E_ARG, "non-finite position");
   }
   {
     long long sum = 0;

@@ -212,6 +212,7 @@ struct Dev {
   // per-atom bond-order workspace (sorted order)
   double *bo0;        // total (uncorrected, then corrected) bond order
   double *Deltap, *Deltap_boc, *Delta, *Delta_e, *Delta_boc, *Delta_val;
+  double *exp_boc;    // 2 * n: exp(-p_boc1 Deltap), exp(-p_boc2 Deltap) per atom
   double *vlpex, *nlp, *Delta_lp, *Delta_lp_temp, *dDelta_lp, *nlp_temp;
   double *dDeltap;    // 3 * n (xyz blocks)
   double *fC;         // 4 * n: force xyz blocks + CdDelta block

@@ -311,6 +311,11 @@ def serve_section(args, local):
     return out
 
 
+def workload_name(n):
+    return (f"H2O/CH4/C2H6/NH3 0.5/0.2/0.2/0.1 mixture, {n} atoms, "
+            "0.8 g/cm3, 300 K, NVE dt 0.25 fs, QEq tol 1e-6, FP64")
+
+
 def reference_arm(args):
     """--impl reference: the reference's CPU algorithm (the oracle port; the
     reference itself needs LAMMPS and the Sunway toolchain) on all host
@@ -332,7 +337,11 @@ def reference_arm(args):
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 0, "impl": "reference",
         "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": "H2O/CH4/C2H6/NH3 mixture 0.8 g/cm3, QEq tol 1e-6, dt 0.25 fs",
+        # the GPU arm's workload; each step times a bounded sample of it
+        "config": {"workload": workload_name(1048576 if args.scale == 1.0 else
+                                             int(round(1048576 * args.scale))),
+                   "atoms": 1048576 if args.scale == 1.0 else int(round(1048576 * args.scale)),
+                   "parallelism": f"{procs} CPU processes",
                    "sample_atoms_per_process": sample, "processes": procs},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": procs, "kind": "port",
                          "sample": f"{procs} processes x one QEq+force step of a "
@@ -492,8 +501,7 @@ def gpu_arm(args):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": tmax * 1e3 / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f64", "data": "synthetic (seeded molecular mixture)",
-        "config": {"workload": f"H2O/CH4/C2H6/NH3 0.5/0.2/0.2/0.1 mixture, {n} atoms, "
-                               "0.8 g/cm3, 300 K, NVE dt 0.25 fs, QEq tol 1e-6, FP64",
+        "config": {"workload": workload_name(n),
                    "atoms": n, "parallelism": f"replicas x{world}",
                    "l2": "inputs larger than L2 (pair list ~GBs)"},
         "e2e": e2e,

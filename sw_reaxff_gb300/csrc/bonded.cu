@@ -507,8 +507,9 @@ __global__ void __launch_bounds__(256) k_hbonds32(Dev d, int eflag) {
         disp32(g, d.xf[k], d.xl[k], hjf, ljf, sx, sy, sz, djk[0], djk[1], djk[2]);
         const float r_jk = sqrtf(djk[0] * djk[0] + djk[1] * djk[1] + djk[2] * djk[2]);
         float theta, cos_theta, di[3], djv[3], dk[3];
-        theta_dcos<float, false>(dij, r_ij, djk, r_jk, theta, cos_theta, di, djv, dk);
-        float sin_xhz4 = (1.f - cos_theta) * 0.5f;   // sin^2(theta/2)
+        theta_dcos<float>(dij, r_ij, djk, r_jk, theta, cos_theta, di, djv, dk);
+        const float sin_theta2 = sinf(theta / 2.f);
+        float sin_xhz4 = sin_theta2 * sin_theta2;
         sin_xhz4 *= sin_xhz4;
         const float cos_xhz1 = 1.f - cos_theta;
         const float exp_hb2 = expf(-hp.p_hb2 * BO);

@@ -239,26 +239,37 @@ __device__ __forceinline__ void nbr_flush(const Dev &d, const Control &C, const 
     img = Q.img[lane];
     int sx, sy, sz;
     img_unpack(img, &sx, &sy, &sz);
+    // membership from the FP32 (hi, lo) displacement away from the
+    // cutoffs, from the exact FP64 distance within MARGIN32 of them
+    const float4 hj = d.xf[j], lj = d.xl[j];
+    float dx, dy, dz;
+    disp32(g, hj, lj, xif, xil, sx, sy, sz, dx, dy, dz);
+    d2f = dx * dx + dy * dy + dz * dz;
+    const float lc2 = C.list_cut2_f;
+    if (d2f <= lc2 * (1.f - MARGIN32)) in = true;
+    else if (d2f > lc2 * (1.f + MARGIN32)) in = false;
+    else in = exact_d2(d, j, sx, sy, sz, xi, g) <= C.list_cut2;
+    const float nc2 = C.near_cut_f * C.near_cut_f;
     if (MIXED) {
-      const float4 hj = d.xf[j], lj = d.xl[j];
-      float dx, dy, dz;
-      disp32(g, hj, lj, xif, xil, sx, sy, sz, dx, dy, dz);
-      d2f = dx * dx + dy * dy + dz * dz;
-      const float lc2 = C.list_cut2_f;
-      if (d2f <= lc2 * (1.f - MARGIN32)) in = true;
-      else if (d2f > lc2 * (1.f + MARGIN32)) in = false;
-      else in = exact_d2(d, j, sx, sy, sz, xi, g) <= C.list_cut2;
       // near part: conservative (the bond pass tests its own cutoffs)
-      const float nc = C.near_cut_f;
-      near = d2f <= nc * nc * (1.f + MARGIN32);
-    } else {
-      d2 = exact_d2(d, j, sx, sy, sz, xi, g);
-      in = d2 <= C.list_cut2;
-      if (in) {
-        if (d2 <= C.near_cut2_lo) near = true;
-        else if (d2 > C.near_cut2_hi) near = false;
-        else near = __dsqrt_rn(d2) <= C.near_cut;
+      near = d2f <= nc2 * (1.f + MARGIN32);
+    } else if (in) {
+      // FP64 form: the reference's near membership, d <= near_cut exactly
+      if (d2f <= nc2 * (1.f - MARGIN32)) near = true;
+      else if (d2f > nc2 * (1.f + MARGIN32)) near = false;
+      else {
+        const double e2 = exact_d2(d, j, sx, sy, sz, xi, g);
+        if (e2 <= C.near_cut2_lo) near = true;
+        else if (e2 > C.near_cut2_hi) near = false;
+        else near = __dsqrt_rn(e2) <= C.near_cut;
       }
+    }
+    if (!MIXED && in) {
+      // r^2 for H: FMA-rounded from the exact displacement (the pair
+      // functions are smooth; membership is decided above)
+      double ex, ey, ez;
+      disp64(g, d.xs[j], xi, sx, sy, sz, ex, ey, ez);
+      d2 = fma(ex, ex, fma(ey, ey, ez * ez));
     }
   }
   const unsigned mn = __ballot_sync(FULL, in && near);
@@ -292,7 +303,9 @@ __device__ __forceinline__ void nbr_flush(const Dev &d, const Control &C, const 
     } else if (MIXED) {
       d.nbr[row + pos] = ((uint32_t)j << 8) | (uint32_t)img;
       d.hval32[row + pos] = 0.f;
-    } else if (d2 <= C.swb2 && C.tab_n && d2 >= C.tab_s0) {
+    } else if (!(C.h_all_listed || d2 <= C.swb2)) {
+      h = 0.0;
+    } else if (C.tab_n && d2f >= C.tab_s0_f) {
       // FP64 table of H_ij (cubic Hermite in r^2, power basis per interval)
       const double x = fma(d2, C.tab_inv_ds, C.tab_x0);
       int k = (int)x;
@@ -303,7 +316,7 @@ __device__ __forceinline__ void nbr_flush(const Dev &d, const Control &C, const 
           reinterpret_cast<const double2 *>(d.tab_h + ((long long)C.tab_pair[ti][tj] * C.tab_n + k) * 4);
       const double2 c01 = T[0], c23 = T[1];
       h = fma(fma(fma(c23.y, u, c23.x), u, c01.y), u, c01.x);
-    } else if (d2 <= C.swb2) {
+    } else {
       // H_ij = Tap(r) * 14.4 / (r^3 + shld)^c, c = 0.3333333333333
       const double r = d2 * rsqrt(d2);
       const double *T = C.qTap;
@@ -339,7 +352,7 @@ __global__ void __launch_bounds__(NB_WARPS * 32) k_build_nbrs(Dev d) {
   const ForceField &F = *d.ff;
   const double4 xi = d.xs[i];
   const float4 xif = d.xf[i];
-  const float4 xil = MIXED ? d.xl[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+  const float4 xil = d.xl[i];
   const int ti = d.ts[i];
   const float cut2f = C.list_pre2_f;
   const SegGeom &g = d.seg[d.seg_s[i]];
@@ -351,23 +364,48 @@ __global__ void __launch_bounds__(NB_WARPS * 32) k_build_nbrs(Dev d) {
   const int cap = d.nb_cap;
   const int nx = ncx;
   int cntN = 0, cntF = 0, qn = 0;
+  // Orthogonal segments clip the stencil to the cutoff sphere: a row of
+  // cells (fixed oy, oz) whose y-z slab is farther from atom i than the
+  // cutoff is skipped, and along x only the cells the sphere reaches at the
+  // row's y-z distance are walked (FP32 geometry with the prefilter's
+  // margin; the unwrapped cell indices give the periodic images' places).
+  const bool clip = !g.tri;
+  const float wx = g.cellw_f[0], wy = g.cellw_f[1], wz = g.cellw_f[2];
   for (int oz = -S; oz <= S; ++oz) {
     int rz = cz + oz, sz = 0;
     while (rz < 0) { rz += ncz; --sz; }
     while (rz >= ncz) { rz -= ncz; ++sz; }
+    float dz2 = 0.f;
+    if (clip) {
+      const float lo = (cz + oz) * wz - xif.z, hi = lo + wz;
+      const float dz = lo > 0.f ? lo : (hi < 0.f ? -hi : 0.f);
+      dz2 = dz * dz;
+      if (dz2 > cut2f) continue;
+    }
     for (int oy = -S; oy <= S; ++oy) {
       int ry = cy + oy, sy = 0;
       while (ry < 0) { ry += ncy; --sy; }
       while (ry >= ncy) { ry -= ncy; ++sy; }
+      int ox_lo = -S, ox_hi = S;
+      if (clip) {
+        const float lo = (cy + oy) * wy - xif.y, hi = lo + wy;
+        const float dy = lo > 0.f ? lo : (hi < 0.f ? -hi : 0.f);
+        const float r2 = cut2f - dz2 - dy * dy;
+        if (r2 < 0.f) continue;
+        const float rx_ = sqrtf(r2);
+        // cells whose x-range meets [x_i - rx_, x_i + rx_]
+        ox_lo = max(ox_lo, (int)floorf((xif.x - rx_) / wx) - cx);
+        ox_hi = min(ox_hi, (int)floorf((xif.x + rx_) / wx) - cx);
+      }
       const int rowcell = g.cell0 + (rz * ncy + ry) * nx;
       // runs of consecutive cells with one x image each
-      int ox = -S;
-      while (ox <= S) {
+      int ox = ox_lo;
+      while (ox <= ox_hi) {
         int rx = cx + ox, sx = 0;
         while (rx < 0) { rx += nx; --sx; }
         while (rx >= nx) { rx -= nx; ++sx; }
         int len = 1;
-        while (ox + len <= S && rx + len < nx) ++len;
+        while (ox + len <= ox_hi && rx + len < nx) ++len;
         const int beg = d.cell_start[rowcell + rx];
         const int end = d.cell_start[rowcell + rx + len];
         ox += len;

@@ -15,7 +15,7 @@
 namespace {
 
 constexpr unsigned FULL = 0xffffffffu;
-constexpr double C_ele = 332.06371;   // reaxc_defs_sunway.h:59
+constexpr double C_ele = RG_C_ELE;
 constexpr int IMG0 = 62;              // img_pack(0,0,0)
 
 __device__ __forceinline__ double warp_sum(double v) {
@@ -55,40 +55,51 @@ __device__ __forceinline__ void taper(const Control &C, double r, double rinv, d
   dTap = fma(Tap[1], rinv, dTap);
 }
 
+__device__ __forceinline__ double cubic_u(const double2 &c01, const double2 &c23, double u) {
+  return fma(fma(fma(c23.y, u, c23.x), u, c01.y), u, c01.x);
+}
+
 // FP64 form: vdW + Coulomb of one queued pair, from the pair-function
-// tables (tabulate > 0) or the reference's expressions; returns (1/r) dE/dr
-// in c and the displacement; energies are added to evdw and eele
-__device__ __forceinline__ void pair_terms(const Dev &d, const ForceField &F, const Control &C,
+// tables (tabulate > 0) or the reference's expressions; returns whether the
+// pair is inside the cutoff, (1/r) dE/dr in c and the displacement; with EF
+// the energies are added to evdw and eele
+template <bool EF>
+__device__ __forceinline__ bool pair_terms(const Dev &d, const ForceField &F, const Control &C,
                                           uint32_t e, bool act, const double4 &xi, int ti,
                                           const SegGeom &g, double &evdw, double &eele,
                                           double &c, double &dx, double &dy, double &dz,
                                           int &j) {
   c = 0.0; dx = dy = dz = 0.0;
   j = (int)(e >> 8);
-  if (!act) return;
+  if (!act) return false;
   int sx, sy, sz;
   img_unpack((int)(e & 255u), &sx, &sy, &sz);
-  // same rounding as the pair-list membership test
   const double4 xj = d.xs[j];
   const double qj = xj.w;
   disp64(g, xj, xi, sx, sy, sz, dx, dy, dz);
-  const double d2 = __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
-  if (d2 > C.nonb_cut2) { dx = dy = dz = 0.0; return; }
+  // the cutoff test with the reference's rounding where the list reaches
+  // beyond nonb_cut; r^2 for the pair functions by FMAs
+  if (!C.nonb_all_listed &&
+      __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz)) > C.nonb_cut2)
+    return false;
+  const double d2 = fma(dx, dx, fma(dy, dy, dz * dz));
   if (C.tab_n && d2 >= C.tab_s0) {
-    // FP64 tables: energies and (1/r) dE/dr = 2 dE/ds by cubic Hermite
-    double h01, t10, t11;
-    const int k = tab_weights(C, d2, h01, t10, t11);
-    const double *T = d.tab_nb + ((long long)C.tab_pair[ti][d.ts[j]] * (C.tab_n + 1) + k) * 6;
-    const double ds = C.tab_ds;
-    const double ev = tab_interp(T[0], T[6], ds * T[1], ds * T[7], h01, t10, t11);
-    const double dv = tab_interp(T[1], T[7], T[2], T[8], h01, t10, t11);
-    const double ec = tab_interp(T[3], T[9], ds * T[4], ds * T[10], h01, t10, t11);
-    const double dcl = tab_interp(T[4], T[10], T[5], T[11], h01, t10, t11);
-    const double qq = C_ele * xi.w * qj;
-    evdw += ev;
-    eele += qq * ec;
-    c = 2.0 * (dv + qq * dcl);
-    return;
+    // FP64 tables in s = r^2: (1/r) dE/dr of vdW and of Coulomb per unit
+    // qi qj (C_ele folded in) as cubics in u of the interval; the energies'
+    // cubics follow and are read on energy steps only
+    const double x = fma(d2, C.tab_inv_ds, C.tab_x0);
+    int k = (int)x;
+    if (k > C.tab_n - 1) k = C.tab_n - 1;
+    const double u = x - (double)k;
+    const double2 *T = reinterpret_cast<const double2 *>(
+        d.tab_nb + ((long long)C.tab_pair[ti][d.ts[j]] * C.tab_n + k) * 16);
+    const double qq = xi.w * qj;
+    c = fma(cubic_u(T[2], T[3], u), qq, cubic_u(T[0], T[1], u));
+    if (EF) {
+      evdw += cubic_u(T[4], T[5], u);
+      eele = fma(qq, cubic_u(T[6], T[7], u), eele);
+    }
+    return true;
   }
   const double rinv = rsqrt(d2);
   const double r = d2 * rinv;
@@ -134,11 +145,13 @@ __device__ __forceinline__ void pair_terms(const Dev &d, const ForceField &F, co
   const double dr3gamij_1 = fma(d2, r, tw.gamma);
   const double inv3 = rpow_third(dr3gamij_1, RG_C3_ELE);
   const double qq = C_ele * xi.w * qj;
-  const double e_ele = qq * Tp * inv3;
   const double CEclmb = qq * (dTap - Tp * r / dr3gamij_1) * inv3;
-  evdw += Tp * (e_vdW + e_core + e_lg);
-  eele += e_ele;
+  if (EF) {
+    evdw += Tp * (e_vdW + e_core + e_lg);
+    eele += qq * Tp * inv3;
+  }
   c = CEvd + CEclmb;
+  return true;
 }
 
 // Mixed form: vdW + Coulomb of one pair entirely in FP32, parameters from
@@ -231,8 +244,8 @@ __device__ __forceinline__ void pair32(const Dev &d, const Control &C, int vdw_t
 
 // one warp per atom i; the pairs (i,j,image) with j > i, or j == i with the
 // "positive" image, are queued and evaluated 32 at a time
-template <typename R, bool VIR>
-__global__ void __launch_bounds__(NBW * 32) k_nonbonded(Dev d, int eflag) {
+template <typename R, bool VIR, bool EF>
+__global__ void __launch_bounds__(NBW * 32) k_nonbonded(Dev d) {
   __shared__ PairQueue queues[NBW];
   const int lane = threadIdx.x & 31;
   const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -282,7 +295,7 @@ __global__ void __launch_bounds__(NBW * 32) k_nonbonded(Dev d, int eflag) {
         if constexpr (std::is_same<R, float>::value) {
           float ev, ee, c, dx, dy, dz;
           pair32(d, C, vdw_type, e, act, xi, xif, xil, ti, g, ev, ee, c, dx, dy, dz, j);
-          if (eflag) {   // energies summed in FP64 (only on energy steps)
+          if (EF) {   // energies summed in FP64 (only on energy steps)
             evdw += (double)ev;
             eele += (double)ee;
           }
@@ -297,8 +310,7 @@ __global__ void __launch_bounds__(NBW * 32) k_nonbonded(Dev d, int eflag) {
           }
         } else {
           double c, dx, dy, dz;
-          pair_terms(d, F, C, e, act, xi, ti, g, evdw, eele, c, dx, dy, dz, j);
-          if (act && c != 0.0) {
+          if (pair_terms<EF>(d, F, C, e, act, xi, ti, g, evdw, eele, c, dx, dy, dz, j)) {
             fx -= c * dx;
             fy -= c * dy;
             fz -= c * dz;
@@ -340,7 +352,7 @@ __global__ void __launch_bounds__(NBW * 32) k_nonbonded(Dev d, int eflag) {
       }
     }
   }
-  if (eflag) {
+  if (EF) {
     const int sg = i < d.n ? d.seg_s[i] : -1;
     const double v[4] = {2.0 * evdw, 2.0 * eele, evdw, eele};
     static_assert(E_ELE == E_VDW + 1, "energy slots");
@@ -353,14 +365,20 @@ __global__ void __launch_bounds__(NBW * 32) k_nonbonded(Dev d, int eflag) {
 
 }  // namespace
 
+template <typename R, bool VIR>
+void launch_nb(const Dev &d, cudaStream_t st, int eflag, unsigned G) {
+  if (eflag) k_nonbonded<R, VIR, true><<<G, NBW * 32, 0, st>>>(d);
+  else k_nonbonded<R, VIR, false><<<G, NBW * 32, 0, st>>>(d);
+}
+
 void launch_nonbonded(const Dev &d, cudaStream_t st, int eflag) {
   const long long threads = (long long)d.n * 32;
   const unsigned G = (unsigned)((threads + NBW * 32 - 1) / (NBW * 32));
   if (d.vflag) {
-    if (d.mixed) k_nonbonded<float, true><<<G, NBW * 32, 0, st>>>(d, eflag);
-    else k_nonbonded<double, true><<<G, NBW * 32, 0, st>>>(d, eflag);
+    if (d.mixed) launch_nb<float, true>(d, st, eflag, G);
+    else launch_nb<double, true>(d, st, eflag, G);
   } else {
-    if (d.mixed) k_nonbonded<float, false><<<G, NBW * 32, 0, st>>>(d, eflag);
-    else k_nonbonded<double, false><<<G, NBW * 32, 0, st>>>(d, eflag);
+    if (d.mixed) launch_nb<float, false>(d, st, eflag, G);
+    else launch_nb<double, false>(d, st, eflag, G);
   }
 }

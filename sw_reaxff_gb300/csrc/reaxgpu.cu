@@ -224,6 +224,7 @@ int setup_cells(rg_system *h) {
       nc = std::max(nc, 1);
       g.nc[k] = nc;
       g.cellw[k] = g.L[k] / nc;
+      g.cellw_f[k] = (float)g.cellw[k];
       nseg_cells *= nc;
     }
     g.cell0 = (int)ncell;
@@ -742,6 +743,7 @@ void init_control(const rg_params &p, const ForceField &ff, Control &c) {
   c.inv_swb_nb = 1.0 / c.nonb_cut;
   c.inv_swb_q = 1.0 / p.qeq_swb;
   c.nonb_all_listed = c.nonb_cut2 >= c.list_cut2;
+  c.h_all_listed = c.swb2 >= c.list_cut2;
   c.list_pre2_f = (float)(c.list_cut2 * (1.0 + 1e-5) + 0.05);
   c.list_cut2_f = (float)c.list_cut2;
   c.thb_cut_f = (float)c.thb_cut;
@@ -887,6 +889,7 @@ int rg_create(const char *ffield_path, const rg_params *pin, rg_system **out) {
     const double s0 = 0.25, s1 = c.list_cut2 * (1.0 + 1e-9);
     c.tab_n = h->p.tabulate;
     c.tab_s0 = s0;
+    c.tab_s0_f = (float)s0;
     c.tab_ds = (s1 - s0) / c.tab_n;
     c.tab_inv_ds = 1.0 / c.tab_ds;
     c.tab_x0 = -s0 * c.tab_inv_ds;

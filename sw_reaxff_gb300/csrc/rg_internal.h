@@ -78,6 +78,7 @@ struct SegGeom {
   float Lh[3], Ll[3]; // L as an unevaluated FP32 pair (hi + lo)
   float Th[3];        // tilts in FP32 (prefilter shifts only)
   double cellw[3];    // orthogonal: cell edges (L / nc)
+  float cellw_f[3];   // the same in FP32 (clipping the stencil)
   int nc[3];          // cells per dimension (fractional axes when tri)
   int S;              // stencil half-width (cells)
   int cell0;          // first global cell index of the segment
@@ -103,10 +104,12 @@ struct Control {
   int tap_factored, qtap_factored;
   double inv_swb_nb, inv_swb_q;
   int nonb_all_listed;   // nonb_cut >= list cutoff: every list entry is a vdW/Coulomb pair
+  int h_all_listed;      // qeq_swb >= list cutoff: every list entry has an H_ij
   // FP64 tables (tables.cpp): tab_n intervals of width tab_ds over
   // s = r^2 in [tab_s0, ...]; 0 = analytic pair functions
   int tab_n;
   double tab_s0, tab_ds, tab_inv_ds, tab_x0;   // tab_x0 = -tab_s0 / tab_ds
+  float tab_s0_f;        // table or analytic form below it (either is the function)
   int tab_pair[RG_MAXT][RG_MAXT];   // unordered type pair -> table index
   // FP32 copies for the prefilters (no FP64 conversions per entry; GB300
   // runs FP64 at 1/64 of the FP32 rate)
@@ -166,8 +169,8 @@ struct Dev {
 
   const ForceField *ff;
   const Control *ctl;
-  const double *tab_nb;  // [pair][node][6]: Ev, dEv/ds, d2Ev/ds2, Ec, dEc/ds, d2Ec/ds2
-  const double *tab_h;   // [pair][node][2]: H, dH/ds
+  const double *tab_nb;  // [pair][interval][16]: cubics in u of Fv, Fc, Ev, Ec (tables.cpp)
+  const double *tab_h;   // [pair][interval][4]: cubic in u of H_ij
 
   // original order (persistent state)
   double *x_o, *v_o, *q_o, *f_o;
@@ -260,6 +263,8 @@ struct Dev {
 enum { ST_OVF = 0, ST_MAXNB = 1, ST_MAXB = 2, ST_MAXHB = 3, ST_NAN = 4 };
 enum { OVF_NBR = 1, OVF_BOND = 2, OVF_HB = 4, OVF_CELL = 8 };
 
+#define RG_C_ELE 332.06371   // Coulomb constant, kcal A / (mol e^2) (reaxc_defs_sunway.h:59)
+
 // x^c for the reference's truncated cube-root exponents c = 0.3333333333333
 // (QEq H, fix_qeq_reax_sw64.c:885) and 0.33333333333333 (Coulomb,
 // reaxc_nonbonded_sw64.c:195): cbrt(x) * x^(c - 1/3), where the tiny second
@@ -331,12 +336,6 @@ __device__ __forceinline__ void vir_acc(double *w, double dx, double dy, double 
   w[5] -= dy * gz;
 }
 
-// x + s L with the reference's rounding; the image-free case (most pairs)
-// skips the product and the add, which leave x unchanged anyway
-__device__ __forceinline__ double img_shift(double x, int s, double L) {
-  return s ? __dadd_rn(x, s * L) : x;
-}
-
 // Lattice translation sx a + sy b + sz c of a segment, rounded per
 // operation in this order (the oracle builds its periodic images the same
 // way); for an orthogonal box it is (sx lx, sy ly, sz lz) exactly.
@@ -348,14 +347,26 @@ __device__ __forceinline__ void img_vec(const SegGeom &g, int sx, int sy, int sz
   vz = __dmul_rn((double)sz, g.L[2]);
 }
 
-// exact displacement (x_j + image) - x_i of the membership tests
+// s in [-2, 2] as a double, from its IEEE-754 bits (integer operations
+// only: a conversion would occupy the FP64 pipe like an FMA)
+__device__ __forceinline__ double small_int_d(int s) {
+  const int a = s < 0 ? -s : s;
+  unsigned hi = a == 0 ? 0u : (a == 1 ? 0x3FF00000u : 0x40000000u);
+  if (s < 0) hi |= 0x80000000u;
+  return __hiloint2double((int)hi, 0);
+}
+
+// exact displacement (x_j + image) - x_i of the membership tests.  For an
+// orthogonal box x_j + s L is one FMA: s L is exact for |s| <= 2, so the
+// FMA rounds the same sum as the reference's add, and s = 0 gives x_j
+// unchanged; no branch on the image keeps the warp's lanes together.
 __device__ __forceinline__ void disp64(const SegGeom &g, const double4 &xj, const double4 &xi,
                                        int sx, int sy, int sz, double &dx, double &dy,
                                        double &dz) {
   if (!g.tri) {
-    dx = __dsub_rn(img_shift(xj.x, sx, g.L[0]), xi.x);
-    dy = __dsub_rn(img_shift(xj.y, sy, g.L[1]), xi.y);
-    dz = __dsub_rn(img_shift(xj.z, sz, g.L[2]), xi.z);
+    dx = __dsub_rn(__fma_rn(small_int_d(sx), g.L[0], xj.x), xi.x);
+    dy = __dsub_rn(__fma_rn(small_int_d(sy), g.L[1], xj.y), xi.y);
+    dz = __dsub_rn(__fma_rn(small_int_d(sz), g.L[2], xj.z), xi.z);
   } else if (sx | sy | sz) {
     double vx, vy, vz;
     img_vec(g, sx, sy, sz, vx, vy, vz);
@@ -428,28 +439,7 @@ __device__ __forceinline__ void frac3(const SegGeom &g, double x, double y, doub
   u = __ddiv_rn(__dsub_rn(__dsub_rn(x, __dmul_rn(v, g.tilt[0])), __dmul_rn(w, g.tilt[1])), g.L[0]);
 }
 
-// cubic Hermite interpolation in the FP64 tables: for s, the interval k,
-// the weight h01 of the right node value and the weights t10, t11 of the
-// node derivatives in units of the spacing; with y0, y1 the node values and
-// p0, p1 the derivatives times the spacing:
-//   y(s) = y0 + h01 (y1 - y0) + t10 p0 + t11 p1
-__device__ __forceinline__ int tab_weights(const Control &C, double s, double &h01, double &t10,
-                                           double &t11) {
-  const double x = fma(s, C.tab_inv_ds, C.tab_x0);
-  int k = (int)x;
-  if (k > C.tab_n - 1) k = C.tab_n - 1;
-  const double u = x - (double)k, u2 = u * u, w = 1.0 - u;
-  h01 = u2 * fma(-2.0, u, 3.0);
-  t10 = u * w * w;
-  t11 = -u2 * w;
-  return k;
-}
-
-__device__ __forceinline__ double tab_interp(double y0, double y1, double p0, double p1, double h01,
-                                             double t10, double t11) {
-  return fma(t11, p1, fma(t10, p0, fma(h01, y1 - y0, y0)));
-}
-
+// x^c for the exponents above: cbrt(x) (1 + (c - 1/3) ln x)
 __device__ __forceinline__ double pow_third(double x, double dc) {
   return cbrt(x) * (1.0 + dc * (double)__logf((float)x));
 }

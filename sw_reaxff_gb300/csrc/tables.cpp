@@ -7,12 +7,12 @@
 // reaxc_ctypes_sunway.h:832-860) that its NULL control path leaves off
 // (tabulate = 0).  Here the table replaces the FP64 transcendental work of
 // the pair kernels (two exp, two log and a cube root per pair, ~240 FP64
-// instructions, on a GPU whose FP64 rate is 1/64 of its FP32 rate) by ~30
-// FP64 instructions and 96 L2-resident bytes.  Interpolating in s needs no
-// square root, and (1/r) dE/dr = 2 dE/ds.  Each node holds the function
-// and its s-derivative (the reference's own force expression, halved), and
-// for the force factor its s-derivative by a fourth-order central
-// difference; with 65536 intervals on [0.25, rc^2] A^2 the interpolants
+// instructions, on a GPU whose FP64 rate is 1/64 of its FP32 rate) by ten
+// FP64 instructions and 64 L2-resident bytes per pair on force-only steps.  Interpolating in s needs no
+// square root, and (1/r) dE/dr = 2 dE/ds.  Each interval's cubic matches
+// the function and its s-derivative at both ends (the energies' derivative
+// is the reference's own force expression, halved; the force factors'
+// derivatives are fourth-order central differences); with 65536 intervals on [0.25, rc^2] A^2 the interpolants
 // agree with the analytic expressions to ~1e-10 (relative to
 // max(|f|, 1e-4 max|f|); checked here, rg_table_info), inside the 1e-9
 // parity bars.
@@ -95,12 +95,6 @@ double deriv(G g, double s, double h) {
   return (-g(s + 2 * h) + 8 * g(s + h) - 8 * g(s - h) + g(s - 2 * h)) / (12 * h);
 }
 
-double hermite(double y0, double d0, double y1, double d1, double u, double ds) {
-  const double u2 = u * u;
-  const double h01 = u2 * (3.0 - 2.0 * u), h00 = 1.0 - h01;
-  const double h10 = ds * u * (1.0 - u) * (1.0 - u), h11 = ds * u2 * (u - 1.0);
-  return h00 * y0 + h01 * y1 + h10 * d0 + h11 * d1;
-}
 
 }  // namespace
 
@@ -109,20 +103,24 @@ int rg_pair_index(int ti, int tj, int nt) {
   return ti * nt - ti * (ti - 1) / 2 + (tj - ti);
 }
 
-// Fills nb[npair][n+1][6] = {Ev, Dv, ds Dv', Ec, Dc, ds Dc'} (D = dE/ds,
-// ' = d/ds, ds the node spacing) per node and hq[npair][n][4] = the Hermite
-// cubic of H (nodes H, ds H') per interval in the power basis
-// c0 + u (c1 + u (c2 + u c3)), u in [0, 1] (three FMAs and no weights on the
-// device; the same 32 bytes per evaluation), over s in [s0, s1] with n
-// intervals; with
-// check, returns the largest deviation of the interpolants from the
-// analytic functions at 5 interior points of every interval (else 0).
+// Fills, per type pair and interval of s in [s0, s1] (n intervals of width
+// ds), the Hermite cubic of each tabulated function in the power basis of
+// u in [0, 1]: c0 + u (c1 + u (c2 + u c3)) (three FMAs, no weights):
+//   nb[npair][n][16] = { Fv[4], Fc[4], Ev[4], Ec[4] }
+//     Fv = (1/r) dE_vdW/dr = 2 dE_vdW/ds, Fc = C_ele (1/r) dE_ele/dr per
+//     unit qi qj, Ev = the tapered vdW energy, Ec = C_ele Tap/(r^3+g)^c;
+//     the force factors come first (the 64 bytes a force-only step reads)
+//   hq[npair][n][4] = H_ij
+// from node values and s-derivatives (the force factors' own derivatives by
+// a fourth-order central difference).  With check, returns the largest
+// deviation of the interpolants from the analytic functions at 5 interior
+// points of every interval (else 0).
 double rg_build_tables(const ForceField &F, const Control &C, int n, double s0, double s1,
                        std::vector<double> &nb, std::vector<double> &hq, bool check) {
   const int nt = F.ntypes;
   const int np = nt * (nt + 1) / 2;
   const double ds = (s1 - s0) / n;
-  nb.assign((size_t)np * (n + 1) * 6, 0.0);
+  nb.assign((size_t)np * n * 16, 0.0);
   hq.assign((size_t)np * n * 4, 0.0);
   std::vector<std::pair<int, int>> pairs;
   for (int ti = 0; ti < nt; ++ti)
@@ -131,69 +129,69 @@ double rg_build_tables(const ForceField &F, const Control &C, int n, double s0, 
   // one host thread per type pair
   auto build_pair = [&](size_t w) {
     const int ti = pairs[w].first, tj = pairs[w].second;
+    const int p = rg_pair_index(ti, tj, nt);
+    auto funcs = [&](double s, double *o) {
+      pair_funcs(F, C, ti, tj, std::sqrt(s), &o[0], &o[1], &o[2], &o[3]);
+      o[2] *= RG_C_ELE;
+      o[3] *= RG_C_ELE;
+    };
+    auto fv = [&](double s) { double o[4]; funcs(s, o); return o[1]; };
+    auto fc = [&](double s) { double o[4]; funcs(s, o); return o[3]; };
+    auto hf = [&](double s) { return h_func(F, C, ti, tj, std::sqrt(s)); };
+    const double h = 1e-4;
+    // node values y and s-derivatives dy of Fv, Fc, Ev, Ec, H
+    std::vector<double> y((size_t)(n + 1) * 5), dy((size_t)(n + 1) * 5);
+    for (int k = 0; k <= n; ++k) {
+      const double s = s0 + k * ds;
+      double o[4];
+      funcs(s, o);
+      double *Y = &y[(size_t)k * 5], *D = &dy[(size_t)k * 5];
+      Y[0] = o[1];
+      D[0] = deriv(fv, s, h);
+      Y[1] = o[3];
+      D[1] = deriv(fc, s, h);
+      Y[2] = o[0];
+      D[2] = 0.5 * o[1];      // dEv/ds = (1/2)(1/r) dEv/dr
+      Y[3] = o[2];
+      D[3] = 0.5 * o[3];
+      Y[4] = hf(s);
+      D[4] = deriv(hf, s, h);
+    }
+    auto coeffs = [&](int k, int f, double *c) {
+      const double y0 = y[(size_t)k * 5 + f], y1 = y[(size_t)(k + 1) * 5 + f];
+      const double p0 = ds * dy[(size_t)k * 5 + f], p1 = ds * dy[(size_t)(k + 1) * 5 + f];
+      c[0] = y0;
+      c[1] = p0;
+      c[2] = 3.0 * (y1 - y0) - 2.0 * p0 - p1;
+      c[3] = 2.0 * (y0 - y1) + p0 + p1;
+    };
+    for (int k = 0; k < n; ++k) {
+      double *e = &nb[((size_t)p * n + k) * 16];
+      for (int f = 0; f < 4; ++f) coeffs(k, f, e + 4 * f);
+      coeffs(k, 4, &hq[((size_t)p * n + k) * 4]);
+    }
+    if (!check) return;
+    // accuracy of the interpolants against the analytic functions:
+    // relative error where |f| >= 1e-4 max|f|, absolute error in units of
+    // 1e-4 max|f| below (near zero crossings and the taper's end, where the
+    // analytic form itself carries the expanded polynomial's cancellation)
+    double M[5] = {0, 0, 0, 0, 0};
+    for (int k = 0; k <= n; ++k)
+      for (int f = 0; f < 5; ++f) M[f] = std::max(M[f], std::fabs(y[(size_t)k * 5 + f]));
     double worst = 0.0;
-    {
-      const int p = rg_pair_index(ti, tj, nt);
-      auto ev = [&](double s) { double a, b, c, d; pair_funcs(F, C, ti, tj, std::sqrt(s), &a, &b, &c, &d); return a; };
-      auto dv = [&](double s) { double a, b, c, d; pair_funcs(F, C, ti, tj, std::sqrt(s), &a, &b, &c, &d); return 0.5 * b; };
-      auto ecf = [&](double s) { double a, b, c, d; pair_funcs(F, C, ti, tj, std::sqrt(s), &a, &b, &c, &d); return c; };
-      auto dc = [&](double s) { double a, b, c, d; pair_funcs(F, C, ti, tj, std::sqrt(s), &a, &b, &c, &d); return 0.5 * d; };
-      auto hf = [&](double s) { return h_func(F, C, ti, tj, std::sqrt(s)); };
-      const double h = 1e-4;
-      double hy0 = 0.0, hp0 = 0.0;
-      for (int k = 0; k <= n; ++k) {
-        const double s = s0 + k * ds;
-        double *e = &nb[((size_t)p * (n + 1) + k) * 6];
-        e[0] = ev(s);
-        e[1] = dv(s);
-        e[2] = ds * deriv(dv, s, h);
-        e[3] = ecf(s);
-        e[4] = dc(s);
-        e[5] = ds * deriv(dc, s, h);
-        // H: the Hermite cubic of each interval in the power basis of u
-        const double hy1 = hf(s), hp1 = ds * deriv(hf, s, h);
-        if (k > 0) {
-          double *q = &hq[((size_t)p * n + (k - 1)) * 4];
-          q[0] = hy0;
-          q[1] = hp0;
-          q[2] = 3.0 * (hy1 - hy0) - 2.0 * hp0 - hp1;
-          q[3] = 2.0 * (hy0 - hy1) + hp0 + hp1;
-        }
-        hy0 = hy1;
-        hp0 = hp1;
-      }
-      if (!check) return;
-      // accuracy of the interpolants against the analytic functions:
-      // relative error where |f| >= 1e-4 max|f|, absolute error in units of
-      // 1e-4 max|f| below (near zero crossings and the taper's end, where the
-      // analytic form itself carries the expanded polynomial's cancellation)
-      double M[5] = {0, 0, 0, 0, 0};
-      for (int k = 0; k <= n; ++k) {
-        const double *e = &nb[((size_t)p * (n + 1) + k) * 6];
-        M[0] = std::max(M[0], std::fabs(e[0]));
-        M[1] = std::max(M[1], std::fabs(2.0 * e[1]));
-        M[2] = std::max(M[2], std::fabs(e[3]));
-        M[3] = std::max(M[3], std::fabs(2.0 * e[4]));
-        if (k < n) M[4] = std::max(M[4], std::fabs(hq[((size_t)p * n + k) * 4]));
-      }
-      for (int k = 0; k < n; ++k) {
-        const double *a = &nb[((size_t)p * (n + 1) + k) * 6], *b = a + 6;
-        const double *qc = &hq[((size_t)p * n + k) * 4];
-        for (int m = 1; m <= 5; ++m) {
-          const double u = m / 6.0, s = s0 + (k + u) * ds;
-          double x[4];
-          pair_funcs(F, C, ti, tj, std::sqrt(s), &x[0], &x[1], &x[2], &x[3]);
-          const double iv[4] = {hermite(a[0], a[1], b[0], b[1], u, ds),
-                                2.0 * hermite(a[1], a[2], b[1], b[2], u, 1.0),
-                                hermite(a[3], a[4], b[3], b[4], u, ds),
-                                2.0 * hermite(a[4], a[5], b[4], b[5], u, 1.0)};
-          for (int c = 0; c < 4; ++c) {
-            const double scale = std::max(std::fabs(x[c]), 1e-4 * M[c]);
-            if (scale > 0.0) worst = std::max(worst, std::fabs(iv[c] - x[c]) / scale);
-          }
-          const double hv = ((qc[3] * u + qc[2]) * u + qc[1]) * u + qc[0], hx = hf(s);
-          const double hs = std::max(std::fabs(hx), 1e-4 * M[4]);
-          if (hs > 0.0) worst = std::max(worst, std::fabs(hv - hx) / hs);
+    for (int k = 0; k < n; ++k) {
+      const double *e = &nb[((size_t)p * n + k) * 16];
+      const double *qc = &hq[((size_t)p * n + k) * 4];
+      for (int m = 1; m <= 5; ++m) {
+        const double u = m / 6.0, s = s0 + (k + u) * ds;
+        double o[4];
+        funcs(s, o);
+        const double x[5] = {o[1], o[3], o[0], o[2], hf(s)};
+        for (int f = 0; f < 5; ++f) {
+          const double *c = f < 4 ? e + 4 * f : qc;
+          const double iv = ((c[3] * u + c[2]) * u + c[1]) * u + c[0];
+          const double scale = std::max(std::fabs(x[f]), 1e-4 * M[f]);
+          if (scale > 0.0) worst = std::max(worst, std::fabs(iv - x[f]) / scale);
         }
       }
     }

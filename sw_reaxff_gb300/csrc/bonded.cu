@@ -108,11 +108,10 @@ __global__ void k_bo_deltap(Dev d) {
   d.exp_boc[d.n + i] = exp(-d.ff->gp[1] * Dp);
 }
 
-__global__ void k_bo_correct(Dev d) {
+// the corrected bond order of bond slot k of atom i (f1 with f4 f5; the
+// reference's quotients taken as products with five reciprocals)
+__device__ __forceinline__ void bo_correct_item(const Dev &d, int i, int k) {
   const int n = d.n;
-  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  const int i = (int)(t % n), k = (int)(t / n);
-  if (k >= d.bond_cap || i >= n || k >= d.nbonds[i]) return;
   const long long s = (long long)k * n + i, S = (long long)d.bond_cap * n;
   const ForceField &F = *d.ff;
   const int j = nbr_of(d.b_nbr[s]);
@@ -133,16 +132,18 @@ __global__ void k_bo_correct(Dev d) {
       const double exp_p1i = d.exp_boc[i], exp_p2i = d.exp_boc[n + i];
       const double exp_p1j = d.exp_boc[j], exp_p2j = d.exp_boc[n + j];
       const double f2 = exp_p1i + exp_p1j;
-      const double f3 = -1.0 / p_boc2 * log(0.5 * (exp_p2i + exp_p2j));
-      f1 = 0.5 * ((val_i + f2) / (val_i + f2 + f3) + (val_j + f2) / (val_j + f2 + f3));
+      const double e22 = exp_p2i + exp_p2j, ie22 = 1.0 / e22;
+      const double f3 = -1.0 / p_boc2 * log(0.5 * e22);
       const double temp = f2 + f3;
       const double u1_ij = val_i + temp, u1_ji = val_j + temp;
-      const double Cf1A_ij = 0.5 * f3 * (1.0 / sqr(u1_ij) + 1.0 / sqr(u1_ji));
-      const double Cf1B_ij = -0.5 * ((u1_ij - f3) / sqr(u1_ij) + (u1_ji - f3) / sqr(u1_ji));
-      const double ep = exp_p2i / (exp_p2i + exp_p2j);
-      Cf1_ij = 0.50 * (-p_boc1 * exp_p1i / u1_ij - ((val_i + f2) / sqr(u1_ij)) * (-p_boc1 * exp_p1i + ep) +
-                       -p_boc1 * exp_p1i / u1_ji - ((val_j + f2) / sqr(u1_ji)) * (-p_boc1 * exp_p1i + ep));
-      Cf1_ji = -Cf1A_ij * p_boc1 * exp_p1j + Cf1B_ij * exp_p2j / (exp_p2i + exp_p2j);
+      const double a = 1.0 / u1_ij, b = 1.0 / u1_ji, a2 = a * a, b2 = b * b;
+      f1 = 0.5 * ((val_i + f2) * a + (val_j + f2) * b);
+      const double Cf1A_ij = 0.5 * f3 * (a2 + b2);
+      const double Cf1B_ij = -0.5 * ((u1_ij - f3) * a2 + (u1_ji - f3) * b2);
+      const double ep = exp_p2i * ie22;
+      Cf1_ij = 0.50 * (-p_boc1 * exp_p1i * a - ((val_i + f2) * a2) * (-p_boc1 * exp_p1i + ep) +
+                       -p_boc1 * exp_p1i * b - ((val_j + f2) * b2) * (-p_boc1 * exp_p1i + ep));
+      Cf1_ji = -Cf1A_ij * p_boc1 * exp_p1j + Cf1B_ij * exp_p2j * ie22;
     } else {
       f1 = 1.0;
       Cf1_ij = Cf1_ji = 0.0;
@@ -161,10 +162,11 @@ __global__ void k_bo_correct(Dev d) {
     }
     const double A0 = f1 * f4f5;
     const double A1 = -2 * tw.p_boc3 * tw.p_boc4 * BO * (Cf45_ij + Cf45_ji);
-    const double A2_ij = Cf1_ij / f1 + tw.p_boc3 * Cf45_ij;
-    const double A2_ji = Cf1_ji / f1 + tw.p_boc3 * Cf45_ji;
-    const double A3_ij = A2_ij + Cf1_ij / f1;
-    const double A3_ji = A2_ji + Cf1_ji / f1;
+    const double if1 = 1.0 / f1;
+    const double A2_ij = Cf1_ij * if1 + tw.p_boc3 * Cf45_ij;
+    const double A2_ji = Cf1_ji * if1 + tw.p_boc3 * Cf45_ji;
+    const double A3_ij = A2_ij + Cf1_ij * if1;
+    const double A3_ji = A2_ji + Cf1_ji * if1;
     BO = BO * A0;
     BOpi = BOpi * A0 * f1;
     BOpi2 = BOpi2 * A0 * f1;
@@ -180,6 +182,12 @@ __global__ void k_bo_correct(Dev d) {
   d.b_BO[s] = BO; d.b_BOs[s] = BOs; d.b_BOpi[s] = BOpi; d.b_BOpi2[s] = BOpi2;
 #pragma unroll
   for (int c = 0; c < 11; ++c) d.b_C[c * S + s] = C[c];
+}
+
+__global__ void __launch_bounds__(256) k_bo_correct(Dev d) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int cnt = i < d.n ? min(d.nbonds[i], d.bond_cap) : 0;
+  warp_items(cnt, i, [&](int a, int k) { bo_correct_item(d, a, k); });
 }
 
 __global__ void k_bo_atom(Dev d) {
@@ -367,8 +375,14 @@ __device__ __forceinline__ double warp_sum_d(double v) {
   return v;
 }
 
-// FP64 form (R = double; the mixed form runs k_hbonds32 below)
-template <typename R, bool VIR>
+// FP64 form (the mixed form runs k_hbonds32 below).  Per acceptor bond the
+// lanes hold exp(-p_hb2 BO) for every partner type (p_hb2 depends on the
+// partner's type, BO on the bond only), and 1/r_ij; per partner one
+// reciprocal square root gives 1/r_jk and r_jk, and 1/r0_hb comes with the
+// parameters, so no division is left in the triple loop.  The partners are
+// taken 32 at a time with all lanes in step (the per-type exponential is a
+// shuffle).
+template <bool VIR>
 __global__ void __launch_bounds__(256) k_hbonds(Dev d, int eflag) {
   const int lane = threadIdx.x & 31;
   const int j = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -388,56 +402,74 @@ __global__ void __launch_bounds__(256) k_hbonds(Dev d, int eflag) {
       const long long s = (long long)q * n + j;
       const int i = nbr_of(d.b_nbr[s]);
       const int ti = d.ts[i];
-      const double BO64 = d.b_BO[s];
-      if (F.sbp[ti].p_hbond != 2 || !(BO64 >= HB_THRESHOLD)) continue;
-      const R BO = (R)BO64;
-      const R dij[3] = {(R)d.b_dx[s], (R)d.b_dy[s], (R)d.b_dz[s]};
-      const R r_ij = (R)d.b_d[s];
+      const double BO = d.b_BO[s];
+      if (F.sbp[ti].p_hbond != 2 || !(BO >= HB_THRESHOLD)) continue;
+      const double dij[3] = {d.b_dx[s], d.b_dy[s], d.b_dz[s]};
+      const double r_ij = d.b_d[s];
+      const double inv_rij = 1.0 / r_ij, sqr_d_ji = r_ij * r_ij;
+      double e2 = 0.0;
+      if (lane < F.ntypes && F.hbp[ti][tj][lane].r0_hb > 0.0)
+        e2 = exp(-F.hbp[ti][tj][lane].p_hb2 * BO);
       const int tag_i = d.tags[i];
       double fix = 0, fiy = 0, fiz = 0, cdbo = 0;
-      for (int pk = lane; pk < nh; pk += 32) {
-        const uint32_t ek = d.hb_nbr[(long long)j * d.hb_cap + pk];
-        const int k = nbr_of(ek), tk = d.ts[k];
-        if (d.tags[k] == tag_i) continue;
+      for (int base = 0; base < nh; base += 32) {
+        const int pk = base + lane;
+        uint32_t ek = 0;
+        int k = 0, tk = 0;
+        bool ok = pk < nh;
+        if (ok) {
+          ek = d.hb_nbr[(long long)j * d.hb_cap + pk];
+          k = nbr_of(ek);
+          tk = d.ts[k];
+          ok = d.tags[k] != tag_i && F.hbp[ti][tj][tk].r0_hb > 0.0;
+        }
+        const double exp_hb2 = __shfl_sync(FULL, e2, tk);
+        if (!ok) continue;
         const Hbp &hbp = F.hbp[ti][tj][tk];
-        if (hbp.r0_hb <= 0.0) continue;
         int sx, sy, sz;
         img_unpack((int)(ek & 255u), &sx, &sy, &sz);
         const double4 xk = d.xs[k];
-        double dk64[3];
-        disp64(g, xk, xj, sx, sy, sz, dk64[0], dk64[1], dk64[2]);
-        const double r64 = __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(dk64[0], dk64[0]),
-                                                          __dmul_rn(dk64[1], dk64[1])),
-                                                __dmul_rn(dk64[2], dk64[2])));
-        const R djk[3] = {(R)dk64[0], (R)dk64[1], (R)dk64[2]};
-        const R r_jk = (R)r64;
-        R theta, cos_theta, di[3], djv[3], dk[3];
-        theta_dcos<R, false>(dij, r_ij, djk, r_jk, theta, cos_theta, di, djv, dk);
+        double djk[3];
+        disp64(g, xk, xj, sx, sy, sz, djk[0], djk[1], djk[2]);
+        const double sqr_d_jk = fma(djk[0], djk[0], fma(djk[1], djk[1], djk[2] * djk[2]));
+        const double inv_rjk = rsqrt(sqr_d_jk);
+        const double r_jk = sqr_d_jk * inv_rjk;
+        // the angle and d(cos theta) (theta_dcos with the reciprocals)
+        const double dot = dij[0] * djk[0] + dij[1] * djk[1] + dij[2] * djk[2];
+        const double inv_dists = inv_rij * inv_rjk;
+        double cos_theta = dot * inv_dists;
+        if (cos_theta > 1.0) cos_theta = 1.0;
+        if (cos_theta < -1.0) cos_theta = -1.0;
+        const double Cdot_inv3 = dot * inv_dists * inv_dists * inv_dists;
+        double di[3], djv[3], dk[3];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+          di[c] = djk[c] * inv_dists - Cdot_inv3 * sqr_d_jk * dij[c];
+          djv[c] = -(djk[c] + dij[c]) * inv_dists + Cdot_inv3 * (sqr_d_jk * dij[c] + sqr_d_ji * djk[c]);
+          dk[c] = dij[c] * inv_dists - Cdot_inv3 * sqr_d_ji * djk[c];
+        }
         // sin^4(theta/2) = ((1 - cos theta) / 2)^2: the reference's
         // sin(acos(c) / 2) without the two transcendentals
-        R sin_xhz4 = (R(1) - cos_theta) / R(2);
-        sin_xhz4 *= sin_xhz4;
-        const R cos_xhz1 = R(1) - cos_theta;
-        const R p_hb1 = (R)hbp.p_hb1, p_hb2 = (R)hbp.p_hb2, p_hb3 = (R)hbp.p_hb3;
-        const R r0_hb = (R)hbp.r0_hb;
-        const R exp_hb2 = exp(-p_hb2 * BO);
-        const R exp_hb3 = exp(-p_hb3 * (r0_hb / r_jk + r_jk / r0_hb - R(2)));
-        const R e_hb = p_hb1 * (R(1) - exp_hb2) * exp_hb3 * sin_xhz4;
-        ehb += (double)e_hb;
-        const R CEhb1 = p_hb1 * p_hb2 * exp_hb2 * exp_hb3 * sin_xhz4;
-        const R CEhb2 = -p_hb1 / R(2) * (R(1) - exp_hb2) * exp_hb3 * cos_xhz1;
-        const R CEhb3 = -p_hb3 * (-r0_hb / sqr(r_jk) + R(1) / r0_hb) * e_hb;
-        cdbo += (double)CEhb1;
-        fix += (double)(CEhb2 * di[0]); fiy += (double)(CEhb2 * di[1]); fiz += (double)(CEhb2 * di[2]);
-        const R c3 = CEhb3 / r_jk;
-        fjx += (double)(CEhb2 * djv[0] - c3 * djk[0]);
-        fjy += (double)(CEhb2 * djv[1] - c3 * djk[1]);
-        fjz += (double)(CEhb2 * djv[2] - c3 * djk[2]);
-        add3(fC, n, k, 1.0, (double)(CEhb2 * dk[0] + c3 * djk[0]), (double)(CEhb2 * dk[1] + c3 * djk[1]),
-             (double)(CEhb2 * dk[2] + c3 * djk[2]));
-        if (VIR)
-          vir_acc(w, dk64[0], dk64[1], dk64[2], (double)(CEhb2 * dk[0] + c3 * djk[0]),
-                  (double)(CEhb2 * dk[1] + c3 * djk[1]), (double)(CEhb2 * dk[2] + c3 * djk[2]));
+        const double cos_xhz1 = 1.0 - cos_theta;
+        const double sin_xhz4 = 0.25 * cos_xhz1 * cos_xhz1;
+        const double p_hb1 = hbp.p_hb1, p_hb2 = hbp.p_hb2, p_hb3 = hbp.p_hb3;
+        const double r0_hb = hbp.r0_hb, inv_r0 = hbp.inv_r0_hb;
+        const double exp_hb3 = exp(-p_hb3 * (r0_hb * inv_rjk + r_jk * inv_r0 - 2.0));
+        const double e_hb = p_hb1 * (1.0 - exp_hb2) * exp_hb3 * sin_xhz4;
+        ehb += e_hb;
+        const double CEhb1 = p_hb1 * p_hb2 * exp_hb2 * exp_hb3 * sin_xhz4;
+        const double CEhb2 = -0.5 * p_hb1 * (1.0 - exp_hb2) * exp_hb3 * cos_xhz1;
+        const double CEhb3 = -p_hb3 * (inv_r0 - r0_hb * inv_rjk * inv_rjk) * e_hb;
+        cdbo += CEhb1;
+        fix += CEhb2 * di[0]; fiy += CEhb2 * di[1]; fiz += CEhb2 * di[2];
+        const double c3 = CEhb3 * inv_rjk;
+        fjx += CEhb2 * djv[0] - c3 * djk[0];
+        fjy += CEhb2 * djv[1] - c3 * djk[1];
+        fjz += CEhb2 * djv[2] - c3 * djk[2];
+        const double fk[3] = {CEhb2 * dk[0] + c3 * djk[0], CEhb2 * dk[1] + c3 * djk[1],
+                              CEhb2 * dk[2] + c3 * djk[2]};
+        add3(fC, n, k, 1.0, fk[0], fk[1], fk[2]);
+        if (VIR) vir_acc(w, djk[0], djk[1], djk[2], fk[0], fk[1], fk[2]);
       }
       if (VIR) vir_acc(w, d.b_dx[s], d.b_dy[s], d.b_dz[s], fix, fiy, fiz);
       cdbo = warp_sum_d(cdbo);
@@ -572,16 +604,17 @@ __global__ void __launch_bounds__(256) k_hbonds32(Dev d, int eflag) {
 // Calculate_Omega, reaxc_torsion_angles_sw64.c:21-102
 template <typename R>
 struct Thb {
-  R theta, di[3], dj[3], dk[3];
+  R theta, sin, cos, di[3], dj[3], dk[3];
 };
 
+// the dihedral's derivative vectors; returns the unnormalised cosine and
+// sine of omega (omega = atan2(us, uc)); the two angles' sines and cosines
+// come with p_ijk and p_jkl
 template <typename R>
-__device__ R calc_omega(const R *dvec_ij, R r_ij, const R *dvec_jk, R r_jk, const R *dvec_kl, R r_kl,
-                        const R *dvec_li, R r_li, const Thb<R> &p_ijk, const Thb<R> &p_jkl, R *doi,
-                        R *doj, R *dok, R *dol) {
-  R sin_ijk, cos_ijk, sin_jkl, cos_jkl;
-  sincos(p_ijk.theta, &sin_ijk, &cos_ijk);
-  sincos(p_jkl.theta, &sin_jkl, &cos_jkl);
+__device__ void calc_omega(const R *dvec_ij, R r_ij, const R *dvec_jk, R r_jk, const R *dvec_kl,
+                           R r_kl, const R *dvec_li, R r_li, const Thb<R> &p_ijk,
+                           const Thb<R> &p_jkl, R *doi, R *doj, R *dok, R *dol, R &uc, R &us) {
+  R sin_ijk = p_ijk.sin, cos_ijk = p_ijk.cos, sin_jkl = p_jkl.sin, cos_jkl = p_jkl.cos;
   const R dij_jk = dvec_ij[0] * dvec_jk[0] + dvec_ij[1] * dvec_jk[1] + dvec_ij[2] * dvec_jk[2];
   const R djk_kl = dvec_jk[0] * dvec_kl[0] + dvec_jk[1] * dvec_kl[1] + dvec_jk[2] * dvec_kl[2];
   const R dij_kl = dvec_ij[0] * dvec_kl[0] + dvec_ij[1] * dvec_kl[1] + dvec_ij[2] * dvec_kl[2];
@@ -590,7 +623,8 @@ __device__ R calc_omega(const R *dvec_ij, R r_ij, const R *dvec_jk, R r_jk, cons
   const R cr1 = dvec_jk[2] * dvec_kl[0] - dvec_jk[0] * dvec_kl[2];
   const R cr2 = dvec_jk[0] * dvec_kl[1] - dvec_jk[1] * dvec_kl[0];
   const R unnorm_sin_omega = -r_jk * (dvec_ij[0] * cr0 + dvec_ij[1] * cr1 + dvec_ij[2] * cr2);
-  const R omega = atan2(unnorm_sin_omega, unnorm_cos_omega);
+  uc = unnorm_cos_omega;
+  us = unnorm_sin_omega;
   const R htra = r_ij + cos_ijk * (r_kl * cos_jkl - r_jk);
   const R htrb = r_jk - r_ij * cos_ijk - r_kl * cos_jkl;
   const R htrc = r_kl + cos_jkl * (r_ij * cos_ijk - r_jk);
@@ -623,7 +657,6 @@ __device__ R calc_omega(const R *dvec_ij, R r_ij, const R *dvec_jk, R r_jk, cons
     dok[t] = p2 * (-a4 * dvec_kl[t] + a5 * dvec_jk[t] - a2 * p_ijk.di[t] - a3 * p_jkl.dj[t]);
     dol[t] = p2 * (a4 * dvec_kl[t] + dvec_li[t] - a3 * p_jkl.dk[t]);
   }
-  return omega;
 }
 
 // ------------------------------------------------------------------
@@ -676,19 +709,33 @@ __global__ void k_vt_prep_center(Dev d) {
   d.c_sbo[2 * n + j] = dSBO1;
   d.c_sbo[3 * n + j] = dSBO2;
   d.c_sbo[4 * n + j] = exp(p_val6 * Delta_j);
+  // the FP64 angles' per-centre exponentials (penalty, coalition, theta_0;
+  // the mixed form's FP64 fallback angles read them too)
+  d.c_sbo[5 * n + j] = exp(-F.gp[20] * d.Delta[j]);
+  d.c_sbo[6 * n + j] = exp(F.gp[21] * d.Delta[j]);
+  d.c_sbo[7 * n + j] = exp(F.gp[2] * d.Delta_val[j]);
+  d.c_sbo[8 * n + j] = exp(-F.gp[17] * (2.0 - SBO2));
 }
 
 // per bond slot: exp(-p_tor2 BOA), exp(-p_cot2 (BOA - 1.5)^2)
-__global__ void k_vt_prep_bond(Dev d) {
+__device__ __forceinline__ void vt_prep_bond_item(const Dev &d, int i, int k) {
   const int n = d.n;
-  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  const int i = (int)(t % n), k = (int)(t / n);
-  if (k >= d.bond_cap || i >= n || k >= d.nbonds[i]) return;
   const long long s = (long long)k * n + i;
   const double BO = d.b_BO[s], BOA = BO - d.ctl->thb_cut;
   d.b_et2[s] = exp(-d.ff->gp[23] * BOA);
   d.b_ec2[s] = exp(-d.ff->gp[27] * sqr(BOA - 1.5));
   d.b_BOf[s] = BO > d.ctl->thb_cut ? (float)BO : 0.f;
+  // the FP64 angles' per-bond exponentials (penalty and coalition)
+  const long long S = (long long)d.bond_cap * n;
+  d.b_vexp[s] = exp(-d.ff->gp[19] * sqr(BOA - 2.0));
+  d.b_vexp[S + s] = exp(-d.ff->gp[38] * sqr(d.bo0[nbr_of(d.b_nbr[s])] - BOA));
+  d.b_vexp[2 * S + s] = exp(-d.ff->gp[30] * sqr(BOA - 1.5));
+}
+
+__global__ void __launch_bounds__(256) k_vt_prep_bond(Dev d) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int cnt = i < d.n ? min(d.nbonds[i], d.bond_cap) : 0;
+  warp_items(cnt, i, [&](int a, int k) { vt_prep_bond_item(d, a, k); });
 }
 
 __device__ __forceinline__ bool fbp_nonzero(const Fbp &p) {
@@ -819,30 +866,47 @@ __device__ __forceinline__ void valence_item(const Dev &d, unsigned long long it
     const R BOA_jk = (R)(d.b_BO[spk] - thb_cut), BOA_hj = (R)(d.b_BO[sph] - thb_cut);
     const R djk[3] = {(R)d.b_dx[spk], (R)d.b_dy[spk], (R)d.b_dz[spk]};
     const R dhj[3] = {(R)d.b_dx[sph], (R)d.b_dy[sph], (R)d.b_dz[sph]};
+    constexpr bool F64 = std::is_same<R, double>::value;
     R theta_hjk, cos_theta_hjk, di[3], dj[3], dk[3];
     theta_dcos<R>(djk, (R)d.b_d[spk], dhj, (R)d.b_d[sph], theta_hjk, cos_theta_hjk, di, dj, dk);
-    R sin_theta_hjk = sin(theta_hjk);
+    // sin(acos c) = sqrt((1 - c)(1 + c)) in FP64 (no sine evaluation)
+    R sin_theta_hjk = F64 ? sqrt((R(1) - cos_theta_hjk) * (R(1) + cos_theta_hjk)) : sin(theta_hjk);
     if (sin_theta_hjk < R(1.0e-5)) sin_theta_hjk = R(1.0e-5);
     const Thbh &thbh = F.thbp[tk][tj][th];
     const R Dj = (R)d.Delta[j], Dval_j = (R)d.Delta_val[j];
     const R bo0k = (R)d.bo0[k], bo0h = (R)d.bo0[h];
+    // FP64: BOA^p_val4 from one logarithm per bond order and angle, and the
+    // per-centre and per-bond exponentials of k_vt_prep_center/_bond
+    const long long S = (long long)d.bond_cap * n;
+    const R Ljk = F64 ? log(BOA_jk) : R(0), Lhj = F64 ? log(BOA_hj) : R(0);
+    const R iBjk = F64 ? R(1) / BOA_jk : R(0), iBhj = F64 ? R(1) / BOA_hj : R(0);
     for (int cnt = 0; cnt < thbh.cnt; ++cnt) {
       const Thbp &tp = thbh.prm[cnt];
       if (!(fabs(tp.p_val1) > 0.001)) continue;
       const R p_val1 = (R)tp.p_val1, p_val2 = (R)tp.p_val2, p_val4 = (R)tp.p_val4, p_val7 = (R)tp.p_val7;
       const R theta_00 = (R)tp.theta_00;
-      const R exp3jk = exp(-p_val3 * pow(BOA_jk, p_val4));
+      R exp3jk, Cf7jk, exp3hj, Cf7hj;
+      if (F64) {
+        const R pjk = exp(p_val4 * Ljk), phj = exp(p_val4 * Lhj);
+        exp3jk = exp(-p_val3 * pjk);
+        Cf7jk = p_val3 * p_val4 * (pjk * iBjk) * exp3jk;
+        exp3hj = exp(-p_val3 * phj);
+        Cf7hj = p_val3 * p_val4 * (phj * iBhj) * exp3hj;
+      } else {
+        exp3jk = exp(-p_val3 * pow(BOA_jk, p_val4));
+        Cf7jk = p_val3 * p_val4 * pow(BOA_jk, p_val4 - R(1)) * exp3jk;
+        exp3hj = exp(-p_val3 * pow(BOA_hj, p_val4));
+        Cf7hj = p_val3 * p_val4 * pow(BOA_hj, p_val4 - R(1)) * exp3hj;
+      }
       const R f7_jk = R(1) - exp3jk;
-      const R Cf7jk = p_val3 * p_val4 * pow(BOA_jk, p_val4 - R(1)) * exp3jk;
-      const R exp3hj = exp(-p_val3 * pow(BOA_hj, p_val4));
       const R f7_hj = R(1) - exp3hj;
-      const R Cf7hj = p_val3 * p_val4 * pow(BOA_hj, p_val4 - R(1)) * exp3hj;
       const R expval7 = exp(-p_val7 * Delta_j);
       const R trm8 = R(1) + expval6 + expval7;
       const R f8_Dj = p_val5 - ((p_val5 - R(1)) * (R(2) + expval6) / trm8);
       const R Cf8j = ((R(1) - p_val5) / sqr(trm8)) *
                      (p_val6 * expval6 * trm8 - (R(2) + expval6) * (p_val6 * expval6 - p_val7 * expval7));
-      R theta_0 = R(180) - theta_00 * (R(1) - exp(-p_val10 * (R(2) - SBO2)));
+      const R exp_val10 = F64 ? (R)d.c_sbo[8 * n + j] : exp(-p_val10 * (R(2) - SBO2));
+      R theta_0 = R(180) - theta_00 * (R(1) - exp_val10);
       theta_0 = deg2rad(theta_0);
       const R expval2theta = exp(-p_val2 * sqr(theta_0 - theta_hjk));
       const R expval12theta = (p_val1 >= R(0)) ? p_val1 * (R(1) - expval2theta) : p_val1 * -expval2theta;
@@ -850,16 +914,16 @@ __device__ __forceinline__ void valence_item(const Dev &d, unsigned long long it
       const R CEval2 = Cf7hj * f7_jk * f8_Dj * expval12theta;
       const R CEval3 = Cf8j * f7_hj * f7_jk * expval12theta;
       const R CEval4 = R(-2) * p_val1 * p_val2 * f7_jk * f7_hj * f8_Dj * expval2theta * (theta_0 - theta_hjk);
-      const R Ctheta_0 = p_val10 * deg2rad(theta_00) * exp(-p_val10 * (R(2) - SBO2));
+      const R Ctheta_0 = p_val10 * deg2rad(theta_00) * exp_val10;
       const R CEval5 = -CEval4 * Ctheta_0 * CSBO2;
       const R CEval6 = CEval5 * dSBO1;
       const R CEval7 = CEval5 * dSBO2;
       const R CEval8 = -CEval4 / sin_theta_hjk;
       e_ang += (double)(f7_jk * f7_hj * f8_Dj * expval12theta);
-      const R exp_pen2jk = exp(-p_pen2 * sqr(BOA_jk - R(2)));
-      const R exp_pen2hj = exp(-p_pen2 * sqr(BOA_hj - R(2)));
-      const R exp_pen3 = exp(-p_pen3 * Dj);
-      const R exp_pen4 = exp(p_pen4 * Dj);
+      const R exp_pen2jk = F64 ? (R)d.b_vexp[spk] : exp(-p_pen2 * sqr(BOA_jk - R(2)));
+      const R exp_pen2hj = F64 ? (R)d.b_vexp[sph] : exp(-p_pen2 * sqr(BOA_hj - R(2)));
+      const R exp_pen3 = F64 ? (R)d.c_sbo[5 * n + j] : exp(-p_pen3 * Dj);
+      const R exp_pen4 = F64 ? (R)d.c_sbo[6 * n + j] : exp(p_pen4 * Dj);
       const R trm_pen34 = R(1) + exp_pen3 + exp_pen4;
       const R f9_Dj = (R(2) + exp_pen3) / trm_pen34;
       const R Cf9j = (-p_pen3 * exp_pen3 * trm_pen34 -
@@ -870,10 +934,13 @@ __device__ __forceinline__ void valence_item(const Dev &d, unsigned long long it
       const R temp = R(-2) * p_pen2 * epen;
       const R CEpen2 = temp * (BOA_jk - R(2));
       const R CEpen3 = temp * (BOA_hj - R(2));
-      const R exp_coa2 = exp(p_coa2 * Dval_j);
-      const R ecoa = (R)tp.p_coa1 / (R(1) + exp_coa2) * exp(-p_coa3 * sqr(bo0k - BOA_jk)) *
-                     exp(-p_coa3 * sqr(bo0h - BOA_hj)) * exp(-p_coa4 * sqr(BOA_jk - R(1.5))) *
-                     exp(-p_coa4 * sqr(BOA_hj - R(1.5)));
+      const R exp_coa2 = F64 ? (R)d.c_sbo[7 * n + j] : exp(p_coa2 * Dval_j);
+      const R ecoa =
+          F64 ? (R)tp.p_coa1 / (R(1) + exp_coa2) * (R)d.b_vexp[S + spk] * (R)d.b_vexp[S + sph] *
+                    (R)d.b_vexp[2 * S + spk] * (R)d.b_vexp[2 * S + sph]
+              : (R)tp.p_coa1 / (R(1) + exp_coa2) * exp(-p_coa3 * sqr(bo0k - BOA_jk)) *
+                    exp(-p_coa3 * sqr(bo0h - BOA_hj)) * exp(-p_coa4 * sqr(BOA_jk - R(1.5))) *
+                    exp(-p_coa4 * sqr(BOA_hj - R(1.5)));
       e_coa += (double)ecoa;
       const R CEcoa1 = R(-2) * p_coa4 * (BOA_jk - R(1.5)) * ecoa;
       const R CEcoa2 = R(-2) * p_coa4 * (BOA_hj - R(1.5)) * ecoa;
@@ -1018,17 +1085,27 @@ __device__ __forceinline__ void torsion_item(const Dev &d, unsigned long long it
     const R dkl[3] = {(R)d.b_dx[spw], (R)d.b_dy[spw], (R)d.b_dz[spw]};
     const R dpj[3] = {(R)d.b_dx[spj], (R)d.b_dy[spj], (R)d.b_dz[spj]};
     const R r_jk = (R)d.b_d[spk], r_ij = (R)d.b_d[sph], r_kl = (R)d.b_d[spw];
+    // FP64: the angles' sines from their cosines, sqrt((1 - c)(1 + c)) =
+    // sin(acos c), and omega's cosines from its two components (no acos,
+    // sincos, atan2 or cos evaluation); FP32: the reference's sequence
+    constexpr bool F64 = std::is_same<R, double>::value;
     Thb<R> p_ijk, p_jkl;
-    R cth;
-    theta_dcos<R>(djk, r_jk, dhj, r_ij, p_ijk.theta, cth, p_ijk.di, p_ijk.dj, p_ijk.dk);
-    theta_dcos<R>(dpj, (R)d.b_d[spj], dkl, r_kl, p_jkl.theta, cth, p_jkl.di, p_jkl.dj, p_jkl.dk);
+    theta_dcos<R, !F64>(djk, r_jk, dhj, r_ij, p_ijk.theta, p_ijk.cos, p_ijk.di, p_ijk.dj, p_ijk.dk);
+    theta_dcos<R, !F64>(dpj, (R)d.b_d[spj], dkl, r_kl, p_jkl.theta, p_jkl.cos, p_jkl.di, p_jkl.dj,
+                        p_jkl.dk);
+    if (F64) {
+      p_ijk.sin = sqrt((R(1) - p_ijk.cos) * (R(1) + p_ijk.cos));
+      p_jkl.sin = sqrt((R(1) - p_jkl.cos) * (R(1) + p_jkl.cos));
+    } else {
+      sincos(p_ijk.theta, &p_ijk.sin, &p_ijk.cos);
+      sincos(p_jkl.theta, &p_jkl.sin, &p_jkl.cos);
+    }
     const R ms = (R)MIN_SINE;
-    R sin_ijk, cos_ijk, tan_ijk_i, sin_jkl, cos_jkl, tan_jkl_i;
-    sincos(p_ijk.theta, &sin_ijk, &cos_ijk);
+    R tan_ijk_i, tan_jkl_i;
+    const R sin_ijk = p_ijk.sin, cos_ijk = p_ijk.cos, sin_jkl = p_jkl.sin, cos_jkl = p_jkl.cos;
     if (sin_ijk >= R(0) && sin_ijk <= ms) tan_ijk_i = cos_ijk / ms;
     else if (sin_ijk <= R(0) && sin_ijk >= -ms) tan_ijk_i = cos_ijk / -ms;
     else tan_ijk_i = cos_ijk / sin_ijk;
-    sincos(p_jkl.theta, &sin_jkl, &cos_jkl);
     if (sin_jkl >= R(0) && sin_jkl <= ms) tan_jkl_i = cos_jkl / ms;
     else if (sin_jkl <= R(0) && sin_jkl >= -ms) tan_jkl_i = cos_jkl / -ms;
     else tan_jkl_i = cos_jkl / sin_jkl;
@@ -1038,11 +1115,21 @@ __device__ __forceinline__ void torsion_item(const Dev &d, unsigned long long it
     dli[2] = dhj[2] - djk[2] - dkl[2];
     const R r_li = sqrt(sqr(dli[0]) + sqr(dli[1]) + sqr(dli[2]));
     R doi[3], doj[3], dok[3], dol[3];
-    const R omega = calc_omega<R>(dhj, r_ij, djk, r_jk, dkl, r_kl, dli, r_li, p_ijk, p_jkl,
-                                  doi, doj, dok, dol);
-    const R cos_omega = cos(omega);
-    const R cos2omega = cos(R(2) * omega);
-    const R cos3omega = cos(R(3) * omega);
+    R uc, us;
+    calc_omega<R>(dhj, r_ij, djk, r_jk, dkl, r_kl, dli, r_li, p_ijk, p_jkl, doi, doj, dok, dol, uc,
+                  us);
+    R cos_omega, cos2omega, cos3omega;
+    if (F64) {
+      const R hyp = sqrt(uc * uc + us * us);
+      cos_omega = hyp > R(0) ? uc / hyp : R(1);   // atan2(0, 0) = 0
+      cos2omega = R(2) * cos_omega * cos_omega - R(1);
+      cos3omega = cos_omega * (R(4) * cos_omega * cos_omega - R(3));
+    } else {
+      const R omega = atan2(us, uc);
+      cos_omega = cos(omega);
+      cos2omega = cos(R(2) * omega);
+      cos3omega = cos(R(3) * omega);
+    }
     const R BOpi_jk = (R)d.b_BOpi[spk];
     const R exp_tor1 = exp(p_tor1 * sqr(R(2) - BOpi_jk - f11_DjDk));
     const R fn10 = (R(1) - exp_tor2_ij) * (R(1) - exp_tor2_jk) * (R(1) - exp_tor2_kl);
@@ -1091,8 +1178,8 @@ __device__ __forceinline__ void torsion_item(const Dev &d, unsigned long long it
     atomicAdd(&d.b_Cdbo[spw], (double)(CEtors6 + CEconj3));
     const R c78 = CEtors7 + CEconj4, c85 = CEtors8 + CEconj5, c96 = CEtors9 + CEconj6;
     if (d.debug) {
-      const double v[] = {BOA_ij, BOA_jk, BOA_kl, p_ijk.theta, p_jkl.theta, sin_ijk, sin_jkl,
-                          tan_ijk_i, tan_jkl_i, omega, r_li, exp_tor1, fn10, CV, c78, c85, c96,
+      const double v[] = {BOA_ij, BOA_jk, BOA_kl, cos_ijk, cos_jkl, sin_ijk, sin_jkl,
+                          tan_ijk_i, tan_jkl_i, cos_omega, r_li, exp_tor1, fn10, CV, c78, c85, c96,
                           CEtors2, CEtors3, CEtors4, CEtors5, CEtors6, doi[0], doj[0], dok[0],
                           dol[0], f11_DjDk, dfn11, Delta_j, Delta_k};
       double sum = 0.0;
@@ -1296,8 +1383,7 @@ void launch_check_finite(const double *a, long long count, int *flag, cudaStream
 void launch_bond_orders(const Dev &d, cudaStream_t st) {
   const int B = 256;
   k_bo_deltap<<<(d.n + B - 1) / B, B, 0, st>>>(d);
-  const long long slots = (long long)d.n * d.bond_cap;
-  k_bo_correct<<<(unsigned)((slots + B - 1) / B), B, 0, st>>>(d);
+  k_bo_correct<<<(unsigned)((d.n + 255) / 256), 256, 0, st>>>(d);
   k_bo_atom<<<(d.n + B - 1) / B, B, 0, st>>>(d);
 }
 
@@ -1310,10 +1396,10 @@ void launch_hbonds(const Dev &d, cudaStream_t st, int eflag) {
   const unsigned G = (unsigned)((threads + 255) / 256);
   if (d.vflag) {
     if (d.mixed) k_hbonds32<true><<<G, 256, 0, st>>>(d, eflag);
-    else k_hbonds<double, true><<<G, 256, 0, st>>>(d, eflag);
+    else k_hbonds<true><<<G, 256, 0, st>>>(d, eflag);
   } else {
     if (d.mixed) k_hbonds32<false><<<G, 256, 0, st>>>(d, eflag);
-    else k_hbonds<double, false><<<G, 256, 0, st>>>(d, eflag);
+    else k_hbonds<false><<<G, 256, 0, st>>>(d, eflag);
   }
 }
 
@@ -1321,7 +1407,7 @@ void launch_vt_count(const Dev &d, cudaStream_t st) {
   const int B = 256;
   const long long slots = (long long)d.n * d.bond_cap;
   k_vt_prep_center<<<(d.n + B - 1) / B, B, 0, st>>>(d);
-  k_vt_prep_bond<<<(unsigned)((slots + B - 1) / B), B, 0, st>>>(d);
+  k_vt_prep_bond<<<(unsigned)((d.n + 255) / 256), 256, 0, st>>>(d);
   k_vt_count<<<(unsigned)((slots + 1 + B - 1) / B), B, 0, st>>>(d);
   launch_scan(d.w_cnt_v, d.w_off_v, (int)(slots + 1), d.w_bsum, st);
   launch_scan(d.w_cnt_t, d.w_off_t, (int)(slots + 1), d.w_bsum, st);

@@ -222,6 +222,7 @@ std::string rg_read_ffield(const char *path, int lgflag, ForceField *ff) {
       if (j < 0 || k < 0 || m < 0 || j >= nt || k >= nt || m >= nt) continue;
       Hbp &h = ff->hbp[j][k][m];
       h.r0_hb = r.d(3); h.p_hb1 = r.d(4); h.p_hb2 = r.d(5); h.p_hb3 = r.d(6);
+      h.inv_r0_hb = h.r0_hb > 0.0 ? 1.0 / h.r0_hb : 0.0;
     }
   }
   const double p_vdW1 = ff->gp[28];

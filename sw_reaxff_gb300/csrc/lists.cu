@@ -512,12 +512,8 @@ __device__ __forceinline__ void bo_prime64(const Control &C, int ti, int tj, con
 // |p_bo1 p_bo2 (d/r)^p_bo2| (up to ~10 for C-C and C-N bonds), and in FP32
 // that left the mixed form's forces on the TATB crystal 1.7e-4 (relative
 // RMS) from the FP64 forces, against 1e-5 with FP64 BO'.
-__global__ void k_bond_prime(Dev d) {
+__device__ __forceinline__ void bond_prime_item(const Dev &d, int i, int k) {
   const int n = d.n;
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  const int k = blockIdx.y;
-  if (i >= n) return;
-  if (k >= min(d.nbonds[i], d.bond_cap)) return;
   const Control &C = *d.ctl;
   const ForceField &F = *d.ff;
   const long long s = (long long)k * n + i;
@@ -560,6 +556,13 @@ __global__ void k_bond_prime(Dev d) {
   d.b_dlnpi[s] = api * dx; d.b_dlnpi[S3 + s] = api * dy; d.b_dlnpi[2 * S3 + s] = api * dz;
   d.b_dlnpi2[s] = api2 * dx; d.b_dlnpi2[S3 + s] = api2 * dy; d.b_dlnpi2[2 * S3 + s] = api2 * dz;
   d.b_Cdbo[s] = 0.0; d.b_Cdbopi[s] = 0.0; d.b_Cdbopi2[s] = 0.0;
+}
+
+// one warp per 32 atoms over all their candidates (warp_items)
+__global__ void __launch_bounds__(256) k_bond_prime(Dev d) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int cnt = i < d.n ? min(d.nbonds[i], d.bond_cap) : 0;
+  warp_items(cnt, i, [&](int a, int k) { bond_prime_item(d, a, k); });
 }
 
 // per atom: drop rejected candidates (keeping the order of the rest), then
@@ -788,8 +791,7 @@ void launch_build_bonds(const Dev &d, cudaStream_t st) {
   const unsigned G = (unsigned)((threads + NB_WARPS * 32 - 1) / (NB_WARPS * 32));
   if (d.mixed) k_build_bonds<true><<<G, NB_WARPS * 32, 0, st>>>(d);
   else k_build_bonds<false><<<G, NB_WARPS * 32, 0, st>>>(d);
-  const dim3 gp((unsigned)((d.n + 127) / 128), (unsigned)d.bond_cap);
-  k_bond_prime<<<gp, 128, 0, st>>>(d);
+  k_bond_prime<<<(unsigned)((d.n + 255) / 256), 256, 0, st>>>(d);
   k_bond_finish<<<(d.n + 255) / 256, 256, 0, st>>>(d);
   const long long slots = (long long)d.n * d.bond_cap;
   k_bond_sym<<<(unsigned)((slots + 255) / 256), 256, 0, st>>>(d);

@@ -294,6 +294,7 @@ int alloc_bonds(rg_system *h) {
   r |= dalloc(h, h->per_b, &d.b_Cdbopi2, S);
   r |= dalloc(h, h->per_b, &d.b_et2, S);
   r |= dalloc(h, h->per_b, &d.b_ec2, S);
+  r |= dalloc(h, h->per_b, &d.b_vexp, 3 * S);
   r |= dalloc(h, h->per_b, &d.b_BOf, S);
   r |= dalloc(h, h->per_b, &d.w_cnt_v, S + 1);
   r |= dalloc(h, h->per_b, &d.w_cnt_t, S + 1);
@@ -384,7 +385,7 @@ int alloc_atoms(rg_system *h, int n) {
   r |= dalloc(h, B, &d.fC, 4 * (size_t)n);
   r |= dalloc(h, B, &d.vsum, 2 * (size_t)n);
   r |= dalloc(h, B, &d.exp_boc, 2 * (size_t)n);
-  r |= dalloc(h, B, &d.c_sbo, 5 * (size_t)n);
+  r |= dalloc(h, B, &d.c_sbo, 9 * (size_t)n);
   double2 **pv[] = {&d.qx, &d.qb, &d.qr, &d.qu, &d.qw, &d.qd, &d.qq, &d.qp, &d.qs, &d.qv, &d.qz, &d.qm};
   for (double2 **q : pv) r |= dalloc(h, B, q, (size_t)n);
   if (d.mixed) r |= dalloc(h, B, &d.qd32, (size_t)n);
@@ -689,7 +690,7 @@ int do_qeq(rg_system *h, int *its, int *itt) {
     if (!d.mixed || refines >= RG_MAX_REFINE) break;
     // residual with FP64 sums; the CG set-up for a restart only where it
     // is above the tolerance
-    { Scope sc(h, PH_QSETUP, 5); launch_qeq_refine_check(d, h->st, tol); }
+    { Scope sc(h, PH_QSETUP, 6); launch_qeq_refine_check(d, h->st, tol); }
     ++refines;
     CK(cudaMemcpyAsync(&active, d.n_active, sizeof(int), cudaMemcpyDeviceToHost, h->st));
     CK(cudaStreamSynchronize(h->st));

@@ -54,6 +54,7 @@ struct Fbh {
 };
 struct Hbp {
   double r0_hb, p_hb1, p_hb2, p_hb3;
+  double inv_r0_hb;   // 1 / r0_hb (derived at load)
 };
 
 // Whole force field, plain data, copied once to device memory.
@@ -235,8 +236,12 @@ struct Dev {
   int *n_active;      // QEq: segments with an active solve (host poll)
 
   // valence / torsion work lists (built per force step)
-  double *c_sbo;      // 5 * n: SBO2, CSBO2, dSBO1, dSBO2, expval6 per centre
+  double *c_sbo;      // 9 * n per centre: SBO2, CSBO2, dSBO1, dSBO2, expval6, and for
+                      // the FP64 angles exp(-p_pen3 Delta), exp(p_pen4 Delta),
+                      // exp(p_coa2 Delta_val), exp(-p_val10 (2 - SBO2))
   double *b_et2, *b_ec2;   // per bond slot: exp(-p_tor2 BOA), exp(-p_cot2 (BOA-1.5)^2)
+  double *b_vexp;     // 3 * slots (FP64 angles): exp(-p_pen2 (BOA-2)^2),
+                      // exp(-p_coa3 (bo0[nbr] - BOA)^2), exp(-p_coa4 (BOA-1.5)^2)
   float *b_BOf;             // per bond slot: BO in FP32, 0 where BO <= thb_cut (exact
                             // FP64 test), for the valence/torsion enumeration
   int *w_cnt_v, *w_cnt_t;  // per (centre, bond) slot counts (+1 trailing zero)
@@ -272,6 +277,36 @@ enum { OVF_NBR = 1, OVF_BOND = 2, OVF_HB = 4, OVF_CELL = 8 };
 #define RG_C3_QEQ (0.3333333333333 - 1.0 / 3.0)
 #define RG_C3_ELE (0.33333333333333 - 1.0 / 3.0)
 #ifdef __CUDACC__
+// Per-atom item lists (bond slots, bond candidates) of the 32 atoms of a
+// warp, taken 32 items at a time: lane l brings cnt items of its atom i, and
+// f(i, c) runs for every item c < cnt of every lane's atom with the warp's
+// lanes on consecutive items, so a short list does not leave lanes idle.
+// Every lane of the warp must call it (cnt = 0 for lanes without an atom).
+template <typename Fn>
+__device__ __forceinline__ void warp_items(int cnt, int i, Fn f) {
+  const unsigned full = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+  int incl = cnt;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int v = __shfl_up_sync(full, incl, o);
+    if (lane >= o) incl += v;
+  }
+  const int total = __shfl_sync(full, incl, 31);
+  const int excl = incl - cnt;
+  for (int base = 0; base < total; base += 32) {
+    const int q = base + lane;
+    // the owner of item q: the first lane whose inclusive count exceeds q
+    int own = 0;
+#pragma unroll
+    for (int step = 16; step > 0; step >>= 1)
+      if (__shfl_sync(full, incl, own + step - 1) <= q) own += step;
+    const int oexcl = __shfl_sync(full, excl, own);
+    const int oi = __shfl_sync(full, i, own);
+    if (q < total) f(oi, q - oexcl);
+  }
+}
+
 // Adds v[0..K) of every thread of the block into dst[seg * stride + c],
 // c = 0..K-1; seg < 0 marks a thread without values.  One FP64 atomic per
 // value per block when the block's threads belong to one segment, per warp

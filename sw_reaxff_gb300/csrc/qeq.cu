@@ -197,23 +197,34 @@ __global__ void __launch_bounds__(256) k_spmv32(Dev d, const double2 *__restrict
   }
   float sh = 0.f, sl = 0.f, th = 0.f, tl = 0.f;
   if (on_s && on_t) {
-    // two entries per lane and step with separate compensated sums: two
-    // independent gathers of x in flight
+    // four entries per lane and step: their index and H loads, then their
+    // four gathers of x, are in flight together; two compensated sums per
+    // system
     float sh1 = 0.f, sl1 = 0.f, th1 = 0.f, tl1 = 0.f;
     int p = gl;
-    for (; p + RW < tot; p += 2 * RW) {
-      const int q = p + RW;
-      const int s0 = p < nn ? p : cap - 1 - (p - nn);
-      const int s1 = q < nn ? q : cap - 1 - (q - nn);
-      const uint32_t e0 = d.nbr[row + s0], e1 = d.nbr[row + s1];
-      const float h0 = d.hval32[row + s0], h1 = d.hval32[row + s1];
-      const float4 x0 = x32[e0 >> 8], x1 = x32[e1 >> 8];
-      df_fma(h0, x0.x, x0.y, sh, sl);
-      df_fma(h0, x0.z, x0.w, th, tl);
-      df_fma(h1, x1.x, x1.y, sh1, sl1);
-      df_fma(h1, x1.z, x1.w, th1, tl1);
+    for (; p + 3 * RW < tot; p += 4 * RW) {
+      uint32_t e4[4];
+      float h4[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const int q = p + u * RW;
+        const int s = q < nn ? q : cap - 1 - (q - nn);
+        e4[u] = d.nbr[row + s];
+        h4[u] = d.hval32[row + s];
+      }
+      float4 x4[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) x4[u] = x32[e4[u] >> 8];
+      df_fma(h4[0], x4[0].x, x4[0].y, sh, sl);
+      df_fma(h4[0], x4[0].z, x4[0].w, th, tl);
+      df_fma(h4[1], x4[1].x, x4[1].y, sh1, sl1);
+      df_fma(h4[1], x4[1].z, x4[1].w, th1, tl1);
+      df_fma(h4[2], x4[2].x, x4[2].y, sh, sl);
+      df_fma(h4[2], x4[2].z, x4[2].w, th, tl);
+      df_fma(h4[3], x4[3].x, x4[3].y, sh1, sl1);
+      df_fma(h4[3], x4[3].z, x4[3].w, th1, tl1);
     }
-    if (p < tot) {
+    for (; p < tot; p += RW) {
       const int slot = p < nn ? p : cap - 1 - (p - nn);
       const uint32_t e = d.nbr[row + slot];
       const float h = d.hval32[row + slot];

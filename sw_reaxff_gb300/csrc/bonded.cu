@@ -709,12 +709,15 @@ __global__ void k_vt_prep_center(Dev d) {
   d.c_sbo[2 * n + j] = dSBO1;
   d.c_sbo[3 * n + j] = dSBO2;
   d.c_sbo[4 * n + j] = exp(p_val6 * Delta_j);
-  // the FP64 angles' per-centre exponentials (penalty, coalition, theta_0;
-  // the mixed form's FP64 fallback angles read them too)
-  d.c_sbo[5 * n + j] = exp(-F.gp[20] * d.Delta[j]);
-  d.c_sbo[6 * n + j] = exp(F.gp[21] * d.Delta[j]);
-  d.c_sbo[7 * n + j] = exp(F.gp[2] * d.Delta_val[j]);
-  d.c_sbo[8 * n + j] = exp(-F.gp[17] * (2.0 - SBO2));
+  if (!d.mixed) {
+    // the FP64 form's per-centre exponentials of its angles (penalty,
+    // coalition, theta_0); the mixed form's few FP64 fallback angles
+    // evaluate them in place
+    d.c_sbo[5 * n + j] = exp(-F.gp[20] * d.Delta[j]);
+    d.c_sbo[6 * n + j] = exp(F.gp[21] * d.Delta[j]);
+    d.c_sbo[7 * n + j] = exp(F.gp[2] * d.Delta_val[j]);
+    d.c_sbo[8 * n + j] = exp(-F.gp[17] * (2.0 - SBO2));
+  }
 }
 
 // per bond slot: exp(-p_tor2 BOA), exp(-p_cot2 (BOA - 1.5)^2)
@@ -725,11 +728,14 @@ __device__ __forceinline__ void vt_prep_bond_item(const Dev &d, int i, int k) {
   d.b_et2[s] = exp(-d.ff->gp[23] * BOA);
   d.b_ec2[s] = exp(-d.ff->gp[27] * sqr(BOA - 1.5));
   d.b_BOf[s] = BO > d.ctl->thb_cut ? (float)BO : 0.f;
-  // the FP64 angles' per-bond exponentials (penalty and coalition)
-  const long long S = (long long)d.bond_cap * n;
-  d.b_vexp[s] = exp(-d.ff->gp[19] * sqr(BOA - 2.0));
-  d.b_vexp[S + s] = exp(-d.ff->gp[38] * sqr(d.bo0[nbr_of(d.b_nbr[s])] - BOA));
-  d.b_vexp[2 * S + s] = exp(-d.ff->gp[30] * sqr(BOA - 1.5));
+  if (!d.mixed) {
+    // the FP64 form's per-bond exponentials of its angles (penalty and
+    // coalition)
+    const long long S = (long long)d.bond_cap * n;
+    d.b_vexp[s] = exp(-d.ff->gp[19] * sqr(BOA - 2.0));
+    d.b_vexp[S + s] = exp(-d.ff->gp[38] * sqr(d.bo0[nbr_of(d.b_nbr[s])] - BOA));
+    d.b_vexp[2 * S + s] = exp(-d.ff->gp[30] * sqr(BOA - 1.5));
+  }
 }
 
 __global__ void __launch_bounds__(256) k_vt_prep_bond(Dev d) {
@@ -867,6 +873,8 @@ __device__ __forceinline__ void valence_item(const Dev &d, unsigned long long it
     const R djk[3] = {(R)d.b_dx[spk], (R)d.b_dy[spk], (R)d.b_dz[spk]};
     const R dhj[3] = {(R)d.b_dx[sph], (R)d.b_dy[sph], (R)d.b_dz[sph]};
     constexpr bool F64 = std::is_same<R, double>::value;
+    // the per-centre and per-bond exponentials exist in the FP64 form only
+    const bool pre = F64 && !d.mixed;
     R theta_hjk, cos_theta_hjk, di[3], dj[3], dk[3];
     theta_dcos<R>(djk, (R)d.b_d[spk], dhj, (R)d.b_d[sph], theta_hjk, cos_theta_hjk, di, dj, dk);
     // sin(acos c) = sqrt((1 - c)(1 + c)) in FP64 (no sine evaluation)
@@ -905,7 +913,7 @@ __device__ __forceinline__ void valence_item(const Dev &d, unsigned long long it
       const R f8_Dj = p_val5 - ((p_val5 - R(1)) * (R(2) + expval6) / trm8);
       const R Cf8j = ((R(1) - p_val5) / sqr(trm8)) *
                      (p_val6 * expval6 * trm8 - (R(2) + expval6) * (p_val6 * expval6 - p_val7 * expval7));
-      const R exp_val10 = F64 ? (R)d.c_sbo[8 * n + j] : exp(-p_val10 * (R(2) - SBO2));
+      const R exp_val10 = pre ? (R)d.c_sbo[8 * n + j] : exp(-p_val10 * (R(2) - SBO2));
       R theta_0 = R(180) - theta_00 * (R(1) - exp_val10);
       theta_0 = deg2rad(theta_0);
       const R expval2theta = exp(-p_val2 * sqr(theta_0 - theta_hjk));
@@ -920,10 +928,10 @@ __device__ __forceinline__ void valence_item(const Dev &d, unsigned long long it
       const R CEval7 = CEval5 * dSBO2;
       const R CEval8 = -CEval4 / sin_theta_hjk;
       e_ang += (double)(f7_jk * f7_hj * f8_Dj * expval12theta);
-      const R exp_pen2jk = F64 ? (R)d.b_vexp[spk] : exp(-p_pen2 * sqr(BOA_jk - R(2)));
-      const R exp_pen2hj = F64 ? (R)d.b_vexp[sph] : exp(-p_pen2 * sqr(BOA_hj - R(2)));
-      const R exp_pen3 = F64 ? (R)d.c_sbo[5 * n + j] : exp(-p_pen3 * Dj);
-      const R exp_pen4 = F64 ? (R)d.c_sbo[6 * n + j] : exp(p_pen4 * Dj);
+      const R exp_pen2jk = pre ? (R)d.b_vexp[spk] : exp(-p_pen2 * sqr(BOA_jk - R(2)));
+      const R exp_pen2hj = pre ? (R)d.b_vexp[sph] : exp(-p_pen2 * sqr(BOA_hj - R(2)));
+      const R exp_pen3 = pre ? (R)d.c_sbo[5 * n + j] : exp(-p_pen3 * Dj);
+      const R exp_pen4 = pre ? (R)d.c_sbo[6 * n + j] : exp(p_pen4 * Dj);
       const R trm_pen34 = R(1) + exp_pen3 + exp_pen4;
       const R f9_Dj = (R(2) + exp_pen3) / trm_pen34;
       const R Cf9j = (-p_pen3 * exp_pen3 * trm_pen34 -
@@ -934,9 +942,9 @@ __device__ __forceinline__ void valence_item(const Dev &d, unsigned long long it
       const R temp = R(-2) * p_pen2 * epen;
       const R CEpen2 = temp * (BOA_jk - R(2));
       const R CEpen3 = temp * (BOA_hj - R(2));
-      const R exp_coa2 = F64 ? (R)d.c_sbo[7 * n + j] : exp(p_coa2 * Dval_j);
+      const R exp_coa2 = pre ? (R)d.c_sbo[7 * n + j] : exp(p_coa2 * Dval_j);
       const R ecoa =
-          F64 ? (R)tp.p_coa1 / (R(1) + exp_coa2) * (R)d.b_vexp[S + spk] * (R)d.b_vexp[S + sph] *
+          pre ? (R)tp.p_coa1 / (R(1) + exp_coa2) * (R)d.b_vexp[S + spk] * (R)d.b_vexp[S + sph] *
                     (R)d.b_vexp[2 * S + spk] * (R)d.b_vexp[2 * S + sph]
               : (R)tp.p_coa1 / (R(1) + exp_coa2) * exp(-p_coa3 * sqr(bo0k - BOA_jk)) *
                     exp(-p_coa3 * sqr(bo0h - BOA_hj)) * exp(-p_coa4 * sqr(BOA_jk - R(1.5))) *

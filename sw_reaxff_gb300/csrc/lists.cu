@@ -370,7 +370,7 @@ __global__ void __launch_bounds__(NB_WARPS * 32) k_build_nbrs(Dev d) {
   // row's y-z distance are walked (FP32 geometry with the prefilter's
   // margin; the unwrapped cell indices give the periodic images' places).
   const bool clip = !g.tri;
-  const float wx = g.cellw_f[0], wy = g.cellw_f[1], wz = g.cellw_f[2];
+  const float wy = g.cellw_f[1], wz = g.cellw_f[2], iwx = 1.f / g.cellw_f[0];
   for (int oz = -S; oz <= S; ++oz) {
     int rz = cz + oz, sz = 0;
     while (rz < 0) { rz += ncz; --sz; }
@@ -394,8 +394,8 @@ __global__ void __launch_bounds__(NB_WARPS * 32) k_build_nbrs(Dev d) {
         if (r2 < 0.f) continue;
         const float rx_ = sqrtf(r2);
         // cells whose x-range meets [x_i - rx_, x_i + rx_]
-        ox_lo = max(ox_lo, (int)floorf((xif.x - rx_) / wx) - cx);
-        ox_hi = min(ox_hi, (int)floorf((xif.x + rx_) / wx) - cx);
+        ox_lo = max(ox_lo, (int)floorf((xif.x - rx_) * iwx) - cx);
+        ox_hi = min(ox_hi, (int)floorf((xif.x + rx_) * iwx) - cx);
       }
       const int rowcell = g.cell0 + (rz * ncy + ry) * nx;
       // runs of consecutive cells with one x image each
@@ -671,11 +671,14 @@ __global__ void __launch_bounds__(NB_WARPS * 32) k_build_bonds(Dev d) {
             ish = hb_rel && df <= hc;
           }
           if (df <= bc * (1.f + MARGIN32)) {
+            // with the hardware exp2/log2 (relative errors ~1e-6, against
+            // the factor 2 between bo_half and bo_cut)
             const Control::BoEst &be = C.bo_est[ti][tj];
+            const float lg = __log2f(df);
             float est = 0.f;
-            if (be.mask & 1) est += C.bo_scale_f * expf(be.p_bo1 * powf(df / be.r_s, be.p_bo2));
-            if (be.mask & 2) est += expf(be.p_bo3 * powf(df / be.r_p, be.p_bo4));
-            if (be.mask & 4) est += expf(be.p_bo5 * powf(df / be.r_pp, be.p_bo6));
+            if (be.mask & 1) est += C.bo_scale_f * exp2f(be.e[0] * exp2f(be.q[0] * (lg - be.l[0])));
+            if (be.mask & 2) est += exp2f(be.e[1] * exp2f(be.q[1] * (lg - be.l[1])));
+            if (be.mask & 4) est += exp2f(be.e[2] * exp2f(be.q[2] * (lg - be.l[2])));
             cand = est >= bo_half;
           }
         }

@@ -800,10 +800,13 @@ void init_control(const rg_params &p, const ForceField &ff, Control &c) {
     for (int b = 0; b < RG_MAXT; ++b) {
       const Tbp &tw = ff.tbp[a][b];
       Control::BoEst &e = c.bo_est[a][b];
-      e.p_bo1 = (float)tw.p_bo1; e.p_bo2 = (float)tw.p_bo2;
-      e.p_bo3 = (float)tw.p_bo3; e.p_bo4 = (float)tw.p_bo4;
-      e.p_bo5 = (float)tw.p_bo5; e.p_bo6 = (float)tw.p_bo6;
-      e.r_s = (float)tw.r_s; e.r_p = (float)tw.r_p; e.r_pp = (float)tw.r_pp;
+      const double pk[3] = {tw.p_bo1, tw.p_bo3, tw.p_bo5}, qk[3] = {tw.p_bo2, tw.p_bo4, tw.p_bo6};
+      const double r0[3] = {tw.r_s, tw.r_p, tw.r_pp};
+      for (int k = 0; k < 3; ++k) {
+        e.e[k] = (float)(pk[k] * 1.4426950408889634);   // log2(e)
+        e.q[k] = (float)qk[k];
+        e.l[k] = r0[k] > 0.0 ? (float)std::log2(r0[k]) : 0.f;
+      }
       c.ln_r[a][b][0] = tw.r_s > 0.0 ? std::log(tw.r_s) : 0.0;
       c.ln_r[a][b][1] = tw.r_p > 0.0 ? std::log(tw.r_p) : 0.0;
       c.ln_r[a][b][2] = tw.r_pp > 0.0 ? std::log(tw.r_pp) : 0.0;

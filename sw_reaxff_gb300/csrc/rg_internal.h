@@ -136,8 +136,10 @@ struct Control {
   // log r_s, log r_pi, log r_pipi per type pair: the FP64 BO' powers as
   // exp(p (log d - log r)) with one log per bond
   double ln_r[RG_MAXT][RG_MAXT][3];
+  // FP32 estimate of BO' = sum_k exp(p_k (r / r0_k)^q_k) as
+  // exp2(e_k exp2(q_k (log2 r - l_k))) with e_k = p_k log2(e), l_k = log2 r0_k
   struct BoEst {
-    float p_bo1, p_bo2, p_bo3, p_bo4, p_bo5, p_bo6, r_s, r_p, r_pp;
+    float e[3], q[3], l[3];
     int mask;          // 1: sigma, 2: pi, 4: pi-pi bond order terms present
   } bo_est[RG_MAXT][RG_MAXT];
 };
@@ -236,11 +238,11 @@ struct Dev {
   int *n_active;      // QEq: segments with an active solve (host poll)
 
   // valence / torsion work lists (built per force step)
-  double *c_sbo;      // 9 * n per centre: SBO2, CSBO2, dSBO1, dSBO2, expval6, and for
-                      // the FP64 angles exp(-p_pen3 Delta), exp(p_pen4 Delta),
+  double *c_sbo;      // 9 * n per centre: SBO2, CSBO2, dSBO1, dSBO2, expval6, and in
+                      // the FP64 form exp(-p_pen3 Delta), exp(p_pen4 Delta),
                       // exp(p_coa2 Delta_val), exp(-p_val10 (2 - SBO2))
   double *b_et2, *b_ec2;   // per bond slot: exp(-p_tor2 BOA), exp(-p_cot2 (BOA-1.5)^2)
-  double *b_vexp;     // 3 * slots (FP64 angles): exp(-p_pen2 (BOA-2)^2),
+  double *b_vexp;     // 3 * slots (FP64 form): exp(-p_pen2 (BOA-2)^2),
                       // exp(-p_coa3 (bo0[nbr] - BOA)^2), exp(-p_coa4 (BOA-1.5)^2)
   float *b_BOf;             // per bond slot: BO in FP32, 0 where BO <= thb_cut (exact
                             // FP64 test), for the valence/torsion enumeration

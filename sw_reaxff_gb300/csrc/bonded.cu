@@ -227,14 +227,12 @@ __global__ void k_bo_atom(Dev d) {
 __global__ void k_atom_energy(Dev d, int eflag) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int n = d.n;
-  double e_lph = 0, e_lp = 0, e_ov = 0, e_un = 0, ebond = 0, estriph = 0;
+  double e_lph = 0, e_lp = 0, e_ov = 0, e_un = 0;
   double pol = 0, pol_w = 0;
   if (i < n) {
     const ForceField &F = *d.ff;
     const double p_lp3 = F.gp[5], p_ovun3 = F.gp[32], p_ovun4 = F.gp[31];
     const double p_ovun6 = F.gp[6], p_ovun7 = F.gp[8], p_ovun8 = F.gp[9];
-    const double gp3 = F.gp[3], gp4 = F.gp[4], gp7 = F.gp[7], gp10 = F.gp[10];
-    const int gp37 = (int)F.gp[37];
     double *CdD = d.fC + 3 * (long long)n;
     const int ti = d.ts[i];
     const Sbp &si = F.sbp[ti];
@@ -317,36 +315,14 @@ __global__ void k_atom_energy(Dev d, int eflag) {
       const int j = nbr_of(e);
       const int tj = d.ts[j];
       const Tbp &tw = F.tbp[ti][tj];
-      const double BOpi = d.b_BOpi[s], BOpi2 = d.b_BOpi2[s], BO = d.b_BO[s];
-      double cdbo = CEover1 * tw.p_ovun1 * tw.De_s;
+      const double BOpi = d.b_BOpi[s], BOpi2 = d.b_BOpi2[s];
+      const double cdbo = CEover1 * tw.p_ovun1 * tw.De_s;
       const double ftmp2 = (1.0 - dfvl * d.dDelta_lp[j]) * (BOpi + BOpi2);
       const double dj = d.Delta[j] - dfvl * d.Delta_lp_temp[j];
-      double cdj = CEover4 * ftmp2 + CEunder4 * ftmp2;
-      double cdpi = CEover4 * dj + CEunder4 * dj;
-      double cdpi2 = cdpi;
-      if (tag_first(d, i, j, e)) {
-        const Sbp &sj = F.sbp[tj];
-        const double BOs = d.b_BOs[s];
-        const double pow_BOs_be2 = (BOs == 0.0) ? 0.0 : pow(BOs, tw.p_be2);
-        const double exp_be12 = exp(tw.p_be1 * (1.0 - pow_BOs_be2));
-        const double CEbo = -tw.De_s * exp_be12 * (1.0 - tw.p_be1 * tw.p_be2 * pow_BOs_be2);
-        ebond += -tw.De_s * BOs * exp_be12 - tw.De_p * BOpi - tw.De_pp * BOpi2;
-        cdbo += CEbo;
-        cdpi -= (CEbo + tw.De_p);
-        cdpi2 -= (CEbo + tw.De_pp);
-        if (BO >= 1.00 && (gp37 == 2 || (si.mass == 12.0000 && sj.mass == 15.9990) ||
-                           (sj.mass == 12.0000 && si.mass == 15.9990))) {
-          const double exphu = exp(-gp7 * sqr(BO - 2.50));
-          const double exphua1 = exp(-gp3 * (d.bo0[i] - BO));
-          const double exphub1 = exp(-gp3 * (d.bo0[j] - BO));
-          const double exphuov = exp(gp4 * (d.Delta[i] + d.Delta[j]));
-          const double hulpov = 1.0 / (1.0 + 25.0 * exphuov);
-          estriph += gp10 * exphu * hulpov * (exphua1 + exphub1);
-          cdbo += gp10 * exphu * hulpov * (exphua1 + exphub1) * (gp3 - 2.0 * gp7 * (BO - 2.50));
-          cd_i += -gp10 * exphu * hulpov * (gp3 * exphua1 + 25.0 * gp4 * exphuov * hulpov * (exphua1 + exphub1));
-          cdj += -gp10 * exphu * hulpov * (gp3 * exphub1 + 25.0 * gp4 * exphuov * hulpov * (exphua1 + exphub1));
-        }
-      }
+      const double cdj = CEover4 * ftmp2 + CEunder4 * ftmp2;
+      const double cdpi = CEover4 * dj + CEunder4 * dj;
+      const double cdpi2 = cdpi;
+      // the bond energy of the bond's first end: k_bond_energy
       d.b_Cdbo[s] += cdbo;
       d.b_Cdbopi[s] += cdpi;
       d.b_Cdbopi2[s] += cdpi2;
@@ -356,13 +332,78 @@ __global__ void k_atom_energy(Dev d, int eflag) {
   }
   if (eflag) {
     const int sg = i < n ? d.seg_s[i] : -1;
-    energy_add(d, ebond + estriph, sg, E_BOND);
     energy_add(d, e_ov + e_un, sg, E_OVUN);
     energy_add(d, e_lp + e_lph, sg, E_LP);
-    energy_add(d, e_lph + e_lp + e_ov + ebond + estriph + e_un, sg, E_ENG_VDWL);
+    energy_add(d, e_lph + e_lp + e_ov + e_un, sg, E_ENG_VDWL);
     energy_add(d, pol, sg, E_ENG_COUL);
     energy_add(d, pol, sg, E_POL_PHYS);
     energy_add(d, pol_w, sg, E_POL);
+  }
+}
+
+// Bond energy (with the triple-bond stabilisation) of every bond, at its
+// first end (tag_first), the reference's Bonds (reaxc_bonds_sw64.c): one
+// warp per 32 atoms over their bond slots (warp_items), so the pow/exp of
+// the half of the slots that carry the energy keep the lanes busy.
+__global__ void __launch_bounds__(256) k_bond_energy(Dev d, int eflag) {
+  const int i0 = blockIdx.x * blockDim.x + threadIdx.x;
+  const int n = d.n;
+  const int cnt = i0 < n ? min(d.nbonds[i0], d.bond_cap) : 0;
+  double eb = 0.0;
+  int sg = -1;
+  warp_items(cnt, i0, [&](int i, int k) {
+    const long long s = (long long)k * n + i;
+    const uint32_t e = d.b_nbr[s];
+    const int j = nbr_of(e);
+    if (!tag_first(d, i, j, e)) return;
+    const ForceField &F = *d.ff;
+    const int ti = d.ts[i], tj = d.ts[j];
+    const Tbp &tw = F.tbp[ti][tj];
+    const Sbp &si = F.sbp[ti], &sj = F.sbp[tj];
+    const double BOpi = d.b_BOpi[s], BOpi2 = d.b_BOpi2[s], BO = d.b_BO[s], BOs = d.b_BOs[s];
+    const double pow_BOs_be2 = (BOs == 0.0) ? 0.0 : pow(BOs, tw.p_be2);
+    const double exp_be12 = exp(tw.p_be1 * (1.0 - pow_BOs_be2));
+    const double CEbo = -tw.De_s * exp_be12 * (1.0 - tw.p_be1 * tw.p_be2 * pow_BOs_be2);
+    double ebond = -tw.De_s * BOs * exp_be12 - tw.De_p * BOpi - tw.De_pp * BOpi2;
+    double cdbo = CEbo;
+    const int gp37 = (int)F.gp[37];
+    if (BO >= 1.00 && (gp37 == 2 || (si.mass == 12.0000 && sj.mass == 15.9990) ||
+                       (sj.mass == 12.0000 && si.mass == 15.9990))) {
+      const double gp3 = F.gp[3], gp4 = F.gp[4], gp7 = F.gp[7], gp10 = F.gp[10];
+      double *CdD = d.fC + 3 * (long long)n;
+      const double exphu = exp(-gp7 * sqr(BO - 2.50));
+      const double exphua1 = exp(-gp3 * (d.bo0[i] - BO));
+      const double exphub1 = exp(-gp3 * (d.bo0[j] - BO));
+      const double exphuov = exp(gp4 * (d.Delta[i] + d.Delta[j]));
+      const double hulpov = 1.0 / (1.0 + 25.0 * exphuov);
+      ebond += gp10 * exphu * hulpov * (exphua1 + exphub1);
+      cdbo += gp10 * exphu * hulpov * (exphua1 + exphub1) * (gp3 - 2.0 * gp7 * (BO - 2.50));
+      atomicAdd(&CdD[i], -gp10 * exphu * hulpov *
+                             (gp3 * exphua1 + 25.0 * gp4 * exphuov * hulpov * (exphua1 + exphub1)));
+      atomicAdd(&CdD[j], -gp10 * exphu * hulpov *
+                             (gp3 * exphub1 + 25.0 * gp4 * exphuov * hulpov * (exphua1 + exphub1)));
+    }
+    d.b_Cdbo[s] += cdbo;
+    d.b_Cdbopi[s] -= CEbo + tw.De_p;
+    d.b_Cdbopi2[s] -= CEbo + tw.De_pp;
+    if (eflag) {
+      // a lane's items can reach into the next segment (batches): the
+      // finished segment's sum goes out directly
+      const int si_seg = d.seg_s[i];
+      if (si_seg != sg) {
+        if (sg >= 0 && eb != 0.0) {
+          atomicAdd(&d.energy[(long long)sg * RG_NE + E_BOND], eb);
+          atomicAdd(&d.energy[(long long)sg * RG_NE + E_ENG_VDWL], eb);
+        }
+        sg = si_seg;
+        eb = 0.0;
+      }
+      eb += ebond;
+    }
+  });
+  if (eflag) {
+    energy_add(d, eb, sg, E_BOND);
+    energy_add(d, eb, sg, E_ENG_VDWL);
   }
 }
 
@@ -1397,6 +1438,7 @@ void launch_bond_orders(const Dev &d, cudaStream_t st) {
 
 void launch_atom_energy(const Dev &d, cudaStream_t st, int eflag) {
   k_atom_energy<<<(d.n + 255) / 256, 256, 0, st>>>(d, eflag);
+  k_bond_energy<<<(d.n + 255) / 256, 256, 0, st>>>(d, eflag);
 }
 
 void launch_hbonds(const Dev &d, cudaStream_t st, int eflag) {

@@ -573,7 +573,7 @@ int do_compute(rg_system *h, int eflag, int vflag = 0) {
     return fail(h, RG_E_NUMERIC, msg);
   };
   { Scope sc(h, PH_BO, 3); launch_bond_orders(d, h->st); }
-  { Scope sc(h, PH_ATOM, 1); launch_atom_energy(d, h->st, eflag); }
+  { Scope sc(h, PH_ATOM, 2); launch_atom_energy(d, h->st, eflag); }
   if ((rc = finite_after("atom_energy"))) return rc;
   { Scope sc(h, PH_HB, 1); launch_hbonds(d, h->st, eflag); }
   if ((rc = finite_after("hbonds"))) return rc;

@@ -860,29 +860,41 @@ __device__ void vt_enumerate(const Dev &d, int j, int kk, int &cv, int &ct, long
   }
 }
 
-__global__ void k_vt_count(Dev d) {
+// items per bond slot (kk of centre j): one warp per 32 centres over their
+// bond slots (warp_items); the slots past a centre's bond count, and the
+// trailing entry of the exclusive scans, get zero
+__global__ void __launch_bounds__(256) k_vt_count(Dev d) {
   const int n = d.n;
-  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  const long long slots = (long long)d.bond_cap * n;
-  if (t > slots) return;
-  if (t == slots) {   // trailing zero for the exclusive scans
-    d.w_cnt_v[t] = 0;
-    d.w_cnt_t[t] = 0;
-    return;
+  const int j0 = blockIdx.x * blockDim.x + threadIdx.x;
+  const int cnt = j0 < n ? min(d.nbonds[j0], d.bond_cap) : 0;
+  if (j0 < n)
+    for (int k = cnt; k < d.bond_cap; ++k) {
+      d.w_cnt_v[(long long)k * n + j0] = 0;
+      d.w_cnt_t[(long long)k * n + j0] = 0;
+    }
+  if (j0 == 0) {
+    const long long slots = (long long)d.bond_cap * n;
+    d.w_cnt_v[slots] = 0;
+    d.w_cnt_t[slots] = 0;
   }
-  int cv, ct;
-  vt_enumerate<false>(d, (int)(t % n), (int)(t / n), cv, ct, 0, 0);
-  d.w_cnt_v[t] = cv;
-  d.w_cnt_t[t] = ct;
+  warp_items(cnt, j0, [&](int j, int kk) {
+    int cv, ct;
+    vt_enumerate<false>(d, j, kk, cv, ct, 0, 0);
+    d.w_cnt_v[(long long)kk * n + j] = cv;
+    d.w_cnt_t[(long long)kk * n + j] = ct;
+  });
 }
 
-__global__ void k_vt_fill(Dev d) {
+__global__ void __launch_bounds__(256) k_vt_fill(Dev d) {
   const int n = d.n;
-  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= (long long)d.bond_cap * n) return;
-  if (d.w_cnt_v[t] == 0 && d.w_cnt_t[t] == 0) return;
-  int cv, ct;
-  vt_enumerate<true>(d, (int)(t % n), (int)(t / n), cv, ct, d.w_off_v[t], d.w_off_t[t]);
+  const int j0 = blockIdx.x * blockDim.x + threadIdx.x;
+  const int cnt = j0 < n ? min(d.nbonds[j0], d.bond_cap) : 0;
+  warp_items(cnt, j0, [&](int j, int kk) {
+    const long long t = (long long)kk * n + j;
+    if (d.w_cnt_v[t] == 0 && d.w_cnt_t[t] == 0) return;
+    int cv, ct;
+    vt_enumerate<true>(d, j, kk, cv, ct, d.w_off_v[t], d.w_off_t[t]);
+  });
 }
 
 // one valence angle h-j-k (with its penalty and coalition terms); R as in
@@ -1458,7 +1470,7 @@ void launch_vt_count(const Dev &d, cudaStream_t st) {
   const long long slots = (long long)d.n * d.bond_cap;
   k_vt_prep_center<<<(d.n + B - 1) / B, B, 0, st>>>(d);
   k_vt_prep_bond<<<(unsigned)((d.n + 255) / 256), 256, 0, st>>>(d);
-  k_vt_count<<<(unsigned)((slots + 1 + B - 1) / B), B, 0, st>>>(d);
+  k_vt_count<<<(unsigned)((d.n + 255) / 256), 256, 0, st>>>(d);
   launch_scan(d.w_cnt_v, d.w_off_v, (int)(slots + 1), d.w_bsum, st);
   launch_scan(d.w_cnt_t, d.w_off_t, (int)(slots + 1), d.w_bsum, st);
 }
@@ -1480,9 +1492,7 @@ static void vt_kernels(const Dev &d, cudaStream_t st, int eflag, long long nval,
 }
 
 void launch_vt_run(const Dev &d, cudaStream_t st, int eflag, long long nval, long long ntor) {
-  const int B = 256;
-  const long long slots = (long long)d.n * d.bond_cap;
-  k_vt_fill<<<(unsigned)((slots + B - 1) / B), B, 0, st>>>(d);
+  k_vt_fill<<<(unsigned)((d.n + 255) / 256), 256, 0, st>>>(d);
   const unsigned gv = (unsigned)((nval + 127) / 128), gt = (unsigned)((ntor + 127) / 128);
   if (d.vflag) vt_kernels<true>(d, st, eflag, nval, ntor, gv, gt);
   else vt_kernels<false>(d, st, eflag, nval, ntor, gv, gt);

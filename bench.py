@@ -47,7 +47,7 @@ SEED = 7
 FP64_PER_UNIT = {
     # phase: (kernel, unit, FLOP per unit, DRAM bytes per unit)
     "pair_list+H": ("k_build_nbrs", "directed pair", 23.00, 11.19),
-    "nonbonded": ("k_nonbonded", "unordered pair", 75.7, 11.7),
+    "nonbonded": ("k_nonbonded", "unordered pair", 39.97, 16.87),
     "qeq_spmv": ("k_spmv", "list entry", 4.12, 12.76),
 }
 

@@ -267,11 +267,12 @@ __global__ void k_atom_energy(Dev d, int eflag) {
         const int j = nbr_of(d.b_nbr[s]);
         if (!F.sbp[d.ts[j]].is_carbon) continue;
         const double Di = d.Delta[i];
-        const double vov3 = d.b_BO[s] - Di - 0.040 * pow(Di, 4.);
+        const double Di2 = Di * Di;
+        const double vov3 = d.b_BO[s] - Di - 0.040 * (Di2 * Di2);
         if (vov3 > 3.) {
           e_lph += p_lp3 * sqr(vov3 - 3.0);
           d.b_Cdbo[s] += 2. * p_lp3 * (vov3 - 3.);
-          cd_i += 2. * p_lp3 * (vov3 - 3.) * (-1. - 0.16 * pow(Di, 3.));
+          cd_i += 2. * p_lp3 * (vov3 - 3.) * (-1. - 0.16 * (Di2 * Di));
         }
       }
     }
@@ -343,15 +344,15 @@ __global__ void k_atom_energy(Dev d, int eflag) {
 
 // Bond energy (with the triple-bond stabilisation) of every bond, at its
 // first end (tag_first), the reference's Bonds (reaxc_bonds_sw64.c): one
-// warp per 32 atoms over their bond slots (warp_items), so the pow/exp of
-// the half of the slots that carry the energy keep the lanes busy.
+// warp per 32 atoms over the bond slots that carry the energy
+// (warp_items_mask), so their log/exp keep the lanes busy.
 __global__ void __launch_bounds__(256) k_bond_energy(Dev d, int eflag) {
   const int i0 = blockIdx.x * blockDim.x + threadIdx.x;
   const int n = d.n;
   const int cnt = i0 < n ? min(d.nbonds[i0], d.bond_cap) : 0;
   double eb = 0.0;
   int sg = -1;
-  warp_items(cnt, i0, [&](int i, int k) {
+  auto item = [&](int i, int k) {
     const long long s = (long long)k * n + i;
     const uint32_t e = d.b_nbr[s];
     const int j = nbr_of(e);
@@ -361,7 +362,9 @@ __global__ void __launch_bounds__(256) k_bond_energy(Dev d, int eflag) {
     const Tbp &tw = F.tbp[ti][tj];
     const Sbp &si = F.sbp[ti], &sj = F.sbp[tj];
     const double BOpi = d.b_BOpi[s], BOpi2 = d.b_BOpi2[s], BO = d.b_BO[s], BOs = d.b_BOs[s];
-    const double pow_BOs_be2 = (BOs == 0.0) ? 0.0 : pow(BOs, tw.p_be2);
+    // BOs^p_be2 as exp(p_be2 ln BOs) (to ~1e-15 relative, without pow's
+    // extended-precision logarithm)
+    const double pow_BOs_be2 = (BOs <= 0.0) ? 0.0 : exp(tw.p_be2 * log(BOs));
     const double exp_be12 = exp(tw.p_be1 * (1.0 - pow_BOs_be2));
     const double CEbo = -tw.De_s * exp_be12 * (1.0 - tw.p_be1 * tw.p_be2 * pow_BOs_be2);
     double ebond = -tw.De_s * BOs * exp_be12 - tw.De_p * BOpi - tw.De_pp * BOpi2;
@@ -400,7 +403,18 @@ __global__ void __launch_bounds__(256) k_bond_energy(Dev d, int eflag) {
       }
       eb += ebond;
     }
-  });
+  };
+  if (d.bond_cap <= 32) {
+    // only the slots that carry the energy (a bit per slot)
+    unsigned first = 0;
+    for (int k = 0; k < cnt; ++k) {
+      const uint32_t e = d.b_nbr[(long long)k * n + i0];
+      if (tag_first(d, i0, nbr_of(e), e)) first |= 1u << k;
+    }
+    warp_items_mask(first, i0, item);
+  } else {
+    warp_items(cnt, i0, item);
+  }
   if (eflag) {
     energy_add(d, eb, sg, E_BOND);
     energy_add(d, eb, sg, E_ENG_VDWL);
@@ -739,11 +753,14 @@ __global__ void k_vt_prep_center(Dev d) {
   double SBO2, CSBO2;
   if (SBO <= 0) SBO2 = 0, CSBO2 = 0;
   else if (SBO > 0 && SBO <= 1) {
-    SBO2 = pow(SBO, p_val9);
-    CSBO2 = p_val9 * pow(SBO, p_val9 - 1);
+    // x^p and p x^(p-1) from one logarithm and one exponential
+    const double xp = exp(p_val9 * log(SBO));
+    SBO2 = xp;
+    CSBO2 = p_val9 * xp / SBO;
   } else if (SBO > 1 && SBO < 2) {
-    SBO2 = 2 - pow(2 - SBO, p_val9);
-    CSBO2 = p_val9 * pow(2 - SBO, p_val9 - 1);
+    const double y = 2 - SBO, yp = exp(p_val9 * log(y));
+    SBO2 = 2 - yp;
+    CSBO2 = p_val9 * yp / y;
   } else SBO2 = 2, CSBO2 = 0;
   d.c_sbo[j] = SBO2;
   d.c_sbo[n + j] = CSBO2;

@@ -502,9 +502,9 @@ __device__ __forceinline__ void bo_prime64(const Control &C, int ti, int tj, con
   }
 }
 
-// BO' of the bond candidates: one thread per candidate slot (blockIdx.y =
-// slot), so the FP64 log/exp run with full warps instead of the few lanes a
-// per-atom warp has candidates for.  Accepted entries get their exact
+// BO' of the bond candidates, 32 candidates of a warp's 32 atoms at a time
+// (warp_items), so the FP64 log/exp run with full warps instead of the few
+// lanes a per-atom warp has candidates for.  Accepted entries get their exact
 // distance, bond orders and dBO' terms; rejected ones (d > bond_cut or
 // BO' < bo_cut) are marked with a negative distance and removed by
 // k_bond_finish.  Both forms take the exact FP64 distance and FP64 BO':

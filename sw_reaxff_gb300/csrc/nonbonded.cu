@@ -244,8 +244,12 @@ __device__ __forceinline__ void pair32(const Dev &d, const Control &C, int vdw_t
 
 // one warp per atom i; the pairs (i,j,image) with j > i, or j == i with the
 // "positive" image, are queued and evaluated 32 at a time
+// the FP64 form is FP64-pipe bound: three blocks per SM (80 registers, a
+// few spilled) keep the pipe busier than two (7 % faster); the FP32 form
+// has no minimum (0) and keeps its 66-80 registers
 template <typename R, bool VIR, bool EF>
-__global__ void __launch_bounds__(NBW * 32) k_nonbonded(Dev d) {
+__global__ void __launch_bounds__(NBW * 32, std::is_same<R, double>::value ? 3 : 0)
+    k_nonbonded(Dev d) {
   __shared__ PairQueue queues[NBW];
   const int lane = threadIdx.x & 31;
   const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;

@@ -68,9 +68,10 @@ typedef struct {
   int qeq_imax;         /* 200   CG iteration limit                     */
   int precision;        /* RG_PREC_FP64 or RG_PREC_MIXED               */
   int device;           /* CUDA device ordinal                          */
-  int tabulate;         /* FP64 form: vdW+Coulomb and QEq H from cubic
-                           Hermite tables in r^2 with this many intervals
-                           per type pair (the reference's control
+  int tabulate;         /* vdW+Coulomb (both forms; the mixed form reads
+                           an FP32 copy) and the FP64 form's QEq H from
+                           cubic Hermite tables in r^2 with this many
+                           intervals per type pair (the reference's control
                            "tabulate_long_range", off in its NULL control);
                            0 = analytic.  Default 65536: ~1e-10 of the
                            analytic pair functions (rg_table_check). */

@@ -154,9 +154,16 @@ __device__ __forceinline__ bool pair_terms(const Dev &d, const ForceField &F, co
   return true;
 }
 
+__device__ __forceinline__ float cubic_uf(const float4 &c, float u) {
+  return fmaf(fmaf(fmaf(c.w, u, c.z), u, c.y), u, c.x);
+}
+
 // Mixed form: vdW + Coulomb of one pair entirely in FP32, parameters from
 // the control block's FP32 copies (no double is read or converted per
-// pair); returns (1/r) dE/dr in c, the displacement and the two energies.
+// pair), or from the FP32 copy of the pair-function tables (their index
+// and fraction from the FP32 r^2, whose rounding the fraction inherits);
+// returns (1/r) dE/dr in c, the displacement and, with EF, the energies.
+template <bool EF>
 __device__ __forceinline__ void pair32(const Dev &d, const Control &C, int vdw_type, uint32_t e,
                                        bool act, const double4 &xi, const float4 &xif,
                                        const float4 &xil, int ti, const SegGeom &g, float &ev,
@@ -188,6 +195,21 @@ __device__ __forceinline__ void pair32(const Dev &d, const Control &C, int vdw_t
     }
   }
   const int tj = __float_as_int(hj.w);
+  if (C.tab_n && d2 >= C.tab_s0_f) {
+    const float x = fmaf(d2, C.tab_inv_ds_f, C.tab_x0_f);
+    int k = (int)x;
+    if (k > C.tab_n - 1) k = C.tab_n - 1;
+    const float u = x - (float)k;
+    const float4 *T = reinterpret_cast<const float4 *>(
+        d.tab_nb32 + ((long long)C.tab_pair[ti][tj] * C.tab_n + k) * 16);
+    const float qq = xil.w * lj.w;   // C_ele is in the Coulomb cubics
+    c = fmaf(cubic_uf(T[1], u), qq, cubic_uf(T[0], u));
+    if (EF) {
+      ev = cubic_uf(T[2], u);
+      ee = qq * cubic_uf(T[3], u);
+    }
+    return;
+  }
   const Control::NbF &P = C.nb32[ti][tj];
   const float rinv = rsqrtf(d2);
   const float r = d2 * rinv;
@@ -298,7 +320,7 @@ __global__ void __launch_bounds__(NBW * 32, std::is_same<R, double>::value ? 3 :
         int j;
         if constexpr (std::is_same<R, float>::value) {
           float ev, ee, c, dx, dy, dz;
-          pair32(d, C, vdw_type, e, act, xi, xif, xil, ti, g, ev, ee, c, dx, dy, dz, j);
+          pair32<EF>(d, C, vdw_type, e, act, xi, xif, xil, ti, g, ev, ee, c, dx, dy, dz, j);
           if (EF) {   // energies summed in FP64 (only on energy steps)
             evdw += (double)ev;
             eele += (double)ee;

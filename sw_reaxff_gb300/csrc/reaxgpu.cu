@@ -80,6 +80,7 @@ struct rg_system {
   ForceField *d_ff = nullptr;
   Control *d_ctl = nullptr;
   double *d_tab = nullptr;        // FP64 tables (nb then H)
+  float *d_tab32 = nullptr;       // mixed form: the nb table in FP32
   double tab_err = 0.0;
   cudaStream_t st = nullptr;
   std::string err;
@@ -886,7 +887,7 @@ int rg_create(const char *ffield_path, const rg_params *pin, rg_system **out) {
   // FP64 tables of the pair functions (tables.cpp)
   std::vector<double> tab_nb, tab_h;
   c.tab_n = 0;
-  if (!h->d.mixed && h->p.tabulate > 0) {
+  if (h->p.tabulate > 0) {
     const int nt = h->ff.ntypes;
     for (int a = 0; a < nt; ++a)
       for (int b = 0; b < nt; ++b) c.tab_pair[a][b] = rg_pair_index(a, b, nt);
@@ -897,6 +898,8 @@ int rg_create(const char *ffield_path, const rg_params *pin, rg_system **out) {
     c.tab_ds = (s1 - s0) / c.tab_n;
     c.tab_inv_ds = 1.0 / c.tab_ds;
     c.tab_x0 = -s0 * c.tab_inv_ds;
+    c.tab_inv_ds_f = (float)c.tab_inv_ds;
+    c.tab_x0_f = (float)c.tab_x0;
     h->tab_err = rg_build_tables(h->ff, c, c.tab_n, s0, s1, tab_nb, tab_h, h->p.tabulate_check != 0);
   }
   cudaError_t ce = cudaSetDevice(h->p.device);
@@ -905,7 +908,14 @@ int rg_create(const char *ffield_path, const rg_params *pin, rg_system **out) {
   if (ce == cudaSuccess) ce = cudaMalloc(&h->d_ctl, sizeof(Control));
   if (ce == cudaSuccess) ce = cudaMemcpy(h->d_ff, &h->ff, sizeof(ForceField), cudaMemcpyHostToDevice);
   if (ce == cudaSuccess) ce = cudaMemcpy(h->d_ctl, &h->ctl, sizeof(Control), cudaMemcpyHostToDevice);
-  if (ce == cudaSuccess && c.tab_n) {
+  if (ce == cudaSuccess && c.tab_n && h->d.mixed) {
+    // the mixed form evaluates the vdW + Coulomb cubics in FP32 (its QEq H
+    // values are FP32 expressions of the pair-list pass)
+    std::vector<float> nb32(tab_nb.begin(), tab_nb.end());
+    ce = cudaMalloc(&h->d_tab32, sizeof(float) * nb32.size());
+    if (ce == cudaSuccess)
+      ce = cudaMemcpy(h->d_tab32, nb32.data(), sizeof(float) * nb32.size(), cudaMemcpyHostToDevice);
+  } else if (ce == cudaSuccess && c.tab_n) {
     ce = cudaMalloc(&h->d_tab, sizeof(double) * (tab_nb.size() + tab_h.size()));
     if (ce == cudaSuccess)
       ce = cudaMemcpy(h->d_tab, tab_nb.data(), sizeof(double) * tab_nb.size(), cudaMemcpyHostToDevice);
@@ -917,6 +927,7 @@ int rg_create(const char *ffield_path, const rg_params *pin, rg_system **out) {
     if (h->d_ff) cudaFree(h->d_ff);
     if (h->d_ctl) cudaFree(h->d_ctl);
     if (h->d_tab) cudaFree(h->d_tab);
+    if (h->d_tab32) cudaFree(h->d_tab32);
   if (h->cg_exec) cudaGraphExecDestroy(h->cg_exec);
     delete h;
     return RG_E_CUDA;
@@ -925,6 +936,7 @@ int rg_create(const char *ffield_path, const rg_params *pin, rg_system **out) {
   h->d.ctl = h->d_ctl;
   h->d.tab_nb = h->d_tab;
   h->d.tab_h = h->d_tab ? h->d_tab + tab_nb.size() : nullptr;
+  h->d.tab_nb32 = h->d_tab32;
   *out = h;
   return RG_OK;
 }
@@ -955,6 +967,7 @@ int rg_destroy(rg_system *h) {
   cudaFree(h->d_ff);
   cudaFree(h->d_ctl);
   if (h->d_tab) cudaFree(h->d_tab);
+  if (h->d_tab32) cudaFree(h->d_tab32);
   if (h->cg_exec) cudaGraphExecDestroy(h->cg_exec);
   cudaStreamDestroy(h->st);
   delete h;

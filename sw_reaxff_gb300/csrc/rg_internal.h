@@ -111,6 +111,7 @@ struct Control {
   int tab_n;
   double tab_s0, tab_ds, tab_inv_ds, tab_x0;   // tab_x0 = -tab_s0 / tab_ds
   float tab_s0_f;        // table or analytic form below it (either is the function)
+  float tab_inv_ds_f, tab_x0_f;   // the mixed form's FP32 lookups
   int tab_pair[RG_MAXT][RG_MAXT];   // unordered type pair -> table index
   // FP32 copies for the prefilters (no FP64 conversions per entry; GB300
   // runs FP64 at 1/64 of the FP32 rate)
@@ -174,6 +175,7 @@ struct Dev {
   const Control *ctl;
   const double *tab_nb;  // [pair][interval][16]: cubics in u of Fv, Fc, Ev, Ec (tables.cpp)
   const double *tab_h;   // [pair][interval][4]: cubic in u of H_ij
+  const float *tab_nb32; // mixed form: tab_nb in FP32
 
   // original order (persistent state)
   double *x_o, *v_o, *q_o, *f_o;

@@ -768,13 +768,20 @@ __global__ void k_vt_prep_center(Dev d) {
   d.c_sbo[3 * n + j] = dSBO2;
   d.c_sbo[4 * n + j] = exp(p_val6 * Delta_j);
   if (!d.mixed) {
-    // the FP64 form's per-centre exponentials of its angles (penalty,
-    // coalition, theta_0); the mixed form's few FP64 fallback angles
-    // evaluate them in place
-    d.c_sbo[5 * n + j] = exp(-F.gp[20] * d.Delta[j]);
-    d.c_sbo[6 * n + j] = exp(F.gp[21] * d.Delta[j]);
-    d.c_sbo[7 * n + j] = exp(F.gp[2] * d.Delta_val[j]);
+    // the FP64 form's per-centre factors of its angles (penalty f9 and
+    // Cf9/f9, coalition 1/(1 + e) and -p_coa2 e/(1 + e), theta_0's
+    // exponential); the mixed form's few FP64 fallback angles evaluate
+    // them in place
+    const double p_pen3 = F.gp[20], p_pen4 = F.gp[21], p_coa2 = F.gp[2];
+    const double e3 = exp(-p_pen3 * d.Delta[j]), e4 = exp(p_pen4 * d.Delta[j]);
+    const double trm = 1.0 + e3 + e4, f9 = (2.0 + e3) / trm;
+    const double Cf9 = (-p_pen3 * e3 * trm - (2.0 + e3) * (-p_pen3 * e3 + p_pen4 * e4)) / sqr(trm);
+    const double ec = exp(p_coa2 * d.Delta_val[j]), ic = 1.0 / (1.0 + ec);
+    d.c_sbo[5 * n + j] = f9;
+    d.c_sbo[6 * n + j] = Cf9 / f9;
+    d.c_sbo[7 * n + j] = ic;
     d.c_sbo[8 * n + j] = exp(-F.gp[17] * (2.0 - SBO2));
+    d.c_sbo[9 * n + j] = -p_coa2 * ec * ic;
   }
 }
 
@@ -1000,29 +1007,46 @@ __device__ __forceinline__ void valence_item(const Dev &d, unsigned long long it
       e_ang += (double)(f7_jk * f7_hj * f8_Dj * expval12theta);
       const R exp_pen2jk = pre ? (R)d.b_vexp[spk] : exp(-p_pen2 * sqr(BOA_jk - R(2)));
       const R exp_pen2hj = pre ? (R)d.b_vexp[sph] : exp(-p_pen2 * sqr(BOA_hj - R(2)));
-      const R exp_pen3 = pre ? (R)d.c_sbo[5 * n + j] : exp(-p_pen3 * Dj);
-      const R exp_pen4 = pre ? (R)d.c_sbo[6 * n + j] : exp(p_pen4 * Dj);
-      const R trm_pen34 = R(1) + exp_pen3 + exp_pen4;
-      const R f9_Dj = (R(2) + exp_pen3) / trm_pen34;
-      const R Cf9j = (-p_pen3 * exp_pen3 * trm_pen34 -
-                      (R(2) + exp_pen3) * (-p_pen3 * exp_pen3 + p_pen4 * exp_pen4)) / sqr(trm_pen34);
+      // f9(Delta_j) and Cf9j / f9 per centre (FP64 form: k_vt_prep_center)
+      R f9_Dj, Cf9_f9;
+      if (pre) {
+        f9_Dj = (R)d.c_sbo[5 * n + j];
+        Cf9_f9 = (R)d.c_sbo[6 * n + j];
+      } else {
+        const R exp_pen3 = exp(-p_pen3 * Dj), exp_pen4 = exp(p_pen4 * Dj);
+        const R trm_pen34 = R(1) + exp_pen3 + exp_pen4;
+        f9_Dj = (R(2) + exp_pen3) / trm_pen34;
+        const R Cf9j = (-p_pen3 * exp_pen3 * trm_pen34 -
+                        (R(2) + exp_pen3) * (-p_pen3 * exp_pen3 + p_pen4 * exp_pen4)) / sqr(trm_pen34);
+        Cf9_f9 = Cf9j / f9_Dj;
+      }
       const R epen = (R)tp.p_pen1 * f9_Dj * exp_pen2jk * exp_pen2hj;
       e_pen += (double)epen;
-      const R CEpen1 = epen * Cf9j / f9_Dj;
+      const R CEpen1 = epen * Cf9_f9;
       const R temp = R(-2) * p_pen2 * epen;
       const R CEpen2 = temp * (BOA_jk - R(2));
       const R CEpen3 = temp * (BOA_hj - R(2));
-      const R exp_coa2 = pre ? (R)d.c_sbo[7 * n + j] : exp(p_coa2 * Dval_j);
+      // 1 / (1 + exp(p_coa2 Delta_val)) and -p_coa2 exp(..) / (1 + exp(..))
+      // per centre in the FP64 form
+      R icoa, kcoa;
+      if (pre) {
+        icoa = (R)d.c_sbo[7 * n + j];
+        kcoa = (R)d.c_sbo[9 * n + j];
+      } else {
+        const R exp_coa2 = exp(p_coa2 * Dval_j);
+        icoa = R(1) / (R(1) + exp_coa2);
+        kcoa = -p_coa2 * exp_coa2 * icoa;
+      }
       const R ecoa =
-          pre ? (R)tp.p_coa1 / (R(1) + exp_coa2) * (R)d.b_vexp[S + spk] * (R)d.b_vexp[S + sph] *
+          pre ? (R)tp.p_coa1 * icoa * (R)d.b_vexp[S + spk] * (R)d.b_vexp[S + sph] *
                     (R)d.b_vexp[2 * S + spk] * (R)d.b_vexp[2 * S + sph]
-              : (R)tp.p_coa1 / (R(1) + exp_coa2) * exp(-p_coa3 * sqr(bo0k - BOA_jk)) *
+              : (R)tp.p_coa1 * icoa * exp(-p_coa3 * sqr(bo0k - BOA_jk)) *
                     exp(-p_coa3 * sqr(bo0h - BOA_hj)) * exp(-p_coa4 * sqr(BOA_jk - R(1.5))) *
                     exp(-p_coa4 * sqr(BOA_hj - R(1.5)));
       e_coa += (double)ecoa;
       const R CEcoa1 = R(-2) * p_coa4 * (BOA_jk - R(1.5)) * ecoa;
       const R CEcoa2 = R(-2) * p_coa4 * (BOA_hj - R(1.5)) * ecoa;
-      const R CEcoa3 = -p_coa2 * exp_coa2 * ecoa / (R(1) + exp_coa2);
+      const R CEcoa3 = kcoa * ecoa;
       const R CEcoa4 = R(-2) * p_coa3 * (bo0k - BOA_jk) * ecoa;
       const R CEcoa5 = R(-2) * p_coa3 * (bo0h - BOA_hj) * ecoa;
       atomicAdd(&d.b_Cdbo[spk], (double)(CEval1 + CEpen2 + (CEcoa1 - CEcoa4)));
@@ -1037,7 +1061,7 @@ __device__ __forceinline__ void valence_item(const Dev &d, unsigned long long it
       if (d.debug) {
         const double v[] = {BOA_jk, BOA_hj, theta_hjk, sin_theta_hjk, SBO2, CSBO2, dSBO1, dSBO2,
                             expval6, Delta_j, f7_jk, f7_hj, f8_Dj, expval2theta, theta_0, CEval1,
-                            CEval2, CEval3, CEval4, CEval5, CEval8, epen, ecoa, exp_coa2, Cf7jk,
+                            CEval2, CEval3, CEval4, CEval5, CEval8, epen, ecoa, icoa, Cf7jk,
                             Cf7hj, Cf8j, CEpen1, CEcoa3, (double)cnt};
         double sum = 0.0;
         for (double x : v) sum += x;

@@ -386,7 +386,7 @@ int alloc_atoms(rg_system *h, int n) {
   r |= dalloc(h, B, &d.fC, 4 * (size_t)n);
   r |= dalloc(h, B, &d.vsum, 2 * (size_t)n);
   r |= dalloc(h, B, &d.exp_boc, 2 * (size_t)n);
-  r |= dalloc(h, B, &d.c_sbo, 9 * (size_t)n);
+  r |= dalloc(h, B, &d.c_sbo, 10 * (size_t)n);
   double2 **pv[] = {&d.qx, &d.qb, &d.qr, &d.qu, &d.qw, &d.qd, &d.qq, &d.qp, &d.qs, &d.qv, &d.qz, &d.qm};
   for (double2 **q : pv) r |= dalloc(h, B, q, (size_t)n);
   if (d.mixed) r |= dalloc(h, B, &d.qd32, (size_t)n);

@@ -240,9 +240,9 @@ struct Dev {
   int *n_active;      // QEq: segments with an active solve (host poll)
 
   // valence / torsion work lists (built per force step)
-  double *c_sbo;      // 9 * n per centre: SBO2, CSBO2, dSBO1, dSBO2, expval6, and in
-                      // the FP64 form exp(-p_pen3 Delta), exp(p_pen4 Delta),
-                      // exp(p_coa2 Delta_val), exp(-p_val10 (2 - SBO2))
+  double *c_sbo;      // 10 * n per centre: SBO2, CSBO2, dSBO1, dSBO2, expval6, and in
+                      // the FP64 form f9(Delta), Cf9/f9, 1/(1 + exp(p_coa2 Delta_val)),
+                      // exp(-p_val10 (2 - SBO2)), -p_coa2 exp(..)/(1 + exp(..))
   double *b_et2, *b_ec2;   // per bond slot: exp(-p_tor2 BOA), exp(-p_cot2 (BOA-1.5)^2)
   double *b_vexp;     // 3 * slots (FP64 form): exp(-p_pen2 (BOA-2)^2),
                       // exp(-p_coa3 (bo0[nbr] - BOA)^2), exp(-p_coa4 (BOA-1.5)^2)

@@ -356,6 +356,37 @@ __global__ void k_cg_A(Dev d) {
   seg_block_add<4>(all, sg, d.red + R_ACC0, RG_NRED);   // ACC0[2], ACC1[2] are contiguous
 }
 
+// k_cg_A for a single segment: a grid-stride loop over the atoms with
+// about four blocks per SM, so the dot products take one FP64 atomic per
+// value and block from ~600 blocks instead of one per 256 atoms
+__global__ void k_cg_A1(Dev d) {
+  const double *R = d.red;
+  const bool as = R[R_ACTIVE] != 0.0, at = R[R_ACTIVE + 1] != 0.0;
+  double all[4] = {0, 0, 0, 0};   // u.r (s, t), u.w (s, t)
+  if (as || at) {
+    const double a_s = R[R_ALPHA], a_t = R[R_ALPHA + 1];
+    for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < d.n; s += gridDim.x * blockDim.x) {
+      const double hi = d.Hdia_inv[s];
+      double2 r = d.qr[s], u = d.qu[s], w = d.qw[s];
+      const double2 ss = d.qs[s], vv = d.qv[s], z = d.qz[s];
+      double2 dd = d.qd[s];
+      if (as) {
+        r.x -= a_s * ss.x; u.x -= a_s * vv.x; w.x -= a_s * z.x;
+        all[0] += u.x * r.x; all[2] += u.x * w.x;
+        dd.x = w.x * hi;
+      }
+      if (at) {
+        r.y -= a_t * ss.y; u.y -= a_t * vv.y; w.y -= a_t * z.y;
+        all[1] += u.y * r.y; all[3] += u.y * w.y;
+        dd.y = w.y * hi;
+      }
+      d.qr[s] = r; d.qu[s] = u; d.qw[s] = w; d.qd[s] = dd;
+      if (d.qd32) d.qd32[s] = split4(dd);
+    }
+  }
+  seg_block_add<4>(all, 0, d.red + R_ACC0, RG_NRED);
+}
+
 // scalars after A: beta, heta, alpha; activity of the next iteration (one
 // thread per segment)
 __global__ void k_cg_ctrl(Dev d) {
@@ -560,7 +591,8 @@ void launch_qeq_cg_init_rest(const Dev &d, cudaStream_t st, double tol, int imax
 // one CG iteration = launch_qeq_cg_A, SpMV of d into q, launch_qeq_cg_C
 void launch_qeq_cg_A(const Dev &d, cudaStream_t st) {
   const int B = 256, G = (d.n + B - 1) / B;
-  k_cg_A<<<G, B, 0, st>>>(d);
+  if (d.nseg == 1) k_cg_A1<<<G < 608 ? G : 608, B, 0, st>>>(d);
+  else k_cg_A<<<G, B, 0, st>>>(d);
 }
 
 void launch_qeq_cg_C(const Dev &d, cudaStream_t st) {

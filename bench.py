@@ -39,9 +39,10 @@ SEED = 7
 # Per-unit FP64 FLOP (2*dfma + dmul + dadd, SASS thread-instruction counts)
 # and DRAM bytes (dram__bytes_read + write) of the kernels that can dominate
 # the FP64 step, from one ncu capture of the 52,428-atom case of the same
-# mixture (profiles/fp64_kernels_tabulated_mixture52k.md): per directed pair
-# for the pair-list build, per unordered pair for the nonbonded kernel, per
-# list entry for one QEq SpMV (two systems).  bench.py multiplies them by
+# mixture (`--scale 0.05`; the nonbonded kernel's force-only variant, which
+# the timed steps run): per directed pair for the pair-list build, per
+# unordered pair for the nonbonded kernel, per list entry for one QEq SpMV
+# (two systems).  bench.py multiplies them by
 # the units of the measured workload; traffic scales with the units because
 # every kernel streams its list once.
 FP64_PER_UNIT = {

@@ -83,11 +83,12 @@ __device__ __forceinline__ void theta_dcos(const R *dji, R d_ji, const R *djk, R
   const R inv_dists = R(1) / (d_ji * d_jk);
   const R inv_dists3 = inv_dists * inv_dists * inv_dists;
   const R Cdot_inv3 = dot * inv_dists3;
+  // the three gradients of cos theta sum to zero: dj = -(di + dk)
 #pragma unroll
   for (int t = 0; t < 3; ++t) {
     di[t] = djk[t] * inv_dists - Cdot_inv3 * sqr_d_jk * dji[t];
-    dj[t] = -(djk[t] + dji[t]) * inv_dists + Cdot_inv3 * (sqr_d_jk * dji[t] + sqr_d_ji * djk[t]);
     dk[t] = dji[t] * inv_dists - Cdot_inv3 * sqr_d_ji * djk[t];
+    dj[t] = -(di[t] + dk[t]);
   }
 }
 
@@ -500,8 +501,8 @@ __global__ void __launch_bounds__(256) k_hbonds(Dev d, int eflag) {
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
           di[c] = djk[c] * inv_dists - Cdot_inv3 * sqr_d_jk * dij[c];
-          djv[c] = -(djk[c] + dij[c]) * inv_dists + Cdot_inv3 * (sqr_d_jk * dij[c] + sqr_d_ji * djk[c]);
           dk[c] = dij[c] * inv_dists - Cdot_inv3 * sqr_d_ji * djk[c];
+          djv[c] = -(di[c] + dk[c]);   // the gradients sum to zero
         }
         // sin^4(theta/2) = ((1 - cos theta) / 2)^2: the reference's
         // sin(acos(c) / 2) without the two transcendentals

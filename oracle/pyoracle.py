@@ -62,6 +62,7 @@ def lib(path=None):
             _reflib.ro_ref_compute.argtypes = [C.c_void_p, P(C.c_double), P(C.c_double),
                                                P(C.c_double), P(C.c_int), P(C.c_int),
                                                P(C.c_int), P(C.c_longlong)]
+            _reflib.ro_ref_use_qeq.argtypes = [C.c_void_p, C.c_int]
         return _reflib
     if _lib is None:
         build()
@@ -110,11 +111,15 @@ def _ip(a):
 class Oracle:
     """Stateful CPU oracle for one periodic system."""
 
-    def __init__(self, ffield: str, reference: bool = False, **control):
+    def __init__(self, ffield: str, reference: bool = False, reference_qeq: bool = False,
+                 **control):
         """reference=True loads the build that also carries the reference's
-        own host-side code (ref_compute)."""
+        own host-side code (ref_compute); reference_qeq=True (implies
+        reference) makes qeq() and run_nve() solve the charges with the
+        reference's own FixQEqReaxSunway::pre_force on this oracle's H
+        matrix."""
         self.h = None
-        L = lib(REF_LIB if reference else None)
+        L = lib(REF_LIB if (reference or reference_qeq) else None)
         ctl = Control()
         L.ro_default_control(C.byref(ctl))
         for k, v in control.items():
@@ -125,6 +130,8 @@ class Oracle:
             raise RuntimeError(err.value.decode())
         self.L = L
         self.n = 0
+        if reference_qeq:
+            L.ro_ref_use_qeq(self.h, 1)
 
     def close(self):
         if self.h:

@@ -135,6 +135,9 @@ struct ro_ctx {
   double *cd_local;     /* n: folded CdDelta */
   /* QEq matrix rows for local atoms */
   long long H_entries;
+  /* QEq driver: NULL = qeq_restated below; the reference build installs the
+   * reference's own FixQEqReaxSunway::pre_force here (oracle/ref) */
+  int (*qeq_driver)(ro_ctx *c, const void *H, int *iters_s, int *iters_t);
   double en[RO_NENERGY];
   double tphase[8];
 };
@@ -1911,11 +1914,11 @@ static int qeq_cg(const ro_ctx *c, const hmat_t *H, const double *b,
   return i;
 }
 
-int ro_qeq(ro_ctx *c, double *q_out, int *iters_s, int *iters_t) {
-  int i, n = c->n, k;
-  double t0;
-  prepare_lists(c);
-  t0 = now_s();
+/* H rows of the local atoms from the full far list (compute_H_Full_C_para,
+ * fix_qeq_reax_sw64.c:768-911, host form :146-181), ghost columns folded
+ * onto their local owners */
+static void qeq_build_H(ro_ctx *c, hmat_t *H_out) {
+  int i, n = c->n;
   const double swbsq = c->ctl.qeq_swb * c->ctl.qeq_swb;
   const double *Tap = c->qTap;
   hmat_t H;
@@ -1951,6 +1954,14 @@ int ro_qeq(ro_ctx *c, double *q_out, int *iters_s, int *iters_t) {
   }
   H.start[n] = (int)top;
   c->H_entries = top;
+  *H_out = H;
+}
+
+/* init_matvec's extrapolation, CG_v2 on s and t, calculate_Q
+ * (fix_qeq_reax_sunway.cpp:539-600, 618-723, 983-1167, 1697-1755) */
+static int qeq_restated(ro_ctx *c, const hmat_t *Hp, int *iters_s, int *iters_t) {
+  int i, n = c->n, k;
+  const hmat_t H = *Hp;
   double *Hdia_inv = (double *)malloc(n * sizeof(double));
   double *b_s = (double *)malloc(n * sizeof(double));
   double *b_t = (double *)malloc(n * sizeof(double));
@@ -1980,12 +1991,25 @@ int ro_qeq(ro_ctx *c, double *q_out, int *iters_s, int *iters_t) {
     c->s_hist[5 * i] = c->s[i];
     c->t_hist[5 * i] = c->t[i];
   }
-  free(H.start); free(H.col); free(H.val); free(Hdia_inv); free(b_s); free(b_t);
-  if (q_out) memcpy(q_out, c->q, n * sizeof(double));
+  free(Hdia_inv); free(b_s); free(b_t);
   if (iters_s) *iters_s = is;
   if (iters_t) *iters_t = it;
-  c->tphase[4] += now_s() - t0;
   return 0;
+}
+
+int ro_qeq(ro_ctx *c, double *q_out, int *iters_s, int *iters_t) {
+  hmat_t H;
+  double t0;
+  int rc;
+  prepare_lists(c);
+  t0 = now_s();
+  qeq_build_H(c, &H);
+  rc = c->qeq_driver ? c->qeq_driver(c, &H, iters_s, iters_t)
+                     : qeq_restated(c, &H, iters_s, iters_t);
+  free(H.start); free(H.col); free(H.val);
+  if (q_out) memcpy(q_out, c->q, c->n * sizeof(double));
+  c->tphase[4] += now_s() - t0;
+  return rc;
 }
 
 /* ------------------------------------------------------------------ */

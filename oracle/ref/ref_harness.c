@@ -382,3 +382,34 @@ int ro_ref_compute(ro_ctx *c, double *f_out, double *energies, double *bo_out,
   free(lists);
   return ref_abort_code;
 }
+
+/* ------------------------------------------------------------------ */
+/* QEq through the reference's own FixQEqReaxSunway::pre_force
+ * (ref_qeq.cpp) on the oracle's H matrix */
+
+int ref_qeq_pre_force(int n, const int *type, int ntypes, const double *chi,
+                      const double *eta, const int *start, const int *col,
+                      const double *val, double tol, double *s_hist, double *t_hist,
+                      double *s, double *t, double *q_out, int *iters_s, int *iters_t);
+
+static int ref_qeq_driver(ro_ctx *c, const void *Hv, int *iters_s, int *iters_t) {
+  const hmat_t *H = (const hmat_t *)Hv;
+  const int nt = c->ff.ntypes;
+  double *chi = (double *)malloc(nt * sizeof(double));
+  double *eta = (double *)malloc(nt * sizeof(double));
+  int k, warn;
+  for (k = 0; k < nt; k++) {
+    chi[k] = c->ff.sbp[k].chi;
+    eta[k] = c->ff.sbp[k].eta;
+  }
+  warn = ref_qeq_pre_force(c->n, c->type, nt, chi, eta, H->start, H->col, H->val,
+                           c->ctl.qeq_tol, c->s_hist, c->t_hist, c->s, c->t, c->q,
+                           iters_s, iters_t);
+  free(chi);
+  free(eta);
+  return warn ? 1 : 0;
+}
+
+/* on != 0: this context's ro_qeq (and ro_run_nve's QEq) run the
+ * reference's pre_force; 0: the oracle's restatement */
+void ro_ref_use_qeq(ro_ctx *c, int on) { c->qeq_driver = on ? ref_qeq_driver : NULL; }

@@ -16,4 +16,16 @@ static inline int MPI_Comm_rank(MPI_Comm c, int *r) { (void)c; *r = 0; return 0;
 static inline int MPI_Comm_size(MPI_Comm c, int *s) { (void)c; *s = 1; return 0; }
 void ro_stub_abort(int code);
 static inline int MPI_Abort(MPI_Comm c, int code) { (void)c; ro_stub_abort(code); return 0; }
+static inline double MPI_Wtime(void) { return 0.0; }
+/* one rank: the reduction is a copy (doubles or ints) */
+static inline int MPI_Allreduce(const void *in, void *out, int count, MPI_Datatype dt,
+                                MPI_Op op, MPI_Comm c) {
+  int k;
+  (void)op; (void)c;
+  if (dt == MPI_DOUBLE)
+    for (k = 0; k < count; k++) ((double *)out)[k] = ((const double *)in)[k];
+  else
+    for (k = 0; k < count; k++) ((int *)out)[k] = ((const int *)in)[k];
+  return 0;
+}
 #endif

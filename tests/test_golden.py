@@ -1,6 +1,8 @@
 """The CPU oracle against golden fixtures produced by the reference's own
 host-side code (tests/golden/make_golden.py): energies, forces, corrected
-bond orders and the H-bond list for the fixture's positions and charges."""
+bond orders and the H-bond list for the fixture's positions and charges;
+the charges of the reference's QEq driver; a 5-step NVE run on the
+reference's QEq."""
 import glob
 import os
 
@@ -24,10 +26,15 @@ def keyset(ti, tj, im):
     return set(zip(ti.tolist(), tj.tolist(), im.tolist()))
 
 
+def o_ffield(o):
+    return o.ffield
+
+
 @pytest.fixture(scope="module", params=FIXTURES, ids=[os.path.basename(f)[:-4] for f in FIXTURES])
 def case(request, ffield):
     g = load(request.param)
     o = Oracle(ffield)
+    o.ffield = ffield
     o.set_system(g["box"], g["x"], g["types"], g["tags"], g["q"])
     f, e = o.compute()
     return g, o, f, e
@@ -63,3 +70,33 @@ def test_bond_orders_match_reference(case):
 def test_hbond_list_matches_reference(case):
     g, o, f, e = case
     assert keyset(*o.hbond_list()) == keyset(g["hb_ti"], g["hb_tj"], g["hb_img"])
+
+
+def test_qeq_matches_reference(case):
+    """Charges of the reference's own QEq driver (pre_force: init_matvec,
+    CG_v2 on s and t, calculate_Q) from zero histories, and its CG
+    iteration counts."""
+    g, o, f, e = case
+    q2 = Oracle(o_ffield(o))
+    q2.set_system(g["box"], g["x"], g["types"], g["tags"], None, g["v"])
+    q, its, itt = q2.qeq()
+    assert (its, itt) == tuple(g["qeq_iters"])
+    assert np.abs(q - g["q"]).max() <= 1e-12
+
+
+def test_nve_matches_reference_qeq(case):
+    """Five NVE steps whose charges came from the reference's QEq each step
+    (warm s/t histories): positions, velocities, charges, forces."""
+    g, o, f, e = case
+    m = Oracle(o_ffield(o))
+    m.set_system(g["box"], g["x"], g["types"], g["tags"], None, g["v"])
+    em = m.run_nve(int(g["nve_steps"]), float(g["nve_dt"]))
+    x, v, q, f5 = m.state()
+    assert np.abs(x - g["nve_x"]).max() <= 1e-10
+    assert np.abs(v - g["nve_v"]).max() <= 1e-10
+    assert np.abs(q - g["nve_q"]).max() <= 1e-10
+    fr = g["nve_f"]
+    assert np.sqrt(((f5 - fr) ** 2).sum() / (fr ** 2).sum()) < 1e-9
+    ref = dict(zip([str(s) for s in g["energy_names"]], g["nve_energies"]))
+    for k in TERMS:
+        assert abs(em[k] - ref[k]) <= max(1e-9 * abs(ref[k]), 1e-7), (k, em[k], ref[k])

@@ -1,7 +1,9 @@
 """The CUDA force step against the golden fixtures of the reference's own
 code (same positions and charges): bond and H-bond lists as sets, corrected
 bond orders within 1e-10, per-term energies within 1e-9 relative, forces
-within 1e-9 relative RMS."""
+within 1e-9 relative RMS.  The CUDA QEq against the charges of the
+reference's own QEq driver (1e-5 e, the charge bar), and 5 NVE steps
+against the fixture's trajectory on the reference's QEq."""
 import glob
 import os
 
@@ -54,3 +56,37 @@ def test_gpu_lists_vs_reference(case):
     for k, v in zip(zip(ti.tolist(), tj.tolist(), im.tolist()), bo):
         np.testing.assert_allclose(v, ref[k], rtol=1e-10, atol=1e-13)
     assert keyset(*gpu.hbond_list()) == keyset(g["hb_ti"], g["hb_tj"], g["hb_img"])
+
+
+@pytest.mark.parametrize("path", FIXTURES, ids=[os.path.basename(f)[:-4] for f in FIXTURES])
+def test_gpu_qeq_vs_reference(path, ffield):
+    g = dict(np.load(path))
+    gpu = ReaxGPU(ffield)
+    gpu.set_box(g["box"])
+    gpu.set_atoms(g["x"], g["types"], g["tags"], None, g["v"])
+    q, its, itt = gpu.qeq()
+    assert np.abs(q - g["q"]).max() < 1e-5
+    assert abs(q.sum()) < 1e-9 * len(q)
+    # same CG from the same guesses: iteration counts within one of the
+    # reference's (the reduction order of the dot products differs)
+    assert abs(its - int(g["qeq_iters"][0])) <= 1 and abs(itt - int(g["qeq_iters"][1])) <= 1
+
+
+@pytest.mark.parametrize("path", FIXTURES, ids=[os.path.basename(f)[:-4] for f in FIXTURES])
+def test_gpu_nve_vs_reference(path, ffield):
+    g = dict(np.load(path))
+    gpu = ReaxGPU(ffield)
+    gpu.set_box(g["box"])
+    gpu.set_atoms(g["x"], g["types"], g["tags"], None, g["v"])
+    e = gpu.run(int(g["nve_steps"]), float(g["nve_dt"]))
+    x, v, q, f = gpu.get_atoms()
+    box = g["box"]
+    dx = x - g["nve_x"]
+    dx -= box * np.round(dx / box)
+    assert np.abs(dx).max() < 1e-7
+    assert np.abs(v - g["nve_v"]).max() < 1e-7
+    assert np.abs(q - g["nve_q"]).max() < 1e-5
+    ref = dict(zip([str(s) for s in g["energy_names"]], g["nve_energies"]))
+    etot = e["eng_vdwl"] + e["eng_coul"]
+    etot_r = ref["eng_vdwl"] + ref["eng_coul"]
+    assert abs(etot - etot_r) < 1e-6 * abs(etot_r)

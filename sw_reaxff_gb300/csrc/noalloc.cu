@@ -6,7 +6,9 @@
 // where a device allocation would synchronize or fail.  The caller owns the
 // input and output device arrays; the QEq matrix H is evaluated on the fly
 // (never stored) and the CG work vectors live in one static device array of
-// fixed size, RG_NOALLOC_MAX_ATOMS atoms.
+// fixed size, RG_NOALLOC_MAX_ATOMS atoms.  Positions may lie outside the
+// box: the first kernel wraps them into [0, L) (in the scratch array), as
+// rg_set_atoms does for the main path.
 //
 // The scratch array is shared by every call on a device and keeps the
 // previous call's contents; each call clears what it needs.  Calls whose
@@ -15,6 +17,7 @@
 // The mathematics is that of rg_qeq's first solve after rg_set_atoms (zero
 // initial guesses): dual pipelined Jacobi-PCG of CG_v2
 // (fix_qeq_reax_sunway.cpp:983-1167) and calculate_Q (:1697-1755).
+#include <cmath>
 #include <cstdio>
 #include <string>
 
@@ -25,22 +28,22 @@ namespace {
 
 constexpr unsigned FULL = 0xffffffffu;
 constexpr int NMAX = RG_NOALLOC_MAX_ATOMS;
-// 12 double2 vectors + Jacobi diagonal + 128 scalars
-constexpr size_t NA_DOUBLES = 24 * (size_t)NMAX + NMAX + 128;
+// 12 double2 vectors + Jacobi diagonal + 128 scalars + wrapped positions
+constexpr size_t NA_DOUBLES = 24 * (size_t)NMAX + NMAX + 128 + 3 * (size_t)NMAX;
 
 __device__ __align__(256) double rg_noalloc_scratch[NA_DOUBLES];
 
 // scalar slots (pairs [s, t]) in the last 128 doubles
 enum {
   S_ACC0 = 0, S_ACC1 = 2, S_ALPHA = 6, S_ALPHA_OLD = 8, S_BETA = 10, S_SIG = 12,
-  S_HETA = 14, S_BNORM = 16, S_ACTIVE = 20, S_ITERS = 22, S_SUM = 24, S_INIT = 32,
-  S_NEXT = 52
+  S_HETA = 14, S_BNORM = 16, S_ACTIVE = 20, S_ITERS = 22, S_SUM = 24, S_BAD = 26,
+  S_INIT = 32, S_NEXT = 52
 };
 
 struct View {
   int n;
   double2 *x, *b, *r, *u, *w, *d, *q, *p, *s, *v, *z, *m;
-  double *hdi, *R;
+  double *hdi, *R, *xw;
 };
 
 View make_view(double *base, int n) {
@@ -51,6 +54,7 @@ View make_view(double *base, int n) {
   for (int k = 0; k < 12; ++k) *slots[k] = vec + (size_t)k * NMAX;
   V.hdi = base + 24 * (size_t)NMAX;
   V.R = base + 25 * (size_t)NMAX;
+  V.xw = V.R + 128;
   return V;
 }
 
@@ -86,10 +90,35 @@ struct Geo {
   int k[3];          // image range per dimension
 };
 
-__global__ void k_na_setup(View V, const int *type, const ForceField *ff) {
+// x - L floor(x / L), rounded per operation like the main path's binning
+__device__ __forceinline__ double na_wrap(double x, double L) {
+  double y = __dsub_rn(x, __dmul_rn(L, floor(__ddiv_rn(x, L))));
+  if (y >= L) y = __dsub_rn(y, L);
+  if (y < 0.0) y = 0.0;
+  return y;
+}
+
+// Jacobi diagonal, right-hand sides, zero guesses, wrapped positions; a
+// non-finite position or a type outside the force field sets R[S_BAD] and
+// leaves the atom out (the host then rejects the call)
+__global__ void k_na_setup(View V, Geo G, const ForceField *ff) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= V.n) return;
-  const Sbp &sb = ff->sbp[type[i]];
+  const int ti = G.type[i];
+  const double x0 = G.x[3 * i], y0 = G.x[3 * i + 1], z0 = G.x[3 * i + 2];
+  const bool ok = ti >= 0 && ti < ff->ntypes && isfinite(x0) && isfinite(y0) && isfinite(z0);
+  if (!ok) {
+    V.R[S_BAD] = 1.0;
+    V.hdi[i] = 0.0;
+    V.b[i] = make_double2(0.0, 0.0);
+    V.x[i] = make_double2(0.0, 0.0);
+    V.xw[3 * i] = V.xw[3 * i + 1] = V.xw[3 * i + 2] = 0.0;
+    return;
+  }
+  V.xw[3 * i] = na_wrap(x0, G.L[0]);
+  V.xw[3 * i + 1] = na_wrap(y0, G.L[1]);
+  V.xw[3 * i + 2] = na_wrap(z0, G.L[2]);
+  const Sbp &sb = ff->sbp[ti];
   V.hdi[i] = 1. / sb.eta;
   V.b[i] = make_double2(-sb.chi, -1.0);
   V.x[i] = make_double2(0.0, 0.0);
@@ -102,13 +131,13 @@ __global__ void __launch_bounds__(256) k_na_matvec(View V, Geo G, const ForceFie
   const int lane = threadIdx.x & 31;
   const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   if (i >= V.n) return;
-  const double xi = G.x[3 * i], yi = G.x[3 * i + 1], zi = G.x[3 * i + 2];
+  const double xi = V.xw[3 * i], yi = V.xw[3 * i + 1], zi = V.xw[3 * i + 2];
   const int ti = G.type[i];
   const double swb2 = ctl->swb2;
   const double *T = ctl->qTap;
   double as = 0.0, at = 0.0;
   for (int j = lane; j < V.n; j += 32) {
-    const double xj = G.x[3 * j], yj = G.x[3 * j + 1], zj = G.x[3 * j + 2];
+    const double xj = V.xw[3 * j], yj = V.xw[3 * j + 1], zj = V.xw[3 * j + 2];
     const double shld = ff->tbp[ti][G.type[j]].gamma;
     const double2 vj = in[j];
     for (int sz = -G.k[2]; sz <= G.k[2]; ++sz)
@@ -288,6 +317,23 @@ __global__ void k_na_finish(View V, double *q_out) {
 // per-device address of the scratch array (set once per device)
 double *g_scratch[64] = {nullptr};
 
+// restores the caller's current device on every return
+struct DeviceRestore {
+  int prev = -1;
+  ~DeviceRestore() {
+    if (prev >= 0) cudaSetDevice(prev);
+  }
+};
+
+int na_fail(rg_system *h, int code, const std::string &msg) {
+  rg_set_error(h, "rg_qeq_noalloc: " + msg);
+  return code;
+}
+
+int na_cuda(rg_system *h, cudaError_t e, const char *what) {
+  return na_fail(h, RG_E_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
 }  // namespace
 
 // The handle supplies only the force-field and control tables it copied to
@@ -295,47 +341,59 @@ double *g_scratch[64] = {nullptr};
 extern "C" int rg_qeq_noalloc(rg_system *h, int n, const double *x, const int *type,
                               const double *box3, double *q_out, int *iters_s, int *iters_t,
                               void *stream) {
-  if (!h || !x || !type || !box3 || !q_out) return RG_E_ARG;
-  if (n < 1 || n > NMAX) {
-    rg_set_error(h, "rg_qeq_noalloc: n must be in [1, " + std::to_string(NMAX) +
-                        "] (static scratch size), got " + std::to_string(n));
-    return RG_E_ARG;
-  }
+  if (!h) return RG_E_ARG;
+  if (!x || !type || !box3 || !q_out)
+    return na_fail(h, RG_E_ARG, "x, type, box3 and q_out must not be NULL");
+  if (n < 1 || n > NMAX)
+    return na_fail(h, RG_E_ARG, "n must be in [1, " + std::to_string(NMAX) +
+                                    "] (static scratch size), got " + std::to_string(n));
   const ForceField *ff = nullptr;
   const Control *ctl = nullptr;
   int device = 0;
   double swb = 0, tol = 0;
   int imax = 0;
   rg_noalloc_tables(h, &ff, &ctl, &device, &swb, &tol, &imax);
-  if (device < 0 || device >= 64) return RG_E_ARG;
-  cudaStream_t st = (cudaStream_t)stream;
-  if (cudaSetDevice(device) != cudaSuccess) return RG_E_CUDA;
-  if (!g_scratch[device]) {
-    void *p = nullptr;
-    const cudaError_t e = cudaGetSymbolAddress(&p, rg_noalloc_scratch);
-    if (e != cudaSuccess || !p) {
-      rg_set_error(h, std::string("rg_qeq_noalloc: cudaGetSymbolAddress: ") + cudaGetErrorString(e));
-      return RG_E_CUDA;
-    }
-    g_scratch[device] = (double *)p;
-  }
+  if (device < 0 || device >= 64)
+    return na_fail(h, RG_E_ARG, "device index " + std::to_string(device) + " outside [0, 64)");
   Geo G;
   G.x = x;
   G.type = type;
   for (int k = 0; k < 3; ++k) {
-    if (!(box3[k] > 0.0)) {
-      rg_set_error(h, "rg_qeq_noalloc: box edges must be positive");
-      return RG_E_ARG;
-    }
+    // the main path's limit: no edge shorter than half the cutoff, which
+    // also bounds the image range below at ceil(swb / L) <= 2
+    if (!std::isfinite(box3[k]) || !(box3[k] >= 0.5 * swb))
+      return na_fail(h, RG_E_ARG, "box edges must be finite and at least half the QEq cutoff (" +
+                                      std::to_string(0.5 * swb) + " A)");
     G.L[k] = box3[k];
-    G.k[k] = (int)ceil(swb / box3[k]);
+    G.k[k] = (int)std::ceil(swb / box3[k]);
   }
+  DeviceRestore restore;
+  cudaError_t e = cudaGetDevice(&restore.prev);
+  if (e != cudaSuccess) return na_cuda(h, e, "cudaGetDevice");
+  if ((e = cudaSetDevice(device)) != cudaSuccess) return na_cuda(h, e, "cudaSetDevice");
+  if (!g_scratch[device]) {
+    void *p = nullptr;
+    e = cudaGetSymbolAddress(&p, rg_noalloc_scratch);
+    if (e != cudaSuccess || !p) return na_cuda(h, e, "cudaGetSymbolAddress");
+    g_scratch[device] = (double *)p;
+  }
+  cudaStream_t st = (cudaStream_t)stream;
   View V = make_view(g_scratch[device], n);
   // scalars start from zero on every call
-  if (cudaMemsetAsync(V.R, 0, 128 * sizeof(double), st) != cudaSuccess) return RG_E_CUDA;
+  if ((e = cudaMemsetAsync(V.R, 0, 128 * sizeof(double), st)) != cudaSuccess)
+    return na_cuda(h, e, "cudaMemsetAsync");
   const int B = 256, Gr = (n + B - 1) / B;
   const unsigned Gw = (unsigned)(((long long)n * 32 + 255) / 256);
-  k_na_setup<<<Gr, B, 0, st>>>(V, type, ff);
+  k_na_setup<<<Gr, B, 0, st>>>(V, G, ff);
+  // the products index the parameter tables by every partner's type: check
+  // the inputs before the first one
+  double bad = 0.0;
+  if ((e = cudaMemcpyAsync(&bad, V.R + S_BAD, sizeof(double), cudaMemcpyDeviceToHost, st)) !=
+          cudaSuccess ||
+      (e = cudaStreamSynchronize(st)) != cudaSuccess)
+    return na_cuda(h, e, "input check");
+  if (bad != 0.0)
+    return na_fail(h, RG_E_ARG, "a position is not finite or a type is outside the force field");
   k_na_matvec<<<Gw, 256, 0, st>>>(V, G, ff, ctl, V.x, V.q);
   k_na_init1<<<Gr, B, 0, st>>>(V);
   k_na_matvec<<<Gw, 256, 0, st>>>(V, G, ff, ctl, V.d, V.q);
@@ -346,15 +404,12 @@ extern "C" int rg_qeq_noalloc(rg_system *h, int n, const double *x, const int *t
   double flags[4];
   int done = 0;
   for (;;) {
-    if (cudaMemcpyAsync(flags, V.R + S_ACTIVE, 4 * sizeof(double), cudaMemcpyDeviceToHost, st) !=
-            cudaSuccess ||
-        cudaStreamSynchronize(st) != cudaSuccess)
-      return RG_E_CUDA;
+    if ((e = cudaMemcpyAsync(flags, V.R + S_ACTIVE, 4 * sizeof(double), cudaMemcpyDeviceToHost,
+                             st)) != cudaSuccess ||
+        (e = cudaStreamSynchronize(st)) != cudaSuccess)
+      return na_cuda(h, e, "CG control read");
     if (flags[0] == 0.0 && flags[1] == 0.0) break;
-    if (done > imax + 8) {
-      rg_set_error(h, "rg_qeq_noalloc: iteration control lost");
-      return RG_E_NUMERIC;
-    }
+    if (done > imax + 8) return na_fail(h, RG_E_NUMERIC, "iteration control lost");
     for (int k = 0; k < 4; ++k) {
       k_na_A<<<Gr, B, 0, st>>>(V);
       k_na_matvec<<<Gw, 256, 0, st>>>(V, G, ff, ctl, V.d, V.q);
@@ -366,8 +421,8 @@ extern "C" int rg_qeq_noalloc(rg_system *h, int n, const double *x, const int *t
   }
   k_na_sums<<<Gr, B, 0, st>>>(V);
   k_na_finish<<<Gr, B, 0, st>>>(V, q_out);
-  if (cudaGetLastError() != cudaSuccess) return RG_E_CUDA;
-  if (cudaStreamSynchronize(st) != cudaSuccess) return RG_E_CUDA;
+  if ((e = cudaGetLastError()) != cudaSuccess) return na_cuda(h, e, "kernel launch");
+  if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return na_cuda(h, e, "final sync");
   if (iters_s) *iters_s = (int)flags[2];
   if (iters_t) *iters_t = (int)flags[3];
   return RG_OK;

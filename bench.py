@@ -36,20 +36,22 @@ UNIT = "atom-steps/s"
 DT = 0.25          # fs
 SEED = 7
 
-# Per-unit FP64 FLOP (2*dfma + dmul + dadd, SASS thread-instruction counts)
-# and DRAM bytes (dram__bytes_read + write) of the kernels that can dominate
-# the FP64 step, from one ncu capture of the 52,428-atom case of the same
-# mixture (`--scale 0.05`; the nonbonded kernel's force-only variant, which
-# the timed steps run): per directed pair for the pair-list build, per
-# unordered pair for the nonbonded kernel, per list entry for one QEq SpMV
-# (two systems).  bench.py multiplies them by
-# the units of the measured workload; traffic scales with the units because
-# every kernel streams its list once.
+# Per-unit figures of the kernels that can dominate the FP64 step.  FLOP
+# (2*dfma + dmul + dadd, SASS thread-instruction counts) and DRAM bytes
+# (dram__bytes_read + write) are from one ncu capture of the 52,428-atom
+# case of the same mixture (`--scale 0.05`; the nonbonded kernel's
+# force-only variant, which the timed steps run); the algorithmic bytes are
+# the compulsory traffic of the canonical layout: per unordered pair one
+# 4-byte index (+ the 8-byte H value where the kernel produces or reads H),
+# plus per-atom position/charge/type reads and result writes.  Units: per
+# directed pair for the pair-list build, per unordered pair for the
+# nonbonded kernel, per list entry for one QEq SpMV (both systems).
 FP64_PER_UNIT = {
-    # phase: (kernel, unit, FLOP per unit, DRAM bytes per unit)
-    "pair_list+H": ("k_build_nbrs", "directed pair", 23.00, 11.19),
-    "nonbonded": ("k_nonbonded", "unordered pair", 39.97, 16.87),
-    "qeq_spmv": ("k_spmv", "list entry", 4.12, 12.76),
+    # phase: (kernel, unit, FLOP/unit, DRAM bytes/unit, algorithmic bytes/unit,
+    #         algorithmic bytes/atom)
+    "pair_list+H": ("k_build_nbrs", "directed pair", 23.00, 11.19, 6.0, 64.0),
+    "nonbonded": ("k_nonbonded", "unordered pair", 39.97, 16.87, 4.0, 60.0),
+    "qeq_spmv": ("k_spmv", "list entry", 4.12, 12.76, 6.0, 96.0),
 }
 
 
@@ -74,6 +76,11 @@ def parse():
                    help="skip the batched single-point measurement (512 small systems)")
     p.add_argument("--no-serve", action="store_true",
                    help="skip the serving-loop measurement (Poisson request stream)")
+    p.add_argument("--no-water", action="store_true",
+                   help="skip the 6,000-atom water measurement (2,000 H2O, 100 NVE steps)")
+    p.add_argument("--water-cpu", action="store_true",
+                   help="also time the oracle on the full 100 steps of the 6,000-atom water "
+                        "box (single thread, a few minutes)")
     p.add_argument("--batch-systems", type=int, default=512)
     p.add_argument("--serve-requests", type=int, default=300)
     return p.parse_args()
@@ -177,27 +184,29 @@ def measured_peaks():
         return {}
 
 
-def cpu_baseline(cpu_scale: float, procs: int = 1):
-    """The oracle (single-threaded restatement of the reference CPU path) on a
-    bounded sample of the same workload: a smaller periodic box of the same
-    mixture at the same density, one MD force step (QEq + forces)."""
+def cpu_baseline(cpu_scale: float, procs: int = 1, warmup: int = 1, steps: int = 2):
+    """The oracle (single-threaded restatement of the reference CPU path,
+    its QEq equal bit for bit to the reference's own) on bounded samples of
+    the same workload: `procs` processes, each a smaller periodic box of the
+    same mixture at the same density (its own seed) running warm NVE steps
+    -- setup evaluation and `warmup` steps untimed, then `steps` timed steps
+    (initial_integrate, QEq from the extrapolated s/t histories, forces,
+    final_integrate).  Returns (atom-steps/s over all processes, processes,
+    atoms per process)."""
     import multiprocessing as mp
+    jobs = [(cpu_scale, SEED + k, warmup, steps) for k in range(procs)]
     if procs <= 1:
-        n, t = _cpu_sample((cpu_scale, SEED))
-        return n / t, 1, n
-    ctx = mp.get_context("spawn")
-    t0 = time.perf_counter()
-    with ctx.Pool(procs) as pool:
-        res = pool.map(_cpu_sample, [(cpu_scale, SEED + k) for k in range(procs)])
-    wall = time.perf_counter() - t0
-    tot = sum(r[0] for r in res)
-    # per-process compute time excludes interpreter start-up
-    slowest = max(r[1] for r in res)
-    return tot / slowest, procs, tot // procs
+        res = [_cpu_md_sample(jobs[0])]
+    else:
+        with mp.get_context("spawn").Pool(procs) as pool:
+            res = pool.map(_cpu_md_sample, jobs)
+    atoms = sum(r[0] for r in res)
+    slowest = max(r[1] for r in res)          # the processes run side by side
+    return atoms * steps / slowest, procs, res[0][0]
 
 
-def _cpu_sample(arg):
-    cpu_scale, seed = arg
+def _cpu_md_sample(arg):
+    cpu_scale, seed, warmup, steps = arg
     sys.path.insert(0, ROOT)
     from oracle.pyoracle import Oracle
     from sw_reaxff_gb300 import systems
@@ -205,9 +214,9 @@ def _cpu_sample(arg):
     s = systems.mixture(scale=cpu_scale, seed=seed)
     o = Oracle(DEFAULT_FFIELD)
     o.set_system(s.box, s.x, s.types(["C", "H", "O", "N"]), s.tag, None, s.v)
+    o.run_nve(max(warmup, 1), DT)             # setup (cold QEq) + warm-up steps
     t0 = time.perf_counter()
-    o.qeq()
-    o.compute()
+    o.md_steps(steps, DT)
     return s.n, time.perf_counter() - t0
 
 
@@ -316,42 +325,89 @@ def serve_section(args, local):
     return out
 
 
+def water_section(args, local):
+    """2,000 H2O (6,000 atoms) at 1.0 g/cm3, 300 K, 100 NVE steps of 0.25 fs,
+    FP64 (the reference's own CPU-runnable scale): the GPU's 100 steps timed
+    with CUDA events after a 5-step warm-up run, and -- with --water-cpu --
+    the oracle's 100 steps on one thread (setup excluded)."""
+    import torch
+    from sw_reaxff_gb300 import ReaxGPU, systems
+    from sw_reaxff_gb300.api import DEFAULT_FFIELD
+    s = systems.water_box(2000, seed=2024)
+    g = ReaxGPU(DEFAULT_FFIELD, device=local)
+    g.set_system(s)
+    g.run(5, DT, energies=False)
+    g.set_system(s)
+    g.run(0, DT, energies=False)              # setup: QEq from zero guesses + forces
+    st = torch.cuda.ExternalStream(g.stream())
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    g.synchronize()
+    e0.record(st)
+    e = g.run(100, DT)
+    e1.record(st)
+    g.synchronize()
+    t = e0.elapsed_time(e1) / 1e3
+    out = {"workload": "2,000 H2O, 6,000 atoms, 1.0 g/cm3, 300 K, 100 NVE steps of 0.25 fs, "
+                       "FP64, QEq tol 1e-6",
+           "gpu": {"atom_steps_per_s": s.n * 100 / t, "ms_per_step": t * 10.0,
+                   "cg_iters_last_step": [g.stats()["cg_iters_s"], g.stats()["cg_iters_t"]],
+                   "potential_energy_last": e["eng_vdwl"] + e["eng_coul"]}}
+    g.close()
+    if args.water_cpu:
+        from oracle.pyoracle import Oracle
+        o = Oracle(DEFAULT_FFIELD)
+        o.set_system(s.box, s.x, s.types(["C", "H", "O", "N"]), s.tag, None, s.v)
+        o.run_nve(0, DT)
+        t0 = time.perf_counter()
+        eo = o.md_steps(100, DT)
+        tc = time.perf_counter() - t0
+        out["cpu_oracle_1_thread"] = {"atom_steps_per_s": s.n * 100 / tc, "s_per_step": tc / 100,
+                                      "potential_energy_last": eo["eng_vdwl"] + eo["eng_coul"]}
+        out["speedup_gpu_vs_cpu"] = out["gpu"]["atom_steps_per_s"] / \
+            out["cpu_oracle_1_thread"]["atom_steps_per_s"]
+    return out
+
+
 def workload_name(n, mixed=False):
     return (f"H2O/CH4/C2H6/NH3 0.5/0.2/0.2/0.1 mixture, {n} atoms, "
             "0.8 g/cm3, 300 K, NVE dt 0.25 fs, QEq tol 1e-6, "
             + ("mixed FP32/FP64 form" if mixed else "FP64"))
 
 
+REF_SAMPLE_SCALE = 0.01      # 10,486-atom boxes of the mixture per process
+
+
 def reference_arm(args):
-    """--impl reference: the reference's CPU algorithm (the oracle port; the
-    reference itself needs LAMMPS and the Sunway toolchain) on all host
-    cores, each process a bounded sample of the workload per step."""
+    """--impl reference: the reference's CPU algorithm on all host cores.
+    The reference itself needs LAMMPS and the Sunway toolchain, so this is
+    the oracle port (force-step routines checked against the reference's own
+    compiled CPU branches, QEq equal bit for bit to the reference's own
+    pre_force).  Every process runs one bounded sample of the workload -- a
+    10,486-atom box of the same mixture -- through warm NVE steps: setup and
+    W warm-up steps untimed, K steps timed."""
     dist = Dist("gloo")
     if dist.rank != 0:
         dist.close()
         return
     procs = os.cpu_count() or 1
-    vals = []
-    for _ in range(args.warmup):
-        pass  # the oracle has no warm-up state worth timing
     t0 = time.perf_counter()
-    for _ in range(max(1, args.steps)):
-        v, cores, sample = cpu_baseline(args.cpu_scale, procs)
-        vals.append(v)
-    value = float(np.mean(vals))
+    value, cores, sample = cpu_baseline(REF_SAMPLE_SCALE, procs, max(args.warmup, 1),
+                                        max(1, args.steps))
+    total = sample * procs
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 0, "impl": "reference",
         "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        # the GPU arm's workload; each step times a bounded sample of it
-        "config": {"workload": workload_name(1048576 if args.scale == 1.0 else
-                                             int(round(1048576 * args.scale))),
-                   "atoms": 1048576 if args.scale == 1.0 else int(round(1048576 * args.scale)),
-                   "parallelism": f"{procs} CPU processes",
+        "config": {"workload": f"{procs} independent {sample}-atom boxes of the "
+                               "H2O/CH4/C2H6/NH3 0.5/0.2/0.2/0.1 mixture, 0.8 g/cm3, 300 K, "
+                               "NVE dt 0.25 fs, QEq tol 1e-6, FP64, warm steps",
+                   "atoms": total, "parallelism": f"{procs} CPU processes",
                    "sample_atoms_per_process": sample, "processes": procs},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": procs, "kind": "port",
-                         "sample": f"{procs} processes x one QEq+force step of a "
-                                   f"{sample}-atom box of the same mixture"},
+                         "sample": f"{procs} processes x {args.steps} warm NVE steps of a "
+                                   f"{sample}-atom box of the same mixture (setup and "
+                                   f"{max(args.warmup, 1)} warm-up steps untimed)"},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "wall_s": time.perf_counter() - t0,
     }
@@ -384,9 +440,11 @@ def gpu_arm(args):
     g.synchronize()
     prof = g.profile_get()
     g.profile(False)
-    # the roofline kernel: the larger of the two force-step kernels with
-    # ncu-counted FP64 work; the timed steps carry events around it alone
-    dom = max(("pair_list+H", "nonbonded"), key=lambda k: prof[k][0])
+    # the roofline kernel: the step's largest phase among those with
+    # per-unit figures (the QEq SpMV included); the timed steps carry events
+    # around it alone (for the SpMV the CG iterations then run as plain
+    # launches instead of their CUDA graph)
+    dom = max(FP64_PER_UNIT, key=lambda k: prof.get(k, (0.0, 0))[0])
     stream = torch.cuda.ExternalStream(g.stream())
     ev0 = torch.cuda.Event(enable_timing=True)
     ev1 = torch.cuda.Event(enable_timing=True)
@@ -395,7 +453,8 @@ def gpu_arm(args):
     g.synchronize()
     torch.cuda.synchronize()
     clocks.start()
-    launches0 = g.stats()["kernel_launches"]
+    st0 = g.stats()
+    launches0 = st0["kernel_launches"]
     g.profile(True, phases=[dom])
     ev0.record(stream)
     g.run(args.steps, DT, energies=False)
@@ -481,32 +540,62 @@ def gpu_arm(args):
         mixed["errors_vs_fp64"] = {
             "force_rel_rms": float(np.sqrt(((f32 - f64) ** 2).sum() / (f64 ** 2).sum())),
             "charge_max_abs": float(np.abs(q32 - q64).max()),
-            "energy_rel": {k: float(abs(e32[k] - e64[k]) / abs(e64[k]))
-                           for k in e64 if e64[k] != 0.0},
+            "energy_rel_max": max(float(abs(e32[k] - e64[k]) / abs(e64[k]))
+                                  for k in e64 if e64[k] != 0.0),
             "qeq_restarts": gm.stats()["qeq_restarts"],
             "bars": {"force_rel_rms": 1e-4, "charge_max_abs": 1e-5}}
         gm.close()
 
-    # roofline of the dominant force-step kernel (bound by the FP64 units),
-    # its launch time measured with CUDA events in the timed steps
+    # roofline of the dominant kernel, its launch time measured with CUDA
+    # events in the timed steps: against the FP64 rate (FMA probe run here)
+    # and against HBM (MEASURED_PEAKS.json); the binding one is reported
     fp64_peak = measure_fp64_peak(local)
+    peaks = measured_peaks()
+    hbm_peak = peaks.get("hbm_gbs")
     phases = {k: v for k, v in prof.items() if v[1] > 0}
     tot_ms = sum(v[0] for v in phases.values())
-    kname, uname, flop_u, bytes_u = FP64_PER_UNIT[dom]
+    kname, uname, flop_u, bytes_u, alg_u, alg_atom = FP64_PER_UNIT[dom]
     units = st["n_pairs"] / 2 if dom == "nonbonded" else st["n_pairs"]
     avg_ms = live[0] / max(live[1], 1)
-    ach = flop_u * units / (avg_ms * 1e-3) / 1e12
+    if dom == "qeq_spmv":
+        # a CG SpMV launch updates the systems still iterating: two DFMA
+        # per entry for each (one system after the other has converged),
+        # and a launch with none left returns at once.  FLOP and bytes are
+        # summed over the timed region and divided by the summed time.
+        sys_iters = st["cg_system_iters"] - st0["cg_system_iters"]
+        passes = st["cg_spmv_rows_passes"] - st0["cg_spmv_rows_passes"]
+        fp64_ach = 4.0 * units * sys_iters / (live[0] * 1e-3) / 1e12
+        alg_bytes = (alg_u * units + alg_atom * n) * passes / max(live[1], 1)
+        flop_note = (f"4 FLOP (2 DFMA) per entry per system still iterating: "
+                     f"{sys_iters} system-SpMVs in {live[1]} launches "
+                     f"({passes} with work)")
+    else:
+        fp64_ach = flop_u * units / (avg_ms * 1e-3) / 1e12
+        alg_bytes = alg_u * units + alg_atom * n
+        flop_note = "ncu-counted FP64 FLOP per unit (52,428-atom capture) x units"
+    hbm_ach = alg_bytes / (avg_ms * 1e-3) / 1e9
+    fp64_frac = fp64_ach / fp64_peak
+    hbm_frac = hbm_ach / hbm_peak if hbm_peak else None
+    bind_fp64 = hbm_frac is None or fp64_frac >= hbm_frac
     roof = {"kernel": kname, "phase": dom, "share": phases[dom][0] / tot_ms if tot_ms else None,
-            "bound": "fp64", "achieved": ach, "peak": fp64_peak, "unit": "TFLOP/s",
-            "frac": ach / fp64_peak, "traffic": bytes_u * units,
+            "bound": "fp64" if bind_fp64 else "hbm",
+            "achieved": fp64_ach if bind_fp64 else hbm_ach,
+            "peak": fp64_peak if bind_fp64 else hbm_peak,
+            "unit": "TFLOP/s" if bind_fp64 else "GB/s",
+            "frac": fp64_frac if bind_fp64 else hbm_frac,
+            "traffic": bytes_u * units,
+            "fp64": {"achieved_tflops": fp64_ach, "peak_tflops": fp64_peak, "frac": fp64_frac,
+                     "flop_count": flop_note,
+                     "peak_source": "FP64 FMA probe measured in this run (MEASURED_PEAKS.json "
+                                    "has no FP64 figure)"},
+            "hbm": {"algorithmic_bytes": alg_bytes, "achieved_gbs": hbm_ach,
+                    "peak_gbs": hbm_peak, "frac": hbm_frac,
+                    "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)"},
             "units_per_launch": units, "unit_of_work": uname, "flop_per_unit": flop_u,
             "avg_launch_ms": avg_ms, "launches_timed": live[1],
-            "peak_source": "FP64 FMA probe measured in this run (MEASURED_PEAKS.json has "
-                           "no FP64 figure); traffic scaled from the 52,428-atom ncu capture",
-            "hbm_gbs_achieved": bytes_u * units / (avg_ms * 1e-3) / 1e9}
+            "traffic_source": "ncu DRAM bytes per unit of the 52,428-atom capture x units"}
     if main_mixed:
         roof = None   # the per-unit FP64 counts are the FP64 kernels
-    peaks = measured_peaks()
 
     line = {
         "metric": METRIC_MIXED if main_mixed else METRIC, "value": value, "unit": UNIT,
@@ -530,15 +619,27 @@ def gpu_arm(args):
         "hbm_peak_gbs": peaks.get("hbm_gbs"),
     }
     line["gpu_launches"] = int(launches)
+    if rank == 0 and not args.no_water:
+        line["water6k"] = water_section(args, local)
     if rank == 0 and not args.no_batched:
         line["batched"] = batched_section(args, local)
     if rank == 0 and not args.no_serve:
         line["serving"] = serve_section(args, local)
     if rank == 0 and not args.no_cpu:
-        v, cores, sample = cpu_baseline(args.cpu_scale, 1)
+        v, cores, sample = cpu_baseline(args.cpu_scale, 1, 1, 2)
         line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
-                                "sample": f"one QEq+force step of a {sample}-atom box of the "
-                                          "same mixture, single thread"}
+                                "sample": f"2 warm NVE steps (after setup and 1 untimed step) "
+                                          f"of a {sample}-atom box of the same mixture, "
+                                          "single thread"}
+    if mixed is not None:
+        # the mixed form's headline figures, last, where a reader of the
+        # line's tail sees them
+        err = mixed.get("errors_vs_fp64", {})
+        line["mixed_summary"] = {"metric": METRIC_MIXED, "value": mixed["value"], "unit": UNIT,
+                                 "ms_per_step": mixed["ms_per_step"],
+                                 "speedup_vs_fp64": mixed["speedup_vs_fp64"],
+                                 "force_rel_rms_vs_fp64": err.get("force_rel_rms"),
+                                 "charge_max_abs_vs_fp64": err.get("charge_max_abs")}
     if rank == 0:
         print(json.dumps(line), flush=True)
     g.close()

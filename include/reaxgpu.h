@@ -110,6 +110,14 @@ typedef struct {
                                   FP64 passes (near-linear, over-coordinated) */
   int cell_div, spmv_rows;     /* the configuration in use (autotuned): cells
                                   of cutoff/cell_div, SpMV lanes per row */
+  long long cg_system_iters;   /* since rg_create: CG loop iterations summed
+                                  over the QEq calls and their two systems
+                                  (each is one system's SpMV over the matrix;
+                                  per call: (iters_s - 1) + (iters_t - 1),
+                                  the slowest segment's counts) */
+  long long cg_spmv_rows_passes; /* since rg_create: CG loop SpMV launches
+                                  that had a system to update (per call:
+                                  max(iters_s, iters_t) - 1) */
 } rg_stats;
 
 void rg_default_params(rg_params *p);
@@ -259,12 +267,18 @@ int rg_profile_phases(rg_system *h, unsigned mask);
  * RG_NOALLOC_MAX_ATOMS atoms: H is evaluated on the fly and the CG vectors
  * live in one static device array of that size, held by every GPU that loads
  * the library until exit.  Inputs and output are the caller's device arrays:
- * x[3n] (wrapped into the box), type[n], q_out[n]; box3 is a host array;
- * stream is a cudaStream_t (NULL: legacy default stream).  h only supplies
- * the force-field tables copied at rg_create.  The first call on a device
- * looks up the array's device address (cudaGetSymbolAddress); make it before
- * any stream capture.  All calls share the array and leave their contents in
- * it; calls whose GPU work overlaps race.  Larger n is rejected (RG_E_ARG). */
+ * x[3n] (positions anywhere; wrapped into the box like rg_set_atoms),
+ * type[n] (0 <= type < the force field's element count), q_out[n]; box3 is
+ * a host array of orthogonal edges, each finite and at least half the QEq
+ * cutoff; stream is a cudaStream_t (NULL: legacy default stream).  h only
+ * supplies the force-field tables copied at rg_create.  The call runs on
+ * h's device and restores the caller's current device before it returns.
+ * The first call on a device looks up the array's device address
+ * (cudaGetSymbolAddress); make it before any stream capture.  All calls share
+ * the array and leave their contents in it; calls whose GPU work overlaps
+ * race.  Larger n, a short or non-finite edge, a non-finite position or a
+ * type outside the force field is rejected (RG_E_ARG, with a message in
+ * rg_last_error) before any product is formed. */
 #define RG_NOALLOC_MAX_ATOMS 8192
 int rg_qeq_noalloc(rg_system *h, int n, const double *x, const int *type,
                    const double *box3, double *q_out, int *iters_s,

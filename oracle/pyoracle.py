@@ -86,6 +86,7 @@ def _declare(L):
         L.ro_qeq.argtypes = [C.c_void_p, P(C.c_double), P(C.c_int), P(C.c_int)]
         L.ro_compute.argtypes = [C.c_void_p, P(C.c_double), P(C.c_double)]
         L.ro_run_nve.argtypes = [C.c_void_p, C.c_int, C.c_double, P(C.c_double)]
+        L.ro_md_steps.argtypes = [C.c_void_p, C.c_int, C.c_double, P(C.c_double)]
         L.ro_get_state.argtypes = [C.c_void_p] + [P(C.c_double)] * 4
         L.ro_get_stats.argtypes = [C.c_void_p, P(Stats)]
         for f in ("ro_dump_far", "ro_dump_hbonds"):
@@ -193,6 +194,12 @@ class Oracle:
     def run_nve(self, nsteps, dt):
         e = np.zeros(NENERGY)
         self.L.ro_run_nve(self.h, nsteps, dt, _dp(e))
+        return dict(zip(ENERGY_NAMES, e))
+
+    def md_steps(self, nsteps, dt):
+        """nsteps more NVE steps from the current state (after run_nve)."""
+        e = np.zeros(NENERGY)
+        self.L.ro_md_steps(self.h, nsteps, dt, _dp(e))
         return dict(zip(ENERGY_NAMES, e))
 
     def state(self):

@@ -2018,10 +2018,14 @@ int ro_qeq(ro_ctx *c, double *q_out, int *iters_s, int *iters_t) {
  * (QEq) -> compute -> final_integrate */
 
 int ro_run_nve(ro_ctx *c, int nsteps, double dt, double *energies_last) {
-  int step, i, d;
-  const double dtf = 0.5 * dt * FTM2V;
   ro_qeq(c, NULL, NULL, NULL);
   ro_compute(c, NULL, energies_last);
+  return ro_md_steps(c, nsteps, dt, energies_last);
+}
+
+int ro_md_steps(ro_ctx *c, int nsteps, double dt, double *energies_last) {
+  int step, i, d;
+  const double dtf = 0.5 * dt * FTM2V;
   for (step = 0; step < nsteps; step++) {
     double t0 = now_s();
     for (i = 0; i < c->n; i++) {

@@ -79,6 +79,9 @@ int ro_compute(ro_ctx *c, double *f_out, double *energies);
 /* NVE velocity Verlet over nsteps (setup: qeq + compute, then per step:
  * initial_integrate, qeq, compute, final_integrate), dt in fs, real units. */
 int ro_run_nve(ro_ctx *c, int nsteps, double dt, double *energies_last);
+/* nsteps more NVE steps continuing from the current state (forces, charges
+ * and QEq histories of the previous step; no setup evaluation) */
+int ro_md_steps(ro_ctx *c, int nsteps, double dt, double *energies_last);
 
 void ro_get_state(const ro_ctx *c, double *x, double *v, double *q,
                   double *f);

@@ -55,7 +55,8 @@ class Stats(C.Structure):
                 ("max_bonds", C.c_int), ("max_hbonds", C.c_int),
                 ("regrows", C.c_int), ("kernel_launches", C.c_longlong),
                 ("qeq_restarts", C.c_int), ("fp64_angles", C.c_int),
-                ("fp64_torsions", C.c_int), ("cell_div", C.c_int), ("spmv_rows", C.c_int)]
+                ("fp64_torsions", C.c_int), ("cell_div", C.c_int), ("spmv_rows", C.c_int),
+                ("cg_system_iters", C.c_longlong), ("cg_spmv_rows_passes", C.c_longlong)]
 
 
 class ReaxError(RuntimeError):

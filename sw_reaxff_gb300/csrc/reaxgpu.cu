@@ -709,6 +709,8 @@ int do_qeq(rg_system *h, int *its, int *itt) {
   h->seg_iters.swap(tot);
   h->stats.cg_iters_s = ms;
   h->stats.cg_iters_t = mt;
+  h->stats.cg_system_iters += std::max(ms - 1, 0) + std::max(mt - 1, 0);
+  h->stats.cg_spmv_rows_passes += std::max(std::max(ms, mt) - 1, 0);
   h->stats.qeq_restarts = refines;
   if (its) *its = ms;
   if (itt) *itt = mt;

@@ -1,0 +1,162 @@
+"""Parity at the sizes of the benchmark workloads, and after a capacity
+regrow (FP64 form).
+
+* 2,000 H2O (6,000 atoms, 1.0 g/cm^3), 100 NVE steps of 0.25 fs: lists
+  bit-exact against the live oracle at step 0 and at step 100 (the oracle
+  given the GPU's step-100 positions and charges), per-term energies at
+  the 1e-9 bar with the same charges, and the trajectory against the
+  frozen oracle trajectory of tests/golden/traj/water6k_nve100.npz, whose
+  charges come from the reference's own QEq driver every step.
+* A 52,428-atom H2O/CH4/C2H6/NH3 mixture (the 1,048,576-atom mixture at
+  1/20 scale) with cells of cutoff/2 and of cutoff/3: pair, bond and
+  H-bond lists bit-exact, energies and forces at the 1e-9 bars with the
+  oracle's charges, charges within 1e-5 e.
+* A water slab in a box twice its length: the capacities estimated from
+  the mean density are too small for the slab's neighbour and H-bond
+  counts, so the first list build overflows, regrows and re-runs; the
+  results must still equal the oracle's.
+"""
+import os
+
+import numpy as np
+import pytest
+
+from oracle.pyoracle import Oracle
+from sw_reaxff_gb300 import ReaxGPU, systems
+from sw_reaxff_gb300.systems import System
+
+pytestmark = pytest.mark.gpu
+HERE = os.path.dirname(os.path.abspath(__file__))
+TRAJ = os.path.join(HERE, "golden", "traj", "water6k_nve100.npz")
+E_TERMS = ["e_bond", "e_ovun", "e_lp", "e_ang", "e_pen", "e_coa", "e_hb",
+           "e_tor", "e_con", "e_vdW", "e_ele", "e_pol", "eng_vdwl", "eng_coul",
+           "e_pol_phys"]
+
+
+def keys(ti, tj, im):
+    """(tag_i, tag_j, image) entries as sorted int64 keys (tags < 2^20)."""
+    k = (ti.astype(np.int64) << 32) | (tj.astype(np.int64) << 12) | im.astype(np.int64)
+    return np.sort(k)
+
+
+def assert_same_lists(g, o):
+    for name, a, b in (("pair", g.pair_list(), o.far_list()),
+                       ("bond", g.bond_list()[:3], o.bond_list()[:3]),
+                       ("H-bond", g.hbond_list(), o.hbond_list())):
+        ka, kb = keys(*a), keys(*b)
+        assert len(kb) > 0
+        assert len(ka) == len(kb) and np.array_equal(ka, kb), \
+            f"{name} list: {len(np.setdiff1d(ka, kb))} extra, {len(np.setdiff1d(kb, ka))} missing"
+
+
+def assert_energies(eg, eo, rel=1e-9):
+    for k in E_TERMS:
+        assert abs(eg[k] - eo[k]) <= max(rel * abs(eo[k]), 1e-7), (k, eg[k], eo[k])
+
+
+def rel_rms(a, b):
+    return np.sqrt(((a - b) ** 2).sum() / (b ** 2).sum())
+
+
+@pytest.fixture(scope="module")
+def traj():
+    return dict(np.load(TRAJ))
+
+
+def test_water6k_step0_lists_and_energies(traj, ffield):
+    g = ReaxGPU(ffield)
+    o = Oracle(ffield)
+    o.set_system(traj["box"], traj["x0"], traj["types"], traj["tags"], None, traj["v0"])
+    qo, _, _ = o.qeq()
+    fo, eo = o.compute()
+    g.set_box(traj["box"])
+    g.set_atoms(traj["x0"], traj["types"], traj["tags"], qo, traj["v0"])
+    fg, eg = g.compute()
+    assert_same_lists(g, o)
+    assert_energies(eg, eo)
+    assert rel_rms(fg, fo) < 1e-9
+    g.set_atoms(traj["x0"], traj["types"], traj["tags"], None, traj["v0"])
+    qg, _, _ = g.qeq()
+    assert np.abs(qg - qo).max() < 1e-5
+
+
+def test_water6k_nve100(traj, ffield):
+    """100 steps against the oracle's trajectory: positions within 5e-5 A,
+    velocities within 1e-5 A/fs, charges within 1e-5 e (the charge bar),
+    potential energy within 1e-6 relative, forces within 1e-4 relative RMS.
+    The runs differ at the start only in the order of floating-point sums
+    (the QEq's dot products above all, which move the charges by ~1e-7 e),
+    and liquid water amplifies such differences: measured on GB300, 6.8e-6 A
+    after 25 fs.  Everything that must not drift -- the lists, the
+    per-term energies and the forces of a given configuration -- is checked
+    bit-exactly or at 1e-9 on the GPU's own step-100 state below."""
+    g = ReaxGPU(ffield)
+    g.set_box(traj["box"])
+    g.set_atoms(traj["x0"], traj["types"], traj["tags"], None, traj["v0"])
+    e = g.run(int(traj["steps"]), float(traj["dt"]))
+    x, v, q, f = g.get_atoms()
+    box = traj["box"]
+    dx = x - traj["x"]
+    dx -= box * np.round(dx / box)
+    ref = dict(zip([str(s) for s in traj["energy_names"]], traj["energies"]))
+    pe, pe_ref = e["eng_vdwl"] + e["eng_coul"], ref["eng_vdwl"] + ref["eng_coul"]
+    dev = {"x": np.abs(dx).max(), "v": np.abs(v - traj["v"]).max(),
+           "q": np.abs(q - traj["q"]).max(), "pe_rel": abs(pe - pe_ref) / abs(pe_ref),
+           "f_rel_rms": rel_rms(f, traj["f"])}
+    print("water6k 100-step deviations from the oracle:", dev)
+    assert dev["x"] < 5e-5 and dev["v"] < 1e-5, dev
+    assert dev["q"] < 1e-5, dev
+    assert dev["pe_rel"] < 1e-6 and dev["f_rel_rms"] < 1e-4, dev
+
+    # step 100: the oracle on the GPU's own positions and charges
+    o = Oracle(ffield)
+    o.set_system(box, x, traj["types"], traj["tags"], q, v)
+    fo, eo = o.compute()
+    assert_same_lists(g, o)
+    assert_energies(e, eo)
+    assert rel_rms(f, fo) < 1e-9
+
+
+@pytest.fixture(scope="module")
+def mixture52k(ffield):
+    s = systems.mixture(scale=0.05, seed=7)
+    o = Oracle(ffield)
+    o.set_system(s.box, s.x, s.types(["C", "H", "O", "N"]), s.tag, None, s.v)
+    qo = o.qeq()
+    fo, eo = o.compute()
+    return s, o, qo, fo, eo
+
+
+@pytest.mark.parametrize("cell_div", [2, 3])
+def test_mixture52k(mixture52k, ffield, cell_div):
+    s, o, (qo, _, _), fo, eo = mixture52k
+    g = ReaxGPU(ffield, cell_div=cell_div, autotune=0)
+    g.set_system(s)
+    qg, _, _ = g.qeq()
+    assert np.abs(qg - qo).max() < 1e-5
+    g.set_atoms(s.x, s.types(g.elements), s.tag, qo, s.v)
+    fg, eg = g.compute()
+    assert g.stats()["cell_div"] == cell_div
+    assert_same_lists(g, o)
+    assert_energies(eg, eo)
+    assert rel_rms(fg, fo) < 1e-9
+
+
+def test_regrow_water_slab(ffield):
+    w = systems.water_box(500, seed=31)
+    box = w.box * np.array([2.0, 1.0, 1.0])
+    s = System(box=box, x=w.x.copy(), elem=w.elem, tag=w.tag, v=w.v, mol=w.mol)
+    g = ReaxGPU(ffield)
+    g.set_system(s)
+    o = Oracle(ffield)
+    o.set_system(s.box, s.x, s.types(g.elements), s.tag, None, s.v)
+    qo, _, _ = o.qeq()
+    fo, eo = o.compute()
+    qg, _, _ = g.qeq()
+    assert g.stats()["regrows"] > 0
+    assert np.abs(qg - qo).max() < 1e-5
+    g.set_atoms(s.x, s.types(g.elements), s.tag, qo, s.v)
+    fg, eg = g.compute()
+    assert_same_lists(g, o)
+    assert_energies(eg, eo)
+    assert rel_rms(fg, fo) < 1e-9

@@ -558,15 +558,16 @@ def gpu_arm(args):
     units = st["n_pairs"] / 2 if dom == "nonbonded" else st["n_pairs"]
     avg_ms = live[0] / max(live[1], 1)
     if dom == "qeq_spmv":
-        # a CG SpMV launch updates the systems still iterating: two DFMA
-        # per entry for each (one system after the other has converged),
+        # a CG SpMV launch updates the systems still iterating: one DFMA
+        # per entry for each (two while both iterate, one after the other
+        # has converged),
         # and a launch with none left returns at once.  FLOP and bytes are
         # summed over the timed region and divided by the summed time.
         sys_iters = st["cg_system_iters"] - st0["cg_system_iters"]
         passes = st["cg_spmv_rows_passes"] - st0["cg_spmv_rows_passes"]
-        fp64_ach = 4.0 * units * sys_iters / (live[0] * 1e-3) / 1e12
+        fp64_ach = 2.0 * units * sys_iters / (live[0] * 1e-3) / 1e12
         alg_bytes = (alg_u * units + alg_atom * n) * passes / max(live[1], 1)
-        flop_note = (f"4 FLOP (2 DFMA) per entry per system still iterating: "
+        flop_note = (f"2 FLOP (one DFMA) per entry for each system still iterating: "
                      f"{sys_iters} system-SpMVs in {live[1]} launches "
                      f"({passes} with work)")
     else:

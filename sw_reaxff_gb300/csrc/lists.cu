@@ -193,14 +193,23 @@ __global__ void k_gather(Dev d) {
 // -------------------------------------------------------------------
 // pair list (full, both directions) + QEq H values
 //
-// One warp per atom i.  The 5x5x5 stencil is walked as 25 rows of cells
-// along x; a row is one or two runs of consecutive cells, i.e. contiguous
-// ranges of the cell-sorted atoms, so 32 candidates are tested per step
-// (FP32 distance prefilter with a safety margin).  Survivors go to a
-// per-warp shared queue; every full batch of 32 is finished with all lanes
-// busy: exact FP64 distance, list membership, near/far split and the H_ij
-// value, written by ballot compaction (near entries from the front of the
-// row, far entries from the back).
+// One warp per atom i walks the half of the cell stencil at
+// lexicographically non-negative offsets (oz, oy, ox) >= (0, 0, 0), taking
+// in its own cell (offset 0, image 0) only partners j > i: every unordered
+// pair (i, j, image) is found once, by one warp, which evaluates the H_ij
+// value once and writes both directed entries -- (j, image) into row i and
+// (i, -image) into row j.  A row's near and far parts are filled by atomic
+// claims (one per warp batch for row i, one per entry for the partner
+// rows), so the order inside a part depends on scheduling; every consumer
+// sums or filters a row's entries without regard to their order.
+//
+// The walk goes along x in runs of consecutive cells (contiguous ranges of
+// the cell-sorted atoms), 32 candidates per step (FP32 distance prefilter
+// with a safety margin); survivors go to a per-warp shared queue, and every
+// full batch of 32 is finished with all lanes busy: list membership and the
+// near/far split of each direction (from the FP32 (hi, lo) distance, or the
+// exact FP64 distance of that direction within 1e-5 of a cutoff, so each
+// directed entry is decided exactly as the oracle decides it), and H.
 
 constexpr int NB_WARPS = 8;          // warps per block in k_build_nbrs
 constexpr int QCAP = 64;             // queue slots per warp
@@ -210,8 +219,8 @@ struct NbrQueue {
   int img[QCAP];
 };
 
-// finish 32 queued candidates (lanes with q < cnt hold one each)
-// exact (FP64, explicitly rounded) squared distance of a queued entry
+// exact (FP64, explicitly rounded) squared distance from an atom at xi to
+// the image (sx, sy, sz) of sorted atom j
 __device__ __forceinline__ double exact_d2(const Dev &d, int j, int sx, int sy, int sz,
                                           const double4 &xi, const SegGeom &g) {
   double dx, dy, dz;
@@ -219,52 +228,55 @@ __device__ __forceinline__ double exact_d2(const Dev &d, int j, int sx, int sy, 
   return __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
 }
 
-// FP32 tests in the mixed form are taken only when d^2 is more than this
-// relative distance from the cutoff; the FP32 d^2 from df_disp is good to a
-// few 1e-7, so the outcome is the FP64 one
+// the reference's near membership, d <= near_cut, from an exact d^2
+__device__ __forceinline__ bool near_exact(double e2, const Control &C) {
+  if (e2 <= C.near_cut2_lo) return true;
+  if (e2 > C.near_cut2_hi) return false;
+  return __dsqrt_rn(e2) <= C.near_cut;
+}
+
+// FP32 tests are taken only when d^2 is more than this relative distance
+// from the cutoff; the FP32 d^2 from df_disp is good to a few 1e-7, so the
+// outcome is the FP64 one
 constexpr float MARGIN32 = 1e-5f;
 
 template <bool MIXED>
 __device__ __forceinline__ void nbr_flush(const Dev &d, const Control &C, const ForceField &F,
                                           const NbrQueue &Q, int cnt, int lane, int i,
                                           const double4 &xi, const float4 &xif, const float4 &xil,
-                                          int ti, long long row, int cap, const SegGeom &g,
-                                          int &cntN, int &cntF) {
-  bool in = false, near = false;
+                                          int ti, const SegGeom &g) {
+  bool in = false, near = false, in_m = false, near_m = false;
   double d2 = 0.0;
   float d2f = 0.f;
-  int j = 0, img = 0;
+  int j = 0, img = 0, sx = 0, sy = 0, sz = 0;
   if (lane < cnt) {
     j = Q.j[lane];
     img = Q.img[lane];
-    int sx, sy, sz;
     img_unpack(img, &sx, &sy, &sz);
-    // membership from the FP32 (hi, lo) displacement away from the
-    // cutoffs, from the exact FP64 distance within MARGIN32 of them
     const float4 hj = d.xf[j], lj = d.xl[j];
     float dx, dy, dz;
     disp32(g, hj, lj, xif, xil, sx, sy, sz, dx, dy, dz);
     d2f = dx * dx + dy * dy + dz * dz;
     const float lc2 = C.list_cut2_f;
-    if (d2f <= lc2 * (1.f - MARGIN32)) in = true;
-    else if (d2f > lc2 * (1.f + MARGIN32)) in = false;
-    else in = exact_d2(d, j, sx, sy, sz, xi, g) <= C.list_cut2;
+    if (d2f <= lc2 * (1.f - MARGIN32)) {
+      in = in_m = true;
+    } else if (d2f <= lc2 * (1.f + MARGIN32)) {
+      in = exact_d2(d, j, sx, sy, sz, xi, g) <= C.list_cut2;
+      in_m = exact_d2(d, i, -sx, -sy, -sz, d.xs[j], g) <= C.list_cut2;
+    }
     const float nc2 = C.near_cut_f * C.near_cut_f;
     if (MIXED) {
       // near part: conservative (the bond pass tests its own cutoffs)
-      near = d2f <= nc2 * (1.f + MARGIN32);
-    } else if (in) {
-      // FP64 form: the reference's near membership, d <= near_cut exactly
-      if (d2f <= nc2 * (1.f - MARGIN32)) near = true;
-      else if (d2f > nc2 * (1.f + MARGIN32)) near = false;
-      else {
-        const double e2 = exact_d2(d, j, sx, sy, sz, xi, g);
-        if (e2 <= C.near_cut2_lo) near = true;
-        else if (e2 > C.near_cut2_hi) near = false;
-        else near = __dsqrt_rn(e2) <= C.near_cut;
+      near = near_m = d2f <= nc2 * (1.f + MARGIN32);
+    } else if (in || in_m) {
+      if (d2f <= nc2 * (1.f - MARGIN32)) {
+        near = near_m = true;
+      } else if (d2f <= nc2 * (1.f + MARGIN32)) {
+        near = near_exact(exact_d2(d, j, sx, sy, sz, xi, g), C);
+        near_m = near_exact(exact_d2(d, i, -sx, -sy, -sz, d.xs[j], g), C);
       }
     }
-    if (!MIXED && in) {
+    if (!MIXED && (in || in_m)) {
       // r^2 for H: FMA-rounded from the exact displacement (the pair
       // functions are smooth; membership is decided above)
       double ex, ey, ez;
@@ -272,16 +284,24 @@ __device__ __forceinline__ void nbr_flush(const Dev &d, const Control &C, const 
       d2 = fma(ex, ex, fma(ey, ey, ez * ez));
     }
   }
+  // row i: claim the batch's near and far slots with one atomic each
   const unsigned mn = __ballot_sync(FULL, in && near);
   const unsigned mf = __ballot_sync(FULL, in && !near);
-  const int tot = cntN + __popc(mn) + cntF + __popc(mf);
-  if (in && tot <= cap) {
-    const int pos = near ? cntN + __popc(mn & lanemask_lt())
-                         : cap - 1 - (cntF + __popc(mf & lanemask_lt()));
-    double h = 0.0;
-    if (MIXED && d2f <= C.swb2_f) {
+  int baseN = 0, baseF = 0;
+  if (lane == 0) {
+    if (mn) baseN = atomicAdd(&d.n_near[i], __popc(mn));
+    if (mf) baseF = atomicAdd(&d.n_far[i], __popc(mf));
+  }
+  baseN = __shfl_sync(FULL, baseN, 0);
+  baseF = __shfl_sync(FULL, baseF, 0);
+  if (!(in || in_m)) return;
+  const int capN = d.nb_capN, capF = d.nb_cap - d.nb_capN;
+  const int tj = __float_as_int(d.xf[j].w);
+  double h = 0.0;
+  float h32 = 0.f;
+  if (MIXED) {
+    if (d2f <= C.swb2_f) {
       // FP32: factored taper when swa = 0
-      const int tj = __float_as_int(d.xf[j].w);
       const float r = d2f * rsqrtf(d2f);
       float tp;
       if (C.qtap_factored) {
@@ -298,46 +318,52 @@ __device__ __forceinline__ void nbr_flush(const Dev &d, const Control &C, const 
         tp = fmaf(tp, r, T[0]);
       }
       const float x = fmaf(d2f, r, C.nb32[ti][tj].gamma);
-      d.nbr[row + pos] = ((uint32_t)j << 8) | (uint32_t)img;
-      d.hval32[row + pos] = tp * 14.4f * rcbrtf(x);
-    } else if (MIXED) {
-      d.nbr[row + pos] = ((uint32_t)j << 8) | (uint32_t)img;
-      d.hval32[row + pos] = 0.f;
-    } else if (!(C.h_all_listed || d2 <= C.swb2)) {
-      h = 0.0;
-    } else if (C.tab_n && d2f >= C.tab_s0_f) {
-      // FP64 table of H_ij (cubic Hermite in r^2, power basis per interval)
-      const double x = fma(d2, C.tab_inv_ds, C.tab_x0);
-      int k = (int)x;
-      if (k > C.tab_n - 1) k = C.tab_n - 1;
-      const double u = x - (double)k;
-      const int tj = __float_as_int(d.xf[j].w);
-      const double2 *T =
-          reinterpret_cast<const double2 *>(d.tab_h + ((long long)C.tab_pair[ti][tj] * C.tab_n + k) * 4);
-      const double2 c01 = T[0], c23 = T[1];
-      h = fma(fma(fma(c23.y, u, c23.x), u, c01.y), u, c01.x);
-    } else {
-      // H_ij = Tap(r) * 14.4 / (r^3 + shld)^c, c = 0.3333333333333
-      const double r = d2 * rsqrt(d2);
-      const double *T = C.qTap;
-      double tp = fma(T[7], r, T[6]);
-      tp = fma(tp, r, T[5]);
-      tp = fma(tp, r, T[4]);
-      tp = fma(tp, r, T[3]);
-      tp = fma(tp, r, T[2]);
-      tp = fma(tp, r, T[1]);
-      tp = fma(tp, r, T[0]);
-      const int tj = __float_as_int(d.xf[j].w);
-      const double x = fma(d2, r, F.tbp[ti][tj].gamma);
-      h = tp * 14.4 * rpow_third(x, RG_C3_QEQ);
+      h32 = tp * 14.4f * rcbrtf(x);
     }
-    if (!MIXED) {
-      d.nbr[row + pos] = ((uint32_t)j << 8) | (uint32_t)img;
-      d.hval[row + pos] = h;
+  } else if (!(C.h_all_listed || d2 <= C.swb2)) {
+    h = 0.0;
+  } else if (C.tab_n && d2f >= C.tab_s0_f) {
+    // FP64 table of H_ij (cubic Hermite in r^2, power basis per interval)
+    const double x = fma(d2, C.tab_inv_ds, C.tab_x0);
+    int k = (int)x;
+    if (k > C.tab_n - 1) k = C.tab_n - 1;
+    const double u = x - (double)k;
+    const double2 *T =
+        reinterpret_cast<const double2 *>(d.tab_h + ((long long)C.tab_pair[ti][tj] * C.tab_n + k) * 4);
+    const double2 c01 = T[0], c23 = T[1];
+    h = fma(fma(fma(c23.y, u, c23.x), u, c01.y), u, c01.x);
+  } else {
+    // H_ij = Tap(r) * 14.4 / (r^3 + shld)^c, c = 0.3333333333333
+    const double r = d2 * rsqrt(d2);
+    const double *T = C.qTap;
+    double tp = fma(T[7], r, T[6]);
+    tp = fma(tp, r, T[5]);
+    tp = fma(tp, r, T[4]);
+    tp = fma(tp, r, T[3]);
+    tp = fma(tp, r, T[2]);
+    tp = fma(tp, r, T[1]);
+    tp = fma(tp, r, T[0]);
+    const double x = fma(d2, r, F.tbp[ti][tj].gamma);
+    h = tp * 14.4 * rpow_third(x, RG_C3_QEQ);
+  }
+  if (in) {
+    const int p = near ? baseN + __popc(mn & lanemask_lt()) : baseF + __popc(mf & lanemask_lt());
+    if (p < (near ? capN : capF)) {
+      const long long slot = (long long)i * d.nb_cap + (near ? p : capN + p);
+      d.nbr[slot] = ((uint32_t)j << 8) | (uint32_t)img;
+      if (MIXED) d.hval32[slot] = h32;
+      else d.hval[slot] = h;
     }
   }
-  cntN += __popc(mn);
-  cntF += __popc(mf);
+  if (in_m) {
+    const int p = atomicAdd(near_m ? &d.n_near[j] : &d.n_far[j], 1);
+    if (p < (near_m ? capN : capF)) {
+      const long long slot = (long long)j * d.nb_cap + (near_m ? p : capN + p);
+      d.nbr[slot] = ((uint32_t)i << 8) | (uint32_t)img_pack(-sx, -sy, -sz);
+      if (MIXED) d.hval32[slot] = h32;
+      else d.hval[slot] = h;
+    }
+  }
 }
 
 template <bool MIXED>
@@ -360,10 +386,8 @@ __global__ void __launch_bounds__(NB_WARPS * 32) k_build_nbrs(Dev d) {
   // the cell the binning put atom i in (integer decomposition, no FP64)
   const int cl = d.cell_o[d.perm[i]] - g.cell0;
   const int cx = cl % ncx, cy = (cl / ncx) % ncy, cz = cl / (ncx * ncy);
-  const long long row = (long long)i * d.nb_cap;
-  const int cap = d.nb_cap;
   const int nx = ncx;
-  int cntN = 0, cntF = 0, qn = 0;
+  int qn = 0;
   // Orthogonal segments clip the stencil to the cutoff sphere: a row of
   // cells (fixed oy, oz) whose y-z slab is farther from atom i than the
   // cutoff is skipped, and along x only the cells the sphere reaches at the
@@ -371,9 +395,8 @@ __global__ void __launch_bounds__(NB_WARPS * 32) k_build_nbrs(Dev d) {
   // margin; the unwrapped cell indices give the periodic images' places).
   const bool clip = !g.tri;
   const float wy = g.cellw_f[1], wz = g.cellw_f[2], iwx = 1.f / g.cellw_f[0];
-  for (int oz = -S; oz <= S; ++oz) {
+  for (int oz = 0; oz <= S; ++oz) {
     int rz = cz + oz, sz = 0;
-    while (rz < 0) { rz += ncz; --sz; }
     while (rz >= ncz) { rz -= ncz; ++sz; }
     float dz2 = 0.f;
     if (clip) {
@@ -382,11 +405,11 @@ __global__ void __launch_bounds__(NB_WARPS * 32) k_build_nbrs(Dev d) {
       dz2 = dz * dz;
       if (dz2 > cut2f) continue;
     }
-    for (int oy = -S; oy <= S; ++oy) {
+    for (int oy = (oz == 0 ? 0 : -S); oy <= S; ++oy) {
       int ry = cy + oy, sy = 0;
       while (ry < 0) { ry += ncy; --sy; }
       while (ry >= ncy) { ry -= ncy; ++sy; }
-      int ox_lo = -S, ox_hi = S;
+      int ox_lo = (oz == 0 && oy == 0) ? 0 : -S, ox_hi = S;
       if (clip) {
         const float lo = (cy + oy) * wy - xif.y, hi = lo + wy;
         const float dy = lo > 0.f ? lo : (hi < 0.f ? -hi : 0.f);
@@ -413,12 +436,14 @@ __global__ void __launch_bounds__(NB_WARPS * 32) k_build_nbrs(Dev d) {
         // exactly); triclinic: the FP32 translation
         float shxf, shyf, shzf;
         img_vec32(g, sx, sy, sz, shxf, shyf, shzf);
+        // image 0 arises only at offset (0, 0, ox >= 0): there the partners
+        // are the atoms after i (its own cell's later atoms, the next cells)
         const bool self_img = (sx == 0 && sy == 0 && sz == 0);
         const int img = img_pack(sx, sy, sz);
-        for (int base = beg; base < end; base += 32) {
+        for (int base = (self_img ? max(beg, i + 1) : beg); base < end; base += 32) {
           const int j = base + lane;
           bool cand = false;
-          if (j < end && !(self_img && j == i)) {
+          if (j < end) {
             const float4 xjf = d.xf[j];
             const float fx = xjf.x + shxf - xif.x;
             const float fy = xjf.y + shyf - xif.y;
@@ -434,7 +459,7 @@ __global__ void __launch_bounds__(NB_WARPS * 32) k_build_nbrs(Dev d) {
           qn += __popc(mc);
           __syncwarp();
           if (qn >= 32) {
-            nbr_flush<MIXED>(d, C, F, Q, 32, lane, i, xi, xif, xil, ti, row, cap, g, cntN, cntF);
+            nbr_flush<MIXED>(d, C, F, Q, 32, lane, i, xi, xif, xil, ti, g);
             __syncwarp();
             // move the leftover (< 32) to the front of the queue
             const int left = qn - 32;
@@ -455,12 +480,26 @@ __global__ void __launch_bounds__(NB_WARPS * 32) k_build_nbrs(Dev d) {
       }
     }
   }
-  if (qn > 0) nbr_flush<MIXED>(d, C, F, Q, qn, lane, i, xi, xif, xil, ti, row, cap, g, cntN, cntF);
-  if (lane == 0) {
-    d.n_near[i] = cntN;
-    d.n_far[i] = cntF;
-    if (cntN + cntF > cap) atomicOr(&d.status[ST_OVF], OVF_NBR);
-    atomicMax(&d.status[ST_MAXNB], cntN + cntF);
+  if (qn > 0) nbr_flush<MIXED>(d, C, F, Q, qn, lane, i, xi, xif, xil, ti, g);
+}
+
+// after the build: rows whose parts overflowed their capacity, and the
+// largest part sizes (the host regrows to them and re-runs the build)
+__global__ void k_nbr_check(Dev d) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  int nn = 0, nf = 0;
+  if (i < d.n) {
+    nn = d.n_near[i];
+    nf = d.n_far[i];
+  }
+  for (int off = 16; off > 0; off >>= 1) {
+    nn = max(nn, __shfl_down_sync(FULL, nn, off));
+    nf = max(nf, __shfl_down_sync(FULL, nf, off));
+  }
+  if ((threadIdx.x & 31) == 0) {
+    if (nn > d.nb_capN || nf > d.nb_cap - d.nb_capN) atomicOr(&d.status[ST_OVF], OVF_NBR);
+    atomicMax(&d.status[ST_MAXNB], nn);
+    atomicMax(&d.status[ST_MAXNF], nf);
   }
 }
 
@@ -622,7 +661,7 @@ __global__ void __launch_bounds__(NB_WARPS * 32) k_build_bonds(Dev d) {
   const Sbp &si = F.sbp[ti];
   const bool ihb = (si.p_hbond == 1) && C.hbond_cut > 0.0;
   const long long row = (long long)i * d.nb_cap;
-  const int nn = d.n_near[i] < d.nb_cap ? d.n_near[i] : d.nb_cap;
+  const int nn = nbr_near_count(d, i);
   const int n = d.n;
   const SegGeom &g = d.seg[d.seg_s[i]];
   const float4 xil = d.xl[i];
@@ -785,8 +824,12 @@ void launch_build_nbrs(const Dev &d, cudaStream_t st) {
   const int B = NB_WARPS * 32;
   const long long threads = (long long)d.n * 32;
   const unsigned G = (unsigned)((threads + B - 1) / B);
+  // the part counters are claimed atomically by the build
+  cudaMemsetAsync(d.n_near, 0, sizeof(int) * (size_t)d.n, st);
+  cudaMemsetAsync(d.n_far, 0, sizeof(int) * (size_t)d.n, st);
   if (d.mixed) k_build_nbrs<true><<<G, B, 0, st>>>(d);
   else k_build_nbrs<false><<<G, B, 0, st>>>(d);
+  k_nbr_check<<<(d.n + 255) / 256, 256, 0, st>>>(d);
 }
 
 void launch_build_bonds(const Dev &d, cudaStream_t st) {

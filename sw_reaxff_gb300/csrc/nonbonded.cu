@@ -288,9 +288,9 @@ __global__ void __launch_bounds__(NBW * 32, std::is_same<R, double>::value ? 3 :
     const int ti = d.ts[i];
     const SegGeom &g = d.seg[d.seg_s[i]];
     const long long row = (long long)i * d.nb_cap;
-    const int nn = d.n_near[i], nf = d.n_far[i];
-    const int cap = d.nb_cap;
-    const int tot = min(nn + nf, cap);
+    const int nn = nbr_near_count(d, i), nf = nbr_far_count(d, i);
+    const int capN = d.nb_capN;
+    const int tot = nn + nf;
     double fx = 0, fy = 0, fz = 0;
     float fx32 = 0.f, fy32 = 0.f, fz32 = 0.f;   // mixed form: FP32 force sums
     double *fC = d.fC;
@@ -302,7 +302,7 @@ __global__ void __launch_bounds__(NBW * 32, std::is_same<R, double>::value ? 3 :
         bool take = false;
         uint32_t e = 0;
         if (p < tot) {
-          const int slot = p < nn ? p : cap - 1 - (p - nn);
+          const int slot = p < nn ? p : capN + (p - nn);
           e = d.nbr[row + slot];
           const int j = (int)(e >> 8);
           take = j > i || (j == i && (int)(e & 255u) > IMG0);

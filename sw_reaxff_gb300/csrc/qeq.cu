@@ -79,8 +79,8 @@ __global__ void __launch_bounds__(256) k_spmv(Dev d, const double2 *__restrict__
   const int i = (int)(tid / RW);
   const bool valid = i < d.n;     // no early return: the row group shuffles
   const long long row = (long long)i * d.nb_cap;
-  const int nn = valid ? d.n_near[i] : 0, nf = valid ? d.n_far[i] : 0, cap = d.nb_cap;
-  const int tot = min(nn + nf, cap);
+  const int nn = valid ? nbr_near_count(d, i) : 0, nf = valid ? nbr_far_count(d, i) : 0;
+  const int tot = nn + nf, capN = d.nb_capN;
   bool on_s = valid, on_t = valid;
   if (use_act && valid) {
     // activity flags are exactly 0.0 or 1.0: compare their bits (no FP64)
@@ -91,7 +91,7 @@ __global__ void __launch_bounds__(256) k_spmv(Dev d, const double2 *__restrict__
   double as = 0.0, at = 0.0;
   if (on_s && on_t) {
     for (int p = gl; p < tot; p += RW) {
-      const int slot = p < nn ? p : cap - 1 - (p - nn);
+      const int slot = p < nn ? p : capN + (p - nn);
       const uint32_t e = d.nbr[row + slot];
       const double h = d.hval[row + slot];
       const double2 xj = x[e >> 8];
@@ -100,7 +100,7 @@ __global__ void __launch_bounds__(256) k_spmv(Dev d, const double2 *__restrict__
     }
   } else if (on_s || on_t) {
     for (int p = gl; p < tot; p += RW) {
-      const int slot = p < nn ? p : cap - 1 - (p - nn);
+      const int slot = p < nn ? p : capN + (p - nn);
       const uint32_t e = d.nbr[row + slot];
       const double h = d.hval[row + slot];
       const double2 xj = x[e >> 8];
@@ -185,8 +185,8 @@ __global__ void __launch_bounds__(256) k_spmv32(Dev d, const double2 *__restrict
   const int i = (int)(tid / RW);
   const bool valid = i < d.n;     // no early return: the row group shuffles
   const long long row = (long long)i * d.nb_cap;
-  const int nn = valid ? d.n_near[i] : 0, nf = valid ? d.n_far[i] : 0, cap = d.nb_cap;
-  const int tot = min(nn + nf, cap);
+  const int nn = valid ? nbr_near_count(d, i) : 0, nf = valid ? nbr_far_count(d, i) : 0;
+  const int tot = nn + nf, capN = d.nb_capN;
   const float4 *__restrict__ x32 = d.qd32;
   bool on_s = valid, on_t = valid;
   if (use_act && valid) {
@@ -208,7 +208,7 @@ __global__ void __launch_bounds__(256) k_spmv32(Dev d, const double2 *__restrict
 #pragma unroll
       for (int u = 0; u < 4; ++u) {
         const int q = p + u * RW;
-        const int s = q < nn ? q : cap - 1 - (q - nn);
+        const int s = q < nn ? q : capN + (q - nn);
         e4[u] = d.nbr[row + s];
         h4[u] = d.hval32[row + s];
       }
@@ -225,7 +225,7 @@ __global__ void __launch_bounds__(256) k_spmv32(Dev d, const double2 *__restrict
       df_fma(h4[3], x4[3].z, x4[3].w, th1, tl1);
     }
     for (; p < tot; p += RW) {
-      const int slot = p < nn ? p : cap - 1 - (p - nn);
+      const int slot = p < nn ? p : capN + (p - nn);
       const uint32_t e = d.nbr[row + slot];
       const float h = d.hval32[row + slot];
       const float4 xj = x32[e >> 8];
@@ -236,14 +236,14 @@ __global__ void __launch_bounds__(256) k_spmv32(Dev d, const double2 *__restrict
     df_add(th, tl, th1, tl1);
   } else if (on_s) {
     for (int p = gl; p < tot; p += RW) {
-      const int slot = p < nn ? p : cap - 1 - (p - nn);
+      const int slot = p < nn ? p : capN + (p - nn);
       const float h = d.hval32[row + slot];
       const float4 xj = x32[d.nbr[row + slot] >> 8];
       df_fma(h, xj.x, xj.y, sh, sl);
     }
   } else if (on_t) {
     for (int p = gl; p < tot; p += RW) {
-      const int slot = p < nn ? p : cap - 1 - (p - nn);
+      const int slot = p < nn ? p : capN + (p - nn);
       const float h = d.hval32[row + slot];
       const float4 xj = x32[d.nbr[row + slot] >> 8];
       df_fma(h, xj.z, xj.w, th, tl);

@@ -395,7 +395,7 @@ int alloc_atoms(rg_system *h, int n) {
   else d.fC32 = nullptr;
   r |= dalloc(h, B, &d.seg_o, (size_t)n);
   r |= dalloc(h, B, &d.seg_s, (size_t)n);
-  r |= dalloc(h, B, &d.status, 8);
+  r |= dalloc(h, B, &d.status, RG_NSTATUS);
   r |= dalloc(h, B, &d.dbg_flag, 1);
   r |= dalloc(h, B, &d.dbg, 40);
   r |= dalloc(h, B, &d.fb_cnt, 2);
@@ -406,9 +406,14 @@ int alloc_atoms(rg_system *h, int n) {
   const double rho = n / vol;
   const double rc = list_cutoff(h);
   const double pi = 3.14159265358979;
-  int nb = (int)(1.6 * 4.0 / 3.0 * pi * rc * rc * rc * rho) + 64;
-  nb = (nb + 31) / 32 * 32;
-  d.nb_cap = nb;
+  // rows: near part (d <= near_cut) and far part, each 1.6x its mean count
+  const double nc = std::min(std::max(h->ctl.near_cut, 1.0), rc);
+  int nbN = (int)(1.6 * 4.0 / 3.0 * pi * nc * nc * nc * rho) + 32;
+  int nbF = (int)(1.6 * 4.0 / 3.0 * pi * (rc * rc * rc - nc * nc * nc) * rho) + 32;
+  nbN = (nbN + 31) / 32 * 32;
+  nbF = (nbF + 31) / 32 * 32;
+  d.nb_capN = nbN;
+  d.nb_cap = nbN + nbF;
   d.bond_cap = 16;
   const double hc = std::max(h->ctl.hbond_cut, 1.0);
   d.hb_cap = (int)(1.6 * 4.0 / 3.0 * pi * hc * hc * hc * rho) + 32;
@@ -420,7 +425,7 @@ int alloc_atoms(rg_system *h, int n) {
 }
 
 int read_status(rg_system *h, int *st) {
-  CK(cudaMemcpyAsync(st, h->d.status, 8 * sizeof(int), cudaMemcpyDeviceToHost, h->st));
+  CK(cudaMemcpyAsync(st, h->d.status, RG_NSTATUS * sizeof(int), cudaMemcpyDeviceToHost, h->st));
   CK(cudaStreamSynchronize(h->st));
   return 0;
 }
@@ -493,12 +498,12 @@ int build_lists(rg_system *h) {
   }
   int rc = setup_cells(h);
   if (rc) return rc;
-  CK(cudaMemsetAsync(d.status, 0, 8 * sizeof(int), h->st));
+  CK(cudaMemsetAsync(d.status, 0, RG_NSTATUS * sizeof(int), h->st));
   {
     Scope sc(h, PH_BIN, 7);
     launch_bin_sort(d, h->st);
   }
-  int st[8];
+  int st[RG_NSTATUS];
   for (int attempt = 0;; ++attempt) {
     {
       Scope sc(h, PH_NBR, 1);
@@ -507,10 +512,13 @@ int build_lists(rg_system *h) {
     if ((rc = read_status(h, st))) return rc;
     if (!(st[ST_OVF] & OVF_NBR)) break;
     if (attempt > 3) return fail(h, RG_E_CAPACITY, "pair list capacity");
-    d.nb_cap = (int)(st[ST_MAXNB] * 1.2) / 32 * 32 + 64;
+    const int capN = std::max(d.nb_capN, (int)(st[ST_MAXNB] * 1.2) / 32 * 32 + 32);
+    const int capF = std::max(d.nb_cap - d.nb_capN, (int)(st[ST_MAXNF] * 1.2) / 32 * 32 + 32);
+    d.nb_capN = capN;
+    d.nb_cap = capN + capF;
     h->stats.regrows++;
     if ((rc = alloc_nbrs(h))) return rc;
-    CK(cudaMemsetAsync(d.status, 0, 8 * sizeof(int), h->st));
+    CK(cudaMemsetAsync(d.status, 0, RG_NSTATUS * sizeof(int), h->st));
   }
   for (int attempt = 0;; ++attempt) {
     {
@@ -530,13 +538,13 @@ int build_lists(rg_system *h) {
       if ((rc = alloc_hb(h))) return rc;
     }
     h->stats.regrows++;
-    CK(cudaMemsetAsync(d.status, 0, 8 * sizeof(int), h->st));
+    CK(cudaMemsetAsync(d.status, 0, RG_NSTATUS * sizeof(int), h->st));
   }
   h->stats.n_pairs = st[5];
   h->stats.n_H_entries = st[5];
   h->stats.n_bonds = st[6];
   h->stats.n_hbond_pairs = st[7];
-  h->stats.max_nbrs = st[ST_MAXNB];
+  h->stats.max_nbrs = st[ST_MAXNB] + st[ST_MAXNF];
   h->stats.max_bonds = st[ST_MAXB];
   h->stats.max_hbonds = st[ST_MAXHB];
   h->lists_valid = true;
@@ -1244,7 +1252,7 @@ int rg_compute(rg_system *h, int eflag, int vflag, double *f_out, double *energi
   if (rc) return rc;
   if (f_out) CK(cudaMemcpyAsync(f_out, h->d.f_o, 3 * sizeof(double) * h->n, cudaMemcpyDeviceToHost, h->st));
   if (energies && (rc = energy_sum(h, energies))) return rc;
-  int st[8];
+  int st[RG_NSTATUS];
   if ((rc = read_status(h, st))) return rc;
   if (st[ST_NAN]) return fail(h, RG_E_NUMERIC, "non-finite force");
   return RG_OK;
@@ -1448,7 +1456,7 @@ extern "C" long long rg_dump_pairs(rg_system *h, int *ti, int *tj, int *img) {
   long long k = 0;
   for (int i = 0; i < n; ++i)
     for (int p = 0; p < nn[i] + nf[i]; ++p) {
-      const int slot = p < nn[i] ? p : cap - 1 - (p - nn[i]);
+      const int slot = p < nn[i] ? p : d.nb_capN + (p - nn[i]);
       const uint32_t e = nbr[(size_t)i * cap + slot];
       ti[k] = tags[i];
       tj[k] = tags[e >> 8];

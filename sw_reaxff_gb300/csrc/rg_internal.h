@@ -159,6 +159,8 @@ struct Dev {
   int n;              // atoms
   int mixed;          // 1: FP32 arithmetic in the pair / bond kernels
   int nb_cap;         // neighbour row capacity (row-major rows)
+  int nb_capN;        // the first nb_capN slots of a row hold its near
+                      // entries, the remaining nb_cap - nb_capN its far ones
   int bond_cap;       // bond slots per atom (slot-major: k*n + i)
   int hb_cap;         // H-bond partner slots per H atom (row-major)
   // independent periodic systems ("segments") in one set of arrays: atoms
@@ -195,12 +197,15 @@ struct Dev {
                       // w: the charge (FP32)
   int *ts, *tags;
 
-  // full pair list, row-major rows of nb_cap; near entries from the front,
-  // far entries from the back
+  // full pair list (both directions), row-major rows of nb_cap: near
+  // entries (d <= near_cut) in slots [0, n_near), far ones in
+  // [nb_capN, nb_capN + n_far); the order within a part is the order the
+  // entries were claimed in (atomically, see k_build_nbrs)
   uint32_t *nbr;      // (j << 8) | image
   double *hval;       // QEq H_ij per entry (FP64 form)
   float *hval32;      // QEq H_ij per entry (mixed form)
-  int *n_near, *n_far;
+  int *n_near, *n_far;  // entries claimed (may exceed the part's capacity
+                        // until the host regrows and re-runs)
 
   // bonds (slot-major, slot = k*n + i)
   int *nbonds;
@@ -264,12 +269,16 @@ struct Dev {
   int *dbg_flag;
   double *dbg;
 
-  int *status;        // [8]: 0 overflow flags, 1 max nbrs, 2 max bonds, 3 max hb, 4 nonfinite,
-                      //      5 pair entries, 6 bonds, 7 H-bond partners
+  int *status;        // [RG_NSTATUS]: 0 overflow flags, 1 max near entries, 2 max bonds,
+                      // 3 max hb, 4 nonfinite, 5 pair entries, 6 bonds, 7 H-bond
+                      // partners, 8 max far entries
 };
 
 // status slots
-enum { ST_OVF = 0, ST_MAXNB = 1, ST_MAXB = 2, ST_MAXHB = 3, ST_NAN = 4 };
+enum { ST_OVF = 0, ST_MAXNB = 1, ST_MAXB = 2, ST_MAXHB = 3, ST_NAN = 4, ST_MAXNF = 8 };
+constexpr int RG_NSTATUS = 16;
+
+
 enum { OVF_NBR = 1, OVF_BOND = 2, OVF_HB = 4, OVF_CELL = 8 };
 
 #define RG_C_ELE 332.06371   // Coulomb constant, kcal A / (mol e^2) (reaxc_defs_sunway.h:59)
@@ -281,6 +290,18 @@ enum { OVF_NBR = 1, OVF_BOND = 2, OVF_HB = 4, OVF_CELL = 8 };
 #define RG_C3_QEQ (0.3333333333333 - 1.0 / 3.0)
 #define RG_C3_ELE (0.33333333333333 - 1.0 / 3.0)
 #ifdef __CUDACC__
+
+// the p-th entry of a row with nn near entries (near entries first)
+inline __host__ __device__ int nbr_slot(const Dev &d, int p, int nn) {
+  return p < nn ? p : d.nb_capN + (p - nn);
+}
+// the clipped part sizes of atom i's row
+__device__ __forceinline__ int nbr_near_count(const Dev &d, int i) {
+  return min(d.n_near[i], d.nb_capN);
+}
+__device__ __forceinline__ int nbr_far_count(const Dev &d, int i) {
+  return min(d.n_far[i], d.nb_cap - d.nb_capN);
+}
 // Per-atom item lists (bond slots, bond candidates) of the 32 atoms of a
 // warp, taken 32 items at a time: lane l brings cnt items of its atom i, and
 // f(i, c) runs for every item c < cnt of every lane's atom with the warp's

@@ -207,7 +207,9 @@ int rg_qeq(rg_system *h, double *q_out, int *iters_s, int *iters_t);
 
 /* Force step.  f_out[3n] host or NULL (forces, kcal/mol/A), energies
  * [RG_NENERGY] host or NULL; eflag = 0 skips the energy reductions;
- * vflag != 0 also accumulates the virial (rg_get_virial). */
+ * vflag & 3 also accumulates the virial (rg_get_virial).  With LAMMPS's
+ * per-atom bits, eflag & 2 or vflag & 4, the step also tallies per-atom
+ * energy and virial (rg_get_atom_tallies). */
 int rg_compute(rg_system *h, int eflag, int vflag, double *f_out,
                double *energies);
 /* Virial of the last force step computed with vflag, per segment
@@ -215,6 +217,18 @@ int rg_compute(rg_system *h, int eflag, int vflag, double *f_out,
  * kcal/mol, the quantity LAMMPS's virial[6] holds (virial_fdotr_compute
  * over local + ghost atoms, pair_reaxc_sunway.cpp:674-763). */
 int rg_get_virial(rg_system *h, double *v);
+
+/* Per-atom energy and virial of the last rg_compute made with eflag & 2
+ * (LAMMPS ENERGY_ATOM) or vflag & 4 (VIRIAL_ATOM), in the caller's atom
+ * order: eatom[n] and vatom[6n] (xx yy zz xy xz yz per atom), either may be
+ * NULL.  As in the reference, only the nonbonded pair terms tally per atom
+ * (ev_tally_full, reaxc_inlines_sw64.h:178-222, called from
+ * vdW_Coulomb_Energy_Full_C, reaxc_nonbonded_sw64.c:198-213): each pair
+ * within the nonbonded cutoff gives each of its atoms half its vdW +
+ * Coulomb energy and half of del (x) del fpair.  The pair style's
+ * eatom/vatom (pair_reaxc_sunway.cpp, ev_setup) are filled from these.
+ * RG_E_STATE if the last force step did not tally. */
+int rg_get_atom_tallies(rg_system *h, double *eatom, double *vatom);
 
 /* Velocity-Verlet halves (dt in fs). */
 int rg_nve_initial(rg_system *h, double dt);

@@ -63,6 +63,7 @@ def lib(path=None):
                                                P(C.c_double), P(C.c_int), P(C.c_int),
                                                P(C.c_int), P(C.c_longlong)]
             _reflib.ro_ref_use_qeq.argtypes = [C.c_void_p, C.c_int]
+            _reflib.ro_ref_atom_tallies.argtypes = [C.c_void_p, P(C.c_double), P(C.c_double)]
         return _reflib
     if _lib is None:
         build()
@@ -87,6 +88,7 @@ def _declare(L):
         L.ro_compute.argtypes = [C.c_void_p, P(C.c_double), P(C.c_double)]
         L.ro_run_nve.argtypes = [C.c_void_p, C.c_int, C.c_double, P(C.c_double)]
         L.ro_md_steps.argtypes = [C.c_void_p, C.c_int, C.c_double, P(C.c_double)]
+        L.ro_atom_tallies.argtypes = [C.c_void_p, P(C.c_double), P(C.c_double)]
         L.ro_get_state.argtypes = [C.c_void_p] + [P(C.c_double)] * 4
         L.ro_get_stats.argtypes = [C.c_void_p, P(Stats)]
         for f in ("ro_dump_far", "ro_dump_hbonds"):
@@ -190,6 +192,16 @@ class Oracle:
             raise RuntimeError(f"reference code aborted with {rc}")
         k = nh.value
         return f, dict(zip(ENERGY_NAMES, e)), bo[:nb], (ti[:k], tj[:k], im[:k])
+
+    def atom_tallies(self, reference=False):
+        """Per-atom energy (n) and virial (n x 6: xx yy zz xy xz yz) of the
+        last compute (reference=True: of the last ref_compute, from the
+        reference's own ev_tally_full)."""
+        ea = np.zeros(self.n)
+        va = np.zeros((self.n, 6))
+        fn = self.L.ro_ref_atom_tallies if reference else self.L.ro_atom_tallies
+        fn(self.h, _dp(ea), _dp(va))
+        return ea, va
 
     def run_nve(self, nsteps, dt):
         e = np.zeros(NENERGY)

@@ -135,6 +135,11 @@ struct ro_ctx {
   double *cd_local;     /* n: folded CdDelta */
   /* QEq matrix rows for local atoms */
   long long H_entries;
+  /* per-atom nonbonded tallies of the last ro_compute (ev_tally_full):
+   * eatom[n], vatom[6n] (xx yy zz xy xz yz per atom); the reference build
+   * keeps the reference's own in ref_eatom / ref_vatom */
+  double *eatom, *vatom, *ref_eatom, *ref_vatom;
+  int tally_n;
   /* QEq driver: NULL = qeq_restated below; the reference build installs the
    * reference's own FixQEqReaxSunway::pre_force here (oracle/ref) */
   int (*qeq_driver)(ro_ctx *c, const void *H, int *iters_s, int *iters_t);
@@ -490,6 +495,7 @@ void ro_destroy(ro_ctx *c) {
   free_work(c);
   free(c->x); free(c->v); free(c->q); free(c->f); free(c->type); free(c->tag);
   free(c->s_hist); free(c->t_hist); free(c->s); free(c->t); free(c->cd_local);
+  free(c->eatom); free(c->vatom); free(c->ref_eatom); free(c->ref_vatom);
   free(c);
 }
 
@@ -1642,12 +1648,26 @@ static void torsion_valence(ro_ctx *c) {
 /* vdW + Coulomb, full list, forces on i only:
  * vdW_Coulomb_Energy_Full_C_test_err, reaxc_nonbonded_sw64.c:40-258 */
 
+static void tally_alloc(ro_ctx *c) {
+  if (c->tally_n != c->n) {
+    free(c->eatom); free(c->vatom); free(c->ref_eatom); free(c->ref_vatom);
+    c->eatom = (double *)calloc((size_t)c->n + 1, sizeof(double));
+    c->vatom = (double *)calloc(6 * (size_t)c->n + 1, sizeof(double));
+    c->ref_eatom = (double *)calloc((size_t)c->n + 1, sizeof(double));
+    c->ref_vatom = (double *)calloc(6 * (size_t)c->n + 1, sizeof(double));
+    c->tally_n = c->n;
+  }
+}
+
 static void nonbonded(ro_ctx *c) {
   const ffield_t *ff = &c->ff;
   const double p_vdW1 = ff->gp[28], p_vdW1i = 1.0 / p_vdW1;
   const double *Tap = c->Tap;
   double e_vdw_full = 0, e_ele_full = 0, eng_vdwl = 0, eng_coul = 0;
   int i;
+  tally_alloc(c);
+  memset(c->eatom, 0, (size_t)c->n * sizeof(double));
+  memset(c->vatom, 0, 6 * (size_t)c->n * sizeof(double));
   for (i = 0; i < c->n; i++) {
     int ti = c->te[i], pj;
     for (pj = c->far_start[i]; pj < c->far_start[i + 1]; pj++) {
@@ -1708,6 +1728,23 @@ static void nonbonded(ro_ctx *c) {
       eng_vdwl += 0.5 * Tp * (e_vdW + e_core + e_lg);
       eng_coul += 0.5 * e_ele;
       add4(&c->fC[4 * i], -(CEvd + CEclmb), &c->far_dvec[3 * pj]);
+      {
+        /* per-atom tallies: ev_tally_full (reaxc_inlines_sw64.h:178-222)
+         * as called at reaxc_nonbonded_sw64.c:198-213, del = x_i - x_j of
+         * the ghost positions, fpair = -(CEvd + CEclmb) */
+        const double pe_vdw = Tp * (e_vdW + e_core + e_lg);
+        const double f_tmp = -(CEvd + CEclmb);
+        const double dx = c->xe[3 * i] - c->xe[3 * j], dy = c->xe[3 * i + 1] - c->xe[3 * j + 1],
+                     dz = c->xe[3 * i + 2] - c->xe[3 * j + 2];
+        double *va = &c->vatom[6 * i];
+        c->eatom[i] += 0.5 * (pe_vdw + e_ele);
+        va[0] += 0.5 * dx * dx * f_tmp;
+        va[1] += 0.5 * dy * dy * f_tmp;
+        va[2] += 0.5 * dz * dz * f_tmp;
+        va[3] += 0.5 * dx * dy * f_tmp;
+        va[4] += 0.5 * dx * dz * f_tmp;
+        va[5] += 0.5 * dy * dz * f_tmp;
+      }
     }
   }
   c->en[RO_E_VDW] += e_vdw_full;
@@ -2047,6 +2084,13 @@ int ro_md_steps(ro_ctx *c, int nsteps, double dt, double *energies_last) {
     c->tphase[5] += now_s() - t0;
   }
   return 0;
+}
+
+void ro_atom_tallies(const ro_ctx *c, double *eatom, double *vatom) {
+  size_t n = (size_t)c->n;
+  if (c->tally_n != c->n) return;
+  if (eatom) memcpy(eatom, c->eatom, n * sizeof(double));
+  if (vatom) memcpy(vatom, c->vatom, 6 * n * sizeof(double));
 }
 
 void ro_get_state(const ro_ctx *c, double *x, double *v, double *q, double *f) {

@@ -86,6 +86,13 @@ int ro_md_steps(ro_ctx *c, int nsteps, double dt, double *energies_last);
 void ro_get_state(const ro_ctx *c, double *x, double *v, double *q,
                   double *f);
 
+/* per-atom tallies of the last ro_compute, as LAMMPS's eatom/vatom with
+ * eflag_atom/vflag_atom: only the nonbonded pair terms tally per atom in
+ * the reference (ev_tally_full, reaxc_nonbonded_sw64.c:198-213): eatom[i] =
+ * sum over i's full list of (E_vdW + E_ele)/2, vatom[6i..6i+5] = sum of
+ * del (x) del fpair / 2 (xx yy zz xy xz yz), del = x_i - x_j */
+void ro_atom_tallies(const ro_ctx *c, double *eatom, double *vatom);
+
 /* list statistics from the last ro_compute / ro_qeq */
 typedef struct {
   long long n_local, n_total, n_far_local, n_far_total, n_bonds_total,

@@ -174,6 +174,11 @@ int ro_ref_compute(ro_ctx *c, double *f_out, double *energies, double *bo_out,
   sys->evflag = 1;
   sys->eflag_global = 1;
   sys->vflag_global = 0;
+  /* per-atom tallies (LAMMPS eflag_atom / vflag_atom) */
+  sys->eflag_atom = 1;
+  sys->vflag_atom = 1;
+  sys->eatom = (double *)zalloc(N * sizeof(double));
+  sys->vatom = (double (*)[6])zalloc(N * 6 * sizeof(double));
   sys->saferzone = 1.4;
 
   control_params *ctl = (control_params *)zalloc(sizeof(control_params));
@@ -307,6 +312,11 @@ int ro_ref_compute(ro_ctx *c, double *f_out, double *energies, double *bo_out,
   Add_All_dBond_to_Forces_C(sys, ctl, data, ws, &lists, mpid);
 
   /* results */
+  tally_alloc(c);
+  for (i = 0; i < n; i++) {
+    c->ref_eatom[i] = sys->eatom[i];
+    for (k = 0; k < 6; k++) c->ref_vatom[6 * i + k] = sys->vatom[i][k];
+  }
   for (i = 0; i < 3 * n; i++) f_out[i] = 0.0;
   for (i = 0; i < N; i++) {
     int o = c->own[i];
@@ -367,7 +377,7 @@ int ro_ref_compute(ro_ctx *c, double *f_out, double *energies, double *bo_out,
     free(R.tbp[t1]); free(R.thbp[t1]); free(R.hbp[t1]); free(R.fbp[t1]);
   }
   free(R.sbp); free(R.tbp); free(R.thbp); free(R.hbp); free(R.fbp);
-  free(sys->packed_atoms); free(sys->Hindex); free(sys->num_bonds); free(sys->num_hbonds);
+  free(sys->packed_atoms); free(sys->eatom); free(sys->vatom); free(sys->Hindex); free(sys->num_bonds); free(sys->num_hbonds);
   free(sys); free(ctl); free(data); free(outc); free(mpid);
   free(ws->bo_dboc); free(ws->Deltap); free(ws->Deltap_boc); free(ws->Delta);
   free(ws->Delta_lp); free(ws->Delta_lp_temp); free(ws->Delta_e); free(ws->Delta_val);
@@ -413,3 +423,11 @@ static int ref_qeq_driver(ro_ctx *c, const void *Hv, int *iters_s, int *iters_t)
 /* on != 0: this context's ro_qeq (and ro_run_nve's QEq) run the
  * reference's pre_force; 0: the oracle's restatement */
 void ro_ref_use_qeq(ro_ctx *c, int on) { c->qeq_driver = on ? ref_qeq_driver : NULL; }
+
+/* the reference's per-atom tallies (eatom[n], vatom[6n]) of the last
+ * ro_ref_compute */
+void ro_ref_atom_tallies(const ro_ctx *c, double *eatom, double *vatom) {
+  if (c->tally_n != c->n) return;
+  if (eatom) memcpy(eatom, c->ref_eatom, (size_t)c->n * sizeof(double));
+  if (vatom) memcpy(vatom, c->ref_vatom, 6 * (size_t)c->n * sizeof(double));
+}

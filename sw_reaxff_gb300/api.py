@@ -33,7 +33,7 @@ EXPORTED = ["rg_default_params", "rg_create", "rg_destroy", "rg_last_error",
             "rg_qeq_noalloc", "rg_set_masses", "rg_ffield_info", "rg_set_segments",
             "rg_num_segments", "rg_get_energies", "rg_get_segment_iters",
             "rg_get_histories", "rg_set_histories", "rg_table_info", "rg_table_check",
-            "rg_get_virial", "rg_bond_table"]
+            "rg_get_virial", "rg_bond_table", "rg_get_atom_tallies"]
 
 
 class Params(C.Structure):
@@ -95,6 +95,7 @@ def load_library(path: str = LIBPATH):
     L.rg_get_histories.argtypes = [C.c_void_p, dp, dp]
     L.rg_table_info.argtypes = [C.c_void_p, ip, dp]
     L.rg_get_virial.argtypes = [C.c_void_p, dp]
+    L.rg_get_atom_tallies.argtypes = [C.c_void_p, dp, dp]
     L.rg_bond_table.argtypes = [C.c_void_p, C.c_double, C.c_int, ip, ip, dp, dp, dp]
     L.rg_table_check.argtypes = [C.c_char_p, P(Params), dp]
     L.rg_set_histories.argtypes = [C.c_void_p, dp, dp]
@@ -331,6 +332,14 @@ class ReaxGPU:
         v = np.zeros((ns, 6))
         self._chk(self.L.rg_get_virial(self.h, _dp(v)), "rg_get_virial")
         return v
+
+    def atom_tallies(self):
+        """Per-atom energy (n) and virial (n x 6: xx yy zz xy xz yz) of the
+        last compute(eflag=3 or vflag=4), in the caller's atom order."""
+        ea = np.zeros(self.n)
+        va = np.zeros((self.n, 6))
+        self._chk(self.L.rg_get_atom_tallies(self.h, _dp(ea), _dp(va)), "rg_get_atom_tallies")
+        return ea, va
 
     def nve_initial(self, dt):
         self._chk(self.L.rg_nve_initial(self.h, dt), "rg_nve_initial")

@@ -367,7 +367,7 @@ __device__ __forceinline__ void nbr_flush(const Dev &d, const Control &C, const 
 }
 
 template <bool MIXED>
-__global__ void __launch_bounds__(NB_WARPS * 32) k_build_nbrs(Dev d) {
+__global__ void __launch_bounds__(NB_WARPS * 32, 3) k_build_nbrs(Dev d) {
   __shared__ NbrQueue queues[NB_WARPS];
   const int lane = threadIdx.x & 31;
   const int wib = threadIdx.x >> 5;

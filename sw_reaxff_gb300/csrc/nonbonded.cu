@@ -66,10 +66,10 @@ __device__ __forceinline__ double cubic_u(const double2 &c01, const double2 &c23
 template <bool EF>
 __device__ __forceinline__ bool pair_terms(const Dev &d, const ForceField &F, const Control &C,
                                           uint32_t e, bool act, const double4 &xi, int ti,
-                                          const SegGeom &g, double &evdw, double &eele,
+                                          const SegGeom &g, double &ev, double &ee,
                                           double &c, double &dx, double &dy, double &dz,
                                           int &j) {
-  c = 0.0; dx = dy = dz = 0.0;
+  c = 0.0; dx = dy = dz = 0.0; ev = ee = 0.0;
   j = (int)(e >> 8);
   if (!act) return false;
   int sx, sy, sz;
@@ -96,8 +96,8 @@ __device__ __forceinline__ bool pair_terms(const Dev &d, const ForceField &F, co
     const double qq = xi.w * qj;
     c = fma(cubic_u(T[2], T[3], u), qq, cubic_u(T[0], T[1], u));
     if (EF) {
-      evdw += cubic_u(T[4], T[5], u);
-      eele = fma(qq, cubic_u(T[6], T[7], u), eele);
+      ev = cubic_u(T[4], T[5], u);
+      ee = qq * cubic_u(T[6], T[7], u);
     }
     return true;
   }
@@ -147,8 +147,8 @@ __device__ __forceinline__ bool pair_terms(const Dev &d, const ForceField &F, co
   const double qq = C_ele * xi.w * qj;
   const double CEclmb = qq * (dTap - Tp * r / dr3gamij_1) * inv3;
   if (EF) {
-    evdw += Tp * (e_vdW + e_core + e_lg);
-    eele += qq * Tp * inv3;
+    ev = Tp * (e_vdW + e_core + e_lg);
+    ee = qq * Tp * inv3;
   }
   c = CEvd + CEclmb;
   return true;
@@ -264,12 +264,34 @@ __device__ __forceinline__ void pair32(const Dev &d, const Control &C, int vdw_t
   c = CEvd + qq * (dTap - Tp * r / dr3) * inv3;
 }
 
+// AT: one pair's halves of energy and virial to atom i (registers, summed
+// per warp at the end) and to atom j (atomics); dx = x_j - x_i and c =
+// (1/r) dE/dr here, so del (x) del fpair = -c dx (x) dx
+__device__ __forceinline__ void atom_tally(const Dev &d, double *ta, int j, double ev, double ee,
+                                           double c, double dx, double dy, double dz) {
+  const double e = 0.5 * (ev + ee), h = -0.5 * c;
+  const double v[6] = {h * dx * dx, h * dy * dy, h * dz * dz, h * dx * dy, h * dx * dz, h * dy * dz};
+  ta[0] += e;
+  atomicAdd(&d.eatom[j], e);
+#pragma unroll
+  for (int k = 0; k < 6; ++k) {
+    ta[1 + k] += v[k];
+    atomicAdd(&d.vatom[(long long)k * d.n + j], v[k]);
+  }
+}
+
 // one warp per atom i; the pairs (i,j,image) with j > i, or j == i with the
 // "positive" image, are queued and evaluated 32 at a time
 // the FP64 form is FP64-pipe bound: three blocks per SM (80 registers, a
 // few spilled) keep the pipe busier than two (7 % faster); the FP32 form
 // has no minimum (0) and keeps its 66-80 registers
-template <typename R, bool VIR, bool EF>
+// AT (only with EF): per-atom tallies of LAMMPS's eflag_atom / vflag_atom,
+// as the reference's ev_tally_full over the full list
+// (reaxc_nonbonded_sw64.c:198-213): each directed pair gives its centre
+// half of the pair's vdW + Coulomb energy and half of del (x) del fpair
+// (del = x_i - x_j, fpair = -(1/r) dE/dr).  An unordered pair here gives
+// both atoms those halves (the two directions have the same values).
+template <typename R, bool VIR, bool EF, bool AT = false>
 __global__ void __launch_bounds__(NBW * 32, std::is_same<R, double>::value ? 3 : 0)
     k_nonbonded(Dev d) {
   __shared__ PairQueue queues[NBW];
@@ -293,6 +315,7 @@ __global__ void __launch_bounds__(NBW * 32, std::is_same<R, double>::value ? 3 :
     const int tot = nn + nf;
     double fx = 0, fy = 0, fz = 0;
     float fx32 = 0.f, fy32 = 0.f, fz32 = 0.f;   // mixed form: FP32 force sums
+    double ta[7] = {0, 0, 0, 0, 0, 0, 0};        // AT: atom i's energy and virial
     double *fC = d.fC;
     const int vdw_type = F.vdw_type;
     int qn = 0;
@@ -334,9 +357,12 @@ __global__ void __launch_bounds__(NBW * 32, std::is_same<R, double>::value ? 3 :
             atomicAdd(&d.fC32[2 * n + j], c * dz);
             if (VIR) vir_acc(w, dx, dy, dz, (double)(c * dx), (double)(c * dy), (double)(c * dz));
           }
+          if (AT && act)
+            atom_tally(d, ta, j, (double)ev, (double)ee, (double)c, (double)dx, (double)dy,
+                       (double)dz);
         } else {
-          double c, dx, dy, dz;
-          if (pair_terms<EF>(d, F, C, e, act, xi, ti, g, evdw, eele, c, dx, dy, dz, j)) {
+          double c, dx, dy, dz, ev, ee;
+          if (pair_terms<EF>(d, F, C, e, act, xi, ti, g, ev, ee, c, dx, dy, dz, j)) {
             fx -= c * dx;
             fy -= c * dy;
             fz -= c * dz;
@@ -344,6 +370,11 @@ __global__ void __launch_bounds__(NBW * 32, std::is_same<R, double>::value ? 3 :
             atomicAdd(&fC[n + j], c * dy);
             atomicAdd(&fC[2 * n + j], c * dz);
             if (VIR) vir_acc(w, dx, dy, dz, c * dx, c * dy, c * dz);
+            if (EF) {
+              evdw += ev;
+              eele += ee;
+            }
+            if (AT) atom_tally(d, ta, j, ev, ee, c, dx, dy, dz);
           }
         }
         __syncwarp();
@@ -377,6 +408,15 @@ __global__ void __launch_bounds__(NBW * 32, std::is_same<R, double>::value ? 3 :
         atomicAdd(&fC[2 * n + i], fz);
       }
     }
+    if (AT) {
+#pragma unroll
+      for (int k = 0; k < 7; ++k) ta[k] = warp_sum(ta[k]);
+      if (lane == 0) {
+        atomicAdd(&d.eatom[i], ta[0]);
+#pragma unroll
+        for (int k = 0; k < 6; ++k) atomicAdd(&d.vatom[(long long)k * n + i], ta[1 + k]);
+      }
+    }
   }
   if (EF) {
     const int sg = i < d.n ? d.seg_s[i] : -1;
@@ -393,7 +433,8 @@ __global__ void __launch_bounds__(NBW * 32, std::is_same<R, double>::value ? 3 :
 
 template <typename R, bool VIR>
 void launch_nb(const Dev &d, cudaStream_t st, int eflag, unsigned G) {
-  if (eflag) k_nonbonded<R, VIR, true><<<G, NBW * 32, 0, st>>>(d);
+  if (d.atom_tally) k_nonbonded<R, VIR, true, true><<<G, NBW * 32, 0, st>>>(d);
+  else if (eflag) k_nonbonded<R, VIR, true><<<G, NBW * 32, 0, st>>>(d);
   else k_nonbonded<R, VIR, false><<<G, NBW * 32, 0, st>>>(d);
 }
 

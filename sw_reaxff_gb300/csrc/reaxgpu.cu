@@ -105,6 +105,7 @@ struct rg_system {
   int ncell_alloc = 0;
   bool lists_valid = false;
   bool forces_valid = false;
+  bool tallies_valid = false;   // per-atom tallies of the last force step
   // autotuned configuration: cells of cutoff/cell_div (2 or 3) and the SpMV
   // lanes per row (d.spmv_rw); tuned_n = atom count it was tuned for
   int cell_div = 2;
@@ -369,6 +370,8 @@ int alloc_atoms(rg_system *h, int n) {
   r |= dalloc(h, B, &d.cell_o, (size_t)n);
   r |= dalloc(h, B, &d.perm, (size_t)n);
   r |= dalloc(h, B, &d.iperm, (size_t)n);
+  r |= dalloc(h, B, &d.eatom, (size_t)n);
+  r |= dalloc(h, B, &d.vatom, 6 * (size_t)n);
   r |= dalloc(h, B, &d.xs, (size_t)n);
   r |= dalloc(h, B, &d.xf, (size_t)n);
   r |= dalloc(h, B, &d.xl, (size_t)n);
@@ -551,7 +554,7 @@ int build_lists(rg_system *h) {
   return 0;
 }
 
-int do_compute(rg_system *h, int eflag, int vflag = 0) {
+int do_compute(rg_system *h, int eflag, int vflag = 0, int atom_tally = 0) {
   Dev &d = h->d;
   int rc;
   if (!h->lists_valid && (rc = build_lists(h))) return rc;
@@ -560,6 +563,12 @@ int do_compute(rg_system *h, int eflag, int vflag = 0) {
   CK(cudaMemsetAsync(d.vsum, 0, 2 * sizeof(double) * (size_t)d.n, h->st));
   CK(cudaMemsetAsync(d.energy, 0, (size_t)d.nseg * RG_NE * sizeof(double), h->st));
   d.vflag = vflag ? 1 : 0;
+  d.atom_tally = atom_tally ? 1 : 0;
+  h->tallies_valid = false;
+  if (atom_tally) {
+    CK(cudaMemsetAsync(d.eatom, 0, sizeof(double) * (size_t)d.n, h->st));
+    CK(cudaMemsetAsync(d.vatom, 0, 6 * sizeof(double) * (size_t)d.n, h->st));
+  }
   if (vflag) CK(cudaMemsetAsync(d.virial, 0, (size_t)d.nseg * 6 * sizeof(double), h->st));
   if (d.debug) CK(cudaMemsetAsync(d.dbg_flag, 0, sizeof(int), h->st));
   auto finite_after = [&](const char *phase) -> int {
@@ -1155,6 +1164,28 @@ int rg_get_virial(rg_system *h, double *v) {
   return RG_OK;
 }
 
+int rg_get_atom_tallies(rg_system *h, double *eatom, double *vatom) {
+  if (!h) return RG_E_ARG;
+  if (!h->tallies_valid)
+    return fail(h, RG_E_STATE, "no per-atom tallies: call rg_compute with eflag & 2 or vflag & 4");
+  CK(cudaSetDevice(h->p.device));
+  const Dev &d = h->d;
+  const size_t n = (size_t)d.n;
+  std::vector<double> e(n), v(6 * n);
+  std::vector<int> perm(n);
+  CK(cudaMemcpyAsync(e.data(), d.eatom, n * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+  CK(cudaMemcpyAsync(v.data(), d.vatom, 6 * n * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+  CK(cudaMemcpyAsync(perm.data(), d.perm, n * sizeof(int), cudaMemcpyDeviceToHost, h->st));
+  CK(cudaStreamSynchronize(h->st));
+  for (size_t s = 0; s < n; ++s) {
+    const size_t o = (size_t)perm[s];
+    if (eatom) eatom[o] = e[s];
+    if (vatom)
+      for (int k = 0; k < 6; ++k) vatom[6 * o + k] = v[(size_t)k * n + s];
+  }
+  return RG_OK;
+}
+
 int rg_get_segment_iters(rg_system *h, int *iters) {
   if (!h || !iters) return RG_E_ARG;
   for (size_t k = 0; k < h->seg_iters.size(); ++k) iters[k] = h->seg_iters[k];
@@ -1248,8 +1279,12 @@ int rg_compute(rg_system *h, int eflag, int vflag, double *f_out, double *energi
   if (!h) return RG_E_ARG;
   if (!h->n) return fail(h, RG_E_STATE, "no atoms set");
   CK(cudaSetDevice(h->p.device));
-  int rc = do_compute(h, eflag || energies != nullptr, vflag);
+  // LAMMPS's flag bits: eflag 1 global energy, 2 per-atom energy; vflag 1|2
+  // global virial, 4 per-atom virial
+  const int atom_tally = (eflag & 2) || (vflag & 4);
+  int rc = do_compute(h, eflag || energies != nullptr, vflag & 3, atom_tally);
   if (rc) return rc;
+  h->tallies_valid = atom_tally != 0;
   if (f_out) CK(cudaMemcpyAsync(f_out, h->d.f_o, 3 * sizeof(double) * h->n, cudaMemcpyDeviceToHost, h->st));
   if (energies && (rc = energy_sum(h, energies))) return rc;
   int st[RG_NSTATUS];

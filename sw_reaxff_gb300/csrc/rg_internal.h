@@ -269,6 +269,11 @@ struct Dev {
   int *dbg_flag;
   double *dbg;
 
+  // per-atom tallies (LAMMPS eflag_atom / vflag_atom) of the nonbonded
+  // pair terms, sorted order: eatom[n], vatom[6][n] (xx yy zz xy xz yz)
+  int atom_tally;
+  double *eatom, *vatom;
+
   int *status;        // [RG_NSTATUS]: 0 overflow flags, 1 max near entries, 2 max bonds,
                       // 3 max hb, 4 nonfinite, 5 pair entries, 6 bonds, 7 H-bond
                       // partners, 8 max far entries

@@ -301,7 +301,18 @@ void PairReaxCGB300::compute(int eflag, int vflag) {
     eng_vdwl = e[14];
     eng_coul = e[15];
   }
-  if (vflag) check(rg_get_virial(h, virial), "rg_get_virial");
+  if (vflag & 3) check(rg_get_virial(h, virial), "rg_get_virial");
+  if ((eflag & 2) || (vflag & 4)) {
+    const int n = atom_->nlocal;
+    std::vector<double> ea(n), va(6 * (size_t)n);
+    check(rg_get_atom_tallies(h, ea.data(), va.data()), "rg_get_atom_tallies");
+    if (eflag & 2) eatom = ea;
+    if (vflag & 4) {
+      vatom.resize(n);
+      for (int i = 0; i < n; ++i)
+        for (int k = 0; k < 6; ++k) vatom[i][k] = va[6 * (size_t)i + k];
+    }
+  }
 }
 
 void *PairReaxCGB300::extract(const char *str, int &dim) {

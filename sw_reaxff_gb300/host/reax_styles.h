@@ -27,6 +27,7 @@
 #include <map>
 #include <stdexcept>
 #include <string>
+#include <array>
 #include <vector>
 
 #include "reaxgpu.h"
@@ -189,6 +190,11 @@ class PairReaxCGB300 {
   double pvector[14] = {0};
   double eng_vdwl = 0.0, eng_coul = 0.0;
   double virial[6] = {0};
+  // per-atom tallies (LAMMPS Pair::eatom / vatom), filled by compute() when
+  // eflag & 2 (ENERGY_ATOM) or vflag & 4 (VIRIAL_ATOM): local atoms only,
+  // the nonbonded pair terms as in the reference
+  std::vector<double> eatom;              // [nlocal]
+  std::vector<std::array<double, 6>> vatom;  // [nlocal] xx yy zz xy xz yz
   int qeqflag = 1;
 
   // shared with the fixes

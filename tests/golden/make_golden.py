@@ -8,7 +8,8 @@ by oracle/ref/Makefile into oracle/_ref/libreax_ref.so):
 For each seeded system it stores the inputs (box, positions, types, tags,
 charges) and the outputs of the reference's host-side routines run on the
 oracle's lists: the 14-term energy vector plus eng_vdwl/eng_coul, the
-per-atom forces, the corrected bond orders of every bond entry (tag_i,
+per-atom forces, the per-atom energy and virial tallies (eatom, vatom of
+eflag_atom / vflag_atom), the corrected bond orders of every bond entry (tag_i,
 tag_j, image) and the H-bond partner list.  Charges are the reference's
 own QEq (FixQEqReaxSunway::pre_force -> init_matvec, CG_v2, calculate_Q,
 compiled from fix_qeq_reax_sunway.cpp by oracle/ref/Makefile) from zero
@@ -55,6 +56,7 @@ def main():
         o.compute()
         ti, tj, im, _ = o.bond_list()
         f, e, bo, hb = o.ref_compute()
+        eatom, vatom = o.atom_tallies(reference=True)
         md = Oracle(DEFAULT_FFIELD, reference_qeq=True)
         md.set_system(s.box, s.x, types, s.tag, None, s.v)
         e_md = md.run_nve(NVE_STEPS, NVE_DT)
@@ -63,7 +65,7 @@ def main():
             os.path.join(HERE, f"{name}.npz"),
             box=s.box, x=s.x, types=types, tags=s.tag, q=q,
             energies=np.array([e[k] for k in ENERGY_NAMES]), energy_names=np.array(ENERGY_NAMES),
-            forces=f, bond_ti=ti, bond_tj=tj, bond_img=im, bond_bo=bo,
+            forces=f, eatom=eatom, vatom=vatom, bond_ti=ti, bond_tj=tj, bond_img=im, bond_bo=bo,
             hb_ti=hb[0], hb_tj=hb[1], hb_img=hb[2], qeq_iters=np.array([its, itt]),
             v=s.v, nve_steps=np.array(NVE_STEPS), nve_dt=np.array(NVE_DT),
             nve_x=x5, nve_v=v5, nve_q=q5, nve_f=f5,

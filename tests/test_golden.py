@@ -100,3 +100,12 @@ def test_nve_matches_reference_qeq(case):
     ref = dict(zip([str(s) for s in g["energy_names"]], g["nve_energies"]))
     for k in TERMS:
         assert abs(em[k] - ref[k]) <= max(1e-9 * abs(ref[k]), 1e-7), (k, em[k], ref[k])
+
+
+def test_atom_tallies_match_reference(case):
+    """Per-atom energy and virial (eflag_atom / vflag_atom) of the
+    reference's ev_tally_full."""
+    g, o, f, e = case
+    ea, va = o.atom_tallies()
+    np.testing.assert_allclose(ea, g["eatom"], rtol=1e-12, atol=1e-12)
+    np.testing.assert_allclose(va, g["vatom"], rtol=1e-12, atol=1e-11)

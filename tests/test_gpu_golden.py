@@ -31,8 +31,19 @@ def case(request, ffield):
     gpu = ReaxGPU(ffield)
     gpu.set_box(g["box"])
     gpu.set_atoms(g["x"], g["types"], g["tags"], g["q"])
-    f, e = gpu.compute()
+    f, e = gpu.compute(eflag=3, vflag=4)
     return g, gpu, f, e
+
+
+def test_gpu_atom_tallies_vs_reference(case):
+    """Per-atom energy and virial against the reference's ev_tally_full:
+    1e-9 relative RMS (the force bar), and their sums against the physical
+    nonbonded energy."""
+    g, gpu, f, e = case
+    ea, va = gpu.atom_tallies()
+    assert np.sqrt(((ea - g["eatom"]) ** 2).sum() / (g["eatom"] ** 2).sum()) < 1e-9
+    assert np.sqrt(((va - g["vatom"]) ** 2).sum() / (g["vatom"] ** 2).sum()) < 1e-9
+    assert abs(ea.sum() - 0.5 * (e["e_vdW"] + e["e_ele"])) <= 1e-9 * abs(ea).sum()
 
 
 def test_gpu_energies_vs_reference(case):

@@ -41,8 +41,8 @@ def run(request, ffield):
     g2 = ReaxGPU(ffield, precision=PREC_MIXED)
     g2.set_box(s.box)
     g2.set_atoms(s.x, s.types(g.elements), s.tag, qo, s.v)
-    fq, eq = g2.compute()
-    return dict(s=s, g=g, o=o, qg=qg, qo=qo, fg=fg, eg=eg, fo=fo, eo=eo, fq=fq, eq=eq)
+    fq, eq = g2.compute(eflag=3, vflag=4)
+    return dict(s=s, g=g, g2=g2, o=o, qg=qg, qo=qo, fg=fg, eg=eg, fo=fo, eo=eo, fq=fq, eq=eq)
 
 
 def test_mixed_lists_equal_fp64(run):
@@ -70,3 +70,12 @@ def test_mixed_energies(run):
     eq, eo = run["eq"], run["eo"]
     for k in TERMS:
         assert abs(eq[k] - eo[k]) <= max(1e-4 * abs(eo[k]), 1e-3), (k, eq[k], eo[k])
+
+
+def test_mixed_atom_tallies(run):
+    """Per-atom energy and virial (eflag_atom / vflag_atom) of the mixed
+    form against the FP64 oracle's, at the force bar."""
+    ea, va = run["g2"].atom_tallies()
+    eo, vo = run["o"].atom_tallies()
+    assert np.sqrt(((ea - eo) ** 2).sum() / (eo ** 2).sum()) < 1e-4
+    assert np.sqrt(((va - vo) ** 2).sum() / (vo ** 2).sum()) < 1e-4

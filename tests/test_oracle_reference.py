@@ -31,7 +31,10 @@ def test_oracle_equals_reference(name, ffield):
     fo, eo = o.compute()
     _, _, _, boo = o.bond_list()
     hb_o = set(zip(*[a.tolist() for a in o.hbond_list()]))
+    ea, va = o.atom_tallies()
     fr, er, bor, hb = o.ref_compute()
+    ear, var = o.atom_tallies(reference=True)
+    assert np.array_equal(ea, ear) and np.array_equal(va, var)
     assert np.abs(boo - bor).max() == 0.0
     assert hb_o == set(zip(*[a.tolist() for a in hb]))
     assert np.sqrt(((fo - fr) ** 2).sum() / (fr ** 2).sum()) < 1e-12

@@ -273,6 +273,24 @@ int rg_profile_get(rg_system *h, int max, char *names, double *ms,
  * launches). */
 int rg_profile_phases(rg_system *h, unsigned mask);
 
+/* Continuous batching: rebuild the set of systems of h on the device from
+ * keep[nkeep] of its own segments (in that order) followed by sel[nsel]
+ * segments of src (another handle on the same device with the same force
+ * field, or NULL with nsel = 0).  Every carried system keeps its box, tilt
+ * and per-atom state -- positions, velocities, forces, charges, types, tags
+ * and the 5-deep s/t QEq histories -- copied device to device; no atom
+ * passes through host memory.  A Verlet run (rg_run) continues from the
+ * carried forces when every carried system had forces.  src's pending work
+ * is waited for on the device; h and src are free again when the call
+ * returns.  No counterpart in the reference (one system per LAMMPS run):
+ * the segments themselves are this library's batching (rg_set_segments). */
+int rg_regroup_segments(rg_system *h, int nkeep, const int *keep, rg_system *src,
+                        int nsel, const int *sel);
+
+/* One segment's atoms (host arrays of that segment's atom count; any may be
+ * NULL): positions, velocities, charges and the forces of the last step. */
+int rg_get_segment_atoms(rg_system *h, int seg, double *x, double *v, double *q, double *f);
+
 /* Allocation-free QEq (no counterpart in the reference).  For callers that
  * cannot call cudaMalloc when they need charges -- code running under a host
  * application's own device-memory manager, or where an allocation would

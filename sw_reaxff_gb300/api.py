@@ -33,7 +33,8 @@ EXPORTED = ["rg_default_params", "rg_create", "rg_destroy", "rg_last_error",
             "rg_qeq_noalloc", "rg_set_masses", "rg_ffield_info", "rg_set_segments",
             "rg_num_segments", "rg_get_energies", "rg_get_segment_iters",
             "rg_get_histories", "rg_set_histories", "rg_table_info", "rg_table_check",
-            "rg_get_virial", "rg_bond_table", "rg_get_atom_tallies"]
+            "rg_get_virial", "rg_bond_table", "rg_get_atom_tallies",
+            "rg_regroup_segments", "rg_get_segment_atoms"]
 
 
 class Params(C.Structure):
@@ -96,6 +97,8 @@ def load_library(path: str = LIBPATH):
     L.rg_table_info.argtypes = [C.c_void_p, ip, dp]
     L.rg_get_virial.argtypes = [C.c_void_p, dp]
     L.rg_get_atom_tallies.argtypes = [C.c_void_p, dp, dp]
+    L.rg_regroup_segments.argtypes = [C.c_void_p, C.c_int, ip, C.c_void_p, C.c_int, ip]
+    L.rg_get_segment_atoms.argtypes = [C.c_void_p, C.c_int, dp, dp, dp, dp]
     L.rg_bond_table.argtypes = [C.c_void_p, C.c_double, C.c_int, ip, ip, dp, dp, dp]
     L.rg_table_check.argtypes = [C.c_char_p, P(Params), dp]
     L.rg_set_histories.argtypes = [C.c_void_p, dp, dp]
@@ -218,6 +221,8 @@ class ReaxGPU:
     def set_box(self, box):
         box = np.ascontiguousarray(box, np.float64)
         self._chk(self.L.rg_set_box(self.h, _dp(box)), "rg_set_box")
+        self._seg_counts = None
+        self.nseg = 1
 
     def set_atoms(self, x, types, tags=None, q=None, v=None):
         x = np.ascontiguousarray(x, np.float64)
@@ -229,6 +234,8 @@ class ReaxGPU:
         self._chk(self.L.rg_set_atoms(self.h, n, _dp(x), _ip(types), _ip(tags), _dp(q), _dp(v)),
                   "rg_set_atoms")
         self.n = n
+        if sum(getattr(self, "_seg_counts", None) or []) != n:
+            self._seg_counts = [n]
 
     def set_tilt(self, tilt):
         """Tilts (xy, xz, yz) of a triclinic box, one row per segment."""
@@ -259,6 +266,7 @@ class ReaxGPU:
         v = np.concatenate([s.v for s in systems_list])
         self.set_atoms(x, types, tags, None, v)
         self.nseg = len(systems_list)
+        self._seg_counts = [int(c) for c in counts]
         return np.concatenate([[0], np.cumsum(counts)[:-1]])
 
     def energies(self):
@@ -332,6 +340,31 @@ class ReaxGPU:
         v = np.zeros((ns, 6))
         self._chk(self.L.rg_get_virial(self.h, _dp(v)), "rg_get_virial")
         return v
+
+    def regroup(self, keep, src=None, sel=()):
+        """Keep the segments `keep` (in that order) and append the segments
+        `sel` of handle `src`, their state carried on the device; returns
+        the new segments' first-atom offsets."""
+        keep = np.ascontiguousarray(keep, np.int32)
+        sel = np.ascontiguousarray(sel, np.int32)
+        self._chk(self.L.rg_regroup_segments(self.h, len(keep), _ip(keep) if len(keep) else None,
+                                             src.h if src is not None else None, len(sel),
+                                             _ip(sel) if len(sel) else None),
+                  "rg_regroup_segments")
+        counts = [self._seg_counts[k] for k in keep] + \
+                 ([src._seg_counts[k] for k in sel] if src is not None else [])
+        self._seg_counts = counts
+        self.nseg = len(counts)
+        self.n = int(sum(counts))
+        return np.concatenate([[0], np.cumsum(counts)[:-1]]).astype(int)
+
+    def segment_atoms(self, seg):
+        """(x, v, q, f) of one segment."""
+        c = self._seg_counts[seg]
+        x = np.zeros((c, 3)); v = np.zeros((c, 3)); q = np.zeros(c); f = np.zeros((c, 3))
+        self._chk(self.L.rg_get_segment_atoms(self.h, seg, _dp(x), _dp(v), _dp(q), _dp(f)),
+                  "rg_get_segment_atoms")
+        return x, v, q, f
 
     def atom_tallies(self):
         """Per-atom energy (n) and virial (n x 6: xx yy zz xy xz yz) of the

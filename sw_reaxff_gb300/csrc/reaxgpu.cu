@@ -160,8 +160,10 @@ template <class T>
 int dalloc(rg_system *h, std::vector<void *> &bucket, T **p, size_t count) {
   void *q = nullptr;
   cudaError_t e = cudaMalloc(&q, std::max<size_t>(count, 1) * sizeof(T));
-  if (e != cudaSuccess)
+  if (e != cudaSuccess) {
+    cudaGetLastError();   // not sticky: keep it from surfacing in a later call
     return fail(h, RG_E_CUDA, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+  }
   bucket.push_back(q);
   *p = (T *)q;
   return 0;
@@ -406,7 +408,9 @@ int alloc_atoms(rg_system *h, int n) {
   // capacity estimates from the mean density
   double vol = 0.0;
   for (const SegGeom &g : h->segs) vol += g.L[0] * g.L[1] * g.L[2];
-  const double rho = n / vol;
+  // (bounded: a liquid's density where no volume is known, and at most a
+  // few times the densest condensed phases; the build regrows anyway)
+  const double rho = vol > 0.0 ? std::min(n / vol, 0.5) : 0.12;
   const double rc = list_cutoff(h);
   const double pi = 3.14159265358979;
   // rows: near part (d <= near_cut) and far part, each 1.6x its mean count
@@ -1183,6 +1187,172 @@ int rg_get_atom_tallies(rg_system *h, double *eatom, double *vatom) {
     if (vatom)
       for (int k = 0; k < 6; ++k) vatom[6 * o + k] = v[(size_t)k * n + s];
   }
+  return RG_OK;
+}
+
+}  // extern "C"
+
+// ------------------------------------------------------------------
+// regrouping systems on the device (continuous batching)
+
+namespace {
+
+// per-atom state in the caller's order: x, v, f (3 per atom), q, type, tag,
+// and the 5-deep s/t histories (history k of atom i at k * n + i)
+struct StateView {
+  double *x, *v, *f, *q, *sh, *th;
+  int *type, *tag;
+  int n;
+};
+
+struct SegMove {
+  int src0, dst0, count;
+};
+
+// copy the atom ranges of moves[] from one state to another; one block per
+// range
+__global__ void k_gather_state(StateView dst, StateView src, const SegMove *moves) {
+  const SegMove m = moves[blockIdx.x];
+  for (int a = threadIdx.x; a < m.count; a += blockDim.x) {
+    const long long s = m.src0 + a, t = m.dst0 + a;
+    for (int c = 0; c < 3; ++c) {
+      dst.x[3 * t + c] = src.x[3 * s + c];
+      dst.v[3 * t + c] = src.v[3 * s + c];
+      dst.f[3 * t + c] = src.f[3 * s + c];
+    }
+    dst.q[t] = src.q[s];
+    dst.type[t] = src.type[s];
+    dst.tag[t] = src.tag[s];
+    for (int k = 0; k < 5; ++k) {
+      dst.sh[(long long)k * dst.n + t] = src.sh[(long long)k * src.n + s];
+      dst.th[(long long)k * dst.n + t] = src.th[(long long)k * src.n + s];
+    }
+  }
+}
+
+StateView state_of(const rg_system *h) {
+  const Dev &d = h->d;
+  return StateView{d.x_o, d.v_o, d.f_o, d.q_o, d.s_hist, d.t_hist, d.type_o, d.tag_o, h->n};
+}
+
+}  // namespace
+
+extern "C" {
+
+int rg_regroup_segments(rg_system *h, int nkeep, const int *keep, rg_system *src, int nsel,
+                        const int *sel) {
+  if (!h || nkeep < 0 || nsel < 0 || (nkeep && !keep) || (nsel && (!src || !sel)))
+    return RG_E_ARG;
+  if (nkeep + nsel == 0) return fail(h, RG_E_ARG, "rg_regroup_segments: no segment selected");
+  if (nkeep && !h->n) return fail(h, RG_E_STATE, "rg_regroup_segments: no atoms set");
+  if (nsel) {
+    if (src == h) return fail(h, RG_E_ARG, "rg_regroup_segments: src must be another handle");
+    if (!src->n) return fail(h, RG_E_STATE, "rg_regroup_segments: src holds no atoms");
+    if (src->p.device != h->p.device || src->ff.ntypes != h->ff.ntypes)
+      return fail(h, RG_E_ARG,
+                  "rg_regroup_segments: src must be on the same device with the same force field");
+  }
+  const int nh = (int)h->segs.size(), ns_src = nsel ? (int)src->segs.size() : 0;
+  std::vector<SegGeom> segs;
+  std::vector<int> counts;
+  std::vector<SegMove> own, other;
+  long long n_new = 0;
+  for (int k = 0; k < nkeep; ++k) {
+    if (keep[k] < 0 || keep[k] >= nh)
+      return fail(h, RG_E_ARG, "rg_regroup_segments: keep index out of range");
+    const SegGeom &g = h->segs[keep[k]];
+    own.push_back(SegMove{g.atom0, (int)n_new, g.natoms});
+    segs.push_back(g);
+    counts.push_back(g.natoms);
+    n_new += g.natoms;
+  }
+  for (int k = 0; k < nsel; ++k) {
+    if (sel[k] < 0 || sel[k] >= ns_src)
+      return fail(h, RG_E_ARG, "rg_regroup_segments: sel index out of range");
+    const SegGeom &g = src->segs[sel[k]];
+    other.push_back(SegMove{g.atom0, (int)n_new, g.natoms});
+    segs.push_back(g);
+    counts.push_back(g.natoms);
+    n_new += g.natoms;
+  }
+  if (n_new >= (1 << 24)) return fail(h, RG_E_ARG, "rg_regroup_segments: too many atoms");
+  CK(cudaSetDevice(h->p.device));
+  cudaStream_t st = h->st;
+  if (nsel) {
+    // the source's pending work must be complete before its state is read
+    cudaEvent_t ev;
+    CK(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+    CK(cudaEventRecord(ev, src->st));
+    CK(cudaStreamWaitEvent(st, ev, 0));
+    CK(cudaEventDestroy(ev));
+  }
+  // gather into stream-ordered temporaries (no device-wide synchronisation)
+  const size_t N = (size_t)n_new;
+  const size_t dbytes = sizeof(double) * N * 20, ibytes = sizeof(int) * N * 2;
+  const size_t mbytes = sizeof(SegMove) * (own.size() + other.size());
+  char *tmp = nullptr;
+  CK(cudaMallocAsync((void **)&tmp, dbytes + ibytes + mbytes, st));
+  double *td = (double *)tmp;
+  StateView T{td, td + 3 * N, td + 6 * N, td + 9 * N, td + 10 * N, td + 15 * N,
+              (int *)(tmp + dbytes), (int *)(tmp + dbytes) + N, (int)n_new};
+  SegMove *dm = (SegMove *)(tmp + dbytes + ibytes);
+  std::vector<SegMove> all(own);
+  all.insert(all.end(), other.begin(), other.end());
+  CK(cudaMemcpyAsync(dm, all.data(), mbytes, cudaMemcpyHostToDevice, st));
+  if (!own.empty()) k_gather_state<<<(unsigned)own.size(), 256, 0, st>>>(T, state_of(h), dm);
+  if (!other.empty())
+    k_gather_state<<<(unsigned)other.size(), 256, 0, st>>>(T, state_of(src), dm + own.size());
+  CK(cudaGetLastError());
+  const bool forces_ok = (nkeep == 0 || h->forces_valid) && (nsel == 0 || src->forces_valid);
+  // the new layout; per-atom arrays grow only when the capacity is exceeded
+  CK(cudaStreamSynchronize(st));
+  // the new segments first: a growing allocation estimates the list
+  // capacities from their volume
+  h->segs = segs;
+  h->seg_counts = counts;
+  h->have_box = true;
+  int rc = alloc_atoms(h, (int)n_new);
+  if (!rc) {
+    h->n = (int)n_new;
+    rc = sync_segments(h);
+  }
+  if (rc) {
+    cudaFreeAsync(tmp, st);
+    cudaStreamSynchronize(st);
+    return rc;
+  }
+  // the temporaries hold the new layout with stride n_new: one copy each
+  const Dev &d = h->d;
+  CK(cudaMemcpyAsync(d.x_o, T.x, 3 * N * sizeof(double), cudaMemcpyDeviceToDevice, st));
+  CK(cudaMemcpyAsync(d.v_o, T.v, 3 * N * sizeof(double), cudaMemcpyDeviceToDevice, st));
+  CK(cudaMemcpyAsync(d.f_o, T.f, 3 * N * sizeof(double), cudaMemcpyDeviceToDevice, st));
+  CK(cudaMemcpyAsync(d.q_o, T.q, N * sizeof(double), cudaMemcpyDeviceToDevice, st));
+  CK(cudaMemcpyAsync(d.s_hist, T.sh, 5 * N * sizeof(double), cudaMemcpyDeviceToDevice, st));
+  CK(cudaMemcpyAsync(d.t_hist, T.th, 5 * N * sizeof(double), cudaMemcpyDeviceToDevice, st));
+  CK(cudaMemcpyAsync(d.type_o, T.type, N * sizeof(int), cudaMemcpyDeviceToDevice, st));
+  CK(cudaMemcpyAsync(d.tag_o, T.tag, N * sizeof(int), cudaMemcpyDeviceToDevice, st));
+  CK(cudaFreeAsync(tmp, st));
+  CK(cudaStreamSynchronize(st));
+  h->lists_valid = false;
+  h->forces_valid = forces_ok;
+  h->tallies_valid = false;
+  h->seg_iters.clear();
+  return RG_OK;
+}
+
+int rg_get_segment_atoms(rg_system *h, int seg, double *x, double *v, double *q, double *f) {
+  if (!h) return RG_E_ARG;
+  if (seg < 0 || seg >= (int)h->segs.size()) return fail(h, RG_E_ARG, "segment index out of range");
+  if (!h->n) return fail(h, RG_E_STATE, "no atoms set");
+  CK(cudaSetDevice(h->p.device));
+  const SegGeom &g = h->segs[seg];
+  const size_t a0 = (size_t)g.atom0, c = (size_t)g.natoms;
+  const Dev &d = h->d;
+  if (x) CK(cudaMemcpyAsync(x, d.x_o + 3 * a0, 3 * c * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+  if (v) CK(cudaMemcpyAsync(v, d.v_o + 3 * a0, 3 * c * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+  if (q) CK(cudaMemcpyAsync(q, d.q_o + a0, c * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+  if (f) CK(cudaMemcpyAsync(f, d.f_o + 3 * a0, 3 * c * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+  CK(cudaStreamSynchronize(h->st));
   return RG_OK;
 }
 

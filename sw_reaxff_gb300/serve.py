@@ -2,25 +2,30 @@
 batching.
 
 A request is a periodic system plus either a single-point evaluation
-(energies, forces and QEq charges) or a short NVE run of n steps.  The loop
-keeps two segment handles (independent systems in one set of device arrays,
-rg_set_segments) and drives them concurrently from two host threads, each
-handle on its own CUDA stream:
+(energies, forces and QEq charges) or a short NVE run of n steps.  Systems
+live as segments of handles (independent systems in one set of device
+arrays, rg_set_segments), and two kinds of work run side by side, each
+handle on its own CUDA stream, driven from worker threads:
 
-* the evaluation batch: every iteration takes the requests admitted since
-  the last one, single points and the first force evaluation of new MD
-  requests alike, and evaluates them together;
-* the MD cohort: the MD requests in flight advance together a few steps per
-  iteration; when requests finish or new ones (evaluated in the previous
-  iteration) are ready, the cohort is rebuilt with the state of every
-  continuing request carried over exactly (positions, velocities, forces,
-  QEq histories), so a trajectory does not depend on what it shares the
-  GPU with.
+* evaluation batches: whenever an evaluation handle is free, every
+  admitted request not yet evaluated is loaded into it and evaluated
+  together -- single points, and the first QEq + force evaluation of new
+  MD requests;
+* the MD cohort: the MD requests in flight advance together a few steps at
+  a time on one handle.  Between two such chunks the cohort is regrouped on
+  the device (rg_regroup_segments): finished trajectories leave, and new
+  MD requests join straight from the evaluation handle that evaluated
+  them, their positions, velocities, forces and QEq histories copied
+  device to device.  No trajectory's state passes through host memory
+  between its input and its result, and a trajectory does not depend on
+  what it shares the GPU with.
 
+An evaluation batch starts as soon as a handle is free, without waiting for
+the MD chunk, and a chunk starts as soon as the previous one is done.
 Admission is by device-memory footprint: a request is admitted when its
 estimated footprint fits beside the requests on the device; requests that
 arrive while others run wait for that.  Latency is completion time minus
-arrival time.
+arrival time, reported per request kind.
 """
 from __future__ import annotations
 
@@ -55,8 +60,6 @@ class Request:
     energies: dict = None
     x: np.ndarray = None
     v: np.ndarray = None
-    # MD state between cohort rebuilds: x, v, f, s_hist, t_hist
-    state: tuple = None
     steps_done: int = 0
 
     @property
@@ -64,96 +67,106 @@ class Request:
         return self.t_done - self.arrival
 
 
+def _pct(lat, p):
+    return float(np.percentile(np.array(lat), p) * 1e3) if lat else None
+
+
 @dataclass
 class ServeStats:
     completed: int = 0
     wall: float = 0.0
-    iterations: int = 0
+    eval_batches: int = 0
+    md_chunks: int = 0
     rebuilds: int = 0
     max_atoms_on_device: int = 0
     latencies: list = field(default_factory=list)
+    latencies_sp: list = field(default_factory=list)
+    latencies_md: list = field(default_factory=list)
+    last_arrival: float = 0.0
 
     def summary(self) -> dict:
-        lat = np.array(self.latencies) if self.latencies else np.zeros(1)
         return {"completed": self.completed, "wall_s": self.wall,
                 "req_per_s": self.completed / self.wall if self.wall > 0 else 0.0,
-                "p50_ms": float(np.percentile(lat, 50) * 1e3),
-                "p99_ms": float(np.percentile(lat, 99) * 1e3),
-                "iterations": self.iterations, "cohort_rebuilds": self.rebuilds,
+                "arrivals_end_s": self.last_arrival,
+                "p50_ms": _pct(self.latencies, 50), "p99_ms": _pct(self.latencies, 99),
+                "single_point": {"count": len(self.latencies_sp),
+                                 "p50_ms": _pct(self.latencies_sp, 50),
+                                 "p99_ms": _pct(self.latencies_sp, 99)},
+                "md": {"count": len(self.latencies_md), "p50_ms": _pct(self.latencies_md, 50),
+                       "p99_ms": _pct(self.latencies_md, 99)},
+                "eval_batches": self.eval_batches, "md_chunks": self.md_chunks,
+                "cohort_regroups": self.rebuilds,
                 "max_atoms_on_device": self.max_atoms_on_device}
 
 
 class ReaxServer:
     def __init__(self, ffield: str, precision: int = PREC_MIXED, hbm_budget: int = 32 << 30,
-                 dt: float = 0.25, md_chunk: int = 10, device: int = 0):
-        self.eval_h = ReaxGPU(ffield, precision=precision, device=device)
+                 dt: float = 0.25, md_chunk: int = 10, device: int = 0, n_eval: int = 3):
+        self.eval_h = [ReaxGPU(ffield, precision=precision, device=device) for _ in range(n_eval)]
         self.md_h = ReaxGPU(ffield, precision=precision, device=device)
         self.bpa = BYTES_PER_ATOM[precision]
         self.budget = hbm_budget
         self.dt = dt
         self.md_chunk = md_chunk
-        self.pool = cf.ThreadPoolExecutor(2)
-        self.md_active: list = []          # requests in the MD cohort, cohort order
-        self.md_ready: list = []           # evaluated, waiting to join the cohort
-        self.md_offsets = None
+        self.pool = cf.ThreadPoolExecutor(n_eval + 1)
+        self.md_active: list = []          # requests of the MD cohort, segment order
+        # per evaluation handle: MD requests evaluated there, waiting to join
+        # the cohort as (segment, request); the handle is not reused before
+        self.hold = [[] for _ in range(n_eval)]
 
     def close(self):
         self.pool.shutdown()
-        self.eval_h.close()
+        for g in self.eval_h:
+            g.close()
         self.md_h.close()
 
-    # -- one evaluation batch (runs in a worker thread) --------------------
-    def _evaluate(self, batch: list):
-        g = self.eval_h
+    # -- one evaluation batch (worker thread) -------------------------------
+    def _evaluate(self, k: int, batch: list):
+        g = self.eval_h[k]
         off = g.set_systems([r.system for r in batch])
         q, _, _ = g.qeq()
         f, _ = g.compute()
         es = g.energies()
-        s_hist, t_hist = g.get_histories() if any(r.kind == "md" for r in batch) else (None, None)
-        for k, r in enumerate(batch):
-            sl = slice(off[k], off[k] + r.system.n)
-            if r.kind == "sp":
-                r.q, r.f, r.energies = q[sl].copy(), f[sl].copy(), es[k]
-            else:
-                r.state = (r.system.x.copy(), r.system.v.copy(), f[sl].copy(),
-                           s_hist[:, sl].copy(), t_hist[:, sl].copy())
-                r.energies = es[k]
+        for s, r in enumerate(batch):
+            sl = slice(off[s], off[s] + r.system.n)
+            r.energies = es[s]
+            if r.kind == "sp" or r.nsteps == 0:
+                r.q, r.f = q[sl].copy(), f[sl].copy()
+                if r.kind == "md":
+                    r.x, r.v = r.system.x.copy(), r.system.v.copy()
         return batch
 
-    # -- the MD cohort ------------------------------------------------------
-    def _save_cohort(self):
-        if not self.md_active:
-            return
-        g = self.md_h
-        x, v, q, f = g.get_atoms()
-        s_hist, t_hist = g.get_histories()
-        for k, r in enumerate(self.md_active):
-            sl = slice(self.md_offsets[k], self.md_offsets[k] + r.system.n)
-            r.state = (x[sl].copy(), v[sl].copy(), f[sl].copy(), s_hist[:, sl].copy(),
-                       t_hist[:, sl].copy())
-            r.q = q[sl].copy()
-
-    def _rebuild_cohort(self, members: list):
-        g = self.md_h
-        self.md_active = members
-        if not members:
-            self.md_offsets = None
-            return
-        systems = [r.system for r in members]
-        self.md_offsets = g.set_systems(systems)
-        x = np.concatenate([r.state[0] for r in members])
-        v = np.concatenate([r.state[1] for r in members])
-        f = np.concatenate([r.state[2] for r in members])
-        s_hist = np.concatenate([r.state[3] for r in members], axis=1)
-        t_hist = np.concatenate([r.state[4] for r in members], axis=1)
-        g.set_state(x, v, f)
-        g.set_histories(s_hist, t_hist)
-
+    # -- one MD chunk (worker thread) ---------------------------------------
     def _advance(self, k: int):
-        if self.md_active and k > 0:
-            self.md_h.run(k, self.dt, energies=False)
-            for r in self.md_active:
-                r.steps_done += k
+        self.md_h.run(k, self.dt, energies=False)
+        for r in self.md_active:
+            r.steps_done += k
+
+    def _regroup(self, stats, finish):
+        """Between chunks: finished trajectories leave the cohort (their
+        results read back), MD requests held by idle evaluation handles join
+        it, all on the device."""
+        done = [i for i, r in enumerate(self.md_active) if r.steps_done >= r.nsteps]
+        for i in done:
+            r = self.md_active[i]
+            r.x, r.v, r.q, r.f = self.md_h.segment_atoms(i)
+            finish(r)
+        keep = [i for i, r in enumerate(self.md_active) if r.steps_done < r.nsteps]
+        ready = [k for k in range(len(self.eval_h)) if self.hold[k] and not self.eval_busy[k]]
+        if not done and not ready:
+            return
+        members = [self.md_active[i] for i in keep]
+        if ready:
+            for j, k in enumerate(ready):
+                sel = [s for s, _ in self.hold[k]]
+                kp = keep if j == 0 else list(range(len(members)))
+                self.md_h.regroup(kp, self.eval_h[k], sel)
+                members += [r for _, r in self.hold[k]]
+                self.hold[k] = []
+        elif keep:
+            self.md_h.regroup(keep)
+        self.md_active = members
+        stats.rebuilds += 1
 
     # -- the loop -----------------------------------------------------------
     def serve(self, requests: list, realtime: bool = True) -> ServeStats:
@@ -162,66 +175,76 @@ class ReaxServer:
         pending = deque(sorted(requests, key=lambda r: r.arrival))
         waiting: deque = deque()
         stats = ServeStats()
+        stats.last_arrival = pending[-1].arrival if pending else 0.0
         t0 = time.perf_counter()
         now = lambda: time.perf_counter() - t0
-        on_device = 0          # atoms of admitted, unfinished requests
-        while pending or waiting or self.md_active or self.md_ready:
+        on_device = [0]          # atoms of admitted, unfinished requests
+        fut_eval = {}            # evaluation handle -> future
+        fut_md = None
+        self.eval_busy = [False] * len(self.eval_h)
+
+        def finish(r):
+            r.t_done = now()
+            on_device[0] -= r.system.n
+            stats.latencies.append(r.latency)
+            (stats.latencies_sp if r.kind == "sp" else stats.latencies_md).append(r.latency)
+            stats.completed += 1
+
+        while pending or waiting or fut_eval or fut_md is not None or self.md_active or \
+                any(self.hold):
             t = now()
             while pending and (not realtime or pending[0].arrival <= t):
                 waiting.append(pending.popleft())
-            if not waiting and not self.md_active and not self.md_ready:
-                # idle until the next arrival
-                time.sleep(max(0.0, pending[0].arrival - now()))
-                continue
-            batch = []
-            while waiting and (on_device + waiting[0].system.n) * self.bpa <= self.budget:
-                r = waiting.popleft()
-                r.t_admit = now()
-                on_device += r.system.n
-                batch.append(r)
-            if not batch and not self.md_active and not self.md_ready and waiting:
-                # a request larger than the whole budget runs alone
-                r = waiting.popleft()
-                r.t_admit = now()
-                on_device += r.system.n
-                batch.append(r)
-            stats.max_atoms_on_device = max(stats.max_atoms_on_device, on_device)
-            # cohort membership changes between iterations only
-            done = [r for r in self.md_active if r.steps_done >= r.nsteps]
-            if done or self.md_ready:
-                self._save_cohort()
-                for r in done:
-                    r.x, r.v, r.f = r.state[0], r.state[1], r.state[2]
-                    r.t_done = now()
-                    on_device -= r.system.n
-                    stats.latencies.append(r.latency)
-                    stats.completed += 1
-                keep = [r for r in self.md_active if r.steps_done < r.nsteps]
-                self._rebuild_cohort(keep + self.md_ready)
-                self.md_ready = []
-                stats.rebuilds += 1
-            k = min([self.md_chunk] + [r.nsteps - r.steps_done for r in self.md_active]) \
-                if self.md_active else 0
-            fe = self.pool.submit(self._evaluate, batch) if batch else None
-            fm = self.pool.submit(self._advance, k) if k > 0 else None
-            if fe is not None:
-                for r in fe.result():
-                    if r.kind == "sp":
-                        r.t_done = now()
-                        on_device -= r.system.n
-                        stats.latencies.append(r.latency)
-                        stats.completed += 1
-                    elif r.nsteps == 0:
-                        r.x, r.v, r.f = r.state[0], r.state[1], r.state[2]
-                        r.t_done = now()
-                        on_device -= r.system.n
-                        stats.latencies.append(r.latency)
-                        stats.completed += 1
+            # finished evaluation batches
+            for k in [k for k, fu in fut_eval.items() if fu.done()]:
+                batch = fut_eval.pop(k).result()
+                self.eval_busy[k] = False
+                for s, r in enumerate(batch):
+                    if r.kind == "sp" or r.nsteps == 0:
+                        finish(r)
                     else:
-                        self.md_ready.append(r)
-            if fm is not None:
-                fm.result()
-            stats.iterations += 1
+                        self.hold[k].append((s, r))
+            # the MD side: regroup between chunks, then the next chunk
+            if fut_md is not None and fut_md.done():
+                fut_md.result()
+                fut_md = None
+            if fut_md is None:
+                self._regroup(stats, finish)
+                if self.md_active:
+                    kk = min([self.md_chunk] + [r.nsteps - r.steps_done for r in self.md_active])
+                    fut_md = self.pool.submit(self._advance, kk)
+                    stats.md_chunks += 1
+            # admission into a free evaluation handle
+            free = [k for k in range(len(self.eval_h))
+                    if not self.eval_busy[k] and not self.hold[k]]
+            if free and waiting:
+                batch = []
+                while waiting and (on_device[0] + waiting[0].system.n) * self.bpa <= self.budget:
+                    r = waiting.popleft()
+                    r.t_admit = now()
+                    on_device[0] += r.system.n
+                    batch.append(r)
+                if not batch and on_device[0] == 0:
+                    # a request larger than the whole budget runs alone
+                    r = waiting.popleft()
+                    r.t_admit = now()
+                    on_device[0] += r.system.n
+                    batch.append(r)
+                if batch:
+                    k = free[0]
+                    self.eval_busy[k] = True
+                    fut_eval[k] = self.pool.submit(self._evaluate, k, batch)
+                    stats.eval_batches += 1
+            stats.max_atoms_on_device = max(stats.max_atoms_on_device, on_device[0])
+            # wait for a worker or the next arrival
+            futs = list(fut_eval.values()) + ([fut_md] if fut_md is not None else [])
+            timeout = None
+            if realtime and pending:
+                timeout = max(0.0, pending[0].arrival - now())
+            if futs:
+                cf.wait(futs, timeout=timeout, return_when=cf.FIRST_COMPLETED)
+            elif timeout is not None:
+                time.sleep(timeout)
         stats.wall = now()
         return stats
 

@@ -246,9 +246,10 @@ def _spawn_pool():
 
 def batched_section(args, local):
     """512 independent small systems, one single point each (QEq + energies
-    + forces), evaluated together as segments of one handle in the mixed
-    form; against the same systems solved one after another with a plain
-    FP64 handle."""
+    + forces), evaluated together as segments of one handle -- the whole
+    step one captured graph launch (rg_single_point) -- in the mixed and the
+    FP64 form; against the same systems solved one after another with a
+    plain FP64 handle."""
     import torch
     from sw_reaxff_gb300 import ReaxGPU
     from sw_reaxff_gb300.api import DEFAULT_FFIELD, PREC_MIXED
@@ -262,21 +263,27 @@ def batched_section(args, local):
         g.set_systems(S)
         st = torch.cuda.ExternalStream(g.stream())
         times = []
-        for it in range(args.warmup + args.steps):
+        for it in range(max(args.warmup, 2) + args.steps):
             g.set_histories(None, None)        # fresh single points
+            if it == max(args.warmup, 2):
+                s0 = g.stats()
             e0 = torch.cuda.Event(enable_timing=True)
             e1 = torch.cuda.Event(enable_timing=True)
             e0.record(st)
-            g.qeq()
-            g.compute()
+            g.single_point()                   # QEq + forces: one graph replay
             e1.record(st)
             g.synchronize()
-            if it >= args.warmup:
+            if it >= max(args.warmup, 2):
                 times.append(e0.elapsed_time(e1) / 1e3)
+        s1 = g.stats()
         t_batch = float(np.mean(times))
         out[label] = {"batch_ms": t_batch * 1e3, "req_per_s": len(S) / t_batch,
                       "p50_ms": t_batch * 1e3, "p99_ms": t_batch * 1e3,
-                      "atom_evals_per_s": natoms / t_batch}
+                      "atom_evals_per_s": natoms / t_batch,
+                      "graph_replays": s1["step_graph_replays"] - s0["step_graph_replays"],
+                      "kernels_per_batch": (s1["kernel_launches"] - s0["kernel_launches"])
+                      / max(1, args.steps),
+                      "cg_iters_s_t": [s1["cg_iters_s"], s1["cg_iters_t"]]}
         g.close()
     # sequential plain FP64 solves (host arrays in and out, one handle), on
     # a sample of the systems

@@ -118,6 +118,10 @@ typedef struct {
   long long cg_spmv_rows_passes; /* since rg_create: CG loop SpMV launches
                                   that had a system to update (per call:
                                   max(iters_s, iters_t) - 1) */
+  long long step_graph_replays; /* rg_single_point calls served by one replay
+                                  of the captured step */
+  long long step_graph_redos;  /* replays that met a list past its capacity
+                                  and redid the step on the regular path */
 } rg_stats;
 
 void rg_default_params(rg_params *p);
@@ -204,6 +208,20 @@ int rg_set_state(rg_system *h, const double *x, const double *v,
 
 /* QEq charge equilibration (pre_force).  q_out[n] host or NULL. */
 int rg_qeq(rg_system *h, double *q_out, int *iters_s, int *iters_t);
+
+/* Single point: QEq (pre_force) then the force step, as rg_qeq followed by
+ * rg_compute with the same flags; q_out[n], f_out[3n], energies
+ * [RG_NENERGY] host or NULL.  After a first call on a given set of arrays
+ * and flags, the whole step -- binning, pair/bond/H-bond lists, the QEq with
+ * its CG iterations (and the mixed form's refinement restarts) as
+ * device-side loops, the force step -- replays as one captured CUDA graph,
+ * with one host synchronisation at its end.  A replay that finds a list
+ * past its capacity restores the QEq histories and redoes the step on the
+ * regular path, which regrows.  No counterpart in the reference (it
+ * launches each phase from the host); the batched evaluation of many small
+ * systems (segments) is its use. */
+int rg_single_point(rg_system *h, int eflag, int vflag, double *q_out, double *f_out,
+                    double *energies);
 
 /* Force step.  f_out[3n] host or NULL (forces, kcal/mol/A), energies
  * [RG_NENERGY] host or NULL; eflag = 0 skips the energy reductions;

@@ -34,7 +34,7 @@ EXPORTED = ["rg_default_params", "rg_create", "rg_destroy", "rg_last_error",
             "rg_num_segments", "rg_get_energies", "rg_get_segment_iters",
             "rg_get_histories", "rg_set_histories", "rg_table_info", "rg_table_check",
             "rg_get_virial", "rg_bond_table", "rg_get_atom_tallies",
-            "rg_regroup_segments", "rg_get_segment_atoms"]
+            "rg_regroup_segments", "rg_get_segment_atoms", "rg_single_point"]
 
 
 class Params(C.Structure):
@@ -57,7 +57,8 @@ class Stats(C.Structure):
                 ("regrows", C.c_int), ("kernel_launches", C.c_longlong),
                 ("qeq_restarts", C.c_int), ("fp64_angles", C.c_int),
                 ("fp64_torsions", C.c_int), ("cell_div", C.c_int), ("spmv_rows", C.c_int),
-                ("cg_system_iters", C.c_longlong), ("cg_spmv_rows_passes", C.c_longlong)]
+                ("cg_system_iters", C.c_longlong), ("cg_spmv_rows_passes", C.c_longlong),
+                ("step_graph_replays", C.c_longlong), ("step_graph_redos", C.c_longlong)]
 
 
 class ReaxError(RuntimeError):
@@ -99,6 +100,7 @@ def load_library(path: str = LIBPATH):
     L.rg_get_atom_tallies.argtypes = [C.c_void_p, dp, dp]
     L.rg_regroup_segments.argtypes = [C.c_void_p, C.c_int, ip, C.c_void_p, C.c_int, ip]
     L.rg_get_segment_atoms.argtypes = [C.c_void_p, C.c_int, dp, dp, dp, dp]
+    L.rg_single_point.argtypes = [C.c_void_p, C.c_int, C.c_int, dp, dp, dp]
     L.rg_bond_table.argtypes = [C.c_void_p, C.c_double, C.c_int, ip, ip, dp, dp, dp]
     L.rg_table_check.argtypes = [C.c_char_p, P(Params), dp]
     L.rg_set_histories.argtypes = [C.c_void_p, dp, dp]
@@ -326,6 +328,16 @@ class ReaxGPU:
         a, b = C.c_int(), C.c_int()
         self._chk(self.L.rg_qeq(self.h, _dp(q), C.byref(a), C.byref(b)), "rg_qeq")
         return q, a.value, b.value
+
+    def single_point(self, eflag=1, vflag=0):
+        """QEq then the force step (rg_single_point: one graph launch once
+        the same arrays were seen twice); returns q, f, energies."""
+        q = np.zeros(self.n)
+        f = np.zeros((self.n, 3))
+        e = np.zeros(NENERGY)
+        self._chk(self.L.rg_single_point(self.h, eflag, vflag, _dp(q), _dp(f), _dp(e)),
+                  "rg_single_point")
+        return q, f, dict(zip(ENERGY_NAMES, e))
 
     def compute(self, eflag=1, vflag=0):
         f = np.zeros((self.n, 3))

@@ -854,7 +854,9 @@ __device__ void vt_enumerate(const Dev &d, int j, int kk, int &cv, int &ct, long
     const int h = nbr_of(ehj), th = d.ts[h];
     if (ph > kk && C.thb_any[tk][tj][th] &&
         above(BO_jk * BO_hj, C.thb_cutsq_f, d.b_BO[spk] * d.b_BO[sph], C.thb_cutsq)) {
-      if (FILL)
+      // (the regular path sizes the list on the host first; a captured
+      // step may meet a list past its capacity: the scan total says so)
+      if (FILL && ov + cv < d.cap_val)
         d.w_val[ov + cv] = ((unsigned long long)j << 16) | ((unsigned long long)kk << 8) | ph;
       ++cv;
     }
@@ -877,7 +879,7 @@ __device__ void vt_enumerate(const Dev &d, int j, int kk, int &cv, int &ct, long
       if (l == h && sjk[0] + skl[0] == shj[0] && sjk[1] + skl[1] == shj[1] &&
           sjk[2] + skl[2] == shj[2])
         continue;   // i and l are the same atom instance
-      if (FILL)
+      if (FILL && ot + ct < d.cap_tor)
         d.w_tor[ot + ct] = ((unsigned long long)j << 24) | ((unsigned long long)kk << 16) |
                            ((unsigned long long)ph << 8) | pw;
       ++ct;
@@ -1103,8 +1105,10 @@ __device__ __forceinline__ void valence_energies(const Dev &d, int eflag, int sg
 }
 
 template <typename R, bool VIR>
-__global__ void __launch_bounds__(128) k_valence(Dev d, int eflag, long long nitems) {
+__global__ void __launch_bounds__(128) k_valence(Dev d, int eflag, long long nitems,
+                                                 const int *ntot) {
   const long long w = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (ntot) nitems = min(nitems, (long long)*ntot);
   double e_ang = 0, e_pen = 0, e_coa = 0;
   double vw[6] = {0, 0, 0, 0, 0, 0};
   int sg = -1;
@@ -1325,8 +1329,10 @@ __device__ __forceinline__ void torsion_energies(const Dev &d, int eflag, int sg
 }
 
 template <typename R, bool VIR>
-__global__ void __launch_bounds__(128) k_torsion(Dev d, int eflag, long long nitems) {
+__global__ void __launch_bounds__(128) k_torsion(Dev d, int eflag, long long nitems,
+                                                 const int *ntot) {
   const long long w = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (ntot) nitems = min(nitems, (long long)*ntot);
   double e_tor = 0, e_con = 0;
   double vw[6] = {0, 0, 0, 0, 0, 0};
   int sg = -1;
@@ -1519,25 +1525,31 @@ void launch_vt_count(const Dev &d, cudaStream_t st) {
 
 template <bool VIR>
 static void vt_kernels(const Dev &d, cudaStream_t st, int eflag, long long nval, long long ntor,
-                       unsigned gv, unsigned gt) {
+                       unsigned gv, unsigned gt, const int *tv, const int *tt) {
   if (d.mixed) {
     cudaMemsetAsync(d.fb_cnt, 0, 2 * sizeof(int), st);
-    if (nval > 0) k_valence<float, VIR><<<gv, 128, 0, st>>>(d, eflag, nval);
-    if (ntor > 0) k_torsion<float, VIR><<<gt, 128, 0, st>>>(d, eflag, ntor);
+    if (nval > 0) k_valence<float, VIR><<<gv, 128, 0, st>>>(d, eflag, nval, tv);
+    if (ntor > 0) k_torsion<float, VIR><<<gt, 128, 0, st>>>(d, eflag, ntor, tt);
     // FP64 passes over the near-linear items (count read on the device;
     // usually none or a few, so a small grid that strides)
     k_vt_fb<VIR><<<32, 128, 0, st>>>(d, eflag);
   } else {
-    if (nval > 0) k_valence<double, VIR><<<gv, 128, 0, st>>>(d, eflag, nval);
-    if (ntor > 0) k_torsion<double, VIR><<<gt, 128, 0, st>>>(d, eflag, ntor);
+    if (nval > 0) k_valence<double, VIR><<<gv, 128, 0, st>>>(d, eflag, nval, tv);
+    if (ntor > 0) k_torsion<double, VIR><<<gt, 128, 0, st>>>(d, eflag, ntor, tt);
   }
 }
 
-void launch_vt_run(const Dev &d, cudaStream_t st, int eflag, long long nval, long long ntor) {
+// nval, ntor: the item counts the host read back, or (device_counts) the
+// list capacities, the kernels then taking the counts from the scan totals
+void launch_vt_run(const Dev &d, cudaStream_t st, int eflag, long long nval, long long ntor,
+                   bool device_counts) {
   k_vt_fill<<<(unsigned)((d.n + 255) / 256), 256, 0, st>>>(d);
   const unsigned gv = (unsigned)((nval + 127) / 128), gt = (unsigned)((ntor + 127) / 128);
-  if (d.vflag) vt_kernels<true>(d, st, eflag, nval, ntor, gv, gt);
-  else vt_kernels<false>(d, st, eflag, nval, ntor, gv, gt);
+  const long long slots = (long long)d.n * d.bond_cap;
+  const int *tv = device_counts ? d.w_off_v + slots : nullptr;
+  const int *tt = device_counts ? d.w_off_t + slots : nullptr;
+  if (d.vflag) vt_kernels<true>(d, st, eflag, nval, ntor, gv, gt, tv, tt);
+  else vt_kernels<false>(d, st, eflag, nval, ntor, gv, gt, tv, tt);
 }
 
 void launch_dbond_forces(const Dev &d, cudaStream_t st) {

@@ -609,3 +609,60 @@ void launch_qeq_finish(const Dev &d, cudaStream_t st) {
   k_qeq_sums<<<G, B, 0, st>>>(d);
   k_qeq_finish<<<G, B, 0, st>>>(d);
 }
+
+// ------------------------------------------------------------------
+// QEq control of the captured step (conditional graph nodes)
+
+namespace {
+
+__global__ void k_set_cond(const int *n_active, cudaGraphConditionalHandle c1,
+                           cudaGraphConditionalHandle c2, int two) {
+  const unsigned v = *n_active > 0 ? 1u : 0u;
+  cudaGraphSetConditional(c1, v);
+  if (two) cudaGraphSetConditional(c2, v);
+}
+
+// after one CG iteration (k_cg_flip has recounted the active segments); the
+// trip limit bounds the loop even if the per-segment iteration limit failed
+__global__ void k_loop_cond(const int *n_active, int *ctl, cudaGraphConditionalHandle c,
+                            int limit) {
+  const int trips = ++ctl[1];
+  unsigned v = *n_active > 0 ? 1u : 0u;
+  if (v && trips >= limit) {
+    ctl[2] = 1;
+    v = 0u;
+  }
+  cudaGraphSetConditional(c, v);
+}
+
+__global__ void k_qeq_tot(Dev d, int pass) {
+  const int g = blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= d.nseg) return;
+  const double *R = d.red + (long long)g * RG_NRED;
+  for (int c = 0; c < 2; ++c) {
+    const int it = (int)R[R_ITERS + c] - (pass ? 1 : 0);
+    d.qeq_tot[2 * g + c] += it > 0 ? it : 0;
+  }
+}
+
+__global__ void k_restart_count(int *ctl) { ++ctl[0]; }
+
+}  // namespace
+
+void launch_qeq_set_cond(const Dev &d, cudaStream_t st, unsigned long long c1,
+                         unsigned long long c2) {
+  k_set_cond<<<1, 1, 0, st>>>(d.n_active, (cudaGraphConditionalHandle)c1,
+                              (cudaGraphConditionalHandle)c2, c2 != 0);
+}
+
+void launch_qeq_loop_cond(const Dev &d, cudaStream_t st, unsigned long long c, int limit) {
+  k_loop_cond<<<1, 1, 0, st>>>(d.n_active, d.qeq_ctl, (cudaGraphConditionalHandle)c, limit);
+}
+
+void launch_qeq_tot(const Dev &d, cudaStream_t st, int pass) {
+  k_qeq_tot<<<(d.nseg + 127) / 128, 128, 0, st>>>(d, pass);
+}
+
+void launch_qeq_restart_count(const Dev &d, cudaStream_t st) {
+  k_restart_count<<<1, 1, 0, st>>>(d.qeq_ctl);
+}

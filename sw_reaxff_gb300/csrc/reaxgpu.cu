@@ -104,6 +104,10 @@ struct rg_system {
   void *cells = nullptr;
   int ncell_alloc = 0;
   bool lists_valid = false;
+  // the force step corrects the bond orders and accumulates Cdbo in the bond
+  // arrays in place: a second force step on the same lists needs them built
+  // again
+  bool bonds_fresh = false;
   bool forces_valid = false;
   bool tallies_valid = false;   // per-atom tallies of the last force step
   // autotuned configuration: cells of cutoff/cell_div (2 or 3) and the SpMV
@@ -120,6 +124,18 @@ struct rg_system {
   cudaGraphExec_t cg_exec = nullptr;
   Dev cg_dev{};
   bool use_graphs = true;
+  // the whole single-point step (lists, QEq with device-side loops, force
+  // step) as one captured graph (rg_single_point), recaptured when the
+  // device arrays, sizes or flags change; streams for the conditional bodies
+  cudaGraphExec_t sp_exec = nullptr;
+  Dev sp_dev{};
+  int sp_flags = -1;
+  long long sp_kernels = 0;         // top-level kernel nodes of one replay
+  bool sp_failed = false;           // a capture failed: the regular path only
+  int sp_trip = 4;                  // CG iterations per device-side loop trip
+  Dev sp_seen{};                    // the previous regular call's arrays and
+  int sp_seen_flags = -1;           // flags: a repeat of them is captured
+  cudaStream_t cap_st[8] = {nullptr};
   rg_stats stats{};
   double energy[RG_NE] = {0};
   Prof prof;
@@ -269,6 +285,8 @@ int alloc_segs(rg_system *h) {
   r |= dalloc(h, h->per_seg, &d.energy, (size_t)cap * RG_NE);
   r |= dalloc(h, h->per_seg, &d.virial, (size_t)cap * 6);
   r |= dalloc(h, h->per_seg, &d.n_active, 1);
+  r |= dalloc(h, h->per_seg, &d.qeq_ctl, 4);
+  r |= dalloc(h, h->per_seg, &d.qeq_tot, 2 * (size_t)cap);
   if (r) return RG_E_CUDA;
   h->nseg_alloc = cap;
   return 0;
@@ -372,6 +390,7 @@ int alloc_atoms(rg_system *h, int n) {
   r |= dalloc(h, B, &d.cell_o, (size_t)n);
   r |= dalloc(h, B, &d.perm, (size_t)n);
   r |= dalloc(h, B, &d.iperm, (size_t)n);
+  r |= dalloc(h, B, &d.hist_save, 10 * (size_t)n);
   r |= dalloc(h, B, &d.eatom, (size_t)n);
   r |= dalloc(h, B, &d.vatom, 6 * (size_t)n);
   r |= dalloc(h, B, &d.xs, (size_t)n);
@@ -555,13 +574,15 @@ int build_lists(rg_system *h) {
   h->stats.max_bonds = st[ST_MAXB];
   h->stats.max_hbonds = st[ST_MAXHB];
   h->lists_valid = true;
+  h->bonds_fresh = true;
   return 0;
 }
 
-int do_compute(rg_system *h, int eflag, int vflag = 0, int atom_tally = 0) {
+int do_compute(rg_system *h, int eflag, int vflag = 0, int atom_tally = 0, bool graph = false) {
   Dev &d = h->d;
   int rc;
-  if (!h->lists_valid && (rc = build_lists(h))) return rc;
+  if ((!h->lists_valid || !h->bonds_fresh) && (rc = build_lists(h))) return rc;
+  h->bonds_fresh = false;
   CK(cudaMemsetAsync(d.fC, 0, 4 * sizeof(double) * (size_t)d.n, h->st));
   if (d.fC32) CK(cudaMemsetAsync(d.fC32, 0, 3 * sizeof(float) * (size_t)d.n, h->st));
   CK(cudaMemsetAsync(d.vsum, 0, 2 * sizeof(double) * (size_t)d.n, h->st));
@@ -603,7 +624,11 @@ int do_compute(rg_system *h, int eflag, int vflag = 0, int atom_tally = 0) {
     Scope sc(h, PH_VALTOR, 9);
     launch_vt_count(d, h->st);
   }
-  {
+  if (graph) {
+    // captured: grids of the list capacities, counts read on the device
+    Scope sc(h, PH_VALTOR, 1 + 2 + (d.mixed ? 1 : 0));
+    launch_vt_run(d, h->st, eflag, d.cap_val, d.cap_tor, true);
+  } else {
     // item totals sit after the last slot of the exclusive scans
     const long long slots = (long long)d.n * d.bond_cap;
     int tot[2];
@@ -737,6 +762,185 @@ int do_qeq(rg_system *h, int *its, int *itt) {
   if (itt) *itt = mt;
   { Scope sc(h, PH_QFIN, 3); launch_qeq_finish(d, h->st); }
   CK(cudaGetLastError());
+  return 0;
+}
+
+// ------------------------------------------------------------------
+// the single-point step as one captured graph (rg_single_point)
+//
+// Lists, QEq and force step without a host synchronisation: the list
+// kernels clip to their capacities and flag an overflow, the valence and
+// torsion kernels take their counts on the device, and the QEq loops are
+// conditional WHILE nodes whose condition a device kernel sets from the
+// number of segments still iterating (bounded by a trip limit); the mixed
+// form's refinement restarts are nested IF nodes.  The step saves the QEq
+// histories first, so that the host can restore them and redo the step on
+// the regular path when the replay reports an overflow.
+
+constexpr int kMaxCapLevels = 8;
+
+int cap_graph(rg_system *h, cudaStream_t s, cudaGraph_t *g) {
+  cudaStreamCaptureStatus cs;
+  CK(cudaStreamGetCaptureInfo(s, &cs, nullptr, g, nullptr, nullptr, nullptr));
+  if (cs != cudaStreamCaptureStatusActive) return fail(h, RG_E_CUDA, "graph capture not active");
+  return 0;
+}
+
+// a conditional node at the capture point of s; its body graph returned
+int add_cond(rg_system *h, cudaStream_t s, cudaGraphConditionalNodeType type,
+             cudaGraphConditionalHandle c, cudaGraph_t *body) {
+  cudaStreamCaptureStatus cs;
+  cudaGraph_t g;
+  const cudaGraphNode_t *deps = nullptr;
+  size_t nd = 0;
+  CK(cudaStreamGetCaptureInfo(s, &cs, nullptr, &g, &deps, nullptr, &nd));
+  cudaGraphNodeParams np{};
+  np.type = cudaGraphNodeTypeConditional;
+  np.conditional.handle = c;
+  np.conditional.type = type;
+  np.conditional.size = 1;
+  cudaGraphNode_t node;
+  CK(cudaGraphAddNode(&node, g, deps, nullptr, nd, &np));
+  *body = np.conditional.phGraph_out[0];
+  CK(cudaStreamUpdateCaptureDependencies(s, &node, nullptr, 1, cudaStreamSetCaptureDependencies));
+  return 0;
+}
+
+// one CG pass at capture level lvl: condition from the active count (also
+// into *started when given), WHILE { iteration }, then the pass's totals
+int cap_cg_pass(rg_system *h, int lvl, int pass, cudaGraphConditionalHandle *started) {
+  if (lvl + 1 >= kMaxCapLevels) return fail(h, RG_E_CUDA, "graph nesting too deep");
+  const Dev &d = h->d;
+  cudaStream_t s = h->cap_st[lvl], sb = h->cap_st[lvl + 1];
+  cudaGraph_t g, body;
+  int rc;
+  if ((rc = cap_graph(h, s, &g))) return rc;
+  cudaGraphConditionalHandle cl, cs0 = 0;
+  CK(cudaGraphConditionalHandleCreate(&cl, g, 0, 0));
+  if (started) {
+    CK(cudaGraphConditionalHandleCreate(started, g, 0, 0));
+    cs0 = *started;
+  }
+  launch_qeq_set_cond(d, s, cl, cs0);
+  if ((rc = add_cond(h, s, cudaGraphCondTypeWhile, cl, &body))) return rc;
+  CK(cudaStreamBeginCaptureToGraph(sb, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
+  // sp_trip CG iterations per loop trip (iterations past a system's
+  // convergence skip their work, as in the host-polled loop)
+  for (int k = 0; k < h->sp_trip; ++k) {
+    launch_qeq_cg_A(d, sb);
+    launch_qeq_spmv(d, sb, d.qd, d.qq, 1);
+    launch_qeq_cg_C(d, sb);
+  }
+  launch_qeq_loop_cond(d, sb, cl, 4 * (h->p.qeq_imax + 8) / h->sp_trip + 4);
+  cudaGraph_t out;
+  CK(cudaStreamEndCapture(sb, &out));
+  launch_qeq_tot(d, s, pass);
+  return 0;
+}
+
+// the mixed form's refinement pass p (1..3) at level lvl: the residual
+// check, then -- only where a segment needs it -- the restart and its CG
+// pass, then (if that pass iterated) the next check
+int cap_refine(rg_system *h, int lvl, int pass) {
+  if (lvl + 2 >= kMaxCapLevels) return fail(h, RG_E_CUDA, "graph nesting too deep");
+  const Dev &d = h->d;
+  cudaStream_t s = h->cap_st[lvl], s1 = h->cap_st[lvl + 1], s2 = h->cap_st[lvl + 2];
+  cudaGraph_t g, body;
+  int rc;
+  if ((rc = cap_graph(h, s, &g))) return rc;
+  launch_qeq_refine_check(d, s, h->p.qeq_tol);
+  launch_qeq_restart_count(d, s);
+  cudaGraphConditionalHandle cb;
+  CK(cudaGraphConditionalHandleCreate(&cb, g, 0, 0));
+  launch_qeq_set_cond(d, s, cb, 0);
+  if ((rc = add_cond(h, s, cudaGraphCondTypeIf, cb, &body))) return rc;
+  CK(cudaStreamBeginCaptureToGraph(s1, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
+  launch_qeq_cg_init_rest(d, s1, h->p.qeq_tol, h->p.qeq_imax);
+  cudaGraphConditionalHandle started = 0;
+  rc = cap_cg_pass(h, lvl + 1, pass, pass < 3 ? &started : nullptr);
+  if (!rc && pass < 3) {
+    cudaGraph_t body2, out2;
+    rc = add_cond(h, s1, cudaGraphCondTypeIf, started, &body2);
+    if (!rc) {
+      CK(cudaStreamBeginCaptureToGraph(s2, body2, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
+      rc = cap_refine(h, lvl + 2, pass + 1);
+      CK(cudaStreamEndCapture(s2, &out2));
+    }
+  }
+  cudaGraph_t out;
+  CK(cudaStreamEndCapture(s1, &out));
+  return rc;
+}
+
+int capture_single_point(rg_system *h, int eflag, int vflag, int atom_tally) {
+  Dev &d = h->d;
+  if (h->sp_exec) {
+    cudaGraphExecDestroy(h->sp_exec);
+    h->sp_exec = nullptr;
+  }
+  for (int k = 0; k < kMaxCapLevels; ++k)
+    if (!h->cap_st[k]) CK(cudaStreamCreateWithFlags(&h->cap_st[k], cudaStreamNonBlocking));
+  cudaStream_t main_st = h->st;
+  h->st = h->cap_st[0];    // the launch helpers use h->st
+  const long long launches0 = h->launches;
+  const bool lists0 = h->lists_valid, forces0 = h->forces_valid, tallies0 = h->tallies_valid;
+  const bool fresh0 = h->bonds_fresh;
+  cudaGraph_t g = nullptr;
+  int rc = 0;
+  cudaError_t e = cudaStreamBeginCapture(h->st, cudaStreamCaptureModeRelaxed);
+  if (e == cudaSuccess) {
+    const size_t n = (size_t)d.n;
+    cudaStream_t s = h->st;
+    cudaMemcpyAsync(d.hist_save, d.s_hist, 5 * n * sizeof(double), cudaMemcpyDeviceToDevice, s);
+    cudaMemcpyAsync(d.hist_save + 5 * n, d.t_hist, 5 * n * sizeof(double),
+                    cudaMemcpyDeviceToDevice, s);
+    cudaMemsetAsync(d.status, 0, RG_NSTATUS * sizeof(int), s);
+    cudaMemsetAsync(d.qeq_ctl, 0, 4 * sizeof(int), s);
+    cudaMemsetAsync(d.qeq_tot, 0, 2 * sizeof(int) * (size_t)d.nseg, s);
+    launch_bin_sort(d, s);
+    launch_build_nbrs(d, s);
+    launch_build_bonds(d, s);
+    launch_count(d, s);
+    launch_qeq_setup(d, s);
+    launch_qeq_cg_init(d, s, h->p.qeq_tol, h->p.qeq_imax);
+    rc = cap_cg_pass(h, 0, 0, nullptr);
+    if (!rc && d.mixed) rc = cap_refine(h, 0, 1);
+    if (!rc) {
+      launch_qeq_finish(d, s);
+      h->lists_valid = true;    // built by the captured kernels above
+      h->bonds_fresh = true;
+      rc = do_compute(h, eflag, vflag, atom_tally, true);
+    }
+    e = cudaStreamEndCapture(s, &g);
+  }
+  h->st = main_st;
+  h->launches = launches0;
+  h->lists_valid = lists0;
+  h->bonds_fresh = fresh0;
+  h->forces_valid = forces0;
+  h->tallies_valid = tallies0;
+  if (e == cudaSuccess && !rc) e = cudaGraphInstantiate(&h->sp_exec, g, 0);
+  if (e == cudaSuccess && !rc) {
+    size_t nn = 0;
+    cudaGraphGetNodes(g, nullptr, &nn);
+    std::vector<cudaGraphNode_t> nodes(nn);
+    cudaGraphGetNodes(g, nodes.data(), &nn);
+    long long k = 0;
+    for (auto nd : nodes) {
+      cudaGraphNodeType t;
+      if (cudaGraphNodeGetType(nd, &t) == cudaSuccess && t == cudaGraphNodeTypeKernel) ++k;
+    }
+    h->sp_kernels = k;
+  }
+  if (g) cudaGraphDestroy(g);
+  cudaGetLastError();
+  if (e != cudaSuccess || rc) {
+    h->sp_exec = nullptr;
+    h->sp_failed = true;
+    return rc ? rc : fail(h, RG_E_CUDA, std::string("single-point graph: ") + cudaGetErrorString(e));
+  }
+  h->sp_dev = d;
+  h->sp_flags = eflag | (vflag << 4) | (atom_tally << 8);
   return 0;
 }
 
@@ -900,6 +1104,9 @@ int rg_create(const char *ffield_path, const rg_params *pin, rg_system **out) {
     h->check_finite = cf && (cf[0] == '1' || cf[0] == '2');
     const char *ng = std::getenv("RG_NO_GRAPHS");
     h->use_graphs = !(ng && ng[0] == '1');
+    // CG iterations per device-side loop trip of the captured step (1-8)
+    const char *tr = std::getenv("RG_SP_TRIP");
+    if (tr && std::atoi(tr) >= 1 && std::atoi(tr) <= 8) h->sp_trip = std::atoi(tr);
     h->d.debug = cf && cf[0] == '2';
   }
   for (int t = 0; t < RG_MAXT; ++t) h->ff.nve_mass[t] = h->ff.sbp[t].mass;
@@ -992,6 +1199,9 @@ int rg_destroy(rg_system *h) {
   if (h->d_tab) cudaFree(h->d_tab);
   if (h->d_tab32) cudaFree(h->d_tab32);
   if (h->cg_exec) cudaGraphExecDestroy(h->cg_exec);
+  if (h->sp_exec) cudaGraphExecDestroy(h->sp_exec);
+  for (cudaStream_t c : h->cap_st)
+    if (c) cudaStreamDestroy(c);
   cudaStreamDestroy(h->st);
   delete h;
   return RG_OK;
@@ -1442,6 +1652,109 @@ int rg_qeq(rg_system *h, double *q_out, int *iters_s, int *iters_t) {
     CK(cudaMemcpyAsync(q_out, h->d.q_o, sizeof(double) * h->n, cudaMemcpyDeviceToHost, h->st));
     CK(cudaStreamSynchronize(h->st));
   }
+  return RG_OK;
+}
+
+int rg_single_point(rg_system *h, int eflag, int vflag, double *q_out, double *f_out,
+                    double *energies) {
+  if (!h) return RG_E_ARG;
+  if (!h->n) return fail(h, RG_E_STATE, "no atoms set");
+  CK(cudaSetDevice(h->p.device));
+  const int atom_tally = (eflag & 2) || (vflag & 4);
+  const int ef = eflag || energies != nullptr, vf = vflag & 3;
+  const int flags = ef | (vf << 4) | (atom_tally << 8);
+  Dev &d = h->d;
+  // the graph holds the device arrays, sizes and flags of its capture, and
+  // the cell grid of the boxes then: the host-side grid set-up runs first
+  // (a changed grid changes the arrays or sizes, so the step is recaptured)
+  int rc;
+  if (h->use_graphs && h->sp_exec && (rc = setup_cells(h))) return rc;
+  d.vflag = vf ? 1 : 0;
+  d.atom_tally = atom_tally ? 1 : 0;
+  const bool eligible = h->use_graphs && !h->prof.on && !h->check_finite && !h->sp_failed;
+  const bool replay = eligible && h->sp_exec && h->sp_flags == flags &&
+                      std::memcmp(&h->sp_dev, &d, sizeof(Dev)) == 0;
+  bool done = false;
+  if (replay) {
+    CK(cudaGraphLaunch(h->sp_exec, h->st));
+    int st[RG_NSTATUS], ctl[4], items[2];
+    const long long slots = (long long)d.n * d.bond_cap;
+    std::vector<int> tot(2 * (size_t)d.nseg);
+    CK(cudaMemcpyAsync(st, d.status, sizeof st, cudaMemcpyDeviceToHost, h->st));
+    CK(cudaMemcpyAsync(ctl, d.qeq_ctl, sizeof ctl, cudaMemcpyDeviceToHost, h->st));
+    CK(cudaMemcpyAsync(&items[0], d.w_off_v + slots, sizeof(int), cudaMemcpyDeviceToHost, h->st));
+    CK(cudaMemcpyAsync(&items[1], d.w_off_t + slots, sizeof(int), cudaMemcpyDeviceToHost, h->st));
+    CK(cudaMemcpyAsync(tot.data(), d.qeq_tot, tot.size() * sizeof(int), cudaMemcpyDeviceToHost,
+                       h->st));
+    CK(cudaStreamSynchronize(h->st));
+    const bool redo = (st[ST_OVF] != 0) || items[0] > d.cap_val || items[1] > d.cap_tor || ctl[2];
+    if (redo) {
+      // a list outgrew its capacity (or a CG loop hit its trip limit): the
+      // QEq histories go back to the step's start and the regular path,
+      // which regrows, redoes the step
+      const size_t n = (size_t)d.n;
+      CK(cudaMemcpyAsync(d.s_hist, d.hist_save, 5 * n * sizeof(double), cudaMemcpyDeviceToDevice,
+                         h->st));
+      CK(cudaMemcpyAsync(d.t_hist, d.hist_save + 5 * n, 5 * n * sizeof(double),
+                         cudaMemcpyDeviceToDevice, h->st));
+      h->lists_valid = false;
+      h->forces_valid = false;
+      h->stats.step_graph_redos++;
+    } else {
+      h->stats.step_graph_replays++;
+      int ms = 0, mt = 0;
+      for (int g = 0; g < d.nseg; ++g) {
+        ms = std::max(ms, tot[2 * g]);
+        mt = std::max(mt, tot[2 * g + 1]);
+      }
+      h->seg_iters.assign(tot.begin(), tot.end());
+      h->stats.cg_iters_s = ms;
+      h->stats.cg_iters_t = mt;
+      h->stats.cg_system_iters += std::max(ms - 1, 0) + std::max(mt - 1, 0);
+      h->stats.cg_spmv_rows_passes += std::max(std::max(ms, mt) - 1, 0);
+      h->stats.qeq_restarts = ctl[0];
+      h->stats.n_pairs = st[5];
+      h->stats.n_H_entries = st[5];
+      h->stats.n_bonds = st[6];
+      h->stats.n_hbond_pairs = st[7];
+      h->stats.max_nbrs = st[ST_MAXNB] + st[ST_MAXNF];
+      h->stats.max_bonds = st[ST_MAXB];
+      h->stats.max_hbonds = st[ST_MAXHB];
+      h->n_val = items[0];
+      h->n_tor = items[1];
+      h->launches += h->sp_kernels + (5LL * h->sp_trip + 1) * ctl[1];
+      h->lists_valid = true;
+      h->bonds_fresh = false;   // the replay's force step used them
+      h->forces_valid = true;
+      h->tallies_valid = atom_tally != 0;
+      if (st[ST_NAN]) return fail(h, RG_E_NUMERIC, "non-finite force");
+      done = true;
+    }
+  }
+  if (!done) {
+    if ((rc = do_qeq(h, nullptr, nullptr))) return rc;
+    if ((rc = do_compute(h, ef, vf, atom_tally))) return rc;
+    h->tallies_valid = atom_tally != 0;
+    int st[RG_NSTATUS];
+    if ((rc = read_status(h, st))) return rc;
+    if (st[ST_NAN]) return fail(h, RG_E_NUMERIC, "non-finite force");
+    // a configuration seen twice in a row is captured for the next call
+    // (one-off batches do not pay for a capture)
+    const bool again = h->sp_seen_flags == flags && std::memcmp(&h->sp_seen, &d, sizeof(Dev)) == 0;
+    h->sp_seen = d;
+    h->sp_seen_flags = flags;
+    if (eligible && again &&
+        !(h->sp_exec && h->sp_flags == flags && std::memcmp(&h->sp_dev, &d, sizeof(Dev)) == 0)) {
+      if ((rc = capture_single_point(h, ef, vf, atom_tally))) {
+        // the regular path keeps working; the reason stays in rg_last_error
+        (void)rc;
+      }
+    }
+  }
+  if (q_out) CK(cudaMemcpyAsync(q_out, d.q_o, sizeof(double) * h->n, cudaMemcpyDeviceToHost, h->st));
+  if (f_out) CK(cudaMemcpyAsync(f_out, d.f_o, 3 * sizeof(double) * h->n, cudaMemcpyDeviceToHost, h->st));
+  if (energies && (rc = energy_sum(h, energies))) return rc;
+  CK(cudaStreamSynchronize(h->st));
   return RG_OK;
 }
 

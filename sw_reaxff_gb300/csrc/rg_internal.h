@@ -269,6 +269,12 @@ struct Dev {
   int *dbg_flag;
   double *dbg;
 
+  // captured single-point step: QEq control on the device (qeq_ctl: 0
+  // restarts, 1 loop trips, 2 trip limit reached), per-segment CG iteration
+  // totals (qeq_tot[2 * nseg]), the histories saved at the step's start
+  int *qeq_ctl, *qeq_tot;
+  double *hist_save;     // [10][n]: s_hist then t_hist
+
   // per-atom tallies (LAMMPS eflag_atom / vflag_atom) of the nonbonded
   // pair terms, sorted order: eatom[n], vatom[6][n] (xx yy zz xy xz yz)
   int atom_tally;
@@ -565,7 +571,8 @@ void launch_atom_energy(const Dev &d, cudaStream_t st, int eflag);
 void launch_hbonds(const Dev &d, cudaStream_t st, int eflag);
 // work-list form: prep + count (then the host reads the totals), fill + run
 void launch_vt_count(const Dev &d, cudaStream_t st);
-void launch_vt_run(const Dev &d, cudaStream_t st, int eflag, long long nval, long long ntor);
+void launch_vt_run(const Dev &d, cudaStream_t st, int eflag, long long nval, long long ntor,
+                   bool device_counts = false);
 void launch_scan(const int *in, int *out, int n, int *bsum, cudaStream_t st);
 void launch_nonbonded(const Dev &d, cudaStream_t st, int eflag);
 void launch_dbond_forces(const Dev &d, cudaStream_t st);
@@ -581,6 +588,17 @@ void launch_qeq_cg_init_rest(const Dev &d, cudaStream_t st, double tol, int imax
 void launch_qeq_cg_A(const Dev &d, cudaStream_t st);
 void launch_qeq_cg_C(const Dev &d, cudaStream_t st);
 void launch_qeq_finish(const Dev &d, cudaStream_t st);
+// the captured step's QEq control (qeq.cu): set_cond sets the graph
+// conditions c1 (and c2 if nonzero) to "a segment is active"; loop_cond ends
+// a CG loop trip: its condition stays set while a segment is active and the
+// trips stay within the limit; tot adds the pass's iterations per segment
+// (less the set-up iteration after the first pass); restart counts a
+// refinement restart
+void launch_qeq_set_cond(const Dev &d, cudaStream_t st, unsigned long long c1,
+                         unsigned long long c2);
+void launch_qeq_loop_cond(const Dev &d, cudaStream_t st, unsigned long long c, int limit);
+void launch_qeq_tot(const Dev &d, cudaStream_t st, int pass);
+void launch_qeq_restart_count(const Dev &d, cudaStream_t st);
 
 // NVE
 void launch_nve_initial(const Dev &d, cudaStream_t st, double dt);

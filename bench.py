@@ -76,6 +76,8 @@ def parse():
                    help="skip the batched single-point measurement (512 small systems)")
     p.add_argument("--no-serve", action="store_true",
                    help="skip the serving-loop measurement (Poisson request stream)")
+    p.add_argument("--pair-kernel", type=int, default=0, choices=[0, 1, 2],
+                   help="pair-list build: 0 autotuned, 1 warp per atom, 2 per-cell tiles")
     p.add_argument("--no-water", action="store_true",
                    help="skip the 6,000-atom water measurement (2,000 H2O, 100 NVE steps)")
     p.add_argument("--water-cpu", action="store_true",
@@ -439,7 +441,8 @@ def gpu_arm(args):
     main_mixed = args.form == "mixed"
     if main_mixed:
         args.no_mixed = True          # the main handle is the mixed form itself
-    g = ReaxGPU(DEFAULT_FFIELD, device=local, precision=PREC_MIXED if main_mixed else 0)
+    g = ReaxGPU(DEFAULT_FFIELD, device=local, precision=PREC_MIXED if main_mixed else 0,
+                pair_kernel=args.pair_kernel)
     g.set_system(s)
     g.run(max(args.warmup, 1), DT, energies=False)          # setup + warm-up steps
     # phase breakdown from a separate, profiled run (events around every
@@ -486,7 +489,8 @@ def gpu_arm(args):
     mixed = None
     if not args.no_mixed:
         from sw_reaxff_gb300.api import PREC_MIXED
-        gm = ReaxGPU(DEFAULT_FFIELD, device=local, precision=PREC_MIXED)
+        gm = ReaxGPU(DEFAULT_FFIELD, device=local, precision=PREC_MIXED,
+                     pair_kernel=args.pair_kernel)
         gm.set_system(s)
         gm.run(max(args.warmup, 1), DT, energies=False)
         sm = torch.cuda.ExternalStream(gm.stream())
@@ -510,7 +514,9 @@ def gpu_arm(args):
                  "ms_per_step": tm * 1e3 / args.steps, "speedup_vs_fp64": tmax / tm,
                  "phases_ms_per_step": {k: round(v[0] / psteps, 4)
                                         for k, v in pm.items() if v[1] > 0},
-                 "autotuned": {"cell_div": smx["cell_div"], "spmv_lanes_per_row": smx["spmv_rows"]},
+                 "autotuned": {"cell_div": smx["cell_div"], "spmv_lanes_per_row": smx["spmv_rows"],
+                               "pair_kernel": "cell tiles" if smx["pair_kernel"] == 2
+                               else "warp per atom"},
                  "fp64_fallback_items": {"angles": smx["fp64_angles"],
                                          "torsions": smx["fp64_torsions"]}}
 
@@ -626,7 +632,8 @@ def gpu_arm(args):
         "phases_ms_per_step": {k: round(v[0] / psteps, 4) for k, v in phases.items()},
         "counts": {"pairs": st["n_pairs"], "bonds": st["n_bonds"], "hbond_pairs": st["n_hbond_pairs"],
                    "cg_iters_s": st["cg_iters_s"], "cg_iters_t": st["cg_iters_t"]},
-        "autotuned": {"cell_div": st["cell_div"], "spmv_lanes_per_row": st["spmv_rows"]},
+        "autotuned": {"cell_div": st["cell_div"], "spmv_lanes_per_row": st["spmv_rows"],
+                      "pair_kernel": "cell tiles" if st["pair_kernel"] == 2 else "warp per atom"},
         "hbm_peak_gbs": peaks.get("hbm_gbs"),
     }
     line["gpu_launches"] = int(launches)

@@ -86,6 +86,10 @@ typedef struct {
                            or cutoff/3 (3 only where every cell width is at
                            least the cutoff), not tuned */
   int spmv_rows;        /* 0 (default): as above; 8, 16 or 32: fixed */
+  int pair_kernel;      /* pair-list build: 0 (default) autotuned with the
+                           cell division (the warp walk when autotuning is
+                           off); 1 one warp per atom; 2 per-cell tiles staged
+                           in shared memory */
 } rg_params;
 
 /* Energy vector of rg_compute: entries 0..13 are the pair's pvector in the
@@ -122,6 +126,8 @@ typedef struct {
                                   of the captured step */
   long long step_graph_redos;  /* replays that met a list past its capacity
                                   and redid the step on the regular path */
+  int pair_kernel;             /* the pair-list build in use: 1 warp per atom,
+                                  2 per-cell tiles */
 } rg_stats;
 
 void rg_default_params(rg_params *p);

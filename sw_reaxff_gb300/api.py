@@ -45,7 +45,7 @@ class Params(C.Structure):
                 ("qeq_tol", C.c_double), ("qeq_imax", C.c_int),
                 ("precision", C.c_int), ("device", C.c_int), ("tabulate", C.c_int),
                 ("tabulate_check", C.c_int), ("autotune", C.c_int), ("cell_div", C.c_int),
-                ("spmv_rows", C.c_int)]
+                ("spmv_rows", C.c_int), ("pair_kernel", C.c_int)]
 
 
 class Stats(C.Structure):
@@ -58,7 +58,8 @@ class Stats(C.Structure):
                 ("qeq_restarts", C.c_int), ("fp64_angles", C.c_int),
                 ("fp64_torsions", C.c_int), ("cell_div", C.c_int), ("spmv_rows", C.c_int),
                 ("cg_system_iters", C.c_longlong), ("cg_spmv_rows_passes", C.c_longlong),
-                ("step_graph_replays", C.c_longlong), ("step_graph_redos", C.c_longlong)]
+                ("step_graph_replays", C.c_longlong), ("step_graph_redos", C.c_longlong),
+                ("pair_kernel", C.c_int)]
 
 
 class ReaxError(RuntimeError):

@@ -240,6 +240,64 @@ __device__ __forceinline__ bool near_exact(double e2, const Control &C) {
 // outcome is the FP64 one
 constexpr float MARGIN32 = 1e-5f;
 
+// QEq H_ij of a listed pair from its r^2: the mixed form in FP32 from the
+// FP32 r^2 (h32), the FP64 form from the FMA-rounded FP64 r^2 (h), from the
+// FP64 table or analytically
+template <bool MIXED>
+__device__ __forceinline__ void pair_h(const Dev &d, const Control &C, const ForceField &F,
+                                       int ti, int tj, double d2, float d2f, double &h,
+                                       float &h32) {
+  h = 0.0;
+  h32 = 0.f;
+  if (MIXED) {
+    if (d2f <= C.swb2_f) {
+      // FP32: factored taper when swa = 0
+      const float r = d2f * rsqrtf(d2f);
+      float tp;
+      if (C.qtap_factored) {
+        const float t = r * C.inv_swb_q_f, u = 1.f - t, u2 = u * u;
+        tp = u2 * u2 * (1.f + t * (4.f + t * (10.f + t * 20.f)));
+      } else {
+        const float *T = C.qTap_f;
+        tp = fmaf(T[7], r, T[6]);
+        tp = fmaf(tp, r, T[5]);
+        tp = fmaf(tp, r, T[4]);
+        tp = fmaf(tp, r, T[3]);
+        tp = fmaf(tp, r, T[2]);
+        tp = fmaf(tp, r, T[1]);
+        tp = fmaf(tp, r, T[0]);
+      }
+      const float x = fmaf(d2f, r, C.nb32[ti][tj].gamma);
+      h32 = tp * 14.4f * rcbrtf(x);
+    }
+  } else if (!(C.h_all_listed || d2 <= C.swb2)) {
+    h = 0.0;
+  } else if (C.tab_n && d2f >= C.tab_s0_f) {
+    // FP64 table of H_ij (cubic Hermite in r^2, power basis per interval)
+    const double x = fma(d2, C.tab_inv_ds, C.tab_x0);
+    int k = (int)x;
+    if (k > C.tab_n - 1) k = C.tab_n - 1;
+    const double u = x - (double)k;
+    const double2 *T =
+        reinterpret_cast<const double2 *>(d.tab_h + ((long long)C.tab_pair[ti][tj] * C.tab_n + k) * 4);
+    const double2 c01 = T[0], c23 = T[1];
+    h = fma(fma(fma(c23.y, u, c23.x), u, c01.y), u, c01.x);
+  } else {
+    // H_ij = Tap(r) * 14.4 / (r^3 + shld)^c, c = 0.3333333333333
+    const double r = d2 * rsqrt(d2);
+    const double *T = C.qTap;
+    double tp = fma(T[7], r, T[6]);
+    tp = fma(tp, r, T[5]);
+    tp = fma(tp, r, T[4]);
+    tp = fma(tp, r, T[3]);
+    tp = fma(tp, r, T[2]);
+    tp = fma(tp, r, T[1]);
+    tp = fma(tp, r, T[0]);
+    const double x = fma(d2, r, F.tbp[ti][tj].gamma);
+    h = tp * 14.4 * rpow_third(x, RG_C3_QEQ);
+  }
+}
+
 template <bool MIXED>
 __device__ __forceinline__ void nbr_flush(const Dev &d, const Control &C, const ForceField &F,
                                           const NbrQueue &Q, int cnt, int lane, int i,
@@ -299,53 +357,7 @@ __device__ __forceinline__ void nbr_flush(const Dev &d, const Control &C, const 
   const int tj = __float_as_int(d.xf[j].w);
   double h = 0.0;
   float h32 = 0.f;
-  if (MIXED) {
-    if (d2f <= C.swb2_f) {
-      // FP32: factored taper when swa = 0
-      const float r = d2f * rsqrtf(d2f);
-      float tp;
-      if (C.qtap_factored) {
-        const float t = r * C.inv_swb_q_f, u = 1.f - t, u2 = u * u;
-        tp = u2 * u2 * (1.f + t * (4.f + t * (10.f + t * 20.f)));
-      } else {
-        const float *T = C.qTap_f;
-        tp = fmaf(T[7], r, T[6]);
-        tp = fmaf(tp, r, T[5]);
-        tp = fmaf(tp, r, T[4]);
-        tp = fmaf(tp, r, T[3]);
-        tp = fmaf(tp, r, T[2]);
-        tp = fmaf(tp, r, T[1]);
-        tp = fmaf(tp, r, T[0]);
-      }
-      const float x = fmaf(d2f, r, C.nb32[ti][tj].gamma);
-      h32 = tp * 14.4f * rcbrtf(x);
-    }
-  } else if (!(C.h_all_listed || d2 <= C.swb2)) {
-    h = 0.0;
-  } else if (C.tab_n && d2f >= C.tab_s0_f) {
-    // FP64 table of H_ij (cubic Hermite in r^2, power basis per interval)
-    const double x = fma(d2, C.tab_inv_ds, C.tab_x0);
-    int k = (int)x;
-    if (k > C.tab_n - 1) k = C.tab_n - 1;
-    const double u = x - (double)k;
-    const double2 *T =
-        reinterpret_cast<const double2 *>(d.tab_h + ((long long)C.tab_pair[ti][tj] * C.tab_n + k) * 4);
-    const double2 c01 = T[0], c23 = T[1];
-    h = fma(fma(fma(c23.y, u, c23.x), u, c01.y), u, c01.x);
-  } else {
-    // H_ij = Tap(r) * 14.4 / (r^3 + shld)^c, c = 0.3333333333333
-    const double r = d2 * rsqrt(d2);
-    const double *T = C.qTap;
-    double tp = fma(T[7], r, T[6]);
-    tp = fma(tp, r, T[5]);
-    tp = fma(tp, r, T[4]);
-    tp = fma(tp, r, T[3]);
-    tp = fma(tp, r, T[2]);
-    tp = fma(tp, r, T[1]);
-    tp = fma(tp, r, T[0]);
-    const double x = fma(d2, r, F.tbp[ti][tj].gamma);
-    h = tp * 14.4 * rpow_third(x, RG_C3_QEQ);
-  }
+  pair_h<MIXED>(d, C, F, ti, tj, d2, d2f, h, h32);
   if (in) {
     const int p = near ? baseN + __popc(mn & lanemask_lt()) : baseF + __popc(mf & lanemask_lt());
     if (p < (near ? capN : capF)) {
@@ -481,6 +493,235 @@ __global__ void __launch_bounds__(NB_WARPS * 32, 3) k_build_nbrs(Dev d) {
     }
   }
   if (qn > 0) nbr_flush<MIXED>(d, C, F, Q, qn, lane, i, xi, xif, xil, ti, g);
+}
+
+// -------------------------------------------------------------------
+// pair list + QEq H values, per-cell tiles (the alternative the autotuner
+// may pick over the warp-per-atom walk above)
+//
+// One block per cell A.  Its atoms, then each run of neighbour cells of the
+// same half stencil (chunks of TB atoms), are staged in shared memory, FP32
+// (hi, lo) and FP64 positions; every (a, b) pair of the tile is prefiltered
+// in FP32 from shared memory into a queue.  For the queued pairs the block
+// decides list membership and the near/far split of each direction (exactly
+// as the warp walk), counts each row's new entries with shared atomics,
+// claims the rows' slots with one global atomic per row part and tile,
+// evaluates H once per pair and writes both directed entries.  The per-atom
+// stencil loop and its per-candidate global loads become one pass per cell.
+
+constexpr int TILE_T = 128;   // threads per block
+constexpr int TA = 64;        // A atoms per tile
+constexpr int TB = 128;       // neighbour atoms per tile
+constexpr int TQ = 1024;      // candidate pairs per queue pass
+
+struct PairTile {
+  double4 ax[TA], bx[TB];
+  float4 af[TA], al[TA], bf[TB], bl[TB];
+  double d2[TQ];                 // FP64 form: FMA-rounded r^2 of queued pairs
+  float d2f[TQ];
+  uint32_t q[TQ];                // queued pair (a << 16) | b
+  unsigned short rk[TQ][2];      // entry's rank in a's row part, in b's
+  unsigned char fl[TQ];          // 1 in, 2 near, 4 mirror in, 8 mirror near
+  int cnt[2][TA + TB];           // per row part: new entries, then claimed base
+  int nq;
+};
+
+__device__ __forceinline__ int seg_of_cell(const Dev &d, int c) {
+  int lo = 0, hi = d.nseg - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (d.seg[mid].cell0 <= c) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
+}
+
+__device__ __forceinline__ double exact_d2v(const double4 &xj, int sx, int sy, int sz,
+                                           const double4 &xi, const SegGeom &g) {
+  double dx, dy, dz;
+  disp64(g, xj, xi, sx, sy, sz, dx, dy, dz);
+  return __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
+}
+
+template <bool MIXED>
+__global__ void __launch_bounds__(TILE_T) k_build_nbrs_tiles(Dev d) {
+  __shared__ PairTile T;
+  const int c = blockIdx.x;
+  const int a_beg = d.cell_start[c], a_end = d.cell_start[c + 1];
+  if (a_beg >= a_end) return;
+  const Control &C = *d.ctl;
+  const ForceField &F = *d.ff;
+  const SegGeom &g = d.seg[seg_of_cell(d, c)];
+  const int ncx = g.nc[0], ncy = g.nc[1], ncz = g.nc[2], S = g.S;
+  const int cl = c - g.cell0;
+  const int cx = cl % ncx, cy = (cl / ncx) % ncy, cz = cl / (ncx * ncy);
+  const float cut2f = C.list_pre2_f;
+  const float lc2 = C.list_cut2_f, nc2 = C.near_cut_f * C.near_cut_f;
+  const bool clip = !g.tri;
+  const float wx = g.cellw_f[0], wy = g.cellw_f[1], wz = g.cellw_f[2];
+  const int tid = threadIdx.x;
+  const int capN = d.nb_capN, capF = d.nb_cap - d.nb_capN;
+  for (int a0 = a_beg; a0 < a_end; a0 += TA) {
+    const int na = min(TA, a_end - a0);
+    __syncthreads();
+    for (int k = tid; k < na; k += TILE_T) {
+      T.ax[k] = d.xs[a0 + k];
+      T.af[k] = d.xf[a0 + k];
+      T.al[k] = d.xl[a0 + k];
+    }
+    for (int oz = 0; oz <= S; ++oz) {
+      int rz = cz + oz, sz = 0;
+      while (rz >= ncz) { rz -= ncz; ++sz; }
+      // orthogonal: gaps between cell A's slab and the row's (FP32 with the
+      // prefilter's margin)
+      const float gz = clip ? (float)max(0, oz - 1) * wz : 0.f;
+      if (gz * gz > cut2f) continue;
+      for (int oy = (oz == 0 ? 0 : -S); oy <= S; ++oy) {
+        int ry = cy + oy, sy = 0;
+        while (ry < 0) { ry += ncy; --sy; }
+        while (ry >= ncy) { ry -= ncy; ++sy; }
+        const float gy = clip ? (float)max(0, abs(oy) - 1) * wy : 0.f;
+        const float r2 = cut2f - gz * gz - gy * gy;
+        if (r2 < 0.f) continue;
+        int ox_lo = (oz == 0 && oy == 0) ? 0 : -S, ox_hi = S;
+        if (clip) {
+          const int m = 1 + (int)floorf(sqrtf(r2) / wx);
+          ox_lo = max(ox_lo, -m);
+          ox_hi = min(ox_hi, m);
+        }
+        const int rowcell = g.cell0 + (rz * ncy + ry) * ncx;
+        int ox = ox_lo;
+        while (ox <= ox_hi) {
+          int rx = cx + ox, sx = 0;
+          while (rx < 0) { rx += ncx; --sx; }
+          while (rx >= ncx) { rx -= ncx; ++sx; }
+          int len = 1;
+          while (ox + len <= ox_hi && rx + len < ncx) ++len;
+          const int beg = d.cell_start[rowcell + rx];
+          const int end = d.cell_start[rowcell + rx + len];
+          ox += len;
+          float shx, shy, shz;
+          img_vec32(g, sx, sy, sz, shx, shy, shz);
+          // image 0 arises only at offset (0, 0, ox >= 0): the partners of
+          // an atom there are the atoms after it
+          const bool self_img = (sx == 0 && sy == 0 && sz == 0);
+          const uint32_t img = (uint32_t)img_pack(sx, sy, sz);
+          const uint32_t img_m = (uint32_t)img_pack(-sx, -sy, -sz);
+          for (int b0 = beg; b0 < end; b0 += TB) {
+            const int nb = min(TB, end - b0);
+            const int nrow = na + nb;
+            __syncthreads();
+            for (int k = tid; k < nb; k += TILE_T) {
+              T.bx[k] = d.xs[b0 + k];
+              T.bf[k] = d.xf[b0 + k];
+              T.bl[k] = d.xl[b0 + k];
+            }
+            for (int k = tid; k < nrow; k += TILE_T) T.cnt[0][k] = T.cnt[1][k] = 0;
+            if (tid == 0) T.nq = 0;
+            __syncthreads();
+            const int np = na * nb;
+            for (int p0 = 0; p0 < np; p0 += TQ) {
+              const int pe = min(np, p0 + TQ);
+              // FP32 prefilter of the tile's pairs into the queue
+              for (int p = p0 + tid; p < pe; p += TILE_T) {
+                const int a = p / nb, b = p - a * nb;
+                if (self_img && b0 + b <= a0 + a) continue;
+                const float4 xa = T.af[a], xb = T.bf[b];
+                const float fx = xb.x + shx - xa.x;
+                const float fy = xb.y + shy - xa.y;
+                const float fz = xb.z + shz - xa.z;
+                if (fx * fx + fy * fy + fz * fz <= cut2f) {
+                  const int slot = atomicAdd(&T.nq, 1);
+                  T.q[slot] = ((uint32_t)a << 16) | (uint32_t)b;
+                }
+              }
+              __syncthreads();
+              const int nq = T.nq;
+              // membership and near/far of each direction; rows' ranks
+              for (int k = tid; k < nq; k += TILE_T) {
+                const int a = (int)(T.q[k] >> 16), b = (int)(T.q[k] & 0xffffu);
+                float dx, dy, dz;
+                disp32(g, T.bf[b], T.bl[b], T.af[a], T.al[a], sx, sy, sz, dx, dy, dz);
+                const float d2f = dx * dx + dy * dy + dz * dz;
+                bool in = false, near = false, in_m = false, near_m = false;
+                if (d2f <= lc2 * (1.f - MARGIN32)) {
+                  in = in_m = true;
+                } else if (d2f <= lc2 * (1.f + MARGIN32)) {
+                  in = exact_d2v(T.bx[b], sx, sy, sz, T.ax[a], g) <= C.list_cut2;
+                  in_m = exact_d2v(T.ax[a], -sx, -sy, -sz, T.bx[b], g) <= C.list_cut2;
+                }
+                if (MIXED) {
+                  near = near_m = d2f <= nc2 * (1.f + MARGIN32);
+                } else if (in || in_m) {
+                  if (d2f <= nc2 * (1.f - MARGIN32)) {
+                    near = near_m = true;
+                  } else if (d2f <= nc2 * (1.f + MARGIN32)) {
+                    near = near_exact(exact_d2v(T.bx[b], sx, sy, sz, T.ax[a], g), C);
+                    near_m = near_exact(exact_d2v(T.ax[a], -sx, -sy, -sz, T.bx[b], g), C);
+                  }
+                }
+                double d2 = 0.0;
+                if (!MIXED && (in || in_m)) {
+                  double ex, ey, ez;
+                  disp64(g, T.bx[b], T.ax[a], sx, sy, sz, ex, ey, ez);
+                  d2 = fma(ex, ex, fma(ey, ey, ez * ez));
+                }
+                T.d2[k] = d2;
+                T.d2f[k] = d2f;
+                T.fl[k] = (unsigned char)((in ? 1 : 0) | (near ? 2 : 0) | (in_m ? 4 : 0) |
+                                          (near_m ? 8 : 0));
+                T.rk[k][0] = in ? (unsigned short)atomicAdd(&T.cnt[near ? 0 : 1][a], 1) : 0;
+                T.rk[k][1] = in_m ? (unsigned short)atomicAdd(&T.cnt[near_m ? 0 : 1][na + b], 1) : 0;
+              }
+              __syncthreads();
+              // claim each row part's slots once per tile pass
+              for (int k = tid; k < 2 * nrow; k += TILE_T) {
+                const int part = k / nrow, t = k - part * nrow;
+                const int cnt = T.cnt[part][t];
+                const int row = t < na ? a0 + t : b0 + (t - na);
+                T.cnt[part][t] = cnt ? atomicAdd(part == 0 ? &d.n_near[row] : &d.n_far[row], cnt) : 0;
+              }
+              __syncthreads();
+              // H once per pair, both entries
+              for (int k = tid; k < nq; k += TILE_T) {
+                const int a = (int)(T.q[k] >> 16), b = (int)(T.q[k] & 0xffffu);
+                const int f = T.fl[k];
+                if (!(f & 5)) continue;
+                const int ta = __float_as_int(T.af[a].w), tb = __float_as_int(T.bf[b].w);
+                double h;
+                float h32;
+                pair_h<MIXED>(d, C, F, ta, tb, T.d2[k], T.d2f[k], h, h32);
+                if (f & 1) {
+                  const bool nr = f & 2;
+                  const int pos = T.cnt[nr ? 0 : 1][a] + T.rk[k][0];
+                  if (pos < (nr ? capN : capF)) {
+                    const long long slot = (long long)(a0 + a) * d.nb_cap + (nr ? pos : capN + pos);
+                    d.nbr[slot] = ((uint32_t)(b0 + b) << 8) | img;
+                    if (MIXED) d.hval32[slot] = h32;
+                    else d.hval[slot] = h;
+                  }
+                }
+                if (f & 4) {
+                  const bool nr = f & 8;
+                  const int pos = T.cnt[nr ? 0 : 1][na + b] + T.rk[k][1];
+                  if (pos < (nr ? capN : capF)) {
+                    const long long slot = (long long)(b0 + b) * d.nb_cap + (nr ? pos : capN + pos);
+                    d.nbr[slot] = ((uint32_t)(a0 + a) << 8) | img_m;
+                    if (MIXED) d.hval32[slot] = h32;
+                    else d.hval[slot] = h;
+                  }
+                }
+              }
+              __syncthreads();
+              for (int k = tid; k < nrow; k += TILE_T) T.cnt[0][k] = T.cnt[1][k] = 0;
+              if (tid == 0) T.nq = 0;
+              __syncthreads();
+            }
+          }
+        }
+      }
+    }
+  }
 }
 
 // after the build: rows whose parts overflowed their capacity, and the
@@ -827,8 +1068,13 @@ void launch_build_nbrs(const Dev &d, cudaStream_t st) {
   // the part counters are claimed atomically by the build
   cudaMemsetAsync(d.n_near, 0, sizeof(int) * (size_t)d.n, st);
   cudaMemsetAsync(d.n_far, 0, sizeof(int) * (size_t)d.n, st);
-  if (d.mixed) k_build_nbrs<true><<<G, B, 0, st>>>(d);
-  else k_build_nbrs<false><<<G, B, 0, st>>>(d);
+  if (d.nbr_tiles) {
+    if (d.mixed) k_build_nbrs_tiles<true><<<d.ncell, TILE_T, 0, st>>>(d);
+    else k_build_nbrs_tiles<false><<<d.ncell, TILE_T, 0, st>>>(d);
+  } else {
+    if (d.mixed) k_build_nbrs<true><<<G, B, 0, st>>>(d);
+    else k_build_nbrs<false><<<G, B, 0, st>>>(d);
+  }
   k_nbr_check<<<(d.n + 255) / 256, 256, 0, st>>>(d);
 }
 

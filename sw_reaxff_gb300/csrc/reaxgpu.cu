@@ -481,16 +481,27 @@ int autotune(rg_system *h) {
   int rc = 0;
   float best = 1e30f;
   int best_div = h->p.cell_div ? h->p.cell_div : 2;
-  for (int div : {2, 3}) {
-    if (h->p.cell_div) break;                 // fixed by the caller
-    if (div == 3 && !div3_ok(h)) continue;
-    h->cell_div = div;
-    if ((rc = build_lists(h))) break;   // capacities for this cell size
-    float ms = 0.f;
-    if ((rc = timed([&] { launch_bin_sort(d, h->st); launch_build_nbrs(d, h->st); }, 2, ms))) break;
-    if (ms < best) best = ms, best_div = div;
+  int best_tiles = h->p.pair_kernel == 2 ? 1 : 0;
+  const bool tune_div = !h->p.cell_div, tune_kernel = !h->p.pair_kernel;
+  if (tune_div || tune_kernel) {
+    for (int div : {2, 3}) {
+      if (!tune_div && div != h->p.cell_div) continue;
+      if (div == 3 && !div3_ok(h)) continue;
+      h->cell_div = div;
+      for (int tiles : {0, 1}) {
+        if (!tune_kernel && tiles != best_tiles) continue;
+        d.nbr_tiles = tiles;
+        if ((rc = build_lists(h))) break;   // capacities for this configuration
+        float ms = 0.f;
+        if ((rc = timed([&] { launch_bin_sort(d, h->st); launch_build_nbrs(d, h->st); }, 2, ms)))
+          break;
+        if (ms < best) best = ms, best_div = div, best_tiles = tiles;
+      }
+      if (rc) break;
+    }
   }
   h->cell_div = best_div;
+  d.nbr_tiles = best_tiles;
   if (!rc) rc = build_lists(h);
   if (!rc && !h->p.spmv_rows) {
     // SpMV lanes per row on the list just built (a zero vector: timing only)
@@ -1098,6 +1109,7 @@ int rg_create(const char *ffield_path, const rg_params *pin, rg_system **out) {
     return RG_E_ARG;
   }
   if (h->p.cell_div) h->cell_div = h->p.cell_div;
+  h->d.nbr_tiles = h->p.pair_kernel == 2 ? 1 : 0;
   if (h->p.spmv_rows) h->d.spmv_rw = h->p.spmv_rows;
   {
     const char *cf = std::getenv("RG_CHECK_FINITE");
@@ -1907,6 +1919,7 @@ int rg_get_stats(const rg_system *h, rg_stats *s) {
   s->fp64_angles = s->fp64_torsions = 0;
   s->cell_div = h->cell_div;
   s->spmv_rows = h->d.spmv_rw;
+  s->pair_kernel = h->d.nbr_tiles ? 2 : 1;
   if (h->d.mixed && h->d.fb_cnt) {
     int fb[2] = {0, 0};
     if (cudaMemcpyAsync(fb, h->d.fb_cnt, sizeof fb, cudaMemcpyDeviceToHost, h->st) == cudaSuccess &&

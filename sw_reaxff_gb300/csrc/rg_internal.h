@@ -159,6 +159,7 @@ struct Dev {
   int n;              // atoms
   int mixed;          // 1: FP32 arithmetic in the pair / bond kernels
   int nb_cap;         // neighbour row capacity (row-major rows)
+  int nbr_tiles;      // pair-list kernel: 0 warp per atom, 1 per-cell tiles
   int nb_capN;        // the first nb_capN slots of a row hold its near
                       // entries, the remaining nb_cap - nb_capN its far ones
   int bond_cap;       // bond slots per atom (slot-major: k*n + i)

@@ -8,7 +8,8 @@ regrow (FP64 form).
   frozen oracle trajectory of tests/golden/traj/water6k_nve100.npz, whose
   charges come from the reference's own QEq driver every step.
 * A 52,428-atom H2O/CH4/C2H6/NH3 mixture (the 1,048,576-atom mixture at
-  1/20 scale) with cells of cutoff/2 and of cutoff/3: pair, bond and
+  1/20 scale) with cells of cutoff/2 and of cutoff/3, the pair list built
+  by one warp per atom and by per-cell tiles: pair, bond and
   H-bond lists bit-exact, energies and forces at the 1e-9 bars with the
   oracle's charges, charges within 1e-5 e.
 * A water slab in a box twice its length: the capacities estimated from
@@ -130,10 +131,11 @@ def mixture52k(ffield):
     return s, o, qo, fo, eo
 
 
+@pytest.mark.parametrize("pair_kernel", [1, 2], ids=["warp_walk", "cell_tiles"])
 @pytest.mark.parametrize("cell_div", [2, 3])
-def test_mixture52k(mixture52k, ffield, cell_div):
+def test_mixture52k(mixture52k, ffield, cell_div, pair_kernel):
     s, o, (qo, _, _), fo, eo = mixture52k
-    g = ReaxGPU(ffield, cell_div=cell_div, autotune=0)
+    g = ReaxGPU(ffield, cell_div=cell_div, pair_kernel=pair_kernel, autotune=0)
     g.set_system(s)
     qg, _, _ = g.qeq()
     assert np.abs(qg - qo).max() < 1e-5

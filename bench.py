@@ -504,12 +504,34 @@ def gpu_arm(args):
         gm.synchronize()
         dist.barrier()
         tm = dist.max(m0.elapsed_time(m1) / 1e3)
+        sm0 = gm.stats()
         gm.profile(True)
         gm.run(psteps, DT, energies=False)
         gm.synchronize()
         pm = gm.profile_get()
         gm.profile(False)
-        smx = gm.stats()
+        smx = sm1 = gm.stats()
+        live_m = pm["qeq_spmv"]
+        # the mixed SpMV against HBM: 8 bytes (index + FP32 H) per entry
+        # streamed per launch with work, and the half-symmetric algorithmic
+        # 4 bytes per directed entry (+ 48 B of vector traffic per atom)
+        # (events around every kernel group in the profiled steps)
+        passes = sm1["cg_spmv_rows_passes"] - sm0["cg_spmv_rows_passes"]
+        ent = sm1["n_pairs"]
+        hbm_peak_m = measured_peaks().get("hbm_gbs")
+        t_spmv = live_m[0] * 1e-3
+        read_b = (8.0 * ent + 48.0 * n) * passes
+        alg_b = (4.0 * ent + 48.0 * n) * passes
+        mixed_roof = {"kernel": "k_spmv32", "bound": "hbm", "launches_timed": live_m[1],
+                      "launches_with_work": passes,
+                      "avg_launch_ms": live_m[0] / max(live_m[1], 1),
+                      "streamed_gbs": read_b / t_spmv / 1e9 if t_spmv > 0 else None,
+                      "algorithmic_gbs": alg_b / t_spmv / 1e9 if t_spmv > 0 else None,
+                      "peak_gbs": hbm_peak_m,
+                      "frac_streamed": read_b / t_spmv / 1e9 / hbm_peak_m
+                      if t_spmv > 0 and hbm_peak_m else None,
+                      "frac_algorithmic": alg_b / t_spmv / 1e9 / hbm_peak_m
+                      if t_spmv > 0 and hbm_peak_m else None}
         mixed = {"value": n * args.steps * world / tm, "unit": UNIT,
                  "ms_per_step": tm * 1e3 / args.steps, "speedup_vs_fp64": tmax / tm,
                  "phases_ms_per_step": {k: round(v[0] / psteps, 4)
@@ -518,7 +540,8 @@ def gpu_arm(args):
                                "pair_kernel": "cell tiles" if smx["pair_kernel"] == 2
                                else "warp per atom"},
                  "fp64_fallback_items": {"angles": smx["fp64_angles"],
-                                         "torsions": smx["fp64_torsions"]}}
+                                         "torsions": smx["fp64_torsions"]},
+                 "spmv_roofline": mixed_roof}
 
     # end to end through the C ABI with host (pinned) buffers: per step the
     # state x, v, f goes host->device, the step runs, x, v, q, f come back

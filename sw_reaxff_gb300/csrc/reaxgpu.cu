@@ -73,6 +73,19 @@ struct Prof {
   }
 };
 
+// one captured step (see rg_single_point / rg_run)
+struct StepGraph {
+  cudaGraphExec_t exec = nullptr;
+  Dev dev{};                        // the device arrays and sizes it holds
+  int flags = -1;                   // eflag | vflag << 4 | tallies << 8
+  double dt = 0.0;                  // MD step: the time step (0: single point)
+  long long kernels = 0;            // top-level kernel nodes of one replay
+  bool failed = false;              // a capture failed: the regular path only
+  Dev seen{};                       // the previous regular step's arrays,
+  int seen_flags = -1;              // flags and time step: a repeat of them
+  double seen_dt = -1.0;            // is captured
+};
+
 struct rg_system {
   rg_params p{};
   ForceField ff{};
@@ -125,16 +138,12 @@ struct rg_system {
   Dev cg_dev{};
   bool use_graphs = true;
   // the whole single-point step (lists, QEq with device-side loops, force
-  // step) as one captured graph (rg_single_point), recaptured when the
-  // device arrays, sizes or flags change; streams for the conditional bodies
-  cudaGraphExec_t sp_exec = nullptr;
-  Dev sp_dev{};
-  int sp_flags = -1;
-  long long sp_kernels = 0;         // top-level kernel nodes of one replay
-  bool sp_failed = false;           // a capture failed: the regular path only
+  // step; rg_single_point) and the whole MD step (the same between the two
+  // Verlet half-steps; rg_run) as captured graphs, recaptured when the
+  // device arrays, sizes, flags or time step change; streams for the
+  // conditional bodies
+  StepGraph sp, md;
   int sp_trip = 4;                  // CG iterations per device-side loop trip
-  Dev sp_seen{};                    // the previous regular call's arrays and
-  int sp_seen_flags = -1;           // flags: a repeat of them is captured
   cudaStream_t cap_st[8] = {nullptr};
   rg_stats stats{};
   double energy[RG_NE] = {0};
@@ -390,7 +399,7 @@ int alloc_atoms(rg_system *h, int n) {
   r |= dalloc(h, B, &d.cell_o, (size_t)n);
   r |= dalloc(h, B, &d.perm, (size_t)n);
   r |= dalloc(h, B, &d.iperm, (size_t)n);
-  r |= dalloc(h, B, &d.hist_save, 10 * (size_t)n);
+  r |= dalloc(h, B, &d.hist_save, 19 * (size_t)n);
   r |= dalloc(h, B, &d.eatom, (size_t)n);
   r |= dalloc(h, B, &d.vatom, 6 * (size_t)n);
   r |= dalloc(h, B, &d.xs, (size_t)n);
@@ -883,11 +892,12 @@ int cap_refine(rg_system *h, int lvl, int pass) {
   return rc;
 }
 
-int capture_single_point(rg_system *h, int eflag, int vflag, int atom_tally) {
+// the single-point step (dt = 0) or the MD step with time step dt
+int capture_step(rg_system *h, StepGraph &G, int eflag, int vflag, int atom_tally, double dt) {
   Dev &d = h->d;
-  if (h->sp_exec) {
-    cudaGraphExecDestroy(h->sp_exec);
-    h->sp_exec = nullptr;
+  if (G.exec) {
+    cudaGraphExecDestroy(G.exec);
+    G.exec = nullptr;
   }
   for (int k = 0; k < kMaxCapLevels; ++k)
     if (!h->cap_st[k]) CK(cudaStreamCreateWithFlags(&h->cap_st[k], cudaStreamNonBlocking));
@@ -905,6 +915,16 @@ int capture_single_point(rg_system *h, int eflag, int vflag, int atom_tally) {
     cudaMemcpyAsync(d.hist_save, d.s_hist, 5 * n * sizeof(double), cudaMemcpyDeviceToDevice, s);
     cudaMemcpyAsync(d.hist_save + 5 * n, d.t_hist, 5 * n * sizeof(double),
                     cudaMemcpyDeviceToDevice, s);
+    if (dt > 0.0) {
+      // an MD step also saves the positions and velocities it advances
+      cudaMemcpyAsync(d.hist_save + 10 * n, d.x_o, 3 * n * sizeof(double),
+                      cudaMemcpyDeviceToDevice, s);
+      cudaMemcpyAsync(d.hist_save + 13 * n, d.v_o, 3 * n * sizeof(double),
+                      cudaMemcpyDeviceToDevice, s);
+      cudaMemcpyAsync(d.hist_save + 16 * n, d.f_o, 3 * n * sizeof(double),
+                      cudaMemcpyDeviceToDevice, s);
+      launch_nve_initial(d, s, dt);
+    }
     cudaMemsetAsync(d.status, 0, RG_NSTATUS * sizeof(int), s);
     cudaMemsetAsync(d.qeq_ctl, 0, 4 * sizeof(int), s);
     cudaMemsetAsync(d.qeq_tot, 0, 2 * sizeof(int) * (size_t)d.nseg, s);
@@ -921,6 +941,7 @@ int capture_single_point(rg_system *h, int eflag, int vflag, int atom_tally) {
       h->lists_valid = true;    // built by the captured kernels above
       h->bonds_fresh = true;
       rc = do_compute(h, eflag, vflag, atom_tally, true);
+      if (!rc && dt > 0.0) launch_nve_final(d, s, dt);
     }
     e = cudaStreamEndCapture(s, &g);
   }
@@ -930,7 +951,7 @@ int capture_single_point(rg_system *h, int eflag, int vflag, int atom_tally) {
   h->bonds_fresh = fresh0;
   h->forces_valid = forces0;
   h->tallies_valid = tallies0;
-  if (e == cudaSuccess && !rc) e = cudaGraphInstantiate(&h->sp_exec, g, 0);
+  if (e == cudaSuccess && !rc) e = cudaGraphInstantiate(&G.exec, g, 0);
   if (e == cudaSuccess && !rc) {
     size_t nn = 0;
     cudaGraphGetNodes(g, nullptr, &nn);
@@ -941,17 +962,104 @@ int capture_single_point(rg_system *h, int eflag, int vflag, int atom_tally) {
       cudaGraphNodeType t;
       if (cudaGraphNodeGetType(nd, &t) == cudaSuccess && t == cudaGraphNodeTypeKernel) ++k;
     }
-    h->sp_kernels = k;
+    G.kernels = k;
   }
   if (g) cudaGraphDestroy(g);
   cudaGetLastError();
   if (e != cudaSuccess || rc) {
-    h->sp_exec = nullptr;
-    h->sp_failed = true;
-    return rc ? rc : fail(h, RG_E_CUDA, std::string("single-point graph: ") + cudaGetErrorString(e));
+    G.exec = nullptr;
+    G.failed = true;
+    return rc ? rc : fail(h, RG_E_CUDA, std::string("step graph: ") + cudaGetErrorString(e));
   }
-  h->sp_dev = d;
-  h->sp_flags = eflag | (vflag << 4) | (atom_tally << 8);
+  G.dev = d;
+  G.flags = eflag | (vflag << 4) | (atom_tally << 8);
+  G.dt = dt;
+  return 0;
+}
+
+// whether G holds the step of the current arrays, flags and time step
+bool step_matches(const rg_system *h, const StepGraph &G, int flags, double dt) {
+  return G.exec && G.flags == flags && G.dt == dt &&
+         std::memcmp(&G.dev, &h->d, sizeof(Dev)) == 0;
+}
+
+// after a regular step: a configuration seen twice in a row is captured
+// (one-off batches and cohorts do not pay for a capture)
+void maybe_capture(rg_system *h, StepGraph &G, int eflag, int vflag, int atom_tally, double dt) {
+  const int flags = eflag | (vflag << 4) | (atom_tally << 8);
+  const bool again = G.seen_flags == flags && G.seen_dt == dt &&
+                     std::memcmp(&G.seen, &h->d, sizeof(Dev)) == 0;
+  G.seen = h->d;
+  G.seen_flags = flags;
+  G.seen_dt = dt;
+  const bool eligible = h->use_graphs && !h->prof.on && !h->check_finite && !G.failed;
+  if (eligible && again && !step_matches(h, G, flags, dt))
+    capture_step(h, G, eflag, vflag, atom_tally, dt);   // failures keep the regular path
+}
+
+// One replay of G and its single read-back.  Returns 1 when the step must be
+// redone on the regular path (a list past its capacity, a work list past
+// its capacity or a tripped CG loop limit); the saved histories (and, for
+// an MD step, positions and velocities) are then restored.
+int replay_step(rg_system *h, StepGraph &G, bool atom_tally) {
+  Dev &d = h->d;
+  CK(cudaGraphLaunch(G.exec, h->st));
+  int st[RG_NSTATUS], ctl[4], items[2];
+  const long long slots = (long long)d.n * d.bond_cap;
+  std::vector<int> tot(2 * (size_t)d.nseg);
+  CK(cudaMemcpyAsync(st, d.status, sizeof st, cudaMemcpyDeviceToHost, h->st));
+  CK(cudaMemcpyAsync(ctl, d.qeq_ctl, sizeof ctl, cudaMemcpyDeviceToHost, h->st));
+  CK(cudaMemcpyAsync(&items[0], d.w_off_v + slots, sizeof(int), cudaMemcpyDeviceToHost, h->st));
+  CK(cudaMemcpyAsync(&items[1], d.w_off_t + slots, sizeof(int), cudaMemcpyDeviceToHost, h->st));
+  CK(cudaMemcpyAsync(tot.data(), d.qeq_tot, tot.size() * sizeof(int), cudaMemcpyDeviceToHost,
+                     h->st));
+  CK(cudaStreamSynchronize(h->st));
+  if ((st[ST_OVF] != 0) || items[0] > d.cap_val || items[1] > d.cap_tor || ctl[2]) {
+    const size_t n = (size_t)d.n;
+    CK(cudaMemcpyAsync(d.s_hist, d.hist_save, 5 * n * sizeof(double), cudaMemcpyDeviceToDevice,
+                       h->st));
+    CK(cudaMemcpyAsync(d.t_hist, d.hist_save + 5 * n, 5 * n * sizeof(double),
+                       cudaMemcpyDeviceToDevice, h->st));
+    if (G.dt > 0.0) {
+      CK(cudaMemcpyAsync(d.x_o, d.hist_save + 10 * n, 3 * n * sizeof(double),
+                         cudaMemcpyDeviceToDevice, h->st));
+      CK(cudaMemcpyAsync(d.v_o, d.hist_save + 13 * n, 3 * n * sizeof(double),
+                         cudaMemcpyDeviceToDevice, h->st));
+      CK(cudaMemcpyAsync(d.f_o, d.hist_save + 16 * n, 3 * n * sizeof(double),
+                         cudaMemcpyDeviceToDevice, h->st));
+    }
+    h->lists_valid = false;
+    h->forces_valid = G.dt > 0.0;   // an MD step restarts from its saved forces
+    h->stats.step_graph_redos++;
+    return 1;
+  }
+  h->stats.step_graph_replays++;
+  int ms = 0, mt = 0;
+  for (int g = 0; g < d.nseg; ++g) {
+    ms = std::max(ms, tot[2 * g]);
+    mt = std::max(mt, tot[2 * g + 1]);
+  }
+  h->seg_iters.assign(tot.begin(), tot.end());
+  h->stats.cg_iters_s = ms;
+  h->stats.cg_iters_t = mt;
+  h->stats.cg_system_iters += std::max(ms - 1, 0) + std::max(mt - 1, 0);
+  h->stats.cg_spmv_rows_passes += std::max(std::max(ms, mt) - 1, 0);
+  h->stats.qeq_restarts = ctl[0];
+  h->stats.n_pairs = st[5];
+  h->stats.n_H_entries = st[5];
+  h->stats.n_bonds = st[6];
+  h->stats.n_hbond_pairs = st[7];
+  h->stats.max_nbrs = st[ST_MAXNB] + st[ST_MAXNF];
+  h->stats.max_bonds = st[ST_MAXB];
+  h->stats.max_hbonds = st[ST_MAXHB];
+  h->n_val = items[0];
+  h->n_tor = items[1];
+  h->launches += G.kernels + (5LL * h->sp_trip + 1) * ctl[1];
+  h->lists_valid = true;
+  h->bonds_fresh = false;   // the replay's force step used them
+  h->forces_valid = true;
+  h->tallies_valid = atom_tally;
+  if (st[ST_NAN]) return fail(h, RG_E_NUMERIC, "non-finite force");
   return 0;
 }
 
@@ -1211,7 +1319,8 @@ int rg_destroy(rg_system *h) {
   if (h->d_tab) cudaFree(h->d_tab);
   if (h->d_tab32) cudaFree(h->d_tab32);
   if (h->cg_exec) cudaGraphExecDestroy(h->cg_exec);
-  if (h->sp_exec) cudaGraphExecDestroy(h->sp_exec);
+  if (h->sp.exec) cudaGraphExecDestroy(h->sp.exec);
+  if (h->md.exec) cudaGraphExecDestroy(h->md.exec);
   for (cudaStream_t c : h->cap_st)
     if (c) cudaStreamDestroy(c);
   cudaStreamDestroy(h->st);
@@ -1676,72 +1785,19 @@ int rg_single_point(rg_system *h, int eflag, int vflag, double *q_out, double *f
   const int ef = eflag || energies != nullptr, vf = vflag & 3;
   const int flags = ef | (vf << 4) | (atom_tally << 8);
   Dev &d = h->d;
+  int rc;
   // the graph holds the device arrays, sizes and flags of its capture, and
   // the cell grid of the boxes then: the host-side grid set-up runs first
   // (a changed grid changes the arrays or sizes, so the step is recaptured)
-  int rc;
-  if (h->use_graphs && h->sp_exec && (rc = setup_cells(h))) return rc;
+  if (h->use_graphs && h->sp.exec && (rc = setup_cells(h))) return rc;
   d.vflag = vf ? 1 : 0;
   d.atom_tally = atom_tally ? 1 : 0;
-  const bool eligible = h->use_graphs && !h->prof.on && !h->check_finite && !h->sp_failed;
-  const bool replay = eligible && h->sp_exec && h->sp_flags == flags &&
-                      std::memcmp(&h->sp_dev, &d, sizeof(Dev)) == 0;
+  const bool eligible = h->use_graphs && !h->prof.on && !h->check_finite && !h->sp.failed;
   bool done = false;
-  if (replay) {
-    CK(cudaGraphLaunch(h->sp_exec, h->st));
-    int st[RG_NSTATUS], ctl[4], items[2];
-    const long long slots = (long long)d.n * d.bond_cap;
-    std::vector<int> tot(2 * (size_t)d.nseg);
-    CK(cudaMemcpyAsync(st, d.status, sizeof st, cudaMemcpyDeviceToHost, h->st));
-    CK(cudaMemcpyAsync(ctl, d.qeq_ctl, sizeof ctl, cudaMemcpyDeviceToHost, h->st));
-    CK(cudaMemcpyAsync(&items[0], d.w_off_v + slots, sizeof(int), cudaMemcpyDeviceToHost, h->st));
-    CK(cudaMemcpyAsync(&items[1], d.w_off_t + slots, sizeof(int), cudaMemcpyDeviceToHost, h->st));
-    CK(cudaMemcpyAsync(tot.data(), d.qeq_tot, tot.size() * sizeof(int), cudaMemcpyDeviceToHost,
-                       h->st));
-    CK(cudaStreamSynchronize(h->st));
-    const bool redo = (st[ST_OVF] != 0) || items[0] > d.cap_val || items[1] > d.cap_tor || ctl[2];
-    if (redo) {
-      // a list outgrew its capacity (or a CG loop hit its trip limit): the
-      // QEq histories go back to the step's start and the regular path,
-      // which regrows, redoes the step
-      const size_t n = (size_t)d.n;
-      CK(cudaMemcpyAsync(d.s_hist, d.hist_save, 5 * n * sizeof(double), cudaMemcpyDeviceToDevice,
-                         h->st));
-      CK(cudaMemcpyAsync(d.t_hist, d.hist_save + 5 * n, 5 * n * sizeof(double),
-                         cudaMemcpyDeviceToDevice, h->st));
-      h->lists_valid = false;
-      h->forces_valid = false;
-      h->stats.step_graph_redos++;
-    } else {
-      h->stats.step_graph_replays++;
-      int ms = 0, mt = 0;
-      for (int g = 0; g < d.nseg; ++g) {
-        ms = std::max(ms, tot[2 * g]);
-        mt = std::max(mt, tot[2 * g + 1]);
-      }
-      h->seg_iters.assign(tot.begin(), tot.end());
-      h->stats.cg_iters_s = ms;
-      h->stats.cg_iters_t = mt;
-      h->stats.cg_system_iters += std::max(ms - 1, 0) + std::max(mt - 1, 0);
-      h->stats.cg_spmv_rows_passes += std::max(std::max(ms, mt) - 1, 0);
-      h->stats.qeq_restarts = ctl[0];
-      h->stats.n_pairs = st[5];
-      h->stats.n_H_entries = st[5];
-      h->stats.n_bonds = st[6];
-      h->stats.n_hbond_pairs = st[7];
-      h->stats.max_nbrs = st[ST_MAXNB] + st[ST_MAXNF];
-      h->stats.max_bonds = st[ST_MAXB];
-      h->stats.max_hbonds = st[ST_MAXHB];
-      h->n_val = items[0];
-      h->n_tor = items[1];
-      h->launches += h->sp_kernels + (5LL * h->sp_trip + 1) * ctl[1];
-      h->lists_valid = true;
-      h->bonds_fresh = false;   // the replay's force step used them
-      h->forces_valid = true;
-      h->tallies_valid = atom_tally != 0;
-      if (st[ST_NAN]) return fail(h, RG_E_NUMERIC, "non-finite force");
-      done = true;
-    }
+  if (eligible && step_matches(h, h->sp, flags, 0.0)) {
+    rc = replay_step(h, h->sp, atom_tally != 0);
+    if (rc < 0) return rc;
+    done = rc == 0;
   }
   if (!done) {
     if ((rc = do_qeq(h, nullptr, nullptr))) return rc;
@@ -1750,18 +1806,7 @@ int rg_single_point(rg_system *h, int eflag, int vflag, double *q_out, double *f
     int st[RG_NSTATUS];
     if ((rc = read_status(h, st))) return rc;
     if (st[ST_NAN]) return fail(h, RG_E_NUMERIC, "non-finite force");
-    // a configuration seen twice in a row is captured for the next call
-    // (one-off batches do not pay for a capture)
-    const bool again = h->sp_seen_flags == flags && std::memcmp(&h->sp_seen, &d, sizeof(Dev)) == 0;
-    h->sp_seen = d;
-    h->sp_seen_flags = flags;
-    if (eligible && again &&
-        !(h->sp_exec && h->sp_flags == flags && std::memcmp(&h->sp_dev, &d, sizeof(Dev)) == 0)) {
-      if ((rc = capture_single_point(h, ef, vf, atom_tally))) {
-        // the regular path keeps working; the reason stays in rg_last_error
-        (void)rc;
-      }
-    }
+    maybe_capture(h, h->sp, ef, vf, atom_tally, 0.0);
   }
   if (q_out) CK(cudaMemcpyAsync(q_out, d.q_o, sizeof(double) * h->n, cudaMemcpyDeviceToHost, h->st));
   if (f_out) CK(cudaMemcpyAsync(f_out, d.f_o, 3 * sizeof(double) * h->n, cudaMemcpyDeviceToHost, h->st));
@@ -1815,13 +1860,33 @@ int rg_run(rg_system *h, int nsteps, double dt, double *energies) {
     if ((rc = do_qeq(h, nullptr, nullptr))) return rc;
     if ((rc = do_compute(h, 1))) return rc;
   }
+  Dev &d = h->d;
   for (int s = 0; s < nsteps; ++s) {
+    const int ef = energies != nullptr && s == nsteps - 1;
+    // a whole step as one replay of the captured MD step (same arrays,
+    // flags and time step), else the regular launches
+    bool done = false;
+    const bool eligible = h->use_graphs && !h->prof.on && !h->check_finite && !h->md.failed;
+    if (eligible && h->md.exec && (rc = setup_cells(h))) return rc;
+    d.vflag = 0;
+    d.atom_tally = 0;
+    if (eligible && step_matches(h, h->md, ef, dt)) {
+      rc = replay_step(h, h->md, false);
+      if (rc < 0) return rc;
+      done = rc == 0;
+    }
+    if (done) continue;
     { Scope sc(h, PH_NVE, 1); launch_nve_initial(h->d, h->st, dt); }
     h->lists_valid = false;
     h->forces_valid = false;
     if ((rc = do_qeq(h, nullptr, nullptr))) return rc;
-    if ((rc = do_compute(h, energies != nullptr && s == nsteps - 1))) return rc;
+    if ((rc = do_compute(h, ef))) return rc;
     { Scope sc(h, PH_NVE, 1); launch_nve_final(h->d, h->st, dt); }
+    if (eligible) {
+      // the capture sees the arrays this step settled on; it runs after the
+      // step's work is queued and launches nothing
+      maybe_capture(h, h->md, ef, 0, 0, dt);
+    }
   }
   if (energies && (rc = energy_sum(h, energies))) return rc;
   CK(cudaStreamSynchronize(h->st));

@@ -274,7 +274,7 @@ struct Dev {
   // restarts, 1 loop trips, 2 trip limit reached), per-segment CG iteration
   // totals (qeq_tot[2 * nseg]), the histories saved at the step's start
   int *qeq_ctl, *qeq_tot;
-  double *hist_save;     // [10][n]: s_hist then t_hist
+  double *hist_save;     // [16][n]: s_hist, t_hist, then (MD step) x, v
 
   // per-atom tallies (LAMMPS eflag_atom / vflag_atom) of the nonbonded
   // pair terms, sorted order: eatom[n], vatom[6][n] (xx yy zz xy xz yz)

@@ -1186,6 +1186,7 @@ void rg_default_params(rg_params *p) {
   p->autotune = 1;
   p->cell_div = 0;
   p->spmv_rows = 0;
+  p->pair_kernel = 0;
 }
 
 int rg_create(const char *ffield_path, const rg_params *pin, rg_system **out) {

@@ -7,10 +7,11 @@
 //  k_spmv        sparse_matvec: b_i = eta_i x_i + sum_j H_ij x_j over the
 //                full rows (fix_qeq_reax_sw64.c:357-498), both systems per
 //                read of H
-//  k_cg_*        CG_v2 (fix_qeq_reax_sunway.cpp:983-1167): the same
-//                recurrences per system; a system that has converged stops
-//                updating, so each keeps the iterate and iteration count
-//                of a solve on its own
+//  k_cg_*, k_pcg_*  CG_v2 (fix_qeq_reax_sunway.cpp:983-1167): Jacobi PCG
+//                with CG_v2's set-up, stopping test and iteration count, in
+//                the standard (not pipelined) recurrences; a system that
+//                has converged stops updating, so each keeps the iterate
+//                and iteration count of a solve on its own
 //  k_qeq_finish  calculate_Q (fix_qeq_reax_sunway.cpp:1697-1755)
 #include "rg_internal.h"
 
@@ -20,12 +21,11 @@ constexpr unsigned FULL = 0xffffffffu;
 
 // scalar slots in d.red (pairs: [s, t])
 enum {
-  R_ACC0 = 0, R_ACC1 = 2, R_ACC2 = 4, R_ALPHA = 6, R_ALPHA_OLD = 8, R_BETA = 10,
-  R_SIG = 12, R_HETA = 14, R_BNORM = 16, R_DOTP = 18, R_ACTIVE = 20, R_ITERS = 22,
-  R_SUM = 24, R_TOL = 26, R_IMAX = 27, R_NEXT = 32, R_INIT = 68
+  R_ACC0 = 0, R_ACC1 = 2, R_BETA = 10, R_RHO = 12, R_BNORM = 16, R_ACTIVE = 20, R_ITERS = 22,
+  R_SUM = 24, R_TOL = 26, R_IMAX = 27, R_INIT = 68
 };
-// (per segment: d.red + seg * RG_NRED; R_NEXT + c: activity of the next
-// iteration; R_INIT..R_INIT+5: the set-up sums b.b, u.r, u.w)
+// (per segment: d.red + seg * RG_NRED; ACC0: p.q, ACC1: u.r of the
+// iteration; R_INIT..R_INIT+3: the set-up sums b.b, u.r)
 
 __device__ __forceinline__ int seg_at(const Dev &d, int s) { return s < d.n ? d.seg_s[s] : -1; }
 
@@ -273,37 +273,21 @@ __global__ void k_cg_init1(Dev d) {
   if (d.qd32) d.qd32[s] = split4(u);
 }
 
-// w = q; m = q*Hdia_inv; d = m
-__global__ void k_cg_init2(Dev d) {
+// set-up sums b.b and u.r (u = r Hdia_inv)
+__global__ void k_cg_init_sums(Dev d) {
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
-  if (s >= d.n) return;
-  const double hi = d.Hdia_inv[s];
-  const double2 q = d.qq[s];
-  d.qw[s] = q;
-  const double2 m = make_double2(q.x * hi, q.y * hi);
-  d.qm[s] = m;
-  d.qd[s] = m;
-  if (d.qd32) d.qd32[s] = split4(m);
-}
-
-// p = u; s = w; v = m; z = q; sums b.b, u.r, u.w
-__global__ void k_cg_init3(Dev d) {
-  const int s = blockIdx.x * blockDim.x + threadIdx.x;
-  double v[6] = {0, 0, 0, 0, 0, 0};
+  double v[4] = {0, 0, 0, 0};
   if (s < d.n) {
-    const double2 u = d.qu[s], w = d.qw[s], m = d.qm[s], r = d.qr[s], b = d.qb[s];
-    d.qp[s] = u;
-    d.qs[s] = w;
-    d.qv[s] = m;
-    d.qz[s] = d.qq[s];
+    const double2 u = d.qu[s], r = d.qr[s], b = d.qb[s];
     v[0] = b.x * b.x; v[1] = b.y * b.y;
     v[2] = u.x * r.x; v[3] = u.y * r.y;
-    v[4] = u.x * w.x; v[5] = u.y * w.y;
   }
-  seg_block_add<6>(v, seg_at(d, s), d.red + R_INIT, RG_NRED);
+  seg_block_add<4>(v, seg_at(d, s), d.red + R_INIT, RG_NRED);
 }
 
-// one thread per segment; counts the segments with an active solve
+// one thread per segment: |b|, rho = u.r, the first iteration's activity
+// (iteration 1 is the set-up, as CG_v2 counts); counts the segments with
+// an active solve
 __global__ void k_cg_init_ctrl(Dev d, double tol, int imax) {
   const int g = blockIdx.x * blockDim.x + threadIdx.x;
   if (g >= d.nseg) return;
@@ -311,12 +295,10 @@ __global__ void k_cg_init_ctrl(Dev d, double tol, int imax) {
   R[R_TOL] = tol;
   R[R_IMAX] = imax;
   for (int c = 0; c < 2; ++c) {
-    const double bb = R[R_INIT + c], ur = R[R_INIT + 2 + c], uw = R[R_INIT + 4 + c];
+    const double bb = R[R_INIT + c], ur = R[R_INIT + 2 + c];
     R[R_BNORM + c] = sqrt(bb);
-    R[R_SIG + c] = ur;
-    R[R_HETA + c] = uw;
-    R[R_ALPHA + c] = ur / uw;
-    R[R_DOTP + c] = ur;
+    R[R_RHO + c] = ur;
+    R[R_BETA + c] = 0.0;
     R[R_ITERS + c] = 1.0;
     R[R_ACTIVE + c] = (1 < imax && sqrt(ur) / R[R_BNORM + c] > tol) ? 1.0 : 0.0;
     R[R_ACC0 + c] = 0.0;
@@ -325,130 +307,124 @@ __global__ void k_cg_init_ctrl(Dev d, double tol, int imax) {
   if (R[R_ACTIVE] != 0.0 || R[R_ACTIVE + 1] != 0.0) atomicAdd(d.n_active, 1);
 }
 
-// A: r -= a s; u -= a v; w -= a z; acc u.r, u.w; d = w*Hdia_inv
-__global__ void k_cg_A(Dev d) {
+// Jacobi-preconditioned CG, per system and segment:
+//   q = H p;  alpha = rho / p.q;  x += alpha p;  r -= alpha q;
+//   u = r Hdia_inv;  rho' = u.r;  beta = rho' / rho;  p = u + beta p
+// The reference's CG_v2 runs the pipelined form of these recurrences
+// (Ghysels-Vanroose: two more products at the set-up, one reduction phase
+// per iteration, to hide MPI reductions); in exact arithmetic both give the
+// same iterates, residuals and iteration counts, and on one GPU the extra
+// reduction phase costs a kernel boundary, not an SpMV.
+
+// p = u + beta p (beta = 0 at the set-up, where p = u already); p is the
+// SpMV's input (qd, and its split copy in the mixed form)
+__global__ void k_pcg_p(Dev d) {
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
-  const int sg = seg_at(d, s);
-  const double *R = d.red + (long long)(sg < 0 ? 0 : sg) * RG_NRED;
+  if (s >= d.n) return;
+  const double *R = d.red + (long long)d.seg_s[s] * RG_NRED;
   const bool as = R[R_ACTIVE] != 0.0, at = R[R_ACTIVE + 1] != 0.0;
-  double v[2] = {0, 0}, v1[2] = {0, 0};
-  if (s < d.n && (as || at)) {
-    const double hi = d.Hdia_inv[s];
-    double2 r = d.qr[s], u = d.qu[s], w = d.qw[s];
-    const double2 ss = d.qs[s], vv = d.qv[s], z = d.qz[s];
-    double2 dd = d.qd[s];
-    if (as) {
-      const double a = R[R_ALPHA];
-      r.x -= a * ss.x; u.x -= a * vv.x; w.x -= a * z.x;
-      v[0] = u.x * r.x; v1[0] = u.x * w.x;
-      dd.x = w.x * hi;
-    }
-    if (at) {
-      const double a = R[R_ALPHA + 1];
-      r.y -= a * ss.y; u.y -= a * vv.y; w.y -= a * z.y;
-      v[1] = u.y * r.y; v1[1] = u.y * w.y;
-      dd.y = w.y * hi;
-    }
-    d.qr[s] = r; d.qu[s] = u; d.qw[s] = w; d.qd[s] = dd;
-    if (d.qd32) d.qd32[s] = split4(dd);
-  }
-  double all[4] = {v[0], v[1], v1[0], v1[1]};
-  seg_block_add<4>(all, sg, d.red + R_ACC0, RG_NRED);   // ACC0[2], ACC1[2] are contiguous
+  if (!(as || at)) return;
+  const double2 u = d.qu[s];
+  double2 p = d.qd[s];
+  if (as) p.x = u.x + R[R_BETA] * p.x;
+  if (at) p.y = u.y + R[R_BETA + 1] * p.y;
+  d.qd[s] = p;
+  if (d.qd32) d.qd32[s] = split4(p);
 }
 
-// k_cg_A for a single segment: a grid-stride loop over the atoms with
-// about four blocks per SM, so the dot products take one FP64 atomic per
-// value and block from ~600 blocks instead of one per 256 atoms
-__global__ void k_cg_A1(Dev d) {
-  const double *R = d.red;
-  const bool as = R[R_ACTIVE] != 0.0, at = R[R_ACTIVE + 1] != 0.0;
-  double all[4] = {0, 0, 0, 0};   // u.r (s, t), u.w (s, t)
-  if (as || at) {
-    const double a_s = R[R_ALPHA], a_t = R[R_ALPHA + 1];
-    for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < d.n; s += gridDim.x * blockDim.x) {
-      const double hi = d.Hdia_inv[s];
-      double2 r = d.qr[s], u = d.qu[s], w = d.qw[s];
-      const double2 ss = d.qs[s], vv = d.qv[s], z = d.qz[s];
-      double2 dd = d.qd[s];
-      if (as) {
-        r.x -= a_s * ss.x; u.x -= a_s * vv.x; w.x -= a_s * z.x;
-        all[0] += u.x * r.x; all[2] += u.x * w.x;
-        dd.x = w.x * hi;
+// p.q per segment (ACC0).  ONE: a single segment, taken by a grid-stride
+// loop over ~600 blocks so the FP64 atomics come from few blocks.
+template <bool ONE>
+__global__ void k_pcg_sigma(Dev d) {
+  double v[2] = {0, 0};
+  int sg = -1;
+  if (ONE) {
+    const bool as = d.red[R_ACTIVE] != 0.0, at = d.red[R_ACTIVE + 1] != 0.0;
+    if (as || at) {
+      for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < d.n; s += gridDim.x * blockDim.x) {
+        const double2 p = d.qd[s], q = d.qq[s];
+        if (as) v[0] += p.x * q.x;
+        if (at) v[1] += p.y * q.y;
       }
-      if (at) {
-        r.y -= a_t * ss.y; u.y -= a_t * vv.y; w.y -= a_t * z.y;
-        all[1] += u.y * r.y; all[3] += u.y * w.y;
-        dd.y = w.y * hi;
-      }
-      d.qr[s] = r; d.qu[s] = u; d.qw[s] = w; d.qd[s] = dd;
-      if (d.qd32) d.qd32[s] = split4(dd);
+    }
+    sg = 0;
+  } else {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    sg = seg_at(d, s);
+    if (sg >= 0) {
+      const double *R = d.red + (long long)sg * RG_NRED;
+      const double2 p = d.qd[s], q = d.qq[s];
+      if (R[R_ACTIVE] != 0.0) v[0] = p.x * q.x;
+      if (R[R_ACTIVE + 1] != 0.0) v[1] = p.y * q.y;
     }
   }
-  seg_block_add<4>(all, 0, d.red + R_ACC0, RG_NRED);
+  seg_block_add<2>(v, sg, d.red + R_ACC0, RG_NRED);
 }
 
-// scalars after A: beta, heta, alpha; activity of the next iteration (one
-// thread per segment)
-__global__ void k_cg_ctrl(Dev d) {
+// alpha = rho / p.q; x += alpha p; r -= alpha q; u = r Hdia_inv; u.r per
+// segment (ACC1).  Clears the active count that k_pcg_ctrl recounts.
+__device__ __forceinline__ void pcg_update(const Dev &d, int s, const double *R, bool as, bool at,
+                                           double *v) {
+  const double hi = d.Hdia_inv[s];
+  const double2 p = d.qd[s], q = d.qq[s];
+  double2 x = d.qx[s], r = d.qr[s], u = d.qu[s];
+  if (as) {
+    const double a = R[R_RHO] / R[R_ACC0];
+    x.x += a * p.x; r.x -= a * q.x; u.x = r.x * hi;
+    v[0] += u.x * r.x;
+  }
+  if (at) {
+    const double a = R[R_RHO + 1] / R[R_ACC0 + 1];
+    x.y += a * p.y; r.y -= a * q.y; u.y = r.y * hi;
+    v[1] += u.y * r.y;
+  }
+  d.qx[s] = x; d.qr[s] = r; d.qu[s] = u;
+}
+
+template <bool ONE>
+__global__ void k_pcg_update(Dev d) {
+  if (blockIdx.x == 0 && threadIdx.x == 0) *d.n_active = 0;
+  double v[2] = {0, 0};
+  int sg = -1;
+  if (ONE) {
+    const bool as = d.red[R_ACTIVE] != 0.0, at = d.red[R_ACTIVE + 1] != 0.0;
+    if (as || at)
+      for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < d.n; s += gridDim.x * blockDim.x)
+        pcg_update(d, s, d.red, as, at, v);
+    sg = 0;
+  } else {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    sg = seg_at(d, s);
+    if (sg >= 0) {
+      const double *R = d.red + (long long)sg * RG_NRED;
+      const bool as = R[R_ACTIVE] != 0.0, at = R[R_ACTIVE + 1] != 0.0;
+      if (as || at) pcg_update(d, s, R, as, at, v);
+    }
+  }
+  seg_block_add<2>(v, sg, d.red + R_ACC1, RG_NRED);
+}
+
+// one thread per segment: beta, the loop increment and the test of the
+// next iteration (CG_v2's criterion sqrt(u.r) / |b| > tol), the active
+// count
+__global__ void k_pcg_ctrl(Dev d) {
   const int g = blockIdx.x * blockDim.x + threadIdx.x;
-  if (g == 0) *d.n_active = 0;   // recounted by k_cg_flip
   if (g >= d.nseg) return;
   double *R = d.red + (long long)g * RG_NRED;
   const double tol = R[R_TOL];
   const int imax = (int)R[R_IMAX];
   for (int c = 0; c < 2; ++c) {
-    if (R[R_ACTIVE + c] == 0.0) {
-      R[R_ACC0 + c] = 0.0;
-      R[R_ACC1 + c] = 0.0;
-      continue;
+    if (R[R_ACTIVE + c] != 0.0) {
+      const double rho = R[R_ACC1 + c];
+      R[R_BETA + c] = rho / R[R_RHO + c];
+      R[R_RHO + c] = rho;
+      const double it = R[R_ITERS + c] + 1.0;
+      R[R_ITERS + c] = it;
+      R[R_ACTIVE + c] = (it < imax && sqrt(rho) / R[R_BNORM + c] > tol) ? 1.0 : 0.0;
     }
-    const double dot0 = R[R_ACC0 + c], dot1 = R[R_ACC1 + c];
-    const double beta = dot0 / R[R_SIG + c];
-    const double heta = dot1 - beta * beta * R[R_HETA + c];
-    R[R_BETA + c] = beta;
-    R[R_HETA + c] = heta;
-    R[R_ALPHA_OLD + c] = R[R_ALPHA + c];
-    R[R_ALPHA + c] = dot0 / heta;
-    R[R_SIG + c] = dot0;
-    R[R_DOTP + c] = dot0;
     R[R_ACC0 + c] = 0.0;
     R[R_ACC1 + c] = 0.0;
-    // loop increment and test of the next iteration
-    const double it = R[R_ITERS + c] + 1.0;
-    R[R_ITERS + c] = it;
-    R[R_NEXT + c] = (it < imax && sqrt(dot0) / R[R_BNORM + c] > tol) ? 1.0 : 0.0;
   }
-}
-
-// C: x += a_old p; p = u + b p; s = w + b s; v = d + b v; z = q + b z
-__global__ void k_cg_C(Dev d) {
-  const int s = blockIdx.x * blockDim.x + threadIdx.x;
-  if (s >= d.n) return;
-  const double *R = d.red + (long long)d.seg_s[s] * RG_NRED;
-  const bool as = R[R_ACTIVE] != 0.0, at = R[R_ACTIVE + 1] != 0.0;
-  if (s < d.n && (as || at)) {
-    double2 x = d.qx[s], p = d.qp[s], ss = d.qs[s], v = d.qv[s], z = d.qz[s];
-    const double2 u = d.qu[s], w = d.qw[s], dd = d.qd[s], q = d.qq[s];
-    if (as) {
-      const double a = R[R_ALPHA_OLD], b = R[R_BETA];
-      x.x += a * p.x; p.x = u.x + p.x * b; ss.x = w.x + ss.x * b; v.x = dd.x + v.x * b; z.x = q.x + z.x * b;
-    }
-    if (at) {
-      const double a = R[R_ALPHA_OLD + 1], b = R[R_BETA + 1];
-      x.y += a * p.y; p.y = u.y + p.y * b; ss.y = w.y + ss.y * b; v.y = dd.y + v.y * b; z.y = q.y + z.y * b;
-    }
-    d.qx[s] = x; d.qp[s] = p; d.qs[s] = ss; d.qv[s] = v; d.qz[s] = z;
-  }
-}
-
-// the activity decided in k_cg_ctrl takes effect for the next iteration;
-// counts the segments still active (one thread per segment)
-__global__ void k_cg_flip(Dev d) {
-  const int g = blockIdx.x * blockDim.x + threadIdx.x;
-  if (g >= d.nseg) return;
-  double *R = d.red + (long long)g * RG_NRED;
-  for (int c = 0; c < 2; ++c)
-    if (R[R_ACTIVE + c] != 0.0) R[R_ACTIVE + c] = R[R_NEXT + c];
   if (R[R_ACTIVE] != 0.0 || R[R_ACTIVE + 1] != 0.0) atomicAdd(d.n_active, 1);
 }
 
@@ -574,33 +550,36 @@ void launch_qeq_refine_check(const Dev &d, cudaStream_t st, double tol) {
   k_refine_ctrl<<<GS, 128, 0, st>>>(d, tol);
 }
 
-// the set-up after r and u (k_cg_init1): the two pipelining SpMVs and the
-// CG scalars
+// the set-up after r and u (k_cg_init1, which also set p = u): the CG
+// scalars
 void launch_qeq_cg_init_rest(const Dev &d, cudaStream_t st, double tol, int imax) {
   const int B = 256, G = (d.n + B - 1) / B;
   const int GS = (d.nseg + 127) / 128;
-  launch_qeq_spmv(d, st, d.qd, d.qq, 0);
-  k_cg_init2<<<G, B, 0, st>>>(d);
-  launch_qeq_spmv(d, st, d.qd, d.qq, 0);
-  k_seg_zero<<<GS, 128, 0, st>>>(d, R_INIT, 6);
-  k_cg_init3<<<G, B, 0, st>>>(d);
+  k_seg_zero<<<GS, 128, 0, st>>>(d, R_INIT, 4);
+  k_cg_init_sums<<<G, B, 0, st>>>(d);
   cudaMemsetAsync(d.n_active, 0, sizeof(int), st);
   k_cg_init_ctrl<<<GS, 128, 0, st>>>(d, tol, imax);
 }
 
-// one CG iteration = launch_qeq_cg_A, SpMV of d into q, launch_qeq_cg_C
+// one CG iteration = launch_qeq_cg_A (p), SpMV of p into q,
+// launch_qeq_cg_C (p.q, the updates and u.r, the control)
 void launch_qeq_cg_A(const Dev &d, cudaStream_t st) {
   const int B = 256, G = (d.n + B - 1) / B;
-  if (d.nseg == 1) k_cg_A1<<<G < 608 ? G : 608, B, 0, st>>>(d);
-  else k_cg_A<<<G, B, 0, st>>>(d);
+  k_pcg_p<<<G, B, 0, st>>>(d);
 }
 
 void launch_qeq_cg_C(const Dev &d, cudaStream_t st) {
   const int B = 256, G = (d.n + B - 1) / B;
   const int GS = (d.nseg + 127) / 128;
-  k_cg_ctrl<<<GS, 128, 0, st>>>(d);
-  k_cg_C<<<G, B, 0, st>>>(d);
-  k_cg_flip<<<GS, 128, 0, st>>>(d);
+  if (d.nseg == 1) {
+    const int G1 = G < 608 ? G : 608;
+    k_pcg_sigma<true><<<G1, B, 0, st>>>(d);
+    k_pcg_update<true><<<G1, B, 0, st>>>(d);
+  } else {
+    k_pcg_sigma<false><<<G, B, 0, st>>>(d);
+    k_pcg_update<false><<<G, B, 0, st>>>(d);
+  }
+  k_pcg_ctrl<<<GS, 128, 0, st>>>(d);
 }
 
 void launch_qeq_finish(const Dev &d, cudaStream_t st) {

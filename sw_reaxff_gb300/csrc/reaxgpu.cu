@@ -420,7 +420,7 @@ int alloc_atoms(rg_system *h, int n) {
   r |= dalloc(h, B, &d.vsum, 2 * (size_t)n);
   r |= dalloc(h, B, &d.exp_boc, 2 * (size_t)n);
   r |= dalloc(h, B, &d.c_sbo, 10 * (size_t)n);
-  double2 **pv[] = {&d.qx, &d.qb, &d.qr, &d.qu, &d.qw, &d.qd, &d.qq, &d.qp, &d.qs, &d.qv, &d.qz, &d.qm};
+  double2 **pv[] = {&d.qx, &d.qb, &d.qr, &d.qu, &d.qd, &d.qq};
   for (double2 **q : pv) r |= dalloc(h, B, q, (size_t)n);
   if (d.mixed) r |= dalloc(h, B, &d.qd32, (size_t)n);
   else d.qd32 = nullptr;
@@ -710,7 +710,7 @@ int do_qeq(rg_system *h, int *its, int *itt) {
   const double tol = h->p.qeq_tol;
   const int imax = h->p.qeq_imax;
   {
-    Scope sc(h, PH_QSETUP, 9 + (d.mixed ? 1 : 0));
+    Scope sc(h, PH_QSETUP, 6 + (d.mixed ? 1 : 0));
     launch_qeq_setup(d, h->st);
     launch_qeq_cg_init(d, h->st, tol, imax);
   }
@@ -762,7 +762,7 @@ int do_qeq(rg_system *h, int *its, int *itt) {
     CK(cudaMemcpyAsync(&active, d.n_active, sizeof(int), cudaMemcpyDeviceToHost, h->st));
     CK(cudaStreamSynchronize(h->st));
     if (active == 0) break;
-    { Scope sc(h, PH_QSETUP, 6); launch_qeq_cg_init_rest(d, h->st, tol, imax); }
+    { Scope sc(h, PH_QSETUP, 3); launch_qeq_cg_init_rest(d, h->st, tol, imax); }
     CK(cudaMemcpyAsync(&active, d.n_active, sizeof(int), cudaMemcpyDeviceToHost, h->st));
     CK(cudaStreamSynchronize(h->st));
     if (active == 0) break;

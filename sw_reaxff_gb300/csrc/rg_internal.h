@@ -235,8 +235,10 @@ struct Dev {
                       // (their share of Cdbopi/Cdbopi2 and Cdbo of every bond
                       // of the centre, applied in k_dbond)
 
-  // QEq vectors (sorted order), two solves s,t interleaved as double2
-  double2 *qx, *qb, *qr, *qu, *qw, *qd, *qq, *qp, *qs, *qv, *qz, *qm;
+  // QEq vectors (sorted order), two solves s,t interleaved as double2:
+  // iterate x, right-hand side b, residual r, preconditioned residual u,
+  // search direction p (qd, the SpMV's input) and its product q = H p
+  double2 *qx, *qb, *qr, *qu, *qd, *qq;
   float4 *qd32;   // mixed form: qd split into FP32 (hi, lo) pairs, s then t
   double *Hdia_inv;
   double *red;        // device scalars / reduction accumulators, RG_NRED per segment

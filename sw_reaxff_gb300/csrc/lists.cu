@@ -792,7 +792,32 @@ __device__ __forceinline__ void bo_prime64(const Control &C, int ti, int tj, con
 // |p_bo1 p_bo2 (d/r)^p_bo2| (up to ~10 for C-C and C-N bonds), and in FP32
 // that left the mixed form's forces on the TATB crystal 1.7e-4 (relative
 // RMS) from the FP64 forces, against 1e-5 with FP64 BO'.
-__device__ __forceinline__ void bond_prime_item(const Dev &d, int i, int k) {
+// BO' is symmetric in the pair.  The candidate of a pair that sorts first
+// (lower atom, then lower image code) evaluates it and fills both
+// directions' slots; the other finds its partner's slot and leaves it.  A
+// candidate whose mirror is not listed evaluates its own slot.
+// Returns the mirror slot (or -1) and whether this candidate evaluates.
+__device__ __forceinline__ long long bond_mirror(const Dev &d, int i, int k, bool &work) {
+  const int n = d.n;
+  const uint32_t e = d.b_nbr[(long long)k * n + i];
+  const int j = (int)(e >> 8);
+  int sx, sy, sz;
+  img_unpack((int)(e & 255u), &sx, &sy, &sz);
+  const uint32_t want = ((uint32_t)i << 8) | (uint32_t)img_pack(-sx, -sy, -sz);
+  const int nbj = min(d.nbonds[j], d.bond_cap);
+  long long m = -1;
+  for (int q = 0; q < nbj; ++q)
+    if (d.b_nbr[(long long)q * n + j] == want) {
+      m = (long long)q * n + j;
+      break;
+    }
+  const bool owner = j > i || (j == i && (e & 255u) < (want & 255u));
+  work = owner || m < 0;
+  return m;
+}
+
+// one candidate's BO' (and its mirror slot m when m >= 0)
+__device__ __forceinline__ void bond_prime_item(const Dev &d, int i, int k, long long m) {
   const int n = d.n;
   const Control &C = *d.ctl;
   const ForceField &F = *d.ff;
@@ -809,6 +834,7 @@ __device__ __forceinline__ void bond_prime_item(const Dev &d, int i, int k) {
       __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz)));
   if (!(dist <= C.bond_cut)) {
     d.b_d[s] = -1.0;
+    if (m >= 0) d.b_d[m] = -1.0;
     return;
   }
   const int ti = d.ts[i], tj = d.ts[j];
@@ -818,31 +844,87 @@ __device__ __forceinline__ void bond_prime_item(const Dev &d, int i, int k) {
   bo_prime64(C, ti, tj, si, sj, tw, dist, BOs, BOpi, BOpi2, C12, C34, C56);
   if (!((BOs + BOpi + BOpi2) >= C.bo_cut)) {
     d.b_d[s] = -1.0;
+    if (m >= 0) d.b_d[m] = -1.0;
     return;
   }
   const double r2 = dist * dist;
   const double Cs = tw.p_bo2 * C12 / r2;
   const double Cpi = tw.p_bo4 * C34 / r2;
   const double Cpi2 = tw.p_bo6 * C56 / r2;
-  d.b_d[s] = dist;
-  d.b_dx[s] = dx; d.b_dy[s] = dy; d.b_dz[s] = dz;
   const double gb = -(BOs * Cs + BOpi * Cpi + BOpi2 * Cpi2);
-  d.b_BO[s] = BOs + BOpi + BOpi2 - C.bo_cut;
-  d.b_BOs[s] = BOs - C.bo_cut;
-  d.b_BOpi[s] = BOpi;
-  d.b_BOpi2[s] = BOpi2;
-  d.b_dBOp[s] = gb * dx; d.b_dBOp[S3 + s] = gb * dy; d.b_dBOp[2 * S3 + s] = gb * dz;
   const double api = -BOpi * Cpi, api2 = -BOpi2 * Cpi2;
-  d.b_dlnpi[s] = api * dx; d.b_dlnpi[S3 + s] = api * dy; d.b_dlnpi[2 * S3 + s] = api * dz;
-  d.b_dlnpi2[s] = api2 * dx; d.b_dlnpi2[S3 + s] = api2 * dy; d.b_dlnpi2[2 * S3 + s] = api2 * dz;
-  d.b_Cdbo[s] = 0.0; d.b_Cdbopi[s] = 0.0; d.b_Cdbopi2[s] = 0.0;
+  // this direction with (dx, dy, dz), the mirror with it negated
+  for (int side = 0; side < (m >= 0 ? 2 : 1); ++side) {
+    const long long t = side ? m : s;
+    const double sg = side ? -1.0 : 1.0;
+    const double ex = sg * dx, ey = sg * dy, ez = sg * dz;
+    d.b_d[t] = dist;
+    d.b_dx[t] = ex; d.b_dy[t] = ey; d.b_dz[t] = ez;
+    d.b_BO[t] = BOs + BOpi + BOpi2 - C.bo_cut;
+    d.b_BOs[t] = BOs - C.bo_cut;
+    d.b_BOpi[t] = BOpi;
+    d.b_BOpi2[t] = BOpi2;
+    d.b_dBOp[t] = gb * ex; d.b_dBOp[S3 + t] = gb * ey; d.b_dBOp[2 * S3 + t] = gb * ez;
+    d.b_dlnpi[t] = api * ex; d.b_dlnpi[S3 + t] = api * ey; d.b_dlnpi[2 * S3 + t] = api * ez;
+    d.b_dlnpi2[t] = api2 * ex; d.b_dlnpi2[S3 + t] = api2 * ey; d.b_dlnpi2[2 * S3 + t] = api2 * ez;
+    d.b_Cdbo[t] = 0.0; d.b_Cdbopi[t] = 0.0; d.b_Cdbopi2[t] = 0.0;
+  }
 }
 
-// one warp per 32 atoms over all their candidates (warp_items)
+struct BondQueue {
+  int i[64], k[64];
+  long long m[64];
+};
+
+// One warp per 32 atoms over all their candidates (warp_items): the
+// candidates that evaluate go to a per-warp queue and are evaluated 32 at
+// a time, so the FP64 log/exp run with full warps
 __global__ void __launch_bounds__(256) k_bond_prime(Dev d) {
+  __shared__ BondQueue queues[8];
+  BondQueue &Q = queues[threadIdx.x >> 5];
+  const int lane = threadIdx.x & 31;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int cnt = i < d.n ? min(d.nbonds[i], d.bond_cap) : 0;
-  warp_items(cnt, i, [&](int a, int k) { bond_prime_item(d, a, k); });
+  int qn = 0;
+  auto drain = [&](bool all) {
+    while (qn >= 32 || (all && qn > 0)) {
+      const int c = min(qn, 32);
+      if (lane < c) bond_prime_item(d, Q.i[lane], Q.k[lane], Q.m[lane]);
+      __syncwarp();
+      const int left = qn - c;
+      int li = 0, lk = 0;
+      long long lm = 0;
+      if (lane < left) {
+        li = Q.i[c + lane];
+        lk = Q.k[c + lane];
+        lm = Q.m[c + lane];
+      }
+      __syncwarp();
+      if (lane < left) {
+        Q.i[lane] = li;
+        Q.k[lane] = lk;
+        Q.m[lane] = lm;
+      }
+      __syncwarp();
+      qn = left;
+    }
+  };
+  warp_items_all(cnt, i, [&](bool has, int a, int k) {
+    bool work = false;
+    long long m = -1;
+    if (has) m = bond_mirror(d, a, k, work);
+    const unsigned mw = __ballot_sync(0xffffffffu, work);
+    if (work) {
+      const int slot = qn + __popc(mw & ((1u << lane) - 1u));
+      Q.i[slot] = a;
+      Q.k[slot] = k;
+      Q.m[slot] = m;
+    }
+    qn += __popc(mw);
+    __syncwarp();
+    drain(false);
+  });
+  drain(true);
 }
 
 // per atom: drop rejected candidates (keeping the order of the rest), then
@@ -906,32 +988,42 @@ __global__ void __launch_bounds__(NB_WARPS * 32) k_build_bonds(Dev d) {
   const int n = d.n;
   const SegGeom &g = d.seg[d.seg_s[i]];
   const float4 xil = d.xl[i];
-  // FP32 prefilter radius: anything that could be within bond_cut, and for
-  // H atoms within hbond_cut
-  const float rpre = (float)((ihb ? fmax(C.bond_cut, C.hbond_cut) : C.bond_cut) + 0.01);
-  const float rpre2 = rpre * rpre;
+  // FP32 prefilter radii: anything that could be within bond_cut, and for
+  // an H atom's acceptor partners within hbond_cut
+  const float rpb = (float)(C.bond_cut + 0.01), rph = (float)(fmax(C.bond_cut, C.hbond_cut) + 0.01);
+  const float rpre2b = rpb * rpb, rpre2h = rph * rph;
   const float bo_half = C.bo_half_f;
   int nb = 0, nh = 0;
+  // the next batch's entry and partner position are loaded while this
+  // batch is tested
+  uint32_t e_nx = 0;
+  float4 xjf_nx = make_float4(0.f, 0.f, 0.f, 0.f);
+  if (lane < nn) {
+    e_nx = d.nbr[row + lane];
+    xjf_nx = d.xf[e_nx >> 8];
+  }
   for (int base = 0; base < nn; base += 32) {
     {
       const int p = base + lane;
       bool ish = false, cand = false;
-      uint32_t e = 0;
+      const uint32_t e = e_nx;
+      const float4 xjf = xjf_nx;
+      if (p + 32 < nn) {
+        e_nx = d.nbr[row + p + 32];
+        xjf_nx = d.xf[e_nx >> 8];
+      }
       if (p < nn) {
-        e = d.nbr[row + p];
         const int j = (int)(e >> 8);
         int sx, sy, sz;
         img_unpack((int)(e & 255u), &sx, &sy, &sz);
-        const float4 xjf = d.xf[j];
         float vx, vy, vz;
         img_vec32(g, sx, sy, sz, vx, vy, vz);
         const float fx = xjf.x + vx - xif.x;
         const float fy = xjf.y + vy - xif.y;
         const float fz = xjf.z + vz - xif.z;
-        if (fx * fx + fy * fy + fz * fz <= rpre2) {
-          const int tj = __float_as_int(xjf.w);
-          const Sbp &sj = F.sbp[tj];
-          const bool hb_rel = ihb && sj.p_hbond == 2;
+        const int tj = __float_as_int(xjf.w);
+        const bool hb_rel = ihb && F.sbp[tj].p_hbond == 2;
+        if (fx * fx + fy * fy + fz * fz <= (hb_rel ? rpre2h : rpre2b)) {
           // FP32 distance from the (hi, lo) positions (a few FP32 ulps of
           // the displacement) decides away from the cutoffs; the exact
           // distance only within MARGIN32 of the H-bond cutoff.  Possible

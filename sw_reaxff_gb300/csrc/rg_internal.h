@@ -346,6 +346,32 @@ __device__ __forceinline__ void warp_items(int cnt, int i, Fn f) {
   }
 }
 
+// The same with every lane calling f(has, i, k) in every batch (has: the
+// lane holds an item), for bodies that use warp-wide collectives.
+template <typename Fn>
+__device__ __forceinline__ void warp_items_all(int cnt, int i, Fn f) {
+  const unsigned full = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+  int incl = cnt;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int v = __shfl_up_sync(full, incl, o);
+    if (lane >= o) incl += v;
+  }
+  const int total = __shfl_sync(full, incl, 31);
+  const int excl = incl - cnt;
+  for (int base = 0; base < total; base += 32) {
+    const int q = base + lane;
+    int own = 0;
+#pragma unroll
+    for (int step = 16; step > 0; step >>= 1)
+      if (__shfl_sync(full, incl, own + step - 1) <= q) own += step;
+    const int oexcl = __shfl_sync(full, excl, own);
+    const int oi = __shfl_sync(full, i, own);
+    f(q < total, oi, q - oexcl);
+  }
+}
+
 // The same over a subset of each atom's slots: bit k of mask marks slot k;
 // f(i, k) runs for the marked slots only.
 template <typename Fn>

@@ -144,5 +144,8 @@ def test_md_step_overflow_redoes_step(ffield):
     ref.run(1, 0.25, energies=False)
     x, v, q, f = g.get_atoms()
     xr, vr, qr, fr = ref.get_atoms()
-    assert np.abs(x - xr).max() < 1e-9 and np.abs(v - vr).max() < 1e-9
+    # (the CG's dot products are FP64 atomics whose order varies from run to
+    # run: the charges move by ~1e-9 e and the velocities after the step by
+    # ~1e-9)
+    assert np.abs(x - xr).max() < 1e-9 and np.abs(v - vr).max() < 1e-7
     assert np.abs(q - qr).max() < 1e-5

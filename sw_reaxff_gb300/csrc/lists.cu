@@ -181,9 +181,11 @@ __global__ void k_gather(Dev d) {
   int t = d.type_o[i];
   const float hx = __double2float_rn(x), hy = __double2float_rn(y), hz = __double2float_rn(z);
   d.xf[s] = make_float4(hx, hy, hz, __int_as_float(t));
-  if (d.xl)
-    d.xl[s] = make_float4(__double2float_rn(x - (double)hx), __double2float_rn(y - (double)hy),
-                          __double2float_rn(z - (double)hz), (float)d.q_o[i]);
+  const double q = d.q_o[i];
+  const float qh = __double2float_rn(q);
+  d.xl[s] = make_float4(__double2float_rn(x - (double)hx), __double2float_rn(y - (double)hy),
+                        __double2float_rn(z - (double)hz), qh);
+  d.qlo[s] = __double2float_rn(q - (double)qh);
   d.ts[s] = t;
   d.tags[s] = d.tag_o[i];
   d.seg_s[s] = d.seg_o[i];
@@ -298,20 +300,40 @@ __device__ __forceinline__ void pair_h(const Dev &d, const Control &C, const For
   }
 }
 
+// FP64 form, orthogonal segments: H_ij from the FP64 table with r^2, the
+// interval offset and the cubic as FP32 pairs (~1e-13 relative, far below
+// the table's 1e-10), so only the final conversion uses the FP64 pipe
+__device__ __forceinline__ double pair_h_fp(const Dev &d, const Control &C, int ti, int tj,
+                                            fpair s2) {
+  int k;
+  fpair u;
+  fp_interval(C, s2, k, u);
+  const float4 *T = d.tab_h_fp + ((long long)C.tab_pair[ti][tj] * C.tab_n + k) * 2;
+  return fp_to_double(fp_cubic(T[0], T[1], u));
+}
+
+// whether the FP64 form takes H_ij from pair_h_fp
+__device__ __forceinline__ bool use_h_fp(const Dev &d, const Control &C, const SegGeom &g,
+                                         float d2f) {
+  return d.tab_h_fp && C.h_all_listed && !g.tri && d2f >= C.tab_s0_f;
+}
+
 template <bool MIXED>
 __device__ __forceinline__ void nbr_flush(const Dev &d, const Control &C, const ForceField &F,
                                           const NbrQueue &Q, int cnt, int lane, int i,
                                           const double4 &xi, const float4 &xif, const float4 &xil,
                                           int ti, const SegGeom &g) {
-  bool in = false, near = false, in_m = false, near_m = false;
+  bool in = false, near = false, in_m = false, near_m = false, hfp = false;
   double d2 = 0.0;
   float d2f = 0.f;
   int j = 0, img = 0, sx = 0, sy = 0, sz = 0;
+  float4 hj = make_float4(0.f, 0.f, 0.f, 0.f), lj = hj;
   if (lane < cnt) {
     j = Q.j[lane];
     img = Q.img[lane];
     img_unpack(img, &sx, &sy, &sz);
-    const float4 hj = d.xf[j], lj = d.xl[j];
+    hj = d.xf[j];
+    lj = d.xl[j];
     float dx, dy, dz;
     disp32(g, hj, lj, xif, xil, sx, sy, sz, dx, dy, dz);
     d2f = dx * dx + dy * dy + dz * dz;
@@ -335,11 +357,14 @@ __device__ __forceinline__ void nbr_flush(const Dev &d, const Control &C, const 
       }
     }
     if (!MIXED && (in || in_m)) {
-      // r^2 for H: FMA-rounded from the exact displacement (the pair
-      // functions are smooth; membership is decided above)
-      double ex, ey, ez;
-      disp64(g, d.xs[j], xi, sx, sy, sz, ex, ey, ez);
-      d2 = fma(ex, ex, fma(ey, ey, ez * ez));
+      hfp = use_h_fp(d, C, g, d2f);
+      if (!hfp) {
+        // r^2 for H: FMA-rounded from the exact displacement (the pair
+        // functions are smooth; membership is decided above)
+        double ex, ey, ez;
+        disp64(g, d.xs[j], xi, sx, sy, sz, ex, ey, ez);
+        d2 = fma(ex, ex, fma(ey, ey, ez * ez));
+      }
     }
   }
   // row i: claim the batch's near and far slots with one atomic each
@@ -357,7 +382,8 @@ __device__ __forceinline__ void nbr_flush(const Dev &d, const Control &C, const 
   const int tj = __float_as_int(d.xf[j].w);
   double h = 0.0;
   float h32 = 0.f;
-  pair_h<MIXED>(d, C, F, ti, tj, d2, d2f, h, h32);
+  if (!MIXED && hfp) h = pair_h_fp(d, C, ti, tj, fp_d2(g, hj, lj, xif, xil, sx, sy, sz));
+  else pair_h<MIXED>(d, C, F, ti, tj, d2, d2f, h, h32);
   if (in) {
     const int p = near ? baseN + __popc(mn & lanemask_lt()) : baseF + __popc(mf & lanemask_lt());
     if (p < (near ? capN : capF)) {
@@ -662,9 +688,15 @@ __global__ void __launch_bounds__(TILE_T) k_build_nbrs_tiles(Dev d) {
                 }
                 double d2 = 0.0;
                 if (!MIXED && (in || in_m)) {
-                  double ex, ey, ez;
-                  disp64(g, T.bx[b], T.ax[a], sx, sy, sz, ex, ey, ez);
-                  d2 = fma(ex, ex, fma(ey, ey, ez * ez));
+                  if (use_h_fp(d, C, g, d2f)) {
+                    // r^2 as an FP32 pair, its bits in the FP64 slot
+                    const fpair p = fp_d2(g, T.bf[b], T.bl[b], T.af[a], T.al[a], sx, sy, sz);
+                    d2 = __hiloint2double(__float_as_int(p.hi), __float_as_int(p.lo));
+                  } else {
+                    double ex, ey, ez;
+                    disp64(g, T.bx[b], T.ax[a], sx, sy, sz, ex, ey, ez);
+                    d2 = fma(ex, ex, fma(ey, ey, ez * ez));
+                  }
                 }
                 T.d2[k] = d2;
                 T.d2f[k] = d2f;
@@ -690,7 +722,13 @@ __global__ void __launch_bounds__(TILE_T) k_build_nbrs_tiles(Dev d) {
                 const int ta = __float_as_int(T.af[a].w), tb = __float_as_int(T.bf[b].w);
                 double h;
                 float h32;
-                pair_h<MIXED>(d, C, F, ta, tb, T.d2[k], T.d2f[k], h, h32);
+                if (!MIXED && use_h_fp(d, C, g, T.d2f[k])) {
+                  const double v = T.d2[k];
+                  h = pair_h_fp(d, C, ta, tb,
+                                {__int_as_float(__double2hiint(v)), __int_as_float(__double2loint(v))});
+                } else {
+                  pair_h<MIXED>(d, C, F, ta, tb, T.d2[k], T.d2f[k], h, h32);
+                }
                 if (f & 1) {
                   const bool nr = f & 2;
                   const int pos = T.cnt[nr ? 0 : 1][a] + T.rk[k][0];

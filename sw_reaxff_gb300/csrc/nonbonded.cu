@@ -65,7 +65,8 @@ __device__ __forceinline__ double cubic_u(const double2 &c01, const double2 &c23
 // the energies are added to evdw and eele
 template <bool EF>
 __device__ __forceinline__ bool pair_terms(const Dev &d, const ForceField &F, const Control &C,
-                                          uint32_t e, bool act, const double4 &xi, int ti,
+                                          uint32_t e, bool act, const double4 &xi,
+                                          const float4 &xif, const float4 &xil, fpair qi, int ti,
                                           const SegGeom &g, double &ev, double &ee,
                                           double &c, double &dx, double &dy, double &dz,
                                           int &j) {
@@ -82,6 +83,27 @@ __device__ __forceinline__ bool pair_terms(const Dev &d, const ForceField &F, co
   if (!C.nonb_all_listed &&
       __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz)) > C.nonb_cut2)
     return false;
+  if (d.tab_nb_fp && !g.tri) {
+    // orthogonal segments: the table lookup with r^2, the interval offset,
+    // the cubics and q_i q_j as FP32 pairs (~1e-13 relative, far below the
+    // tables' 1e-10); the FP64 pipe takes the conversions, the
+    // displacement and the force products only
+    const float4 hj = d.xf[j], lj = d.xl[j];
+    const fpair s2 = fp_d2(g, hj, lj, xif, xil, sx, sy, sz);
+    if (s2.hi >= C.tab_s0_f) {
+      int k;
+      fpair u;
+      fp_interval(C, s2, k, u);
+      const float4 *T = d.tab_nb_fp + ((long long)C.tab_pair[ti][__float_as_int(hj.w)] * C.tab_n + k) * 8;
+      const fpair qq = fp_mul(qi, {lj.w, d.qlo[j]});
+      c = fp_to_double(fp_add(fp_cubic(T[0], T[1], u), fp_mul(qq, fp_cubic(T[2], T[3], u))));
+      if (EF) {
+        ev = fp_to_double(fp_cubic(T[4], T[5], u));
+        ee = fp_to_double(fp_mul(qq, fp_cubic(T[6], T[7], u)));
+      }
+      return true;
+    }
+  }
   const double d2 = fma(dx, dx, fma(dy, dy, dz * dz));
   if (C.tab_n && d2 >= C.tab_s0) {
     // FP64 tables in s = r^2: (1/r) dE/dr of vdW and of Coulomb per unit
@@ -306,7 +328,8 @@ __global__ void __launch_bounds__(NBW * 32, std::is_same<R, double>::value ? 3 :
     const int n = d.n;
     const double4 xi = d.xs[i];
     const float4 xif = d.xf[i];
-    const float4 xil = d.mixed ? d.xl[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+    const float4 xil = d.xl[i];
+    const fpair qi = {xil.w, d.mixed ? 0.f : d.qlo[i]};
     const int ti = d.ts[i];
     const SegGeom &g = d.seg[d.seg_s[i]];
     const long long row = (long long)i * d.nb_cap;
@@ -362,7 +385,7 @@ __global__ void __launch_bounds__(NBW * 32, std::is_same<R, double>::value ? 3 :
                        (double)dz);
         } else {
           double c, dx, dy, dz, ev, ee;
-          if (pair_terms<EF>(d, F, C, e, act, xi, ti, g, ev, ee, c, dx, dy, dz, j)) {
+          if (pair_terms<EF>(d, F, C, e, act, xi, xif, xil, qi, ti, g, ev, ee, c, dx, dy, dz, j)) {
             fx -= c * dx;
             fy -= c * dy;
             fz -= c * dz;

@@ -450,7 +450,9 @@ __global__ void k_qeq_finish(Dev d) {
   const double q = x.x - u * x.y;
   d.q_o[i] = q;
   d.xs[s].w = q;
-  if (d.xl) d.xl[s].w = (float)q;
+  const float qh = __double2float_rn(q);
+  d.xl[s].w = qh;
+  d.qlo[s] = __double2float_rn(q - (double)qh);
   for (int k = 4; k > 0; --k) {
     d.s_hist[k * n + i] = d.s_hist[(k - 1) * n + i];
     d.t_hist[k * n + i] = d.t_hist[(k - 1) * n + i];

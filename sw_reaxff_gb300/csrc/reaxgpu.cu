@@ -93,7 +93,8 @@ struct rg_system {
   ForceField *d_ff = nullptr;
   Control *d_ctl = nullptr;
   double *d_tab = nullptr;        // FP64 tables (nb then H)
-  float *d_tab32 = nullptr;       // mixed form: the nb table in FP32
+  float *d_tab32 = nullptr;       // FP32 tables: the mixed form's nb table, or the FP64
+                                  // form's nb and H tables as FP32 pairs
   double tab_err = 0.0;
   cudaStream_t st = nullptr;
   std::string err;
@@ -405,6 +406,7 @@ int alloc_atoms(rg_system *h, int n) {
   r |= dalloc(h, B, &d.xs, (size_t)n);
   r |= dalloc(h, B, &d.xf, (size_t)n);
   r |= dalloc(h, B, &d.xl, (size_t)n);
+  r |= dalloc(h, B, &d.qlo, (size_t)n);
   r |= dalloc(h, B, &d.ts, (size_t)n);
   r |= dalloc(h, B, &d.tags, (size_t)n);
   r |= dalloc(h, B, &d.n_near, (size_t)n);
@@ -1251,6 +1253,8 @@ int rg_create(const char *ffield_path, const rg_params *pin, rg_system **out) {
     c.tab_x0 = -s0 * c.tab_inv_ds;
     c.tab_inv_ds_f = (float)c.tab_inv_ds;
     c.tab_x0_f = (float)c.tab_x0;
+    c.tab_inv_ds_l = (float)(c.tab_inv_ds - (double)c.tab_inv_ds_f);
+    c.tab_x0_l = (float)(c.tab_x0 - (double)c.tab_x0_f);
     h->tab_err = rg_build_tables(h->ff, c, c.tab_n, s0, s1, tab_nb, tab_h, h->p.tabulate_check != 0);
   }
   cudaError_t ce = cudaSetDevice(h->p.device);
@@ -1273,6 +1277,19 @@ int rg_create(const char *ffield_path, const rg_params *pin, rg_system **out) {
     if (ce == cudaSuccess)
       ce = cudaMemcpy(h->d_tab + tab_nb.size(), tab_h.data(), sizeof(double) * tab_h.size(),
                       cudaMemcpyHostToDevice);
+    // the same coefficients as FP32 pairs (hi, lo) for the orthogonal
+    // segments' pairs
+    std::vector<float> fp(2 * (tab_nb.size() + tab_h.size()));
+    size_t o = 0;
+    for (const std::vector<double> *t : {&tab_nb, &tab_h})
+      for (double v : *t) {
+        const float hi = (float)v;
+        fp[o++] = hi;
+        fp[o++] = (float)(v - (double)hi);
+      }
+    if (ce == cudaSuccess) ce = cudaMalloc(&h->d_tab32, sizeof(float) * fp.size());
+    if (ce == cudaSuccess)
+      ce = cudaMemcpy(h->d_tab32, fp.data(), sizeof(float) * fp.size(), cudaMemcpyHostToDevice);
   }
   if (ce != cudaSuccess) {
     if (h->d_ff) cudaFree(h->d_ff);
@@ -1287,7 +1304,15 @@ int rg_create(const char *ffield_path, const rg_params *pin, rg_system **out) {
   h->d.ctl = h->d_ctl;
   h->d.tab_nb = h->d_tab;
   h->d.tab_h = h->d_tab ? h->d_tab + tab_nb.size() : nullptr;
-  h->d.tab_nb32 = h->d_tab32;
+  if (h->d.mixed) {
+    h->d.tab_nb32 = h->d_tab32;
+    h->d.tab_nb_fp = h->d.tab_h_fp = nullptr;
+  } else {
+    h->d.tab_nb32 = nullptr;
+    h->d.tab_nb_fp = reinterpret_cast<const float4 *>(h->d_tab32);
+    h->d.tab_h_fp = h->d_tab32 ? reinterpret_cast<const float4 *>(h->d_tab32 + 2 * tab_nb.size())
+                               : nullptr;
+  }
   *out = h;
   return RG_OK;
 }

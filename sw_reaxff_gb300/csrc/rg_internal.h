@@ -112,6 +112,7 @@ struct Control {
   double tab_s0, tab_ds, tab_inv_ds, tab_x0;   // tab_x0 = -tab_s0 / tab_ds
   float tab_s0_f;        // table or analytic form below it (either is the function)
   float tab_inv_ds_f, tab_x0_f;   // the mixed form's FP32 lookups
+  float tab_inv_ds_l, tab_x0_l;   // with these: tab_inv_ds, tab_x0 as FP32 pairs
   int tab_pair[RG_MAXT][RG_MAXT];   // unordered type pair -> table index
   // FP32 copies for the prefilters (no FP64 conversions per entry; GB300
   // runs FP64 at 1/64 of the FP32 rate)
@@ -179,6 +180,9 @@ struct Dev {
   const double *tab_nb;  // [pair][interval][16]: cubics in u of Fv, Fc, Ev, Ec (tables.cpp)
   const double *tab_h;   // [pair][interval][4]: cubic in u of H_ij
   const float *tab_nb32; // mixed form: tab_nb in FP32
+  // FP64 form: tab_nb and tab_h with each coefficient as an FP32 pair
+  // (float4 = two coefficients), for the orthogonal segments' pairs
+  const float4 *tab_nb_fp, *tab_h_fp;
 
   // original order (persistent state)
   double *x_o, *v_o, *q_o, *f_o;
@@ -194,8 +198,9 @@ struct Dev {
   // sorted atoms
   double4 *xs;        // x, y, z, q
   float4 *xf;         // fp32 x, y, z, (type as float)
-  float4 *xl;         // mixed form: x - xf (FP32), so x = xf + xl to ~2^-48;
+  float4 *xl;         // x - xf (FP32), so x = xf + xl to ~2^-48;
                       // w: the charge (FP32)
+  float *qlo;         // q - xl.w (FP32): the charge as an FP32 pair
   int *ts, *tags;
 
   // full pair list (both directions), row-major rows of nb_cap: near
@@ -540,6 +545,93 @@ __device__ __forceinline__ float df_disp2(float hj, float lj, float hi, float li
   const float a = __fsub_rn(__fadd_rn(hj, vh), hi);
   const float b = __fsub_rn(__fadd_rn(lj, vl), li);
   return __fadd_rn(a, b);
+}
+
+// Unevaluated FP32 pairs (value = hi + lo) for the FP64 form's tabulated
+// pair functions: positions, charges and table coefficients are exact FP32
+// pairs (to ~2^-48), and the operations below keep ~2^-46 relative (of the
+// operands' magnitudes) on the FP32 units, where GB300's FP64 rate is 1/64
+// of FP32.  Explicitly rounded: no contraction may change them.
+struct fpair {
+  float hi, lo;
+};
+
+// Knuth's TwoSum: hi + lo = a + b exactly
+__device__ __forceinline__ fpair fp_two_sum(float a, float b) {
+  const float s = __fadd_rn(a, b);
+  const float bb = __fsub_rn(s, a);
+  return {s, __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb))};
+}
+
+// the same for |a| >= |b| (Dekker)
+__device__ __forceinline__ fpair fp_fast(float a, float b) {
+  const float s = __fadd_rn(a, b);
+  return {s, __fsub_rn(b, __fsub_rn(s, a))};
+}
+
+__device__ __forceinline__ fpair fp_add(fpair a, fpair b) {
+  const fpair s = fp_two_sum(a.hi, b.hi);
+  return fp_fast(s.hi, __fadd_rn(s.lo, __fadd_rn(a.lo, b.lo)));
+}
+
+__device__ __forceinline__ fpair fp_mul(fpair a, fpair b) {
+  const float p = __fmul_rn(a.hi, b.hi);
+  float e = __fmaf_rn(a.hi, b.hi, -p);
+  e = __fmaf_rn(a.hi, b.lo, e);
+  e = __fmaf_rn(a.lo, b.hi, e);
+  return fp_fast(p, e);
+}
+
+__device__ __forceinline__ fpair fp_sqr(fpair a) {
+  const float p = __fmul_rn(a.hi, a.hi);
+  float e = __fmaf_rn(a.hi, a.hi, -p);
+  e = __fmaf_rn(__fadd_rn(a.hi, a.hi), a.lo, e);
+  return fp_fast(p, e);
+}
+
+__device__ __forceinline__ double fp_to_double(fpair a) {
+  return __dadd_rn((double)a.hi, (double)a.lo);
+}
+
+// (x_j + s L) - x_i of one coordinate from (hi, lo) positions and the box
+// edge L = Lh + Ll of an orthogonal segment (s Lh and s Ll are exact for
+// |s| <= 2)
+__device__ __forceinline__ fpair fp_disp(float hj, float lj, float hi, float li, int s, float Lh,
+                                         float Ll) {
+  const float sf = (float)s;
+  const fpair a = fp_two_sum(hj, __fmul_rn(sf, Lh));
+  const fpair b = fp_two_sum(a.hi, -hi);
+  const float lo = __fadd_rn(__fadd_rn(__fsub_rn(lj, li), __fadd_rn(a.lo, b.lo)), __fmul_rn(sf, Ll));
+  return fp_fast(b.hi, lo);
+}
+
+// r^2 of a pair of an orthogonal segment as an FP32 pair
+__device__ __forceinline__ fpair fp_d2(const SegGeom &g, const float4 &hj, const float4 &lj,
+                                       const float4 &hi, const float4 &li, int sx, int sy, int sz) {
+  const fpair dx = fp_disp(hj.x, lj.x, hi.x, li.x, sx, g.Lh[0], g.Ll[0]);
+  const fpair dy = fp_disp(hj.y, lj.y, hi.y, li.y, sy, g.Lh[1], g.Ll[1]);
+  const fpair dz = fp_disp(hj.z, lj.z, hi.z, li.z, sz, g.Lh[2], g.Ll[2]);
+  return fp_add(fp_add(fp_sqr(dx), fp_sqr(dy)), fp_sqr(dz));
+}
+
+// table interval k and offset u in [0, 1] of s = r^2 >= tab_s0 (the FP64
+// tables' intervals)
+__device__ __forceinline__ void fp_interval(const Control &C, fpair s2, int &k, fpair &u) {
+  const fpair x = fp_add(fp_mul(s2, {C.tab_inv_ds_f, C.tab_inv_ds_l}), {C.tab_x0_f, C.tab_x0_l});
+  int kk = (int)x.hi;
+  if ((float)kk == x.hi && x.lo < 0.f) --kk;
+  kk = min(max(kk, 0), C.tab_n - 1);
+  k = kk;
+  u = fp_fast(__fsub_rn(x.hi, (float)kk), x.lo);
+}
+
+// c0 + u (c1 + u (c2 + u c3)) with the coefficients as FP32 pairs
+// (c01 = c0.hi, c0.lo, c1.hi, c1.lo; c23 likewise)
+__device__ __forceinline__ fpair fp_cubic(const float4 &c01, const float4 &c23, fpair u) {
+  fpair h = {c23.z, c23.w};
+  h = fp_add(fp_mul(h, u), {c23.x, c23.y});
+  h = fp_add(fp_mul(h, u), {c01.z, c01.w});
+  return fp_add(fp_mul(h, u), {c01.x, c01.y});
 }
 
 // mixed-form displacement (x_j + image) - x_i; a triclinic image is formed

@@ -176,6 +176,58 @@ __device__ __forceinline__ bool pair_terms(const Dev &d, const ForceField &F, co
   return true;
 }
 
+__device__ __forceinline__ fpair fp_split(double v) {
+  const float h = __double2float_rn(v);
+  return {h, __double2float_rn(v - (double)h)};
+}
+
+// FP64 form, orthogonal segment, every listed pair inside the cutoff, no
+// virial or per-atom tally: the pair's force g = (1/r) dE/dr (x_j - x_i)
+// with the displacement, the table lookup and the products as FP32 pairs
+// (~1e-13 relative); the FP64 pipe converts g for the partner's atomics
+// only.  Pairs below the tables take the FP64 expressions.
+template <bool EF>
+__device__ __forceinline__ bool pair_fp(const Dev &d, const ForceField &F, const Control &C,
+                                       uint32_t e, bool act, const double4 &xi, const float4 &xif,
+                                       const float4 &xil, fpair qi, int ti, const SegGeom &g,
+                                       double &ev, double &ee, fpair &gx, fpair &gy, fpair &gz,
+                                       int &j) {
+  gx = gy = gz = {0.f, 0.f};
+  ev = ee = 0.0;
+  j = (int)(e >> 8);
+  if (!act) return false;
+  int sx, sy, sz;
+  img_unpack((int)(e & 255u), &sx, &sy, &sz);
+  const float4 hj = d.xf[j], lj = d.xl[j];
+  const fpair dx = fp_disp(hj.x, lj.x, xif.x, xil.x, sx, g.Lh[0], g.Ll[0]);
+  const fpair dy = fp_disp(hj.y, lj.y, xif.y, xil.y, sy, g.Lh[1], g.Ll[1]);
+  const fpair dz = fp_disp(hj.z, lj.z, xif.z, xil.z, sz, g.Lh[2], g.Ll[2]);
+  const fpair s2 = fp_add(fp_add(fp_sqr(dx), fp_sqr(dy)), fp_sqr(dz));
+  if (!(s2.hi >= C.tab_s0_f)) {
+    double c, ex, ey, ez;
+    if (!pair_terms<EF>(d, F, C, e, act, xi, xif, xil, qi, ti, g, ev, ee, c, ex, ey, ez, j))
+      return false;
+    gx = fp_split(c * ex);
+    gy = fp_split(c * ey);
+    gz = fp_split(c * ez);
+    return true;
+  }
+  int k;
+  fpair u;
+  fp_interval(C, s2, k, u);
+  const float4 *T = d.tab_nb_fp + ((long long)C.tab_pair[ti][__float_as_int(hj.w)] * C.tab_n + k) * 8;
+  const fpair qq = fp_mul(qi, {lj.w, d.qlo[j]});
+  const fpair c = fp_add(fp_cubic(T[0], T[1], u), fp_mul(qq, fp_cubic(T[2], T[3], u)));
+  gx = fp_mul(c, dx);
+  gy = fp_mul(c, dy);
+  gz = fp_mul(c, dz);
+  if (EF) {
+    ev = fp_to_double(fp_cubic(T[4], T[5], u));
+    ee = fp_to_double(fp_mul(qq, fp_cubic(T[6], T[7], u)));
+  }
+  return true;
+}
+
 __device__ __forceinline__ float cubic_uf(const float4 &c, float u) {
   return fmaf(fmaf(fmaf(c.w, u, c.z), u, c.y), u, c.x);
 }
@@ -337,6 +389,8 @@ __global__ void __launch_bounds__(NBW * 32, std::is_same<R, double>::value ? 3 :
     const int capN = d.nb_capN;
     const int tot = nn + nf;
     double fx = 0, fy = 0, fz = 0;
+    fpair gxs = {0.f, 0.f}, gys = gxs, gzs = gxs;  // pair_fp: sum of the pairs' g
+    const bool fast = !VIR && !AT && d.tab_nb_fp && !g.tri && C.nonb_all_listed;
     float fx32 = 0.f, fy32 = 0.f, fz32 = 0.f;   // mixed form: FP32 force sums
     double ta[7] = {0, 0, 0, 0, 0, 0, 0};        // AT: atom i's energy and virial
     double *fC = d.fC;
@@ -383,6 +437,21 @@ __global__ void __launch_bounds__(NBW * 32, std::is_same<R, double>::value ? 3 :
           if (AT && act)
             atom_tally(d, ta, j, (double)ev, (double)ee, (double)c, (double)dx, (double)dy,
                        (double)dz);
+        } else if (fast) {
+          fpair gx, gy, gz;
+          double ev, ee;
+          if (pair_fp<EF>(d, F, C, e, act, xi, xif, xil, qi, ti, g, ev, ee, gx, gy, gz, j)) {
+            gxs = fp_add(gxs, gx);
+            gys = fp_add(gys, gy);
+            gzs = fp_add(gzs, gz);
+            atomicAdd(&fC[j], fp_to_double(gx));
+            atomicAdd(&fC[n + j], fp_to_double(gy));
+            atomicAdd(&fC[2 * n + j], fp_to_double(gz));
+            if (EF) {
+              evdw += ev;
+              eele += ee;
+            }
+          }
         } else {
           double c, dx, dy, dz, ev, ee;
           if (pair_terms<EF>(d, F, C, e, act, xi, xif, xil, qi, ti, g, ev, ee, c, dx, dy, dz, j)) {
@@ -422,6 +491,11 @@ __global__ void __launch_bounds__(NBW * 32, std::is_same<R, double>::value ? 3 :
         atomicAdd(&d.fC32[2 * n + i], fz32);
       }
     } else {
+      if (fast) {
+        fx -= fp_to_double(gxs);
+        fy -= fp_to_double(gys);
+        fz -= fp_to_double(gzs);
+      }
       fx = warp_sum(fx);
       fy = warp_sum(fy);
       fz = warp_sum(fz);

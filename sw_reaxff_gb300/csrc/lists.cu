@@ -302,14 +302,20 @@ __device__ __forceinline__ void pair_h(const Dev &d, const Control &C, const For
 
 // FP64 form, orthogonal segments: H_ij from the FP64 table with r^2, the
 // interval offset and the cubic as FP32 pairs (~1e-13 relative, far below
-// the table's 1e-10), so only the final conversion uses the FP64 pipe
-__device__ __forceinline__ double pair_h_fp(const Dev &d, const Control &C, int ti, int tj,
-                                            fpair s2) {
+// the table's 1e-10), on the FP32 units only
+__device__ __forceinline__ fpair pair_h_fp(const Dev &d, const Control &C, int ti, int tj,
+                                           fpair s2) {
   int k;
   fpair u;
   fp_interval(C, s2, k, u);
   const float4 *T = d.tab_h_fp + ((long long)C.tab_pair[ti][tj] * C.tab_n + k) * 2;
-  return fp_to_double(fp_cubic(T[0], T[1], u));
+  return fp_cubic(T[0], T[1], u);
+}
+
+// an FP64 H_ij as the FP32 pair the FP64 form stores
+__device__ __forceinline__ float2 h_pair(double h) {
+  const float hi = __double2float_rn(h);
+  return make_float2(hi, __double2float_rn(h - (double)hi));
 }
 
 // whether the FP64 form takes H_ij from pair_h_fp
@@ -382,15 +388,21 @@ __device__ __forceinline__ void nbr_flush(const Dev &d, const Control &C, const 
   const int tj = __float_as_int(d.xf[j].w);
   double h = 0.0;
   float h32 = 0.f;
-  if (!MIXED && hfp) h = pair_h_fp(d, C, ti, tj, fp_d2(g, hj, lj, xif, xil, sx, sy, sz));
-  else pair_h<MIXED>(d, C, F, ti, tj, d2, d2f, h, h32);
+  float2 hp = make_float2(0.f, 0.f);   // FP64 form: H_ij as an FP32 pair
+  if (!MIXED && hfp) {
+    const fpair v = pair_h_fp(d, C, ti, tj, fp_d2(g, hj, lj, xif, xil, sx, sy, sz));
+    hp = make_float2(v.hi, v.lo);
+  } else {
+    pair_h<MIXED>(d, C, F, ti, tj, d2, d2f, h, h32);
+    if (!MIXED) hp = h_pair(h);
+  }
   if (in) {
     const int p = near ? baseN + __popc(mn & lanemask_lt()) : baseF + __popc(mf & lanemask_lt());
     if (p < (near ? capN : capF)) {
       const long long slot = (long long)i * d.nb_cap + (near ? p : capN + p);
       d.nbr[slot] = ((uint32_t)j << 8) | (uint32_t)img;
       if (MIXED) d.hval32[slot] = h32;
-      else d.hval[slot] = h;
+      else d.hvalp[slot] = hp;
     }
   }
   if (in_m) {
@@ -399,7 +411,7 @@ __device__ __forceinline__ void nbr_flush(const Dev &d, const Control &C, const 
       const long long slot = (long long)j * d.nb_cap + (near_m ? p : capN + p);
       d.nbr[slot] = ((uint32_t)i << 8) | (uint32_t)img_pack(-sx, -sy, -sz);
       if (MIXED) d.hval32[slot] = h32;
-      else d.hval[slot] = h;
+      else d.hvalp[slot] = hp;
     }
   }
 }
@@ -722,12 +734,15 @@ __global__ void __launch_bounds__(TILE_T) k_build_nbrs_tiles(Dev d) {
                 const int ta = __float_as_int(T.af[a].w), tb = __float_as_int(T.bf[b].w);
                 double h;
                 float h32;
+                float2 hp = make_float2(0.f, 0.f);
                 if (!MIXED && use_h_fp(d, C, g, T.d2f[k])) {
                   const double v = T.d2[k];
-                  h = pair_h_fp(d, C, ta, tb,
-                                {__int_as_float(__double2hiint(v)), __int_as_float(__double2loint(v))});
+                  const fpair w = pair_h_fp(
+                      d, C, ta, tb, {__int_as_float(__double2hiint(v)), __int_as_float(__double2loint(v))});
+                  hp = make_float2(w.hi, w.lo);
                 } else {
                   pair_h<MIXED>(d, C, F, ta, tb, T.d2[k], T.d2f[k], h, h32);
+                  if (!MIXED) hp = h_pair(h);
                 }
                 if (f & 1) {
                   const bool nr = f & 2;
@@ -736,7 +751,7 @@ __global__ void __launch_bounds__(TILE_T) k_build_nbrs_tiles(Dev d) {
                     const long long slot = (long long)(a0 + a) * d.nb_cap + (nr ? pos : capN + pos);
                     d.nbr[slot] = ((uint32_t)(b0 + b) << 8) | img;
                     if (MIXED) d.hval32[slot] = h32;
-                    else d.hval[slot] = h;
+                    else d.hvalp[slot] = hp;
                   }
                 }
                 if (f & 4) {
@@ -746,7 +761,7 @@ __global__ void __launch_bounds__(TILE_T) k_build_nbrs_tiles(Dev d) {
                     const long long slot = (long long)(b0 + b) * d.nb_cap + (nr ? pos : capN + pos);
                     d.nbr[slot] = ((uint32_t)(a0 + a) << 8) | img_m;
                     if (MIXED) d.hval32[slot] = h32;
-                    else d.hval[slot] = h;
+                    else d.hvalp[slot] = hp;
                   }
                 }
               }

@@ -4,9 +4,10 @@
 //  k_qeq_setup   init_matvec: Jacobi diagonal, b_s = -chi, b_t = -1, cubic
 //                (s) / quadratic (t) extrapolation from the 5-deep
 //                histories (fix_qeq_reax_sunway.cpp:618-723)
-//  k_spmv        sparse_matvec: b_i = eta_i x_i + sum_j H_ij x_j over the
-//                full rows (fix_qeq_reax_sw64.c:357-498), both systems per
-//                read of H
+//  k_spmvp, k_spmv32  sparse_matvec: b_i = eta_i x_i + sum_j H_ij x_j over
+//                the full rows (fix_qeq_reax_sw64.c:357-498), both systems
+//                per read of H, in compensated FP32 arithmetic (FP64 form:
+//                H as an FP32 pair; mixed form: H in FP32)
 //  k_cg_*, k_pcg_*  CG_v2 (fix_qeq_reax_sunway.cpp:983-1167): Jacobi PCG
 //                with CG_v2's set-up, stopping test and iteration count, in
 //                the standard (not pipelined) recurrences; a system that
@@ -57,68 +58,6 @@ __global__ void k_qeq_setup(Dev d) {
 // y = H x (+ eta x on the diagonal), one warp per row; FP64 form.  In the
 // CG iterations (use_act) a system whose solve has converged is skipped:
 // its half of y is not read again
-// Half a warp per row (rows average several hundred entries): each lane
-// keeps the s and t partial sums of its entries; the two sums are reduced
-// together (the first exchange swaps halves, so every later level is one
-// add per lane for both systems), and lanes 0 and 1 of the row group write
-// y_s and y_t.
-template <int RW>
-__device__ __forceinline__ double pair_sum(double a, double b, int gl) {
-  const bool odd = gl & 1;
-  double v = odd ? b : a;
-  v += __shfl_xor_sync(0xffffffffu, odd ? a : b, 1);
-  for (int off = 2; off < RW; off <<= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
-  return v;   // group lane 0: sum of a; group lane 1: sum of b
-}
-
-template <int RW>
-__global__ void __launch_bounds__(256) k_spmv(Dev d, const double2 *__restrict__ x, double2 *__restrict__ y,
-                                              int use_act) {
-  const long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  const int gl = (int)(tid & (RW - 1));
-  const int i = (int)(tid / RW);
-  const bool valid = i < d.n;     // no early return: the row group shuffles
-  const long long row = (long long)i * d.nb_cap;
-  const int nn = valid ? nbr_near_count(d, i) : 0, nf = valid ? nbr_far_count(d, i) : 0;
-  const int tot = nn + nf, capN = d.nb_capN;
-  bool on_s = valid, on_t = valid;
-  if (use_act && valid) {
-    // activity flags are exactly 0.0 or 1.0: compare their bits (no FP64)
-    const long long *R = reinterpret_cast<const long long *>(d.red + (long long)d.seg_s[i] * RG_NRED);
-    on_s = R[R_ACTIVE] != 0;
-    on_t = R[R_ACTIVE + 1] != 0;
-  }
-  double as = 0.0, at = 0.0;
-  if (on_s && on_t) {
-    for (int p = gl; p < tot; p += RW) {
-      const int slot = p < nn ? p : capN + (p - nn);
-      const uint32_t e = d.nbr[row + slot];
-      const double h = d.hval[row + slot];
-      const double2 xj = x[e >> 8];
-      as = fma(h, xj.x, as);
-      at = fma(h, xj.y, at);
-    }
-  } else if (on_s || on_t) {
-    for (int p = gl; p < tot; p += RW) {
-      const int slot = p < nn ? p : capN + (p - nn);
-      const uint32_t e = d.nbr[row + slot];
-      const double h = d.hval[row + slot];
-      const double2 xj = x[e >> 8];
-      as = fma(h, on_s ? xj.x : xj.y, as);
-    }
-    if (on_t) {
-      at = as;
-      as = 0.0;
-    }
-  }
-  const double v = pair_sum<RW>(as, at, gl);
-  if (valid && gl < 2) {
-    const double eta = d.ff->sbp[d.ts[i]].eta;
-    const double *xi = reinterpret_cast<const double *>(x) + 2 * (long long)i;
-    reinterpret_cast<double *>(y)[2 * (long long)i + gl] = fma(eta, xi[gl], v);
-  }
-}
-
 // mixed form: the FP32 H with compensated FP32 arithmetic.  The vector is
 // read as FP32 (hi, lo) pairs (x = hi + lo to ~2^-48), each product is
 // formed exactly as p + e (fmaf) plus h*lo, and the row sum is carried as an
@@ -157,7 +96,8 @@ __device__ __forceinline__ float4 split4(double2 v) {
   return make_float4(sh, __double2float_rn(v.x - (double)sh), th, __double2float_rn(v.y - (double)th));
 }
 
-// Half a warp per row as in k_spmv.  The compensated pairs of the two
+// RW lanes per row (rows average several hundred entries), each keeping
+// the s and t sums of its entries.  The compensated pairs of the two
 // systems are reduced together (the first exchange swaps halves, each later
 // level is one compensated add per lane), and lanes 0 and 1 of the row
 // group finish y_s and y_t: the FP64 tail (conversion, eta x) is one warp
@@ -258,6 +198,103 @@ __global__ void __launch_bounds__(256) k_spmv32(Dev d, const double2 *__restrict
   }
 }
 
+
+// (sh, sl) += (hh + hl) * (xh + xl): the leading product exact (fmaf), the
+// cross terms hh xl and hl xh added to its error (hl xl, ~2^-48 of the
+// product, is left out)
+__device__ __forceinline__ void dd_fma(float hh, float hl, float xh, float xl, float &sh, float &sl) {
+  const float p = __fmul_rn(hh, xh);
+  float e = __fmaf_rn(hh, xh, -p);
+  e = __fmaf_rn(hh, xl, e);
+  e = __fmaf_rn(hl, xh, e);
+  float s, err;
+  two_sum(sh, p, s, err);
+  sh = s;
+  sl = __fadd_rn(sl, __fadd_rn(err, e));
+}
+
+// FP64 form: H_ij stored as an FP32 pair (its table value to ~2^-48) times
+// the vector's FP32 (hi, lo) pairs, summed as in k_spmv32: the products and
+// sums keep ~2^-46 of |H||x| (the FP64 DFMA form's 2^-53 is not needed by a
+// solve to 1e-6, and GB300 runs FP64 FMAs at 1/64 of the FP32 rate).
+// 12 bytes of index and H per entry.
+template <int RW>
+__global__ void __launch_bounds__(256) k_spmvp(Dev d, const double2 *__restrict__ x, double2 *__restrict__ y,
+                                               int use_act) {
+  const long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const int gl = (int)(tid & (RW - 1));
+  const int i = (int)(tid / RW);
+  const bool valid = i < d.n;     // no early return: the row group shuffles
+  const long long row = (long long)i * d.nb_cap;
+  const int nn = valid ? nbr_near_count(d, i) : 0, nf = valid ? nbr_far_count(d, i) : 0;
+  const int tot = nn + nf, capN = d.nb_capN;
+  const float4 *__restrict__ x32 = d.qd32;
+  const float2 *__restrict__ H = d.hvalp;
+  bool on_s = valid, on_t = valid;
+  if (use_act && valid) {
+    const long long *R = reinterpret_cast<const long long *>(d.red + (long long)d.seg_s[i] * RG_NRED);
+    on_s = R[R_ACTIVE] != 0;
+    on_t = R[R_ACTIVE + 1] != 0;
+  }
+  float sh = 0.f, sl = 0.f, th = 0.f, tl = 0.f;
+  if (on_s && on_t) {
+    float sh1 = 0.f, sl1 = 0.f, th1 = 0.f, tl1 = 0.f;
+    int p = gl;
+    for (; p + 3 * RW < tot; p += 4 * RW) {
+      uint32_t e4[4];
+      float2 h4[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const int q = p + u * RW;
+        const int s = q < nn ? q : capN + (q - nn);
+        e4[u] = d.nbr[row + s];
+        h4[u] = H[row + s];
+      }
+      float4 x4[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) x4[u] = x32[e4[u] >> 8];
+      dd_fma(h4[0].x, h4[0].y, x4[0].x, x4[0].y, sh, sl);
+      dd_fma(h4[0].x, h4[0].y, x4[0].z, x4[0].w, th, tl);
+      dd_fma(h4[1].x, h4[1].y, x4[1].x, x4[1].y, sh1, sl1);
+      dd_fma(h4[1].x, h4[1].y, x4[1].z, x4[1].w, th1, tl1);
+      dd_fma(h4[2].x, h4[2].y, x4[2].x, x4[2].y, sh, sl);
+      dd_fma(h4[2].x, h4[2].y, x4[2].z, x4[2].w, th, tl);
+      dd_fma(h4[3].x, h4[3].y, x4[3].x, x4[3].y, sh1, sl1);
+      dd_fma(h4[3].x, h4[3].y, x4[3].z, x4[3].w, th1, tl1);
+    }
+    for (; p < tot; p += RW) {
+      const int slot = p < nn ? p : capN + (p - nn);
+      const uint32_t e = d.nbr[row + slot];
+      const float2 h = H[row + slot];
+      const float4 xj = x32[e >> 8];
+      dd_fma(h.x, h.y, xj.x, xj.y, sh, sl);
+      dd_fma(h.x, h.y, xj.z, xj.w, th, tl);
+    }
+    df_add(sh, sl, sh1, sl1);
+    df_add(th, tl, th1, tl1);
+  } else if (on_s) {
+    for (int p = gl; p < tot; p += RW) {
+      const int slot = p < nn ? p : capN + (p - nn);
+      const float2 h = H[row + slot];
+      const float4 xj = x32[d.nbr[row + slot] >> 8];
+      dd_fma(h.x, h.y, xj.x, xj.y, sh, sl);
+    }
+  } else if (on_t) {
+    for (int p = gl; p < tot; p += RW) {
+      const int slot = p < nn ? p : capN + (p - nn);
+      const float2 h = H[row + slot];
+      const float4 xj = x32[d.nbr[row + slot] >> 8];
+      dd_fma(h.x, h.y, xj.z, xj.w, th, tl);
+    }
+  }
+  float vh, vl;
+  df_pair_sum<RW>(vh, vl, sh, sl, th, tl, gl);
+  if (valid && gl < 2) {
+    const double eta = d.ff->sbp[d.ts[i]].eta;
+    const double *xi = reinterpret_cast<const double *>(x) + 2 * (long long)i;
+    reinterpret_cast<double *>(y)[2 * (long long)i + gl] = fma(eta, xi[gl], (double)vh + (double)vl);
+  }
+}
 
 // r = b - q; u = r*Hdia_inv; d = u
 __global__ void k_cg_init1(Dev d) {
@@ -473,7 +510,7 @@ template <int RW>
 static void spmv_rw(const Dev &d, cudaStream_t st, const double2 *x, double2 *y, int use_act,
                     int kind) {
   const unsigned G = (unsigned)(((long long)d.n * RW + 255) / 256);
-  if (kind == 0) k_spmv<RW><<<G, 256, 0, st>>>(d, x, y, use_act);
+  if (kind == 0) k_spmvp<RW><<<G, 256, 0, st>>>(d, x, y, use_act);
   else k_spmv32<RW><<<G, 256, 0, st>>>(d, x, y, use_act);
 }
 
@@ -484,8 +521,9 @@ static void spmv_kind(const Dev &d, cudaStream_t st, const double2 *x, double2 *
   else spmv_rw<16>(d, st, x, y, use_act, kind);
 }
 
-// FP64 form: the FP64 SpMV of x; mixed form: the compensated SpMV of the
-// split copy of x in qd32 (of qd after the kernels that update it)
+// the compensated SpMV of the split copy of x in qd32 (of qd after the
+// kernels that update it), with the FP64 form's FP32-pair H or the mixed
+// form's FP32 H
 void launch_qeq_spmv(const Dev &d, cudaStream_t st, const double2 *x, double2 *y, int use_act) {
   spmv_kind(d, st, x, y, use_act, d.mixed ? 1 : 0);
 }
@@ -496,18 +534,13 @@ __global__ void k_split_x(Dev d, const double2 *__restrict__ x) {
   if (i < d.n) d.qd32[i] = split4(x[i]);
 }
 
-// r = b - H x of the current iterate starts the pipelined CG.  The mixed
-// form's first pass, whose iterate the refinement checks in FP64 anyway,
-// takes it from the compensated FP32 SpMV of the iterations; its restarts
-// come from launch_qeq_refine_check + launch_qeq_cg_init_rest.
+// r = b - H x of the current iterate starts the CG (the SpMV of the
+// iterations, on the split copy of x); the mixed form's restarts come from
+// launch_qeq_refine_check + launch_qeq_cg_init_rest.
 void launch_qeq_cg_init(const Dev &d, cudaStream_t st, double tol, int imax) {
   const int B = 256, G = (d.n + B - 1) / B;
-  if (d.mixed) {
-    k_split_x<<<G, B, 0, st>>>(d, d.qx);
-    spmv_kind(d, st, d.qx, d.qq, 0, 1);
-  } else {
-    launch_qeq_spmv(d, st, d.qx, d.qq, 0);
-  }
+  k_split_x<<<G, B, 0, st>>>(d, d.qx);
+  launch_qeq_spmv(d, st, d.qx, d.qq, 0);
   k_cg_init1<<<G, B, 0, st>>>(d);
   launch_qeq_cg_init_rest(d, st, tol, imax);
 }

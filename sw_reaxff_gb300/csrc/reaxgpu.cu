@@ -361,9 +361,9 @@ int alloc_nbrs(rg_system *h) {
   r |= dalloc(h, h->per_nb, &d.nbr, S);
   if (d.mixed) {
     r |= dalloc(h, h->per_nb, &d.hval32, S);
-    d.hval = nullptr;
+    d.hvalp = nullptr;
   } else {
-    r |= dalloc(h, h->per_nb, &d.hval, S);
+    r |= dalloc(h, h->per_nb, &d.hvalp, S);
     d.hval32 = nullptr;
   }
   return r;
@@ -424,8 +424,7 @@ int alloc_atoms(rg_system *h, int n) {
   r |= dalloc(h, B, &d.c_sbo, 10 * (size_t)n);
   double2 **pv[] = {&d.qx, &d.qb, &d.qr, &d.qu, &d.qd, &d.qq};
   for (double2 **q : pv) r |= dalloc(h, B, q, (size_t)n);
-  if (d.mixed) r |= dalloc(h, B, &d.qd32, (size_t)n);
-  else d.qd32 = nullptr;
+  r |= dalloc(h, B, &d.qd32, (size_t)n);
   if (d.mixed) r |= dalloc(h, B, &d.fC32, 3 * (size_t)n);
   else d.fC32 = nullptr;
   r |= dalloc(h, B, &d.seg_o, (size_t)n);

@@ -208,7 +208,7 @@ struct Dev {
   // [nb_capN, nb_capN + n_far); the order within a part is the order the
   // entries were claimed in (atomically, see k_build_nbrs)
   uint32_t *nbr;      // (j << 8) | image
-  double *hval;       // QEq H_ij per entry (FP64 form)
+  float2 *hvalp;      // QEq H_ij per entry (FP64 form) as an FP32 pair (hi, lo)
   float *hval32;      // QEq H_ij per entry (mixed form)
   int *n_near, *n_far;  // entries claimed (may exceed the part's capacity
                         // until the host regrows and re-runs)
@@ -244,7 +244,7 @@ struct Dev {
   // iterate x, right-hand side b, residual r, preconditioned residual u,
   // search direction p (qd, the SpMV's input) and its product q = H p
   double2 *qx, *qb, *qr, *qu, *qd, *qq;
-  float4 *qd32;   // mixed form: qd split into FP32 (hi, lo) pairs, s then t
+  float4 *qd32;   // qd split into FP32 (hi, lo) pairs, s then t (the SpMVs' input)
   double *Hdia_inv;
   double *red;        // device scalars / reduction accumulators, RG_NRED per segment
   double *energy;     // [nseg][RG_NE]

@@ -36,22 +36,24 @@ UNIT = "atom-steps/s"
 DT = 0.25          # fs
 SEED = 7
 
-# Per-unit figures of the kernels that can dominate the FP64 step.  FLOP
-# (2*dfma + dmul + dadd, SASS thread-instruction counts) and DRAM bytes
-# (dram__bytes_read + write) are from one ncu capture of the 52,428-atom
-# case of the same mixture (`--scale 0.05`; the nonbonded kernel's
-# force-only variant, which the timed steps run); the algorithmic bytes are
-# the compulsory traffic of the canonical layout: per unordered pair one
-# 4-byte index (+ the 8-byte H value where the kernel produces or reads H),
-# plus per-atom position/charge/type reads and result writes.  Units: per
-# directed pair for the pair-list build, per unordered pair for the
+# Per-unit figures of the kernels that can dominate the FP64 step.  FP64
+# FLOP (2*dfma + dmul + dadd, SASS thread-instruction counts) and DRAM
+# bytes (dram__bytes_read + write) are from one ncu capture of the
+# 52,428-atom case of the same mixture (`--scale 0.05`; the nonbonded
+# kernel's force-only variant, which the timed steps run); the algorithmic
+# bytes are the compulsory traffic of the canonical layout: per unordered
+# pair one 4-byte index (+ the 8-byte H value where the kernel produces or
+# reads H), plus per-atom position/charge/type reads and result writes; the
+# streamed bytes are what the kernel's layout reads per unit (the QEq
+# SpMV's full rows: index and FP32-pair H of every directed entry).  Units:
+# per directed pair for the pair-list build, per unordered pair for the
 # nonbonded kernel, per list entry for one QEq SpMV (both systems).
 FP64_PER_UNIT = {
-    # phase: (kernel, unit, FLOP/unit, DRAM bytes/unit, algorithmic bytes/unit,
-    #         algorithmic bytes/atom)
-    "pair_list+H": ("k_build_nbrs", "directed pair", 23.00, 11.19, 6.0, 64.0),
-    "nonbonded": ("k_nonbonded", "unordered pair", 39.97, 16.87, 4.0, 60.0),
-    "qeq_spmv": ("k_spmv", "list entry", 4.12, 12.76, 6.0, 96.0),
+    # phase: (kernel, unit, FP64 FLOP/unit, DRAM bytes/unit, algorithmic
+    #         bytes/unit, algorithmic bytes/atom, streamed bytes/unit)
+    "pair_list+H": ("k_build_nbrs_tiles", "directed pair", 0.0006, 11.61, 6.0, 64.0, 12.0),
+    "nonbonded": ("k_nonbonded", "unordered pair", 5.80, 17.78, 4.0, 60.0, 8.0),
+    "qeq_spmv": ("k_spmvp", "list entry", 0.013, 12.71, 6.0, 96.0, 12.0),
 }
 
 
@@ -593,27 +595,28 @@ def gpu_arm(args):
     hbm_peak = peaks.get("hbm_gbs")
     phases = {k: v for k, v in prof.items() if v[1] > 0}
     tot_ms = sum(v[0] for v in phases.values())
-    kname, uname, flop_u, bytes_u, alg_u, alg_atom = FP64_PER_UNIT[dom]
+    kname, uname, flop_u, bytes_u, alg_u, alg_atom, stream_u = FP64_PER_UNIT[dom]
     units = st["n_pairs"] / 2 if dom == "nonbonded" else st["n_pairs"]
     avg_ms = live[0] / max(live[1], 1)
     if dom == "qeq_spmv":
-        # a CG SpMV launch updates the systems still iterating: one DFMA
-        # per entry for each (two while both iterate, one after the other
-        # has converged),
-        # and a launch with none left returns at once.  FLOP and bytes are
-        # summed over the timed region and divided by the summed time.
-        sys_iters = st["cg_system_iters"] - st0["cg_system_iters"]
+        # a CG SpMV launch streams the rows when a system is still
+        # iterating (its products and sums run on the FP32 units, as FP32
+        # pairs), and a launch with none left returns at once: bytes are
+        # summed over the timed region and divided by the summed time
         passes = st["cg_spmv_rows_passes"] - st0["cg_spmv_rows_passes"]
-        fp64_ach = 2.0 * units * sys_iters / (live[0] * 1e-3) / 1e12
-        alg_bytes = (alg_u * units + alg_atom * n) * passes / max(live[1], 1)
-        flop_note = (f"2 FLOP (one DFMA) per entry for each system still iterating: "
-                     f"{sys_iters} system-SpMVs in {live[1]} launches "
-                     f"({passes} with work)")
+        per = passes / max(live[1], 1)
+        fp64_ach = flop_u * units * per / (avg_ms * 1e-3) / 1e12
+        alg_bytes = (alg_u * units + alg_atom * n) * per
+        stream_bytes = (stream_u * units + 48.0 * n) * per
+        flop_note = (f"FP64 instructions per entry from ncu ({flop_u}: the row tails); "
+                     f"{passes} of {live[1]} launches had a system to update")
     else:
         fp64_ach = flop_u * units / (avg_ms * 1e-3) / 1e12
         alg_bytes = alg_u * units + alg_atom * n
+        stream_bytes = stream_u * units + alg_atom * n
         flop_note = "ncu-counted FP64 FLOP per unit (52,428-atom capture) x units"
     hbm_ach = alg_bytes / (avg_ms * 1e-3) / 1e9
+    stream_ach = stream_bytes / (avg_ms * 1e-3) / 1e9
     fp64_frac = fp64_ach / fp64_peak
     hbm_frac = hbm_ach / hbm_peak if hbm_peak else None
     bind_fp64 = hbm_frac is None or fp64_frac >= hbm_frac
@@ -630,6 +633,8 @@ def gpu_arm(args):
                                     "has no FP64 figure)"},
             "hbm": {"algorithmic_bytes": alg_bytes, "achieved_gbs": hbm_ach,
                     "peak_gbs": hbm_peak, "frac": hbm_frac,
+                    "streamed_bytes": stream_bytes, "streamed_gbs": stream_ach,
+                    "streamed_frac": stream_ach / hbm_peak if hbm_peak else None,
                     "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)"},
             "units_per_launch": units, "unit_of_work": uname, "flop_per_unit": flop_u,
             "avg_launch_ms": avg_ms, "launches_timed": live[1],

@@ -1,5 +1,6 @@
 // QEq charge equilibration: the s and t systems of the reference solved
-// together ("dual"), each with the reference's pipelined Jacobi-PCG.
+// together ("dual"), each with a Jacobi-preconditioned CG that keeps the
+// set-up, stopping test and iteration count of the reference's CG_v2.
 //
 //  k_qeq_setup   init_matvec: Jacobi diagonal, b_s = -chi, b_t = -1, cubic
 //                (s) / quadratic (t) extrapolation from the 5-deep
@@ -63,9 +64,9 @@ __global__ void k_qeq_setup(Dev d) {
 // formed exactly as p + e (fmaf) plus h*lo, and the row sum is carried as an
 // unevaluated FP32 pair with Knuth's TwoSum, across the warp too; the pair
 // becomes FP64 once per row.  The sums so carry ~46 significant bits: the
-// pipelined CG then follows the FP64 iterates (it stagnates with plain FP32
-// sums), while reading 8 bytes of H and index per entry and running on the
-// FP32 units.
+// CG then follows the FP64 iterates (it stagnates with plain FP32 sums),
+// while reading 8 bytes of H and index per entry and running on the FP32
+// units.
 // (explicitly rounded operations: no contraction into FMAs may change them)
 __device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
   s = __fadd_rn(a, b);

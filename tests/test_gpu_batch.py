@@ -2,7 +2,7 @@
 single-point evaluation).  Each system's charges, forces, energies and CG
 iteration counts in the batch must be those of the same system run alone
 (same library, same form): the batch changes only the order of FP64
-reductions, which moves the pipelined CG's charges by 1e-7 to a few 1e-6
+reductions, which moves the CG's charges by 1e-7 to a few 1e-6
 (the iterate at the 1e-6 residual tolerance is itself ~2e-5 e from the
 converged charges).  Stated tolerance for "the same alone and in the mix":
 charges 1e-5 e (the QEq bar of the parity tests), forces 1e-5 relative

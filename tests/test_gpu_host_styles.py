@@ -63,7 +63,7 @@ def test_deck_single_point_matches_abi_and_oracle(tmp_path, ffield):
     order = np.argsort(s.tag)
     assert np.array_equal(st["tag"], s.tag[order])
     # same library, same calls: equal up to the order of FP64 atomics, which
-    # moves the pipelined CG's charges by up to a few 1e-6 (bars of the
+    # moves the CG's charges by up to a few 1e-6 (bars of the
     # batch tests: 1e-5)
     assert np.abs(st["q"] - qg[order]).max() < 1e-5
     assert np.sqrt(((st["f"] - fg[order]) ** 2).sum() / (fg ** 2).sum()) < 1e-5

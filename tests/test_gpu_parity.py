@@ -7,7 +7,7 @@ energies within 1e-9 relative (or 1e-7 kcal/mol absolute for terms that
 are zero up to round-off) and forces within 1e-9 relative RMS.
 
 QEq charges within 1e-5 e (the bar the mixed form is held to as well): the
-pipelined CG stops at a 1e-6 relative residual, and the oracle's own
+CG stops at a 1e-6 relative residual, and the oracle's own
 charges move by up to ~1e-7 (and the iteration count by one) when the
 input positions are perturbed at the 1e-15..1e-13 level, so agreement
 below the solver tolerance is not a property of the algorithm.  The whole

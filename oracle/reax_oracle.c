@@ -1954,23 +1954,46 @@ static int qeq_cg(const ro_ctx *c, const hmat_t *H, const double *b,
 /* H rows of the local atoms from the full far list (compute_H_Full_C_para,
  * fix_qeq_reax_sw64.c:768-911, host form :146-181), ghost columns folded
  * onto their local owners */
+/* The fix's neighbour list reaches the pair cutoff plus the skin
+ * (cutmax + skin, the ghosts' range), and compute_H keeps r <= swb: within
+ * nonb_cut that is the far list; for swb > nonb_cut the pairs are searched
+ * among all ghosts (a plain loop: such runs are small test cases). */
 static void qeq_build_H(ro_ctx *c, hmat_t *H_out) {
   int i, n = c->n;
   const double swbsq = c->ctl.qeq_swb * c->ctl.qeq_swb;
+  const int wide = c->ctl.qeq_swb > c->nonb_cut;
   const double *Tap = c->qTap;
   hmat_t H;
   H.start = (int *)malloc((n + 1) * sizeof(int));
-  long long cap = c->far_start[n] + 16, top = 0;
+  long long cap = wide ? (long long)n * 64 + 16 : c->far_start[n] + 16, top = 0;
   H.col = (int *)malloc(cap * sizeof(int));
   H.val = (double *)malloc(cap * sizeof(double));
   for (i = 0; i < n; i++) {
     int pj, ti = c->type[i];
     H.start[i] = (int)top;
-    for (pj = c->far_start[i]; pj < c->far_start[i + 1]; pj++) {
-      int j = c->far_nbr[pj];
-      const double *dv = &c->far_dvec[3 * pj];
+    const int p0 = wide ? 0 : c->far_start[i], p1 = wide ? c->N : c->far_start[i + 1];
+    for (pj = p0; pj < p1; pj++) {
+      int j;
+      double dvw[3];
+      const double *dv;
+      if (wide) {
+        j = pj;
+        if (j == i) continue;
+        dvw[0] = c->xe[3 * j + 0] - c->xe[3 * i + 0];
+        dvw[1] = c->xe[3 * j + 1] - c->xe[3 * i + 1];
+        dvw[2] = c->xe[3 * j + 2] - c->xe[3 * i + 2];
+        dv = dvw;
+      } else {
+        j = c->far_nbr[pj];
+        dv = &c->far_dvec[3 * pj];
+      }
       double r_sqr = SQR(dv[0]) + SQR(dv[1]) + SQR(dv[2]);
       if (r_sqr <= swbsq) {
+        if (top >= cap) {
+          cap *= 2;
+          H.col = (int *)xrealloc(H.col, cap * sizeof(int));
+          H.val = (double *)xrealloc(H.val, cap * sizeof(double));
+        }
         double r = sqrt(r_sqr);
         /* shld = pow(gamma_i*gamma_j, -1.5), init_shielding :440-454 */
         double gamma = pow(c->ff.sbp[ti].gamma * c->ff.sbp[c->te[j]].gamma, -1.5);

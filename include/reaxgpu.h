@@ -66,7 +66,14 @@ typedef struct {
   double qeq_swb;       /* 10.0  QEq taper outer radius                 */
   double qeq_tol;       /* 1e-6  CG relative tolerance                  */
   int qeq_imax;         /* 200   CG iteration limit                     */
-  int precision;        /* RG_PREC_FP64 or RG_PREC_MIXED               */
+  int precision;        /* RG_PREC_FP64: FP64 accuracy throughout (list
+                           decisions, bond orders, angles, accumulations
+                           in FP64; the tabulated pair functions, the
+                           pair forces and the QEq SpMV of orthogonal
+                           boxes as FP32 pairs, ~1e-13 relative);
+                           RG_PREC_MIXED: pair, H-bond, angle and SpMV
+                           arithmetic in FP32 (forces ~1e-6 relative to
+                           the FP64 form, charges ~5e-6 e)                */
   int device;           /* CUDA device ordinal                          */
   int tabulate;         /* vdW+Coulomb (both forms; the mixed form reads
                            an FP32 copy) and the FP64 form's QEq H from

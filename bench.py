@@ -53,7 +53,7 @@ FP64_PER_UNIT = {
     #         bytes/unit, algorithmic bytes/atom, streamed bytes/unit)
     "pair_list+H": ("k_build_nbrs_tiles", "directed pair", 0.0006, 11.61, 6.0, 64.0, 12.0),
     "nonbonded": ("k_nonbonded", "unordered pair", 5.80, 17.78, 4.0, 60.0, 8.0),
-    "qeq_spmv": ("k_spmvp", "list entry", 0.013, 12.71, 6.0, 96.0, 12.0),
+    "qeq_spmv": ("k_spmvp", "list entry", 0.013, 12.79, 6.0, 96.0, 12.0),
 }
 
 

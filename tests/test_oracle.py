@@ -72,3 +72,29 @@ def test_list_statistics(mix):
     assert 0.8 * expect < st["n_far_local"] / s.n < 1.2 * expect
     assert st["n_bonds_local"] > s.n
     assert st["n_total"] > st["n_local"]
+
+
+@pytest.mark.parametrize("swb", [9.0, 10.0, 11.0])
+def test_qeq_h_pairs_within_swb(ffield, swb):
+    """The QEq H holds every (local atom, partner image) pair within the
+    taper radius once, below and above the nonbonded cutoff (above it the
+    pairs come from all ghosts, as the fix's own neighbour list reaches the
+    pair cutoff plus the skin); counted here by brute force over images."""
+    s = systems.water_box(60, seed=2)          # 180 atoms, edge ~12.1 A
+    o = Oracle(ffield, qeq_swb=swb)
+    o.set_system(s.box, s.x, s.types(ELEMENTS), s.tag, None, s.v)
+    o.qeq()
+    L = np.asarray(s.box, float)
+    x = np.asarray(s.x, float) % L
+    count = 0
+    r = range(-2, 3)
+    for sx in r:
+        for sy in r:
+            for sz in r:
+                d = x[None, :, :] + np.array([sx, sy, sz]) * L - x[:, None, :]
+                d2 = (d ** 2).sum(-1)
+                ok = d2 <= swb * swb
+                if sx == sy == sz == 0:
+                    np.fill_diagonal(ok, False)
+                count += int(ok.sum())
+    assert o.stats()["n_H_entries"] == count
